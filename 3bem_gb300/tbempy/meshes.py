@@ -1,0 +1,140 @@
+"""Seeded synthetic meshes and point sets for the BEM operator apply.
+
+The reference builds point data from a triangle mesh with
+``nbody_src_from_bem`` (cpp/nbody_operator.h:56-76): one point per (facet,
+quadrature point), weight = w_q * jacobian with jacobian = 2 * area
+(cpp/numerics.h:33-35), normal = facet normal.  The workloads here use a
+3-point symmetric triangle rule (reference-triangle weights 1/6 each, i.e.
+area/3 after the jacobian), which the reference does not ship
+(``tri_gauss(n)`` gives n^2 points, cpp/gauss_quad.cpp:124-152).
+
+Generators:
+  * ``icosphere(n_subdiv)``  -- icosahedron refined 1->4, vertices projected
+    to the unit sphere (5,120 triangles at n_subdiv=4);
+  * ``dipping_fault(n, dip)`` -- planar 2 x 2 square dipping ``dip`` degrees,
+    an n x n quad grid, each quad split into 2 triangles;
+  * ``points_from_mesh`` -- the 3-point rule -> (locs, normals, weights).
+"""
+import numpy as np
+
+# Barycentric coordinates of the 3-point rule (degree 2, interior points).
+_TRI3_BARY = np.array([[2.0 / 3.0, 1.0 / 6.0, 1.0 / 6.0],
+                       [1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0],
+                       [1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0]])
+
+
+def icosphere(n_subdiv, radius=1.0, center=(0.0, 0.0, 0.0)):
+    """Icosahedron subdivided ``n_subdiv`` times, projected to a sphere.
+
+    Returns (verts [nv,3] float64, tris [nt,3] int64) with outward orientation.
+    """
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0],
+                  [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], dtype=np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11],
+                  [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6], [7, 1, 8],
+                  [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9],
+                  [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]],
+                 dtype=np.int64)
+    verts = [row for row in v]
+    for _ in range(n_subdiv):
+        cache = {}
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            idx = cache.get(key)
+            if idx is None:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                idx = len(verts) - 1
+                cache[key] = idx
+            return idx
+
+        nf = np.empty((4 * len(f), 3), dtype=np.int64)
+        for i, (a, b, c) in enumerate(f):
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf[4 * i + 0] = (a, ab, ca)
+            nf[4 * i + 1] = (b, bc, ab)
+            nf[4 * i + 2] = (c, ca, bc)
+            nf[4 * i + 3] = (ab, bc, ca)
+        f = nf
+    verts = np.asarray(verts) * radius + np.asarray(center, dtype=np.float64)
+    # orient outward: normal . (centroid - center) > 0
+    p = verts[f]
+    n = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    flip = np.einsum("ij,ij->i", n, p.mean(axis=1) - np.asarray(center)) < 0
+    f[flip] = f[flip][:, ::-1]
+    return verts, f
+
+
+def dipping_fault(n, dip_deg=45.0, width=2.0, center=(0.0, 0.0, -1.0)):
+    """Planar ``width`` x ``width`` square fault dipping ``dip_deg`` degrees.
+
+    Strike along x; the down-dip direction is (0, cos(dip), -sin(dip)).  The
+    n x n quad grid is split into 2 n^2 triangles (diagonal lower-left to
+    upper-right).  Returns (verts, tris, uv) with uv in [-1,1]^2 per vertex.
+    """
+    s = np.linspace(-1.0, 1.0, n + 1)
+    u, w = np.meshgrid(s, s, indexing="ij")
+    dip = np.deg2rad(dip_deg)
+    h = 0.5 * width
+    x = h * u
+    y = h * w * np.cos(dip)
+    z = -h * w * np.sin(dip)
+    verts = np.stack([x, y, z], axis=-1).reshape(-1, 3) + np.asarray(center)
+    uv = np.stack([u, w], axis=-1).reshape(-1, 2)
+    idx = np.arange((n + 1) * (n + 1)).reshape(n + 1, n + 1)
+    a = idx[:-1, :-1].ravel()
+    b = idx[1:, :-1].ravel()
+    c = idx[1:, 1:].ravel()
+    d = idx[:-1, 1:].ravel()
+    tris = np.concatenate([np.stack([a, b, c], 1), np.stack([a, c, d], 1)])
+    return verts, tris.astype(np.int64), uv
+
+
+def points_from_mesh(verts, tris):
+    """3-point rule on every triangle -> (locs [N,3], normals [N,3], weights [N]).
+
+    Point order is facet-major (facet f, point q -> row 3 f + q), matching the
+    reference's dof numbering obs_idx * n_quad + q (cpp/nbody_operator.h:62-70).
+    """
+    p = verts[tris]                                   # [nt, 3, 3]
+    cr = np.cross(p[:, 2] - p[:, 0], p[:, 2] - p[:, 1])  # reference unscaled_normal
+    nrm = np.linalg.norm(cr, axis=1)
+    normals = cr / nrm[:, None]
+    area = 0.5 * nrm
+    locs = np.einsum("qk,tkd->tqd", _TRI3_BARY, p).reshape(-1, 3)
+    normals = np.repeat(normals, 3, axis=0)
+    # w_q * jacobian = (1/6) * (2 * area) = area / 3
+    weights = np.repeat((1.0 / 6.0) * (2.0 * area), 3)
+    return (np.ascontiguousarray(locs), np.ascontiguousarray(normals),
+            np.ascontiguousarray(weights))
+
+
+def sphere_points(n_subdiv=4):
+    """Unit icosphere points: 3 per triangle (15,360 at n_subdiv=4)."""
+    v, t = icosphere(n_subdiv)
+    return points_from_mesh(v, t)
+
+
+def fault_points(n=128, dip_deg=45.0):
+    """Dipping-fault points (98,304 at n=128) plus each point's (u, v)."""
+    v, t, uv = dipping_fault(n, dip_deg)
+    locs, normals, weights = points_from_mesh(v, t)
+    uvp = np.einsum("qk,tkd->tqd", _TRI3_BARY, uv[t]).reshape(-1, 2)
+    return locs, normals, weights, uvp
+
+
+def tapered_slip(uv, seed=1):
+    """3-component slip: uniform[-1,1] times a cosine taper to zero at edges.
+
+    Returned component-major ([3 * N], x[d * N + i]) like the reference's
+    operator inputs (cpp/fmm.cpp:189-190).
+    """
+    rng = np.random.default_rng(seed)
+    n = uv.shape[0]
+    taper = np.cos(0.5 * np.pi * uv[:, 0]) * np.cos(0.5 * np.pi * uv[:, 1])
+    s = rng.uniform(-1.0, 1.0, size=(3, n)) * taper[None, :]
+    return np.ascontiguousarray(s.reshape(-1))

@@ -1,0 +1,261 @@
+"""ORACLE -- test infrastructure, not product code.
+
+Python side of the CPU restatement of the reference KIFMM (fmm_oracle.cpp):
+builds the shared library, computes the check-to-equivalent pseudo-inverses
+with LAPACK dgesvd exactly as the reference's ``svd_pseudoinverse`` does
+(cpp/blas_wrapper.cpp:67-127: the row-major matrix is handed to column-major
+LAPACK, singular values <= 1e-10 * s_max are dropped, cpp/fmm.cpp:122), and
+exposes the apply, the direct sum and the tree/list dumps.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline / reference
+arm import this module, and only as the checker.  ``RefLib`` wraps the
+reference itself compiled from its own sources (oracle/_ref, built by
+oracle/ref/Makefile where the reference checkout exists) to pin this
+restatement.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import scipy.linalg
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libtbem_ref.so")
+
+KERNELS = {"LaplaceSingle": 0, "LaplaceDouble": 1, "ElasticDisplacement": 2,
+           "ElasticTraction": 3, "ElasticAdjointTraction": 4, "IdentityScalar": 5}
+TENSOR_KERNELS = (2, 3, 4)
+LISTS = ["p2m", "m2m", "p2p", "m2p", "p2l", "m2l", "l2l", "l2p"]
+
+
+def build(force=False):
+    """Compile fmm_oracle.cpp (g++ -O3 -fopenmp, no FMA contraction)."""
+    src = os.path.join(HERE, "fmm_oracle.cpp")
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
+        return LIB_PATH
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    subprocess.check_call(["g++", "-std=c++17", "-O3", "-fopenmp", "-fPIC", "-shared",
+                           "-ffp-contract=off", src, "-o", tmp])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_ref(ref_root="/root/reference"):
+    """Compile the reference's own sources into oracle/_ref (needs the checkout)."""
+    if not os.path.isdir(os.path.join(ref_root, "cpp")):
+        return None
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"),
+                           "REF=" + ref_root, "-j8"])
+    return REF_LIB_PATH
+
+
+_P = C.c_void_p
+_D = C.c_double
+_L = C.c_long
+_I = C.c_int
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def pinv_reference(A, threshold=1e-10):
+    """Thresholded pseudo-inverse of a row-major square A, the reference way.
+
+    LAPACK sees the row-major buffer as A^T (column-major); dgesvd gives
+    A^T = U S V^T and the result is pinv(A) = U S^-1 V^T restricted to the
+    singular values above threshold * s_max (cpp/blas_wrapper.cpp:109-169).
+    """
+    u, s, vt = scipy.linalg.svd(A.T, full_matrices=True, lapack_driver="gesvd")
+    keep = s > threshold * s[0]
+    return np.ascontiguousarray((u[:, keep] / s[keep]) @ vt[keep, :])
+
+
+class _Lib:
+    _cache = {}
+
+    def __init__(self, path, prefix):
+        self.lib = C.CDLL(path)
+        self.prefix = prefix
+
+    def fn(self, name, restype, argtypes):
+        f = getattr(self.lib, self.prefix + name)
+        f.restype = restype
+        f.argtypes = argtypes
+        return f
+
+
+def _lib():
+    if "oracle" not in _Lib._cache:
+        _Lib._cache["oracle"] = _Lib(build(), "oracle_")
+    return _Lib._cache["oracle"]
+
+
+class _FMMBase:
+    """Shared ctypes surface of the oracle and the reference shim."""
+
+    def _setup(self, L, kernel, obs_locs, obs_normals, src_locs, src_normals,
+               src_weights, mac, order, min_pts, d, small_cells, mu, nu):
+        self.L = L
+        self.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+        self.R = 3 if self.kernel in TENSOR_KERNELS else 1
+        self.obs_locs, self.obs_normals = _f64(obs_locs), _f64(obs_normals)
+        self.src_locs, self.src_normals = _f64(src_locs), _f64(src_normals)
+        self.src_weights = _f64(src_weights)
+        self.n_obs, self.n_src = len(self.obs_locs), len(self.src_locs)
+        create = L.fn("fmm_create" if L.prefix == "ref_" else "create", _P,
+                      [_I, _D, _D, _P, _P, _L, _P, _P, _P, _L, _D, _L, _L, _D, _I])
+        self.h = create(self.kernel, mu, nu, _ptr(self.obs_locs), _ptr(self.obs_normals),
+                        self.n_obs, _ptr(self.src_locs), _ptr(self.src_normals),
+                        _ptr(self.src_weights), self.n_src, mac, order, min_pts, d,
+                        int(bool(small_cells)))
+        if not self.h:
+            raise ValueError("fmm create failed (bad kernel or config)")
+
+    def tree(self, which):
+        """Cells in pre-order: dict of level, index, center, hw, n_idx, n_children, indices."""
+        pre = "fmm_" if self.L.prefix == "ref_" else ""
+        f = self.L.fn(pre + "tree_cells", _L, [_P, _I, _P, _P, _P, _P, _P, _P])
+        n = f(self.h, which, None, None, None, None, None, None)
+        out = {k: np.zeros(n, dtype=np.int64) for k in ("level", "index", "n_idx", "n_children")}
+        out["center"] = np.zeros((n, 3))
+        out["hw"] = np.zeros((n, 3))
+        f(self.h, which, _ptr(out["level"]), _ptr(out["index"]), _ptr(out["center"]),
+          _ptr(out["hw"]), _ptr(out["n_idx"]), _ptr(out["n_children"]))
+        g = self.L.fn(pre + "tree_indices", _L, [_P, _I, _P])
+        m = g(self.h, which, None)
+        idx = np.zeros(m, dtype=np.int64)
+        g(self.h, which, _ptr(idx))
+        out["indices"] = np.split(idx, np.cumsum(out["n_idx"])[:-1])
+        return out
+
+    def list(self, kind):
+        pre = "fmm_" if self.L.prefix == "ref_" else ""
+        f = self.L.fn(pre + "list", _L, [_P, _I, _P, _P])
+        k = LISTS.index(kind) if isinstance(kind, str) else int(kind)
+        n = f(self.h, k, None, None)
+        a = np.zeros(n, dtype=np.int64)
+        b = np.zeros(n, dtype=np.int64)
+        f(self.h, k, _ptr(a), _ptr(b))
+        return a, b
+
+    def n_surf(self):
+        pre = "fmm_" if self.L.prefix == "ref_" else ""
+        return self.L.fn(pre + "n_surf", _L, [_P])(self.h)
+
+
+class OracleFMM(_FMMBase):
+    """The oracle restatement of FMMOperator<3,R,C> (cpp/fmm.h:131-237)."""
+
+    def __init__(self, kernel, obs_locs, obs_normals, src_locs, src_normals, src_weights,
+                 mac, order, min_pts, d=0.05, small_cells=False, mu=1.0, nu=0.25):
+        self._setup(_lib(), kernel, obs_locs, obs_normals, src_locs, src_normals,
+                    src_weights, mac, order, min_pts, d, small_cells, mu, nu)
+        L = self.L
+        nlev = L.fn("n_levels", _L, [_P, _I])
+        sysf = L.fn("c2e_system", _L, [_P, _I, _L, _P])
+        setf = L.fn("set_c2e", _L, [_P, _I, _L, _P])
+        n = self.n_surf() * self.R
+        self.c2e = {0: [], 1: []}
+        for which in (0, 1):
+            for lev in range(nlev(self.h, which)):
+                A = np.zeros((n, n))
+                sysf(self.h, which, lev, _ptr(A))
+                P = pinv_reference(A)
+                self.c2e[which].append(P)
+                setf(self.h, which, lev, _ptr(P))
+        self._apply = L.fn("apply", None, [_P, _P, _P, _I, _D])
+
+    def apply(self, x, mask=0xff, list_fraction=1.0):
+        x = _f64(x)
+        assert x.shape == (self.R * self.n_src,)
+        y = np.zeros(self.R * self.n_obs)
+        self._apply(self.h, _ptr(x), _ptr(y), int(mask), float(list_fraction))
+        return y
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.fn("destroy", None, [_P])(self.h)
+            self.h = None
+
+
+class RefFMM(_FMMBase):
+    """The reference FMMOperator itself, built from its sources (oracle/_ref)."""
+
+    def __init__(self, kernel, obs_locs, obs_normals, src_locs, src_normals, src_weights,
+                 mac, order, min_pts, d=0.05, small_cells=False, mu=1.0, nu=0.25):
+        if "ref" not in _Lib._cache:
+            _Lib._cache["ref"] = _Lib(REF_LIB_PATH, "ref_")
+        self._setup(_Lib._cache["ref"], kernel, obs_locs, obs_normals, src_locs,
+                    src_normals, src_weights, mac, order, min_pts, d, small_cells, mu, nu)
+
+    def apply(self, x, mask=0xff):
+        x = _f64(x)
+        y = np.zeros(self.R * self.n_obs)
+        self.L.fn("fmm_apply_masked", None, [_P, _I, _P, _P])(self.h, int(mask), _ptr(x), _ptr(y))
+        return y
+
+    def c2e(self, which, level):
+        f = self.L.fn("fmm_c2e", _L, [_P, _I, _L, _P])
+        n = self.n_surf() * self.R
+        A = np.zeros((n, n))
+        f(self.h, which, level, _ptr(A))
+        return A
+
+    def n_levels(self, which):
+        return self.L.fn("fmm_c2e", _L, [_P, _I, _L, _P])(self.h, which, -1, None)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.fn("fmm_destroy", None, [_P])(self.h)
+            self.h = None
+
+
+def ref_available():
+    return os.path.exists(REF_LIB_PATH)
+
+
+def direct(kernel, obs_locs, obs_normals, src_locs, src_normals, src_weights, x,
+           mu=1.0, nu=0.25):
+    """FP64 direct N-body sum (the reference's nbody_eval over all pairs)."""
+    k = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+    R = 3 if k in TENSOR_KERNELS else 1
+    ol, on = _f64(obs_locs), _f64(obs_normals)
+    sl, sn, sw = _f64(src_locs), _f64(src_normals), _f64(src_weights)
+    x = _f64(x)
+    y = np.zeros(R * len(ol))
+    f = _lib().fn("direct", _I, [_I, _D, _D, _P, _P, _L, _P, _P, _P, _L, _P, _P])
+    f(k, mu, nu, _ptr(ol), _ptr(on), len(ol), _ptr(sl), _ptr(sn), _ptr(sw), len(sl),
+      _ptr(x), _ptr(y))
+    return y
+
+
+def kernel_tensor(kernel, obs, src, nobs, nsrc, mu=1.0, nu=0.25, lib="oracle"):
+    """One kernel tensor K(obs, src, nobs, nsrc) as an R x C array."""
+    k = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+    L = _lib() if lib == "oracle" else _Lib._cache.setdefault("ref", _Lib(REF_LIB_PATH, "ref_"))
+    f = L.fn("kernel", _I, [_I, _D, _D, _P, _P, _P, _P, _P])
+    out = np.zeros(9)
+    args = [_f64(a) for a in (obs, src, nobs, nsrc)]
+    n = f(k, mu, nu, *[_ptr(a) for a in args], _ptr(out))
+    R = 3 if n == 9 else 1
+    return out[:n].reshape(R, R)
+
+
+def surface(order):
+    f = _lib().fn("surface", _L, [_L, _P])
+    n = f(int(order), None)
+    p = np.zeros((n, 3))
+    f(int(order), _ptr(p))
+    return p
+
+
+def max_threads():
+    return _lib().fn("max_threads", _I, [])()
