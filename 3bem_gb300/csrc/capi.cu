@@ -1,0 +1,231 @@
+// extern "C" entry points (include/tbem_gpu.h).  Every call catches the
+// internal exceptions and turns them into a status code plus a thread-local
+// message; nothing aborts.
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "plan.h"
+
+struct TbemFmm {
+    tbem::Plan plan;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+template <typename F>
+int guarded(F&& f)
+{
+    try {
+        g_last_error.clear();
+        f();
+        return TBEM_OK;
+    } catch (const tbem::Error& e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(TBEM_ERR_ALLOC, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(TBEM_ERR_ARG, e.what());
+    }
+}
+}  // namespace
+
+namespace tbem {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace tbem
+
+extern "C" {
+
+const char* tbem_last_error(void) { return g_last_error.c_str(); }
+
+void tbem_default_options(TbemGpuOptions* opt)
+{
+    if (!opt) return;
+    std::memset(opt, 0, sizeof(*opt));
+    opt->precision = TBEM_PRECISION_FP64;
+    opt->device = 0;
+    opt->svd_threshold = 1e-10;
+}
+
+int tbem_fmm_create(int kernel, const double* kernel_params, const double* obs_locs,
+                    const double* obs_normals, long n_obs, const double* src_locs,
+                    const double* src_normals, const double* src_weights, long n_src,
+                    const TbemFmmConfig* config, const TbemGpuOptions* options, TbemFmm** out)
+{
+    if (!out || !config) return fail(TBEM_ERR_ARG, "null config or output handle");
+    *out = nullptr;
+    TbemGpuOptions opt;
+    tbem_default_options(&opt);
+    if (options) opt = *options;
+    TbemFmm* h = nullptr;
+    int rc = guarded([&] {
+        h = new TbemFmm();
+        h->plan.build(kernel, kernel_params, obs_locs, obs_normals, n_obs, src_locs, src_normals,
+                      src_weights, n_src, *config, opt);
+    });
+    if (rc != TBEM_OK) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return TBEM_OK;
+}
+
+int tbem_fmm_apply(TbemFmm* h, const double* x, double* y, int n_rhs, void* stream)
+{
+    if (!h || !y || (!x && tbem_fmm_n_cols(h) > 0)) return fail(TBEM_ERR_ARG, "null argument");
+    return guarded([&] { h->plan.apply(x, y, n_rhs, (cudaStream_t)stream, false); });
+}
+
+int tbem_fmm_apply_adjoint(TbemFmm* h, const double* z, double* w, int n_rhs, void* stream)
+{
+    if (!h || !w || (!z && tbem_fmm_n_rows(h) > 0)) return fail(TBEM_ERR_ARG, "null argument");
+    return guarded([&] { h->plan.apply(z, w, n_rhs, (cudaStream_t)stream, true); });
+}
+
+long tbem_fmm_n_rows(const TbemFmm* h) { return h ? h->plan.R * h->plan.n_obs : TBEM_ERR_ARG; }
+long tbem_fmm_n_cols(const TbemFmm* h) { return h ? h->plan.R * h->plan.n_src : TBEM_ERR_ARG; }
+
+int tbem_fmm_clone(const TbemFmm* h, TbemFmm** out)
+{
+    if (!h || !out) return fail(TBEM_ERR_ARG, "null argument");
+    const tbem::Plan& p = h->plan;
+    double params[2] = {p.mu, p.nu};
+    int rc = tbem_fmm_create(p.kid, params, p.h_obs_locs.data(), p.h_obs_normals.data(), p.n_obs,
+                             p.h_src_locs.data(), p.h_src_normals.data(), p.h_src_weights.data(),
+                             p.n_src, &p.cfg, &p.opt, out);
+    if (rc != TBEM_OK) return rc;
+    if (!p.f.mixed) {
+        // carry over installed check-to-equivalent operators
+        return guarded([&] {
+            std::vector<double> buf((size_t)p.n * p.n);
+            for (int w = 0; w < 2; w++) {
+                long nl = (long)(w == 0 ? p.f.c2e_up_off.size() : p.f.c2e_dn_off.size());
+                for (long l = 0; l < nl; l++) {
+                    p.get_c2e(w, l, buf.data());
+                    (*out)->plan.set_c2e(w, l, buf.data());
+                }
+            }
+        });
+    }
+    return TBEM_OK;
+}
+
+void tbem_fmm_destroy(TbemFmm* h) { delete h; }
+
+long tbem_fmm_tree_cells(const TbemFmm* h, int which, long* level, long* index, double* center,
+                         double* half_width, long* n_points, long* n_children)
+{
+    if (!h || (which != 0 && which != 1)) return fail(TBEM_ERR_ARG, "bad handle or tree");
+    const tbem::Tree& t = which == 0 ? *h->plan.stree : h->plan.otree;
+    for (size_t k = 0; k < t.preorder.size(); k++) {
+        const tbem::Cell& c = t.cells[t.preorder[k]];
+        if (level) level[k] = c.level;
+        if (index) index[k] = c.ref_index;
+        if (center) for (int d = 0; d < 3; d++) center[3 * k + d] = c.center[d];
+        if (half_width) for (int d = 0; d < 3; d++) half_width[3 * k + d] = c.hw[d];
+        if (n_points) n_points[k] = c.n_points();
+        if (n_children) n_children[k] = c.n_children;
+    }
+    return (long)t.preorder.size();
+}
+
+long tbem_fmm_tree_indices(const TbemFmm* h, int which, long* out)
+{
+    if (!h || (which != 0 && which != 1)) return fail(TBEM_ERR_ARG, "bad handle or tree");
+    const tbem::Tree& t = which == 0 ? *h->plan.stree : h->plan.otree;
+    long k = 0;
+    std::vector<long> tmp;
+    for (int f : t.preorder) {
+        const tbem::Cell& c = t.cells[f];
+        // the reference lists a cell's points in ascending original order
+        tmp.assign(t.perm.begin() + c.pt_begin, t.perm.begin() + c.pt_end);
+        std::sort(tmp.begin(), tmp.end());
+        for (long v : tmp) {
+            if (out) out[k] = v;
+            k++;
+        }
+    }
+    return k;
+}
+
+long tbem_fmm_list(const TbemFmm* h, int kind, long* obs_index, long* src_index)
+{
+    if (!h || kind < 0 || kind > 7) return fail(TBEM_ERR_ARG, "bad handle or list kind");
+    const tbem::Plan& p = h->plan;
+    const tbem::Tree& O = p.otree;
+    const tbem::Tree& S = *p.stree;
+    auto cells = [&](const std::vector<int>& v, const tbem::Tree& t) {
+        for (size_t i = 0; i < v.size(); i++) {
+            if (obs_index) obs_index[i] = t.cells[v[i]].ref_index;
+            if (src_index) src_index[i] = -1;
+        }
+        return (long)v.size();
+    };
+    auto pairs = [&](const std::vector<tbem::CellPair>& v) {
+        for (size_t i = 0; i < v.size(); i++) {
+            if (obs_index) obs_index[i] = O.cells[v[i].obs].ref_index;
+            if (src_index) src_index[i] = S.cells[v[i].src].ref_index;
+        }
+        return (long)v.size();
+    };
+    switch (kind) {
+    case 0: return cells(p.L.p2m, S);
+    case 1: return cells(p.L.m2m, S);
+    case 2: return pairs(p.L.p2p);
+    case 3: return pairs(p.L.m2p);
+    case 4: return pairs(p.L.p2l);
+    case 5: return pairs(p.L.m2l);
+    case 6: return cells(p.L.l2l, O);
+    default: return cells(p.L.l2p, O);
+    }
+}
+
+long tbem_fmm_n_surface(const TbemFmm* h) { return h ? h->plan.ns : TBEM_ERR_ARG; }
+
+long tbem_fmm_n_c2e_levels(const TbemFmm* h, int which)
+{
+    if (!h || (which != 0 && which != 1)) return fail(TBEM_ERR_ARG, "bad handle");
+    return (long)(which == 0 ? h->plan.f.c2e_up_off.size() : h->plan.f.c2e_dn_off.size());
+}
+
+int tbem_fmm_get_c2e(const TbemFmm* h, int which, long level, double* out)
+{
+    if (!h || !out) return fail(TBEM_ERR_ARG, "null argument");
+    return guarded([&] { h->plan.get_c2e(which, level, out); });
+}
+
+int tbem_fmm_set_c2e(TbemFmm* h, int which, long level, const double* op)
+{
+    if (!h || !op) return fail(TBEM_ERR_ARG, "null argument");
+    return guarded([&] { h->plan.set_c2e(which, level, op); });
+}
+
+int tbem_fmm_set_timing(TbemFmm* h, int enabled)
+{
+    if (!h) return fail(TBEM_ERR_ARG, "null handle");
+    h->plan.timing = enabled != 0;
+    return TBEM_OK;
+}
+
+int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int cap)
+{
+    if (!h) return fail(TBEM_ERR_ARG, "null handle");
+    const auto& v = h->plan.phase_ms;
+    int k = 0;
+    for (size_t i = 1; i < v.size(); i++, k++) {
+        if (k >= cap) continue;
+        if (names) names[k] = v[i].first.c_str();
+        if (ms) ms[k] = v[i].second;
+    }
+    return k;
+}
+
+}  // extern "C"

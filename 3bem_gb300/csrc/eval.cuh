@@ -1,0 +1,238 @@
+// Obs-owner N-body evaluation: the device form of the reference's
+// nbody_eval (cpp/nbody_operator.h:117-141) as it is called by P2P, P2M,
+// P2L, M2P, L2P (and M2M/L2L/M2L when they are evaluated on the fly),
+// cpp/fmm.cpp:163-441.
+//
+// A task = one target block (a range of permuted points, or the translation
+// surface of one cell) plus a list of source blocks (point ranges or cell
+// surfaces with densities).  One CTA owns a chunk of (128 / TPT) targets of
+// one task, so every output is written by exactly one thread: no atomics and
+// a fixed summation order.  TPT threads share a target and split its
+// sources; their partial sums meet in a warp-shuffle reduction.  Sources are
+// staged through shared memory in tiles of 128 that run across source-block
+// boundaries.  Coordinates are shifted to the task's origin (the target
+// cell's centre) in FP64 before the pair arithmetic, so the FP32 variant
+// keeps full relative accuracy in the separations.  The FP32 variant sums
+// each tile in FP32 and folds the tile sums into a compensated (Kahan) pair.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.cuh"
+
+namespace tbem {
+
+constexpr int EVAL_THREADS = 128;
+
+template <typename T>
+struct EvalArgs {
+    // work items: CTA b handles task item_task[b], targets from item_start[b]
+    const int* item_task;
+    const int* item_start;
+    // tasks
+    const long* task_tgt;        // target block: first point, or cell id for surfaces
+    const int* task_tgt_count;   // number of targets
+    const double* task_origin;   // [ntask][3]
+    const int* task_src_ptr;     // CSR into the source-block arrays
+    const long* src_blk;         // first point, or cell id for surfaces
+    const int* src_blk_count;
+    const int* src_blk_prefix;   // sources before this block within its task
+    // target geometry
+    const double* t_xyz;         // [N][3] permuted points (point targets)
+    const T* t_nrm;              // [N][3]
+    const double* t_center;      // [cells][3] (surface targets)
+    const double* t_rad;         // [cells] |half width|
+    double t_rref;
+    // source geometry and strengths
+    const double* s_xyz;
+    const T* s_nrm;
+    const T* s_str;              // point strengths [rhs][C][N] (weights applied)
+    long s_n;                    // N (component stride); rhs stride = C * N
+    const double* s_center;
+    const double* s_rad;
+    double s_rref;
+    const T* q;                  // surface densities [cell][rhs][C * ns]
+    const double* unit;          // [ns][3] unit sphere points (also the normals)
+    int ns;
+    // outputs
+    double* y;                   // point outputs [rhs][R][y_n]
+    long y_n;
+    T* c;                        // surface outputs [cell][rhs][R * ns]
+    int nrhs;                    // total right-hand sides (buffer strides)
+    int rhs0;                    // first rhs handled by this launch
+    int add;                     // 0: store, 1: add
+    T c2;
+    double scale;
+};
+
+template <typename T>
+__device__ __forceinline__ void kahan_add(T& hi, T& lo, T v)
+{
+    T y = v - lo;
+    T t = hi + y;
+    lo = (t - hi) - y;
+    hi = t;
+}
+
+template <int KID, bool TRANS, typename T, int NR, bool TGT_SURF, bool SRC_SURF, int TPT>
+__global__ void __launch_bounds__(EVAL_THREADS)
+eval_kernel(const EvalArgs<T> a)
+{
+    constexpr int R = kernel_dim(KID);
+    constexpr int TPB = EVAL_THREADS / TPT;  // targets per CTA
+    constexpr bool COMP = sizeof(T) == 4;    // compensated accumulation in FP32
+    __shared__ T sx[EVAL_THREADS], sy[EVAL_THREADS], sz[EVAL_THREADS];
+    __shared__ T snx[EVAL_THREADS], sny[EVAL_THREADS], snz[EVAL_THREADS];
+    __shared__ T sv[NR * R][EVAL_THREADS];
+
+    const int task = a.item_task[blockIdx.x];
+    const int t0 = a.item_start[blockIdx.x];
+    const int ntgt = a.task_tgt_count[task];
+    const int lt = threadIdx.x / TPT;
+    const int lane = threadIdx.x % TPT;
+    const int ti = t0 + lt;
+    const bool active = lt < TPB && ti < ntgt;
+    const double ox = a.task_origin[3 * task], oy = a.task_origin[3 * task + 1],
+                 oz = a.task_origin[3 * task + 2];
+    const long tb = a.task_tgt[task];
+
+    // target point relative to the origin
+    T px = 0, py = 0, pz = 0, pnx = 0, pny = 0, pnz = 0;
+    if (active) {
+        if (TGT_SURF) {
+            const double r = a.t_rad[tb];
+            const double ux = a.unit[3 * ti], uy = a.unit[3 * ti + 1], uz = a.unit[3 * ti + 2];
+            px = T(r * (a.t_rref * ux) + a.t_center[3 * tb] - ox);
+            py = T(r * (a.t_rref * uy) + a.t_center[3 * tb + 1] - oy);
+            pz = T(r * (a.t_rref * uz) + a.t_center[3 * tb + 2] - oz);
+            pnx = T(ux); pny = T(uy); pnz = T(uz);
+        } else {
+            const long p = tb + ti;
+            px = T(a.t_xyz[3 * p] - ox);
+            py = T(a.t_xyz[3 * p + 1] - oy);
+            pz = T(a.t_xyz[3 * p + 2] - oz);
+            pnx = a.t_nrm[3 * p]; pny = a.t_nrm[3 * p + 1]; pnz = a.t_nrm[3 * p + 2];
+        }
+    }
+
+    T acc[NR * R], lo[NR * R], part[NR * R];
+#pragma unroll
+    for (int i = 0; i < NR * R; i++) { acc[i] = 0; lo[i] = 0; part[i] = 0; }
+
+    const int b0 = a.task_src_ptr[task], b1 = a.task_src_ptr[task + 1];
+    const int total = b1 > b0 ? a.src_blk_prefix[b1 - 1] + a.src_blk_count[b1 - 1] : 0;
+    const int nr_here = min(NR, a.nrhs - a.rhs0);
+    int blk = b0;  // block containing this thread's next slot (advances monotonically)
+    for (int tile = 0; tile < total; tile += EVAL_THREADS) {
+        const int g = tile + threadIdx.x;
+        if (g < total) {
+            while (blk + 1 < b1 && a.src_blk_prefix[blk + 1] <= g) blk++;
+            const int li = g - a.src_blk_prefix[blk];
+            const long sb = a.src_blk[blk];
+            double qx, qy, qz;
+            T nx, ny, nz;
+            if (SRC_SURF) {
+                const double r = a.s_rad[sb];
+                const double ux = a.unit[3 * li], uy = a.unit[3 * li + 1], uz = a.unit[3 * li + 2];
+                qx = r * (a.s_rref * ux) + a.s_center[3 * sb];
+                qy = r * (a.s_rref * uy) + a.s_center[3 * sb + 1];
+                qz = r * (a.s_rref * uz) + a.s_center[3 * sb + 2];
+                nx = T(ux); ny = T(uy); nz = T(uz);
+                const int cn = R * a.ns;
+#pragma unroll
+                for (int r_ = 0; r_ < NR; r_++)
+#pragma unroll
+                    for (int d = 0; d < R; d++)
+                        sv[r_ * R + d][threadIdx.x] =
+                            r_ < nr_here ? a.q[(sb * a.nrhs + a.rhs0 + r_) * cn + d * a.ns + li] : T(0);
+            } else {
+                const long p = sb + li;
+                qx = a.s_xyz[3 * p]; qy = a.s_xyz[3 * p + 1]; qz = a.s_xyz[3 * p + 2];
+                nx = a.s_nrm[3 * p]; ny = a.s_nrm[3 * p + 1]; nz = a.s_nrm[3 * p + 2];
+#pragma unroll
+                for (int r_ = 0; r_ < NR; r_++)
+#pragma unroll
+                    for (int d = 0; d < R; d++)
+                        sv[r_ * R + d][threadIdx.x] =
+                            r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
+            }
+            sx[threadIdx.x] = T(qx - ox); sy[threadIdx.x] = T(qy - oy); sz[threadIdx.x] = T(qz - oz);
+            snx[threadIdx.x] = nx; sny[threadIdx.x] = ny; snz[threadIdx.x] = nz;
+        }
+        __syncthreads();
+        if (active) {
+            const int n_here = min(EVAL_THREADS, total - tile);
+            for (int j = lane; j < n_here; j += TPT) {
+                const T dx = sx[j] - px, dy = sy[j] - py, dz = sz[j] - pz;
+                T v[R];
+#pragma unroll
+                for (int r_ = 0; r_ < NR; r_++) {
+#pragma unroll
+                    for (int d = 0; d < R; d++) v[d] = sv[r_ * R + d][j];
+                    // transposed apply: the target is the forward source and
+                    // the source the forward observer, so the separation
+                    // (forward src - forward obs) flips sign and the normals swap
+                    if (TRANS)
+                        accumulate<KID, true, T>(-dx, -dy, -dz, snx[j], sny[j], snz[j], pnx,
+                                                 pny, pnz, a.c2, v, &part[r_ * R]);
+                    else
+                        accumulate<KID, false, T>(dx, dy, dz, pnx, pny, pnz, snx[j], sny[j],
+                                                  snz[j], a.c2, v, &part[r_ * R]);
+                }
+            }
+            if (COMP) {
+#pragma unroll
+                for (int i = 0; i < NR * R; i++) { kahan_add(acc[i], lo[i], part[i]); part[i] = 0; }
+            }
+        }
+        __syncthreads();
+    }
+    if (!COMP) {
+#pragma unroll
+        for (int i = 0; i < NR * R; i++) acc[i] = part[i];
+    }
+    // reduce the TPT partial sums of a target (consecutive lanes of one warp)
+#pragma unroll
+    for (int off = TPT / 2; off > 0; off /= 2) {
+#pragma unroll
+        for (int i = 0; i < NR * R; i++) {
+            T o = __shfl_xor_sync(0xffffffffu, acc[i], off);
+            if (COMP) {
+                // a pair (hi, lo) stands for hi - lo
+                T ol = __shfl_xor_sync(0xffffffffu, lo[i], off);
+                kahan_add(acc[i], lo[i], o);
+                lo[i] += ol;
+            } else {
+                acc[i] += o;
+            }
+        }
+    }
+    if (!active || lane != 0) return;
+    if (TGT_SURF) {
+        const int cn = R * a.ns;
+#pragma unroll
+        for (int r_ = 0; r_ < NR; r_++) {
+            if (r_ >= nr_here) break;
+#pragma unroll
+            for (int d = 0; d < R; d++) {
+                T val = T(a.scale) * (acc[r_ * R + d] - (COMP ? lo[r_ * R + d] : T(0)));
+                T* dst = &a.c[(tb * a.nrhs + a.rhs0 + r_) * cn + d * a.ns + ti];
+                *dst = a.add ? *dst + val : val;
+            }
+        }
+    } else {
+        const long p = tb + ti;
+#pragma unroll
+        for (int r_ = 0; r_ < NR; r_++) {
+            if (r_ >= nr_here) break;
+#pragma unroll
+            for (int d = 0; d < R; d++) {
+                double val = a.scale * ((double)acc[r_ * R + d] - (COMP ? (double)lo[r_ * R + d] : 0.0));
+                double* dst = &a.y[((long)(a.rhs0 + r_) * R + d) * a.y_n + p];
+                *dst = a.add ? *dst + val : val;
+            }
+        }
+    }
+}
+
+}  // namespace tbem

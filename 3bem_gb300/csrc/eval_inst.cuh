@@ -1,0 +1,46 @@
+// Instantiates the evaluation kernels of one kernel id (EVAL_KID).
+#include "eval_launch.h"
+
+namespace tbem {
+
+namespace {
+template <typename T, bool TR, bool TS, bool SS>
+cudaError_t go(int nr, int n_items, const void* args, cudaStream_t s)
+{
+    const EvalArgs<T>& a = *static_cast<const EvalArgs<T>*>(args);
+    if (n_items <= 0) return cudaSuccess;
+    if (nr == 1)
+        eval_kernel<EVAL_KID, TR, T, 1, TS, SS, 4><<<n_items, EVAL_THREADS, 0, s>>>(a);
+    else
+        eval_kernel<EVAL_KID, TR, T, EVAL_NR, TS, SS, 4><<<n_items, EVAL_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t go_t(const EvalLaunch& L, const void* args, cudaStream_t s)
+{
+    const EvalArgs<T>& a = *static_cast<const EvalArgs<T>*>(args);
+    const int nr = (a.nrhs - a.rhs0) > 1 ? EVAL_NR : 1;
+    const int idx = (L.trans ? 4 : 0) + (L.tgt_surf ? 2 : 0) + (L.src_surf ? 1 : 0);
+    switch (idx) {
+    case 0: return go<T, false, false, false>(nr, L.n_items, args, s);
+    case 1: return go<T, false, false, true>(nr, L.n_items, args, s);
+    case 2: return go<T, false, true, false>(nr, L.n_items, args, s);
+    case 3: return go<T, false, true, true>(nr, L.n_items, args, s);
+    case 4: return go<T, true, false, false>(nr, L.n_items, args, s);
+    case 5: return go<T, true, false, true>(nr, L.n_items, args, s);
+    case 6: return go<T, true, true, false>(nr, L.n_items, args, s);
+    default: return go<T, true, true, true>(nr, L.n_items, args, s);
+    }
+}
+}  // namespace
+
+#define TBEM_CAT2(a, b) a##b
+#define TBEM_CAT(a, b) TBEM_CAT2(a, b)
+cudaError_t TBEM_CAT(launch_eval_k, EVAL_KID)(const EvalLaunch& L, const void* args, bool fp32,
+                                              cudaStream_t s)
+{
+    return fp32 ? go_t<float>(L, args, s) : go_t<double>(L, args, s);
+}
+
+}  // namespace tbem

@@ -1,0 +1,42 @@
+// Host-side launcher of the obs-owner evaluation kernels (eval.cuh).
+#pragma once
+#include <cuda_runtime.h>
+#include "eval.cuh"
+
+namespace tbem {
+
+struct EvalLaunch {
+    int kid;
+    bool trans;
+    bool tgt_surf;
+    bool src_surf;
+    int n_items;
+};
+
+// One function per kernel id (eval_k<id>.cu) so that the instantiations
+// compile in parallel.
+cudaError_t launch_eval_k0(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k1(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k2(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k3(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k4(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k5(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+
+// rhs chunk per launch (the kernel keeps NR x R accumulators per thread)
+constexpr int EVAL_NR = 4;
+
+template <typename T>
+inline cudaError_t launch_eval(const EvalLaunch& L, const EvalArgs<T>& a, cudaStream_t s)
+{
+    const bool fp32 = sizeof(T) == 4;
+    switch (L.kid) {
+    case 0: return launch_eval_k0(L, &a, fp32, s);
+    case 1: return launch_eval_k1(L, &a, fp32, s);
+    case 2: return launch_eval_k2(L, &a, fp32, s);
+    case 3: return launch_eval_k3(L, &a, fp32, s);
+    case 4: return launch_eval_k4(L, &a, fp32, s);
+    default: return launch_eval_k5(L, &a, fp32, s);
+    }
+}
+
+}  // namespace tbem

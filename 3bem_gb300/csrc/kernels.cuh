@@ -1,0 +1,145 @@
+// Device-side BEM kernels (3D), templated on the arithmetic type.
+//
+// Each kernel K(x, y; n_x, n_y) is an R x C tensor evaluated with
+// delta = y - x and the reference's self-pair rule: zero when r^2 < 1e-12
+// (cpp/kernel.h:19-33).  Formulas: LaplaceSingle 1/(4 pi r)
+// (cpp/laplace_kernels.h:25), LaplaceDouble n_y.delta/(4 pi r^3) (:41),
+// ElasticDisplacement / Traction / AdjointTraction
+// (cpp/elastic_kernels.h:192-311), IdentityScalar (cpp/identity_kernels.h).
+//
+// accumulate<KID, TRANS>() adds K v (or K^T v for the transposed apply) for
+// one pair directly, without forming the tensor: the elastic kernels reduce
+// to dot products with delta and the normals.  The kernel's leading constant
+// (1/(4 pi), C1) is applied once per target by the caller (kernel_scale).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace tbem {
+
+enum KernelId { LAP_S = 0, LAP_D = 1, EL_DISP = 2, EL_TRAC = 3, EL_ADJ = 4, IDENT = 5 };
+
+__host__ __device__ constexpr int kernel_dim(int kid)
+{
+    return (kid == EL_DISP || kid == EL_TRAC || kid == EL_ADJ) ? 3 : 1;
+}
+
+// Constants of a kernel instance (mu, nu enter through c1, c2).
+struct KParams {
+    double scale;  // leading constant applied once per target
+    double c2;     // second elastic constant (3-4nu for disp, 1-2nu for traction)
+};
+
+inline KParams make_kparams(int kid, double mu, double nu)
+{
+    const double pi = 3.14159265358979323846;
+    KParams p{1.0, 0.0};
+    switch (kid) {
+    case LAP_S: p.scale = 1.0 / (4.0 * pi); break;
+    case LAP_D: p.scale = 1.0 / (4.0 * pi); break;
+    case EL_DISP: p.scale = 1.0 / (16 * pi * mu * (1 - nu)); p.c2 = 3 - 4 * nu; break;
+    case EL_TRAC:
+    case EL_ADJ: p.scale = 1.0 / (8 * pi * (1 - nu)); p.c2 = 1 - 2 * nu; break;
+    default: p.scale = 1.0; break;
+    }
+    return p;
+}
+
+template <typename T>
+__device__ __forceinline__ T dev_rsqrt(T x);
+template <>
+__device__ __forceinline__ double dev_rsqrt<double>(double x) { return rsqrt(x); }
+template <>
+__device__ __forceinline__ float dev_rsqrt<float>(float x) { return rsqrtf(x); }
+
+// u += K(x,y) v  (TRANS: u += K(x,y)^T v), without the leading constant.
+// d = y - x; no = n_x (observation normal), ns = n_y (source normal).
+// Returns false (adds nothing) for the self pair.
+template <int KID, bool TRANS, typename T>
+__device__ __forceinline__ void accumulate(T dx, T dy, T dz, T nox, T noy, T noz, T nsx, T nsy,
+                                           T nsz, T c2, const T* v, T* u)
+{
+    const T r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < T(1e-12)) return;
+    const T ir = dev_rsqrt<T>(r2);
+    if (KID == LAP_S) {
+        u[0] += v[0] * ir;
+    } else if (KID == LAP_D) {
+        const T dn = nsx * dx + nsy * dy + nsz * dz;
+        u[0] += v[0] * (dn * ir * ir * ir);
+    } else if (KID == IDENT) {
+        u[0] += v[0];
+    } else if (KID == EL_DISP) {
+        // K_kj = (1/r)(c2 delta_kj + d_k d_j / r^2): symmetric
+        const T ir2 = ir * ir;
+        const T t = (dx * v[0] + dy * v[1] + dz * v[2]) * ir2;
+        u[0] += ir * (c2 * v[0] + dx * t);
+        u[1] += ir * (c2 * v[1] + dy * t);
+        u[2] += ir * (c2 * v[2] + dz * t);
+    } else if (KID == EL_TRAC || KID == EL_ADJ) {
+        // K_kj = s/r^2 [ (c2 delta_kj + 3 d_k d_j / r^2) drdm + sgn c2 (m_j d_k - m_k d_j)/r ]
+        // with m = n_y, s = -1, sgn = -1 for the traction kernel and m = n_x,
+        // s = +1, sgn = +1 for the adjoint traction kernel.
+        const T mx = KID == EL_TRAC ? nsx : nox;
+        const T my = KID == EL_TRAC ? nsy : noy;
+        const T mz = KID == EL_TRAC ? nsz : noz;
+        const T ir2 = ir * ir;
+        const T dm = dx * mx + dy * my + dz * mz;
+        const T drdm = dm * ir;
+        const T dv = dx * v[0] + dy * v[1] + dz * v[2];
+        const T mv = mx * v[0] + my * v[1] + mz * v[2];
+        const T a = T(3) * dv * ir2;
+        // term2 contraction: sum_j (m_j d_k - m_k d_j) v_j = d_k mv - m_k dv; transposed:
+        // sum_k (m_j d_k - m_k d_j) v_k = m_j dv - d_j mv.
+        const T sg = KID == EL_TRAC ? T(-1) : T(1);
+        const T b = sg * c2 * ir;
+        const T s = (KID == EL_TRAC ? T(-1) : T(1)) * ir2;
+        if (!TRANS) {
+            u[0] += s * (drdm * (c2 * v[0] + dx * a) + b * (dx * mv - mx * dv));
+            u[1] += s * (drdm * (c2 * v[1] + dy * a) + b * (dy * mv - my * dv));
+            u[2] += s * (drdm * (c2 * v[2] + dz * a) + b * (dz * mv - mz * dv));
+        } else {
+            u[0] += s * (drdm * (c2 * v[0] + dx * a) + b * (mx * dv - dx * mv));
+            u[1] += s * (drdm * (c2 * v[1] + dy * a) + b * (my * dv - dy * mv));
+            u[2] += s * (drdm * (c2 * v[2] + dz * a) + b * (mz * dv - dz * mv));
+        }
+    }
+}
+
+// Full tensor (row-major R x C, constant included) for operator assembly.
+template <typename T>
+__device__ __forceinline__ void kernel_tensor(int kid, T dx, T dy, T dz, T nox, T noy, T noz,
+                                              T nsx, T nsy, T nsz, const KParams& p, T* out)
+{
+    const int R = kernel_dim(kid);
+    const T r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < T(1e-12)) {
+        for (int i = 0; i < R * R; i++) out[i] = 0;
+        return;
+    }
+    const T r = sqrt(r2);
+    const T d[3] = {dx, dy, dz};
+    if (kid == LAP_S) {
+        out[0] = T(p.scale) / r;
+    } else if (kid == LAP_D) {
+        out[0] = T(p.scale) * (nsx * dx + nsy * dy + nsz * dz) / (r2 * r);
+    } else if (kid == IDENT) {
+        out[0] = 1;
+    } else if (kid == EL_DISP) {
+        for (int k = 0; k < 3; k++)
+            for (int j = 0; j < 3; j++)
+                out[3 * k + j] = (T(p.scale) / r) * (T(p.c2) * (k == j) + d[k] * d[j] / r2);
+    } else {
+        const bool trac = kid == EL_TRAC;
+        const T m[3] = {trac ? nsx : nox, trac ? nsy : noy, trac ? nsz : noz};
+        const T drdm = (d[0] * m[0] + d[1] * m[1] + d[2] * m[2]) / r;
+        for (int k = 0; k < 3; k++)
+            for (int j = 0; j < 3; j++) {
+                const T term1 = T(p.c2) * (k == j) + T(3) * d[k] * d[j] / r2;
+                const T term2 = T(p.c2) * (m[j] * d[k] - m[k] * d[j]) / r;
+                out[3 * k + j] = trac ? -(T(p.scale) / r2) * (term1 * drdm - term2)
+                                      : (T(p.scale) / r2) * (term1 * drdm + term2);
+            }
+    }
+}
+
+}  // namespace tbem

@@ -1,0 +1,1221 @@
+// FMM plan construction and the apply sequences (forward and transposed),
+// for the plain FP64 form and the precision (mixed) form.
+//
+// Reference schedule (execute_tasks, cpp/fmm.cpp:445-548): P2M, M2M, P2P,
+// M2P, P2L, M2L, L2L, L2P.  Here the per-task C2E products are hoisted to
+// one grouped GEMM per level (linearity: the reference adds
+// C2E_l (K m) for every pair, this adds the K m first), the M2M / L2L / M2L
+// kernel matrices are deduplicated by translation (all cells of one level
+// share their half widths, cpp/geometry.cpp:20-28), and the levels run
+// bottom-up / top-down instead of the serial post-/pre-order walks
+// (cpp/fmm.cpp:467-482, 523-538), which respects the same dependencies.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <tuple>
+
+#include "plan.h"
+
+namespace tbem {
+
+void check_cuda(cudaError_t e, const char* what, const char* file, int line)
+{
+    if (e == cudaSuccess) return;
+    cudaGetLastError();
+    throw Error(e == cudaErrorMemoryAllocation ? TBEM_ERR_ALLOC : TBEM_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e) + " (" + file + ":" +
+                    std::to_string(line) + ")");
+}
+void check_cublas(cublasStatus_t e, const char* what, const char* file, int line)
+{
+    if (e == CUBLAS_STATUS_SUCCESS) return;
+    throw Error(TBEM_ERR_CUDA, std::string(what) + ": cuBLAS status " + std::to_string((int)e) +
+                                   " (" + file + ":" + std::to_string(line) + ")");
+}
+void check_cusolver(cusolverStatus_t e, const char* what, const char* file, int line)
+{
+    if (e == CUSOLVER_STATUS_SUCCESS) return;
+    throw Error(TBEM_ERR_CUDA, std::string(what) + ": cuSOLVER status " +
+                                   std::to_string((int)e) + " (" + file + ":" +
+                                   std::to_string(line) + ")");
+}
+
+// ------------------------------------------------------------------ helpers
+
+void TaskSet::add(long target, int count, const double* org,
+                  const std::vector<std::pair<long, int>>& srcs, int targets_per_cta)
+{
+    int pre = 0;
+    for (auto& s : srcs) pre += std::max(s.second, 0);
+    if (count <= 0 || pre == 0) return;
+    const int t = (int)tgt.size();
+    tgt.push_back(target);
+    tgt_count.push_back(count);
+    origin.insert(origin.end(), org, org + 3);
+    pre = 0;
+    for (auto& s : srcs) {
+        if (s.second <= 0) continue;
+        blk.push_back(s.first);
+        blk_count.push_back(s.second);
+        blk_prefix.push_back(pre);
+        pre += s.second;
+    }
+    src_ptr.push_back((int)blk.size());
+    n_pairs += (long)count * pre;
+    for (int st = 0; st < count; st += targets_per_cta) {
+        item_task.push_back(t);
+        item_start.push_back(st);
+    }
+}
+
+void TaskSet::upload()
+{
+    d_tgt.upload(tgt);
+    d_tgt_count.upload(tgt_count);
+    d_origin.upload(origin);
+    d_src_ptr.upload(src_ptr);
+    d_blk.upload(blk);
+    d_blk_count.upload(blk_count);
+    d_blk_prefix.upload(blk_prefix);
+    d_item_task.upload(item_task);
+    d_item_start.upload(item_start);
+}
+
+void GemmSet::add_group(long a_off, const std::vector<std::pair<int, int>>& pairs)
+{
+    if (pairs.empty()) return;
+    A_off.push_back(a_off);
+    pair0.push_back((long)in_cell.size());
+    npairs.push_back((int)pairs.size());
+    for (auto& p : pairs) {
+        in_cell.push_back(p.first);
+        out_cell.push_back(p.second);
+    }
+}
+
+void GemmSet::upload(const void* pool, size_t esz)
+{
+    std::vector<const void*> ptrs(A_off.size());
+    for (size_t g = 0; g < A_off.size(); g++)
+        ptrs[g] = static_cast<const char*>(pool) + A_off[g] * esz;
+    d_A.upload(ptrs);
+    d_pair0.upload(pair0);
+    d_npairs.upload(npairs);
+    d_in.upload(in_cell);
+    d_out.upload(out_cell);
+    tiles.clear();
+}
+
+template <typename T>
+void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s)
+{
+    if (empty()) return;
+    auto it = tiles.find(nrhs);
+    if (it == tiles.end()) {
+        std::vector<int> tg, tc;
+        for (size_t g = 0; g < npairs.size(); g++) {
+            int ncols = npairs[g] * nrhs;
+            for (int c = 0; c < ncols; c += GM_BN) {
+                tg.push_back((int)g);
+                tc.push_back(c);
+            }
+        }
+        auto& e = tiles[nrhs];
+        e.first.upload(tg);
+        e.second.upload(tc);
+        it = tiles.find(nrhs);
+    }
+    GemmArgs<T> a;
+    a.A = reinterpret_cast<const T* const*>(d_A.p);
+    a.g_pair0 = d_pair0.p;
+    a.g_npairs = d_npairs.p;
+    a.tile_group = it->second.first.p;
+    a.tile_col0 = it->second.second.p;
+    a.in_cell = d_in.p;
+    a.out_cell = d_out.p;
+    a.B = B;
+    a.D = D;
+    a.n = n;
+    a.nrhs = nrhs;
+    a.trans = trans;
+    a.mode = mode;
+    dim3 grid((unsigned)it->second.first.n, (unsigned)((n + GM_BM - 1) / GM_BM));
+    grouped_gemm_kernel<T><<<grid, GM_THREADS, 0, s>>>(a);
+    TBEM_CK(cudaGetLastError());
+}
+
+template void GemmSet::run<double>(const double*, double*, int, int, int, int, cudaStream_t);
+template void GemmSet::run<float>(const float*, float*, int, int, int, int, cudaStream_t);
+
+// ------------------------------------------------------------ device kernels
+
+namespace {
+
+// Surface point r * (rref * u) + c with the reference's rounding (no FMA),
+// TranslationSurface::scale then ::move, cpp/fmm.h:19-40.
+__device__ __forceinline__ double surf_coord(double r, double rref, double u, double c)
+{
+    return __dadd_rn(__dmul_rn(r, __dmul_rn(rref, u)), c);
+}
+
+struct SurfJob {
+    double tc[3];
+    double tr, trref;
+    double sc[3];
+    double sr, srref;
+    long out_off;
+};
+
+// Kernel matrix between two translation surfaces, the nbody_matrix layout
+// (cpp/nbody_operator.h:87-115): row d1 * ns + i, column d2 * ns + j, weight 1.
+__global__ void surf_matrix_kernel(const SurfJob* jobs, const double* unit, int ns, int kid,
+                                   KParams kp, double* out)
+{
+    const SurfJob J = jobs[blockIdx.y];
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)ns * ns) return;
+    const int i = (int)(idx / ns), j = (int)(idx % ns);
+    const int R = kernel_dim(kid);
+    const double ux = unit[3 * i], uy = unit[3 * i + 1], uz = unit[3 * i + 2];
+    const double vx = unit[3 * j], vy = unit[3 * j + 1], vz = unit[3 * j + 2];
+    const double tx = surf_coord(J.tr, J.trref, ux, J.tc[0]);
+    const double ty = surf_coord(J.tr, J.trref, uy, J.tc[1]);
+    const double tz = surf_coord(J.tr, J.trref, uz, J.tc[2]);
+    const double sx = surf_coord(J.sr, J.srref, vx, J.sc[0]);
+    const double sy = surf_coord(J.sr, J.srref, vy, J.sc[1]);
+    const double sz = surf_coord(J.sr, J.srref, vz, J.sc[2]);
+    double k[9];
+    kernel_tensor<double>(kid, sx - tx, sy - ty, sz - tz, ux, uy, uz, vx, vy, vz, kp, k);
+    const long ld = (long)R * ns;
+    double* o = out + J.out_off;
+    for (int d1 = 0; d1 < R; d1++)
+        for (int d2 = 0; d2 < R; d2++) o[((long)d1 * ns + i) * ld + (long)d2 * ns + j] = k[d1 * R + d2];
+}
+
+// Kernel matrix from a leaf's points to a cell surface: row (i * R + d1),
+// column d2 * ns + j (the per-leaf L2P operator of the precision form).
+__global__ void pts_surf_matrix_kernel(const long* pt0, const int* npts, const int* cell,
+                                       const long* row0, const double* xyz, const double* nrm,
+                                       const double* center, const double* rad, double rref,
+                                       const double* unit, int ns, int kid, KParams kp,
+                                       double* out, long out_row_base)
+{
+    const int t = blockIdx.y;
+    const int np = npts[t];
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)np * ns) return;
+    const int i = (int)(idx / ns), j = (int)(idx % ns);
+    const int R = kernel_dim(kid);
+    const long p = pt0[t] + i;
+    const int c = cell[t];
+    const double vx = unit[3 * j], vy = unit[3 * j + 1], vz = unit[3 * j + 2];
+    const double sx = surf_coord(rad[c], rref, vx, center[3 * c]);
+    const double sy = surf_coord(rad[c], rref, vy, center[3 * c + 1]);
+    const double sz = surf_coord(rad[c], rref, vz, center[3 * c + 2]);
+    double k[9];
+    kernel_tensor<double>(kid, sx - xyz[3 * p], sy - xyz[3 * p + 1], sz - xyz[3 * p + 2],
+                          nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2], vx, vy, vz, kp, k);
+    const long ld = (long)R * ns;
+    double* o = out + (row0[t] - out_row_base) * ld;
+    for (int d1 = 0; d1 < R; d1++)
+        for (int d2 = 0; d2 < R; d2++) o[((long)i * R + d1) * ld + (long)d2 * ns + j] = k[d1 * R + d2];
+}
+
+// Column k of U (column-major) times 1/s_k, or zero below the cutoff
+// (svd_pseudoinverse, cpp/blas_wrapper.cpp:96-127).
+__global__ void pinv_scale_kernel(double* U, const double* S, int N, double threshold)
+{
+    const int k = blockIdx.x;
+    const double cutoff = threshold * S[0];
+    const double f = S[k] > cutoff ? 1.0 / S[k] : 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) U[(long)k * N + i] *= f;
+}
+
+template <typename T>
+__global__ void convert_kernel(const double* in, T* out, long n)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = T(in[i]);
+}
+
+// s[r][d][i] = w[i] x[r][d][perm[i]]   (tree order; w may be null)
+template <typename T>
+__global__ void gather_kernel(const double* x, const long* perm, const double* w, T* s, long N,
+                              int C, int nrhs)
+{
+    const long total = N * C * nrhs;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long)gridDim.x * blockDim.x) {
+        const long i = t % N, rd = t / N;
+        const double v = x[rd * N + perm[i]];
+        s[t] = T(w ? w[i] * v : v);
+    }
+}
+
+// y[r][d][perm[i]] = w[i] acc[r][d][i]   (w may be null)
+__global__ void scatter_kernel(const double* acc, const long* perm, const double* w, double* y,
+                               long N, int R, int nrhs)
+{
+    const long total = N * R * nrhs;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long)gridDim.x * blockDim.x) {
+        const long i = t % N, rd = t / N;
+        y[rd * N + perm[i]] = w ? w[i] * acc[t] : acc[t];
+    }
+}
+
+__global__ void add_kernel(const double* in, float* out, long n)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] += float(in[i]);
+}
+
+__global__ void promote_kernel(const float* in, double* out, long n)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = double(in[i]);
+}
+
+// Precision-form L2P: y[r][d][pt0 + i] += sum_k E[row0 + i R + d][k] cd[leaf][r][k].
+// One CTA per leaf, one warp per output row.
+__global__ void l2p_mixed_kernel(const float* E, const long* row0, const int* leaf,
+                                 const long* pt0, const int* npts, const float* cd, int n, int R,
+                                 int nrhs, double* y, long y_n)
+{
+    const int t = blockIdx.x;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
+    const int rows = npts[t] * R;
+    const float* c0 = cd + (long)leaf[t] * nrhs * n;
+    for (int row = warp; row < rows; row += nw) {
+        const float* e = E + (row0[t] + row) * (long)n;
+        const int i = row / R, d = row % R;
+        for (int r = 0; r < nrhs; r++) {
+            const float* c = c0 + (long)r * n;
+            float acc = 0.f;
+            for (int k = lane; k < n; k += 32) acc += e[k] * c[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) y[((long)r * R + d) * y_n + pt0[t] + i] += (double)acc;
+        }
+    }
+}
+
+// Its transpose: cd[leaf][r][k] = sum_rows E[row][k] z[r][d][pt0 + i].
+__global__ void l2p_mixed_t_kernel(const float* E, const long* row0, const int* leaf,
+                                   const long* pt0, const int* npts, const float* z, long z_n,
+                                   int n, int R, int nrhs, float* cd)
+{
+    const int t = blockIdx.x;
+    const int rows = npts[t] * R;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        for (int r = 0; r < nrhs; r++) {
+            float acc = 0.f;
+            for (int row = 0; row < rows; row++) {
+                const int i = row / R, d = row % R;
+                acc += E[(row0[t] + row) * (long)n + k] * z[((long)r * R + d) * z_n + pt0[t] + i];
+            }
+            cd[((long)leaf[t] * nrhs + r) * n + k] = acc;
+        }
+    }
+}
+
+inline unsigned grid_for(long n, int threads = 256)
+{
+    long b = (n + threads - 1) / threads;
+    return (unsigned)std::max<long>(1, std::min<long>(b, 152L * 64));
+}
+
+inline double hypot_ref(const double* v)
+{
+    return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ plan
+
+Plan::~Plan()
+{
+    for (auto e : events) cudaEventDestroy(e);
+    if (cublas) cublasDestroy(cublas);
+    if (solver) cusolverDnDestroy(solver);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void Plan::upload_tree(const Tree& t, const double* locs, const double* normals,
+                       const double* weights, DTree& d)
+{
+    const long N = t.n_points();
+    std::vector<double> xyz(3 * N), nrm(3 * N), w;
+    std::vector<float> nrm32(3 * N);
+    for (long i = 0; i < N; i++) {
+        long o = t.perm[i];
+        for (int k = 0; k < 3; k++) {
+            xyz[3 * i + k] = locs[3 * o + k];
+            nrm[3 * i + k] = normals[3 * o + k];
+            nrm32[3 * i + k] = (float)normals[3 * o + k];
+        }
+    }
+    if (weights) {
+        w.resize(N);
+        for (long i = 0; i < N; i++) w[i] = weights[t.perm[i]];
+        d.w.upload(w);
+    }
+    d.xyz.upload(xyz);
+    d.nrm64.upload(nrm);
+    d.nrm32.upload(nrm32);
+    d.perm.upload(t.perm);
+    std::vector<double> c(3 * t.cells.size()), r(t.cells.size());
+    for (size_t i = 0; i < t.cells.size(); i++) {
+        for (int k = 0; k < 3; k++) c[3 * i + k] = t.cells[i].center[k];
+        r[i] = hypot_ref(t.cells[i].hw);
+    }
+    d.center.upload(c);
+    d.rad.upload(r);
+}
+
+void Plan::build(int kernel, const double* params, const double* obs_locs,
+                 const double* obs_normals, long n_obs_, const double* src_locs,
+                 const double* src_normals, const double* src_weights, long n_src_,
+                 const TbemFmmConfig& cfg_, const TbemGpuOptions& opt_)
+{
+    if (kernel < 0 || kernel > 5) throw Error(TBEM_ERR_ARG, "unknown kernel id");
+    if (cfg_.min_pts_per_cell <= 0) throw Error(TBEM_ERR_ARG, "min_pts_per_cell must be > 0");
+    if (cfg_.order <= 0) throw Error(TBEM_ERR_ARG, "order must be > 0");
+    if (!(cfg_.mac > 0)) throw Error(TBEM_ERR_ARG, "mac must be > 0");
+    if (n_obs_ < 0 || n_src_ < 0) throw Error(TBEM_ERR_ARG, "negative point count");
+    if ((n_obs_ > 0 && (!obs_locs || !obs_normals)) ||
+        (n_src_ > 0 && (!src_locs || !src_normals || !src_weights)))
+        throw Error(TBEM_ERR_ARG, "null point array");
+    if (opt_.precision != TBEM_PRECISION_FP64 && opt_.precision != TBEM_PRECISION_MIXED)
+        throw Error(TBEM_ERR_ARG, "unknown precision form");
+    kid = kernel;
+    R = kernel_dim(kid);
+    mu = (params && R == 3) ? params[0] : 1.0;
+    nu = (params && R == 3) ? params[1] : 0.25;
+    kp = make_kparams(kid, mu, nu);
+    cfg = cfg_;
+    opt = opt_;
+    if (!(opt.svd_threshold > 0)) opt.svd_threshold = 1e-10;
+    n_obs = n_obs_;
+    n_src = n_src_;
+    h_obs_locs.assign(obs_locs, obs_locs + 3 * n_obs);
+    h_obs_normals.assign(obs_normals, obs_normals + 3 * n_obs);
+    h_src_locs.assign(src_locs, src_locs + 3 * n_src);
+    h_src_normals.assign(src_normals, src_normals + 3 * n_src);
+    h_src_weights.assign(src_weights, src_weights + n_src);
+
+    if (!opt.host_only) {
+        TBEM_CK(cudaSetDevice(opt.device));
+        TBEM_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        TBEM_CKB(cublasCreate(&cublas));
+        TBEM_CKB(cublasSetStream(cublas, stream));
+        TBEM_CKS(cusolverDnCreate(&solver));
+        TBEM_CKS(cusolverDnSetStream(solver, stream));
+    }
+
+    otree = build_tree(h_obs_locs.data(), n_obs, cfg.min_pts_per_cell);
+    same_tree = n_obs == n_src &&
+                (n_obs == 0 || std::memcmp(h_obs_locs.data(), h_src_locs.data(),
+                                           3 * n_obs * sizeof(double)) == 0);
+    if (same_tree) {
+        stree = &otree;
+    } else {
+        stree_own = build_tree(h_src_locs.data(), n_src, cfg.min_pts_per_cell);
+        stree = &stree_own;
+    }
+    unit = sphere_surface(cfg.order);
+    ns = (int)(unit.size() / 3);
+    n = R * ns;
+    L = build_lists(otree, *stree, cfg.mac, ns, cfg.account_for_small_cells != 0);
+    if (opt.host_only) return;
+    d_unit.upload(unit);
+    upload_tree(otree, h_obs_locs.data(), h_obs_normals.data(), nullptr, dobs);
+    upload_tree(*stree, h_src_locs.data(), h_src_normals.data(), h_src_weights.data(), dsrc_own);
+    dsrc = &dsrc_own;
+    build_tasks();
+    build_form();
+    TBEM_CK(cudaStreamSynchronize(stream));
+}
+
+void Plan::build_tasks()
+{
+    const Tree& O = otree;
+    const Tree& S = *stree;
+    constexpr int TPB = EVAL_THREADS / 4;
+    // forward
+    for (int c : L.p2m) {
+        const Cell& cc = S.cells[c];
+        p2m.add(c, ns, cc.center, {{cc.pt_begin, (int)cc.n_points()}}, TPB);
+    }
+    std::vector<std::vector<int>> p2p_of(O.cells.size()), m2p_of(O.cells.size()),
+        p2l_of(O.cells.size()), m2l_of(O.cells.size());
+    std::vector<std::vector<int>> p2p_by_src(S.cells.size()), m2p_by_src(S.cells.size()),
+        p2l_by_src(S.cells.size()), m2l_by_src(S.cells.size());
+    for (auto& p : L.p2p) { p2p_of[p.obs].push_back(p.src); p2p_by_src[p.src].push_back(p.obs); }
+    for (auto& p : L.m2p) { m2p_of[p.obs].push_back(p.src); m2p_by_src[p.src].push_back(p.obs); }
+    for (auto& p : L.p2l) { p2l_of[p.obs].push_back(p.src); p2l_by_src[p.src].push_back(p.obs); }
+    for (auto& p : L.m2l) { m2l_of[p.obs].push_back(p.src); m2l_by_src[p.src].push_back(p.obs); }
+
+    // point targets collect the lists of the leaf and of all its ancestors
+    for (size_t c = 0; c < O.cells.size(); c++) {
+        const Cell& leaf = O.cells[c];
+        if (!leaf.is_leaf()) continue;
+        std::vector<std::pair<long, int>> pp, mp;
+        for (int a = (int)c; a >= 0; a = O.cells[a].parent) {
+            for (int s : p2p_of[a]) pp.push_back({S.cells[s].pt_begin, (int)S.cells[s].n_points()});
+            for (int s : m2p_of[a]) mp.push_back({s, ns});
+        }
+        p2p.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, TPB);
+        m2p.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, mp, TPB);
+    }
+    for (size_t c = 0; c < O.cells.size(); c++) {
+        const Cell& oc = O.cells[c];
+        std::vector<std::pair<long, int>> pl, ml;
+        for (int s : p2l_of[c]) pl.push_back({S.cells[s].pt_begin, (int)S.cells[s].n_points()});
+        for (int s : m2l_of[c]) ml.push_back({s, ns});
+        p2l.add((long)c, ns, oc.center, pl, TPB);
+        m2l_fly.add((long)c, ns, oc.center, ml, TPB);
+    }
+    for (int c : L.l2p) {
+        const Cell& cc = O.cells[c];
+        l2p.add(cc.pt_begin, (int)cc.n_points(), cc.center, {{c, ns}}, TPB);
+    }
+    // transposed: targets live in the source tree, sources in the observation tree
+    for (int c : L.p2m) {
+        const Cell& cc = S.cells[c];
+        p2m_t.add(cc.pt_begin, (int)cc.n_points(), cc.center, {{c, ns}}, TPB);
+    }
+    for (size_t c = 0; c < S.cells.size(); c++) {
+        const Cell& leaf = S.cells[c];
+        if (!leaf.is_leaf()) continue;
+        std::vector<std::pair<long, int>> pp, pl;
+        for (int a = (int)c; a >= 0; a = S.cells[a].parent) {
+            for (int o : p2p_by_src[a]) pp.push_back({O.cells[o].pt_begin, (int)O.cells[o].n_points()});
+            for (int o : p2l_by_src[a]) pl.push_back({o, ns});
+        }
+        p2p_t.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, TPB);
+        p2l_t.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pl, TPB);
+    }
+    for (size_t c = 0; c < S.cells.size(); c++) {
+        const Cell& sc = S.cells[c];
+        std::vector<std::pair<long, int>> mp, ml;
+        for (int o : m2p_by_src[c]) mp.push_back({O.cells[o].pt_begin, (int)O.cells[o].n_points()});
+        for (int o : m2l_by_src[c]) ml.push_back({o, ns});
+        m2p_t.add((long)c, ns, sc.center, mp, TPB);
+        m2l_fly_t.add((long)c, ns, sc.center, ml, TPB);
+    }
+    for (int c : L.l2p) {
+        const Cell& cc = O.cells[c];
+        l2p_t.add(c, ns, cc.center, {{cc.pt_begin, (int)cc.n_points()}}, TPB);
+    }
+    for (TaskSet* t : {&p2m, &p2p, &m2p, &p2l, &l2p, &m2l_fly, &p2m_t, &p2p_t, &m2p_t, &p2l_t,
+                       &l2p_t, &m2l_fly_t})
+        t->upload();
+
+    // dedup keys of the M2M / L2L octant translations and the M2L translations
+    const int LS = S.n_levels(), LO = O.n_levels();
+    m2m_pairs.assign(std::max(LS, 1) * 8, {});
+    m2m_canon.assign(std::max(LS, 1) * 8, {-1, -1});
+    for (int c : L.m2m) {
+        const Cell& p = S.cells[c];
+        for (int k = 0; k < p.n_children; k++) {
+            int ch = p.first_child + k;
+            int key = p.level * 8 + S.cells[ch].octant;
+            if (m2m_canon[key].first < 0) m2m_canon[key] = {c, ch};
+            m2m_pairs[key].push_back({ch, c});  // (in = child, out = parent)
+        }
+    }
+    l2l_pairs.assign(std::max(LO, 1) * 8, {});
+    l2l_canon.assign(std::max(LO, 1) * 8, {-1, -1});
+    for (int c : L.l2l) {
+        const Cell& p = O.cells[c];
+        for (int k = 0; k < p.n_children; k++) {
+            int ch = p.first_child + k;
+            int key = p.level * 8 + O.cells[ch].octant;
+            if (l2l_canon[key].first < 0) l2l_canon[key] = {c, ch};
+            l2l_pairs[key].push_back({c, ch});  // (in = parent, out = child)
+        }
+    }
+    // M2L keys: (obs level, src level, integer offset in units of the finer half width)
+    m2l_groups.clear();
+    m2l_key_ls.clear();
+    m2l_canon.clear();
+    f.m2l_on_the_fly = !same_tree;
+    if (same_tree) {
+        std::map<std::tuple<int, int, long, long, long>, int> keys;
+        for (size_t pi = 0; pi < L.m2l.size() && !f.m2l_on_the_fly; pi++) {
+            const Cell& o = O.cells[L.m2l[pi].obs];
+            const Cell& s = S.cells[L.m2l[pi].src];
+            const double* hf = o.level >= s.level ? o.hw : s.hw;
+            long off[3];
+            for (int d = 0; d < 3; d++) {
+                double delta = s.center[d] - o.center[d];
+                if (hf[d] == 0.0) {
+                    if (delta != 0.0) f.m2l_on_the_fly = true;
+                    off[d] = 0;
+                    continue;
+                }
+                double q = delta / hf[d];
+                double r = std::nearbyint(q);
+                if (std::fabs(q - r) > 1e-6 * std::max(1.0, std::fabs(q))) f.m2l_on_the_fly = true;
+                off[d] = (long)r;
+            }
+            auto key = std::make_tuple(o.level, s.level, off[0], off[1], off[2]);
+            auto it = keys.find(key);
+            int g;
+            if (it == keys.end()) {
+                g = (int)m2l_groups.size();
+                keys[key] = g;
+                m2l_groups.push_back({});
+                m2l_key_ls.push_back(s.level);
+                m2l_canon.push_back({L.m2l[pi].obs, L.m2l[pi].src});
+            } else {
+                g = it->second;
+            }
+            m2l_groups[g].push_back((int)pi);
+        }
+    }
+}
+
+// Pseudo-inverses of the check-to-equivalent systems of every level
+// (build_check_to_equiv + svd_inverse_nbody, cpp/fmm.cpp:113-160), FP64 on
+// the GPU with cuSOLVER gesvd.
+void Plan::build_c2e(Form& F)
+{
+    const Tree* trees[2] = {stree, &otree};
+    double r_eq[2] = {F.r_ue, F.r_de}, r_ck[2] = {F.r_uc, F.r_dc};
+    std::vector<SurfJob> jobs;
+    std::vector<long>* offs[2] = {&F.c2e_up_off, &F.c2e_dn_off};
+    const long nn = (long)n * n;
+    long total = 0;
+    for (int w = 0; w < 2; w++) {
+        offs[w]->clear();
+        const Tree& t = *trees[w];
+        for (int l = 0; l < t.n_levels(); l++) {
+            int c = t.first_at_level[l];
+            const Cell& cc = t.cells[c];
+            SurfJob J;
+            double r = hypot_ref(cc.hw);
+            for (int d = 0; d < 3; d++) J.tc[d] = J.sc[d] = cc.center[d];
+            J.tr = J.sr = r;
+            J.trref = r_ck[w];
+            J.srref = r_eq[w];
+            J.out_off = total;
+            jobs.push_back(J);
+            offs[w]->push_back(total);
+            total += nn;
+        }
+    }
+    F.c2e.alloc(total);
+    if (jobs.empty()) return;
+    DBuf<double> sys;
+    sys.alloc(total);
+    DBuf<SurfJob> dj;
+    dj.alloc(jobs.size());
+    TBEM_CK(cudaMemcpy(dj.p, jobs.data(), jobs.size() * sizeof(SurfJob), cudaMemcpyHostToDevice));
+    dim3 g((unsigned)((ns * ns + 255) / 256), (unsigned)jobs.size());
+    surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p, d_unit.p, ns, kid, kp, sys.p);
+    TBEM_CK(cudaGetLastError());
+    int lwork = 0;
+    TBEM_CKS(cusolverDnDgesvd_bufferSize(solver, n, n, &lwork));
+    DBuf<double> work, S, U, VT;
+    DBuf<int> info;
+    work.alloc(std::max(lwork, 1));
+    S.alloc(n);
+    U.alloc(nn);
+    VT.alloc(nn);
+    info.alloc(1);
+    for (size_t k = 0; k < jobs.size(); k++) {
+        double* A = sys.p + jobs[k].out_off;
+        // the row-major system seen column-major is A^T = U S V^T; the
+        // row-major result pinv(A) is V^T^T-times-scaled-U^T in column-major
+        char ju = 'A', jv = 'A';
+        TBEM_CKS(cusolverDnDgesvd(solver, ju, jv, n, n, A, n, S.p, U.p, n, VT.p, n, work.p, lwork,
+                                  nullptr, info.p));
+        pinv_scale_kernel<<<n, 256, 0, stream>>>(U.p, S.p, n, opt.svd_threshold);
+        TBEM_CK(cudaGetLastError());
+        const double one = 1.0, zero = 0.0;
+        TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_T, n, n, n, &one, VT.p, n, U.p, n, &zero,
+                             F.c2e.p + jobs[k].out_off, n));
+        int h_info = 0;
+        TBEM_CK(cudaMemcpyAsync(&h_info, info.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        TBEM_CK(cudaStreamSynchronize(stream));
+        if (h_info != 0)
+            throw Error(TBEM_ERR_CUDA, "cuSOLVER gesvd did not converge (info " +
+                                           std::to_string(h_info) + ")");
+    }
+}
+
+void Plan::build_form()
+{
+    Form& F = f;
+    F.mixed = opt.precision == TBEM_PRECISION_MIXED;
+    if (!F.mixed) {
+        // reference radii (cpp/fmm.h:42-66)
+        const double far = 4.0 - std::sqrt(2) - 2 * cfg.d;
+        F.r_ue = 0.3;
+        F.r_uc = far;
+        F.r_dc = 0.3;
+        F.r_de = far;
+    } else {
+        // enclosing surfaces: the down-check sphere contains the cell, so
+        // the local field is interpolated, never extrapolated
+        F.r_ue = 1.05;
+        F.r_uc = 2.5;
+        F.r_dc = 1.05;
+        F.r_de = 2.5;
+    }
+    build_c2e(F);
+    if (F.mixed) build_mixed_ops(F);
+    else build_plain_ops(F);
+}
+
+namespace {
+
+// The kernel-matrix jobs of the dedup'd translations (M2M / L2L octant
+// operators and M2L offsets) at the radii of a form.
+void translation_jobs(const Plan& P, const Form& F, std::vector<SurfJob>& jobs,
+                      std::vector<long>& m2m_off, std::vector<long>& l2l_off,
+                      std::vector<long>& m2l_off, long nn)
+{
+    const Tree& S = *P.stree;
+    const Tree& O = P.otree;
+    long total = 0;
+    auto add = [&](const Cell& t, double trr, const Cell& s, double srr) {
+        SurfJob J;
+        for (int d = 0; d < 3; d++) { J.tc[d] = t.center[d]; J.sc[d] = s.center[d]; }
+        J.tr = hypot_ref(t.hw);
+        J.sr = hypot_ref(s.hw);
+        J.trref = trr;
+        J.srref = srr;
+        J.out_off = total;
+        jobs.push_back(J);
+        total += nn;
+        return J.out_off;
+    };
+    m2m_off.assign(P.m2m_canon.size(), -1);
+    for (size_t k = 0; k < P.m2m_canon.size(); k++) {
+        if (P.m2m_canon[k].first < 0) continue;  // (parent, child): up-check(parent) <- up-equiv(child)
+        m2m_off[k] = add(S.cells[P.m2m_canon[k].first], F.r_uc, S.cells[P.m2m_canon[k].second], F.r_ue);
+    }
+    l2l_off.assign(P.l2l_canon.size(), -1);
+    for (size_t k = 0; k < P.l2l_canon.size(); k++) {
+        if (P.l2l_canon[k].first < 0) continue;  // (parent, child): down-check(child) <- down-equiv(parent)
+        l2l_off[k] = add(O.cells[P.l2l_canon[k].second], F.r_dc, O.cells[P.l2l_canon[k].first], F.r_de);
+    }
+    m2l_off.assign(P.m2l_canon.size(), -1);
+    for (size_t k = 0; k < P.m2l_canon.size(); k++)  // down-check(obs) <- up-equiv(src)
+        m2l_off[k] = add(O.cells[P.m2l_canon[k].first], F.r_dc, S.cells[P.m2l_canon[k].second], F.r_ue);
+}
+
+}  // namespace
+
+void Plan::build_gemm_sets(Form& F, long, long, long, const std::vector<long>& m2m_off,
+                           const std::vector<long>& l2l_off, const std::vector<long>& m2l_off)
+{
+    const Tree& S = *stree;
+    const Tree& O = otree;
+    const int LS = S.n_levels(), LO = O.n_levels();
+    auto swap_pairs = [](const std::vector<std::pair<int, int>>& v) {
+        std::vector<std::pair<int, int>> o(v.size());
+        for (size_t i = 0; i < v.size(); i++) o[i] = {v[i].second, v[i].first};
+        return o;
+    };
+    F.m2m.clear();
+    F.m2m.resize(std::max(LS, 0));
+    F.m2m_t.clear();
+    F.m2m_t.resize(std::max(LS, 0));
+    for (int l = 0; l < LS; l++)
+        for (int o = 0; o < 8; o++) {
+            int key = l * 8 + o;
+            if (m2m_off[key] < 0) continue;
+            F.m2m[l].add_group(m2m_off[key], m2m_pairs[key]);
+            F.m2m_t[l].add_group(m2m_off[key], swap_pairs(m2m_pairs[key]));
+        }
+    F.l2l.clear();
+    F.l2l.resize(std::max(LO, 0));
+    F.l2l_t.clear();
+    F.l2l_t.resize(std::max(LO, 0));
+    for (int l = 0; l < LO; l++)
+        for (int o = 0; o < 8; o++) {
+            int key = l * 8 + o;
+            if (l2l_off[key] < 0) continue;
+            F.l2l[l].add_group(l2l_off[key], l2l_pairs[key]);
+            F.l2l_t[l].add_group(l2l_off[key], swap_pairs(l2l_pairs[key]));
+        }
+    F.m2l = GemmSet();
+    F.m2l_t = GemmSet();
+    for (size_t k = 0; k < m2l_groups.size(); k++) {
+        std::vector<std::pair<int, int>> pr;
+        for (int pi : m2l_groups[k]) pr.push_back({L.m2l[pi].src, L.m2l[pi].obs});
+        F.m2l.add_group(m2l_off[k], pr);
+        F.m2l_t.add_group(m2l_off[k], swap_pairs(pr));
+    }
+    const void* pool = F.mixed ? (const void*)F.ops32.p : (const void*)F.ops64.p;
+    const size_t esz = F.mixed ? sizeof(float) : sizeof(double);
+    for (auto& g : F.m2m) g.upload(pool, esz);
+    for (auto& g : F.m2m_t) g.upload(pool, esz);
+    for (auto& g : F.l2l) g.upload(pool, esz);
+    for (auto& g : F.l2l_t) g.upload(pool, esz);
+    F.m2l.upload(pool, esz);
+    F.m2l_t.upload(pool, esz);
+    // check-to-equivalent products, one group per level (FP64 pool)
+    F.c2e_up.clear();
+    F.c2e_up.resize(LS);
+    F.c2e_up_t.clear();
+    F.c2e_up_t.resize(LS);
+    for (int l = 0; l < LS; l++) {
+        std::vector<std::pair<int, int>> pr;
+        for (int c = S.level_start[l]; c < S.level_start[l + 1]; c++) pr.push_back({c, c});
+        F.c2e_up[l].add_group(F.c2e_up_off[l], pr);
+        F.c2e_up_t[l].add_group(F.c2e_up_off[l], pr);
+        F.c2e_up[l].upload(F.c2e.p, sizeof(double));
+        F.c2e_up_t[l].upload(F.c2e.p, sizeof(double));
+    }
+    F.c2e_dn.clear();
+    F.c2e_dn.resize(LO);
+    F.c2e_dn_t.clear();
+    F.c2e_dn_t.resize(LO);
+    for (int l = 0; l < LO; l++) {
+        std::vector<std::pair<int, int>> pr;
+        for (int c = O.level_start[l]; c < O.level_start[l + 1]; c++) pr.push_back({c, c});
+        F.c2e_dn[l].add_group(F.c2e_dn_off[l], pr);
+        F.c2e_dn_t[l].add_group(F.c2e_dn_off[l], pr);
+        F.c2e_dn[l].upload(F.c2e.p, sizeof(double));
+        F.c2e_dn_t[l].upload(F.c2e.p, sizeof(double));
+    }
+}
+
+void Plan::build_plain_ops(Form& F)
+{
+    const long nn = (long)n * n;
+    std::vector<SurfJob> jobs;
+    std::vector<long> m2m_off, l2l_off, m2l_off;
+    translation_jobs(*this, F, jobs, m2m_off, l2l_off, m2l_off, nn);
+    F.ops64.alloc(std::max<long>((long)jobs.size() * nn, 1));
+    if (!jobs.empty()) {
+        DBuf<SurfJob> dj;
+        dj.alloc(jobs.size());
+        TBEM_CK(cudaMemcpy(dj.p, jobs.data(), jobs.size() * sizeof(SurfJob), cudaMemcpyHostToDevice));
+        for (size_t j0 = 0; j0 < jobs.size(); j0 += 32768) {
+            unsigned nj = (unsigned)std::min<size_t>(32768, jobs.size() - j0);
+            dim3 g((unsigned)((ns * ns + 255) / 256), nj);
+            surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p + j0, d_unit.p, ns, kid, kp, F.ops64.p);
+            TBEM_CK(cudaGetLastError());
+        }
+        TBEM_CK(cudaStreamSynchronize(stream));
+    }
+    build_gemm_sets(F, 0, 0, 0, m2m_off, l2l_off, m2l_off);
+}
+
+void Plan::build_mixed_ops(Form& F)
+{
+    const long nn = (long)n * n;
+    std::vector<SurfJob> jobs;
+    std::vector<long> m2m_off, l2l_off, m2l_off;
+    translation_jobs(*this, F, jobs, m2m_off, l2l_off, m2l_off, nn);
+    const long total = (long)jobs.size() * nn;
+    F.ops32.alloc(std::max<long>(total, 1));
+    const double one = 1.0, zero = 0.0;
+    // combined operator of job k: K_k * C2E(level of the k-th operator's source side)
+    std::vector<long> c2e_of(jobs.size(), -1);
+    {
+        const Tree& S = *stree;
+        const Tree& O = otree;
+        for (size_t k = 0; k < m2m_off.size(); k++)
+            if (m2m_off[k] >= 0) c2e_of[m2m_off[k] / nn] = F.c2e_up_off[S.cells[m2m_canon[k].second].level];
+        for (size_t k = 0; k < l2l_off.size(); k++)
+            if (l2l_off[k] >= 0) c2e_of[l2l_off[k] / nn] = F.c2e_dn_off[O.cells[l2l_canon[k].first].level];
+        for (size_t k = 0; k < m2l_off.size(); k++)
+            c2e_of[m2l_off[k] / nn] = F.c2e_up_off[S.cells[m2l_canon[k].second].level];
+    }
+    if (!jobs.empty()) {
+        // in chunks to bound the FP64 scratch
+        const size_t chunk = std::max<size_t>(1, (size_t)(2e9 / (8.0 * nn)));
+        DBuf<double> K, Y;
+        DBuf<SurfJob> dj;
+        K.alloc(std::min(chunk, jobs.size()) * nn);
+        Y.alloc(std::min(chunk, jobs.size()) * nn);
+        for (size_t j0 = 0; j0 < jobs.size(); j0 += chunk) {
+            size_t nj = std::min(chunk, jobs.size() - j0);
+            std::vector<SurfJob> sub(jobs.begin() + j0, jobs.begin() + j0 + nj);
+            for (size_t k = 0; k < nj; k++) sub[k].out_off = (long)k * nn;
+            dj.alloc(nj);
+            TBEM_CK(cudaMemcpy(dj.p, sub.data(), nj * sizeof(SurfJob), cudaMemcpyHostToDevice));
+            dim3 g((unsigned)((ns * ns + 255) / 256), (unsigned)nj);
+            surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p, d_unit.p, ns, kid, kp, K.p);
+            TBEM_CK(cudaGetLastError());
+            for (size_t k = 0; k < nj; k++) {
+                // row-major Y = K * C  <=>  column-major Y^T = C^T K^T
+                TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one,
+                                     F.c2e.p + c2e_of[j0 + k], n, K.p + k * nn, n, &zero,
+                                     Y.p + k * nn, n));
+            }
+            convert_kernel<float><<<grid_for(nj * nn), 256, 0, stream>>>(Y.p, F.ops32.p + j0 * nn, nj * nn);
+            TBEM_CK(cudaGetLastError());
+            TBEM_CK(cudaStreamSynchronize(stream));
+        }
+    }
+    build_gemm_sets(F, 0, 0, 0, m2m_off, l2l_off, m2l_off);
+
+    // per-leaf L2P operators E = K(points, down-equiv) * C2E_down(level)
+    const Tree& O = otree;
+    std::vector<int> leaves(L.l2p.begin(), L.l2p.end());
+    std::stable_sort(leaves.begin(), leaves.end(),
+                     [&](int a, int b) { return O.cells[a].level < O.cells[b].level; });
+    std::vector<long> row0, pt0;
+    std::vector<int> cell, npts;
+    long rows = 0;
+    for (int c : leaves) {
+        const Cell& cc = O.cells[c];
+        if (cc.n_points() == 0) continue;
+        row0.push_back(rows);
+        pt0.push_back(cc.pt_begin);
+        cell.push_back(c);
+        npts.push_back((int)cc.n_points());
+        rows += cc.n_points() * R;
+    }
+    F.n_l2p = (int)cell.size();
+    F.E.alloc(std::max<long>(rows * n, 1));
+    F.E_row0.upload(row0);
+    F.E_pt0.upload(pt0);
+    F.E_leaf.upload(cell);
+    F.E_npts.upload(npts);
+    if (rows > 0) {
+        const long max_rows = std::max<long>((long)R * 64, (long)(1.5e9 / (8.0 * n)));
+        DBuf<double> K, Y;
+        // chunks of consecutive leaves of one level
+        size_t t0 = 0;
+        while (t0 < cell.size()) {
+            const int lev = O.cells[cell[t0]].level;
+            size_t t1 = t0;
+            long r = 0;
+            while (t1 < cell.size() && O.cells[cell[t1]].level == lev &&
+                   (r + (long)npts[t1] * R <= max_rows || t1 == t0)) {
+                r += (long)npts[t1] * R;
+                t1++;
+            }
+            K.ensure(r * n);
+            Y.ensure(r * n);
+            int maxp = 0;
+            for (size_t t = t0; t < t1; t++) maxp = std::max(maxp, npts[t]);
+            dim3 g((unsigned)(((long)maxp * ns + 255) / 256), (unsigned)(t1 - t0));
+            pts_surf_matrix_kernel<<<g, 256, 0, stream>>>(
+                F.E_pt0.p + t0, F.E_npts.p + t0, F.E_leaf.p + t0, F.E_row0.p + t0, dobs.xyz.p,
+                dobs.nrm64.p, dobs.center.p, dobs.rad.p, F.r_de, d_unit.p, ns, kid, kp, K.p,
+                row0[t0]);
+            TBEM_CK(cudaGetLastError());
+            TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)r, n, &one,
+                                 F.c2e.p + F.c2e_dn_off[lev], n, K.p, n, &zero, Y.p, n));
+            convert_kernel<float><<<grid_for(r * n), 256, 0, stream>>>(Y.p, F.E.p + row0[t0] * n, r * n);
+            TBEM_CK(cudaGetLastError());
+            TBEM_CK(cudaStreamSynchronize(stream));
+            t0 = t1;
+        }
+    }
+}
+
+void Plan::set_c2e(int which, long level, const double* op)
+{
+    if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
+    if (f.mixed) throw Error(TBEM_ERR_STATE, "set_c2e is only valid for the FP64 form");
+    const auto& offs = which == 0 ? f.c2e_up_off : f.c2e_dn_off;
+    if (level < 0 || level >= (long)offs.size()) throw Error(TBEM_ERR_ARG, "level out of range");
+    TBEM_CK(cudaMemcpy(f.c2e.p + offs[level], op, (size_t)n * n * sizeof(double),
+                       cudaMemcpyHostToDevice));
+}
+
+void Plan::get_c2e(int which, long level, double* out) const
+{
+    if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
+    const auto& offs = which == 0 ? f.c2e_up_off : f.c2e_dn_off;
+    if (level < 0 || level >= (long)offs.size()) throw Error(TBEM_ERR_ARG, "level out of range");
+    TBEM_CK(cudaMemcpy(out, f.c2e.p + offs[level], (size_t)n * n * sizeof(double),
+                       cudaMemcpyDeviceToHost));
+}
+
+// ------------------------------------------------------------------ apply
+
+void Plan::ensure_rhs(int nrhs)
+{
+    if (nrhs <= cap_rhs) return;
+    const long ncs = (long)stree->cells.size(), nco = (long)otree.cells.size();
+    const long N = std::max(n_obs, n_src);
+    io_x.ensure((size_t)R * std::max<long>(n_src, n_obs) * nrhs);
+    io_y.ensure((size_t)R * N * nrhs);
+    s64.ensure((size_t)R * N * nrhs);
+    y64.ensure((size_t)R * N * nrhs);
+    if (f.mixed) {
+        s32.ensure((size_t)R * N * nrhs);
+        cu32.ensure((size_t)ncs * nrhs * n);
+        cd32.ensure((size_t)nco * nrhs * n);
+        if (!L.m2p.empty() || f.m2l_on_the_fly) {
+            cu64.ensure((size_t)ncs * nrhs * n);
+            qu64.ensure((size_t)ncs * nrhs * n);
+            cd64.ensure((size_t)nco * nrhs * n);
+        }
+    } else {
+        cu64.ensure((size_t)ncs * nrhs * n);
+        qu64.ensure((size_t)ncs * nrhs * n);
+        cd64.ensure((size_t)nco * nrhs * n);
+        qd64.ensure((size_t)nco * nrhs * n);
+    }
+    cap_rhs = nrhs;
+}
+
+void Plan::mark(const char* name, cudaStream_t s)
+{
+    if (!timing) return;
+    cudaEvent_t e;
+    TBEM_CK(cudaEventCreate(&e));
+    TBEM_CK(cudaEventRecord(e, s));
+    events.push_back(e);
+    phase_ms.push_back({name, 0.0});
+}
+
+template <typename T>
+void Plan::eval(const TaskSet& ts, int, bool tgt_surf, bool src_surf, const Tree&,
+                const DTree& dt, double t_rref, const DTree& ds, double s_rref, const T* s_str,
+                long s_n, const T* q, double* y, long y_n, T* c, int add, int nrhs,
+                cudaStream_t s, bool trans)
+{
+    if (ts.n_items() == 0) return;
+    EvalArgs<T> a;
+    ts.fill(a);
+    a.t_xyz = dt.xyz.p;
+    if constexpr (sizeof(T) == 4) a.t_nrm = dt.nrm32.p; else a.t_nrm = dt.nrm64.p;
+    a.t_center = dt.center.p;
+    a.t_rad = dt.rad.p;
+    a.t_rref = t_rref;
+    a.s_xyz = ds.xyz.p;
+    if constexpr (sizeof(T) == 4) a.s_nrm = ds.nrm32.p; else a.s_nrm = ds.nrm64.p;
+    a.s_str = s_str;
+    a.s_n = s_n;
+    a.s_center = ds.center.p;
+    a.s_rad = ds.rad.p;
+    a.s_rref = s_rref;
+    a.q = q;
+    a.unit = d_unit.p;
+    a.ns = ns;
+    a.y = y;
+    a.y_n = y_n;
+    a.c = c;
+    a.nrhs = nrhs;
+    a.add = add;
+    a.c2 = T(kp.c2);
+    a.scale = kp.scale;
+    EvalLaunch Lc{kid, trans, tgt_surf, src_surf, ts.n_items()};
+    for (int r0 = 0; r0 < nrhs; r0 += (nrhs - r0 > 1 ? EVAL_NR : 1)) {
+        a.rhs0 = r0;
+        TBEM_CK(launch_eval<T>(Lc, a, s));
+    }
+}
+
+void Plan::forward(int nrhs, cudaStream_t s)
+{
+    const Tree& S = *stree;
+    const Tree& O = otree;
+    const long NS = n_src, NO = n_obs;
+    const long ncs = (long)S.cells.size(), nco = (long)O.cells.size();
+    Form& F = f;
+    mark("start", s);
+    TBEM_CK(cudaMemsetAsync(y64.p, 0, sizeof(double) * R * NO * nrhs, s));
+    if (!F.mixed) {
+        gather_kernel<double><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s64.p, NS, R, nrhs);
+        TBEM_CK(cudaGetLastError());
+        TBEM_CK(cudaMemsetAsync(cu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
+        TBEM_CK(cudaMemsetAsync(cd64.p, 0, sizeof(double) * nco * nrhs * n, s));
+        mark("gather", s);
+        eval<double>(p2m, 0, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cu64.p, 0, nrhs, s, false);
+        mark("p2m", s);
+        for (int l = S.n_levels() - 1; l >= 0; l--) {
+            if (l < (int)F.m2m.size()) F.m2m[l].run<double>(qu64.p, cu64.p, n, nrhs, 0, GEMM_ATOMIC, s);
+            F.c2e_up[l].run<double>(cu64.p, qu64.p, n, nrhs, 0, GEMM_STORE, s);
+        }
+        mark("m2m+c2e_up", s);
+        eval<double>(p2p, 0, false, false, O, dobs, 0, *dsrc, 0, s64.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
+        mark("p2p", s);
+        eval<double>(m2p, 0, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+        eval<double>(p2l, 0, true, false, O, dobs, F.r_dc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cd64.p, 1, nrhs, s, false);
+        mark("m2p+p2l", s);
+        if (F.m2l_on_the_fly)
+            eval<double>(m2l_fly, 0, true, true, O, dobs, F.r_dc, *dsrc, F.r_ue, nullptr, 0, qu64.p, nullptr, 0, cd64.p, 1, nrhs, s, false);
+        else
+            F.m2l.run<double>(qu64.p, cd64.p, n, nrhs, 0, GEMM_ATOMIC, s);
+        mark("m2l", s);
+        for (int l = 0; l < O.n_levels(); l++) {
+            if (l > 0 && l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<double>(qd64.p, cd64.p, n, nrhs, 0, GEMM_ADD, s);
+            F.c2e_dn[l].run<double>(cd64.p, qd64.p, n, nrhs, 0, GEMM_STORE, s);
+        }
+        mark("l2l+c2e_down", s);
+        eval<double>(l2p, 0, false, true, O, dobs, 0, dobs, F.r_de, nullptr, 0, qd64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+        mark("l2p", s);
+    } else {
+        gather_kernel<float><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s32.p, NS, R, nrhs);
+        TBEM_CK(cudaGetLastError());
+        TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
+        TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
+        mark("gather", s);
+        eval<float>(p2m, 0, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
+        mark("p2m", s);
+        for (int l = S.n_levels() - 1; l >= 0; l--)
+            if (l < (int)F.m2m.size()) F.m2m[l].run<float>(cu32.p, cu32.p, n, nrhs, 0, GEMM_ATOMIC, s);
+        mark("m2m", s);
+        eval<float>(p2p, 0, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
+        mark("p2p", s);
+        const bool need64 = !L.m2p.empty() || F.m2l_on_the_fly;
+        if (need64) {
+            // explicit equivalent densities in FP64 (see the form notes)
+            promote_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu32.p, cu64.p, ncs * nrhs * n);
+            TBEM_CK(cudaGetLastError());
+            for (int l = 0; l < S.n_levels(); l++) F.c2e_up[l].run<double>(cu64.p, qu64.p, n, nrhs, 0, GEMM_STORE, s);
+            eval<double>(m2p, 0, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+        }
+        eval<float>(p2l, 0, true, false, O, dobs, F.r_dc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cd32.p, 1, nrhs, s, false);
+        mark("m2p+p2l", s);
+        if (F.m2l_on_the_fly) {
+            TBEM_CK(cudaMemsetAsync(cd64.p, 0, sizeof(double) * nco * nrhs * n, s));
+            eval<double>(m2l_fly, 0, true, true, O, dobs, F.r_dc, *dsrc, F.r_ue, nullptr, 0, qu64.p, nullptr, 0, cd64.p, 1, nrhs, s, false);
+            add_kernel<<<grid_for(nco * nrhs * n), 256, 0, s>>>(cd64.p, cd32.p, nco * nrhs * n);
+            TBEM_CK(cudaGetLastError());
+        } else {
+            F.m2l.run<float>(cu32.p, cd32.p, n, nrhs, 0, GEMM_ATOMIC, s);
+        }
+        mark("m2l", s);
+        for (int l = 1; l < O.n_levels(); l++)
+            if (l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 0, GEMM_ADD, s);
+        mark("l2l", s);
+        if (F.n_l2p > 0) {
+            l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cd32.p, n, R, nrhs, y64.p, NO);
+            TBEM_CK(cudaGetLastError());
+        }
+        mark("l2p", s);
+    }
+    scatter_kernel<<<grid_for(NO * R * nrhs), 256, 0, s>>>(y64.p, dobs.perm.p, nullptr, io_y.p, NO, R, nrhs);
+    TBEM_CK(cudaGetLastError());
+    mark("scatter", s);
+}
+
+void Plan::adjoint(int nrhs, cudaStream_t s)
+{
+    const Tree& S = *stree;
+    const Tree& O = otree;
+    const long NS = n_src, NO = n_obs;
+    const long ncs = (long)S.cells.size(), nco = (long)O.cells.size();
+    Form& F = f;
+    mark("start", s);
+    // y64 holds the transposed inputs (observation space, tree order), s64 the
+    // accumulated outputs (source space) before the weights
+    TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * NS * nrhs, s));
+    if (!F.mixed) {
+        gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
+        TBEM_CK(cudaGetLastError());
+        TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
+        TBEM_CK(cudaMemsetAsync(qd64.p, 0, sizeof(double) * nco * nrhs * n, s));
+        // L2P^T, M2P^T, P2P^T
+        eval<double>(l2p_t, 0, true, false, O, dobs, F.r_de, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qd64.p, 1, nrhs, s, true);
+        eval<double>(m2p_t, 0, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
+        eval<double>(p2p_t, 0, false, false, S, *dsrc, 0, dobs, 0, y64.p, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
+        // down pass reversed: deepest level first
+        for (int l = O.n_levels() - 1; l >= 0; l--) {
+            F.c2e_dn_t[l].run<double>(qd64.p, cd64.p, n, nrhs, 1, GEMM_STORE, s);
+            if (l > 0 && l - 1 < (int)F.l2l_t.size()) F.l2l_t[l - 1].run<double>(cd64.p, qd64.p, n, nrhs, 1, GEMM_ATOMIC, s);
+        }
+        if (F.m2l_on_the_fly)
+            eval<double>(m2l_fly_t, 0, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
+        else
+            F.m2l_t.run<double>(cd64.p, qu64.p, n, nrhs, 1, GEMM_ATOMIC, s);
+        eval<double>(p2l_t, 0, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+        // up pass reversed: root first
+        for (int l = 0; l < S.n_levels(); l++) {
+            F.c2e_up_t[l].run<double>(qu64.p, cu64.p, n, nrhs, 1, GEMM_STORE, s);
+            if (l < (int)F.m2m_t.size()) F.m2m_t[l].run<double>(cu64.p, qu64.p, n, nrhs, 1, GEMM_ADD, s);
+        }
+        eval<double>(p2m_t, 0, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+    } else {
+        gather_kernel<float><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, s32.p, NO, R, nrhs);
+        TBEM_CK(cudaGetLastError());
+        TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
+        TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
+        if (F.n_l2p > 0) {
+            l2p_mixed_t_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, s32.p, NO, n, R, nrhs, cd32.p);
+            TBEM_CK(cudaGetLastError());
+        }
+        eval<float>(p2p_t, 0, false, false, S, *dsrc, 0, dobs, 0, s32.p, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
+        const bool need64 = !L.m2p.empty() || F.m2l_on_the_fly;
+        if (need64) {
+            TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
+            // obs-space inputs in FP64 for the FP64 sub-paths
+            gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
+            TBEM_CK(cudaGetLastError());
+            eval<double>(m2p_t, 0, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
+        }
+        for (int l = O.n_levels() - 1; l >= 1; l--)
+            if (l - 1 < (int)F.l2l_t.size()) F.l2l_t[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 1, GEMM_ATOMIC, s);
+        if (F.m2l_on_the_fly) {
+            promote_kernel<<<grid_for(nco * nrhs * n), 256, 0, s>>>(cd32.p, cd64.p, nco * nrhs * n);
+            TBEM_CK(cudaGetLastError());
+            eval<double>(m2l_fly_t, 0, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
+        } else {
+            F.m2l_t.run<float>(cd32.p, cu32.p, n, nrhs, 1, GEMM_ATOMIC, s);
+        }
+        if (need64) {
+            // g_cup += C2E_up^T g_qup  (FP64), folded into the FP32 buffer
+            for (int l = 0; l < S.n_levels(); l++) F.c2e_up_t[l].run<double>(qu64.p, cu64.p, n, nrhs, 1, GEMM_STORE, s);
+            add_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu64.p, cu32.p, ncs * nrhs * n);
+            TBEM_CK(cudaGetLastError());
+        }
+        eval<float>(p2l_t, 0, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+        for (int l = 0; l < S.n_levels(); l++)
+            if (l < (int)F.m2m_t.size()) F.m2m_t[l].run<float>(cu32.p, cu32.p, n, nrhs, 1, GEMM_ADD, s);
+        eval<float>(p2m_t, 0, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+    }
+    scatter_kernel<<<grid_for(NS * R * nrhs), 256, 0, s>>>(s64.p, dsrc->perm.p, dsrc->w.p, io_y.p, NS, R, nrhs);
+    TBEM_CK(cudaGetLastError());
+    mark("scatter", s);
+}
+
+void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
+{
+    if (nrhs <= 0) throw Error(TBEM_ERR_ARG, "n_rhs must be > 0");
+    if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
+    if (!s) s = stream;
+    const long n_in = adj ? (long)R * n_obs : (long)R * n_src;
+    const long n_out = adj ? (long)R * n_src : (long)R * n_obs;
+    if (n_out == 0) return;
+    cudaPointerAttributes ax{}, ay{};
+    bool x_dev = x && cudaPointerGetAttributes(&ax, x) == cudaSuccess &&
+                 (ax.type == cudaMemoryTypeDevice || ax.type == cudaMemoryTypeManaged);
+    bool y_dev = y && cudaPointerGetAttributes(&ay, y) == cudaSuccess &&
+                 (ay.type == cudaMemoryTypeDevice || ay.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    if (n_in == 0) {
+        if (y_dev) TBEM_CK(cudaMemsetAsync(y, 0, sizeof(double) * n_out * nrhs, s));
+        else std::memset(y, 0, sizeof(double) * n_out * nrhs);
+        if (y_dev) TBEM_CK(cudaStreamSynchronize(s));
+        return;
+    }
+    ensure_rhs(nrhs);
+    for (auto e : events) cudaEventDestroy(e);
+    events.clear();
+    phase_ms.clear();
+    TBEM_CK(cudaMemcpyAsync(io_x.p, x, sizeof(double) * n_in * nrhs,
+                            x_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    if (adj) adjoint(nrhs, s);
+    else forward(nrhs, s);
+    TBEM_CK(cudaMemcpyAsync(y, io_y.p, sizeof(double) * n_out * nrhs,
+                            y_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    if (!y_dev || timing) TBEM_CK(cudaStreamSynchronize(s));
+    if (timing && events.size() > 1) {
+        for (size_t i = 1; i < events.size(); i++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, events[i - 1], events[i]);
+            phase_ms[i].second = ms;
+        }
+    }
+}
+
+}  // namespace tbem

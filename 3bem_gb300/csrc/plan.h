@@ -1,0 +1,243 @@
+// FMM plan: everything built once per geometry (the reference's FMMOperator
+// constructor, cpp/fmm.cpp:72-101) and the apply sequences.
+#pragma once
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/tbem_gpu.h"
+#include "eval_launch.h"
+#include "gemm.cuh"
+#include "kernels.cuh"
+#include "tree.h"
+
+namespace tbem {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// Records the message returned by tbem_last_error() on the calling thread.
+void set_last_error(const std::string& msg);
+
+void check_cuda(cudaError_t e, const char* what, const char* file, int line);
+void check_cublas(cublasStatus_t e, const char* what, const char* file, int line);
+void check_cusolver(cusolverStatus_t e, const char* what, const char* file, int line);
+#define TBEM_CK(x) ::tbem::check_cuda((x), #x, __FILE__, __LINE__)
+#define TBEM_CKB(x) ::tbem::check_cublas((x), #x, __FILE__, __LINE__)
+#define TBEM_CKS(x) ::tbem::check_cusolver((x), #x, __FILE__, __LINE__)
+
+// Owning device buffer.
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf& operator=(DBuf&& o) noexcept
+    {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count)
+    {
+        if (count == n && p) return;
+        release();
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            throw Error(TBEM_ERR_ALLOC, "cudaMalloc of " + std::to_string(count * sizeof(T)) +
+                                            " bytes failed: " + cudaGetErrorString(e));
+        }
+        n = count;
+    }
+    void ensure(size_t count)
+    {
+        if (count > n) alloc(count);
+    }
+    void upload(const std::vector<T>& v)
+    {
+        alloc(v.size());
+        if (!v.empty()) TBEM_CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    std::vector<T> download() const
+    {
+        std::vector<T> v(n);
+        if (n) TBEM_CK(cudaMemcpy(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
+        return v;
+    }
+};
+
+// A set of obs-owner evaluation tasks (eval.cuh).
+struct TaskSet {
+    std::vector<long> tgt;
+    std::vector<int> tgt_count;
+    std::vector<double> origin;
+    std::vector<int> src_ptr{0};
+    std::vector<long> blk;
+    std::vector<int> blk_count, blk_prefix;
+    std::vector<int> item_task, item_start;
+    DBuf<long> d_tgt, d_blk;
+    DBuf<int> d_tgt_count, d_src_ptr, d_blk_count, d_blk_prefix, d_item_task, d_item_start;
+    DBuf<double> d_origin;
+    long n_pairs = 0;  // sum over tasks of targets x sources (work estimate)
+
+    int n_tasks() const { return (int)tgt.size(); }
+    int n_items() const { return (int)item_task.size(); }
+    void add(long target, int count, const double* org, const std::vector<std::pair<long, int>>& srcs,
+             int targets_per_cta);
+    void upload();
+    template <typename T>
+    void fill(EvalArgs<T>& a) const
+    {
+        a.item_task = d_item_task.p;
+        a.item_start = d_item_start.p;
+        a.task_tgt = d_tgt.p;
+        a.task_tgt_count = d_tgt_count.p;
+        a.task_origin = d_origin.p;
+        a.task_src_ptr = d_src_ptr.p;
+        a.src_blk = d_blk.p;
+        a.src_blk_count = d_blk_count.p;
+        a.src_blk_prefix = d_blk_prefix.p;
+    }
+};
+
+// A set of GEMM groups (gemm.cuh) sharing B and D buffers.
+struct GemmSet {
+    std::vector<long> A_off;  // operator offsets (elements) into an operator pool
+    std::vector<long> pair0;
+    std::vector<int> npairs;
+    std::vector<int> in_cell, out_cell;
+    DBuf<long> d_pair0;
+    DBuf<int> d_npairs, d_in, d_out;
+    DBuf<const void*> d_A;  // resolved pointers
+    std::map<int, std::pair<DBuf<int>, DBuf<int>>> tiles;  // per nrhs
+    long total_pairs() const { return (long)in_cell.size(); }
+    bool empty() const { return in_cell.empty(); }
+    void add_group(long a_off, const std::vector<std::pair<int, int>>& pairs);
+    void upload(const void* pool, size_t elem_size);
+    template <typename T>
+    void run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s);
+};
+
+struct DTree {
+    DBuf<double> center, rad, xyz, w;
+    DBuf<double> nrm64;
+    DBuf<float> nrm32;
+    DBuf<long> perm;
+};
+
+// Operators and task sets of one precision form.
+struct Form {
+    bool mixed = false;
+    double r_ue = 0, r_uc = 0, r_dc = 0, r_de = 0;
+    std::vector<long> c2e_up_off, c2e_dn_off;  // offsets into c2e pool (FP64, n x n)
+    DBuf<double> c2e;
+    DBuf<double> ops64;                         // plain: Mop, Lop, T_k
+    DBuf<float> ops32;                          // mixed: combined M2M', L2L', U_k
+    std::vector<GemmSet> c2e_up, m2m, l2l, c2e_dn;  // per level
+    GemmSet m2l;
+    // transposed sets (in/out swapped) for the adjoint apply
+    std::vector<GemmSet> c2e_up_t, m2m_t, l2l_t, c2e_dn_t;
+    GemmSet m2l_t;
+    bool m2l_on_the_fly = false;
+    // mixed: per-leaf L2P operators
+    DBuf<float> E;
+    DBuf<long> E_row0;  // per l2p task
+    DBuf<int> E_leaf, E_npts;
+    DBuf<long> E_pt0;
+    int n_l2p = 0;
+};
+
+struct Plan {
+    int kid = 0, R = 1;
+    double mu = 1.0, nu = 0.25;
+    KParams kp{};
+    TbemFmmConfig cfg{};
+    TbemGpuOptions opt{};
+    long n_obs = 0, n_src = 0;
+    int ns = 0, n = 0;
+    bool same_tree = false;
+    Tree otree, stree_own;
+    const Tree* stree = nullptr;
+    TaskLists L;
+    std::vector<double> unit;
+    DBuf<double> d_unit;
+    DTree dobs, dsrc_own;
+    DTree* dsrc = nullptr;
+    Form f;
+    // evaluation task sets (forward); adjoint sets swap roles
+    TaskSet p2m, p2p, m2p, p2l, l2p, m2l_fly;
+    TaskSet p2m_t, p2p_t, m2p_t, p2l_t, l2p_t, m2l_fly_t;
+    // work buffers
+    int cap_rhs = 0;
+    DBuf<double> io_x, io_y;            // device staging of caller data (original order)
+    DBuf<double> s64, y64;              // strengths / outputs in tree order
+    DBuf<float> s32;
+    DBuf<double> cu64, qu64, cd64, qd64;  // cell buffers [cell][rhs][n]
+    DBuf<float> cu32, cd32;
+    cudaStream_t stream = nullptr;
+    cublasHandle_t cublas = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+    bool timing = false;
+    std::vector<std::pair<std::string, double>> phase_ms;
+    std::vector<cudaEvent_t> events;
+    // kept for clone()
+    std::vector<double> h_obs_locs, h_obs_normals, h_src_locs, h_src_normals, h_src_weights;
+
+    ~Plan();
+    void build(int kernel, const double* params, const double* obs_locs, const double* obs_normals,
+               long n_obs, const double* src_locs, const double* src_normals,
+               const double* src_weights, long n_src, const TbemFmmConfig& cfg,
+               const TbemGpuOptions& opt);
+    void apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adjoint);
+    void set_c2e(int which, long level, const double* op);
+    void get_c2e(int which, long level, double* out) const;
+
+    void upload_tree(const Tree& t, const double* locs, const double* normals,
+                     const double* weights, DTree& d);
+    void build_tasks();
+    void build_form();
+    void build_c2e(Form& F);
+    void build_plain_ops(Form& F);
+    void build_mixed_ops(Form& F);
+    void build_gemm_sets(Form& F, long op_base_m2m, long op_base_l2l, long op_base_m2l,
+                         const std::vector<long>& m2m_off, const std::vector<long>& l2l_off,
+                         const std::vector<long>& m2l_off);
+    void ensure_rhs(int nrhs);
+    void forward(int nrhs, cudaStream_t s);
+    void adjoint(int nrhs, cudaStream_t s);
+    template <typename T>
+    void eval(const TaskSet& ts, int kid_trans, bool tgt_surf, bool src_surf, const Tree& tt,
+              const DTree& dt, double t_rref, const DTree& ds, double s_rref, const T* s_str,
+              long s_n, const T* q, double* y, long y_n, T* c, int add, int nrhs, cudaStream_t s,
+              bool trans);
+    void mark(const char* name, cudaStream_t s);
+    // operator pool layout of the current form
+    std::vector<int> m2m_key_level, l2l_key_level;
+    std::vector<std::vector<int>> m2l_groups;  // pair indices per M2L key
+    std::vector<int> m2l_key_ls;               // source level per key
+    std::vector<std::pair<int, int>> m2l_canon;
+    std::vector<std::vector<std::pair<int, int>>> m2m_pairs, l2l_pairs;  // per (level*8+oct)
+    std::vector<std::pair<int, int>> m2m_canon, l2l_canon;
+};
+
+}  // namespace tbem

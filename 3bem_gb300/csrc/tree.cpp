@@ -1,0 +1,314 @@
+// Host octree + task lists.  Compiled with -ffp-contract=off so that the box
+// arithmetic rounds exactly like the reference on every host architecture.
+#include "tree.h"
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+
+namespace tbem {
+namespace {
+
+struct Box {
+    double c[3], h[3];
+};
+
+// Box::bounding_box over zero-radius balls (cpp/geometry.cpp:61-80).
+Box bounding_box(const double* pts, const std::vector<long>& idx)
+{
+    Box b{{0, 0, 0}, {0, 0, 0}};
+    if (idx.empty()) return b;
+    double mn[3], mx[3];
+    for (int d = 0; d < 3; d++) mn[d] = mx[d] = pts[3 * idx[0] + d];
+    for (size_t i = 1; i < idx.size(); i++)
+        for (int d = 0; d < 3; d++) {
+            double v = pts[3 * idx[i] + d];
+            mn[d] = std::min(mn[d], v - 0.0);
+            mx[d] = std::max(mx[d], v + 0.0);
+        }
+    for (int d = 0; d < 3; d++) {
+        b.c[d] = (mx[d] + mn[d]) / 2.0;
+        b.h[d] = (mx[d] - mn[d]) / 2.0;
+    }
+    return b;
+}
+
+// expand_by_max_axis_multiple (cpp/geometry.cpp:13-17)
+Box expand(const Box& b, double f)
+{
+    double m = std::max(b.h[0], std::max(b.h[1], b.h[2]));
+    double e = f * m;
+    return Box{{b.c[0], b.c[1], b.c[2]}, {b.h[0] + e, b.h[1] + e, b.h[2] + e}};
+}
+
+// get_subcell with make_child_idx's bit order (x is bit 2), cpp/geometry.cpp:20-28
+Box subcell(const Box& b, int oct)
+{
+    int idx[3] = {(oct >> 2) & 1, (oct >> 1) & 1, oct & 1};
+    Box o;
+    for (int d = 0; d < 3; d++) {
+        o.h[d] = b.h[d] / 2.0;
+        o.c[d] = b.c[d] + ((static_cast<double>(idx[d]) * 2) - 1) * o.h[d];
+    }
+    return o;
+}
+
+// find_containing_subcell: strict '>' (cpp/geometry.cpp:83-95)
+int containing(const Box& b, const double* p)
+{
+    int c = 0;
+    for (int d = 0; d < 3; d++) {
+        if (p[d] > b.c[d]) c++;
+        if (d < 2) c <<= 1;
+    }
+    return c;
+}
+
+struct Node {
+    Box b;
+    std::vector<long> idx;
+    int level;
+    long ref_index;
+    int child[8];
+    int octant;
+};
+
+struct Builder {
+    const double* pts;
+    long min_pts;
+    std::vector<Node> nodes;
+    long next_index = 1;
+
+    // build_children (cpp/octree.cpp:97-153) run sequentially: a child's
+    // index is taken after its subtree is built (post-order).
+    void build_children(int node, const Box& bounds, int level)
+    {
+        const std::vector<long> idx = nodes[node].idx;  // copy: nodes may reallocate
+        if ((long)idx.size() <= min_pts) return;
+        std::vector<long> part[8];
+        for (long i : idx) part[containing(bounds, &pts[3 * i])].push_back(i);
+        for (int o = 0; o < 8; o++) {
+            if (part[o].empty()) continue;
+            Box cb = subcell(bounds, o);
+            Box tight = bounding_box(pts, part[o]);
+            Node n;
+            n.b = cb;
+            n.idx = std::move(part[o]);
+            n.level = level + 1;
+            n.ref_index = -1;
+            n.octant = o;
+            for (int k = 0; k < 8; k++) n.child[k] = -1;
+            nodes.push_back(std::move(n));
+            int id = (int)nodes.size() - 1;
+            nodes[node].child[o] = id;
+            if (tight.h[0] != 0.0 || tight.h[1] != 0.0 || tight.h[2] != 0.0)
+                build_children(id, cb, level + 1);
+            nodes[id].ref_index = next_index++;
+        }
+    }
+};
+
+}  // namespace
+
+Tree build_tree(const double* pts, long n, long min_pts)
+{
+    Builder B;
+    B.pts = pts;
+    B.min_pts = min_pts;
+    std::vector<long> all(n);
+    for (long i = 0; i < n; i++) all[i] = i;
+    Box box = bounding_box(pts, all);
+    Node root;
+    root.b = expand(box, 1e-5);  // the root's bounds are the expanded box ...
+    root.idx = all;
+    root.level = 0;
+    root.ref_index = 0;
+    root.octant = -1;
+    for (int k = 0; k < 8; k++) root.child[k] = -1;
+    B.nodes.reserve(2 * (size_t)(n / std::max<long>(min_pts, 1)) + 16);
+    B.nodes.push_back(std::move(root));
+    B.build_children(0, box, 0);  // ... but its children are cut from the unexpanded one
+
+    const auto& N = B.nodes;
+    Tree T;
+    // level-major flattening: FIFO over the nodes, children pushed in octant order
+    std::vector<int> order;
+    std::vector<int> flat_of(N.size(), -1);
+    order.push_back(0);
+    for (size_t q = 0; q < order.size(); q++) {
+        const Node& nd = N[order[q]];
+        for (int o = 0; o < 8; o++)
+            if (nd.child[o] >= 0) order.push_back(nd.child[o]);
+    }
+    for (size_t i = 0; i < order.size(); i++) flat_of[order[i]] = (int)i;
+    T.cells.resize(order.size());
+    int max_level = 0;
+    for (size_t i = 0; i < order.size(); i++) {
+        const Node& nd = N[order[i]];
+        Cell& c = T.cells[i];
+        for (int d = 0; d < 3; d++) {
+            c.center[d] = nd.b.c[d];
+            c.hw[d] = nd.b.h[d];
+        }
+        c.level = nd.level;
+        c.octant = nd.octant;
+        c.ref_index = nd.ref_index;
+        c.parent = -1;
+        c.first_child = -1;
+        c.n_children = 0;
+        for (int o = 0; o < 8; o++) {
+            if (nd.child[o] < 0) continue;
+            int f = flat_of[nd.child[o]];
+            if (c.first_child < 0) c.first_child = f;
+            c.n_children++;
+        }
+        max_level = std::max(max_level, nd.level);
+    }
+    for (size_t i = 0; i < T.cells.size(); i++) {
+        const Cell& c = T.cells[i];
+        for (int k = 0; k < c.n_children; k++) T.cells[c.first_child + k].parent = (int)i;
+    }
+    T.level_start.assign(max_level + 2, 0);
+    for (const Cell& c : T.cells) T.level_start[c.level + 1]++;
+    for (int l = 0; l <= max_level; l++) T.level_start[l + 1] += T.level_start[l];
+
+    // pre-order and permuted point ranges (leaves in pre-order; inside a
+    // leaf the reference's ascending index order)
+    T.perm.reserve(n);
+    T.first_at_level.assign(max_level + 1, -1);
+    std::vector<std::pair<int, int>> stack;  // (node, state)
+    stack.push_back({0, 0});
+    while (!stack.empty()) {
+        auto [node, state] = stack.back();
+        stack.pop_back();
+        int f = flat_of[node];
+        Cell& c = T.cells[f];
+        if (state == 0) {
+            T.preorder.push_back(f);
+            if (T.first_at_level[c.level] < 0) T.first_at_level[c.level] = f;
+            c.pt_begin = (long)T.perm.size();
+            if (c.n_children == 0) {
+                for (long i : N[node].idx) T.perm.push_back(i);
+                c.pt_end = (long)T.perm.size();
+            } else {
+                stack.push_back({node, 1});
+                for (int o = 7; o >= 0; o--)
+                    if (N[node].child[o] >= 0) stack.push_back({N[node].child[o], 0});
+            }
+        } else {
+            c.pt_end = (long)T.perm.size();
+        }
+    }
+    return T;
+}
+
+namespace {
+
+inline double hyp(const double* v)
+{
+    return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+}
+
+struct ListBuilder {
+    const Tree& obs;
+    const Tree& src;
+    double mac;
+    long n_surf;
+    bool small_cells;
+    TaskLists L;
+
+    // upward_traversal (cpp/fmm.cpp:561-575): leaves -> p2m, then the cell -> m2m
+    void upward(int c)
+    {
+        const Cell& cell = src.cells[c];
+        if (cell.is_leaf()) {
+            L.p2m.push_back(c);
+            return;
+        }
+        for (int k = 0; k < cell.n_children; k++) upward(cell.first_child + k);
+        L.m2m.push_back(c);
+    }
+
+    // dual_tree (cpp/fmm.cpp:578-630)
+    void dual(int o, int s)
+    {
+        const Cell& oc = obs.cells[o];
+        const Cell& sc = src.cells[s];
+        double r_src = hyp(sc.hw), r_obs = hyp(oc.hw);
+        double r_max = std::max(r_src, r_obs), r_min = std::min(r_src, r_obs);
+        double dc[3] = {oc.center[0] - sc.center[0], oc.center[1] - sc.center[1],
+                        oc.center[2] - sc.center[2]};
+        double sep = hyp(dc);
+        if (r_max + mac * r_min <= mac * sep) {
+            bool small_src = sc.n_points() <= n_surf;
+            bool small_obs = oc.n_points() <= n_surf;
+            if (small_cells) {
+                if (small_obs && small_src) L.p2p.push_back({o, s});
+                else if (small_obs) L.m2p.push_back({o, s});
+                else if (small_src) L.p2l.push_back({o, s});
+                else L.m2l.push_back({o, s});
+            } else {
+                L.m2l.push_back({o, s});
+            }
+            return;
+        }
+        if (oc.is_leaf() && sc.is_leaf()) {
+            L.p2p.push_back({o, s});
+            return;
+        }
+        bool src_is_shallower = oc.level > sc.level;
+        bool split_src = (src_is_shallower && !sc.is_leaf()) || oc.is_leaf();
+        if (split_src) {
+            for (int k = 0; k < sc.n_children; k++) dual(o, sc.first_child + k);
+        } else {
+            for (int k = 0; k < oc.n_children; k++) dual(oc.first_child + k, s);
+        }
+    }
+
+    // downward_traversal (cpp/fmm.cpp:633-648): the cell -> l2l, then children
+    void downward(int c)
+    {
+        const Cell& cell = obs.cells[c];
+        if (cell.is_leaf()) {
+            L.l2p.push_back(c);
+            return;
+        }
+        L.l2l.push_back(c);
+        for (int k = 0; k < cell.n_children; k++) downward(cell.first_child + k);
+    }
+};
+
+}  // namespace
+
+TaskLists build_lists(const Tree& obs, const Tree& src, double mac, long n_surf,
+                      bool small_cells)
+{
+    ListBuilder B{obs, src, mac, n_surf, small_cells, {}};
+    if (src.n_points() > 0) B.upward(0);
+    if (obs.n_points() > 0 && src.n_points() > 0) B.dual(0, 0);
+    if (obs.n_points() > 0) B.downward(0);
+    return std::move(B.L);
+}
+
+std::vector<double> sphere_surface(long order)
+{
+    std::vector<double> pts;
+    double a = 4 * M_PI / order;
+    double d = std::sqrt(a);
+    auto M_theta = static_cast<size_t>(std::round(M_PI / d));
+    double d_theta = M_PI / M_theta;
+    double d_phi = a / d_theta;
+    for (size_t m = 0; m < M_theta; m++) {
+        double theta = M_PI * (m + 0.5) / M_theta;
+        auto M_phi = static_cast<size_t>(std::round(2 * M_PI * std::sin(theta) / d_phi));
+        for (size_t k = 0; k < M_phi; k++) {
+            double phi = 2 * M_PI * k / M_phi;
+            pts.push_back(std::sin(theta) * std::cos(phi));
+            pts.push_back(std::sin(theta) * std::sin(phi));
+            pts.push_back(std::cos(theta));
+        }
+    }
+    return pts;
+}
+
+}  // namespace tbem

@@ -1,0 +1,7 @@
+"""tbempy: GPU (sm_103a) BEM operator apply with the reference's Python names.
+
+Submodules: ``ThreeD`` (operators over lib/libtbem_gpu.so), ``meshes``
+(seeded synthetic meshes), ``autograd`` (torch.autograd wrapper), ``solve``
+(GMRES with FP64 iterative refinement).
+"""
+from . import ThreeD, meshes  # noqa: F401

@@ -1,0 +1,88 @@
+"""ctypes binding of lib/libtbem_gpu.so (the C ABI in include/tbem_gpu.h).
+
+The library is the only compute path: importing an operator without it
+raises, there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libtbem_gpu.so")
+
+TBEM_OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA failure", -3: "allocation failure",
+          -4: "invalid state", -5: "device wait timed out"}
+
+PRECISION = {"fp64": 0, "mixed": 1}
+
+
+class TbemFmmConfig(C.Structure):
+    _fields_ = [("mac", C.c_double), ("order", C.c_long), ("min_pts_per_cell", C.c_long),
+                ("d", C.c_double), ("account_for_small_cells", C.c_int)]
+
+
+class TbemGpuOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("device", C.c_int), ("svd_threshold", C.c_double),
+                ("m2l_path", C.c_int), ("p2p_block", C.c_int), ("host_only", C.c_int),
+                ("reserved", C.c_int * 3)]
+
+
+class TbemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "error"), code, msg))
+        self.code = code
+
+
+_P, _L, _I, _D = C.c_void_p, C.c_long, C.c_int, C.c_double
+
+# name -> (restype, argtypes); every symbol include/tbem_gpu.h declares
+SIGNATURES = {
+    "tbem_default_options": (None, [_P]),
+    "tbem_fmm_create": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _P]),
+    "tbem_fmm_apply": (_I, [_P, _P, _P, _I, _P]),
+    "tbem_fmm_apply_adjoint": (_I, [_P, _P, _P, _I, _P]),
+    "tbem_fmm_n_rows": (_L, [_P]),
+    "tbem_fmm_n_cols": (_L, [_P]),
+    "tbem_fmm_clone": (_I, [_P, _P]),
+    "tbem_fmm_destroy": (None, [_P]),
+    "tbem_fmm_tree_cells": (_L, [_P, _I, _P, _P, _P, _P, _P, _P]),
+    "tbem_fmm_tree_indices": (_L, [_P, _I, _P]),
+    "tbem_fmm_list": (_L, [_P, _I, _P, _P]),
+    "tbem_fmm_n_surface": (_L, [_P]),
+    "tbem_fmm_n_c2e_levels": (_L, [_P, _I]),
+    "tbem_fmm_get_c2e": (_I, [_P, _I, _L, _P]),
+    "tbem_fmm_set_c2e": (_I, [_P, _I, _L, _P]),
+    "tbem_fmm_set_timing": (_I, [_P, _I]),
+    "tbem_fmm_phase_times": (_I, [_P, _P, _P, _I]),
+    "tbem_direct_apply": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _I, _P]),
+    "tbem_csr_create": (_I, [_L, _L, _P, _P, _P, _P]),
+    "tbem_csr_apply": (_I, [_P, _P, _P, _I, _P]),
+    "tbem_csr_nnz": (_L, [_P]),
+    "tbem_csr_destroy": (None, [_P]),
+    "tbem_last_error": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the library (raises if it was not built: no fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libtbem_gpu.so not built (run __graft_entry__.build() or "
+                              "python 3bem_gb300/build.py): " + LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc < 0:
+        msg = lib().tbem_last_error()
+        raise TbemError(rc, msg.decode() if msg else "")
+    return rc

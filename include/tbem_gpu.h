@@ -1,0 +1,163 @@
+/* tbem_gpu.h -- C ABI of the GB300 BEM operator apply (KIFMM + direct + CSR).
+ *
+ * Drop-in for the reference's operator interface on the hot path
+ * (tbenthompson/3bem):
+ *   struct OperatorI { n_rows(); n_cols(); apply(x); clone(); }   cpp/operator.h:14-19
+ *   FMMOperator<3,R,C>(Kernel, NBodyData, FMMConfig)              cpp/fmm.h:131-147
+ *   FMMConfig(mac, order, min_pts_per_cell, d, account_for_small_cells)  cpp/fmm.h:73-96
+ *   SparseOperator::apply (CSR SpMV)                              cpp/sparse_operator.cpp:19-28
+ *   make_direct_nbody_operator / nbody_eval (direct sum)          cpp/nbody_operator.h:117-152
+ *
+ * Conventions (those of the reference):
+ *   - points are row-major float64 [n][3]; weights float64 [n];
+ *   - densities are component-major per right-hand side: x[r][d][j] =
+ *     x[(r*C + d)*n_src + j] (cpp/fmm.cpp:189-190); outputs likewise
+ *     y[(r*R + d)*n_obs + i];
+ *   - n_rows = R*n_obs, n_cols = C*n_src (cpp/fmm.h:235-236).
+ * Pointers passed to the apply calls may be host or device memory (detected);
+ * host buffers are copied in and out inside the call.  Every function returns
+ * TBEM_OK or a negative status; tbem_last_error() gives the message.  Nothing
+ * aborts.  Empty point sets are valid (the reference requires empty meshes
+ * not to error, acceptance_tests/test_empty_operator.py:10-17).
+ */
+#ifndef TBEM_GPU_H
+#define TBEM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define TBEM_OK 0
+#define TBEM_ERR_ARG (-1)      /* invalid argument / config            */
+#define TBEM_ERR_CUDA (-2)     /* CUDA runtime or library failure      */
+#define TBEM_ERR_ALLOC (-3)    /* device or host allocation failed     */
+#define TBEM_ERR_STATE (-4)    /* call not valid for this handle state */
+#define TBEM_ERR_TIMEOUT (-5)  /* a bounded device wait gave up        */
+
+/* kernel ids: cpp/laplace_kernels.h:19-48, cpp/elastic_kernels.h:192-311,
+ * cpp/identity_kernels.h:9-40 (IdentityScalar, a test kernel). */
+#define TBEM_LAPLACE_SINGLE 0
+#define TBEM_LAPLACE_DOUBLE 1
+#define TBEM_ELASTIC_DISPLACEMENT 2
+#define TBEM_ELASTIC_TRACTION 3
+#define TBEM_ELASTIC_ADJOINT_TRACTION 4
+#define TBEM_IDENTITY_SCALAR 5
+
+/* precision forms */
+#define TBEM_PRECISION_FP64 0   /* plain: reference surfaces and formulation, FP64 */
+#define TBEM_PRECISION_MIXED 1  /* precision form: tensor-core M2L/M2M/L2L, FP32 P2P */
+
+/* FMMConfig, cpp/fmm.h:73-96 (same five fields and meaning; `order` is the
+ * requested number of translation-surface points, cpp/fmm.h:76-82). */
+typedef struct {
+    double mac;
+    long order;
+    long min_pts_per_cell;
+    double d;
+    int account_for_small_cells;
+} TbemFmmConfig;
+
+/* GPU-side options that have no reference counterpart. */
+typedef struct {
+    int precision;         /* TBEM_PRECISION_*                                   */
+    int device;            /* CUDA device ordinal                                */
+    double svd_threshold;  /* singular-value cutoff (reference: 1e-10, fmm.cpp:122) */
+    int m2l_path;          /* 0 auto, 1 SIMT FP32 GEMM, 2 tcgen05 3xBF16 (mixed only) */
+    int p2p_block;         /* 0 auto; else threads per target in the P2P kernel (1,2,4,8) */
+    int host_only;         /* 1: build trees and task lists only (no device use);
+                              apply calls then fail with TBEM_ERR_STATE            */
+    int reserved[3];
+} TbemGpuOptions;
+
+typedef struct TbemFmm TbemFmm;
+
+/* Fill *opt with defaults (FP64, device 0, threshold 1e-10, auto paths). */
+void tbem_default_options(TbemGpuOptions* opt);
+
+/* Replaces FMMOperator<3,R,C>::FMMOperator(K, NBodyData, FMMConfig)
+ * (cpp/fmm.cpp:72-101): builds both octrees, the task lists, the translation
+ * surfaces and the per-level check-to-equivalent operators, and uploads
+ * everything to the device.  kernel_params = {shear_modulus, poisson_ratio}
+ * for the elastic kernels (may be NULL for the scalar ones). */
+int tbem_fmm_create(int kernel, const double* kernel_params,
+                    const double* obs_locs, const double* obs_normals, long n_obs,
+                    const double* src_locs, const double* src_normals,
+                    const double* src_weights, long n_src,
+                    const TbemFmmConfig* config, const TbemGpuOptions* options,
+                    TbemFmm** out);
+
+/* Replaces FMMOperator::apply (cpp/fmm.cpp:551-557) for n_rhs right-hand
+ * sides at once; stream is a cudaStream_t (NULL = the handle's stream). */
+int tbem_fmm_apply(TbemFmm* h, const double* x, double* y, int n_rhs, void* stream);
+
+/* Transpose apply: w = A^T z with A the operator tbem_fmm_apply applies
+ * (the FMM passes run transposed and in reverse order).  No reference
+ * counterpart; the reference's transpose partner kernel is
+ * ElasticAdjointTraction (cpp/elastic_kernels.h:272-311). */
+int tbem_fmm_apply_adjoint(TbemFmm* h, const double* z, double* w, int n_rhs, void* stream);
+
+/* OperatorI::n_rows / n_cols (cpp/operator.h:15-16, cpp/fmm.h:235-236). */
+long tbem_fmm_n_rows(const TbemFmm* h);
+long tbem_fmm_n_cols(const TbemFmm* h);
+
+/* OperatorI::clone (cpp/fmm.cpp:103-109): an independent operator. */
+int tbem_fmm_clone(const TbemFmm* h, TbemFmm** out);
+
+void tbem_fmm_destroy(TbemFmm* h);
+
+/* Introspection for bit-exact checks against the reference octree
+ * (cpp/octree.h:14-25) and task lists (FMMTasks, cpp/fmm.h:98-120).
+ * which: 0 = source tree, 1 = observation tree.  Cells are reported in
+ * pre-order with the reference's post-order `index`; any output pointer may
+ * be NULL; returns the number of cells (or a negative status). */
+long tbem_fmm_tree_cells(const TbemFmm* h, int which, long* level, long* index,
+                         double* center, double* half_width, long* n_points,
+                         long* n_children);
+/* Point indices of every cell, concatenated in the same pre-order. */
+long tbem_fmm_tree_indices(const TbemFmm* h, int which, long* out);
+/* kind: 0 p2m, 1 m2m, 2 p2p, 3 m2p, 4 p2l, 5 m2l, 6 l2l, 7 l2p; pairs as
+ * (obs cell index, src cell index), cell tasks with src = -1. */
+long tbem_fmm_list(const TbemFmm* h, int kind, long* obs_index, long* src_index);
+/* Number of translation-surface points actually used (cpp/fmm.cpp:22-45). */
+long tbem_fmm_n_surface(const TbemFmm* h);
+/* Number of check-to-equivalent levels (which: 0 up, 1 down). */
+long tbem_fmm_n_c2e_levels(const TbemFmm* h, int which);
+/* Read / replace the check-to-equivalent operator of one level (row-major,
+ * (C n_s) x (R n_s), cpp/fmm.cpp:130-160).  Replacing is for the plain form
+ * only: it lets a caller install operators from its own LAPACK. */
+int tbem_fmm_get_c2e(const TbemFmm* h, int which, long level, double* out);
+int tbem_fmm_set_c2e(TbemFmm* h, int which, long level, const double* op);
+
+/* Per-phase device times (ms) of the last apply, measured with CUDA events
+ * when timing is enabled (tbem_fmm_set_timing).  names/ms are NULL-able;
+ * returns the number of phases. */
+int tbem_fmm_set_timing(TbemFmm* h, int enabled);
+int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int cap);
+
+/* Direct N-body sum on the GPU in FP64 (nbody_eval over all pairs,
+ * cpp/nbody_operator.h:117-141; the dense oracle make_direct_nbody_operator,
+ * :143-152, matrix-free).  Same layouts as tbem_fmm_apply. */
+int tbem_direct_apply(int kernel, const double* kernel_params,
+                      const double* obs_locs, const double* obs_normals, long n_obs,
+                      const double* src_locs, const double* src_normals,
+                      const double* src_weights, long n_src,
+                      const double* x, double* y, int n_rhs, void* stream);
+
+/* CSR operator (SparseOperator, cpp/sparse_operator.h:44-83):
+ * y = A x for n_rhs right-hand sides (x[r*n_cols + j], y[r*n_rows + i]).
+ * Column indices are int64 like the reference's size_t.  FP64. */
+typedef struct TbemCsr TbemCsr;
+int tbem_csr_create(long n_rows, long n_cols, const double* values,
+                    const long* column_indices, const long* row_ptrs, TbemCsr** out);
+int tbem_csr_apply(TbemCsr* h, const double* x, double* y, int n_rhs, void* stream);
+long tbem_csr_nnz(const TbemCsr* h);
+void tbem_csr_destroy(TbemCsr* h);
+
+/* Last error message of the calling thread ("" if none). */
+const char* tbem_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TBEM_GPU_H */
