@@ -208,6 +208,8 @@ int tbem_fmm_set_c2e(TbemFmm* h, int which, long level, const double* op)
     return guarded([&] { h->plan.set_c2e(which, level, op); });
 }
 
+long tbem_fmm_last_launches(const TbemFmm* h) { return h ? h->plan.launches : TBEM_ERR_ARG; }
+
 int tbem_fmm_set_timing(TbemFmm* h, int enabled)
 {
     if (!h) return fail(TBEM_ERR_ARG, "null handle");

@@ -109,9 +109,11 @@ void GemmSet::upload(const void* pool, size_t esz)
 }
 
 template <typename T>
-void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s)
+void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s,
+                  long* launches)
 {
     if (empty()) return;
+    if (launches) (*launches)++;
     auto it = tiles.find(nrhs);
     if (it == tiles.end()) {
         std::vector<int> tg, tc;
@@ -146,8 +148,8 @@ void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaSt
     TBEM_CK(cudaGetLastError());
 }
 
-template void GemmSet::run<double>(const double*, double*, int, int, int, int, cudaStream_t);
-template void GemmSet::run<float>(const float*, float*, int, int, int, int, cudaStream_t);
+template void GemmSet::run<double>(const double*, double*, int, int, int, int, cudaStream_t, long*);
+template void GemmSet::run<float>(const float*, float*, int, int, int, int, cudaStream_t, long*);
 
 // ------------------------------------------------------------ device kernels
 
@@ -617,7 +619,8 @@ void Plan::build_c2e(Form& F)
     dj.alloc(jobs.size());
     TBEM_CK(cudaMemcpy(dj.p, jobs.data(), jobs.size() * sizeof(SurfJob), cudaMemcpyHostToDevice));
     dim3 g((unsigned)((ns * ns + 255) / 256), (unsigned)jobs.size());
-    surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p, d_unit.p, ns, kid, kp, sys.p);
+    surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p, d_unit.p, ns, F.g_kid,
+                                               make_kparams(F.g_kid, mu, nu), sys.p);
     TBEM_CK(cudaGetLastError());
     int lwork = 0;
     TBEM_CKS(cusolverDnDgesvd_bufferSize(solver, n, n, &lwork));
@@ -654,19 +657,30 @@ void Plan::build_form()
     Form& F = f;
     F.mixed = opt.precision == TBEM_PRECISION_MIXED;
     if (!F.mixed) {
-        // reference radii (cpp/fmm.h:42-66)
+        // reference radii (cpp/fmm.h:42-66) and the operator's own kernel everywhere
         const double far = 4.0 - std::sqrt(2) - 2 * cfg.d;
         F.r_ue = 0.3;
         F.r_uc = far;
         F.r_dc = 0.3;
         F.r_de = far;
+        F.g_kid = F.ks_kid = F.kt_kid = kid;
     } else {
-        // enclosing surfaces: the down-check sphere contains the cell, so
-        // the local field is interpolated, never extrapolated
-        F.r_ue = 1.05;
-        F.r_uc = 2.5;
-        F.r_dc = 1.05;
-        F.r_de = 2.5;
+        // enclosing surfaces: the down-check sphere contains the cell, so the
+        // local field is interpolated, never extrapolated, and the combined
+        // operators stay O(1).  Equivalent sources are single-layer (Laplace
+        // single layer / Kelvin displacement): the far field of every kernel
+        // here is a harmonic potential or a Navier displacement field, which
+        // single-layer densities represent; the traction kernels as their own
+        // equivalent kernel converge poorly on enclosing spheres.
+        F.r_ue = 1.1;
+        F.r_uc = 2.9;
+        F.r_dc = 1.1;
+        F.r_de = 2.9;
+        const bool elastic = kid == EL_DISP || kid == EL_TRAC || kid == EL_ADJ;
+        F.g_kid = kid == IDENT ? IDENT : (elastic ? EL_DISP : LAP_S);
+        // adjoint traction: point-force sources, traction observed at the targets
+        F.ks_kid = kid == EL_ADJ ? EL_DISP : kid;
+        F.kt_kid = kid == EL_ADJ ? EL_ADJ : F.g_kid;
     }
     build_c2e(F);
     if (F.mixed) build_mixed_ops(F);
@@ -803,7 +817,8 @@ void Plan::build_plain_ops(Form& F)
         for (size_t j0 = 0; j0 < jobs.size(); j0 += 32768) {
             unsigned nj = (unsigned)std::min<size_t>(32768, jobs.size() - j0);
             dim3 g((unsigned)((ns * ns + 255) / 256), nj);
-            surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p + j0, d_unit.p, ns, kid, kp, F.ops64.p);
+            surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p + j0, d_unit.p, ns, F.g_kid,
+                                                       make_kparams(F.g_kid, mu, nu), F.ops64.p);
             TBEM_CK(cudaGetLastError());
         }
         TBEM_CK(cudaStreamSynchronize(stream));
@@ -846,7 +861,8 @@ void Plan::build_mixed_ops(Form& F)
             dj.alloc(nj);
             TBEM_CK(cudaMemcpy(dj.p, sub.data(), nj * sizeof(SurfJob), cudaMemcpyHostToDevice));
             dim3 g((unsigned)((ns * ns + 255) / 256), (unsigned)nj);
-            surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p, d_unit.p, ns, kid, kp, K.p);
+            surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p, d_unit.p, ns, F.g_kid,
+                                                       make_kparams(F.g_kid, mu, nu), K.p);
             TBEM_CK(cudaGetLastError());
             for (size_t k = 0; k < nj; k++) {
                 // row-major Y = K * C  <=>  column-major Y^T = C^T K^T
@@ -905,8 +921,8 @@ void Plan::build_mixed_ops(Form& F)
             dim3 g((unsigned)(((long)maxp * ns + 255) / 256), (unsigned)(t1 - t0));
             pts_surf_matrix_kernel<<<g, 256, 0, stream>>>(
                 F.E_pt0.p + t0, F.E_npts.p + t0, F.E_leaf.p + t0, F.E_row0.p + t0, dobs.xyz.p,
-                dobs.nrm64.p, dobs.center.p, dobs.rad.p, F.r_de, d_unit.p, ns, kid, kp, K.p,
-                row0[t0]);
+                dobs.nrm64.p, dobs.center.p, dobs.rad.p, F.r_de, d_unit.p, ns, F.kt_kid,
+                make_kparams(F.kt_kid, mu, nu), K.p, row0[t0]);
             TBEM_CK(cudaGetLastError());
             TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)r, n, &one,
                                  F.c2e.p + F.c2e_dn_off[lev], n, K.p, n, &zero, Y.p, n));
@@ -977,7 +993,7 @@ void Plan::mark(const char* name, cudaStream_t s)
 }
 
 template <typename T>
-void Plan::eval(const TaskSet& ts, int, bool tgt_surf, bool src_surf, const Tree&,
+void Plan::eval(const TaskSet& ts, int ekid, bool tgt_surf, bool src_surf, const Tree&,
                 const DTree& dt, double t_rref, const DTree& ds, double s_rref, const T* s_str,
                 long s_n, const T* q, double* y, long y_n, T* c, int add, int nrhs,
                 cudaStream_t s, bool trans)
@@ -1005,12 +1021,14 @@ void Plan::eval(const TaskSet& ts, int, bool tgt_surf, bool src_surf, const Tree
     a.c = c;
     a.nrhs = nrhs;
     a.add = add;
-    a.c2 = T(kp.c2);
-    a.scale = kp.scale;
-    EvalLaunch Lc{kid, trans, tgt_surf, src_surf, ts.n_items()};
+    const KParams ep = make_kparams(ekid, mu, nu);
+    a.c2 = T(ep.c2);
+    a.scale = ep.scale;
+    EvalLaunch Lc{ekid, trans, tgt_surf, src_surf, ts.n_items()};
     for (int r0 = 0; r0 < nrhs; r0 += (nrhs - r0 > 1 ? EVAL_NR : 1)) {
         a.rhs0 = r0;
         TBEM_CK(launch_eval<T>(Lc, a, s));
+        launches++;
     }
 }
 
@@ -1026,76 +1044,82 @@ void Plan::forward(int nrhs, cudaStream_t s)
     if (!F.mixed) {
         gather_kernel<double><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s64.p, NS, R, nrhs);
         TBEM_CK(cudaGetLastError());
+        launches++;
         TBEM_CK(cudaMemsetAsync(cu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
         TBEM_CK(cudaMemsetAsync(cd64.p, 0, sizeof(double) * nco * nrhs * n, s));
         mark("gather", s);
-        eval<double>(p2m, 0, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cu64.p, 0, nrhs, s, false);
+        eval<double>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cu64.p, 0, nrhs, s, false);
         mark("p2m", s);
         for (int l = S.n_levels() - 1; l >= 0; l--) {
-            if (l < (int)F.m2m.size()) F.m2m[l].run<double>(qu64.p, cu64.p, n, nrhs, 0, GEMM_ATOMIC, s);
-            F.c2e_up[l].run<double>(cu64.p, qu64.p, n, nrhs, 0, GEMM_STORE, s);
+            if (l < (int)F.m2m.size()) F.m2m[l].run<double>(qu64.p, cu64.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
+            F.c2e_up[l].run<double>(cu64.p, qu64.p, n, nrhs, 0, GEMM_STORE, s, &launches);
         }
         mark("m2m+c2e_up", s);
-        eval<double>(p2p, 0, false, false, O, dobs, 0, *dsrc, 0, s64.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
+        eval<double>(p2p, kid, false, false, O, dobs, 0, *dsrc, 0, s64.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
         mark("p2p", s);
-        eval<double>(m2p, 0, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
-        eval<double>(p2l, 0, true, false, O, dobs, F.r_dc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cd64.p, 1, nrhs, s, false);
+        eval<double>(m2p, F.kt_kid, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+        eval<double>(p2l, F.ks_kid, true, false, O, dobs, F.r_dc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cd64.p, 1, nrhs, s, false);
         mark("m2p+p2l", s);
         if (F.m2l_on_the_fly)
-            eval<double>(m2l_fly, 0, true, true, O, dobs, F.r_dc, *dsrc, F.r_ue, nullptr, 0, qu64.p, nullptr, 0, cd64.p, 1, nrhs, s, false);
+            eval<double>(m2l_fly, F.g_kid, true, true, O, dobs, F.r_dc, *dsrc, F.r_ue, nullptr, 0, qu64.p, nullptr, 0, cd64.p, 1, nrhs, s, false);
         else
-            F.m2l.run<double>(qu64.p, cd64.p, n, nrhs, 0, GEMM_ATOMIC, s);
+            F.m2l.run<double>(qu64.p, cd64.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
         mark("m2l", s);
         for (int l = 0; l < O.n_levels(); l++) {
-            if (l > 0 && l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<double>(qd64.p, cd64.p, n, nrhs, 0, GEMM_ADD, s);
-            F.c2e_dn[l].run<double>(cd64.p, qd64.p, n, nrhs, 0, GEMM_STORE, s);
+            if (l > 0 && l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<double>(qd64.p, cd64.p, n, nrhs, 0, GEMM_ADD, s, &launches);
+            F.c2e_dn[l].run<double>(cd64.p, qd64.p, n, nrhs, 0, GEMM_STORE, s, &launches);
         }
         mark("l2l+c2e_down", s);
-        eval<double>(l2p, 0, false, true, O, dobs, 0, dobs, F.r_de, nullptr, 0, qd64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+        eval<double>(l2p, F.kt_kid, false, true, O, dobs, 0, dobs, F.r_de, nullptr, 0, qd64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
         mark("l2p", s);
     } else {
         gather_kernel<float><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s32.p, NS, R, nrhs);
         TBEM_CK(cudaGetLastError());
+        launches++;
         TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
         TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
         mark("gather", s);
-        eval<float>(p2m, 0, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
+        eval<float>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
         mark("p2m", s);
         for (int l = S.n_levels() - 1; l >= 0; l--)
-            if (l < (int)F.m2m.size()) F.m2m[l].run<float>(cu32.p, cu32.p, n, nrhs, 0, GEMM_ATOMIC, s);
+            if (l < (int)F.m2m.size()) F.m2m[l].run<float>(cu32.p, cu32.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
         mark("m2m", s);
-        eval<float>(p2p, 0, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
+        eval<float>(p2p, kid, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
         mark("p2p", s);
         const bool need64 = !L.m2p.empty() || F.m2l_on_the_fly;
         if (need64) {
             // explicit equivalent densities in FP64 (see the form notes)
             promote_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu32.p, cu64.p, ncs * nrhs * n);
             TBEM_CK(cudaGetLastError());
-            for (int l = 0; l < S.n_levels(); l++) F.c2e_up[l].run<double>(cu64.p, qu64.p, n, nrhs, 0, GEMM_STORE, s);
-            eval<double>(m2p, 0, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+            launches++;
+            for (int l = 0; l < S.n_levels(); l++) F.c2e_up[l].run<double>(cu64.p, qu64.p, n, nrhs, 0, GEMM_STORE, s, &launches);
+            eval<double>(m2p, F.kt_kid, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
         }
-        eval<float>(p2l, 0, true, false, O, dobs, F.r_dc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cd32.p, 1, nrhs, s, false);
+        eval<float>(p2l, F.ks_kid, true, false, O, dobs, F.r_dc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cd32.p, 1, nrhs, s, false);
         mark("m2p+p2l", s);
         if (F.m2l_on_the_fly) {
             TBEM_CK(cudaMemsetAsync(cd64.p, 0, sizeof(double) * nco * nrhs * n, s));
-            eval<double>(m2l_fly, 0, true, true, O, dobs, F.r_dc, *dsrc, F.r_ue, nullptr, 0, qu64.p, nullptr, 0, cd64.p, 1, nrhs, s, false);
+            eval<double>(m2l_fly, F.g_kid, true, true, O, dobs, F.r_dc, *dsrc, F.r_ue, nullptr, 0, qu64.p, nullptr, 0, cd64.p, 1, nrhs, s, false);
             add_kernel<<<grid_for(nco * nrhs * n), 256, 0, s>>>(cd64.p, cd32.p, nco * nrhs * n);
             TBEM_CK(cudaGetLastError());
+            launches++;
         } else {
-            F.m2l.run<float>(cu32.p, cd32.p, n, nrhs, 0, GEMM_ATOMIC, s);
+            F.m2l.run<float>(cu32.p, cd32.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
         }
         mark("m2l", s);
         for (int l = 1; l < O.n_levels(); l++)
-            if (l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 0, GEMM_ADD, s);
+            if (l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 0, GEMM_ADD, s, &launches);
         mark("l2l", s);
         if (F.n_l2p > 0) {
             l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cd32.p, n, R, nrhs, y64.p, NO);
             TBEM_CK(cudaGetLastError());
+            launches++;
         }
         mark("l2p", s);
     }
     scatter_kernel<<<grid_for(NO * R * nrhs), 256, 0, s>>>(y64.p, dobs.perm.p, nullptr, io_y.p, NO, R, nrhs);
     TBEM_CK(cudaGetLastError());
+    launches++;
     mark("scatter", s);
 }
 
@@ -1113,68 +1137,75 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
     if (!F.mixed) {
         gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
         TBEM_CK(cudaGetLastError());
+        launches++;
         TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
         TBEM_CK(cudaMemsetAsync(qd64.p, 0, sizeof(double) * nco * nrhs * n, s));
         // L2P^T, M2P^T, P2P^T
-        eval<double>(l2p_t, 0, true, false, O, dobs, F.r_de, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qd64.p, 1, nrhs, s, true);
-        eval<double>(m2p_t, 0, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
-        eval<double>(p2p_t, 0, false, false, S, *dsrc, 0, dobs, 0, y64.p, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
+        eval<double>(l2p_t, F.kt_kid, true, false, O, dobs, F.r_de, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qd64.p, 1, nrhs, s, true);
+        eval<double>(m2p_t, F.kt_kid, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
+        eval<double>(p2p_t, kid, false, false, S, *dsrc, 0, dobs, 0, y64.p, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
         // down pass reversed: deepest level first
         for (int l = O.n_levels() - 1; l >= 0; l--) {
-            F.c2e_dn_t[l].run<double>(qd64.p, cd64.p, n, nrhs, 1, GEMM_STORE, s);
-            if (l > 0 && l - 1 < (int)F.l2l_t.size()) F.l2l_t[l - 1].run<double>(cd64.p, qd64.p, n, nrhs, 1, GEMM_ATOMIC, s);
+            F.c2e_dn_t[l].run<double>(qd64.p, cd64.p, n, nrhs, 1, GEMM_STORE, s, &launches);
+            if (l > 0 && l - 1 < (int)F.l2l_t.size()) F.l2l_t[l - 1].run<double>(cd64.p, qd64.p, n, nrhs, 1, GEMM_ATOMIC, s, &launches);
         }
         if (F.m2l_on_the_fly)
-            eval<double>(m2l_fly_t, 0, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
+            eval<double>(m2l_fly_t, F.g_kid, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
         else
-            F.m2l_t.run<double>(cd64.p, qu64.p, n, nrhs, 1, GEMM_ATOMIC, s);
-        eval<double>(p2l_t, 0, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+            F.m2l_t.run<double>(cd64.p, qu64.p, n, nrhs, 1, GEMM_ATOMIC, s, &launches);
+        eval<double>(p2l_t, F.ks_kid, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
         // up pass reversed: root first
         for (int l = 0; l < S.n_levels(); l++) {
-            F.c2e_up_t[l].run<double>(qu64.p, cu64.p, n, nrhs, 1, GEMM_STORE, s);
-            if (l < (int)F.m2m_t.size()) F.m2m_t[l].run<double>(cu64.p, qu64.p, n, nrhs, 1, GEMM_ADD, s);
+            F.c2e_up_t[l].run<double>(qu64.p, cu64.p, n, nrhs, 1, GEMM_STORE, s, &launches);
+            if (l < (int)F.m2m_t.size()) F.m2m_t[l].run<double>(cu64.p, qu64.p, n, nrhs, 1, GEMM_ADD, s, &launches);
         }
-        eval<double>(p2m_t, 0, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+        eval<double>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
     } else {
         gather_kernel<float><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, s32.p, NO, R, nrhs);
         TBEM_CK(cudaGetLastError());
+        launches++;
         TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
         TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
         if (F.n_l2p > 0) {
             l2p_mixed_t_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, s32.p, NO, n, R, nrhs, cd32.p);
             TBEM_CK(cudaGetLastError());
+            launches++;
         }
-        eval<float>(p2p_t, 0, false, false, S, *dsrc, 0, dobs, 0, s32.p, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
+        eval<float>(p2p_t, kid, false, false, S, *dsrc, 0, dobs, 0, s32.p, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
         const bool need64 = !L.m2p.empty() || F.m2l_on_the_fly;
         if (need64) {
             TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
             // obs-space inputs in FP64 for the FP64 sub-paths
             gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
             TBEM_CK(cudaGetLastError());
-            eval<double>(m2p_t, 0, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
+            launches++;
+            eval<double>(m2p_t, F.kt_kid, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
         }
         for (int l = O.n_levels() - 1; l >= 1; l--)
-            if (l - 1 < (int)F.l2l_t.size()) F.l2l_t[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 1, GEMM_ATOMIC, s);
+            if (l - 1 < (int)F.l2l_t.size()) F.l2l_t[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 1, GEMM_ATOMIC, s, &launches);
         if (F.m2l_on_the_fly) {
             promote_kernel<<<grid_for(nco * nrhs * n), 256, 0, s>>>(cd32.p, cd64.p, nco * nrhs * n);
             TBEM_CK(cudaGetLastError());
-            eval<double>(m2l_fly_t, 0, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
+            launches++;
+            eval<double>(m2l_fly_t, F.g_kid, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
         } else {
-            F.m2l_t.run<float>(cd32.p, cu32.p, n, nrhs, 1, GEMM_ATOMIC, s);
+            F.m2l_t.run<float>(cd32.p, cu32.p, n, nrhs, 1, GEMM_ATOMIC, s, &launches);
         }
         if (need64) {
             // g_cup += C2E_up^T g_qup  (FP64), folded into the FP32 buffer
-            for (int l = 0; l < S.n_levels(); l++) F.c2e_up_t[l].run<double>(qu64.p, cu64.p, n, nrhs, 1, GEMM_STORE, s);
+            for (int l = 0; l < S.n_levels(); l++) F.c2e_up_t[l].run<double>(qu64.p, cu64.p, n, nrhs, 1, GEMM_STORE, s, &launches);
             add_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu64.p, cu32.p, ncs * nrhs * n);
             TBEM_CK(cudaGetLastError());
+            launches++;
         }
-        eval<float>(p2l_t, 0, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+        eval<float>(p2l_t, F.ks_kid, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
         for (int l = 0; l < S.n_levels(); l++)
-            if (l < (int)F.m2m_t.size()) F.m2m_t[l].run<float>(cu32.p, cu32.p, n, nrhs, 1, GEMM_ADD, s);
-        eval<float>(p2m_t, 0, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+            if (l < (int)F.m2m_t.size()) F.m2m_t[l].run<float>(cu32.p, cu32.p, n, nrhs, 1, GEMM_ADD, s, &launches);
+        eval<float>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
     }
     scatter_kernel<<<grid_for(NS * R * nrhs), 256, 0, s>>>(s64.p, dsrc->perm.p, dsrc->w.p, io_y.p, NS, R, nrhs);
     TBEM_CK(cudaGetLastError());
+    launches++;
     mark("scatter", s);
 }
 
@@ -1199,6 +1230,7 @@ void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
         return;
     }
     ensure_rhs(nrhs);
+    launches = 0;
     for (auto e : events) cudaEventDestroy(e);
     events.clear();
     phase_ms.clear();

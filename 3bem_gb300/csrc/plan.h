@@ -135,7 +135,8 @@ struct GemmSet {
     void add_group(long a_off, const std::vector<std::pair<int, int>>& pairs);
     void upload(const void* pool, size_t elem_size);
     template <typename T>
-    void run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s);
+    void run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s,
+             long* launches = nullptr);
 };
 
 struct DTree {
@@ -148,6 +149,11 @@ struct DTree {
 // Operators and task sets of one precision form.
 struct Form {
     bool mixed = false;
+    // kernels of the form: translations / check-to-equivalent systems use
+    // g_kid, real sources enter the check surfaces through ks_kid and the
+    // equivalent sources reach the targets through kt_kid (all equal to the
+    // operator's kernel in the plain form)
+    int g_kid = 0, ks_kid = 0, kt_kid = 0;
     double r_ue = 0, r_uc = 0, r_dc = 0, r_de = 0;
     std::vector<long> c2e_up_off, c2e_dn_off;  // offsets into c2e pool (FP64, n x n)
     DBuf<double> c2e;
@@ -198,6 +204,7 @@ struct Plan {
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t solver = nullptr;
     bool timing = false;
+    long launches = 0;  // kernel launches of the last apply
     std::vector<std::pair<std::string, double>> phase_ms;
     std::vector<cudaEvent_t> events;
     // kept for clone()
@@ -226,7 +233,7 @@ struct Plan {
     void forward(int nrhs, cudaStream_t s);
     void adjoint(int nrhs, cudaStream_t s);
     template <typename T>
-    void eval(const TaskSet& ts, int kid_trans, bool tgt_surf, bool src_surf, const Tree& tt,
+    void eval(const TaskSet& ts, int ekid, bool tgt_surf, bool src_surf, const Tree& tt,
               const DTree& dt, double t_rref, const DTree& ds, double s_rref, const T* s_str,
               long s_n, const T* q, double* y, long y_n, T* c, int add, int nrhs, cudaStream_t s,
               bool trans);

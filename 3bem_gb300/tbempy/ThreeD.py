@@ -112,7 +112,10 @@ def _ptr(a):
 
 def _stream_of(t):
     if torch is not None and isinstance(t, torch.Tensor) and t.is_cuda:
-        return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+        h = torch.cuda.current_stream(t.device).cuda_stream
+        # torch's default stream is the legacy stream (handle 0); NULL means
+        # "the operator's own stream" in the C ABI, so name it explicitly
+        return C.c_void_p(h if h else 1)
     return None
 
 
@@ -126,6 +129,9 @@ def _prep_in(x, n_cols):
         return xx, xx.shape[0], True, squeeze
     x = np.asarray(x, dtype=np.float64)
     squeeze = x.ndim == 1
+    if n_cols == 0:
+        xx = np.zeros((1 if squeeze else max(x.shape[0], 1), 0))
+        return xx, xx.shape[0], False, squeeze
     xx = np.ascontiguousarray(x.reshape(-1, n_cols))
     return xx, xx.shape[0], False, squeeze
 
@@ -269,6 +275,10 @@ class FMMOperator(OperatorI):
 
     def set_timing(self, enabled=True):
         check(_L.lib().tbem_fmm_set_timing(self._h, int(bool(enabled))))
+
+    def last_launches(self):
+        """Kernel launches made by the last apply."""
+        return check(_L.lib().tbem_fmm_last_launches(self._h))
 
     def phase_times(self):
         cap = 32

@@ -135,6 +135,10 @@ int tbem_fmm_set_c2e(TbemFmm* h, int which, long level, const double* op);
 int tbem_fmm_set_timing(TbemFmm* h, int enabled);
 int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int cap);
 
+/* Number of kernel launches the last apply made on the device (no
+ * reference counterpart; used to report the launch count of a timed run). */
+long tbem_fmm_last_launches(const TbemFmm* h);
+
 /* Direct N-body sum on the GPU in FP64 (nbody_eval over all pairs,
  * cpp/nbody_operator.h:117-141; the dense oracle make_direct_nbody_operator,
  * :143-152, matrix-free).  Same layouts as tbem_fmm_apply. */

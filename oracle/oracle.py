@@ -173,6 +173,12 @@ class OracleFMM(_FMMBase):
                 setf(self.h, which, lev, _ptr(P))
         self._apply = L.fn("apply", None, [_P, _P, _P, _I, _D])
 
+    def set_c2e(self, which, level, op):
+        """Install a check-to-equivalent operator (e.g. the reference's own)."""
+        op = _f64(op)
+        self.c2e[which][level] = op
+        self.L.fn("set_c2e", _L, [_P, _I, _L, _P])(self.h, which, level, _ptr(op))
+
     def apply(self, x, mask=0xff, list_fraction=1.0):
         x = _f64(x)
         assert x.shape == (self.R * self.n_src,)

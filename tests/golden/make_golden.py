@@ -1,0 +1,140 @@
+"""Generate the golden fixtures in this folder from the REFERENCE itself.
+
+Runs the unmodified reference FMM (tbenthompson/3bem cpp/, compiled from its
+own sources into oracle/_ref by oracle/ref/Makefile) through its C shim on
+small seeded inputs, and stores inputs, reference outputs, the reference's
+check-to-equivalent operators, trees and task lists.  The GPU tests compare
+the product against these without needing the reference checkout.
+
+    python tests/golden/make_golden.py [/root/reference]
+
+The reference's LAPACK (scipy's OpenBLAS) is run single-threaded so that
+the stored operators are reproducible.
+"""
+import os
+import sys
+
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+os.environ.setdefault("OMP_NUM_THREADS", "4")
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "3bem_gb300"))
+
+import numpy as np  # noqa: E402
+
+from oracle import oracle  # noqa: E402
+from tbempy import meshes  # noqa: E402
+
+# (name, kernel, n_src, n_obs (0 = same points), order, leaf, small_cells, seed, geometry)
+CASES = [
+    ("laps_cube", "LaplaceSingle", 600, 0, 35, 20, False, 1, "cube"),
+    ("laps_cube_small", "LaplaceSingle", 600, 0, 35, 20, True, 2, "cube"),
+    ("lapd_cube", "LaplaceDouble", 600, 0, 35, 20, False, 3, "cube"),
+    ("eldisp_cube", "ElasticDisplacement", 400, 0, 12, 20, False, 4, "cube"),
+    ("eltrac_cube_small", "ElasticTraction", 400, 0, 12, 20, True, 5, "cube"),
+    ("eladj_cube", "ElasticAdjointTraction", 400, 0, 12, 20, False, 6, "cube"),
+    ("laps_two_sets", "LaplaceSingle", 500, 300, 35, 20, False, 7, "cube"),
+    ("laps_sphere", "LaplaceSingle", 960, 0, 35, 30, False, 8, "sphere2"),
+    ("eldisp_fault", "ElasticDisplacement", 1536, 0, 12, 64, False, 9, "fault16"),
+]
+
+
+def points(geom, n, seed):
+    rng = np.random.default_rng(seed)
+    if geom == "cube":
+        locs = rng.uniform(0, 1, (n, 3))
+        nrm = rng.normal(size=(n, 3))
+        nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+        w = rng.uniform(0.5, 1.0, n)
+        return locs, nrm, w
+    if geom == "sphere2":
+        return meshes.sphere_points(2)
+    if geom == "fault16":
+        l, nn, w, _ = meshes.fault_points(16)
+        return l, nn, w
+    raise ValueError(geom)
+
+
+def make_case(name, kernel, n_src, n_obs, order, leaf, small, seed, geom):
+    locs, nrm, w = points(geom, n_src, seed)
+    if n_obs:
+        ol, on, _ = points("cube", n_obs, seed + 100)
+    else:
+        ol, on = locs, nrm
+    ref = oracle.RefFMM(kernel, ol, on, locs, nrm, w, 0.3, order, leaf, 0.05, small)
+    R = ref.R
+    rng = np.random.default_rng(seed + 1000)
+    x = rng.uniform(-1, 1, R * len(locs))
+    out = dict(kernel=kernel, order=order, leaf=leaf, small=int(small), mac=0.3, d=0.05,
+               obs_locs=ol, obs_normals=on, src_locs=locs, src_normals=nrm, src_weights=w,
+               x=x, y_ref=ref.apply(x),
+               y_direct=oracle.direct(kernel, ol, on, locs, nrm, w, x),
+               n_surf=ref.n_surf())
+    for which in (0, 1):
+        t = ref.tree(which)
+        for k in ("level", "index", "center", "hw", "n_idx", "n_children"):
+            out["tree%d_%s" % (which, k)] = t[k]
+        out["tree%d_indices" % which] = np.concatenate(t["indices"])
+        nl = ref.n_levels(which)
+        out["c2e%d" % which] = np.stack([ref.c2e(which, lev) for lev in range(nl)])
+    for kind in oracle.LISTS:
+        a, b = ref.list(kind)
+        out["list_%s_obs" % kind] = a
+        out["list_%s_src" % kind] = b
+    return out
+
+
+def kernel_vectors():
+    """Reference kernel tensors at seeded random configurations."""
+    rng = np.random.default_rng(42)
+    rows = []
+    for k in range(6):
+        for _ in range(40):
+            obs, src = rng.uniform(-1, 1, 3), rng.uniform(-1, 1, 3)
+            no, ns = rng.normal(size=3), rng.normal(size=3)
+            no /= np.linalg.norm(no)
+            ns /= np.linalg.norm(ns)
+            mu, nu = rng.uniform(0.5, 40.0), rng.uniform(0.1, 0.45)
+            K = oracle.kernel_tensor(k, obs, src, no, ns, mu, nu, lib="ref")
+            rows.append(np.concatenate([[k, mu, nu], obs, src, no, ns, np.pad(K.ravel(), (0, 9 - K.size))]))
+    # the self-pair rule: r^2 < 1e-12 gives a zero tensor
+    for k in range(6):
+        p = rng.uniform(-1, 1, 3)
+        K = oracle.kernel_tensor(k, p, p + 1e-7, np.array([1.0, 0, 0]), np.array([0, 1.0, 0]),
+                                 1.0, 0.25, lib="ref")
+        rows.append(np.concatenate([[k, 1.0, 0.25], p, p + 1e-7, [1, 0, 0], [0, 1, 0],
+                                    np.pad(K.ravel(), (0, 9 - K.size))]))
+    return np.array(rows)
+
+
+def main(ref_root="/root/reference"):
+    oracle.build()
+    if oracle.build_ref(ref_root) is None:
+        raise SystemExit("the reference checkout is needed to regenerate the fixtures")
+    for case in CASES:
+        data = make_case(*case)
+        np.savez_compressed(os.path.join(HERE, "fmm_%s.npz" % case[0]), **data)
+        print("wrote", case[0], {k: v.shape for k, v in data.items() if hasattr(v, "shape") and v.ndim})
+    np.savez_compressed(os.path.join(HERE, "kernels.npz"), rows=kernel_vectors())
+    surf = {str(o): oracle.RefFMM("LaplaceSingle", np.zeros((1, 3)), np.zeros((1, 3)),
+                                  np.zeros((1, 3)), np.zeros((1, 3)), np.ones(1), 0.3, o, 1,
+                                  0.05, False).n_surf() for o in (1, 6, 8, 20, 35, 75, 100, 152, 296)}
+    # the octree of the reference's degenerate-line test (unit_tests/test_octree.cpp:144-155),
+    # restated in 3D: points i and i + 1 on the x axis, one point per cell
+    line = np.array([[float(i), 0.0, 0.0] for i in range(10)] +
+                    [[float(i + 1), 0.0, 0.0] for i in range(10)])
+    ref = oracle.RefFMM("LaplaceSingle", line, np.ones_like(line), line, np.ones_like(line),
+                        np.ones(len(line)), 0.3, 6, 1, 0.05, False)
+    t = ref.tree(0)
+    np.savez_compressed(os.path.join(HERE, "misc.npz"),
+                        surf_orders=np.array([int(k) for k in surf]),
+                        surf_counts=np.array(list(surf.values())),
+                        line_pts=line, line_n_cells=len(t["level"]),
+                        line_levels=t["level"], line_n_idx=t["n_idx"])
+    print("surface counts", surf, "line cells", len(t["level"]))
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])

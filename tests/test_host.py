@@ -1,0 +1,123 @@
+"""CPU tests of the product's host side: the C ABI library loads and exports
+every symbol include/tbem_gpu.h declares, the host octree / task lists are
+bit-identical to the reference's (golden fixtures), and argument errors come
+back as status codes.  No device compute happens here (host_only plans)."""
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+CASES = sorted(glob.glob(os.path.join(GOLDEN, "fmm_*.npz")))
+LISTS = ["p2m", "m2m", "p2p", "m2p", "p2l", "m2l", "l2l", "l2p"]
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "tbem_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(tbem_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    from tbempy import _lib
+    L = _lib.lib()
+    names = header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    # and the ctypes table covers exactly the header
+    assert sorted(_lib.SIGNATURES) == names
+
+
+def kernel_from_name(name):
+    from tbempy import ThreeD
+    k = getattr(ThreeD, name)
+    return k(1.0, 0.25) if name.startswith("Elastic") else k()
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(p)[4:-4] for p in CASES])
+def test_host_tree_and_lists_match_reference(path):
+    from tbempy import ThreeD
+    g = dict(np.load(path))
+    cfg = ThreeD.FMMConfig(float(g["mac"]), int(g["order"]), int(g["leaf"]), float(g["d"]),
+                           bool(g["small"]))
+    op = ThreeD.FMMOperator(kernel_from_name(str(g["kernel"])), g["obs_locs"], g["obs_normals"],
+                            g["src_locs"], g["src_normals"], g["src_weights"], cfg, host_only=True)
+    assert op.n_surface() == int(g["n_surf"])
+    for which in (0, 1):
+        t = op.tree(which)
+        for k in ("level", "index", "center", "hw", "n_idx", "n_children"):
+            assert np.array_equal(t[k], g["tree%d_%s" % (which, k)]), k
+        assert np.array_equal(np.concatenate(t["indices"]), g["tree%d_indices" % which])
+    for kind in LISTS:
+        a, b = op.list(kind)
+        assert np.array_equal(a, g["list_%s_obs" % kind]), kind
+        assert np.array_equal(b, g["list_%s_src" % kind]), kind
+
+
+def test_host_tree_matches_oracle_on_fault():
+    from oracle import oracle
+    from tbempy import ThreeD, meshes
+    locs, nrm, w, _ = meshes.fault_points(32)
+    for small in (False, True):
+        cfg = ThreeD.FMMConfig(0.3, 50, 64, 0.05, small)
+        op = ThreeD.FMMOperator(ThreeD.ElasticTraction(1.0, 0.25), locs, nrm, locs, nrm, w, cfg,
+                                host_only=True)
+        orc = oracle.OracleFMM("ElasticTraction", locs, nrm, locs, nrm, w, 0.3, 50, 64, 0.05, small)
+        for kind in LISTS:
+            for u, v in zip(op.list(kind), orc.list(kind)):
+                assert np.array_equal(u, v)
+
+
+def test_degenerate_inputs_build():
+    """Coincident and nearly coincident points (unit_tests/test_octree.cpp:113-125)."""
+    from tbempy import ThreeD
+    cfg = ThreeD.FMMConfig(0.3, 6, 1, 0.05, False)
+    for pts in (np.array([[1.0, 2.0, 0.0], [1.0, 2.0, 0.0]]),
+                np.array([[1.0, 2.0, 0.0], [1.0, 2.0 - 1e-20, 0.0], [0.0, 0.0, 0.0]])):
+        op = ThreeD.FMMOperator(ThreeD.LaplaceSingle(), pts, pts, pts, pts, np.ones(len(pts)),
+                                cfg, host_only=True)
+        t = op.tree(0)
+        assert t["n_idx"][0] == len(pts)
+
+
+def test_empty_meshes_build():
+    """Empty meshes must not error (acceptance_tests/test_empty_operator.py:10-17)."""
+    from tbempy import ThreeD
+    e = np.zeros((0, 3))
+    cfg = ThreeD.FMMConfig(0.3, 20, 10, 0.05, False)
+    op = ThreeD.FMMOperator(ThreeD.LaplaceSingle(), e, e, e, e, np.zeros(0), cfg, host_only=True)
+    assert op.n_rows() == 0 and op.n_cols() == 0
+
+
+def test_argument_errors_are_status_codes():
+    from tbempy import ThreeD
+    from tbempy._lib import TbemError
+    p = np.random.default_rng(0).uniform(0, 1, (10, 3))
+    with pytest.raises(TbemError) as e:
+        ThreeD.FMMOperator(ThreeD.LaplaceSingle(), p, p, p, p, np.ones(10),
+                           ThreeD.FMMConfig(0.3, 20, 0, 0.05, False), host_only=True)
+    assert e.value.code == -1 and "min_pts" in str(e.value)
+
+    class Bad(ThreeD.Kernel):
+        kernel_id = 42
+    with pytest.raises(TbemError):
+        ThreeD.FMMOperator(Bad(), p, p, p, p, np.ones(10),
+                           ThreeD.FMMConfig(0.3, 20, 5, 0.05, False), host_only=True)
+    op = ThreeD.FMMOperator(ThreeD.LaplaceSingle(), p, p, p, p, np.ones(10),
+                            ThreeD.FMMConfig(0.3, 20, 5, 0.05, False), host_only=True)
+    with pytest.raises(TbemError) as e:
+        op.apply(np.ones(10))
+    assert e.value.code == -4
+
+
+def test_csr_create_validates():
+    from tbempy import ThreeD
+    from tbempy._lib import TbemError
+    with pytest.raises(TbemError):
+        ThreeD.SparseOperator(2, 2, [1.0], [5], [0, 1, 1])   # column out of range
+    with pytest.raises(TbemError):
+        ThreeD.SparseOperator(2, 2, [1.0, 2.0], [0, 1], [0, 2, 1])  # decreasing row_ptrs

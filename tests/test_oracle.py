@@ -1,0 +1,207 @@
+"""CPU tests: the oracle (restatement of the reference KIFMM) pinned against
+the reference's own outputs (golden fixtures made by tests/golden/make_golden.py
+from the reference compiled from its sources), against the reference's
+known-answer tests, and -- where the reference checkout is present -- against
+the reference library itself."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = sorted(glob.glob(os.path.join(GOLDEN, "fmm_*.npz")))
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def load(path):
+    return dict(np.load(path, allow_pickle=False))
+
+
+def oracle_for(g):
+    return oracle.OracleFMM(str(g["kernel"]), g["obs_locs"], g["obs_normals"], g["src_locs"],
+                            g["src_normals"], g["src_weights"], float(g["mac"]), int(g["order"]),
+                            int(g["leaf"]), float(g["d"]), bool(g["small"]))
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(p)[4:-4] for p in CASES])
+def test_oracle_matches_reference_fixture(path):
+    g = load(path)
+    o = oracle_for(g)
+    assert o.n_surf() == int(g["n_surf"])
+    for which in (0, 1):
+        t = o.tree(which)
+        for k in ("level", "index", "center", "hw", "n_idx", "n_children"):
+            assert np.array_equal(t[k], g["tree%d_%s" % (which, k)]), k
+        assert np.array_equal(np.concatenate(t["indices"]), g["tree%d_indices" % which])
+    for kind in oracle.LISTS:
+        a, b = o.list(kind)
+        assert np.array_equal(a, g["list_%s_obs" % kind]) and np.array_equal(b, g["list_%s_src" % kind])
+    # the reference's own check-to-equivalent operators: the apply agrees to rounding
+    for which in (0, 1):
+        for lev, op in enumerate(g["c2e%d" % which]):
+            o.set_c2e(which, lev, op)
+    assert rel(o.apply(g["x"]), g["y_ref"]) < 1e-12
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(p)[4:-4] for p in CASES])
+def test_direct_matches_reference_fixture(path):
+    g = load(path)
+    y = oracle.direct(str(g["kernel"]), g["obs_locs"], g["obs_normals"], g["src_locs"],
+                      g["src_normals"], g["src_weights"], g["x"])
+    assert rel(y, g["y_direct"]) < 1e-13
+
+
+def test_pinv_matches_reference_operators():
+    """The oracle's LAPACK pseudo-inverse reproduces the reference's operators."""
+    g = load(os.path.join(GOLDEN, "fmm_laps_cube.npz"))
+    o = oracle_for(g)
+    for which in (0, 1):
+        for lev, op in enumerate(g["c2e%d" % which]):
+            assert np.linalg.norm(o.c2e[which][lev] - op) <= 1e-10 * np.linalg.norm(op)
+
+
+def test_kernel_golden_vectors():
+    rows = np.load(os.path.join(GOLDEN, "kernels.npz"))["rows"]
+    for r in rows:
+        k, mu, nu = int(r[0]), r[1], r[2]
+        K = oracle.kernel_tensor(k, r[3:6], r[6:9], r[9:12], r[12:15], mu, nu)
+        ref = r[15:15 + K.size].reshape(K.shape)
+        assert np.allclose(K, ref, rtol=1e-14, atol=0), (k, K, ref)
+
+
+REF_ELASTIC = "/root/reference/unit_tests/test_data_elastic3"
+
+
+@pytest.mark.skipif(not os.path.exists(REF_ELASTIC), reason="reference checkout absent")
+def test_elastic_kernels_against_reference_sympy_data():
+    """The reference's symbolic golden data (unit_tests/test_data_elastic3,
+    checked by unit_tests/test_elastic_kernels.cpp:54-103 at 1e-8)."""
+    ids = {"disp": 2, "trac": 3, "adj_trac": 4}
+    n = 0
+    with open(REF_ELASTIC) as f:
+        for line in f:
+            e = line.strip().split(",")
+            if e[1] not in ids:
+                continue
+            k, j = int(e[2]), int(e[3])
+            v = [float(t) for t in e[8:20]]
+            K = oracle.kernel_tensor(ids[e[1]], v[3:6], v[0:3], v[9:12], v[6:9], float(e[4]), float(e[5]))
+            exact = float(e[0])
+            if exact != 0.0:
+                err = abs(exact - K[k, j]) / ((abs(exact) + abs(K[k, j])) / 2)
+                assert err < 1e-8
+            else:
+                assert K[k, j] == 0.0
+            n += 1
+    assert n == 270
+
+
+def test_laplace_nbody_known_values():
+    """unit_tests/test_nbody_operator.cpp:27-41."""
+    obs = np.array([[0, 0, 0], [0, 2, 0], [0, 0, -1.0]])
+    src = np.array([[1, 0, 0], [0, 1, 0.0]])
+    y = oracle.direct("LaplaceSingle", obs, np.zeros((3, 3)), src, np.zeros((2, 3)),
+                      np.ones(2), np.array([4.0, 0.0]))
+    assert np.allclose(y, [0.3183, 0.1424, 0.2251], atol=1e-3)
+
+
+def test_pseudoinverse_known_answers():
+    """unit_tests/test_blas_wrapper.cpp:32-66."""
+    assert np.allclose(oracle.pinv_reference(np.array([[2, 1], [-1, 0.5]]), 1e-16),
+                       [[0.25, -0.5], [0.5, 1.0]], atol=1e-14)
+    m = np.array([[0.0238032718573239, 0.1524037864980028],
+                  [0.1524037864980028, 0.9762067281426762]])
+    assert np.allclose(oracle.pinv_reference(m, 1e-16),
+                       [[97620.6728142285282956, -15240.3786497941800917],
+                        [-15240.3786497941782727, 2380.3271857314393856]], atol=1e-4)
+    assert np.allclose(oracle.pinv_reference(m, 1e-4),
+                       [[0.0237935097924219, 0.1524053105511083],
+                        [0.1524053105511085, 0.9762064902075779]], atol=1e-12)
+
+
+def test_surface_point_counts():
+    g = load(os.path.join(GOLDEN, "misc.npz"))
+    for o, c in zip(g["surf_orders"], g["surf_counts"]):
+        assert len(oracle.surface(int(o))) == c
+
+
+def test_degenerate_line_octree():
+    """The reference's degenerate-line octree test (unit_tests/test_octree.cpp:144-155),
+    restated in 3D; the count comes from the reference itself."""
+    g = load(os.path.join(GOLDEN, "misc.npz"))
+    line = g["line_pts"]
+    o = oracle.OracleFMM("LaplaceSingle", line, np.ones_like(line), line, np.ones_like(line),
+                         np.ones(len(line)), 0.3, 6, 1, 0.05, False)
+    t = o.tree(0)
+    assert len(t["level"]) == int(g["line_n_cells"])
+    assert np.array_equal(t["n_idx"], g["line_n_idx"])
+
+
+def test_octree_structure():
+    """Point conservation, unique indices, balance (unit_tests/test_octree.cpp:22-111,173-178)."""
+    rng = np.random.default_rng(0)
+    pts = rng.uniform(0, 1, (20000, 3))
+    o = oracle.OracleFMM("LaplaceSingle", pts[:10], np.ones((10, 3)), pts, np.ones_like(pts),
+                         np.ones(len(pts)), 0.3, 6, 100, 0.05, False)
+    t = o.tree(0)
+    assert len(np.unique(t["index"])) == len(t["index"])
+    assert t["n_idx"][0] == len(pts)
+    # children of the root hold about n/8 points each
+    kids = np.where(t["level"] == 1)[0]
+    assert len(kids) == 8
+    assert np.all(np.abs(t["n_idx"][kids] - len(pts) / 8) < len(pts) / 16)
+    # leaves partition the points
+    leaves = np.where(t["n_children"] == 0)[0]
+    allpts = np.sort(np.concatenate([t["indices"][i] for i in leaves]))
+    assert np.array_equal(allpts, np.arange(len(pts)))
+
+
+def _ref_error(out, exact):
+    """Per-entry min(|d/exact|, |d/mean|exact||) of unit_tests/test_fmm.cpp:70-98."""
+    avg = np.mean(np.abs(exact))
+    d = out - exact
+    with np.errstate(divide="ignore", invalid="ignore"):
+        e1 = np.abs(d / exact)
+    return np.minimum(np.nan_to_num(e1, nan=np.inf), np.abs(d / avg))
+
+
+@pytest.mark.parametrize("name,order", [("LaplaceSingle", 35), ("LaplaceDouble", 75)])
+def test_oracle_fmm_accuracy_reference_cases(name, order):
+    """unit_tests/test_fmm.cpp:129-137: 100 random points, mac 0.35, one point
+    per cell, d = 0.05, error <= 1e-4 against the direct operator."""
+    rng = np.random.default_rng(1)
+    src, obs, nrm = rng.uniform(0, 1, (100, 3)), rng.uniform(0, 1, (100, 3)), rng.uniform(0, 1, (100, 3))
+    o = oracle.OracleFMM(name, obs, nrm, src, nrm, np.ones(100), 0.35, order, 1, 0.05, False)
+    x = np.ones(100)
+    exact = oracle.direct(name, obs, nrm, src, nrm, np.ones(100), x)
+    assert np.all(_ref_error(o.apply(x), exact) <= 1e-4)
+
+
+def test_identity_fmm_known_answer():
+    rng = np.random.default_rng(2)
+    pts = rng.uniform(0, 1, (300, 3))
+    o = oracle.OracleFMM("IdentityScalar", pts, pts, pts, pts, np.ones(300), 0.3, 6, 8, 0.05, False)
+    assert np.allclose(o.apply(np.ones(300)), 299.0, rtol=1e-9)
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference library not built here")
+@pytest.mark.parametrize("small", [False, True])
+def test_oracle_vs_reference_library(small):
+    rng = np.random.default_rng(3)
+    pts = rng.uniform(0, 1, (1500, 3))
+    nrm = rng.normal(size=(1500, 3))
+    w = rng.uniform(0.5, 1, 1500)
+    for name, order in (("LaplaceDouble", 35), ("ElasticTraction", 20)):
+        a = oracle.OracleFMM(name, pts, nrm, pts, nrm, w, 0.3, order, 30, 0.05, small)
+        b = oracle.RefFMM(name, pts, nrm, pts, nrm, w, 0.3, order, 30, 0.05, small)
+        for which in (0, 1):
+            for lev in range(b.n_levels(which)):
+                a.set_c2e(which, lev, b.c2e(which, lev))
+        x = rng.uniform(-1, 1, a.R * 1500)
+        assert rel(a.apply(x), b.apply(x)) < 1e-12
