@@ -202,4 +202,4 @@ def test_torch_device_tensors():
     x = np.random.default_rng(21).uniform(-1, 1, 600)
     y_np = op.apply(x)
     y_t = op.apply(torch.tensor(x, device="cuda"))
-    assert y_t.is_cuda and rel(y_t.cpu().numpy(), y_np) < 1e-14
+    assert y_t.is_cuda and rel(y_t.cpu().numpy(), y_np) < 1e-12  # float atomics order
