@@ -148,6 +148,21 @@ int tbem_direct_apply(int kernel, const double* kernel_params,
                       const double* src_weights, long n_src,
                       const double* x, double* y, int n_rhs, void* stream);
 
+/* The direct FP64 sum of tbem_direct_apply for callers that cannot allocate
+ * device memory.  No counterpart in the reference.  Every data pointer must be
+ * device memory; nothing is copied, allocated or freed.  Its scratch (weighted
+ * strengths and work items) is a static 16 MiB device array kept by every GPU
+ * that loads the library: R * n_src * n_rhs must not exceed 1,966,080 and
+ * n_obs must stay below about 3 million, else TBEM_ERR_ARG.  The first call on
+ * a device looks up the array's device address (make it before any stream
+ * capture).  All calls share the array: calls that overlap on the GPU race.
+ * Asynchronous on `stream`. */
+int tbem_direct_apply_noalloc(int kernel, const double* kernel_params,
+                              const double* obs_locs, const double* obs_normals, long n_obs,
+                              const double* src_locs, const double* src_normals,
+                              const double* src_weights, long n_src,
+                              const double* x, double* y, int n_rhs, void* stream);
+
 /* CSR operator (SparseOperator, cpp/sparse_operator.h:44-83):
  * y = A x for n_rhs right-hand sides (x[r*n_cols + j], y[r*n_rows + i]).
  * Column indices are int64 like the reference's size_t.  FP64. */
