@@ -1,0 +1,95 @@
+"""GMRES and FP64 iterative refinement around the operator apply.
+
+The reference solves with scipy's GMRES on a LinearOperator whose matvec is
+``op.apply`` (acceptance_tests/laplace.py:21-31).  Here:
+
+* ``gmres(matvec, b, restart, tol, maxiter)`` -- restarted GMRES with modified
+  Gram-Schmidt and Givens rotations, on numpy or torch vectors (whatever the
+  matvec takes and returns);
+* ``refined_solve(apply_fp64, apply_fast, b, tol)`` -- FP64 iterative
+  refinement: the residual r = b - A x is formed with the FP64 operator, the
+  correction A d = r is solved loosely with the fast (mixed-precision)
+  operator, x += d, until ||r|| / ||b|| <= tol.  The fast operator's own error
+  only slows the outer iteration; the answer is the FP64 operator's.
+"""
+import math
+
+import numpy as np
+
+
+def _dot(a, b):
+    return float((a * b).sum())
+
+
+def _norm(a):
+    return math.sqrt(_dot(a, a))
+
+
+def gmres(matvec, b, x0=None, restart=50, tol=1e-10, maxiter=1000, callback=None):
+    """Restarted GMRES(restart).  Returns (x, info, iterations); info = 0 on
+    convergence (||b - A x|| <= tol ||b||), 1 otherwise."""
+    x = b * 0 if x0 is None else x0.copy() if hasattr(x0, "copy") else x0.clone()
+    bnorm = _norm(b)
+    if bnorm == 0.0:
+        return x, 0, 0
+    it = 0
+    while it < maxiter:
+        r = b - matvec(x)
+        beta = _norm(r)
+        if beta <= tol * bnorm:
+            return x, 0, it
+        V = [r / beta]
+        H = np.zeros((restart + 1, restart))
+        cs = np.zeros(restart)
+        sn = np.zeros(restart)
+        g = np.zeros(restart + 1)
+        g[0] = beta
+        k_done = 0
+        for k in range(restart):
+            w = matvec(V[k])
+            for j in range(k + 1):
+                H[j, k] = _dot(w, V[j])
+                w = w - H[j, k] * V[j]
+            H[k + 1, k] = _norm(w)
+            V.append(w / H[k + 1, k] if H[k + 1, k] > 0 else w)
+            for j in range(k):
+                t = cs[j] * H[j, k] + sn[j] * H[j + 1, k]
+                H[j + 1, k] = -sn[j] * H[j, k] + cs[j] * H[j + 1, k]
+                H[j, k] = t
+            den = math.hypot(H[k, k], H[k + 1, k])
+            cs[k], sn[k] = (1.0, 0.0) if den == 0 else (H[k, k] / den, H[k + 1, k] / den)
+            H[k, k] = cs[k] * H[k, k] + sn[k] * H[k + 1, k]
+            H[k + 1, k] = 0.0
+            g[k + 1] = -sn[k] * g[k]
+            g[k] = cs[k] * g[k]
+            it += 1
+            k_done = k + 1
+            if callback:
+                callback(abs(g[k + 1]) / bnorm)
+            if abs(g[k + 1]) <= tol * bnorm or it >= maxiter:
+                break
+        y = np.linalg.solve(np.triu(H[:k_done, :k_done]), g[:k_done])
+        for j in range(k_done):
+            x = x + y[j] * V[j]
+    r = b - matvec(x)
+    return x, 0 if _norm(r) <= tol * bnorm else 1, it
+
+
+def refined_solve(apply_fp64, apply_fast, b, tol=1e-10, inner_tol=1e-6, restart=50,
+                  max_outer=20, inner_maxiter=500):
+    """FP64 iterative refinement.  Returns (x, history) where history holds
+    (outer iteration, inner iterations, relative FP64 residual)."""
+    x = b * 0
+    bnorm = _norm(b)
+    history = []
+    r = b - apply_fp64(x)
+    for outer in range(max_outer):
+        rel = _norm(r) / bnorm
+        if rel <= tol:
+            history.append((outer, 0, rel))
+            break
+        d, _, its = gmres(apply_fast, r, restart=restart, tol=inner_tol, maxiter=inner_maxiter)
+        x = x + d
+        r = b - apply_fp64(x)
+        history.append((outer, its, _norm(r) / bnorm))
+    return x, history

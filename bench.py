@@ -43,9 +43,9 @@ N_GRID = 128
 N_ERR_ROWS = 4096
 
 
-def workload():
+def workload(grid=N_GRID):
     from tbempy import meshes
-    locs, nrm, w, uv = meshes.fault_points(N_GRID, 45.0)
+    locs, nrm, w, uv = meshes.fault_points(grid, 45.0)
     x = meshes.tapered_slip(uv, seed=1)
     return locs, nrm, w, x
 
@@ -113,6 +113,19 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": float(max(smax)) if smax else None,
                 "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def aggregate(seconds, units_per_rank, dist=None, device=None):
+    """Whole-job throughput of independent replicas: every rank processed
+    `units_per_rank`; the job took the slowest rank's time."""
+    world = 1
+    if dist is not None and dist.is_initialized():
+        import torch
+        world = dist.get_world_size()
+        t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        seconds = float(t.item())
+    return world * units_per_rank / seconds, seconds
 
 
 def m2l_flops(op, n_rhs):
@@ -194,6 +207,10 @@ def main():
     ap.add_argument("--cpu-fraction", type=float, default=0.01)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--grid", type=int, default=N_GRID,
+                    help="quads per fault side (128 = the workload; smaller for ncu captures)")
+    ap.add_argument("--kernels", default="both", choices=["both", "disp"])
+    ap.add_argument("--m2l-path", type=int, default=0, help="0 auto, 1 SIMT FP32, 2 tcgen05")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
@@ -211,12 +228,15 @@ def main():
         dist.init_process_group("nccl")
 
     from tbempy import ThreeD
-    locs, nrm, w, x = workload()
+    locs, nrm, w, x = workload(args.grid)
     N = len(locs)
     cfg = ThreeD.FMMConfig(MAC, ORDER, LEAF, D, False)
     kernels = [ThreeD.ElasticDisplacement(MU, NU), ThreeD.ElasticTraction(MU, NU)]
+    if args.kernels == "disp":
+        kernels = kernels[:1]
     t0 = time.perf_counter()
-    ops = [ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed", device=local)
+    ops = [ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed", device=local,
+                              m2l_path=args.m2l_path)
            for K in kernels]
     setup_s = time.perf_counter() - t0
     n_rhs = args.rhs
@@ -247,11 +267,8 @@ def main():
             dist.barrier()
     ms = e0.elapsed_time(e1) / args.steps
     launches = sum(op.last_launches() for op in ops) * args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 2 * N * n_rhs / (ms / 1e3)
+    value, sec = aggregate(ms / 1e3, len(ops) * N * n_rhs, dist, "cuda")
+    ms = sec * 1e3
 
     # -- end to end through the C ABI with host buffers (pinned)
     xh = torch.tensor(X).pin_memory()
@@ -273,11 +290,7 @@ def main():
     for _ in range(args.steps):
         step_e2e()
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * 2 * N * n_rhs / e2e_s
+    e2e_value, e2e_s = aggregate(e2e_s, len(ops) * N * n_rhs, dist, "cuda")
 
     # -- accuracy against the FP64 direct sum on 4,096 random rows
     rng = np.random.default_rng(7)
@@ -327,7 +340,7 @@ def main():
             exact = direct.apply(x)
             got = op.apply(x).reshape(3, N)[:, rows].reshape(-1)
             perr[type(K).__name__] = float(np.linalg.norm(got - exact) / np.linalg.norm(exact))
-        plain = {"ms_per_step": pms, "points_rhs_per_s": 2 * N * n_rhs / (pms / 1e3),
+        plain = {"ms_per_step": pms, "points_rhs_per_s": len(pops) * N * n_rhs / (pms / 1e3),
                  "rel_err_vs_direct": perr, "speedup_mixed_vs_plain": pms / ms}
         del pops
 

@@ -1,0 +1,92 @@
+"""GPU tests of the differentiation form (autograd through the transposed
+apply), the FP64 iterative refinement around the precision form, and the
+IntegralOperator composition A = G F I + N + C."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def cloud(n, seed):
+    rng = np.random.default_rng(seed)
+    locs = rng.uniform(0, 1, (n, 3))
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    return locs, nrm, rng.uniform(0.5, 1.0, n)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_misfit_gradient_matches_transpose_and_finite_differences(prec):
+    torch = pytest.importorskip("torch")
+    from tbempy import ThreeD, autograd
+    src, sn, w = cloud(400, 1)
+    obs, on, _ = cloud(300, 2)
+    op = ThreeD.FMMOperator(ThreeD.ElasticDisplacement(1.0, 0.25), obs, on, src, sn, w,
+                            ThreeD.FMMConfig(0.3, 296 if prec == "mixed" else 35, 30, 0.05, False),
+                            precision=prec)
+    rng = np.random.default_rng(3)
+    s = torch.tensor(rng.uniform(-1, 1, op.n_cols()), device="cuda", requires_grad=True)
+    d = torch.tensor(rng.normal(size=op.n_rows()), device="cuda")
+    L = autograd.misfit(op, s, d)
+    L.backward()
+    g = s.grad.cpu().numpy()
+    # against the dense transpose: A^T (A s - d)
+    A = op.apply(np.eye(op.n_cols())).T
+    r = A @ s.detach().cpu().numpy() - d.cpu().numpy()
+    g_dense = A.T @ r
+    # the precision form's forward M2L runs on the tensor cores (3xBF16) and its
+    # transpose on the FP32 pipes: the two agree to the split's rounding
+    tol = 1e-11 if prec == "fp64" else 2e-5
+    assert np.linalg.norm(g - g_dense) <= tol * np.linalg.norm(g_dense)
+    # central finite differences on 64 random coordinates (h = 1e-6)
+    h = 1e-6
+    s0 = s.detach()
+    for j in rng.choice(op.n_cols(), 64, replace=False):
+        e = torch.zeros_like(s0)
+        e[j] = h
+        fd = (autograd.misfit(op, s0 + e, d) - autograd.misfit(op, s0 - e, d)).item() / (2 * h)
+        assert abs(fd - g[j]) <= 1e-6 * max(1.0, np.abs(g).max())
+
+
+def test_refined_gmres_reaches_fp64_residual():
+    """Second-kind Laplace system (0.5 I + D) sigma = f on a sphere: inner
+    GMRES with the precision form, FP64 residuals with the plain form."""
+    from tbempy import ThreeD, meshes, solve
+    locs, nrm, w = meshes.sphere_points(3)
+    cfg = ThreeD.FMMConfig(0.3, 152, 40, 0.05, False)
+    K = ThreeD.LaplaceDouble()
+    plain = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="fp64")
+    fast = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed")
+    A64 = lambda v: 0.5 * v + plain.apply(v)
+    A32 = lambda v: 0.5 * v + fast.apply(v)
+    f = 1.0 / np.linalg.norm(locs - np.array([0.1, 0.2, 0.3]), axis=1)
+    x, hist = solve.refined_solve(A64, A32, f, tol=1e-10, inner_tol=1e-6)
+    assert hist[-1][2] <= 1e-10, hist
+    assert np.linalg.norm(A64(x) - f) <= 1e-10 * np.linalg.norm(f)
+
+
+def test_integral_operator_composition():
+    from tbempy import ThreeD
+    rng = np.random.default_rng(4)
+    locs, nrm, w = cloud(500, 5)
+    far = ThreeD.FMMOperator(ThreeD.LaplaceSingle(), locs, nrm, locs, nrm, w,
+                             ThreeD.FMMConfig(0.3, 35, 25, 0.05, False))
+    n_dof = 200
+
+    def rand_csr(n_rows, n_cols, nnz):
+        r = rng.integers(0, n_rows, nnz)
+        c = rng.integers(0, n_cols, nnz)
+        v = rng.normal(size=nnz)
+        D = np.zeros((n_rows, n_cols))
+        np.add.at(D, (r, c), v)
+        return ThreeD.SparseOperator.csr_from_coo(n_rows, n_cols, r, c, v), D
+
+    interp, I = rand_csr(500, n_dof, 1500)
+    galerkin, G = rand_csr(n_dof, 500, 1500)
+    near, N = rand_csr(n_dof, n_dof, 800)
+    corr, Cm = rand_csr(n_dof, n_dof, 800)
+    op = ThreeD.IntegralOperator(near, corr, galerkin, far, interp)
+    x = rng.normal(size=n_dof)
+    expect = G @ far.apply(I @ x) + N @ x + Cm @ x
+    assert np.linalg.norm(op.apply(x) - expect) <= 1e-12 * np.linalg.norm(expect)
+    assert op.n_rows() == n_dof and op.n_cols() == n_dof
