@@ -876,6 +876,14 @@ void Plan::build_mixed_ops(Form& F)
         }
     }
     build_gemm_sets(F, 0, 0, 0, m2m_off, l2l_off, m2l_off);
+    // m2l_path: 0 auto (tensor cores for M2L, M2M and L2L), 1 SIMT FP32 for all,
+    // 2 tensor cores for M2L only, 3 tensor cores for all
+    F.use_tc = opt.m2l_path != 1 && !jobs.empty();
+    F.use_tc_updown = F.use_tc && (opt.m2l_path == 0 || opt.m2l_path == 3);
+    if (F.use_tc) {
+        F.tc.build(F.ops32.p, (long)jobs.size(), n, stream);
+        TBEM_CK(cudaStreamSynchronize(stream));
+    }
 
     // per-leaf L2P operators E = K(points, down-equiv) * C2E_down(level)
     const Tree& O = otree;
@@ -1081,8 +1089,19 @@ void Plan::forward(int nrhs, cudaStream_t s)
         mark("gather", s);
         eval<float>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
         mark("p2m", s);
-        for (int l = S.n_levels() - 1; l >= 0; l--)
-            if (l < (int)F.m2m.size()) F.m2m[l].run<float>(cu32.p, cu32.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
+        for (int l = S.n_levels() - 1; l >= 0; l--) {
+            if (l >= (int)F.m2m.size() || F.m2m[l].empty()) continue;
+            if (F.use_tc_updown) {
+                // children of level l live at level l + 1 (contiguous cells)
+                const long r0 = (long)S.level_start[l + 1] * nrhs;
+                const long rn = (long)(S.level_start[l + 2] - S.level_start[l + 1]) * nrhs;
+                F.tc.split_b_rows(cu32.p, r0, rn, ncs * nrhs, s);
+                launches++;
+                F.m2m[l].run_tc(F.tc, cu32.p, n, nrhs, 1, (long)n * n, s, &launches);
+            } else {
+                F.m2m[l].run<float>(cu32.p, cu32.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
+            }
+        }
         mark("m2m", s);
         eval<float>(p2p, kid, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
         mark("p2p", s);
@@ -1103,12 +1122,27 @@ void Plan::forward(int nrhs, cudaStream_t s)
             add_kernel<<<grid_for(nco * nrhs * n), 256, 0, s>>>(cd64.p, cd32.p, nco * nrhs * n);
             TBEM_CK(cudaGetLastError());
             launches++;
+        } else if (F.use_tc) {
+            F.tc.split_b_rows(cu32.p, 0, ncs * nrhs, std::max(ncs, nco) * nrhs, s);
+            launches++;
+            F.m2l.run_tc(F.tc, cd32.p, n, nrhs, 1, (long)n * n, s, &launches);
         } else {
             F.m2l.run<float>(cu32.p, cd32.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
         }
         mark("m2l", s);
-        for (int l = 1; l < O.n_levels(); l++)
-            if (l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 0, GEMM_ADD, s, &launches);
+        for (int l = 1; l < O.n_levels(); l++) {
+            if (l - 1 >= (int)F.l2l.size() || F.l2l[l - 1].empty()) continue;
+            if (F.use_tc_updown) {
+                // parents at level l - 1 (contiguous cells)
+                const long r0 = (long)O.level_start[l - 1] * nrhs;
+                const long rn = (long)(O.level_start[l] - O.level_start[l - 1]) * nrhs;
+                F.tc.split_b_rows(cd32.p, r0, rn, std::max(ncs, nco) * nrhs, s);
+                launches++;
+                F.l2l[l - 1].run_tc(F.tc, cd32.p, n, nrhs, 0, (long)n * n, s, &launches);
+            } else {
+                F.l2l[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 0, GEMM_ADD, s, &launches);
+            }
+        }
         mark("l2l", s);
         if (F.n_l2p > 0) {
             l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cd32.p, n, R, nrhs, y64.p, NO);
@@ -1240,7 +1274,14 @@ void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
     else forward(nrhs, s);
     TBEM_CK(cudaMemcpyAsync(y, io_y.p, sizeof(double) * n_out * nrhs,
                             y_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
-    if (!y_dev || timing) TBEM_CK(cudaStreamSynchronize(s));
+    if (!y_dev || timing) {
+        TBEM_CK(cudaStreamSynchronize(s));
+        if (f.use_tc) {
+            int flag = 0;
+            TBEM_CK(cudaMemcpy(&flag, f.tc.err.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (flag) throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
+        }
+    }
     if (timing && events.size() > 1) {
         for (size_t i = 1; i < events.size(); i++) {
             float ms = 0;

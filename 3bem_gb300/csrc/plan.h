@@ -2,6 +2,7 @@
 // constructor, cpp/fmm.cpp:72-101) and the apply sequences.
 #pragma once
 #include <cublas_v2.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 
@@ -120,6 +121,19 @@ struct TaskSet {
     }
 };
 
+// bf16 hi/lo planes of the precision form's FP32 operators, padded for the
+// tensor-core GEMM (tc_gemm.cu), plus the split of the current B operand.
+struct TcPlanes {
+    int n = 0, m_pad = 0, k_pad = 0;
+    DBuf<__nv_bfloat16> hi, lo, bhi, blo;
+    DBuf<int> err;  // set by a tensor-core GEMM whose bounded wait gave up
+    void build(const float* ops32, long n_ops, int n, cudaStream_t s);
+    void split_b(const float* cells, long rows, cudaStream_t s);
+    // split only rows [row0, row0 + rows) of a [rows_total][n] buffer into
+    // the same rows of the planes (capacity for rows_total rows)
+    void split_b_rows(const float* cells, long row0, long rows, long rows_total, cudaStream_t s);
+};
+
 // A set of GEMM groups (gemm.cuh) sharing B and D buffers.
 struct GemmSet {
     std::vector<long> A_off;  // operator offsets (elements) into an operator pool
@@ -137,6 +151,11 @@ struct GemmSet {
     template <typename T>
     void run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s,
              long* launches = nullptr);
+    // tensor-core path (B taken from P's split planes); nn = elements per operator
+    DBuf<int> d_op;
+    std::map<int, std::pair<DBuf<int>, DBuf<int>>> tc_tiles;
+    void run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, long nn, cudaStream_t s,
+                long* launches);
 };
 
 struct DTree {
@@ -165,6 +184,10 @@ struct Form {
     std::vector<GemmSet> c2e_up_t, m2m_t, l2l_t, c2e_dn_t;
     GemmSet m2l_t;
     bool m2l_on_the_fly = false;
+    // mixed: tensor-core planes of ops32 (M2L on tcgen05 when use_tc)
+    TcPlanes tc;
+    bool use_tc = false;
+    bool use_tc_updown = false;
     // mixed: per-leaf L2P operators
     DBuf<float> E;
     DBuf<long> E_row0;  // per l2p task

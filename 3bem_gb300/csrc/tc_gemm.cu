@@ -1,0 +1,382 @@
+// Tensor-core (tcgen05, sm_103a) grouped gather/scatter GEMM for the
+// precision form's translations:  D[:, out(p), r] += A_g B[:, in(p), r].
+//
+// The FP32 operands are split into bf16 pairs, a = a_hi + a_lo, and the
+// product is accumulated from three bf16 MMAs (hi.hi + hi.lo + lo.hi) in an
+// FP32 accumulator in tensor memory: about 16 significant bits per product,
+// FP32 accumulation.  The operators' planes are built once at setup; the
+// check potentials (B) are split before every use.
+//
+// CTA: 128 threads, one 128 x 128 accumulator (128 TMEM columns).  K runs in
+// chunks of 64 bf16 (128-byte rows) through a 3-stage shared-memory ring.
+// All threads stage a chunk (A rows from the operator planes, B rows gathered
+// by pair) into 128B-swizzled K-major tiles; one thread issues the 12 MMAs of
+// the chunk and commits them to the stage's mbarrier, which the threads wait
+// on (with a bounded wait) before they overwrite that stage.  The epilogue
+// reads the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31)
+// and scatters it into D.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "plan.h"
+
+namespace tbem {
+
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 3, TC_THREADS = 128;
+constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;            // 16 KB: one 128 x 64 bf16 plane tile
+constexpr int TC_STAGE_BYTES = 4 * TC_TILE_BYTES;           // A_hi, A_lo, B_hi, B_lo
+constexpr int TC_SMEM_BYTES = TC_STAGES * TC_STAGE_BYTES + 1024;
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
+
+struct TcArgs {
+    const __nv_bfloat16* Ahi;
+    const __nv_bfloat16* Alo;
+    long a_op_stride;   // m_pad * k_pad
+    int k_pad;
+    const int* g_op;    // per group: operator index
+    const long* g_pair0;
+    const int* g_npairs;
+    const int* tile_group;
+    const int* tile_col0;
+    const int* in_cell;
+    const int* out_cell;
+    const __nv_bfloat16* Bhi;  // [cell][rhs][k_pad]
+    const __nv_bfloat16* Blo;
+    float* D;                  // [cell][rhs][n]
+    int n;
+    int nrhs;
+    int atomic;
+    int* err;
+};
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused with this swizzle)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;             // descriptor version
+    d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor: kind::f16 with bf16 A/B, FP32 D, both K-major, M = N = 128.
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
+                              ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accum)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(TC_IDESC), "r"(accum));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false if the phase did not complete within the budget.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+{
+    long long t0 = clock64();
+    while (!mbar_try(mbar, parity)) {
+        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+        "%28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Copy 8 x 16 bytes of one 128-byte row into its swizzled place.
+__device__ __forceinline__ void stage_row(uint8_t* tile, int row, const uint4* src, bool valid)
+{
+    uint4 v[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) v[j] = valid ? __ldg(src + j) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        *reinterpret_cast<uint4*>(tile + row * 128 + ((j ^ (row & 7)) << 4)) = v[j];
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
+{
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t mbar[TC_STAGES];
+    __shared__ uint32_t tmem_slot;
+    uint8_t* smem = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+
+    const int tid = threadIdx.x, warp = tid / 32;
+    const int tile = blockIdx.x;
+    const int g = a.tile_group[tile];
+    const int col0 = a.tile_col0[tile];
+    const int m0 = blockIdx.y * TC_BM;
+    const long pair0 = a.g_pair0[g];
+    const int ncols = a.g_npairs[g] * a.nrhs;
+    const int nk = a.k_pad / TC_BK;
+    const __nv_bfloat16* Ahi = a.Ahi + (long)a.g_op[g] * a.a_op_stride + (long)(m0 + tid) * a.k_pad;
+    const __nv_bfloat16* Alo = a.Alo + (long)a.g_op[g] * a.a_op_stride + (long)(m0 + tid) * a.k_pad;
+    // B row of this thread: one gathered (cell, rhs) column
+    const int c = col0 + tid;
+    const bool bvalid = c < ncols;
+    long brow = 0;
+    if (bvalid) {
+        const int p = c / a.nrhs, r = c % a.nrhs;
+        brow = ((long)a.in_cell[pair0 + p] * a.nrhs + r) * a.k_pad;
+    }
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_slot)),
+                     "r"(TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < TC_STAGES; s++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[s])));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    bool ok = true;
+    int issued = 0;  // chunks whose MMAs were committed
+    for (int kc = 0; kc < nk; kc++) {
+        const int s = kc % TC_STAGES;
+        uint8_t* st = smem + s * TC_STAGE_BYTES;
+        if (kc >= TC_STAGES) {
+            // the stage is free once the MMAs of chunk kc - TC_STAGES completed;
+            // the decision is made CTA-wide so that no thread is left at a barrier
+            const bool w = mbar_wait(smem_u32(&mbar[s]), ((kc - TC_STAGES) / TC_STAGES) & 1);
+            ok = __syncthreads_and(w);
+            if (!ok) break;
+        }
+        const int k0 = kc * TC_BK;
+        stage_row(st, tid, reinterpret_cast<const uint4*>(Ahi + k0), true);
+        stage_row(st + TC_TILE_BYTES, tid, reinterpret_cast<const uint4*>(Alo + k0), true);
+        stage_row(st + 2 * TC_TILE_BYTES, tid, reinterpret_cast<const uint4*>(a.Bhi + brow + k0), bvalid);
+        stage_row(st + 3 * TC_TILE_BYTES, tid, reinterpret_cast<const uint4*>(a.Blo + brow + k0), bvalid);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ah = smem_u32(st), al = ah + TC_TILE_BYTES;
+            const uint32_t bh = ah + 2 * TC_TILE_BYTES, bl = ah + 3 * TC_TILE_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; kk++) {
+                const uint32_t off = kk * 32;  // 16 bf16 along K inside the swizzle atom
+                mma_bf16(tmem, sw128_desc(ah + off), sw128_desc(bh + off), (kc | kk) != 0);
+                mma_bf16(tmem, sw128_desc(ah + off), sw128_desc(bl + off), 1);
+                mma_bf16(tmem, sw128_desc(al + off), sw128_desc(bh + off), 1);
+            }
+            mma_commit(smem_u32(&mbar[s]));
+        }
+        issued = kc + 1;
+    }
+    // the commit of the last issued chunk covers every MMA issued before it;
+    // after a timeout this still drains what is in flight before TMEM is freed
+    if (issued > 0) {
+        const bool w = mbar_wait(smem_u32(&mbar[(issued - 1) % TC_STAGES]), ((issued - 1) / TC_STAGES) & 1);
+        ok = __syncthreads_and(w && ok);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) {
+        if (tid == 0) atomicExch(a.err, 1);
+    } else {
+        const int row = m0 + warp * 32 + (tid % 32);
+#pragma unroll 1
+        for (int cc = 0; cc < TC_BN / 32; cc++) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cc * 32, v);
+            if (row >= a.n) continue;
+#pragma unroll 4
+            for (int j = 0; j < 32; j++) {
+                const int col = col0 + cc * 32 + j;
+                if (col >= ncols) break;
+                const int p = col / a.nrhs, r = col % a.nrhs;
+                float* dst = a.D + ((long)a.out_cell[pair0 + p] * a.nrhs + r) * a.n + row;
+                if (a.atomic) atomicAdd(dst, v[j]);
+                else *dst += v[j];
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+}
+
+// in [rows][n] FP32 -> hi/lo bf16 [rows][k_pad] (columns >= n zero)
+__global__ void split_rows_kernel(const float* in, long rows, int n, int k_pad,
+                                  __nv_bfloat16* hi, __nv_bfloat16* lo)
+{
+    const long total = rows * k_pad;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k_pad;
+        const int k = (int)(t % k_pad);
+        const float v = k < n ? in[r * n + k] : 0.f;
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[t] = h;
+        lo[t] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
+// operators [op][n][n] FP32 -> hi/lo [op][m_pad][k_pad] (zero padding)
+__global__ void split_ops_kernel(const float* in, long n_ops, int n, int m_pad, int k_pad,
+                                 __nv_bfloat16* hi, __nv_bfloat16* lo)
+{
+    const long total = n_ops * m_pad * (long)k_pad;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % k_pad);
+        const long rm = t / k_pad;
+        const int m = (int)(rm % m_pad);
+        const long op = rm / m_pad;
+        const float v = (m < n && k < n) ? in[(op * n + m) * (long)n + k] : 0.f;
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[t] = h;
+        lo[t] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
+}  // namespace
+
+void TcPlanes::build(const float* ops32, long n_ops, int n, cudaStream_t s)
+{
+    this->n = n;
+    m_pad = (n + TC_BM - 1) / TC_BM * TC_BM;
+    k_pad = (n + TC_BK - 1) / TC_BK * TC_BK;
+    const long total = n_ops * (long)m_pad * k_pad;
+    hi.alloc(std::max<long>(total, 1));
+    lo.alloc(std::max<long>(total, 1));
+    if (total > 0) {
+        split_ops_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
+            ops32, n_ops, n, m_pad, k_pad, hi.p, lo.p);
+        TBEM_CK(cudaGetLastError());
+    }
+    err.alloc(1);
+    TBEM_CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+    // per device: set on every build (the plan's device is current)
+    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TC_SMEM_BYTES));
+}
+
+void TcPlanes::split_b(const float* cells, long rows, cudaStream_t s)
+{
+    const long total = rows * (long)k_pad;
+    bhi.ensure(std::max<long>(total, 1));
+    blo.ensure(std::max<long>(total, 1));
+    if (total > 0) {
+        split_rows_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
+            cells, rows, n, k_pad, bhi.p, blo.p);
+        TBEM_CK(cudaGetLastError());
+    }
+}
+
+void TcPlanes::split_b_rows(const float* cells, long row0, long rows, long rows_total,
+                            cudaStream_t s)
+{
+    bhi.ensure(std::max<long>(rows_total * (long)k_pad, 1));
+    blo.ensure(std::max<long>(rows_total * (long)k_pad, 1));
+    const long total = rows * (long)k_pad;
+    if (total > 0) {
+        split_rows_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
+            cells + row0 * (long)n, rows, n, k_pad, bhi.p + row0 * k_pad, blo.p + row0 * k_pad);
+        TBEM_CK(cudaGetLastError());
+    }
+}
+
+void GemmSet::run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, long nn,
+                     cudaStream_t s, long* launches)
+{
+    if (empty()) return;
+    if (d_op.n == 0) {
+        std::vector<int> op(A_off.size());
+        for (size_t g = 0; g < A_off.size(); g++) op[g] = (int)(A_off[g] / nn);
+        d_op.upload(op);
+    }
+    auto it = tc_tiles.find(nrhs);
+    if (it == tc_tiles.end()) {
+        std::vector<int> tg, tc;
+        for (size_t g = 0; g < npairs.size(); g++) {
+            const int ncols = npairs[g] * nrhs;
+            for (int c = 0; c < ncols; c += TC_BN) {
+                tg.push_back((int)g);
+                tc.push_back(c);
+            }
+        }
+        auto& e = tc_tiles[nrhs];
+        e.first.upload(tg);
+        e.second.upload(tc);
+        it = tc_tiles.find(nrhs);
+    }
+    TcArgs a;
+    a.Ahi = P.hi.p;
+    a.Alo = P.lo.p;
+    a.a_op_stride = (long)P.m_pad * P.k_pad;
+    a.k_pad = P.k_pad;
+    a.g_op = d_op.p;
+    a.g_pair0 = d_pair0.p;
+    a.g_npairs = d_npairs.p;
+    a.tile_group = it->second.first.p;
+    a.tile_col0 = it->second.second.p;
+    a.in_cell = d_in.p;
+    a.out_cell = d_out.p;
+    a.Bhi = P.bhi.p;
+    a.Blo = P.blo.p;
+    a.D = D;
+    a.n = n;
+    a.nrhs = nrhs;
+    a.atomic = atomic;
+    a.err = P.err.p;
+    dim3 grid((unsigned)it->second.first.n, (unsigned)(P.m_pad / TC_BM));
+    tc_gemm_kernel<<<grid, TC_THREADS, TC_SMEM_BYTES, s>>>(a);
+    TBEM_CK(cudaGetLastError());
+    if (launches) (*launches)++;
+}
+
+}  // namespace tbem

@@ -63,7 +63,9 @@ typedef struct {
     int precision;         /* TBEM_PRECISION_*                                   */
     int device;            /* CUDA device ordinal                                */
     double svd_threshold;  /* singular-value cutoff (reference: 1e-10, fmm.cpp:122) */
-    int m2l_path;          /* 0 auto, 1 SIMT FP32 GEMM, 2 tcgen05 3xBF16 (mixed only) */
+    int m2l_path;          /* precision form's dense translations: 0 auto (tcgen05
+                              3xBF16 for M2L, M2M and L2L), 1 SIMT FP32 for all,
+                              2 tcgen05 for M2L only, 3 tcgen05 for all           */
     int p2p_block;         /* 0 auto; else threads per target in the P2P kernel (1,2,4,8) */
     int host_only;         /* 1: build trees and task lists only (no device use);
                               apply calls then fail with TBEM_ERR_STATE            */
@@ -147,6 +149,22 @@ int tbem_direct_apply(int kernel, const double* kernel_params,
                       const double* src_locs, const double* src_normals,
                       const double* src_weights, long n_src,
                       const double* x, double* y, int n_rhs, void* stream);
+
+/* Kernel-gradient pass of the direct FP64 operator (no reference
+ * counterpart: the reference has no derivatives).  With A_ij =
+ * w_j K(x_i, y_j; n_i, n_j) and L = r^T A x it writes dL/d(obs_locs) [n_obs][3],
+ * dL/d(obs_normals), dL/d(src_locs) [n_src][3], dL/d(src_normals),
+ * dL/d(src_weights) [n_src] and dL/dx = A^T r [C][n_src].  Kernel derivatives
+ * are exact (forward-mode dual numbers on the device).  Any output may be
+ * NULL; host or device memory. */
+int tbem_direct_gradients(int kernel, const double* kernel_params,
+                          const double* obs_locs, const double* obs_normals, long n_obs,
+                          const double* src_locs, const double* src_normals,
+                          const double* src_weights, long n_src,
+                          const double* x, const double* r,
+                          double* g_obs_locs, double* g_obs_normals,
+                          double* g_src_locs, double* g_src_normals,
+                          double* g_src_weights, double* g_x, void* stream);
 
 /* The direct FP64 sum of tbem_direct_apply for callers that cannot allocate
  * device memory.  No counterpart in the reference.  Every data pointer must be

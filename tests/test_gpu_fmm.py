@@ -41,12 +41,13 @@ def kernel_obj(name):
     return k(1.0, 0.25) if name.startswith("Elastic") else k()
 
 
-def make_pair(name, locs, nrm, w, order, leaf, small, precision="fp64", obs=None):
+def make_pair(name, locs, nrm, w, order, leaf, small, precision="fp64", obs=None, m2l_path=0):
     from tbempy import ThreeD
     ol, on = (locs, nrm) if obs is None else obs
     orc = oracle.OracleFMM(name, ol, on, locs, nrm, w, 0.3, order, leaf, 0.05, small)
     op = ThreeD.FMMOperator(kernel_obj(name), ol, on, locs, nrm, w,
-                            ThreeD.FMMConfig(0.3, order, leaf, 0.05, small), precision=precision)
+                            ThreeD.FMMConfig(0.3, order, leaf, 0.05, small), precision=precision,
+                            m2l_path=m2l_path)
     return orc, op
 
 
@@ -119,6 +120,20 @@ def test_mixed_vs_direct(name):
     assert err < 2e-6, err
 
 
+@pytest.mark.parametrize("name,order", [("LaplaceSingle", 152), ("ElasticTraction", 296)])
+def test_mixed_tensor_core_m2l_matches_simt(name, order):
+    """tcgen05 3xBF16 M2L against the FP32 SIMT M2L on the same operators."""
+    from tbempy import ThreeD, meshes
+    locs, nrm, w = meshes.sphere_points(3)
+    cfg = ThreeD.FMMConfig(0.3, order, 40, 0.05, False)
+    tc = ThreeD.FMMOperator(kernel_obj(name), locs, nrm, locs, nrm, w, cfg, precision="mixed",
+                            m2l_path=2)
+    simt = ThreeD.FMMOperator(kernel_obj(name), locs, nrm, locs, nrm, w, cfg, precision="mixed",
+                              m2l_path=1)
+    X = np.random.default_rng(22).uniform(-1, 1, (3, tc.n_cols()))
+    assert rel(tc.apply(X), simt.apply(X)) < 2e-6
+
+
 def test_multi_rhs_matches_single():
     locs, nrm, w = cloud(900, 10)
     for prec in ("fp64", "mixed"):
@@ -135,7 +150,8 @@ def test_adjoint_is_transpose(prec, name):
     locs, nrm, w = cloud(300, 12)
     ol, on, _ = cloud(250, 13)
     for obs in (None, (ol, on)):
-        orc, op = make_pair(name, locs, nrm, w, 20, 20, True, precision=prec, obs=obs)
+        # the transposed passes run on the FP32 pipes: compare with the same pipes forward
+        orc, op = make_pair(name, locs, nrm, w, 20, 20, True, precision=prec, obs=obs, m2l_path=1)
         nc, nr = op.n_cols(), op.n_rows()
         A = op.apply(np.eye(nc)).T           # column j = A e_j
         At = op.apply_adjoint(np.eye(nr)).T  # column i = A^T e_i
