@@ -323,6 +323,40 @@ class DirectOperator(OperatorI):
                               self._src_normals, self._src_weights)
 
 
+def direct_gradients(K, obs_locs, obs_normals, src_locs, src_normals, src_weights, x, r):
+    """Kernel-gradient pass: derivatives of L = r^T A x (A the direct
+    operator) with respect to every point position, normal and weight and to
+    x.  Arrays may be numpy (host) or float64 CUDA tensors; returns the same
+    kind, keyed obs_locs, obs_normals, src_locs, src_normals, src_weights, x."""
+    is_t = torch is not None and isinstance(obs_locs, torch.Tensor)
+
+    def prep(a, shape):
+        if is_t:
+            return a.reshape(shape).contiguous()
+        return _f64(a, shape)
+
+    ol, on = prep(obs_locs, (-1, 3)), prep(obs_normals, (-1, 3))
+    sl, sn = prep(src_locs, (-1, 3)), prep(src_normals, (-1, 3))
+    sw = prep(src_weights, (-1,))
+    xx, rr = prep(x, (-1,)), prep(r, (-1,))
+    n_obs, n_src = ol.shape[0], sl.shape[0]
+
+    def out(shape):
+        if is_t:
+            return torch.empty(shape, dtype=torch.float64, device=ol.device)
+        return np.empty(shape)
+
+    g = {"obs_locs": out((n_obs, 3)), "obs_normals": out((n_obs, 3)),
+         "src_locs": out((n_src, 3)), "src_normals": out((n_src, 3)),
+         "src_weights": out((n_src,)), "x": out((K.tensor_dim * n_src,))}
+    check(_L.lib().tbem_direct_gradients(
+        K.kernel_id, _ptr(K.params()), _ptr(ol), _ptr(on), n_obs, _ptr(sl), _ptr(sn), _ptr(sw),
+        n_src, _ptr(xx), _ptr(rr), _ptr(g["obs_locs"]), _ptr(g["obs_normals"]),
+        _ptr(g["src_locs"]), _ptr(g["src_normals"]), _ptr(g["src_weights"]), _ptr(g["x"]),
+        _stream_of(ol)))
+    return g
+
+
 class SparseOperator(OperatorI):
     """CSR operator (cpp/sparse_operator.h:44-83) with a GPU apply."""
 

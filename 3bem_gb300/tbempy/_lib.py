@@ -56,6 +56,8 @@ SIGNATURES = {
     "tbem_fmm_phase_times": (_I, [_P, _P, _P, _I]),
     "tbem_fmm_last_launches": (_L, [_P]),
     "tbem_direct_apply": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _I, _P]),
+    "tbem_direct_gradients": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _P, _P, _P, _P,
+                                   _P, _P, _P]),
     "tbem_direct_apply_noalloc": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _I, _P]),
     "tbem_csr_create": (_I, [_L, _L, _P, _P, _P, _P]),
     "tbem_csr_apply": (_I, [_P, _P, _P, _I, _P]),

@@ -33,3 +33,33 @@ def misfit(op, s, d):
     """L = 0.5 ||A s - d||^2 (the differentiated workload's loss)."""
     r = fmm_apply(op, s) - d
     return 0.5 * (r * r).sum()
+
+
+class _DirectApply(torch.autograd.Function):
+    """y = A x with A_ij = w_j K(x_i, y_j; n_i, n_j), differentiable in the
+    densities and in every point position, normal and weight."""
+
+    @staticmethod
+    def forward(ctx, obs_locs, obs_normals, src_locs, src_normals, src_weights, x, K):
+        from .ThreeD import DirectOperator
+        ctx.K = K
+        ctx.save_for_backward(obs_locs, obs_normals, src_locs, src_normals, src_weights, x)
+        op = DirectOperator(K, obs_locs.detach().cpu().numpy(), obs_normals.detach().cpu().numpy(),
+                            src_locs.detach().cpu().numpy(), src_normals.detach().cpu().numpy(),
+                            src_weights.detach().cpu().numpy())
+        return op.apply(x.detach().contiguous())
+
+    @staticmethod
+    def backward(ctx, grad):
+        from .ThreeD import direct_gradients
+        ol, on, sl, sn, sw, x = ctx.saved_tensors
+        g = direct_gradients(ctx.K, ol.detach(), on.detach(), sl.detach(), sn.detach(), sw.detach(),
+                             x.detach(), grad.contiguous())
+        return (g["obs_locs"], g["obs_normals"], g["src_locs"], g["src_normals"],
+                g["src_weights"], g["x"], None)
+
+
+def direct_apply(K, obs_locs, obs_normals, src_locs, src_normals, src_weights, x):
+    """Differentiable direct (FP64) operator apply on the GPU; all inputs
+    float64 CUDA tensors ([n,3] points/normals, [n] weights, [C n_src] x)."""
+    return _DirectApply.apply(obs_locs, obs_normals, src_locs, src_normals, src_weights, x, K)

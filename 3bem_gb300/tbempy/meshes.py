@@ -138,3 +138,19 @@ def tapered_slip(uv, seed=1):
     taper = np.cos(0.5 * np.pi * uv[:, 0]) * np.cos(0.5 * np.pi * uv[:, 1])
     s = rng.uniform(-1.0, 1.0, size=(3, n)) * taper[None, :]
     return np.ascontiguousarray(s.reshape(-1))
+
+
+def points_from_mesh_torch(verts, tris):
+    """points_from_mesh with torch tensors (differentiable in the vertices):
+    3-point rule locations, unit normals and weights area / 3."""
+    import torch
+    t = torch.as_tensor(tris, dtype=torch.long, device=verts.device)
+    p = verts[t]                                           # [nt, 3, 3]
+    cr = torch.cross(p[:, 2] - p[:, 0], p[:, 2] - p[:, 1], dim=1)
+    nrm = torch.linalg.norm(cr, dim=1)
+    normals = cr / nrm[:, None]
+    bary = torch.as_tensor(_TRI3_BARY, dtype=verts.dtype, device=verts.device)
+    locs = torch.einsum("qk,tkd->tqd", bary, p).reshape(-1, 3)
+    normals = normals.repeat_interleave(3, dim=0)
+    weights = ((1.0 / 6.0) * nrm).repeat_interleave(3)    # (1/6) (2 area)
+    return locs, normals, weights
