@@ -121,11 +121,11 @@ struct TaskSet {
     }
 };
 
-// bf16 hi/lo planes of the precision form's FP32 operators, padded for the
-// tensor-core GEMM (tc_gemm.cu), plus the split of the current B operand.
+// Three-term bf16 planes of the precision form's FP32 operators, padded for
+// the tensor-core GEMM (tc_gemm.cu), plus the split of the current B operand.
 struct TcPlanes {
     int n = 0, m_pad = 0, k_pad = 0;
-    DBuf<__nv_bfloat16> hi, lo, bhi, blo;
+    DBuf<__nv_bfloat16> a[3], b[3];
     DBuf<int> err;  // set by a tensor-core GEMM whose bounded wait gave up
     void build(const float* ops32, long n_ops, int n, cudaStream_t s);
     void split_b(const float* cells, long rows, cudaStream_t s);

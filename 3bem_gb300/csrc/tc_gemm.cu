@@ -1,18 +1,20 @@
 // Tensor-core (tcgen05, sm_103a) grouped gather/scatter GEMM for the
-// precision form's translations:  D[:, out(p), r] += A_g B[:, in(p), r].
+// precision form's translations:  D[:, out(p), r] (+)= A_g B[:, in(p), r].
 //
-// The FP32 operands are split into bf16 pairs, a = a_hi + a_lo, and the
-// product is accumulated from three bf16 MMAs (hi.hi + hi.lo + lo.hi) in an
-// FP32 accumulator in tensor memory: about 16 significant bits per product,
-// FP32 accumulation.  The operators' planes are built once at setup; the
-// check potentials (B) are split before every use.
+// Every FP32 operand is split into three bf16 terms, a = a0 + a1 + a2 (each
+// term holds the next 8 significant bits), and the product is accumulated
+// from the six bf16 MMAs that reach 2^-24 relative size (a0b0, a0b1, a1b0,
+// a0b2, a1b1, a2b0) in an FP32 accumulator in tensor memory: FP32-level
+// accuracy on the bf16 tensor pipe.  The operators' planes are built once at
+// setup; the check potentials (B) are split before every use.
 //
 // CTA: 128 threads, one 128 x 128 accumulator (128 TMEM columns).  K runs in
-// chunks of 64 bf16 (128-byte rows) through a 3-stage shared-memory ring.
-// All threads stage a chunk (A rows from the operator planes, B rows gathered
-// by pair) into 128B-swizzled K-major tiles; one thread issues the 12 MMAs of
-// the chunk and commits them to the stage's mbarrier, which the threads wait
-// on (with a bounded wait) before they overwrite that stage.  The epilogue
+// chunks of 64 bf16 (128-byte rows) through a 2-stage shared-memory ring of
+// six 128B-swizzled K-major planes per stage.  All threads stage a chunk with
+// cp.async (A rows from the operator planes, B rows gathered by pair; 48
+// copies per thread in flight), one thread issues the chunk's 24 MMAs and
+// commits them to the stage's mbarrier; the next chunk's copies overlap the
+// current chunk's MMAs.  Waits are bounded and CTA-uniform.  The epilogue
 // reads the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31)
 // and scatters it into D.
 #include <cuda_bf16.h>
@@ -22,27 +24,26 @@
 
 namespace tbem {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 3, TC_THREADS = 128;
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 2, TC_THREADS = 128;
+constexpr int TC_TERMS = 3;                                  // bf16 terms per operand
 constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;            // 16 KB: one 128 x 64 bf16 plane tile
-constexpr int TC_STAGE_BYTES = 4 * TC_TILE_BYTES;           // A_hi, A_lo, B_hi, B_lo
+constexpr int TC_STAGE_BYTES = 2 * TC_TERMS * TC_TILE_BYTES; // A0..A2, B0..B2
 constexpr int TC_SMEM_BYTES = TC_STAGES * TC_STAGE_BYTES + 1024;
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
 
 struct TcArgs {
-    const __nv_bfloat16* Ahi;
-    const __nv_bfloat16* Alo;
-    long a_op_stride;   // m_pad * k_pad
+    const __nv_bfloat16* A[TC_TERMS];  // [op][m_pad][k_pad] per term
+    long a_op_stride;                  // m_pad * k_pad
     int k_pad;
-    const int* g_op;    // per group: operator index
+    const int* g_op;                   // per group: operator index
     const long* g_pair0;
     const int* g_npairs;
     const int* tile_group;
     const int* tile_col0;
     const int* in_cell;
     const int* out_cell;
-    const __nv_bfloat16* Bhi;  // [cell][rhs][k_pad]
-    const __nv_bfloat16* Blo;
-    float* D;                  // [cell][rhs][n]
+    const __nv_bfloat16* B[TC_TERMS];  // [cell][rhs][k_pad] per term
+    float* D;                          // [cell][rhs][n]
     int n;
     int nrhs;
     int atomic;
@@ -128,15 +129,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// Copy 8 x 16 bytes of one 128-byte row into its swizzled place.
-__device__ __forceinline__ void stage_row(uint8_t* tile, int row, const uint4* src, bool valid)
+// cp.async of one 128-byte row (8 x 16 bytes) into its swizzled place; a
+// row that is not valid is zero-filled (source size 0, nothing is read).
+__device__ __forceinline__ void stage_row_async(uint32_t tile, int row, const __nv_bfloat16* src,
+                                                bool valid)
 {
-    uint4 v[8];
+    const uint32_t n = valid ? 16u : 0u;
 #pragma unroll
-    for (int j = 0; j < 8; j++) v[j] = valid ? __ldg(src + j) : make_uint4(0, 0, 0, 0);
-#pragma unroll
-    for (int j = 0; j < 8; j++)
-        *reinterpret_cast<uint4*>(tile + row * 128 + ((j ^ (row & 7)) << 4)) = v[j];
+    for (int j = 0; j < 8; j++) {
+        const uint32_t dst = tile + row * 128 + ((j ^ (row & 7)) << 4);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst),
+                     "l"(src + j * 8), "r"(n)
+                     : "memory");
+    }
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
@@ -155,8 +160,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     const long pair0 = a.g_pair0[g];
     const int ncols = a.g_npairs[g] * a.nrhs;
     const int nk = a.k_pad / TC_BK;
-    const __nv_bfloat16* Ahi = a.Ahi + (long)a.g_op[g] * a.a_op_stride + (long)(m0 + tid) * a.k_pad;
-    const __nv_bfloat16* Alo = a.Alo + (long)a.g_op[g] * a.a_op_stride + (long)(m0 + tid) * a.k_pad;
+    const long a_off = (long)a.g_op[g] * a.a_op_stride + (long)(m0 + tid) * a.k_pad;
     // B row of this thread: one gathered (cell, rhs) column
     const int c = col0 + tid;
     const bool bvalid = c < ncols;
@@ -181,41 +185,64 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
+    const uint32_t smem0 = smem_u32(smem);
+
+    auto load_stage = [&](int stage, int kc) {
+        const uint32_t st = smem0 + stage * TC_STAGE_BYTES;
+        const int k0 = kc * TC_BK;
+#pragma unroll
+        for (int t = 0; t < TC_TERMS; t++) {
+            stage_row_async(st + t * TC_TILE_BYTES, tid, a.A[t] + a_off + k0, true);
+            stage_row_async(st + (TC_TERMS + t) * TC_TILE_BYTES, tid,
+                            bvalid ? a.B[t] + brow + k0 : a.B[t], bvalid);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
 
     bool ok = true;
     int issued = 0;  // chunks whose MMAs were committed
+    if (nk > 0) load_stage(0, 0);
     for (int kc = 0; kc < nk; kc++) {
         const int s = kc % TC_STAGES;
-        uint8_t* st = smem + s * TC_STAGE_BYTES;
-        if (kc >= TC_STAGES) {
-            // the stage is free once the MMAs of chunk kc - TC_STAGES completed;
-            // the decision is made CTA-wide so that no thread is left at a barrier
-            const bool w = mbar_wait(smem_u32(&mbar[s]), ((kc - TC_STAGES) / TC_STAGES) & 1);
-            ok = __syncthreads_and(w);
-            if (!ok) break;
+        if (kc + 1 < nk) {
+            const int ns = (kc + 1) % TC_STAGES;
+            if (kc + 1 >= TC_STAGES) {
+                // stage ns is free once the MMAs of chunk kc + 1 - TC_STAGES completed;
+                // decided CTA-wide so that no thread is left at a barrier
+                const int prev = kc + 1 - TC_STAGES;
+                const bool w = mbar_wait(smem_u32(&mbar[ns]), (prev / TC_STAGES) & 1);
+                ok = __syncthreads_and(w);
+                if (!ok) break;
+            }
+            load_stage(ns, kc + 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
-        const int k0 = kc * TC_BK;
-        stage_row(st, tid, reinterpret_cast<const uint4*>(Ahi + k0), true);
-        stage_row(st + TC_TILE_BYTES, tid, reinterpret_cast<const uint4*>(Alo + k0), true);
-        stage_row(st + 2 * TC_TILE_BYTES, tid, reinterpret_cast<const uint4*>(a.Bhi + brow + k0), bvalid);
-        stage_row(st + 3 * TC_TILE_BYTES, tid, reinterpret_cast<const uint4*>(a.Blo + brow + k0), bvalid);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t ah = smem_u32(st), al = ah + TC_TILE_BYTES;
-            const uint32_t bh = ah + 2 * TC_TILE_BYTES, bl = ah + 3 * TC_TILE_BYTES;
+            const uint32_t st = smem0 + s * TC_STAGE_BYTES;
 #pragma unroll
             for (int kk = 0; kk < TC_BK / 16; kk++) {
                 const uint32_t off = kk * 32;  // 16 bf16 along K inside the swizzle atom
-                mma_bf16(tmem, sw128_desc(ah + off), sw128_desc(bh + off), (kc | kk) != 0);
-                mma_bf16(tmem, sw128_desc(ah + off), sw128_desc(bl + off), 1);
-                mma_bf16(tmem, sw128_desc(al + off), sw128_desc(bh + off), 1);
+                const uint32_t a0 = st + off, a1 = a0 + TC_TILE_BYTES, a2 = a0 + 2 * TC_TILE_BYTES;
+                const uint32_t b0 = a0 + 3 * TC_TILE_BYTES, b1 = b0 + TC_TILE_BYTES,
+                               b2 = b0 + 2 * TC_TILE_BYTES;
+                mma_bf16(tmem, sw128_desc(a0), sw128_desc(b0), (kc | kk) != 0);
+                mma_bf16(tmem, sw128_desc(a0), sw128_desc(b1), 1);
+                mma_bf16(tmem, sw128_desc(a1), sw128_desc(b0), 1);
+                mma_bf16(tmem, sw128_desc(a0), sw128_desc(b2), 1);
+                mma_bf16(tmem, sw128_desc(a1), sw128_desc(b1), 1);
+                mma_bf16(tmem, sw128_desc(a2), sw128_desc(b0), 1);
             }
             mma_commit(smem_u32(&mbar[s]));
         }
         issued = kc + 1;
     }
+    // no copy may still be in flight when the kernel leaves
+    asm volatile("cp.async.wait_all;" ::: "memory");
     // the commit of the last issued chunk covers every MMA issued before it;
     // after a timeout this still drains what is in flight before TMEM is freed
     if (issued > 0) {
@@ -249,25 +276,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
 }
 
-// in [rows][n] FP32 -> hi/lo bf16 [rows][k_pad] (columns >= n zero)
+// v -> three bf16 terms t0 + t1 + t2 (each the rounding of what is left)
+__device__ __forceinline__ void split3(float v, __nv_bfloat16& t0, __nv_bfloat16& t1,
+                                       __nv_bfloat16& t2)
+{
+    t0 = __float2bfloat16_rn(v);
+    const float r1 = v - __bfloat162float(t0);
+    t1 = __float2bfloat16_rn(r1);
+    t2 = __float2bfloat16_rn(r1 - __bfloat162float(t1));
+}
+
+// in [rows][n] FP32 -> three bf16 planes [rows][k_pad] (columns >= n zero)
 __global__ void split_rows_kernel(const float* in, long rows, int n, int k_pad,
-                                  __nv_bfloat16* hi, __nv_bfloat16* lo)
+                                  __nv_bfloat16* o0, __nv_bfloat16* o1, __nv_bfloat16* o2)
 {
     const long total = rows * k_pad;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long)gridDim.x * blockDim.x) {
         const long r = t / k_pad;
         const int k = (int)(t % k_pad);
-        const float v = k < n ? in[r * n + k] : 0.f;
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        hi[t] = h;
-        lo[t] = __float2bfloat16_rn(v - __bfloat162float(h));
+        split3(k < n ? in[r * n + k] : 0.f, o0[t], o1[t], o2[t]);
     }
 }
 
-// operators [op][n][n] FP32 -> hi/lo [op][m_pad][k_pad] (zero padding)
+// operators [op][n][n] FP32 -> three bf16 planes [op][m_pad][k_pad] (zero padding)
 __global__ void split_ops_kernel(const float* in, long n_ops, int n, int m_pad, int k_pad,
-                                 __nv_bfloat16* hi, __nv_bfloat16* lo)
+                                 __nv_bfloat16* o0, __nv_bfloat16* o1, __nv_bfloat16* o2)
 {
     const long total = n_ops * m_pad * (long)k_pad;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
@@ -276,10 +310,7 @@ __global__ void split_ops_kernel(const float* in, long n_ops, int n, int m_pad, 
         const long rm = t / k_pad;
         const int m = (int)(rm % m_pad);
         const long op = rm / m_pad;
-        const float v = (m < n && k < n) ? in[(op * n + m) * (long)n + k] : 0.f;
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        hi[t] = h;
-        lo[t] = __float2bfloat16_rn(v - __bfloat162float(h));
+        split3((m < n && k < n) ? in[(op * n + m) * (long)n + k] : 0.f, o0[t], o1[t], o2[t]);
     }
 }
 
@@ -291,11 +322,10 @@ void TcPlanes::build(const float* ops32, long n_ops, int n, cudaStream_t s)
     m_pad = (n + TC_BM - 1) / TC_BM * TC_BM;
     k_pad = (n + TC_BK - 1) / TC_BK * TC_BK;
     const long total = n_ops * (long)m_pad * k_pad;
-    hi.alloc(std::max<long>(total, 1));
-    lo.alloc(std::max<long>(total, 1));
+    for (auto& p : a) p.alloc(std::max<long>(total, 1));
     if (total > 0) {
         split_ops_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
-            ops32, n_ops, n, m_pad, k_pad, hi.p, lo.p);
+            ops32, n_ops, n, m_pad, k_pad, a[0].p, a[1].p, a[2].p);
         TBEM_CK(cudaGetLastError());
     }
     err.alloc(1);
@@ -308,11 +338,10 @@ void TcPlanes::build(const float* ops32, long n_ops, int n, cudaStream_t s)
 void TcPlanes::split_b(const float* cells, long rows, cudaStream_t s)
 {
     const long total = rows * (long)k_pad;
-    bhi.ensure(std::max<long>(total, 1));
-    blo.ensure(std::max<long>(total, 1));
+    for (auto& p : b) p.ensure(std::max<long>(total, 1));
     if (total > 0) {
         split_rows_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
-            cells, rows, n, k_pad, bhi.p, blo.p);
+            cells, rows, n, k_pad, b[0].p, b[1].p, b[2].p);
         TBEM_CK(cudaGetLastError());
     }
 }
@@ -320,12 +349,12 @@ void TcPlanes::split_b(const float* cells, long rows, cudaStream_t s)
 void TcPlanes::split_b_rows(const float* cells, long row0, long rows, long rows_total,
                             cudaStream_t s)
 {
-    bhi.ensure(std::max<long>(rows_total * (long)k_pad, 1));
-    blo.ensure(std::max<long>(rows_total * (long)k_pad, 1));
+    for (auto& p : b) p.ensure(std::max<long>(rows_total * (long)k_pad, 1));
     const long total = rows * (long)k_pad;
     if (total > 0) {
         split_rows_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
-            cells + row0 * (long)n, rows, n, k_pad, bhi.p + row0 * k_pad, blo.p + row0 * k_pad);
+            cells + row0 * (long)n, rows, n, k_pad, b[0].p + row0 * k_pad, b[1].p + row0 * k_pad,
+            b[2].p + row0 * k_pad);
         TBEM_CK(cudaGetLastError());
     }
 }
@@ -355,8 +384,10 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, l
         it = tc_tiles.find(nrhs);
     }
     TcArgs a;
-    a.Ahi = P.hi.p;
-    a.Alo = P.lo.p;
+    for (int t = 0; t < TC_TERMS; t++) {
+        a.A[t] = P.a[t].p;
+        a.B[t] = P.b[t].p;
+    }
     a.a_op_stride = (long)P.m_pad * P.k_pad;
     a.k_pad = P.k_pad;
     a.g_op = d_op.p;
@@ -366,8 +397,6 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, l
     a.tile_col0 = it->second.second.p;
     a.in_cell = d_in.p;
     a.out_cell = d_out.p;
-    a.Bhi = P.bhi.p;
-    a.Blo = P.blo.p;
     a.D = D;
     a.n = n;
     a.nrhs = nrhs;

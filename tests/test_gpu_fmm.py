@@ -132,6 +132,10 @@ def test_mixed_tensor_core_m2l_matches_simt(name, order):
                               m2l_path=1)
     X = np.random.default_rng(22).uniform(-1, 1, (3, tc.n_cols()))
     assert rel(tc.apply(X), simt.apply(X)) < 2e-6
+    # M2M and L2L on the tensor cores as well (the default path)
+    full = ThreeD.FMMOperator(kernel_obj(name), locs, nrm, locs, nrm, w, cfg, precision="mixed",
+                              m2l_path=0)
+    assert rel(full.apply(X), simt.apply(X)) < 2e-6
 
 
 def test_multi_rhs_matches_single():
