@@ -208,6 +208,14 @@ int tbem_fmm_set_c2e(TbemFmm* h, int which, long level, const double* op)
     return guarded([&] { h->plan.set_c2e(which, level, op); });
 }
 
+long tbem_fmm_p2p_block(const TbemFmm* h) { return h ? h->plan.p2p_tpt : TBEM_ERR_ARG; }
+
+long tbem_fmm_tc_tile(const TbemFmm* h)
+{
+    if (!h) return TBEM_ERR_ARG;
+    return h->plan.f.use_tc ? h->plan.f.m2l.tc_bn : 0;
+}
+
 long tbem_fmm_last_launches(const TbemFmm* h) { return h ? h->plan.launches : TBEM_ERR_ARG; }
 
 int tbem_fmm_set_timing(TbemFmm* h, int enabled)

@@ -4,15 +4,24 @@
 namespace tbem {
 
 namespace {
+template <typename T, bool TR, bool TS, bool SS, int TPT>
+void go_tpt(int nr, int n_items, const EvalArgs<T>& a, cudaStream_t s)
+{
+    if (nr == 1)
+        eval_kernel<EVAL_KID, TR, T, 1, TS, SS, TPT><<<n_items, EVAL_THREADS, 0, s>>>(a);
+    else
+        eval_kernel<EVAL_KID, TR, T, EVAL_NR, TS, SS, TPT><<<n_items, EVAL_THREADS, 0, s>>>(a);
+}
+
 template <typename T, bool TR, bool TS, bool SS>
-cudaError_t go(int nr, int n_items, const void* args, cudaStream_t s)
+cudaError_t go(int nr, int n_items, int tpt, const void* args, cudaStream_t s)
 {
     const EvalArgs<T>& a = *static_cast<const EvalArgs<T>*>(args);
     if (n_items <= 0) return cudaSuccess;
-    if (nr == 1)
-        eval_kernel<EVAL_KID, TR, T, 1, TS, SS, 4><<<n_items, EVAL_THREADS, 0, s>>>(a);
-    else
-        eval_kernel<EVAL_KID, TR, T, EVAL_NR, TS, SS, 4><<<n_items, EVAL_THREADS, 0, s>>>(a);
+    // the point-to-point pass has autotuned variants; every other pass uses 4
+    if (!TR && !TS && !SS && tpt == 2) go_tpt<T, TR, TS, SS, 2>(nr, n_items, a, s);
+    else if (!TR && !TS && !SS && tpt == 8) go_tpt<T, TR, TS, SS, 8>(nr, n_items, a, s);
+    else go_tpt<T, TR, TS, SS, 4>(nr, n_items, a, s);
     return cudaGetLastError();
 }
 
@@ -23,14 +32,14 @@ cudaError_t go_t(const EvalLaunch& L, const void* args, cudaStream_t s)
     const int nr = (a.nrhs - a.rhs0) > 1 ? EVAL_NR : 1;
     const int idx = (L.trans ? 4 : 0) + (L.tgt_surf ? 2 : 0) + (L.src_surf ? 1 : 0);
     switch (idx) {
-    case 0: return go<T, false, false, false>(nr, L.n_items, args, s);
-    case 1: return go<T, false, false, true>(nr, L.n_items, args, s);
-    case 2: return go<T, false, true, false>(nr, L.n_items, args, s);
-    case 3: return go<T, false, true, true>(nr, L.n_items, args, s);
-    case 4: return go<T, true, false, false>(nr, L.n_items, args, s);
-    case 5: return go<T, true, false, true>(nr, L.n_items, args, s);
-    case 6: return go<T, true, true, false>(nr, L.n_items, args, s);
-    default: return go<T, true, true, true>(nr, L.n_items, args, s);
+    case 0: return go<T, false, false, false>(nr, L.n_items, L.tpt, args, s);
+    case 1: return go<T, false, false, true>(nr, L.n_items, 4, args, s);
+    case 2: return go<T, false, true, false>(nr, L.n_items, 4, args, s);
+    case 3: return go<T, false, true, true>(nr, L.n_items, 4, args, s);
+    case 4: return go<T, true, false, false>(nr, L.n_items, 4, args, s);
+    case 5: return go<T, true, false, true>(nr, L.n_items, 4, args, s);
+    case 6: return go<T, true, true, false>(nr, L.n_items, 4, args, s);
+    default: return go<T, true, true, true>(nr, L.n_items, 4, args, s);
     }
 }
 }  // namespace

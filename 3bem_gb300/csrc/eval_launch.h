@@ -11,6 +11,7 @@ struct EvalLaunch {
     bool tgt_surf;
     bool src_surf;
     int n_items;
+    int tpt = 4;  // threads per target (2, 4 or 8 for the point-to-point pass; 4 otherwise)
 };
 
 // One function per kernel id (eval_k<id>.cu) so that the instantiations

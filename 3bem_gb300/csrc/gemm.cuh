@@ -17,7 +17,9 @@ namespace tbem {
 
 constexpr int GM_BM = 64, GM_BN = 64, GM_BK = 16, GM_THREADS = 256;
 
-enum GemmMode { GEMM_STORE = 0, GEMM_ADD = 1, GEMM_ATOMIC = 2 };
+// GEMM_WAVES: deterministic accumulation -- the groups run in conflict-free
+// waves (no output written twice within a wave), each wave with GEMM_ADD.
+enum GemmMode { GEMM_STORE = 0, GEMM_ADD = 1, GEMM_ATOMIC = 2, GEMM_WAVES = 3 };
 
 template <typename T>
 struct GemmArgs {

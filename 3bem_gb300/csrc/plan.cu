@@ -108,25 +108,52 @@ void GemmSet::upload(const void* pool, size_t esz)
     tiles.clear();
 }
 
+// Greedy wave assignment: a group goes one wave after the latest wave that
+// already writes any of its output cells, so no wave writes a cell twice.
+void GemmSet::build_waves()
+{
+    int max_cell = 0;
+    for (int c : out_cell) max_cell = std::max(max_cell, c);
+    std::vector<int> last(max_cell + 1, -1);
+    wave_of.assign(npairs.size(), 0);
+    n_waves = 0;
+    for (size_t g = 0; g < npairs.size(); g++) {
+        int w = 0;
+        for (long p = pair0[g]; p < pair0[g] + npairs[g]; p++) w = std::max(w, last[out_cell[p]] + 1);
+        for (long p = pair0[g]; p < pair0[g] + npairs[g]; p++) last[out_cell[p]] = w;
+        wave_of[g] = w;
+        n_waves = std::max(n_waves, w + 1);
+    }
+}
+
 template <typename T>
 void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s,
                   long* launches)
 {
     if (empty()) return;
-    if (launches) (*launches)++;
+    const bool waves = mode == GEMM_WAVES;
+    if (waves && wave_of.empty()) build_waves();
     auto it = tiles.find(nrhs);
     if (it == tiles.end()) {
-        std::vector<int> tg, tc;
-        for (size_t g = 0; g < npairs.size(); g++) {
-            int ncols = npairs[g] * nrhs;
-            for (int c = 0; c < ncols; c += GM_BN) {
-                tg.push_back((int)g);
-                tc.push_back(c);
+        // tiles ordered by wave (a single wave when waves are not used)
+        std::vector<int> tg, tc, start;
+        const int nw = wave_of.empty() ? 1 : n_waves;
+        for (int w = 0; w < nw; w++) {
+            start.push_back((int)tg.size());
+            for (size_t g = 0; g < npairs.size(); g++) {
+                if (!wave_of.empty() && wave_of[g] != w) continue;
+                int ncols = npairs[g] * nrhs;
+                for (int c = 0; c < ncols; c += GM_BN) {
+                    tg.push_back((int)g);
+                    tc.push_back(c);
+                }
             }
         }
+        start.push_back((int)tg.size());
         auto& e = tiles[nrhs];
         e.first.upload(tg);
         e.second.upload(tc);
+        wave_tile_start[nrhs] = start;
         it = tiles.find(nrhs);
     }
     GemmArgs<T> a;
@@ -142,10 +169,20 @@ void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaSt
     a.n = n;
     a.nrhs = nrhs;
     a.trans = trans;
-    a.mode = mode;
-    dim3 grid((unsigned)it->second.first.n, (unsigned)((n + GM_BM - 1) / GM_BM));
-    grouped_gemm_kernel<T><<<grid, GM_THREADS, 0, s>>>(a);
-    TBEM_CK(cudaGetLastError());
+    a.mode = waves ? GEMM_ADD : mode;
+    const std::vector<int>& st = wave_tile_start[nrhs];
+    const int nw = (int)st.size() - 1;
+    if (!waves && nw != 1) throw Error(TBEM_ERR_STATE, "a wave-ordered GEMM set run without waves");
+    for (int w = 0; w < nw; w++) {
+        const int nt = st[w + 1] - st[w];
+        if (nt == 0) continue;
+        a.tile_group = it->second.first.p + st[w];
+        a.tile_col0 = it->second.second.p + st[w];
+        dim3 grid((unsigned)nt, (unsigned)((n + GM_BM - 1) / GM_BM));
+        grouped_gemm_kernel<T><<<grid, GM_THREADS, 0, s>>>(a);
+        TBEM_CK(cudaGetLastError());
+        if (launches) (*launches)++;
+    }
 }
 
 template void GemmSet::run<double>(const double*, double*, int, int, int, int, cudaStream_t, long*);
@@ -268,6 +305,18 @@ __global__ void scatter_kernel(const double* acc, const long* perm, const double
     }
 }
 
+// rows of length n -> rows of stride ld (the padding columns are zeroed)
+__global__ void convert_rows_kernel(const double* in, float* out, long rows, int n, int ld)
+{
+    const long total = rows * ld;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long)gridDim.x * blockDim.x) {
+        const long r = t / ld;
+        const int k = (int)(t % ld);
+        out[t] = k < n ? float(in[r * n + k]) : 0.f;
+    }
+}
+
 __global__ void add_kernel(const double* in, float* out, long n)
 {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -281,25 +330,38 @@ __global__ void promote_kernel(const float* in, double* out, long n)
 }
 
 // Precision-form L2P: y[r][d][pt0 + i] += sum_k E[row0 + i R + d][k] cd[leaf][r][k].
-// One CTA per leaf, one warp per output row.
-__global__ void l2p_mixed_kernel(const float* E, const long* row0, const int* leaf,
-                                 const long* pt0, const int* npts, const float* cd, int n, int R,
-                                 int nrhs, double* y, long y_n)
+// E rows are padded to ld (a multiple of 128 floats, zero beyond n): one CTA
+// per leaf stages the leaf's check potentials of one RHS in shared memory,
+// and each warp streams whole rows with float4 loads.  HBM-bound on E.
+constexpr int L2P_MAX_LD = 2048;
+__global__ void __launch_bounds__(256) l2p_mixed_kernel(const float* E, const long* row0,
+                                                        const int* leaf, const long* pt0,
+                                                        const int* npts, const float* cd, int n,
+                                                        int ld, int R, int nrhs, double* y, long y_n)
 {
+    __shared__ __align__(16) float c[L2P_MAX_LD];
     const int t = blockIdx.x;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
     const int rows = npts[t] * R;
     const float* c0 = cd + (long)leaf[t] * nrhs * n;
-    for (int row = warp; row < rows; row += nw) {
-        const float* e = E + (row0[t] + row) * (long)n;
-        const int i = row / R, d = row % R;
-        for (int r = 0; r < nrhs; r++) {
-            const float* c = c0 + (long)r * n;
+    for (int r = 0; r < nrhs; r++) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < ld; k += blockDim.x) c[k] = k < n ? c0[(long)r * n + k] : 0.f;
+        __syncthreads();
+        for (int row = warp; row < rows; row += nw) {
+            const float4* e = reinterpret_cast<const float4*>(E + (row0[t] + row) * (long)ld);
+            const float4* cv = reinterpret_cast<const float4*>(c);
             float acc = 0.f;
-            for (int k = lane; k < n; k += 32) acc += e[k] * c[k];
+            for (int k4 = lane; k4 < ld / 4; k4 += 32) {
+                const float4 a = __ldg(e + k4), b = cv[k4];
+                acc += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+            }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) y[((long)r * R + d) * y_n + pt0[t] + i] += (double)acc;
+            if (lane == 0) {
+                const int i = row / R, d = row % R;
+                y[((long)r * R + d) * y_n + pt0[t] + i] += (double)acc;
+            }
         }
     }
 }
@@ -307,7 +369,7 @@ __global__ void l2p_mixed_kernel(const float* E, const long* row0, const int* le
 // Its transpose: cd[leaf][r][k] = sum_rows E[row][k] z[r][d][pt0 + i].
 __global__ void l2p_mixed_t_kernel(const float* E, const long* row0, const int* leaf,
                                    const long* pt0, const int* npts, const float* z, long z_n,
-                                   int n, int R, int nrhs, float* cd)
+                                   int n, int ld, int R, int nrhs, float* cd)
 {
     const int t = blockIdx.x;
     const int rows = npts[t] * R;
@@ -316,7 +378,7 @@ __global__ void l2p_mixed_t_kernel(const float* E, const long* row0, const int* 
             float acc = 0.f;
             for (int row = 0; row < rows; row++) {
                 const int i = row / R, d = row % R;
-                acc += E[(row0[t] + row) * (long)n + k] * z[((long)r * R + d) * z_n + pt0[t] + i];
+                acc += E[(row0[t] + row) * (long)ld + k] * z[((long)r * R + d) * z_n + pt0[t] + i];
             }
             cd[((long)leaf[t] * nrhs + r) * n + k] = acc;
         }
@@ -440,6 +502,90 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     build_tasks();
     build_form();
     TBEM_CK(cudaStreamSynchronize(stream));
+    if (opt.p2p_block == 2 || opt.p2p_block == 4 || opt.p2p_block == 8) p2p_tpt = opt.p2p_block;
+    else autotune_p2p();
+    autotune_tc();
+}
+
+// Picks the tensor-core GEMM's N tile for the M2L set (and uses it for the
+// level translations too) by timing both shapes on this operator's own pair
+// lists with zero operands (the cost does not depend on the values).
+void Plan::autotune_tc()
+{
+    if (!f.use_tc || f.m2l.empty()) return;
+    ensure_rhs(1);
+    const long ncs = (long)stree->cells.size(), nco = (long)otree.cells.size();
+    TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * n, stream));
+    f.tc.split_b_rows(cu32.p, 0, ncs, std::max(ncs, nco), stream);
+    cudaEvent_t e0, e1;
+    TBEM_CK(cudaEventCreate(&e0));
+    TBEM_CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_bn = 128;
+    for (int bn : {128, 64}) {
+        f.m2l.tc_bn = bn;
+        float ms = 0.f;
+        for (int rep = 0; rep < 3; rep++) {
+            TBEM_CK(cudaEventRecord(e0, stream));
+            f.m2l.run_tc(f.tc, cd32.p, n, 1, 1, (long)n * n, stream, nullptr);
+            TBEM_CK(cudaEventRecord(e1, stream));
+            TBEM_CK(cudaEventSynchronize(e1));
+            float t = 0.f;
+            TBEM_CK(cudaEventElapsedTime(&t, e0, e1));
+            if (rep > 0) ms += t;
+        }
+        if (ms < best) {
+            best = ms;
+            best_bn = bn;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    f.m2l.tc_bn = best_bn;
+    for (auto& g : f.m2m) g.tc_bn = best_bn;
+    for (auto& g : f.l2l) g.tc_bn = best_bn;
+}
+
+// Picks the point-to-point pass's threads per target (2, 4 or 8) by timing
+// each variant on this operator's own task lists (zero densities: the cost
+// does not depend on the values).
+void Plan::autotune_p2p()
+{
+    if (p2p.n_items() == 0) return;
+    ensure_rhs(1);
+    const bool mixed = f.mixed;
+    if (mixed) TBEM_CK(cudaMemsetAsync(s32.p, 0, sizeof(float) * R * n_src, stream));
+    else TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * n_src, stream));
+    cudaEvent_t e0, e1;
+    TBEM_CK(cudaEventCreate(&e0));
+    TBEM_CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_tpt = 4;
+    for (int tpt : {4, 2, 8}) {
+        p2p_tpt = tpt;
+        float ms = 0.f;
+        for (int rep = 0; rep < 3; rep++) {
+            TBEM_CK(cudaEventRecord(e0, stream));
+            if (mixed)
+                eval<float>(p2p_set(), kid, false, false, otree, dobs, 0, *dsrc, 0, s32.p, n_src,
+                            nullptr, y64.p, n_obs, nullptr, 1, 1, stream, false);
+            else
+                eval<double>(p2p_set(), kid, false, false, otree, dobs, 0, *dsrc, 0, s64.p, n_src,
+                             nullptr, y64.p, n_obs, nullptr, 1, 1, stream, false);
+            TBEM_CK(cudaEventRecord(e1, stream));
+            TBEM_CK(cudaEventSynchronize(e1));
+            float t = 0.f;
+            TBEM_CK(cudaEventElapsedTime(&t, e0, e1));
+            if (rep > 0) ms += t;  // the first run warms the caches
+        }
+        if (ms < best) {
+            best = ms;
+            best_tpt = tpt;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p2p_tpt = best_tpt;
 }
 
 void Plan::build_tasks()
@@ -471,6 +617,8 @@ void Plan::build_tasks()
             for (int s : m2p_of[a]) mp.push_back({s, ns});
         }
         p2p.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, TPB);
+        p2p_tpt2.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, EVAL_THREADS / 2);
+        p2p_tpt8.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, EVAL_THREADS / 8);
         m2p.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, mp, TPB);
     }
     for (size_t c = 0; c < O.cells.size(); c++) {
@@ -513,8 +661,10 @@ void Plan::build_tasks()
         const Cell& cc = O.cells[c];
         l2p_t.add(c, ns, cc.center, {{cc.pt_begin, (int)cc.n_points()}}, TPB);
     }
-    for (TaskSet* t : {&p2m, &p2p, &m2p, &p2l, &l2p, &m2l_fly, &p2m_t, &p2p_t, &m2p_t, &p2l_t,
-                       &l2p_t, &m2l_fly_t})
+    p2p_tpt2.tpt = 2;
+    p2p_tpt8.tpt = 8;
+    for (TaskSet* t : {&p2m, &p2p, &p2p_tpt2, &p2p_tpt8, &m2p, &p2l, &l2p, &m2l_fly, &p2m_t, &p2p_t,
+                       &m2p_t, &p2l_t, &l2p_t, &m2l_fly_t})
         t->upload();
 
     // dedup keys of the M2M / L2L octant translations and the M2L translations
@@ -710,19 +860,51 @@ void translation_jobs(const Plan& P, const Form& F, std::vector<SurfJob>& jobs,
         total += nn;
         return J.out_off;
     };
+    // In the precision form the combined operators (kernel matrix times the
+    // pseudo-inverse) do not depend on the level: every kernel here is
+    // homogeneous, the surfaces of level l + 1 are those of level l scaled by
+    // exactly 1/2 (cells halve, cpp/geometry.cpp:20-28), and the thresholded
+    // pseudo-inverse of lambda A is pinv(A) / lambda.  Below the root (whose
+    // box is the expanded one) one representative per octant / per (level
+    // difference, offset) serves every level.
+    const bool merge = F.mixed;
     m2m_off.assign(P.m2m_canon.size(), -1);
+    std::map<int, long> m2m_rep;
     for (size_t k = 0; k < P.m2m_canon.size(); k++) {
         if (P.m2m_canon[k].first < 0) continue;  // (parent, child): up-check(parent) <- up-equiv(child)
+        const int lev = (int)k / 8, oct = (int)k % 8;
+        if (merge && lev >= 1 && m2m_rep.count(oct)) { m2m_off[k] = m2m_rep[oct]; continue; }
         m2m_off[k] = add(S.cells[P.m2m_canon[k].first], F.r_uc, S.cells[P.m2m_canon[k].second], F.r_ue);
+        if (merge && lev >= 1) m2m_rep[oct] = m2m_off[k];
     }
     l2l_off.assign(P.l2l_canon.size(), -1);
+    std::map<int, long> l2l_rep;
     for (size_t k = 0; k < P.l2l_canon.size(); k++) {
         if (P.l2l_canon[k].first < 0) continue;  // (parent, child): down-check(child) <- down-equiv(parent)
+        const int lev = (int)k / 8, oct = (int)k % 8;
+        if (merge && lev >= 1 && l2l_rep.count(oct)) { l2l_off[k] = l2l_rep[oct]; continue; }
         l2l_off[k] = add(O.cells[P.l2l_canon[k].second], F.r_dc, O.cells[P.l2l_canon[k].first], F.r_de);
+        if (merge && lev >= 1) l2l_rep[oct] = l2l_off[k];
     }
     m2l_off.assign(P.m2l_canon.size(), -1);
-    for (size_t k = 0; k < P.m2l_canon.size(); k++)  // down-check(obs) <- up-equiv(src)
-        m2l_off[k] = add(O.cells[P.m2l_canon[k].first], F.r_dc, S.cells[P.m2l_canon[k].second], F.r_ue);
+    std::map<std::tuple<int, long, long, long>, long> m2l_rep;
+    for (size_t k = 0; k < P.m2l_canon.size(); k++) {  // down-check(obs) <- up-equiv(src)
+        const Cell& o = O.cells[P.m2l_canon[k].first];
+        const Cell& sc = S.cells[P.m2l_canon[k].second];
+        std::tuple<int, long, long, long> key;
+        const bool mergeable = merge && o.level >= 1 && sc.level >= 1;
+        if (mergeable) {
+            const double* hf = o.level >= sc.level ? o.hw : sc.hw;
+            long off[3];
+            for (int d = 0; d < 3; d++)
+                off[d] = hf[d] == 0.0 ? 0 : (long)std::nearbyint((sc.center[d] - o.center[d]) / hf[d]);
+            key = std::make_tuple(o.level - sc.level, off[0], off[1], off[2]);
+            auto it = m2l_rep.find(key);
+            if (it != m2l_rep.end()) { m2l_off[k] = it->second; continue; }
+        }
+        m2l_off[k] = add(o, F.r_dc, sc, F.r_ue);
+        if (mergeable) m2l_rep[key] = m2l_off[k];
+    }
 }
 
 }  // namespace
@@ -762,11 +944,18 @@ void Plan::build_gemm_sets(Form& F, long, long, long, const std::vector<long>& m
         }
     F.m2l = GemmSet();
     F.m2l_t = GemmSet();
+    // keys that share an operator form one group (an observation cell still
+    // appears at most once per group: its level and offset fix the key)
+    std::map<long, std::vector<std::pair<int, int>>> by_op;
+    std::vector<long> op_order;
     for (size_t k = 0; k < m2l_groups.size(); k++) {
-        std::vector<std::pair<int, int>> pr;
+        auto& pr = by_op[m2l_off[k]];
+        if (pr.empty()) op_order.push_back(m2l_off[k]);
         for (int pi : m2l_groups[k]) pr.push_back({L.m2l[pi].src, L.m2l[pi].obs});
-        F.m2l.add_group(m2l_off[k], pr);
-        F.m2l_t.add_group(m2l_off[k], swap_pairs(pr));
+    }
+    for (long off : op_order) {
+        F.m2l.add_group(off, by_op[off]);
+        F.m2l_t.add_group(off, swap_pairs(by_op[off]));
     }
     const void* pool = F.mixed ? (const void*)F.ops32.p : (const void*)F.ops64.p;
     const size_t esz = F.mixed ? sizeof(float) : sizeof(double);
@@ -840,12 +1029,17 @@ void Plan::build_mixed_ops(Form& F)
     {
         const Tree& S = *stree;
         const Tree& O = otree;
+        // the pseudo-inverse of the level the operator's job was built at (the
+        // first key that uses a job is the one that created it)
         for (size_t k = 0; k < m2m_off.size(); k++)
-            if (m2m_off[k] >= 0) c2e_of[m2m_off[k] / nn] = F.c2e_up_off[S.cells[m2m_canon[k].second].level];
+            if (m2m_off[k] >= 0 && c2e_of[m2m_off[k] / nn] < 0)
+                c2e_of[m2m_off[k] / nn] = F.c2e_up_off[S.cells[m2m_canon[k].second].level];
         for (size_t k = 0; k < l2l_off.size(); k++)
-            if (l2l_off[k] >= 0) c2e_of[l2l_off[k] / nn] = F.c2e_dn_off[O.cells[l2l_canon[k].first].level];
+            if (l2l_off[k] >= 0 && c2e_of[l2l_off[k] / nn] < 0)
+                c2e_of[l2l_off[k] / nn] = F.c2e_dn_off[O.cells[l2l_canon[k].first].level];
         for (size_t k = 0; k < m2l_off.size(); k++)
-            c2e_of[m2l_off[k] / nn] = F.c2e_up_off[S.cells[m2l_canon[k].second].level];
+            if (c2e_of[m2l_off[k] / nn] < 0)
+                c2e_of[m2l_off[k] / nn] = F.c2e_up_off[S.cells[m2l_canon[k].second].level];
     }
     if (!jobs.empty()) {
         // in chunks to bound the FP64 scratch
@@ -903,7 +1097,9 @@ void Plan::build_mixed_ops(Form& F)
         rows += cc.n_points() * R;
     }
     F.n_l2p = (int)cell.size();
-    F.E.alloc(std::max<long>(rows * n, 1));
+    F.E_ld = (n + 127) / 128 * 128;
+    if (F.E_ld > 2048) throw Error(TBEM_ERR_ARG, "translation surface too large for the L2P kernel");
+    F.E.alloc(std::max<long>(rows * F.E_ld, 1));
     F.E_row0.upload(row0);
     F.E_pt0.upload(pt0);
     F.E_leaf.upload(cell);
@@ -934,7 +1130,8 @@ void Plan::build_mixed_ops(Form& F)
             TBEM_CK(cudaGetLastError());
             TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)r, n, &one,
                                  F.c2e.p + F.c2e_dn_off[lev], n, K.p, n, &zero, Y.p, n));
-            convert_kernel<float><<<grid_for(r * n), 256, 0, stream>>>(Y.p, F.E.p + row0[t0] * n, r * n);
+            convert_rows_kernel<<<grid_for(r * F.E_ld), 256, 0, stream>>>(Y.p, F.E.p + row0[t0] * F.E_ld,
+                                                                         r, n, F.E_ld);
             TBEM_CK(cudaGetLastError());
             TBEM_CK(cudaStreamSynchronize(stream));
             t0 = t1;
@@ -1033,6 +1230,7 @@ void Plan::eval(const TaskSet& ts, int ekid, bool tgt_surf, bool src_surf, const
     a.c2 = T(ep.c2);
     a.scale = ep.scale;
     EvalLaunch Lc{ekid, trans, tgt_surf, src_surf, ts.n_items()};
+    Lc.tpt = ts.tpt;
     for (int r0 = 0; r0 < nrhs; r0 += (nrhs - r0 > 1 ? EVAL_NR : 1)) {
         a.rhs0 = r0;
         TBEM_CK(launch_eval<T>(Lc, a, s));
@@ -1059,11 +1257,11 @@ void Plan::forward(int nrhs, cudaStream_t s)
         eval<double>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cu64.p, 0, nrhs, s, false);
         mark("p2m", s);
         for (int l = S.n_levels() - 1; l >= 0; l--) {
-            if (l < (int)F.m2m.size()) F.m2m[l].run<double>(qu64.p, cu64.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
+            if (l < (int)F.m2m.size()) F.m2m[l].run<double>(qu64.p, cu64.p, n, nrhs, 0, GEMM_WAVES, s, &launches);
             F.c2e_up[l].run<double>(cu64.p, qu64.p, n, nrhs, 0, GEMM_STORE, s, &launches);
         }
         mark("m2m+c2e_up", s);
-        eval<double>(p2p, kid, false, false, O, dobs, 0, *dsrc, 0, s64.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
+        eval<double>(p2p_set(), kid, false, false, O, dobs, 0, *dsrc, 0, s64.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
         mark("p2p", s);
         eval<double>(m2p, F.kt_kid, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
         eval<double>(p2l, F.ks_kid, true, false, O, dobs, F.r_dc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cd64.p, 1, nrhs, s, false);
@@ -1071,7 +1269,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
         if (F.m2l_on_the_fly)
             eval<double>(m2l_fly, F.g_kid, true, true, O, dobs, F.r_dc, *dsrc, F.r_ue, nullptr, 0, qu64.p, nullptr, 0, cd64.p, 1, nrhs, s, false);
         else
-            F.m2l.run<double>(qu64.p, cd64.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
+            F.m2l.run<double>(qu64.p, cd64.p, n, nrhs, 0, GEMM_WAVES, s, &launches);
         mark("m2l", s);
         for (int l = 0; l < O.n_levels(); l++) {
             if (l > 0 && l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<double>(qd64.p, cd64.p, n, nrhs, 0, GEMM_ADD, s, &launches);
@@ -1103,7 +1301,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
             }
         }
         mark("m2m", s);
-        eval<float>(p2p, kid, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
+        eval<float>(p2p_set(), kid, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
         mark("p2p", s);
         const bool need64 = !L.m2p.empty() || F.m2l_on_the_fly;
         if (need64) {
@@ -1145,7 +1343,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
         }
         mark("l2l", s);
         if (F.n_l2p > 0) {
-            l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cd32.p, n, R, nrhs, y64.p, NO);
+            l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cd32.p, n, F.E_ld, R, nrhs, y64.p, NO);
             TBEM_CK(cudaGetLastError());
             launches++;
         }
@@ -1181,12 +1379,12 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
         // down pass reversed: deepest level first
         for (int l = O.n_levels() - 1; l >= 0; l--) {
             F.c2e_dn_t[l].run<double>(qd64.p, cd64.p, n, nrhs, 1, GEMM_STORE, s, &launches);
-            if (l > 0 && l - 1 < (int)F.l2l_t.size()) F.l2l_t[l - 1].run<double>(cd64.p, qd64.p, n, nrhs, 1, GEMM_ATOMIC, s, &launches);
+            if (l > 0 && l - 1 < (int)F.l2l_t.size()) F.l2l_t[l - 1].run<double>(cd64.p, qd64.p, n, nrhs, 1, GEMM_WAVES, s, &launches);
         }
         if (F.m2l_on_the_fly)
             eval<double>(m2l_fly_t, F.g_kid, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
         else
-            F.m2l_t.run<double>(cd64.p, qu64.p, n, nrhs, 1, GEMM_ATOMIC, s, &launches);
+            F.m2l_t.run<double>(cd64.p, qu64.p, n, nrhs, 1, GEMM_WAVES, s, &launches);
         eval<double>(p2l_t, F.ks_kid, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
         // up pass reversed: root first
         for (int l = 0; l < S.n_levels(); l++) {
@@ -1201,7 +1399,7 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
         TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
         TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
         if (F.n_l2p > 0) {
-            l2p_mixed_t_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, s32.p, NO, n, R, nrhs, cd32.p);
+            l2p_mixed_t_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, s32.p, NO, n, F.E_ld, R, nrhs, cd32.p);
             TBEM_CK(cudaGetLastError());
             launches++;
         }

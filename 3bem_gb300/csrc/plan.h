@@ -100,6 +100,7 @@ struct TaskSet {
     DBuf<int> d_tgt_count, d_src_ptr, d_blk_count, d_blk_prefix, d_item_task, d_item_start;
     DBuf<double> d_origin;
     long n_pairs = 0;  // sum over tasks of targets x sources (work estimate)
+    int tpt = 4;       // threads per target the items were cut for
 
     int n_tasks() const { return (int)tgt.size(); }
     int n_items() const { return (int)item_task.size(); }
@@ -144,6 +145,11 @@ struct GemmSet {
     DBuf<int> d_npairs, d_in, d_out;
     DBuf<const void*> d_A;  // resolved pointers
     std::map<int, std::pair<DBuf<int>, DBuf<int>>> tiles;  // per nrhs
+    // conflict-free waves for GEMM_WAVES (built on first use)
+    std::vector<int> wave_of;
+    int n_waves = 0;
+    std::map<int, std::vector<int>> wave_tile_start;  // per nrhs: first tile of every wave
+    void build_waves();
     long total_pairs() const { return (long)in_cell.size(); }
     bool empty() const { return in_cell.empty(); }
     void add_group(long a_off, const std::vector<std::pair<int, int>>& pairs);
@@ -154,6 +160,7 @@ struct GemmSet {
     // tensor-core path (B taken from P's split planes); nn = elements per operator
     DBuf<int> d_op;
     std::map<int, std::pair<DBuf<int>, DBuf<int>>> tc_tiles;
+    int tc_bn = 128;  // N tile of the tensor-core path (128 or 64; autotuned)
     void run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, long nn, cudaStream_t s,
                 long* launches);
 };
@@ -194,6 +201,7 @@ struct Form {
     DBuf<int> E_leaf, E_npts;
     DBuf<long> E_pt0;
     int n_l2p = 0;
+    int E_ld = 0;  // padded row stride of E (multiple of 128 floats)
 };
 
 struct Plan {
@@ -215,6 +223,12 @@ struct Plan {
     Form f;
     // evaluation task sets (forward); adjoint sets swap roles
     TaskSet p2m, p2p, m2p, p2l, l2p, m2l_fly;
+    // point-to-point variants for 2 and 8 threads per target (autotuned)
+    TaskSet p2p_tpt2, p2p_tpt8;
+    int p2p_tpt = 4;
+    void autotune_p2p();
+    void autotune_tc();  // N tile (128 / 64) of the tensor-core translations
+    const TaskSet& p2p_set() const { return p2p_tpt == 2 ? p2p_tpt2 : p2p_tpt == 8 ? p2p_tpt8 : p2p; }
     TaskSet p2m_t, p2p_t, m2p_t, p2l_t, l2p_t, m2l_fly_t;
     // work buffers
     int cap_rhs = 0;

@@ -4,11 +4,15 @@
 // Every FP32 operand is split into three bf16 terms, a = a0 + a1 + a2 (each
 // term holds the next 8 significant bits), and the product is accumulated
 // from the six bf16 MMAs that reach 2^-24 relative size (a0b0, a0b1, a1b0,
-// a0b2, a1b1, a2b0) in an FP32 accumulator in tensor memory: FP32-level
-// accuracy on the bf16 tensor pipe.  The operators' planes are built once at
+// a0b2, a1b1, a2b0) in FP32 accumulators in tensor memory: FP32-level
+// accuracy on the bf16 tensor pipe.  The dominant product a0b0 and the five
+// small ones go to two separate accumulators that are added in the epilogue,
+// so the small terms are never rounded against the large running sum (the
+// error of accumulating them into one accumulator grew with the number of
+// MMAs).  The operators' planes are built once at
 // setup; the check potentials (B) are split before every use.
 //
-// CTA: 128 threads, one 128 x 128 accumulator (128 TMEM columns).  K runs in
+// CTA: 128 threads, two 128 x BN accumulators (2 BN TMEM columns).  K runs in
 // chunks of 64 bf16 (128-byte rows) through a 2-stage shared-memory ring of
 // six 128B-swizzled K-major planes per stage.  All threads stage a chunk with
 // cp.async (A rows from the operator planes, B rows gathered by pair; 48
@@ -24,12 +28,25 @@
 
 namespace tbem {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 2, TC_THREADS = 128;
+constexpr int TC_BM = 128, TC_BK = 64, TC_THREADS = 128;
 constexpr int TC_TERMS = 3;                                  // bf16 terms per operand
-constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;            // 16 KB: one 128 x 64 bf16 plane tile
-constexpr int TC_STAGE_BYTES = 2 * TC_TERMS * TC_TILE_BYTES; // A0..A2, B0..B2
-constexpr int TC_SMEM_BYTES = TC_STAGES * TC_STAGE_BYTES + 1024;
+constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;            // 16 KB: one 128 x 64 bf16 A plane tile
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
+
+// Tile shapes (the autotuner picks one per operator set): N = 128 columns
+// with a 2-stage ring, or N = 64 columns with a 3-stage ring.
+template <int BN>
+struct TcShape {
+    static constexpr int STAGES = BN == 128 ? 2 : 3;
+    static constexpr int B_TILE = BN * TC_BK * 2;                         // one B plane tile
+    static constexpr int STAGE_BYTES = TC_TERMS * (TC_TILE_BYTES + B_TILE);
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+    // kind::f16, bf16 A/B, FP32 D, K-major A and B, M = 128, N = BN
+    static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
+                                      ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+};
+static_assert(TcShape<128>::SMEM_BYTES <= 227 * 1024 && TcShape<64>::SMEM_BYTES <= 227 * 1024,
+              "shared memory budget");
 
 struct TcArgs {
     const __nv_bfloat16* A[TC_TERMS];  // [op][m_pad][k_pad] per term
@@ -70,16 +87,13 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
     return d;
 }
 
-// Instruction descriptor: kind::f16 with bf16 A/B, FP32 D, both K-major, M = N = 128.
-constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
-                              ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accum)
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accum)
 {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-        "l"(a), "l"(b), "r"(TC_IDESC), "r"(accum));
+        "l"(a), "l"(b), "r"(idesc), "r"(accum));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar)
@@ -129,14 +143,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// cp.async of one 128-byte row (8 x 16 bytes) into its swizzled place; a
-// row that is not valid is zero-filled (source size 0, nothing is read).
-__device__ __forceinline__ void stage_row_async(uint32_t tile, int row, const __nv_bfloat16* src,
-                                                bool valid)
+// cp.async of 16-byte pieces [j0, j0 + NJ) of one 128-byte row into their
+// swizzled places; a row that is not valid is zero-filled (source size 0,
+// nothing is read).
+template <int NJ>
+__device__ __forceinline__ void stage_row_async(uint32_t tile, int row, int j0,
+                                                const __nv_bfloat16* src, bool valid)
 {
     const uint32_t n = valid ? 16u : 0u;
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
+    for (int jj = 0; jj < NJ; jj++) {
+        const int j = j0 + jj;
         const uint32_t dst = tile + row * 128 + ((j ^ (row & 7)) << 4);
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst),
                      "l"(src + j * 8), "r"(n)
@@ -144,8 +161,14 @@ __device__ __forceinline__ void stage_row_async(uint32_t tile, int row, const __
     }
 }
 
+template <int BN>
 __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
 {
+    using Sh = TcShape<BN>;
+    constexpr int TC_STAGES = Sh::STAGES;
+    constexpr int TC_STAGE_BYTES = Sh::STAGE_BYTES;
+    constexpr int B_BASE = TC_TERMS * TC_TILE_BYTES;  // B planes follow the A planes
+    constexpr int BJ = 8 * BN / TC_THREADS;           // 16-byte pieces of B per thread
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t mbar[TC_STAGES];
     __shared__ uint32_t tmem_slot;
@@ -161,8 +184,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     const int ncols = a.g_npairs[g] * a.nrhs;
     const int nk = a.k_pad / TC_BK;
     const long a_off = (long)a.g_op[g] * a.a_op_stride + (long)(m0 + tid) * a.k_pad;
-    // B row of this thread: one gathered (cell, rhs) column
-    const int c = col0 + tid;
+    // B row of this thread: one gathered (cell, rhs) column (with BN = 64 two
+    // threads share a row, four 16-byte pieces each)
+    const int brow_i = tid % BN;
+    const int bj0 = (tid / BN) * BJ;
+    const int c = col0 + brow_i;
     const bool bvalid = c < ncols;
     long brow = 0;
     if (bvalid) {
@@ -173,7 +199,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&tmem_slot)),
-                     "r"(TC_BN));
+                     "r"(2 * BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
@@ -192,9 +218,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
         const int k0 = kc * TC_BK;
 #pragma unroll
         for (int t = 0; t < TC_TERMS; t++) {
-            stage_row_async(st + t * TC_TILE_BYTES, tid, a.A[t] + a_off + k0, true);
-            stage_row_async(st + (TC_TERMS + t) * TC_TILE_BYTES, tid,
-                            bvalid ? a.B[t] + brow + k0 : a.B[t], bvalid);
+            stage_row_async<8>(st + t * TC_TILE_BYTES, tid, 0, a.A[t] + a_off + k0, true);
+            stage_row_async<BJ>(st + B_BASE + t * Sh::B_TILE, brow_i, bj0,
+                                bvalid ? a.B[t] + brow + k0 : a.B[t], bvalid);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -228,14 +254,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
             for (int kk = 0; kk < TC_BK / 16; kk++) {
                 const uint32_t off = kk * 32;  // 16 bf16 along K inside the swizzle atom
                 const uint32_t a0 = st + off, a1 = a0 + TC_TILE_BYTES, a2 = a0 + 2 * TC_TILE_BYTES;
-                const uint32_t b0 = a0 + 3 * TC_TILE_BYTES, b1 = b0 + TC_TILE_BYTES,
-                               b2 = b0 + 2 * TC_TILE_BYTES;
-                mma_bf16(tmem, sw128_desc(a0), sw128_desc(b0), (kc | kk) != 0);
-                mma_bf16(tmem, sw128_desc(a0), sw128_desc(b1), 1);
-                mma_bf16(tmem, sw128_desc(a1), sw128_desc(b0), 1);
-                mma_bf16(tmem, sw128_desc(a0), sw128_desc(b2), 1);
-                mma_bf16(tmem, sw128_desc(a1), sw128_desc(b1), 1);
-                mma_bf16(tmem, sw128_desc(a2), sw128_desc(b0), 1);
+                const uint32_t b0 = st + B_BASE + off, b1 = b0 + Sh::B_TILE, b2 = b0 + 2 * Sh::B_TILE;
+                constexpr uint32_t ID = Sh::IDESC;
+                const uint32_t first = (kc | kk) != 0;
+                const uint32_t small = tmem + BN;  // second accumulator
+                mma_bf16(tmem, sw128_desc(a0), sw128_desc(b0), ID, first);
+                mma_bf16(small, sw128_desc(a0), sw128_desc(b1), ID, first);
+                mma_bf16(small, sw128_desc(a1), sw128_desc(b0), ID, 1);
+                mma_bf16(small, sw128_desc(a0), sw128_desc(b2), ID, 1);
+                mma_bf16(small, sw128_desc(a1), sw128_desc(b1), ID, 1);
+                mma_bf16(small, sw128_desc(a2), sw128_desc(b0), ID, 1);
             }
             mma_commit(smem_u32(&mbar[s]));
         }
@@ -255,9 +283,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     } else {
         const int row = m0 + warp * 32 + (tid % 32);
 #pragma unroll 1
-        for (int cc = 0; cc < TC_BN / 32; cc++) {
-            float v[32];
+        for (int cc = 0; cc < BN / 32; cc++) {
+            float v[32], w[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cc * 32, v);
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + BN + cc * 32, w);
+#pragma unroll
+            for (int j = 0; j < 32; j++) v[j] += w[j];
             if (row >= a.n) continue;
 #pragma unroll 4
             for (int j = 0; j < 32; j++) {
@@ -273,7 +304,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
 }
 
 // v -> three bf16 terms t0 + t1 + t2 (each the rounding of what is left)
@@ -331,8 +362,10 @@ void TcPlanes::build(const float* ops32, long n_ops, int n, cudaStream_t s)
     err.alloc(1);
     TBEM_CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
     // per device: set on every build (the plan's device is current)
-    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 TC_SMEM_BYTES));
+    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TcShape<128>::SMEM_BYTES));
+    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TcShape<64>::SMEM_BYTES));
 }
 
 void TcPlanes::split_b(const float* cells, long rows, cudaStream_t s)
@@ -368,20 +401,22 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, l
         for (size_t g = 0; g < A_off.size(); g++) op[g] = (int)(A_off[g] / nn);
         d_op.upload(op);
     }
-    auto it = tc_tiles.find(nrhs);
+    const int bn = tc_bn == 64 ? 64 : 128;
+    const int key = nrhs * 1024 + bn;
+    auto it = tc_tiles.find(key);
     if (it == tc_tiles.end()) {
         std::vector<int> tg, tc;
         for (size_t g = 0; g < npairs.size(); g++) {
             const int ncols = npairs[g] * nrhs;
-            for (int c = 0; c < ncols; c += TC_BN) {
+            for (int c = 0; c < ncols; c += bn) {
                 tg.push_back((int)g);
                 tc.push_back(c);
             }
         }
-        auto& e = tc_tiles[nrhs];
+        auto& e = tc_tiles[key];
         e.first.upload(tg);
         e.second.upload(tc);
-        it = tc_tiles.find(nrhs);
+        it = tc_tiles.find(key);
     }
     TcArgs a;
     for (int t = 0; t < TC_TERMS; t++) {
@@ -403,7 +438,8 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, l
     a.atomic = atomic;
     a.err = P.err.p;
     dim3 grid((unsigned)it->second.first.n, (unsigned)(P.m_pad / TC_BM));
-    tc_gemm_kernel<<<grid, TC_THREADS, TC_SMEM_BYTES, s>>>(a);
+    if (bn == 64) tc_gemm_kernel<64><<<grid, TC_THREADS, TcShape<64>::SMEM_BYTES, s>>>(a);
+    else tc_gemm_kernel<128><<<grid, TC_THREADS, TcShape<128>::SMEM_BYTES, s>>>(a);
     TBEM_CK(cudaGetLastError());
     if (launches) (*launches)++;
 }

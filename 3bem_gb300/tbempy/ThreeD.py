@@ -276,6 +276,14 @@ class FMMOperator(OperatorI):
     def set_timing(self, enabled=True):
         check(_L.lib().tbem_fmm_set_timing(self._h, int(bool(enabled))))
 
+    def p2p_block(self):
+        """Threads per target of the point-to-point pass (autotuned)."""
+        return check(_L.lib().tbem_fmm_p2p_block(self._h))
+
+    def tc_tile(self):
+        """N tile of the tensor-core translations (autotuned; 0 if unused)."""
+        return check(_L.lib().tbem_fmm_tc_tile(self._h))
+
     def last_launches(self):
         """Kernel launches made by the last apply."""
         return check(_L.lib().tbem_fmm_last_launches(self._h))

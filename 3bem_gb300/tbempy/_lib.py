@@ -55,6 +55,8 @@ SIGNATURES = {
     "tbem_fmm_set_timing": (_I, [_P, _I]),
     "tbem_fmm_phase_times": (_I, [_P, _P, _P, _I]),
     "tbem_fmm_last_launches": (_L, [_P]),
+    "tbem_fmm_p2p_block": (_L, [_P]),
+    "tbem_fmm_tc_tile": (_L, [_P]),
     "tbem_direct_apply": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _I, _P]),
     "tbem_direct_gradients": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P]),

@@ -137,6 +137,13 @@ int tbem_fmm_set_c2e(TbemFmm* h, int which, long level, const double* op);
 int tbem_fmm_set_timing(TbemFmm* h, int enabled);
 int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int cap);
 
+/* Threads per target the point-to-point pass uses (chosen by timing the
+ * candidates 2, 4, 8 at creation unless TbemGpuOptions.p2p_block fixed it). */
+long tbem_fmm_p2p_block(const TbemFmm* h);
+/* N tile (columns) of the precision form's tensor-core translations, chosen
+ * by timing the 128- and 64-column shapes at creation (0 when unused). */
+long tbem_fmm_tc_tile(const TbemFmm* h);
+
 /* Number of kernel launches the last apply made on the device (no
  * reference counterpart; used to report the launch count of a timed run). */
 long tbem_fmm_last_launches(const TbemFmm* h);

@@ -132,10 +132,29 @@ def test_mixed_tensor_core_m2l_matches_simt(name, order):
                               m2l_path=1)
     X = np.random.default_rng(22).uniform(-1, 1, (3, tc.n_cols()))
     assert rel(tc.apply(X), simt.apply(X)) < 2e-6
+    assert tc.tc_tile() in (64, 128) and simt.tc_tile() == 0
+    assert tc.p2p_block() in (2, 4, 8)
     # M2M and L2L on the tensor cores as well (the default path)
     full = ThreeD.FMMOperator(kernel_obj(name), locs, nrm, locs, nrm, w, cfg, precision="mixed",
                               m2l_path=0)
     assert rel(full.apply(X), simt.apply(X)) < 2e-6
+
+
+@pytest.mark.parametrize("name", ["LaplaceDouble", "ElasticDisplacement"])
+def test_plain_form_is_deterministic(name):
+    """The plain form accumulates in conflict-free waves (no float atomics):
+    repeated applies agree bit for bit, so FP64 residuals are reproducible."""
+    locs, nrm, w = cloud(1200, 23)
+    ol, on, _ = cloud(500, 24)
+    for obs in (None, (ol, on)):
+        orc, op = make_pair(name, locs, nrm, w, 35, 25, False, obs=obs)
+        x = np.random.default_rng(25).uniform(-1, 1, op.n_cols())
+        y0 = op.apply(x)
+        for _ in range(3):
+            assert np.array_equal(op.apply(x), y0)
+        z = np.random.default_rng(26).uniform(-1, 1, op.n_rows())
+        w0 = op.apply_adjoint(z)
+        assert np.array_equal(op.apply_adjoint(z), w0)
 
 
 def test_multi_rhs_matches_single():

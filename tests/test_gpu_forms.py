@@ -35,17 +35,23 @@ def test_misfit_gradient_matches_transpose_and_finite_differences(prec):
     r = A @ s.detach().cpu().numpy() - d.cpu().numpy()
     g_dense = A.T @ r
     # the precision form's forward M2L runs on the tensor cores (3xBF16) and its
-    # transpose on the FP32 pipes: the two agree to the split's rounding
-    tol = 1e-11 if prec == "fp64" else 2e-5
+    # transpose on the FP32 pipes: the two agree to the split's rounding.  The
+    # plain form's check-to-equivalent pseudo-inverse (condition ~1e9) turns the
+    # 1e-16 differences between its forward and transposed arithmetic into
+    # ~1e-10: 1e-9 is the transpose bound there.
+    tol = 1e-9 if prec == "fp64" else 2e-5
     assert np.linalg.norm(g - g_dense) <= tol * np.linalg.norm(g_dense)
-    # central finite differences on 64 random coordinates (h = 1e-6)
-    h = 1e-6
+    # central finite differences on 64 random coordinates: h = 1e-6 in FP64;
+    # in the precision form (FP32 noise in every apply) h = 0.1, which is exact
+    # for this quadratic loss and keeps the noise below the tolerance
+    h = 1e-6 if prec == "fp64" else 0.1
+    fd_tol = 1e-6 if prec == "fp64" else 2e-5
     s0 = s.detach()
     for j in rng.choice(op.n_cols(), 64, replace=False):
         e = torch.zeros_like(s0)
         e[j] = h
         fd = (autograd.misfit(op, s0 + e, d) - autograd.misfit(op, s0 - e, d)).item() / (2 * h)
-        assert abs(fd - g[j]) <= 1e-6 * max(1.0, np.abs(g).max())
+        assert abs(fd - g[j]) <= fd_tol * max(1.0, np.abs(g).max())
 
 
 def test_refined_gmres_reaches_fp64_residual():
