@@ -5,14 +5,14 @@
 // term holds the next 8 significant bits), and the product is accumulated
 // from the six bf16 MMAs that reach 2^-24 relative size (a0b0, a0b1, a1b0,
 // a0b2, a1b1, a2b0) in FP32 accumulators in tensor memory: FP32-level
-// accuracy on the bf16 tensor pipe.  The dominant product a0b0 and the five
-// small ones go to two separate accumulators that are added in the epilogue,
-// so the small terms are never rounded against the large running sum (the
-// error of accumulating them into one accumulator grew with the number of
-// MMAs).  The operators' planes are built once at
+// accuracy on the bf16 tensor pipe.  The accumulation error of an FP32
+// tensor-memory accumulator grows with the number of MMAs added into it, so
+// the dominant product a0b0 goes to two accumulators (even and odd K chunks)
+// and the five small products to a third; the epilogue adds the three in
+// FP32 registers.  Small terms are never rounded against the large sum.  The operators' planes are built once at
 // setup; the check potentials (B) are split before every use.
 //
-// CTA: 128 threads, two 128 x BN accumulators (2 BN TMEM columns).  K runs in
+// CTA: 128 threads, three 128 x BN accumulators (4 BN TMEM columns allocated).  K runs in
 // chunks of 64 bf16 (128-byte rows) through a 2-stage shared-memory ring of
 // six 128B-swizzled K-major planes per stage.  All threads stage a chunk with
 // cp.async (A rows from the operator planes, B rows gathered by pair; 48
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&tmem_slot)),
-                     "r"(2 * BN));
+                     "r"(4 * BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
@@ -256,10 +256,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
                 const uint32_t a0 = st + off, a1 = a0 + TC_TILE_BYTES, a2 = a0 + 2 * TC_TILE_BYTES;
                 const uint32_t b0 = st + B_BASE + off, b1 = b0 + Sh::B_TILE, b2 = b0 + 2 * Sh::B_TILE;
                 constexpr uint32_t ID = Sh::IDESC;
-                const uint32_t first = (kc | kk) != 0;
-                const uint32_t small = tmem + BN;  // second accumulator
-                mma_bf16(tmem, sw128_desc(a0), sw128_desc(b0), ID, first);
-                mma_bf16(small, sw128_desc(a0), sw128_desc(b1), ID, first);
+                const uint32_t big = tmem + (kc & 1) * BN;   // a0b0: even / odd chunks
+                const uint32_t small = tmem + 2 * BN;        // the five small products
+                mma_bf16(big, sw128_desc(a0), sw128_desc(b0), ID, (kc >= 2 || kk != 0) ? 1u : 0u);
+                mma_bf16(small, sw128_desc(a0), sw128_desc(b1), ID, (kc | kk) != 0);
                 mma_bf16(small, sw128_desc(a1), sw128_desc(b0), ID, 1);
                 mma_bf16(small, sw128_desc(a0), sw128_desc(b2), ID, 1);
                 mma_bf16(small, sw128_desc(a1), sw128_desc(b1), ID, 1);
@@ -285,8 +285,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
 #pragma unroll 1
         for (int cc = 0; cc < BN / 32; cc++) {
             float v[32], w[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cc * 32, v);
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + BN + cc * 32, w);
+            const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + cc * 32;
+            tmem_ld32(lane_base + 2 * BN, v);  // small terms first
+            if (nk > 1) {
+                tmem_ld32(lane_base + BN, w);
+#pragma unroll
+                for (int j = 0; j < 32; j++) v[j] += w[j];
+            }
+            tmem_ld32(lane_base, w);
 #pragma unroll
             for (int j = 0; j < 32; j++) v[j] += w[j];
             if (row >= a.n) continue;
@@ -304,7 +310,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(4 * BN));
 }
 
 // v -> three bf16 terms t0 + t1 + t2 (each the rounding of what is left)

@@ -41,10 +41,12 @@ def test_misfit_gradient_matches_transpose_and_finite_differences(prec):
     # ~1e-10: 1e-9 is the transpose bound there.
     tol = 1e-9 if prec == "fp64" else 2e-5
     assert np.linalg.norm(g - g_dense) <= tol * np.linalg.norm(g_dense)
-    # central finite differences on 64 random coordinates: h = 1e-6 in FP64;
-    # in the precision form (FP32 noise in every apply) h = 0.1, which is exact
-    # for this quadratic loss and keeps the noise below the tolerance
-    h = 1e-6 if prec == "fp64" else 0.1
+    # central finite differences on 64 random coordinates.  The loss is exactly
+    # quadratic in s, so central differences are exact for any step; a unit
+    # step keeps each apply's rounding noise (plain form: ~3e-9 relative, see
+    # test_plain_fmm_linearity_floor; precision form: FP32) far below the
+    # tolerance
+    h = 1.0
     fd_tol = 1e-6 if prec == "fp64" else 2e-5
     s0 = s.detach()
     for j in rng.choice(op.n_cols(), 64, replace=False):
@@ -54,21 +56,43 @@ def test_misfit_gradient_matches_transpose_and_finite_differences(prec):
         assert abs(fd - g[j]) <= fd_tol * max(1.0, np.abs(g).max())
 
 
+def test_plain_fmm_linearity_floor():
+    """The reference's FMM formulation is linear only up to ~1e-9: its
+    pseudo-inverse (condition ~1e9) turns rounding into input-dependent noise.
+    Bit-reproducible, but A(x1 + x2) != A x1 + A x2 at that level -- the floor
+    of any FP64 residual formed with it."""
+    from tbempy import ThreeD, meshes
+    locs, nrm, w = meshes.sphere_points(3)
+    op = ThreeD.FMMOperator(ThreeD.LaplaceDouble(), locs, nrm, locs, nrm, w,
+                            ThreeD.FMMConfig(0.3, 152, 40, 0.05, False), precision="fp64")
+    rng = np.random.default_rng(5)
+    x1, x2 = rng.uniform(-1, 1, (2, op.n_cols()))
+    y1, y2, y12 = op.apply(x1), op.apply(x2), op.apply(x1 + x2)
+    nonlin = np.linalg.norm(y12 - y1 - y2) / np.linalg.norm(y12)
+    assert nonlin < 1e-7
+    assert np.array_equal(op.apply(x1), y1)
+
+
 def test_refined_gmres_reaches_fp64_residual():
-    """Second-kind Laplace system (0.5 I + D) sigma = f on a sphere: inner
-    GMRES with the precision form, FP64 residuals with the plain form."""
+    """Second-kind Laplace system (0.5 I + D) sigma = f on a sphere: the inner
+    GMRES runs on the precision-form FMM, the FP64 residual uses the GPU FP64
+    direct operator (linear to rounding); the refined solve reaches 1e-10."""
     from tbempy import ThreeD, meshes, solve
     locs, nrm, w = meshes.sphere_points(3)
     cfg = ThreeD.FMMConfig(0.3, 152, 40, 0.05, False)
     K = ThreeD.LaplaceDouble()
-    plain = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="fp64")
+    direct = ThreeD.DirectOperator(K, locs, nrm, locs, nrm, w)
     fast = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed")
-    A64 = lambda v: 0.5 * v + plain.apply(v)
+    A64 = lambda v: 0.5 * v + direct.apply(v)
     A32 = lambda v: 0.5 * v + fast.apply(v)
     f = 1.0 / np.linalg.norm(locs - np.array([0.1, 0.2, 0.3]), axis=1)
     x, hist = solve.refined_solve(A64, A32, f, tol=1e-10, inner_tol=1e-6)
     assert hist[-1][2] <= 1e-10, hist
     assert np.linalg.norm(A64(x) - f) <= 1e-10 * np.linalg.norm(f)
+    # the plain FP64 GMRES on the same system, against the same residual
+    plain = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="fp64")
+    xp, info, _ = solve.gmres(lambda v: 0.5 * v + plain.apply(v), f, restart=50, tol=1e-10)
+    assert np.linalg.norm(A64(xp) - f) <= 1e-6 * np.linalg.norm(f)
 
 
 def test_integral_operator_composition():
@@ -127,6 +151,7 @@ def test_vertex_gradients_match_central_differences(name):
 
     L = loss(V)
     L.backward()
+    # the direct operator is linear to rounding, so a small step is usable here
     g = V.grad.cpu().numpy().ravel()
     h = 1e-6
     flat = v.ravel()
