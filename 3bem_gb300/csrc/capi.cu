@@ -52,6 +52,7 @@ void tbem_default_options(TbemGpuOptions* opt)
     opt->precision = TBEM_PRECISION_FP64;
     opt->device = 0;
     opt->svd_threshold = 1e-10;
+    opt->m2l_rank_tol = 1e-7;
 }
 
 int tbem_fmm_create(int kernel, const double* kernel_params, const double* obs_locs,
@@ -214,6 +215,15 @@ long tbem_fmm_tc_tile(const TbemFmm* h)
 {
     if (!h) return TBEM_ERR_ARG;
     return h->plan.f.use_tc ? h->plan.f.m2l.tc_bn : 0;
+}
+
+int tbem_fmm_m2l_ranks(const TbemFmm* h, long* r_in, long* r_out)
+{
+    if (!h) return fail(TBEM_ERR_ARG, "null handle");
+    const bool c = h->plan.f.m2l_compressed;
+    if (r_in) *r_in = c ? h->plan.f.r_in : 0;
+    if (r_out) *r_out = c ? h->plan.f.r_out : 0;
+    return TBEM_OK;
 }
 
 long tbem_fmm_last_launches(const TbemFmm* h) { return h ? h->plan.launches : TBEM_ERR_ARG; }

@@ -127,8 +127,8 @@ void GemmSet::build_waves()
 }
 
 template <typename T>
-void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s,
-                  long* launches)
+void GemmSet::run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int trans, int mode,
+                       cudaStream_t s, long* launches)
 {
     if (empty()) return;
     const bool waves = mode == GEMM_WAVES;
@@ -166,7 +166,9 @@ void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaSt
     a.out_cell = d_out.p;
     a.B = B;
     a.D = D;
-    a.n = n;
+    a.m = m;
+    a.k = k;
+    a.lda = lda;
     a.nrhs = nrhs;
     a.trans = trans;
     a.mode = waves ? GEMM_ADD : mode;
@@ -178,15 +180,17 @@ void GemmSet::run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaSt
         if (nt == 0) continue;
         a.tile_group = it->second.first.p + st[w];
         a.tile_col0 = it->second.second.p + st[w];
-        dim3 grid((unsigned)nt, (unsigned)((n + GM_BM - 1) / GM_BM));
-        grouped_gemm_kernel<T><<<grid, GM_THREADS, 0, s>>>(a);
+        const int bm = gemm_bm(m);
+        dim3 grid((unsigned)nt, (unsigned)((m + bm - 1) / bm));
+        if (bm == 128) grouped_gemm_kernel<T, 128><<<grid, GM_THREADS, 0, s>>>(a);
+        else grouped_gemm_kernel<T, 64><<<grid, GM_THREADS, 0, s>>>(a);
         TBEM_CK(cudaGetLastError());
         if (launches) (*launches)++;
     }
 }
 
-template void GemmSet::run<double>(const double*, double*, int, int, int, int, cudaStream_t, long*);
-template void GemmSet::run<float>(const float*, float*, int, int, int, int, cudaStream_t, long*);
+template void GemmSet::run_rect<double>(const double*, double*, int, int, int, int, int, int, cudaStream_t, long*);
+template void GemmSet::run_rect<float>(const float*, float*, int, int, int, int, int, int, cudaStream_t, long*);
 
 // ------------------------------------------------------------ device kernels
 
@@ -314,6 +318,19 @@ __global__ void convert_rows_kernel(const double* in, float* out, long rows, int
         const long r = t / ld;
         const int k = (int)(t % ld);
         out[t] = k < n ? float(in[r * n + k]) : 0.f;
+    }
+}
+
+// the last r columns (largest eigenvalues) of a column-major n x n
+// eigenvector matrix -> row-major n x r FP32
+__global__ void basis_rows_kernel(const double* evec, int n, int r, float* out)
+{
+    const long total = (long)n * r;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long)gridDim.x * blockDim.x) {
+        const long i = t / r;
+        const int j = (int)(t % r);
+        out[t] = float(evec[(long)(n - r + j) * n + i]);
     }
 }
 
@@ -1026,6 +1043,7 @@ void Plan::build_mixed_ops(Form& F)
     const double one = 1.0, zero = 0.0;
     // combined operator of job k: K_k * C2E(level of the k-th operator's source side)
     std::vector<long> c2e_of(jobs.size(), -1);
+    std::vector<int> job_ls(jobs.size(), 0);  // M2L jobs: source level they were built at
     {
         const Tree& S = *stree;
         const Tree& O = otree;
@@ -1038,9 +1056,24 @@ void Plan::build_mixed_ops(Form& F)
             if (l2l_off[k] >= 0 && c2e_of[l2l_off[k] / nn] < 0)
                 c2e_of[l2l_off[k] / nn] = F.c2e_dn_off[O.cells[l2l_canon[k].first].level];
         for (size_t k = 0; k < m2l_off.size(); k++)
-            if (c2e_of[m2l_off[k] / nn] < 0)
+            if (c2e_of[m2l_off[k] / nn] < 0) {
                 c2e_of[m2l_off[k] / nn] = F.c2e_up_off[S.cells[m2l_canon[k].second].level];
+                job_ls[m2l_off[k] / nn] = S.cells[m2l_canon[k].second].level;
+            }
     }
+    // m2l_path: 0 auto (compressed M2L where the operators are precomputed),
+    // 1 SIMT FP32 for all, 2 tensor cores for the M2L only, 3 tensor cores for
+    // all, 4 compressed M2L
+    const int path = opt.m2l_path == 0 ? 4 : opt.m2l_path;
+    // FP64 copies of the M2L kernel matrices for the compression (compact
+    // index), scaled to the root level (see build_m2l_compression)
+    const bool compress = path == 4 && !F.m2l_on_the_fly && !m2l_off.empty();
+    std::vector<long> m2l_index(jobs.size(), -1);
+    long n_m2l_ops = 0;
+    for (long off : m2l_off)
+        if (off >= 0 && m2l_index[off / nn] < 0) m2l_index[off / nn] = n_m2l_ops++;
+    DBuf<double> U64;
+    if (compress) U64.alloc((size_t)n_m2l_ops * nn);
     if (!jobs.empty()) {
         // in chunks to bound the FP64 scratch
         const size_t chunk = std::max<size_t>(1, (size_t)(2e9 / (8.0 * nn)));
@@ -1066,14 +1099,24 @@ void Plan::build_mixed_ops(Form& F)
             }
             convert_kernel<float><<<grid_for(nj * nn), 256, 0, stream>>>(Y.p, F.ops32.p + j0 * nn, nj * nn);
             TBEM_CK(cudaGetLastError());
+            if (compress)
+                for (size_t k = 0; k < nj; k++)
+                    if (m2l_index[j0 + k] >= 0) {
+                        double* dst = U64.p + m2l_index[j0 + k] * nn;
+                        TBEM_CK(cudaMemcpyAsync(dst, K.p + k * nn, sizeof(double) * nn,
+                                                cudaMemcpyDeviceToDevice, stream));
+                        const double f = std::ldexp(1.0, -job_ls[j0 + k]);
+                        TBEM_CKB(cublasDscal(cublas, (int)nn, &f, dst, 1));
+                    }
             TBEM_CK(cudaStreamSynchronize(stream));
         }
     }
     build_gemm_sets(F, 0, 0, 0, m2m_off, l2l_off, m2l_off);
-    // m2l_path: 0 auto (tensor cores for M2L, M2M and L2L), 1 SIMT FP32 for all,
-    // 2 tensor cores for M2L only, 3 tensor cores for all
-    F.use_tc = opt.m2l_path != 1 && !jobs.empty();
-    F.use_tc_updown = F.use_tc && (opt.m2l_path == 0 || opt.m2l_path == 3);
+    F.m2l_compressed = false;
+    if (compress) build_m2l_compression(F, U64.p, n_m2l_ops, m2l_index);
+    U64.release();
+    F.use_tc = (path == 2 || path == 3) && !jobs.empty();
+    F.use_tc_updown = F.use_tc && path == 3;
     if (F.use_tc) {
         F.tc.build(F.ops32.p, (long)jobs.size(), n, stream);
         TBEM_CK(cudaStreamSynchronize(stream));
@@ -1139,6 +1182,163 @@ void Plan::build_mixed_ops(Form& F)
     }
 }
 
+// SVD-compressed M2L (Fong & Darve, J. Comput. Phys. 228 (2009) 8712-8725,
+// sec. 3.3).  The M2L operator of a pair is U = T C2E_up(l_s): the kernel
+// matrix T (down-check surface of the target <- up-equivalent surface of the
+// source) times the source level's check-to-equivalent operator.  The bases
+// come from the kernel matrices, not from U: the pseudo-inverse magnifies the
+// directions the check potentials never carry, which would make U look full
+// rank.  Both translation kernels are homogeneous of degree -1, so a pair at
+// source level l_s has T = 2^l_s T0 with T0 the root-scaled matrix of its
+// (level difference, offset) class, and
+//   U = T0 (2^l_s C2E_up(l_s)) ~= V (V^T T0 W) (W^T 2^l_s C2E_up(l_s))
+//     = V C_k P_(l_s),
+// W the leading eigenvectors of sum_k T0_k^T T0_k (input side), V those of
+// sum_k T0_k T0_k^T (output side), cut where the eigenvalue falls below
+// tol^2 times the largest (singular values of the stacks below tol times the
+// largest).  r_out is rounded up to the GEMM's 64-row tile and r_in to its
+// 16-deep k step: the extra vectors cost nothing in the M2L products.  The
+// M2L then runs as compress (P_l, once per source cell), r_out x r_in
+// products C_k per pair, and decompress (V, once per target cell).  U64
+// holds the root-scaled T0 of every M2L class (compact index).
+void Plan::build_m2l_compression(Form& F, const double* U64, long n_ops,
+                                 const std::vector<long>& op_index)
+{
+    if (F.g_kid != LAP_S && F.g_kid != EL_DISP)
+        throw Error(TBEM_ERR_STATE, "compressed M2L needs a degree -1 translation kernel");
+    const long nn = (long)n * n;
+    const double one = 1.0, zero = 0.0;
+    const double tol = opt.m2l_rank_tol > 0 ? opt.m2l_rank_tol : 1e-7;
+    DBuf<double> Gi, Go;
+    Gi.alloc(nn);
+    Go.alloc(nn);
+    // G_in = sum_k T_k^T T_k = X X^T, X = [T_1^T ... T_K^T]: the column-major
+    // view of the row-major matrices side by side (chunks bound the int sizes)
+    const long step = std::max<long>(1, (1L << 30) / std::max(nn, 1L));
+    for (long k0 = 0; k0 < n_ops; k0 += step) {
+        const long kb = std::min(step, n_ops - k0);
+        const double beta = k0 == 0 ? 0.0 : 1.0;
+        TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, n, (int)(kb * n), &one,
+                             U64 + k0 * nn, n, &beta, Gi.p, n));
+    }
+    // G_out = sum_k T_k T_k^T: one rank-n update per matrix
+    for (long k = 0; k < n_ops; k++) {
+        const double beta = k == 0 ? 0.0 : 1.0;
+        TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, n, n, &one, U64 + k * nn, n,
+                             &beta, Go.p, n));
+    }
+    // eigenvectors (ascending eigenvalues) overwrite the Gram matrices
+    DBuf<double> ev;
+    ev.alloc(2 * (size_t)n);
+    int lwork = 0;
+    TBEM_CKS(cusolverDnDsyevd_bufferSize(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
+                                         Gi.p, n, ev.p, &lwork));
+    DBuf<double> work;
+    work.alloc(std::max(lwork, 1));
+    DBuf<int> info;
+    info.alloc(2);
+    TBEM_CKS(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, Gi.p, n,
+                              ev.p, work.p, lwork, info.p));
+    TBEM_CKS(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, Go.p, n,
+                              ev.p + n, work.p, lwork, info.p + 1));
+    std::vector<double> h_ev = ev.download();
+    std::vector<int> h_info = info.download();
+    if (h_info[0] != 0 || h_info[1] != 0)
+        throw Error(TBEM_ERR_CUDA, "eigen-decomposition of the M2L Gram matrices failed");
+    auto rank_of = [&](const double* e) {
+        const double top = e[n - 1];
+        int r = 0;
+        for (int i = 0; i < n; i++)
+            if (e[i] > tol * tol * top) r++;
+        return std::max(r, 1);
+    };
+    const int ri = std::min(n, (rank_of(h_ev.data()) + 15) / 16 * 16);
+    const int ro = std::min(n, (rank_of(h_ev.data() + n) + 63) / 64 * 64);
+    // no gain once the compressed products approach the dense ones
+    if ((long)ri * ro > nn / 2) return;
+    F.r_in = ri;
+    F.r_out = ro;
+    const double* W = Gi.p + (long)(n - ri) * n;  // column-major n x ri
+    const double* V = Go.p + (long)(n - ro) * n;  // column-major n x ro
+    F.Vb.alloc((size_t)n * ro);
+    basis_rows_kernel<<<grid_for((long)n * ro), 256, 0, stream>>>(Go.p, n, ro, F.Vb.p);
+    TBEM_CK(cudaGetLastError());
+    // compress operators P_l = 2^l W^T C2E_up(l), row-major ri x n = the
+    // column-major n x ri product 2^l C2E_up(l)^T W (C2E_up(l)^T being the
+    // column-major view of the stored operator)
+    const Tree& S = *stree;
+    const int LS = S.n_levels();
+    {
+        DBuf<double> Pl;
+        Pl.alloc((size_t)n * ri);
+        F.Wb.alloc((size_t)LS * n * ri);
+        for (int l = 0; l < LS; l++) {
+            const double f = std::ldexp(1.0, l);
+            TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ri, n, &f, F.c2e.p + F.c2e_up_off[l],
+                                 n, W, n, &zero, Pl.p, n));
+            convert_kernel<float><<<grid_for((long)n * ri), 256, 0, stream>>>(Pl.p, F.Wb.p + (long)l * n * ri,
+                                                                             (long)n * ri);
+            TBEM_CK(cudaGetLastError());
+        }
+        TBEM_CK(cudaStreamSynchronize(stream));
+    }
+    // C_k (row-major ro x ri) = column-major C_k^T = W^T T_k^T V, T_k^T being
+    // the column-major view of the stored matrix
+    const long cc = (long)ro * ri;
+    F.Cops.alloc((size_t)n_ops * cc);
+    const long cb = std::max<long>(1, std::min<long>(n_ops, (long)(1e9 / (8.0 * n * ro))));
+    DBuf<double> P, CT;
+    P.alloc((size_t)cb * n * ro);
+    CT.alloc((size_t)cb * cc);
+    for (long k0 = 0; k0 < n_ops; k0 += cb) {
+        const long kb = std::min(cb, n_ops - k0);
+        TBEM_CKB(cublasDgemmStridedBatched(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ro, n, &one,
+                                           U64 + k0 * nn, n, nn, V, n, 0, &zero, P.p, n,
+                                           (long long)n * ro, (int)kb));
+        TBEM_CKB(cublasDgemmStridedBatched(cublas, CUBLAS_OP_T, CUBLAS_OP_N, ri, ro, n, &one, W, n, 0,
+                                           P.p, n, (long long)n * ro, &zero, CT.p, ri, cc, (int)kb));
+        convert_kernel<float><<<grid_for(kb * cc), 256, 0, stream>>>(CT.p, F.Cops.p + k0 * cc, kb * cc);
+        TBEM_CK(cudaGetLastError());
+    }
+    TBEM_CK(cudaStreamSynchronize(stream));
+    // the compressed sets: F.m2l's groups on the C_k pool; the compress sets
+    // pair every M2L source cell with itself (one group per level: P_l), the
+    // decompress set every M2L target cell (one group: V)
+    F.m2l_c = GemmSet();
+    F.m2l_c_t = GemmSet();
+    F.comp_src = GemmSet();
+    F.comp_obs = GemmSet();
+    std::vector<char> is_src(S.cells.size(), 0), is_obs(otree.cells.size(), 0);
+    for (size_t g = 0; g < F.m2l.A_off.size(); g++) {
+        std::vector<std::pair<int, int>> pr, pt;
+        for (long p = F.m2l.pair0[g]; p < F.m2l.pair0[g] + F.m2l.npairs[g]; p++) {
+            pr.push_back({F.m2l.in_cell[p], F.m2l.out_cell[p]});
+            pt.push_back({F.m2l.out_cell[p], F.m2l.in_cell[p]});
+            is_src[F.m2l.in_cell[p]] = 1;
+            is_obs[F.m2l.out_cell[p]] = 1;
+        }
+        const long idx = op_index[F.m2l.A_off[g] / nn];
+        if (idx < 0) throw Error(TBEM_ERR_STATE, "M2L operator without a compressed copy");
+        F.m2l_c.add_group(idx * cc, pr);
+        F.m2l_c_t.add_group(idx * cc, pt);
+    }
+    for (int l = 0; l < LS; l++) {
+        std::vector<std::pair<int, int>> ps;
+        for (int c = S.level_start[l]; c < S.level_start[l + 1]; c++)
+            if (is_src[c]) ps.push_back({c, c});
+        F.comp_src.add_group((long)l * n * ri, ps);
+    }
+    std::vector<std::pair<int, int>> po;
+    for (int c = 0; c < (int)is_obs.size(); c++)
+        if (is_obs[c]) po.push_back({c, c});
+    F.comp_obs.add_group(0, po);
+    F.m2l_c.upload(F.Cops.p, sizeof(float));
+    F.m2l_c_t.upload(F.Cops.p, sizeof(float));
+    F.comp_src.upload(F.Wb.p, sizeof(float));
+    F.comp_obs.upload(F.Vb.p, sizeof(float));
+    F.m2l_compressed = true;
+}
+
 void Plan::set_c2e(int which, long level, const double* op)
 {
     if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
@@ -1173,6 +1373,10 @@ void Plan::ensure_rhs(int nrhs)
         s32.ensure((size_t)R * N * nrhs);
         cu32.ensure((size_t)ncs * nrhs * n);
         cd32.ensure((size_t)nco * nrhs * n);
+        if (f.m2l_compressed) {
+            cuc32.ensure((size_t)ncs * nrhs * f.r_in);
+            cdc32.ensure((size_t)nco * nrhs * f.r_out);
+        }
         if (!L.m2p.empty() || f.m2l_on_the_fly) {
             cu64.ensure((size_t)ncs * nrhs * n);
             qu64.ensure((size_t)ncs * nrhs * n);
@@ -1320,6 +1524,14 @@ void Plan::forward(int nrhs, cudaStream_t s)
             add_kernel<<<grid_for(nco * nrhs * n), 256, 0, s>>>(cd64.p, cd32.p, nco * nrhs * n);
             TBEM_CK(cudaGetLastError());
             launches++;
+        } else if (F.m2l_compressed) {
+            // compress (P_l per source cell), r_out x r_in products, decompress
+            // (V per target cell, added to the down-check potentials)
+            const int ri = F.r_in, ro = F.r_out;
+            F.comp_src.run_rect<float>(cu32.p, cuc32.p, ri, n, n, nrhs, 0, GEMM_STORE, s, &launches);
+            TBEM_CK(cudaMemsetAsync(cdc32.p, 0, sizeof(float) * nco * nrhs * ro, s));
+            F.m2l_c.run_rect<float>(cuc32.p, cdc32.p, ro, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
+            F.comp_obs.run_rect<float>(cdc32.p, cd32.p, n, ro, ro, nrhs, 0, GEMM_ADD, s, &launches);
         } else if (F.use_tc) {
             F.tc.split_b_rows(cu32.p, 0, ncs * nrhs, std::max(ncs, nco) * nrhs, s);
             launches++;
@@ -1420,6 +1632,13 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
             TBEM_CK(cudaGetLastError());
             launches++;
             eval<double>(m2l_fly_t, F.g_kid, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
+        } else if (F.m2l_compressed) {
+            // U^T ~= P_l^T C_k^T V^T: V^T per target cell, C_k^T per pair, P_l^T per source cell
+            const int ri = F.r_in, ro = F.r_out;
+            F.comp_obs.run_rect<float>(cd32.p, cdc32.p, ro, n, ro, nrhs, 1, GEMM_STORE, s, &launches);
+            TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
+            F.m2l_c_t.run_rect<float>(cdc32.p, cuc32.p, ri, ro, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
+            F.comp_src.run_rect<float>(cuc32.p, cu32.p, n, ri, n, nrhs, 1, GEMM_ADD, s, &launches);
         } else {
             F.m2l_t.run<float>(cd32.p, cu32.p, n, nrhs, 1, GEMM_ATOMIC, s, &launches);
         }

@@ -156,7 +156,14 @@ struct GemmSet {
     void upload(const void* pool, size_t elem_size);
     template <typename T>
     void run(const T* B, T* D, int n, int nrhs, int trans, int mode, cudaStream_t s,
-             long* launches = nullptr);
+             long* launches = nullptr)
+    {
+        run_rect<T>(B, D, n, n, n, nrhs, trans, mode, s, launches);
+    }
+    // op(A) is m x k; A is stored row-major with rows of length lda
+    template <typename T>
+    void run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int trans, int mode,
+                  cudaStream_t s, long* launches = nullptr);
     // tensor-core path (B taken from P's split planes); nn = elements per operator
     DBuf<int> d_op;
     std::map<int, std::pair<DBuf<int>, DBuf<int>>> tc_tiles;
@@ -195,6 +202,15 @@ struct Form {
     TcPlanes tc;
     bool use_tc = false;
     bool use_tc_updown = false;
+    // mixed: SVD-compressed M2L, U ~= V C_k P_l with bases shared by every
+    // operator: Wb holds the per-source-level compress operators P_l (r_in x
+    // n), Vb the decompress basis V (n x r_out), Cops the C_k (r_out x r_in),
+    // all row-major FP32; comp_src / comp_obs pair every M2L source / target
+    // cell with itself (one group per level: P_l / one group: V)
+    bool m2l_compressed = false;
+    int r_in = 0, r_out = 0;
+    DBuf<float> Wb, Vb, Cops;
+    GemmSet m2l_c, m2l_c_t, comp_src, comp_obs;
     // mixed: per-leaf L2P operators
     DBuf<float> E;
     DBuf<long> E_row0;  // per l2p task
@@ -237,6 +253,7 @@ struct Plan {
     DBuf<float> s32;
     DBuf<double> cu64, qu64, cd64, qd64;  // cell buffers [cell][rhs][n]
     DBuf<float> cu32, cd32;
+    DBuf<float> cuc32, cdc32;  // compressed M2L coefficients [cell][rhs][r_in | r_out]
     cudaStream_t stream = nullptr;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t solver = nullptr;
@@ -263,6 +280,7 @@ struct Plan {
     void build_c2e(Form& F);
     void build_plain_ops(Form& F);
     void build_mixed_ops(Form& F);
+    void build_m2l_compression(Form& F, const double* U64, long n_ops, const std::vector<long>& op_index);
     void build_gemm_sets(Form& F, long op_base_m2m, long op_base_l2l, long op_base_m2l,
                          const std::vector<long>& m2m_off, const std::vector<long>& l2l_off,
                          const std::vector<long>& m2l_off);

@@ -168,7 +168,7 @@ class FMMOperator(OperatorI):
 
     def __init__(self, K, obs_locs, obs_normals, src_locs, src_normals, src_weights, config,
                  precision="fp64", device=0, svd_threshold=1e-10, host_only=False,
-                 m2l_path=0, _handle=None):
+                 m2l_path=0, m2l_rank_tol=1e-7, _handle=None):
         self.K = K
         self.config = config
         self.precision = precision
@@ -188,6 +188,7 @@ class FMMOperator(OperatorI):
         opt.svd_threshold = float(svd_threshold)
         opt.host_only = int(bool(host_only))
         opt.m2l_path = int(m2l_path)
+        opt.m2l_rank_tol = float(m2l_rank_tol)
         cfg = config._c()
         h = C.c_void_p()
         params = K.params()
@@ -283,6 +284,12 @@ class FMMOperator(OperatorI):
     def tc_tile(self):
         """N tile of the tensor-core translations (autotuned; 0 if unused)."""
         return check(_L.lib().tbem_fmm_tc_tile(self._h))
+
+    def m2l_ranks(self):
+        """(r_in, r_out) of the SVD-compressed M2L; (0, 0) when uncompressed."""
+        a, b = C.c_long(), C.c_long()
+        check(_L.lib().tbem_fmm_m2l_ranks(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def last_launches(self):
         """Kernel launches made by the last apply."""

@@ -24,7 +24,7 @@ class TbemFmmConfig(C.Structure):
 class TbemGpuOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("svd_threshold", C.c_double),
                 ("m2l_path", C.c_int), ("p2p_block", C.c_int), ("host_only", C.c_int),
-                ("reserved", C.c_int * 3)]
+                ("m2l_rank_tol", C.c_double), ("reserved", C.c_int * 2)]
 
 
 class TbemError(RuntimeError):
@@ -57,6 +57,7 @@ SIGNATURES = {
     "tbem_fmm_last_launches": (_L, [_P]),
     "tbem_fmm_p2p_block": (_L, [_P]),
     "tbem_fmm_tc_tile": (_L, [_P]),
+    "tbem_fmm_m2l_ranks": (_I, [_P, _P, _P]),
     "tbem_direct_apply": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _I, _P]),
     "tbem_direct_gradients": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P]),

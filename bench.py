@@ -210,7 +210,10 @@ def main():
     ap.add_argument("--grid", type=int, default=N_GRID,
                     help="quads per fault side (128 = the workload; smaller for ncu captures)")
     ap.add_argument("--kernels", default="both", choices=["both", "disp"])
-    ap.add_argument("--m2l-path", type=int, default=0, help="0 auto, 1 SIMT FP32, 2 tcgen05")
+    ap.add_argument("--m2l-path", type=int, default=0,
+                    help="0 auto, 1 SIMT FP32, 2 tcgen05 M2L, 3 tcgen05 all, 4 compressed M2L")
+    ap.add_argument("--m2l-rank-tol", type=float, default=1e-7,
+                    help="singular-value cut of the compressed M2L")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
@@ -236,7 +239,7 @@ def main():
         kernels = kernels[:1]
     t0 = time.perf_counter()
     ops = [ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed", device=local,
-                              m2l_path=args.m2l_path)
+                              m2l_path=args.m2l_path, m2l_rank_tol=args.m2l_rank_tol)
            for K in kernels]
     setup_s = time.perf_counter() - t0
     n_rhs = args.rhs
@@ -375,6 +378,7 @@ def main():
             "plain_fp64": plain,
             "cpu_baseline": cpu,
             "setup_s": setup_s,
+            "m2l_ranks": [list(op.m2l_ranks()) for op in ops],
         }
         print(json.dumps(line), flush=True)
     if dist:

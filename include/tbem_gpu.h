@@ -63,13 +63,19 @@ typedef struct {
     int precision;         /* TBEM_PRECISION_*                                   */
     int device;            /* CUDA device ordinal                                */
     double svd_threshold;  /* singular-value cutoff (reference: 1e-10, fmm.cpp:122) */
-    int m2l_path;          /* precision form's dense translations: 0 auto (tcgen05
-                              3xBF16 for M2L, M2M and L2L), 1 SIMT FP32 for all,
-                              2 tcgen05 for M2L only, 3 tcgen05 for all           */
+    int m2l_path;          /* precision form's dense translations:
+                              0 auto (= 4 where the M2L operators are precomputed),
+                              1 SIMT FP32 for all (uncompressed M2L),
+                              2 tcgen05 3xBF16 for the uncompressed M2L only,
+                              3 tcgen05 3xBF16 for M2L, M2M and L2L,
+                              4 SVD-compressed M2L on the SIMT FP32 pipes         */
     int p2p_block;         /* 0 auto; else threads per target in the P2P kernel (1,2,4,8) */
     int host_only;         /* 1: build trees and task lists only (no device use);
                               apply calls then fail with TBEM_ERR_STATE            */
-    int reserved[3];
+    double m2l_rank_tol;   /* compressed M2L: singular values of the stacked M2L
+                              operators kept down to this fraction of the largest
+                              (0: 1e-7)                                           */
+    int reserved[2];
 } TbemGpuOptions;
 
 typedef struct TbemFmm TbemFmm;
@@ -143,6 +149,10 @@ long tbem_fmm_p2p_block(const TbemFmm* h);
 /* N tile (columns) of the precision form's tensor-core translations, chosen
  * by timing the 128- and 64-column shapes at creation (0 when unused). */
 long tbem_fmm_tc_tile(const TbemFmm* h);
+
+/* Ranks of the SVD-compressed M2L (input side, output side); both 0 when
+ * the M2L is not compressed.  Returns 0 or a TBEM_ERR_* code. */
+int tbem_fmm_m2l_ranks(const TbemFmm* h, long* r_in, long* r_out);
 
 /* Number of kernel launches the last apply made on the device (no
  * reference counterpart; used to report the launch count of a timed run). */

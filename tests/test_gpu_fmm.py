@@ -134,10 +134,43 @@ def test_mixed_tensor_core_m2l_matches_simt(name, order):
     assert rel(tc.apply(X), simt.apply(X)) < 2e-6
     assert tc.tc_tile() in (64, 128) and simt.tc_tile() == 0
     assert tc.p2p_block() in (2, 4, 8)
-    # M2M and L2L on the tensor cores as well (the default path)
+    # M2M and L2L on the tensor cores as well
     full = ThreeD.FMMOperator(kernel_obj(name), locs, nrm, locs, nrm, w, cfg, precision="mixed",
-                              m2l_path=0)
+                              m2l_path=3)
     assert rel(full.apply(X), simt.apply(X)) < 2e-6
+
+
+@pytest.mark.parametrize("name,order", [("LaplaceSingle", 152), ("ElasticTraction", 296)])
+def test_compressed_m2l(name, order):
+    """SVD-compressed M2L (the default path of the precision form) against
+    the uncompressed FP32 M2L on the same operators, and its transposed
+    apply against the forward one through <A x, z> = <x, A^T z>."""
+    from tbempy import ThreeD, meshes
+    locs, nrm, w = meshes.sphere_points(3)
+    cfg = ThreeD.FMMConfig(0.3, order, 40, 0.05, False)
+    K = kernel_obj(name)
+    comp = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed")
+    simt = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed", m2l_path=1)
+    n = comp.n_surface() * K.tensor_dim
+    ri, ro = comp.m2l_ranks()
+    assert 0 < ri <= n and 0 < ro <= n and ri * ro <= n * n // 2, (ri, ro, n)
+    assert ri % 16 == 0 or ri == n
+    assert simt.m2l_ranks() == (0, 0)
+    rng = np.random.default_rng(31)
+    X = rng.uniform(-1, 1, (3, comp.n_cols()))
+    assert rel(comp.apply(X), simt.apply(X)) < 1e-6
+    # a looser cut keeps fewer vectors and still approximates
+    loose = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed",
+                               m2l_rank_tol=1e-4)
+    li, lo = loose.m2l_ranks()
+    assert li <= ri and lo <= ro and li * lo < ri * ro
+    assert rel(loose.apply(X), simt.apply(X)) < 1e-3
+    Z = rng.uniform(-1, 1, (3, comp.n_rows()))
+    AX = comp.apply(X)
+    AtZ = comp.apply_adjoint(Z)
+    for r in range(3):
+        lhs, rhs = AX[r] @ Z[r], X[r] @ AtZ[r]
+        assert abs(lhs - rhs) <= 1e-6 * np.linalg.norm(AX[r]) * np.linalg.norm(Z[r])
 
 
 @pytest.mark.parametrize("name", ["LaplaceDouble", "ElasticDisplacement"])
