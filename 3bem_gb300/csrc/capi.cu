@@ -214,6 +214,7 @@ long tbem_fmm_p2p_block(const TbemFmm* h) { return h ? h->plan.p2p_tpt : TBEM_ER
 long tbem_fmm_tc_tile(const TbemFmm* h)
 {
     if (!h) return TBEM_ERR_ARG;
+    if (h->plan.f.use_tc_c) return h->plan.f.m2l_c.tc_bn;
     return h->plan.f.use_tc ? h->plan.f.m2l.tc_bn : 0;
 }
 

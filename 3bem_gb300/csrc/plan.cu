@@ -322,15 +322,15 @@ __global__ void convert_rows_kernel(const double* in, float* out, long rows, int
 }
 
 // the last r columns (largest eigenvalues) of a column-major n x n
-// eigenvector matrix -> row-major n x r FP32
-__global__ void basis_rows_kernel(const double* evec, int n, int r, float* out)
+// eigenvector matrix, times scale -> row-major n x r FP32
+__global__ void basis_rows_kernel(const double* evec, int n, int r, double scale, float* out)
 {
     const long total = (long)n * r;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long)gridDim.x * blockDim.x) {
         const long i = t / r;
         const int j = (int)(t % r);
-        out[t] = float(evec[(long)(n - r + j) * n + i]);
+        out[t] = float(scale * evec[(long)(n - r + j) * n + i]);
     }
 }
 
@@ -529,22 +529,28 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
 // lists with zero operands (the cost does not depend on the values).
 void Plan::autotune_tc()
 {
-    if (!f.use_tc || f.m2l.empty()) return;
+    const bool comp = f.use_tc_c && !f.m2l_c.empty();
+    if (!comp && (!f.use_tc || f.m2l.empty())) return;
     ensure_rhs(1);
     const long ncs = (long)stree->cells.size(), nco = (long)otree.cells.size();
-    TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * n, stream));
-    f.tc.split_b_rows(cu32.p, 0, ncs, std::max(ncs, nco), stream);
+    TcPlanes& P = comp ? f.tc_c : f.tc;
+    GemmSet& G = comp ? f.m2l_c : f.m2l;
+    float* in = comp ? cuc32.p : cu32.p;
+    float* out = comp ? cdc32.p : cd32.p;
+    const long nn = comp ? (long)f.r_out * f.r_in : (long)n * n;
+    TBEM_CK(cudaMemsetAsync(in, 0, sizeof(float) * ncs * P.k, stream));
+    P.split_b_rows(in, 0, ncs, std::max(ncs, nco), stream);
     cudaEvent_t e0, e1;
     TBEM_CK(cudaEventCreate(&e0));
     TBEM_CK(cudaEventCreate(&e1));
     float best = 1e30f;
     int best_bn = 128;
     for (int bn : {128, 64}) {
-        f.m2l.tc_bn = bn;
+        G.tc_bn = bn;
         float ms = 0.f;
         for (int rep = 0; rep < 3; rep++) {
             TBEM_CK(cudaEventRecord(e0, stream));
-            f.m2l.run_tc(f.tc, cd32.p, n, 1, 1, (long)n * n, stream, nullptr);
+            G.run_tc(P, out, 1, 1, nn, stream, nullptr);
             TBEM_CK(cudaEventRecord(e1, stream));
             TBEM_CK(cudaEventSynchronize(e1));
             float t = 0.f;
@@ -558,7 +564,7 @@ void Plan::autotune_tc()
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    f.m2l.tc_bn = best_bn;
+    G.tc_bn = best_bn;
     for (auto& g : f.m2m) g.tc_bn = best_bn;
     for (auto& g : f.l2l) g.tc_bn = best_bn;
 }
@@ -785,6 +791,7 @@ void Plan::build_c2e(Form& F)
     DBuf<SurfJob> dj;
     dj.alloc(jobs.size());
     TBEM_CK(cudaMemcpy(dj.p, jobs.data(), jobs.size() * sizeof(SurfJob), cudaMemcpyHostToDevice));
+    TBEM_CK(cudaStreamSynchronize(cudaStreamLegacy));
     dim3 g((unsigned)((ns * ns + 255) / 256), (unsigned)jobs.size());
     surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p, d_unit.p, ns, F.g_kid,
                                                make_kparams(F.g_kid, mu, nu), sys.p);
@@ -1020,6 +1027,7 @@ void Plan::build_plain_ops(Form& F)
         DBuf<SurfJob> dj;
         dj.alloc(jobs.size());
         TBEM_CK(cudaMemcpy(dj.p, jobs.data(), jobs.size() * sizeof(SurfJob), cudaMemcpyHostToDevice));
+        TBEM_CK(cudaStreamSynchronize(cudaStreamLegacy));
         for (size_t j0 = 0; j0 < jobs.size(); j0 += 32768) {
             unsigned nj = (unsigned)std::min<size_t>(32768, jobs.size() - j0);
             dim3 g((unsigned)((ns * ns + 255) / 256), nj);
@@ -1061,19 +1069,35 @@ void Plan::build_mixed_ops(Form& F)
                 job_ls[m2l_off[k] / nn] = S.cells[m2l_canon[k].second].level;
             }
     }
-    // m2l_path: 0 auto (compressed M2L where the operators are precomputed),
+    // m2l_path: 0 auto (compressed where the M2L operators are precomputed),
     // 1 SIMT FP32 for all, 2 tensor cores for the M2L only, 3 tensor cores for
-    // all, 4 compressed M2L
+    // all, 4 compressed, 5 compressed with the M2L products on tensor cores
     const int path = opt.m2l_path == 0 ? 4 : opt.m2l_path;
     // FP64 copies of the M2L kernel matrices for the compression (compact
     // index), scaled to the root level (see build_m2l_compression)
-    const bool compress = path == 4 && !F.m2l_on_the_fly && !m2l_off.empty();
+    const bool compress = (path == 4 || path == 5) && !F.m2l_on_the_fly && !m2l_off.empty();
     std::vector<long> m2l_index(jobs.size(), -1);
     long n_m2l_ops = 0;
     for (long off : m2l_off)
         if (off >= 0 && m2l_index[off / nn] < 0) m2l_index[off / nn] = n_m2l_ops++;
-    DBuf<double> U64;
-    if (compress) U64.alloc((size_t)n_m2l_ops * nn);
+    // and of the M2M kernel matrices / combined L2L operators (compact; the
+    // first key of a job is the one that built it)
+    std::vector<long> m2m_index(jobs.size(), -1), l2l_index(jobs.size(), -1);
+    std::vector<int> m2m_lc;
+    long n_m2m_ops = 0, n_l2l_ops = 0;
+    for (size_t k = 0; k < m2m_off.size(); k++)
+        if (m2m_off[k] >= 0 && m2m_index[m2m_off[k] / nn] < 0) {
+            m2m_index[m2m_off[k] / nn] = n_m2m_ops++;
+            m2m_lc.push_back(stree->cells[m2m_canon[k].second].level);
+        }
+    for (size_t k = 0; k < l2l_off.size(); k++)
+        if (l2l_off[k] >= 0 && l2l_index[l2l_off[k] / nn] < 0) l2l_index[l2l_off[k] / nn] = n_l2l_ops++;
+    DBuf<double> U64, KM, YL;
+    if (compress) {
+        U64.alloc((size_t)n_m2l_ops * nn);
+        KM.alloc(std::max<long>(n_m2m_ops, 1) * nn);
+        YL.alloc(std::max<long>(n_l2l_ops, 1) * nn);
+    }
     if (!jobs.empty()) {
         // in chunks to bound the FP64 scratch
         const size_t chunk = std::max<size_t>(1, (size_t)(2e9 / (8.0 * nn)));
@@ -1087,6 +1111,7 @@ void Plan::build_mixed_ops(Form& F)
             for (size_t k = 0; k < nj; k++) sub[k].out_off = (long)k * nn;
             dj.alloc(nj);
             TBEM_CK(cudaMemcpy(dj.p, sub.data(), nj * sizeof(SurfJob), cudaMemcpyHostToDevice));
+            TBEM_CK(cudaStreamSynchronize(cudaStreamLegacy));
             dim3 g((unsigned)((ns * ns + 255) / 256), (unsigned)nj);
             surf_matrix_kernel<<<g, 256, 0, stream>>>(dj.p, d_unit.p, ns, F.g_kid,
                                                        make_kparams(F.g_kid, mu, nu), K.p);
@@ -1108,17 +1133,37 @@ void Plan::build_mixed_ops(Form& F)
                         const double f = std::ldexp(1.0, -job_ls[j0 + k]);
                         TBEM_CKB(cublasDscal(cublas, (int)nn, &f, dst, 1));
                     }
+            if (compress)
+                for (size_t k = 0; k < nj; k++) {
+                    if (m2m_index[j0 + k] >= 0)
+                        TBEM_CK(cudaMemcpyAsync(KM.p + m2m_index[j0 + k] * nn, K.p + k * nn, sizeof(double) * nn,
+                                                cudaMemcpyDeviceToDevice, stream));
+                    if (l2l_index[j0 + k] >= 0)
+                        TBEM_CK(cudaMemcpyAsync(YL.p + l2l_index[j0 + k] * nn, Y.p + k * nn, sizeof(double) * nn,
+                                                cudaMemcpyDeviceToDevice, stream));
+                }
             TBEM_CK(cudaStreamSynchronize(stream));
         }
     }
     build_gemm_sets(F, 0, 0, 0, m2m_off, l2l_off, m2l_off);
     F.m2l_compressed = false;
-    if (compress) build_m2l_compression(F, U64.p, n_m2l_ops, m2l_index);
+    if (compress) {
+        CompressionInput in{U64.p, n_m2l_ops, &m2l_index, KM.p, &m2m_lc, &m2m_index,
+                            YL.p, &l2l_index, &m2m_off, &l2l_off};
+        build_compression(F, in);
+    }
     U64.release();
+    KM.release();
+    YL.release();
+    if (F.m2l_compressed && path == 5) {
+        F.use_tc_c = true;
+        F.tc_c.build(F.Cops.p, n_m2l_ops, F.r_out, F.r_in, stream);
+        TBEM_CK(cudaStreamSynchronize(stream));
+    }
     F.use_tc = (path == 2 || path == 3) && !jobs.empty();
     F.use_tc_updown = F.use_tc && path == 3;
     if (F.use_tc) {
-        F.tc.build(F.ops32.p, (long)jobs.size(), n, stream);
+        F.tc.build(F.ops32.p, (long)jobs.size(), n, n, stream);
         TBEM_CK(cudaStreamSynchronize(stream));
     }
 
@@ -1140,7 +1185,9 @@ void Plan::build_mixed_ops(Form& F)
         rows += cc.n_points() * R;
     }
     F.n_l2p = (int)cell.size();
-    F.E_ld = (n + 127) / 128 * 128;
+    // compressed form: E V, taking the r_out downward coefficients directly
+    const int ecols = F.m2l_compressed ? F.r_out : n;
+    F.E_ld = (ecols + 127) / 128 * 128;
     if (F.E_ld > 2048) throw Error(TBEM_ERR_ARG, "translation surface too large for the L2P kernel");
     F.E.alloc(std::max<long>(rows * F.E_ld, 1));
     F.E_row0.upload(row0);
@@ -1149,7 +1196,7 @@ void Plan::build_mixed_ops(Form& F)
     F.E_npts.upload(npts);
     if (rows > 0) {
         const long max_rows = std::max<long>((long)R * 64, (long)(1.5e9 / (8.0 * n)));
-        DBuf<double> K, Y;
+        DBuf<double> K, Y, EV;
         // chunks of consecutive leaves of one level
         size_t t0 = 0;
         while (t0 < cell.size()) {
@@ -1173,42 +1220,65 @@ void Plan::build_mixed_ops(Form& F)
             TBEM_CK(cudaGetLastError());
             TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)r, n, &one,
                                  F.c2e.p + F.c2e_dn_off[lev], n, K.p, n, &zero, Y.p, n));
-            convert_rows_kernel<<<grid_for(r * F.E_ld), 256, 0, stream>>>(Y.p, F.E.p + row0[t0] * F.E_ld,
-                                                                         r, n, F.E_ld);
+            if (F.m2l_compressed) {
+                // row-major E V (r x r_out) = column-major V^T E^T
+                EV.ensure(r * F.r_out);
+                TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, F.r_out, (int)r, n, &one, F.V64.p, n,
+                                     Y.p, n, &zero, EV.p, F.r_out));
+                convert_rows_kernel<<<grid_for(r * F.E_ld), 256, 0, stream>>>(EV.p, F.E.p + row0[t0] * F.E_ld,
+                                                                             r, F.r_out, F.E_ld);
+            } else {
+                convert_rows_kernel<<<grid_for(r * F.E_ld), 256, 0, stream>>>(Y.p, F.E.p + row0[t0] * F.E_ld,
+                                                                             r, n, F.E_ld);
+            }
             TBEM_CK(cudaGetLastError());
             TBEM_CK(cudaStreamSynchronize(stream));
             t0 = t1;
         }
     }
+    F.V64.release();
 }
 
-// SVD-compressed M2L (Fong & Darve, J. Comput. Phys. 228 (2009) 8712-8725,
-// sec. 3.3).  The M2L operator of a pair is U = T C2E_up(l_s): the kernel
-// matrix T (down-check surface of the target <- up-equivalent surface of the
-// source) times the source level's check-to-equivalent operator.  The bases
-// come from the kernel matrices, not from U: the pseudo-inverse magnifies the
-// directions the check potentials never carry, which would make U look full
-// rank.  Both translation kernels are homogeneous of degree -1, so a pair at
-// source level l_s has T = 2^l_s T0 with T0 the root-scaled matrix of its
-// (level difference, offset) class, and
-//   U = T0 (2^l_s C2E_up(l_s)) ~= V (V^T T0 W) (W^T 2^l_s C2E_up(l_s))
-//     = V C_k P_(l_s),
+// The compressed precision form.  The bases are those of SVD-compressed M2L
+// (Fong & Darve, J. Comput. Phys. 228 (2009) 8712-8725, sec. 3.3), taken from
+// the M2L kernel matrices T (down-check surface of the target <- up-
+// equivalent surface of the source), not from the combined operators
+// T C2E_up: the pseudo-inverse magnifies directions the check potentials
+// never carry, which would make those look full rank.  Both translation
+// kernels are homogeneous of degree -1, so a pair at source level l_s has
+// T = 2^l_s T0 with T0 the root-scaled matrix of its (level difference,
+// offset) class, and
+//   T C2E_up(l_s) = T0 (2^l_s C2E_up(l_s)) ~= V (V^T T0 W) (W^T 2^l_s C2E_up(l_s))
+//                 = V C_k P_(l_s),
 // W the leading eigenvectors of sum_k T0_k^T T0_k (input side), V those of
 // sum_k T0_k T0_k^T (output side), cut where the eigenvalue falls below
 // tol^2 times the largest (singular values of the stacks below tol times the
 // largest).  r_out is rounded up to the GEMM's 64-row tile and r_in to its
-// 16-deep k step: the extra vectors cost nothing in the M2L products.  The
-// M2L then runs as compress (P_l, once per source cell), r_out x r_in
-// products C_k per pair, and decompress (V, once per target cell).  U64
-// holds the root-scaled T0 of every M2L class (compact index).
-void Plan::build_m2l_compression(Form& F, const double* U64, long n_ops,
-                                 const std::vector<long>& op_index)
+// 16-deep k step: the extra vectors cost nothing in the products.
+//
+// The whole far field then lives in these bases.  A source cell carries
+// u~ = P_l u (u its up-check potentials): its root-scaled equivalent density
+// q0 = 2^l C2E_up(l) u seen through W.  The M2M of child c (level l_c) into
+// parent p (level l_p) adds K q_c to the parent's check potentials (K the
+// kernel matrix parent up-check <- child up-equivalent), with
+// q_c ~= 2^-l_c W u~_c, so u~_p += X u~_c with X = P_(l_p) K W 2^-l_c.
+// Dropping the part of q_c outside W is what the M2L drops as well: a
+// translation to a farther, larger cell only maps expansion content of a
+// given order into content of the same or higher order.  A target cell
+// carries d~ with its down-check potentials d ~= V d~; the L2L combined
+// operator L (child down-check <- parent down-check) becomes V^T L V and the
+// L2P operator E of a leaf becomes E V.  Source points reaching a target's
+// down-check surface directly (P2L) enter through V^T; the equivalent
+// densities of an M2P source are 2^-l W u~.
+void Plan::build_compression(Form& F, const CompressionInput& in)
 {
     if (F.g_kid != LAP_S && F.g_kid != EL_DISP)
-        throw Error(TBEM_ERR_STATE, "compressed M2L needs a degree -1 translation kernel");
+        throw Error(TBEM_ERR_STATE, "compressed form needs a degree -1 translation kernel");
     const long nn = (long)n * n;
     const double one = 1.0, zero = 0.0;
     const double tol = opt.m2l_rank_tol > 0 ? opt.m2l_rank_tol : 1e-7;
+    const double* T0 = in.T0;
+    const long n_ops = in.n_m2l;
     DBuf<double> Gi, Go;
     Gi.alloc(nn);
     Go.alloc(nn);
@@ -1219,12 +1289,12 @@ void Plan::build_m2l_compression(Form& F, const double* U64, long n_ops,
         const long kb = std::min(step, n_ops - k0);
         const double beta = k0 == 0 ? 0.0 : 1.0;
         TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, n, (int)(kb * n), &one,
-                             U64 + k0 * nn, n, &beta, Gi.p, n));
+                             T0 + k0 * nn, n, &beta, Gi.p, n));
     }
     // G_out = sum_k T_k T_k^T: one rank-n update per matrix
     for (long k = 0; k < n_ops; k++) {
         const double beta = k == 0 ? 0.0 : 1.0;
-        TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, n, n, &one, U64 + k * nn, n,
+        TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, n, n, &one, T0 + k * nn, n,
                              &beta, Go.p, n));
     }
     // eigenvectors (ascending eigenvalues) overwrite the Gram matrices
@@ -1260,82 +1330,160 @@ void Plan::build_m2l_compression(Form& F, const double* U64, long n_ops,
     F.r_out = ro;
     const double* W = Gi.p + (long)(n - ri) * n;  // column-major n x ri
     const double* V = Go.p + (long)(n - ro) * n;  // column-major n x ro
+    F.V64.alloc((size_t)n * ro);
+    TBEM_CK(cudaMemcpyAsync(F.V64.p, V, sizeof(double) * n * ro, cudaMemcpyDeviceToDevice, stream));
     F.Vb.alloc((size_t)n * ro);
-    basis_rows_kernel<<<grid_for((long)n * ro), 256, 0, stream>>>(Go.p, n, ro, F.Vb.p);
+    basis_rows_kernel<<<grid_for((long)n * ro), 256, 0, stream>>>(Go.p, n, ro, 1.0, F.Vb.p);
     TBEM_CK(cudaGetLastError());
-    // compress operators P_l = 2^l W^T C2E_up(l), row-major ri x n = the
-    // column-major n x ri product 2^l C2E_up(l)^T W (C2E_up(l)^T being the
-    // column-major view of the stored operator)
     const Tree& S = *stree;
-    const int LS = S.n_levels();
-    {
-        DBuf<double> Pl;
-        Pl.alloc((size_t)n * ri);
-        F.Wb.alloc((size_t)LS * n * ri);
-        for (int l = 0; l < LS; l++) {
-            const double f = std::ldexp(1.0, l);
-            TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ri, n, &f, F.c2e.p + F.c2e_up_off[l],
-                                 n, W, n, &zero, Pl.p, n));
-            convert_kernel<float><<<grid_for((long)n * ri), 256, 0, stream>>>(Pl.p, F.Wb.p + (long)l * n * ri,
-                                                                             (long)n * ri);
-            TBEM_CK(cudaGetLastError());
-        }
-        TBEM_CK(cudaStreamSynchronize(stream));
+    const Tree& O = otree;
+    const int LS = S.n_levels(), LO = O.n_levels();
+    // P_l = 2^l W^T C2E_up(l), row-major ri x n = the column-major n x ri
+    // product 2^l C2E_up(l)^T W (C2E_up(l)^T being the column-major view of
+    // the stored operator); kept in FP64 for the M2M operators
+    DBuf<double> P64;
+    P64.alloc((size_t)LS * n * ri);
+    F.Pb.alloc((size_t)LS * n * ri);
+    F.Wl.alloc((size_t)LS * n * ri);
+    for (int l = 0; l < LS; l++) {
+        const double f = std::ldexp(1.0, l);
+        TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ri, n, &f, F.c2e.p + F.c2e_up_off[l], n, W,
+                             n, &zero, P64.p + (long)l * n * ri, n));
+        basis_rows_kernel<<<grid_for((long)n * ri), 256, 0, stream>>>(Gi.p, n, ri, std::ldexp(1.0, -l),
+                                                                     F.Wl.p + (long)l * n * ri);
+        TBEM_CK(cudaGetLastError());
     }
+    convert_kernel<float><<<grid_for((long)LS * n * ri), 256, 0, stream>>>(P64.p, F.Pb.p, (long)LS * n * ri);
+    TBEM_CK(cudaGetLastError());
     // C_k (row-major ro x ri) = column-major C_k^T = W^T T_k^T V, T_k^T being
     // the column-major view of the stored matrix
     const long cc = (long)ro * ri;
     F.Cops.alloc((size_t)n_ops * cc);
     const long cb = std::max<long>(1, std::min<long>(n_ops, (long)(1e9 / (8.0 * n * ro))));
+    const long n_m2m = (long)in.m2m_lc->size();
+    long n_l2l = 0;
+    for (long v : *in.l2l_index) n_l2l = std::max(n_l2l, v + 1);
     DBuf<double> P, CT;
-    P.alloc((size_t)cb * n * ro);
-    CT.alloc((size_t)cb * cc);
+    P.alloc((size_t)cb * n * std::max(ro, ri));
+    CT.alloc((size_t)std::max(cb * cc, std::max(n_m2m * ri * ri, n_l2l * ro * ro)));
     for (long k0 = 0; k0 < n_ops; k0 += cb) {
         const long kb = std::min(cb, n_ops - k0);
         TBEM_CKB(cublasDgemmStridedBatched(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ro, n, &one,
-                                           U64 + k0 * nn, n, nn, V, n, 0, &zero, P.p, n,
+                                           T0 + k0 * nn, n, nn, V, n, 0, &zero, P.p, n,
                                            (long long)n * ro, (int)kb));
         TBEM_CKB(cublasDgemmStridedBatched(cublas, CUBLAS_OP_T, CUBLAS_OP_N, ri, ro, n, &one, W, n, 0,
                                            P.p, n, (long long)n * ro, &zero, CT.p, ri, cc, (int)kb));
         convert_kernel<float><<<grid_for(kb * cc), 256, 0, stream>>>(CT.p, F.Cops.p + k0 * cc, kb * cc);
         TBEM_CK(cudaGetLastError());
+        TBEM_CK(cudaStreamSynchronize(stream));
+    }
+    // X (row-major ri x ri) = column-major X^T = 2^-l_c W^T (K^T P_(l_p)^T)
+    F.Xops.alloc(std::max<long>(n_m2m, 1) * ri * ri);
+    for (long j = 0; j < n_m2m; j++) {
+        const int lc = (*in.m2m_lc)[j], lp = lc - 1;
+        const double f = std::ldexp(1.0, -lc);
+        TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ri, n, &one, in.KM + j * nn, n,
+                             P64.p + (long)lp * n * ri, n, &zero, P.p, n));
+        TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, ri, ri, n, &f, W, n, P.p, n, &zero,
+                             CT.p + j * (long)ri * ri, ri));
+    }
+    if (n_m2m > 0) {
+        convert_kernel<float><<<grid_for(n_m2m * ri * ri), 256, 0, stream>>>(CT.p, F.Xops.p, n_m2m * ri * ri);
+        TBEM_CK(cudaGetLastError());
     }
     TBEM_CK(cudaStreamSynchronize(stream));
-    // the compressed sets: F.m2l's groups on the C_k pool; the compress sets
-    // pair every M2L source cell with itself (one group per level: P_l), the
-    // decompress set every M2L target cell (one group: V)
+    // Y (row-major ro x ro) = column-major Y^T = V^T (L^T V), L^T the
+    // column-major view of the combined operator
+    F.Yops.alloc(std::max<long>(n_l2l, 1) * ro * ro);
+    for (long j = 0; j < n_l2l; j++) {
+        TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ro, n, &one, in.YL + j * nn, n, V, n,
+                             &zero, P.p, n));
+        TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, ro, ro, n, &one, V, n, P.p, n, &zero,
+                             CT.p + j * (long)ro * ro, ro));
+    }
+    if (n_l2l > 0) {
+        convert_kernel<float><<<grid_for(n_l2l * ro * ro), 256, 0, stream>>>(CT.p, F.Yops.p, n_l2l * ro * ro);
+        TBEM_CK(cudaGetLastError());
+    }
+    TBEM_CK(cudaStreamSynchronize(stream));
+
+    // GEMM sets.  M2L: F.m2l's groups on the C_k pool.
+    auto swap_pairs = [](const std::vector<std::pair<int, int>>& v) {
+        std::vector<std::pair<int, int>> o(v.size());
+        for (size_t i = 0; i < v.size(); i++) o[i] = {v[i].second, v[i].first};
+        return o;
+    };
     F.m2l_c = GemmSet();
     F.m2l_c_t = GemmSet();
-    F.comp_src = GemmSet();
-    F.comp_obs = GemmSet();
-    std::vector<char> is_src(S.cells.size(), 0), is_obs(otree.cells.size(), 0);
     for (size_t g = 0; g < F.m2l.A_off.size(); g++) {
-        std::vector<std::pair<int, int>> pr, pt;
-        for (long p = F.m2l.pair0[g]; p < F.m2l.pair0[g] + F.m2l.npairs[g]; p++) {
+        std::vector<std::pair<int, int>> pr;
+        for (long p = F.m2l.pair0[g]; p < F.m2l.pair0[g] + F.m2l.npairs[g]; p++)
             pr.push_back({F.m2l.in_cell[p], F.m2l.out_cell[p]});
-            pt.push_back({F.m2l.out_cell[p], F.m2l.in_cell[p]});
-            is_src[F.m2l.in_cell[p]] = 1;
-            is_obs[F.m2l.out_cell[p]] = 1;
-        }
-        const long idx = op_index[F.m2l.A_off[g] / nn];
+        const long idx = (*in.m2l_index)[F.m2l.A_off[g] / nn];
         if (idx < 0) throw Error(TBEM_ERR_STATE, "M2L operator without a compressed copy");
         F.m2l_c.add_group(idx * cc, pr);
-        F.m2l_c_t.add_group(idx * cc, pt);
+        F.m2l_c_t.add_group(idx * cc, swap_pairs(pr));
     }
+    // M2M / L2L per level and octant on the X / Y pools
+    F.m2m_c.clear();
+    F.m2m_c.resize(std::max(LS, 0));
+    F.m2m_c_t.clear();
+    F.m2m_c_t.resize(std::max(LS, 0));
+    for (int l = 0; l < LS; l++)
+        for (int o = 0; o < 8; o++) {
+            const int key = l * 8 + o;
+            const long off = (*in.m2m_off)[key];
+            if (off < 0) continue;
+            const long idx = (*in.m2m_index)[off / nn];
+            F.m2m_c[l].add_group(idx * ri * ri, m2m_pairs[key]);
+            F.m2m_c_t[l].add_group(idx * ri * ri, swap_pairs(m2m_pairs[key]));
+        }
+    F.l2l_c.clear();
+    F.l2l_c.resize(std::max(LO, 0));
+    F.l2l_c_t.clear();
+    F.l2l_c_t.resize(std::max(LO, 0));
+    for (int l = 0; l < LO; l++)
+        for (int o = 0; o < 8; o++) {
+            const int key = l * 8 + o;
+            const long off = (*in.l2l_off)[key];
+            if (off < 0) continue;
+            const long idx = (*in.l2l_index)[off / nn];
+            F.l2l_c[l].add_group(idx * ro * ro, l2l_pairs[key]);
+            F.l2l_c_t[l].add_group(idx * ro * ro, swap_pairs(l2l_pairs[key]));
+        }
+    // compress the P2M cells (P_l per level), rebuild the densities of the M2P
+    // sources (2^-l W per level), move the P2L targets through V
+    F.comp_p2m = GemmSet();
+    F.decomp_m2p = GemmSet();
+    F.comp_p2l = GemmSet();
+    std::vector<char> is_p2m(S.cells.size(), 0), is_m2p(S.cells.size(), 0), is_p2l(O.cells.size(), 0);
+    for (int c : L.p2m) is_p2m[c] = 1;
+    for (const auto& pr : L.m2p) is_m2p[pr.src] = 1;
+    for (const auto& pr : L.p2l) is_p2l[pr.obs] = 1;
     for (int l = 0; l < LS; l++) {
-        std::vector<std::pair<int, int>> ps;
-        for (int c = S.level_start[l]; c < S.level_start[l + 1]; c++)
-            if (is_src[c]) ps.push_back({c, c});
-        F.comp_src.add_group((long)l * n * ri, ps);
+        std::vector<std::pair<int, int>> a, b;
+        for (int c = S.level_start[l]; c < S.level_start[l + 1]; c++) {
+            if (is_p2m[c]) a.push_back({c, c});
+            if (is_m2p[c]) b.push_back({c, c});
+        }
+        F.comp_p2m.add_group((long)l * n * ri, a);
+        F.decomp_m2p.add_group((long)l * n * ri, b);
     }
-    std::vector<std::pair<int, int>> po;
-    for (int c = 0; c < (int)is_obs.size(); c++)
-        if (is_obs[c]) po.push_back({c, c});
-    F.comp_obs.add_group(0, po);
+    {
+        std::vector<std::pair<int, int>> a;
+        for (int c = 0; c < (int)O.cells.size(); c++)
+            if (is_p2l[c]) a.push_back({c, c});
+        F.comp_p2l.add_group(0, a);
+    }
     F.m2l_c.upload(F.Cops.p, sizeof(float));
     F.m2l_c_t.upload(F.Cops.p, sizeof(float));
-    F.comp_src.upload(F.Wb.p, sizeof(float));
-    F.comp_obs.upload(F.Vb.p, sizeof(float));
+    for (auto& g : F.m2m_c) g.upload(F.Xops.p, sizeof(float));
+    for (auto& g : F.m2m_c_t) g.upload(F.Xops.p, sizeof(float));
+    for (auto& g : F.l2l_c) g.upload(F.Yops.p, sizeof(float));
+    for (auto& g : F.l2l_c_t) g.upload(F.Yops.p, sizeof(float));
+    F.comp_p2m.upload(F.Pb.p, sizeof(float));
+    F.decomp_m2p.upload(F.Wl.p, sizeof(float));
+    F.comp_p2l.upload(F.Vb.p, sizeof(float));
     F.m2l_compressed = true;
 }
 
@@ -1345,8 +1493,10 @@ void Plan::set_c2e(int which, long level, const double* op)
     if (f.mixed) throw Error(TBEM_ERR_STATE, "set_c2e is only valid for the FP64 form");
     const auto& offs = which == 0 ? f.c2e_up_off : f.c2e_dn_off;
     if (level < 0 || level >= (long)offs.size()) throw Error(TBEM_ERR_ARG, "level out of range");
+    TBEM_CK(cudaStreamSynchronize(stream));
     TBEM_CK(cudaMemcpy(f.c2e.p + offs[level], op, (size_t)n * n * sizeof(double),
                        cudaMemcpyHostToDevice));
+    TBEM_CK(cudaStreamSynchronize(cudaStreamLegacy));
 }
 
 void Plan::get_c2e(int which, long level, double* out) const
@@ -1354,6 +1504,7 @@ void Plan::get_c2e(int which, long level, double* out) const
     if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
     const auto& offs = which == 0 ? f.c2e_up_off : f.c2e_dn_off;
     if (level < 0 || level >= (long)offs.size()) throw Error(TBEM_ERR_ARG, "level out of range");
+    TBEM_CK(cudaStreamSynchronize(stream));
     TBEM_CK(cudaMemcpy(out, f.c2e.p + offs[level], (size_t)n * n * sizeof(double),
                        cudaMemcpyDeviceToHost));
 }
@@ -1451,7 +1602,9 @@ void Plan::forward(int nrhs, cudaStream_t s)
     Form& F = f;
     mark("start", s);
     TBEM_CK(cudaMemsetAsync(y64.p, 0, sizeof(double) * R * NO * nrhs, s));
-    if (!F.mixed) {
+    if (F.mixed && F.m2l_compressed) {
+        forward_compressed(nrhs, s);
+    } else if (!F.mixed) {
         gather_kernel<double><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s64.p, NS, R, nrhs);
         TBEM_CK(cudaGetLastError());
         launches++;
@@ -1499,7 +1652,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
                 const long rn = (long)(S.level_start[l + 2] - S.level_start[l + 1]) * nrhs;
                 F.tc.split_b_rows(cu32.p, r0, rn, ncs * nrhs, s);
                 launches++;
-                F.m2m[l].run_tc(F.tc, cu32.p, n, nrhs, 1, (long)n * n, s, &launches);
+                F.m2m[l].run_tc(F.tc, cu32.p, nrhs, 1, (long)n * n, s, &launches);
             } else {
                 F.m2m[l].run<float>(cu32.p, cu32.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
             }
@@ -1524,18 +1677,10 @@ void Plan::forward(int nrhs, cudaStream_t s)
             add_kernel<<<grid_for(nco * nrhs * n), 256, 0, s>>>(cd64.p, cd32.p, nco * nrhs * n);
             TBEM_CK(cudaGetLastError());
             launches++;
-        } else if (F.m2l_compressed) {
-            // compress (P_l per source cell), r_out x r_in products, decompress
-            // (V per target cell, added to the down-check potentials)
-            const int ri = F.r_in, ro = F.r_out;
-            F.comp_src.run_rect<float>(cu32.p, cuc32.p, ri, n, n, nrhs, 0, GEMM_STORE, s, &launches);
-            TBEM_CK(cudaMemsetAsync(cdc32.p, 0, sizeof(float) * nco * nrhs * ro, s));
-            F.m2l_c.run_rect<float>(cuc32.p, cdc32.p, ro, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
-            F.comp_obs.run_rect<float>(cdc32.p, cd32.p, n, ro, ro, nrhs, 0, GEMM_ADD, s, &launches);
         } else if (F.use_tc) {
             F.tc.split_b_rows(cu32.p, 0, ncs * nrhs, std::max(ncs, nco) * nrhs, s);
             launches++;
-            F.m2l.run_tc(F.tc, cd32.p, n, nrhs, 1, (long)n * n, s, &launches);
+            F.m2l.run_tc(F.tc, cd32.p, nrhs, 1, (long)n * n, s, &launches);
         } else {
             F.m2l.run<float>(cu32.p, cd32.p, n, nrhs, 0, GEMM_ATOMIC, s, &launches);
         }
@@ -1548,7 +1693,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
                 const long rn = (long)(O.level_start[l] - O.level_start[l - 1]) * nrhs;
                 F.tc.split_b_rows(cd32.p, r0, rn, std::max(ncs, nco) * nrhs, s);
                 launches++;
-                F.l2l[l - 1].run_tc(F.tc, cd32.p, n, nrhs, 0, (long)n * n, s, &launches);
+                F.l2l[l - 1].run_tc(F.tc, cd32.p, nrhs, 0, (long)n * n, s, &launches);
             } else {
                 F.l2l[l - 1].run<float>(cd32.p, cd32.p, n, nrhs, 0, GEMM_ADD, s, &launches);
             }
@@ -1578,7 +1723,9 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
     // y64 holds the transposed inputs (observation space, tree order), s64 the
     // accumulated outputs (source space) before the weights
     TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * NS * nrhs, s));
-    if (!F.mixed) {
+    if (F.mixed && F.m2l_compressed) {
+        adjoint_compressed(nrhs, s);
+    } else if (!F.mixed) {
         gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
         TBEM_CK(cudaGetLastError());
         launches++;
@@ -1632,13 +1779,6 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
             TBEM_CK(cudaGetLastError());
             launches++;
             eval<double>(m2l_fly_t, F.g_kid, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
-        } else if (F.m2l_compressed) {
-            // U^T ~= P_l^T C_k^T V^T: V^T per target cell, C_k^T per pair, P_l^T per source cell
-            const int ri = F.r_in, ro = F.r_out;
-            F.comp_obs.run_rect<float>(cd32.p, cdc32.p, ro, n, ro, nrhs, 1, GEMM_STORE, s, &launches);
-            TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
-            F.m2l_c_t.run_rect<float>(cdc32.p, cuc32.p, ri, ro, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
-            F.comp_src.run_rect<float>(cuc32.p, cu32.p, n, ri, n, nrhs, 1, GEMM_ADD, s, &launches);
         } else {
             F.m2l_t.run<float>(cd32.p, cu32.p, n, nrhs, 1, GEMM_ATOMIC, s, &launches);
         }
@@ -1658,6 +1798,109 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
     TBEM_CK(cudaGetLastError());
     launches++;
     mark("scatter", s);
+}
+
+// The compressed precision form (see build_compression): the same passes as
+// the uncompressed one with every cell state in the SVD bases.
+void Plan::forward_compressed(int nrhs, cudaStream_t s)
+{
+    const Tree& S = *stree;
+    const Tree& O = otree;
+    const long NS = n_src, NO = n_obs;
+    const long ncs = (long)S.cells.size(), nco = (long)O.cells.size();
+    Form& F = f;
+    const int ri = F.r_in, ro = F.r_out;
+    gather_kernel<float><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s32.p, NS, R, nrhs);
+    TBEM_CK(cudaGetLastError());
+    launches++;
+    TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
+    TBEM_CK(cudaMemsetAsync(cdc32.p, 0, sizeof(float) * nco * nrhs * ro, s));
+    mark("gather", s);
+    // P2M into the leaves' check potentials, then u~ = P_l u
+    eval<float>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
+    F.comp_p2m.run_rect<float>(cu32.p, cuc32.p, ri, n, n, nrhs, 0, GEMM_STORE, s, &launches);
+    mark("p2m", s);
+    for (int l = S.n_levels() - 1; l >= 0; l--)
+        if (l < (int)F.m2m_c.size()) F.m2m_c[l].run_rect<float>(cuc32.p, cuc32.p, ri, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
+    mark("m2m", s);
+    eval<float>(p2p_set(), kid, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
+    mark("p2p", s);
+    if (!L.m2p.empty()) {
+        // equivalent densities 2^-l W u~ of the M2P sources, evaluated in FP64
+        F.decomp_m2p.run_rect<float>(cuc32.p, cu32.p, n, ri, ri, nrhs, 0, GEMM_STORE, s, &launches);
+        promote_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu32.p, qu64.p, ncs * nrhs * n);
+        TBEM_CK(cudaGetLastError());
+        launches++;
+        eval<double>(m2p, F.kt_kid, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+    }
+    if (!L.p2l.empty()) {
+        TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
+        eval<float>(p2l, F.ks_kid, true, false, O, dobs, F.r_dc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cd32.p, 1, nrhs, s, false);
+        F.comp_p2l.run_rect<float>(cd32.p, cdc32.p, ro, n, ro, nrhs, 1, GEMM_ADD, s, &launches);
+    }
+    mark("m2p+p2l", s);
+    if (F.use_tc_c) {
+        F.tc_c.split_b_rows(cuc32.p, 0, ncs * nrhs, std::max(ncs, nco) * nrhs, s);
+        launches++;
+        F.m2l_c.run_tc(F.tc_c, cdc32.p, nrhs, 1, (long)ro * ri, s, &launches);
+    } else {
+        F.m2l_c.run_rect<float>(cuc32.p, cdc32.p, ro, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
+    }
+    mark("m2l", s);
+    for (int l = 1; l < O.n_levels(); l++)
+        if (l - 1 < (int)F.l2l_c.size()) F.l2l_c[l - 1].run_rect<float>(cdc32.p, cdc32.p, ro, ro, ro, nrhs, 0, GEMM_ADD, s, &launches);
+    mark("l2l", s);
+    if (F.n_l2p > 0) {
+        l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cdc32.p, ro, F.E_ld, R, nrhs, y64.p, NO);
+        TBEM_CK(cudaGetLastError());
+        launches++;
+    }
+    mark("l2p", s);
+}
+
+void Plan::adjoint_compressed(int nrhs, cudaStream_t s)
+{
+    const Tree& S = *stree;
+    const Tree& O = otree;
+    const long NS = n_src, NO = n_obs;
+    const long ncs = (long)S.cells.size(), nco = (long)O.cells.size();
+    Form& F = f;
+    const int ri = F.r_in, ro = F.r_out;
+    gather_kernel<float><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, s32.p, NO, R, nrhs);
+    TBEM_CK(cudaGetLastError());
+    launches++;
+    TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
+    TBEM_CK(cudaMemsetAsync(cdc32.p, 0, sizeof(float) * nco * nrhs * ro, s));
+    if (F.n_l2p > 0) {
+        l2p_mixed_t_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, s32.p, NO, ro, F.E_ld, R, nrhs, cdc32.p);
+        TBEM_CK(cudaGetLastError());
+        launches++;
+    }
+    eval<float>(p2p_t, kid, false, false, S, *dsrc, 0, dobs, 0, s32.p, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
+    for (int l = O.n_levels() - 1; l >= 1; l--)
+        if (l - 1 < (int)F.l2l_c_t.size()) F.l2l_c_t[l - 1].run_rect<float>(cdc32.p, cdc32.p, ro, ro, ro, nrhs, 1, GEMM_ATOMIC, s, &launches);
+    F.m2l_c_t.run_rect<float>(cdc32.p, cuc32.p, ri, ro, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
+    if (!L.p2l.empty()) {
+        F.comp_p2l.run_rect<float>(cdc32.p, cd32.p, n, ro, ro, nrhs, 0, GEMM_STORE, s, &launches);
+        eval<float>(p2l_t, F.ks_kid, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+    }
+    if (!L.m2p.empty()) {
+        // density gradients in FP64, folded into u~ through (2^-l W)^T
+        TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
+        gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
+        TBEM_CK(cudaGetLastError());
+        launches++;
+        eval<double>(m2p_t, F.kt_kid, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
+        TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
+        add_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(qu64.p, cu32.p, ncs * nrhs * n);
+        TBEM_CK(cudaGetLastError());
+        launches++;
+        F.decomp_m2p.run_rect<float>(cu32.p, cuc32.p, ri, n, ri, nrhs, 1, GEMM_ADD, s, &launches);
+    }
+    for (int l = 0; l < S.n_levels(); l++)
+        if (l < (int)F.m2m_c_t.size()) F.m2m_c_t[l].run_rect<float>(cuc32.p, cuc32.p, ri, ri, ri, nrhs, 1, GEMM_ADD, s, &launches);
+    F.comp_p2m.run_rect<float>(cuc32.p, cu32.p, n, ri, n, nrhs, 1, GEMM_STORE, s, &launches);
+    eval<float>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
 }
 
 void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
@@ -1693,9 +1936,10 @@ void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
                             y_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     if (!y_dev || timing) {
         TBEM_CK(cudaStreamSynchronize(s));
-        if (f.use_tc) {
+        for (const TcPlanes* P : {&f.tc, &f.tc_c}) {
+            if (!P->err.p) continue;
             int flag = 0;
-            TBEM_CK(cudaMemcpy(&flag, f.tc.err.p, sizeof(int), cudaMemcpyDeviceToHost));
+            TBEM_CK(cudaMemcpy(&flag, P->err.p, sizeof(int), cudaMemcpyDeviceToHost));
             if (flag) throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
         }
     }

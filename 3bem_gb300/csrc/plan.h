@@ -74,15 +74,24 @@ struct DBuf {
     {
         if (count > n) alloc(count);
     }
+    // Setup-time copies.  The plans compute on non-blocking streams, which a
+    // plain cudaMemcpy (legacy default stream) does not order against: an
+    // upload waits for its DMA to land, a download for all device work.
     void upload(const std::vector<T>& v)
     {
         alloc(v.size());
-        if (!v.empty()) TBEM_CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (!v.empty()) {
+            TBEM_CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+            TBEM_CK(cudaStreamSynchronize(cudaStreamLegacy));
+        }
     }
     std::vector<T> download() const
     {
         std::vector<T> v(n);
-        if (n) TBEM_CK(cudaMemcpy(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
+        if (n) {
+            TBEM_CK(cudaDeviceSynchronize());
+            TBEM_CK(cudaMemcpy(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
+        }
         return v;
     }
 };
@@ -125,12 +134,12 @@ struct TaskSet {
 // Three-term bf16 planes of the precision form's FP32 operators, padded for
 // the tensor-core GEMM (tc_gemm.cu), plus the split of the current B operand.
 struct TcPlanes {
-    int n = 0, m_pad = 0, k_pad = 0;
+    int m = 0, k = 0, m_pad = 0, k_pad = 0;  // operators m x k (row-major)
     DBuf<__nv_bfloat16> a[3], b[3];
     DBuf<int> err;  // set by a tensor-core GEMM whose bounded wait gave up
-    void build(const float* ops32, long n_ops, int n, cudaStream_t s);
+    void build(const float* ops32, long n_ops, int m, int k, cudaStream_t s);
     void split_b(const float* cells, long rows, cudaStream_t s);
-    // split only rows [row0, row0 + rows) of a [rows_total][n] buffer into
+    // split only rows [row0, row0 + rows) of a [rows_total][k] buffer into
     // the same rows of the planes (capacity for rows_total rows)
     void split_b_rows(const float* cells, long row0, long rows, long rows_total, cudaStream_t s);
 };
@@ -164,11 +173,12 @@ struct GemmSet {
     template <typename T>
     void run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int trans, int mode,
                   cudaStream_t s, long* launches = nullptr);
-    // tensor-core path (B taken from P's split planes); nn = elements per operator
+    // tensor-core path (B taken from P's split planes; D columns of P.m rows);
+    // nn = elements per operator in the pool the groups' offsets refer to
     DBuf<int> d_op;
     std::map<int, std::pair<DBuf<int>, DBuf<int>>> tc_tiles;
     int tc_bn = 128;  // N tile of the tensor-core path (128 or 64; autotuned)
-    void run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, long nn, cudaStream_t s,
+    void run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn, cudaStream_t s,
                 long* launches);
 };
 
@@ -201,16 +211,27 @@ struct Form {
     // mixed: tensor-core planes of ops32 (M2L on tcgen05 when use_tc)
     TcPlanes tc;
     bool use_tc = false;
+    // compressed form: tensor-core planes of the C_k (m2l_path 5)
+    TcPlanes tc_c;
+    bool use_tc_c = false;
     bool use_tc_updown = false;
-    // mixed: SVD-compressed M2L, U ~= V C_k P_l with bases shared by every
-    // operator: Wb holds the per-source-level compress operators P_l (r_in x
-    // n), Vb the decompress basis V (n x r_out), Cops the C_k (r_out x r_in),
-    // all row-major FP32; comp_src / comp_obs pair every M2L source / target
-    // cell with itself (one group per level: P_l / one group: V)
+    // mixed, compressed (m2l_path 0 / 4): the far field runs in the SVD bases
+    // of the M2L kernel matrices.  Upward states are r_in coefficients
+    // u~ = P_l u, downward states r_out coefficients (d ~= V d~).  All
+    // operators row-major FP32:
+    //   Pb   per source level  P_l (r_in x n): leaf check potentials -> u~
+    //   Wl   per source level  2^-l W (n x r_in): u~ -> equivalent densities (M2P)
+    //   Vb   V (n x r_out): down-check potentials <-> d~ (P2L)
+    //   Cops per M2L class     C_k (r_out x r_in)
+    //   Xops per M2M operator  X (r_in x r_in)
+    //   Yops per L2L operator  Y (r_out x r_out)
+    // and the L2P operators E take d~ directly (E V).
     bool m2l_compressed = false;
     int r_in = 0, r_out = 0;
-    DBuf<float> Wb, Vb, Cops;
-    GemmSet m2l_c, m2l_c_t, comp_src, comp_obs;
+    DBuf<float> Pb, Wl, Vb, Cops, Xops, Yops;
+    DBuf<double> V64;  // V in FP64 (column-major n x r_out) while the L2P operators are built
+    GemmSet m2l_c, m2l_c_t, comp_p2m, decomp_m2p, comp_p2l;
+    std::vector<GemmSet> m2m_c, m2m_c_t, l2l_c, l2l_c_t;  // per level
     // mixed: per-leaf L2P operators
     DBuf<float> E;
     DBuf<long> E_row0;  // per l2p task
@@ -280,7 +301,21 @@ struct Plan {
     void build_c2e(Form& F);
     void build_plain_ops(Form& F);
     void build_mixed_ops(Form& F);
-    void build_m2l_compression(Form& F, const double* U64, long n_ops, const std::vector<long>& op_index);
+    struct CompressionInput {
+        const double* T0;                  // root-scaled M2L kernel matrices (compact)
+        long n_m2l;
+        const std::vector<long>* m2l_index;  // job -> compact M2L index
+        const double* KM;                  // M2M kernel matrices (compact)
+        const std::vector<int>* m2m_lc;    // compact M2M -> child level
+        const std::vector<long>* m2m_index;
+        const double* YL;                  // combined L2L operators (compact)
+        const std::vector<long>* l2l_index;
+        const std::vector<long>* m2m_off;
+        const std::vector<long>* l2l_off;
+    };
+    void build_compression(Form& F, const CompressionInput& in);
+    void forward_compressed(int nrhs, cudaStream_t s);
+    void adjoint_compressed(int nrhs, cudaStream_t s);
     void build_gemm_sets(Form& F, long op_base_m2m, long op_base_l2l, long op_base_m2l,
                          const std::vector<long>& m2m_off, const std::vector<long>& l2l_off,
                          const std::vector<long>& m2l_off);

@@ -336,33 +336,34 @@ __global__ void split_rows_kernel(const float* in, long rows, int n, int k_pad,
     }
 }
 
-// operators [op][n][n] FP32 -> three bf16 planes [op][m_pad][k_pad] (zero padding)
-__global__ void split_ops_kernel(const float* in, long n_ops, int n, int m_pad, int k_pad,
+// operators [op][m][k] FP32 -> three bf16 planes [op][m_pad][k_pad] (zero padding)
+__global__ void split_ops_kernel(const float* in, long n_ops, int m, int k, int m_pad, int k_pad,
                                  __nv_bfloat16* o0, __nv_bfloat16* o1, __nv_bfloat16* o2)
 {
     const long total = n_ops * m_pad * (long)k_pad;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long)gridDim.x * blockDim.x) {
-        const int k = (int)(t % k_pad);
+        const int kk = (int)(t % k_pad);
         const long rm = t / k_pad;
-        const int m = (int)(rm % m_pad);
+        const int mm = (int)(rm % m_pad);
         const long op = rm / m_pad;
-        split3((m < n && k < n) ? in[(op * n + m) * (long)n + k] : 0.f, o0[t], o1[t], o2[t]);
+        split3((mm < m && kk < k) ? in[(op * m + mm) * (long)k + kk] : 0.f, o0[t], o1[t], o2[t]);
     }
 }
 
 }  // namespace
 
-void TcPlanes::build(const float* ops32, long n_ops, int n, cudaStream_t s)
+void TcPlanes::build(const float* ops32, long n_ops, int m, int k, cudaStream_t s)
 {
-    this->n = n;
-    m_pad = (n + TC_BM - 1) / TC_BM * TC_BM;
-    k_pad = (n + TC_BK - 1) / TC_BK * TC_BK;
+    this->m = m;
+    this->k = k;
+    m_pad = (m + TC_BM - 1) / TC_BM * TC_BM;
+    k_pad = (k + TC_BK - 1) / TC_BK * TC_BK;
     const long total = n_ops * (long)m_pad * k_pad;
     for (auto& p : a) p.alloc(std::max<long>(total, 1));
     if (total > 0) {
         split_ops_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
-            ops32, n_ops, n, m_pad, k_pad, a[0].p, a[1].p, a[2].p);
+            ops32, n_ops, m, k, m_pad, k_pad, a[0].p, a[1].p, a[2].p);
         TBEM_CK(cudaGetLastError());
     }
     err.alloc(1);
@@ -380,7 +381,7 @@ void TcPlanes::split_b(const float* cells, long rows, cudaStream_t s)
     for (auto& p : b) p.ensure(std::max<long>(total, 1));
     if (total > 0) {
         split_rows_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
-            cells, rows, n, k_pad, b[0].p, b[1].p, b[2].p);
+            cells, rows, k, k_pad, b[0].p, b[1].p, b[2].p);
         TBEM_CK(cudaGetLastError());
     }
 }
@@ -392,14 +393,14 @@ void TcPlanes::split_b_rows(const float* cells, long row0, long rows, long rows_
     const long total = rows * (long)k_pad;
     if (total > 0) {
         split_rows_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 152L * 64), 256, 0, s>>>(
-            cells + row0 * (long)n, rows, n, k_pad, b[0].p + row0 * k_pad, b[1].p + row0 * k_pad,
+            cells + row0 * (long)k, rows, k, k_pad, b[0].p + row0 * k_pad, b[1].p + row0 * k_pad,
             b[2].p + row0 * k_pad);
         TBEM_CK(cudaGetLastError());
     }
 }
 
-void GemmSet::run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, long nn,
-                     cudaStream_t s, long* launches)
+void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn, cudaStream_t s,
+                     long* launches)
 {
     if (empty()) return;
     if (d_op.n == 0) {
@@ -439,7 +440,7 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int n, int nrhs, int atomic, l
     a.in_cell = d_in.p;
     a.out_cell = d_out.p;
     a.D = D;
-    a.n = n;
+    a.n = P.m;
     a.nrhs = nrhs;
     a.atomic = atomic;
     a.err = P.err.p;

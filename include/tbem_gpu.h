@@ -68,7 +68,8 @@ typedef struct {
                               1 SIMT FP32 for all (uncompressed M2L),
                               2 tcgen05 3xBF16 for the uncompressed M2L only,
                               3 tcgen05 3xBF16 for M2L, M2M and L2L,
-                              4 SVD-compressed M2L on the SIMT FP32 pipes         */
+                              4 SVD-compressed far field on the SIMT FP32 pipes,
+                              5 as 4 with the M2L products on tcgen05 3xBF16      */
     int p2p_block;         /* 0 auto; else threads per target in the P2P kernel (1,2,4,8) */
     int host_only;         /* 1: build trees and task lists only (no device use);
                               apply calls then fail with TBEM_ERR_STATE            */
