@@ -239,9 +239,11 @@ int tbem_fmm_set_timing(TbemFmm* h, int enabled)
 int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int cap)
 {
     if (!h) return fail(TBEM_ERR_ARG, "null handle");
+    int rc = guarded([&] { const_cast<TbemFmm*>(h)->plan.read_phases(); });
+    if (rc != TBEM_OK) return rc;
     const auto& v = h->plan.phase_ms;
     int k = 0;
-    for (size_t i = 1; i < v.size(); i++, k++) {
+    for (size_t i = 0; i < v.size(); i++, k++) {
         if (k >= cap) continue;
         if (names) names[k] = v[i].first.c_str();
         if (ms) ms[k] = v[i].second;

@@ -12,7 +12,9 @@
 // length m.
 //
 // CTA: 256 threads, tile BM x 64 (BM = 128 or 64: the choice that pads m the
-// least), each thread an (BM / 16) x 4 block of outputs.  K runs in steps of
+// least), each thread an (BM / 16) x 4 block of outputs.  A launch with too
+// few tiles to fill the GPU splits K over blockIdx.z (partial products added
+// atomically).  K runs in steps of
 // BK through two shared-memory buffers: the next step's global loads are in
 // registers while the current step is multiplied, so one barrier per step
 // and the load latency overlaps the FMAs.  Shared tiles are stored k-major
@@ -46,6 +48,7 @@ struct GemmArgs {
     int nrhs;
     int trans;  // op(A) = A^T
     int mode;
+    int kchunk;  // split K: CTA z covers [z * kchunk, (z + 1) * kchunk) (multiple of BK)
 };
 
 template <typename T>
@@ -114,18 +117,21 @@ __global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs
     }
 
     T ra[NA], rb[NB];
+    // this CTA's K range (split K: the partial products meet in GEMM_ATOMIC)
+    const int kb = blockIdx.z * a.kchunk;
+    const int kend = min(K, kb + a.kchunk);
     auto load = [&](int k0) {
 #pragma unroll
         for (int i = 0; i < NA; i++) {
             const int gm = m0 + am[i], gk = k0 + ak[i];
             T v = T(0);
-            if (gm < M && gk < K) v = a.trans ? A[(long)gk * lda + gm] : A[(long)gm * lda + gk];
+            if (gm < M && gk < kend) v = a.trans ? A[(long)gk * lda + gm] : A[(long)gm * lda + gk];
             ra[i] = v;
         }
 #pragma unroll
         for (int i = 0; i < NB; i++) {
             const int gk = k0 + bk[i];
-            rb[i] = (bcol[i] && gk < K) ? bcol[i][gk] : T(0);
+            rb[i] = (bcol[i] && gk < kend) ? bcol[i][gk] : T(0);
         }
     };
     auto store = [&](int buf) {
@@ -141,13 +147,13 @@ __global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs
 #pragma unroll
         for (int j = 0; j < TN; j++) acc[i][j] = T(0);
 
-    const int nk = (K + BK - 1) / BK;
-    load(0);
+    const int nk = (kend - kb + BK - 1) / BK;
+    load(kb);
     store(0);
     __syncthreads();
     for (int kt = 0; kt < nk; kt++) {
         const int buf = kt & 1;
-        if (kt + 1 < nk) load((kt + 1) * BK);
+        if (kt + 1 < nk) load(kb + (kt + 1) * BK);
 #pragma unroll
         for (int kk = 0; kk < BK; kk++) {
             T av[TM], bv[TN];
@@ -178,12 +184,21 @@ __global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs
         if (kt + 1 < nk) store(buf ^ 1);
         __syncthreads();
     }
+    // resolve the output columns before the first store (no load behind a store)
+    T* dcols[TN];
 #pragma unroll
     for (int j = 0; j < TN; j++) {
         const int c = col0 + tx * TN + j;
-        if (c >= ncols) continue;
-        const int p = c / a.nrhs, r = c % a.nrhs;
-        T* dcol = a.D + (long)a.out_cell[pair0 + p] * ldd + (long)r * M;
+        dcols[j] = nullptr;
+        if (c < ncols) {
+            const int p = c / a.nrhs, r = c % a.nrhs;
+            dcols[j] = a.D + (long)a.out_cell[pair0 + p] * ldd + (long)r * M;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < TN; j++) {
+        T* dcol = dcols[j];
+        if (!dcol) continue;
 #pragma unroll
         for (int i = 0; i < TM; i++) {
             const int gm = m0 + ty * TM + i;

@@ -175,13 +175,30 @@ void GemmSet::run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int tr
     const std::vector<int>& st = wave_tile_start[nrhs];
     const int nw = (int)st.size() - 1;
     if (!waves && nw != 1) throw Error(TBEM_ERR_STATE, "a wave-ordered GEMM set run without waves");
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        TBEM_CK(cudaGetDevice(&dev));
+        TBEM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    }
     for (int w = 0; w < nw; w++) {
         const int nt = st[w + 1] - st[w];
         if (nt == 0) continue;
         a.tile_group = it->second.first.p + st[w];
         a.tile_col0 = it->second.second.p + st[w];
         const int bm = gemm_bm(m);
-        dim3 grid((unsigned)nt, (unsigned)((m + bm - 1) / bm));
+        const long ctas = (long)nt * ((m + bm - 1) / bm);
+        // split K when the tiles fill less than two CTAs per SM and the
+        // accumulation is atomic anyway (never for the deterministic modes)
+        a.kchunk = k;
+        int split = 1;
+        if (mode == GEMM_ATOMIC && ctas < 2L * sms && k >= 128) {
+            const int bk = GemmK<T>::BK;
+            split = (int)std::min<long>(std::min<long>((2L * sms + ctas - 1) / ctas, 8), k / 64);
+            a.kchunk = ((k + split - 1) / split + bk - 1) / bk * bk;
+            split = (k + a.kchunk - 1) / a.kchunk;
+        }
+        dim3 grid((unsigned)nt, (unsigned)((m + bm - 1) / bm), (unsigned)split);
         if (bm == 128) grouped_gemm_kernel<T, 128><<<grid, GM_THREADS, 0, s>>>(a);
         else grouped_gemm_kernel<T, 64><<<grid, GM_THREADS, 0, s>>>(a);
         TBEM_CK(cudaGetLastError());
@@ -419,7 +436,9 @@ inline double hypot_ref(const double* v)
 
 Plan::~Plan()
 {
-    for (auto e : events) cudaEventDestroy(e);
+    for (auto& m : marks) cudaEventDestroy(m.second);
+    for (auto e : event_pool) cudaEventDestroy(e);
+    if (h_err) cudaFreeHost(h_err);
     if (cublas) cublasDestroy(cublas);
     if (solver) cusolverDnDestroy(solver);
     if (stream) cudaStreamDestroy(stream);
@@ -1069,10 +1088,11 @@ void Plan::build_mixed_ops(Form& F)
                 job_ls[m2l_off[k] / nn] = S.cells[m2l_canon[k].second].level;
             }
     }
-    // m2l_path: 0 auto (compressed where the M2L operators are precomputed),
+    // m2l_path: 0 auto (= 5 where the M2L operators are precomputed and
+    // compress, else SIMT FP32),
     // 1 SIMT FP32 for all, 2 tensor cores for the M2L only, 3 tensor cores for
     // all, 4 compressed, 5 compressed with the M2L products on tensor cores
-    const int path = opt.m2l_path == 0 ? 4 : opt.m2l_path;
+    const int path = opt.m2l_path == 0 ? 5 : opt.m2l_path;
     // FP64 copies of the M2L kernel matrices for the compression (compact
     // index), scaled to the root level (see build_m2l_compression)
     const bool compress = (path == 4 || path == 5) && !F.m2l_on_the_fly && !m2l_off.empty();
@@ -1546,10 +1566,38 @@ void Plan::mark(const char* name, cudaStream_t s)
 {
     if (!timing) return;
     cudaEvent_t e;
-    TBEM_CK(cudaEventCreate(&e));
+    if (!event_pool.empty()) {
+        e = event_pool.back();
+        event_pool.pop_back();
+    } else {
+        TBEM_CK(cudaEventCreate(&e));
+    }
     TBEM_CK(cudaEventRecord(e, s));
-    events.push_back(e);
-    phase_ms.push_back({name, 0.0});
+    marks.push_back({name, e});
+}
+
+void Plan::read_phases()
+{
+    if (marks.empty()) return;
+    TBEM_CK(cudaEventSynchronize(marks.back().second));
+    std::vector<std::pair<std::string, double>> sum;
+    int applies = 0;
+    for (size_t i = 0; i < marks.size(); i++) {
+        if (marks[i].first == "start") {
+            applies++;
+            continue;
+        }
+        if (i == 0) continue;
+        float ms = 0.f;
+        TBEM_CK(cudaEventElapsedTime(&ms, marks[i - 1].second, marks[i].second));
+        auto it = std::find_if(sum.begin(), sum.end(), [&](const auto& q) { return q.first == marks[i].first; });
+        if (it == sum.end()) sum.push_back({marks[i].first, ms});
+        else it->second += ms;
+    }
+    for (auto& q : sum) q.second /= std::max(applies, 1);
+    phase_ms = sum;
+    for (auto& m : marks) event_pool.push_back(m.second);
+    marks.clear();
 }
 
 template <typename T>
@@ -1818,7 +1866,7 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     mark("gather", s);
     // P2M into the leaves' check potentials, then u~ = P_l u
     eval<float>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
-    F.comp_p2m.run_rect<float>(cu32.p, cuc32.p, ri, n, n, nrhs, 0, GEMM_STORE, s, &launches);
+    F.comp_p2m.run_rect<float>(cu32.p, cuc32.p, ri, n, n, nrhs, 0, GEMM_ATOMIC, s, &launches);  // into zeros
     mark("p2m", s);
     for (int l = S.n_levels() - 1; l >= 0; l--)
         if (l < (int)F.m2m_c.size()) F.m2m_c[l].run_rect<float>(cuc32.p, cuc32.p, ri, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
@@ -1836,19 +1884,20 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     if (!L.p2l.empty()) {
         TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
         eval<float>(p2l, F.ks_kid, true, false, O, dobs, F.r_dc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cd32.p, 1, nrhs, s, false);
-        F.comp_p2l.run_rect<float>(cd32.p, cdc32.p, ro, n, ro, nrhs, 1, GEMM_ADD, s, &launches);
+        F.comp_p2l.run_rect<float>(cd32.p, cdc32.p, ro, n, ro, nrhs, 1, GEMM_ATOMIC, s, &launches);
     }
     mark("m2p+p2l", s);
     if (F.use_tc_c) {
         F.tc_c.split_b_rows(cuc32.p, 0, ncs * nrhs, std::max(ncs, nco) * nrhs, s);
         launches++;
+        mark("m2l_split", s);
         F.m2l_c.run_tc(F.tc_c, cdc32.p, nrhs, 1, (long)ro * ri, s, &launches);
     } else {
         F.m2l_c.run_rect<float>(cuc32.p, cdc32.p, ro, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
     }
     mark("m2l", s);
     for (int l = 1; l < O.n_levels(); l++)
-        if (l - 1 < (int)F.l2l_c.size()) F.l2l_c[l - 1].run_rect<float>(cdc32.p, cdc32.p, ro, ro, ro, nrhs, 0, GEMM_ADD, s, &launches);
+        if (l - 1 < (int)F.l2l_c.size()) F.l2l_c[l - 1].run_rect<float>(cdc32.p, cdc32.p, ro, ro, ro, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("l2l", s);
     if (F.n_l2p > 0) {
         l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cdc32.p, ro, F.E_ld, R, nrhs, y64.p, NO);
@@ -1895,10 +1944,10 @@ void Plan::adjoint_compressed(int nrhs, cudaStream_t s)
         add_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(qu64.p, cu32.p, ncs * nrhs * n);
         TBEM_CK(cudaGetLastError());
         launches++;
-        F.decomp_m2p.run_rect<float>(cu32.p, cuc32.p, ri, n, ri, nrhs, 1, GEMM_ADD, s, &launches);
+        F.decomp_m2p.run_rect<float>(cu32.p, cuc32.p, ri, n, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
     }
     for (int l = 0; l < S.n_levels(); l++)
-        if (l < (int)F.m2m_c_t.size()) F.m2m_c_t[l].run_rect<float>(cuc32.p, cuc32.p, ri, ri, ri, nrhs, 1, GEMM_ADD, s, &launches);
+        if (l < (int)F.m2m_c_t.size()) F.m2m_c_t[l].run_rect<float>(cuc32.p, cuc32.p, ri, ri, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
     F.comp_p2m.run_rect<float>(cuc32.p, cu32.p, n, ri, n, nrhs, 1, GEMM_STORE, s, &launches);
     eval<float>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
 }
@@ -1923,32 +1972,40 @@ void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
         if (y_dev) TBEM_CK(cudaStreamSynchronize(s));
         return;
     }
+    if (h_err && (h_err[0] || h_err[1]))  // raised by an earlier apply
+        throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
     ensure_rhs(nrhs);
     launches = 0;
-    for (auto e : events) cudaEventDestroy(e);
-    events.clear();
-    phase_ms.clear();
     TBEM_CK(cudaMemcpyAsync(io_x.p, x, sizeof(double) * n_in * nrhs,
                             x_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
     if (adj) adjoint(nrhs, s);
     else forward(nrhs, s);
     TBEM_CK(cudaMemcpyAsync(y, io_y.p, sizeof(double) * n_out * nrhs,
                             y_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
-    if (!y_dev || timing) {
-        TBEM_CK(cudaStreamSynchronize(s));
-        for (const TcPlanes* P : {&f.tc, &f.tc_c}) {
-            if (!P->err.p) continue;
-            int flag = 0;
-            TBEM_CK(cudaMemcpy(&flag, P->err.p, sizeof(int), cudaMemcpyDeviceToHost));
-            if (flag) throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
-        }
+    check_tc_flags(!y_dev, s);
+}
+
+// Copies the tensor-core timeout flags into pinned memory on stream s and,
+// when wait_device, waits for them (host outputs: the apply is synchronous
+// anyway); otherwise the copy is read by the next call.  A raised flag stays
+// raised: the operator reports TBEM_ERR_TIMEOUT from then on.
+void Plan::check_tc_flags(bool wait_device, cudaStream_t s)
+{
+    const TcPlanes* P[2] = {&f.tc, &f.tc_c};
+    if (!P[0]->err.p && !P[1]->err.p) {
+        if (wait_device) TBEM_CK(cudaStreamSynchronize(s));
+        return;
     }
-    if (timing && events.size() > 1) {
-        for (size_t i = 1; i < events.size(); i++) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, events[i - 1], events[i]);
-            phase_ms[i].second = ms;
-        }
+    if (!h_err) {
+        TBEM_CK(cudaMallocHost(&h_err, 2 * sizeof(int)));
+        h_err[0] = h_err[1] = 0;
+    }
+    if (h_err[0] || h_err[1]) throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
+    for (int i = 0; i < 2; i++)
+        if (P[i]->err.p) TBEM_CK(cudaMemcpyAsync(h_err + i, P[i]->err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (wait_device) {
+        TBEM_CK(cudaStreamSynchronize(s));
+        if (h_err[0] || h_err[1]) throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
     }
 }
 

@@ -278,10 +278,19 @@ struct Plan {
     cudaStream_t stream = nullptr;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t solver = nullptr;
+    // tensor-core timeout flags copied to pinned memory after every apply;
+    // an apply with device outputs reports a flag raised by the previous one
+    int* h_err = nullptr;
+    void check_tc_flags(bool wait_device, cudaStream_t s);
     bool timing = false;
     long launches = 0;  // kernel launches of the last apply
+    // phase timing: events recorded on the apply's stream (no synchronization);
+    // read_phases() turns the marks of the applies since the last read into
+    // mean milliseconds per apply
+    std::vector<std::pair<std::string, cudaEvent_t>> marks;
+    std::vector<cudaEvent_t> event_pool;
     std::vector<std::pair<std::string, double>> phase_ms;
-    std::vector<cudaEvent_t> events;
+    void read_phases();
     // kept for clone()
     std::vector<double> h_obs_locs, h_obs_normals, h_src_locs, h_src_normals, h_src_weights;
 

@@ -7,20 +7,30 @@
 // a0b2, a1b1, a2b0) in FP32 accumulators in tensor memory: FP32-level
 // accuracy on the bf16 tensor pipe.  The accumulation error of an FP32
 // tensor-memory accumulator grows with the number of MMAs added into it, so
-// the dominant product a0b0 goes to two accumulators (even and odd K chunks)
-// and the five small products to a third; the epilogue adds the three in
-// FP32 registers.  Small terms are never rounded against the large sum.  The operators' planes are built once at
-// setup; the check potentials (B) are split before every use.
+// the dominant product a0b0 and the five small products go to separate
+// accumulators, added in FP32 registers by the epilogue: small terms are
+// never rounded against the large sum.  The operators' planes are built once
+// at setup; the B operand (cell coefficients) is split before every use.
 //
-// CTA: 128 threads, three 128 x BN accumulators (4 BN TMEM columns allocated).  K runs in
-// chunks of 64 bf16 (128-byte rows) through a 2-stage shared-memory ring of
-// six 128B-swizzled K-major planes per stage.  All threads stage a chunk with
-// cp.async (A rows from the operator planes, B rows gathered by pair; 48
-// copies per thread in flight), one thread issues the chunk's 24 MMAs and
-// commits them to the stage's mbarrier; the next chunk's copies overlap the
-// current chunk's MMAs.  Waits are bounded and CTA-uniform.  The epilogue
-// reads the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31)
-// and scatters it into D.
+// Persistent and warp-specialized: one CTA per SM walks the 128 x BN output
+// tiles (all row tiles of a column tile back to back, so the gathered B
+// columns are reused from L2).  K runs in chunks of 64 bf16 (128-byte rows)
+// through a ring of shared-memory stages, each holding six 128B-swizzled
+// K-major planes (three of A, three of B).
+//   warps 4-7  producers: cp.async of the A rows and the B rows (gathered by
+//              pair), four whole 128-byte rows per warp instruction; a stage
+//              is handed over through its "full" mbarrier once the copies
+//              have landed;
+//   warp 8     one thread issues the chunk's 24 MMAs and commits them to the
+//              stage's "empty" mbarrier (and, after a tile's last chunk, to
+//              the accumulator's "full" mbarrier);
+//   warps 0-3  epilogue: tcgen05.ld of the tile's two accumulators (warp w
+//              owns TMEM lanes 32w..32w+31), scatter into D, release the
+//              accumulator.  Two accumulator buffers let a tile's epilogue
+//              overlap the next tile's MMAs.
+// Every wait is bounded; a timed-out wait raises a CTA-wide abort flag that
+// ends every role's loop, the MMAs in flight are drained (bounded) before
+// tensor memory is freed, and the kernel reports through the error flag.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -28,7 +38,7 @@
 
 namespace tbem {
 
-constexpr int TC_BM = 128, TC_BK = 64, TC_THREADS = 128;
+constexpr int TC_BM = 128, TC_BK = 64;
 constexpr int TC_TERMS = 3;                                  // bf16 terms per operand
 constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;            // 16 KB: one 128 x 64 bf16 A plane tile
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
@@ -41,12 +51,15 @@ struct TcShape {
     static constexpr int B_TILE = BN * TC_BK * 2;                         // one B plane tile
     static constexpr int STAGE_BYTES = TC_TERMS * (TC_TILE_BYTES + B_TILE);
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+    static constexpr uint32_t TMEM_COLS = 4 * BN;  // 2 buffers x (big, small) accumulators
     // kind::f16, bf16 A/B, FP32 D, K-major A and B, M = 128, N = BN
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
                                       ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
 };
 static_assert(TcShape<128>::SMEM_BYTES <= 227 * 1024 && TcShape<64>::SMEM_BYTES <= 227 * 1024,
               "shared memory budget");
+constexpr int TC_PRODUCERS = 128;                      // producer threads (warps 4-7)
+constexpr int TC_THREADS_P = 128 + TC_PRODUCERS + 32;  // epilogue + producers + MMA warp
 
 struct TcArgs {
     const __nv_bfloat16* A[TC_TERMS];  // [op][m_pad][k_pad] per term
@@ -143,68 +156,44 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// cp.async of 16-byte pieces [j0, j0 + NJ) of one 128-byte row into their
-// swizzled places; a row that is not valid is zero-filled (source size 0,
-// nothing is read).
-template <int NJ>
-__device__ __forceinline__ void stage_row_async(uint32_t tile, int row, int j0,
-                                                const __nv_bfloat16* src, bool valid)
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar)
 {
-    const uint32_t n = valid ? 16u : 0u;
-#pragma unroll
-    for (int jj = 0; jj < NJ; jj++) {
-        const int j = j0 + jj;
-        const uint32_t dst = tile + row * 128 + ((j ^ (row & 7)) << 4);
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst),
-                     "l"(src + j * 8), "r"(n)
-                     : "memory");
-    }
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
 }
 
 template <int BN>
-__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
+__global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a, int n_ctiles, int m_tiles)
 {
     using Sh = TcShape<BN>;
-    constexpr int TC_STAGES = Sh::STAGES;
-    constexpr int TC_STAGE_BYTES = Sh::STAGE_BYTES;
+    constexpr int STAGES = Sh::STAGES;
     constexpr int B_BASE = TC_TERMS * TC_TILE_BYTES;  // B planes follow the A planes
-    constexpr int BJ = 8 * BN / TC_THREADS;           // 16-byte pieces of B per thread
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t mbar[TC_STAGES];
+    __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accf_bar[2], acce_bar[2], drain_bar;
     __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
     uint8_t* smem = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-
-    const int tid = threadIdx.x, warp = tid / 32;
-    const int tile = blockIdx.x;
-    const int g = a.tile_group[tile];
-    const int col0 = a.tile_col0[tile];
-    const int m0 = blockIdx.y * TC_BM;
-    const long pair0 = a.g_pair0[g];
-    const int ncols = a.g_npairs[g] * a.nrhs;
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     const int nk = a.k_pad / TC_BK;
-    const long a_off = (long)a.g_op[g] * a.a_op_stride + (long)(m0 + tid) * a.k_pad;
-    // B row of this thread: one gathered (cell, rhs) column (with BN = 64 two
-    // threads share a row, four 16-byte pieces each)
-    const int brow_i = tid % BN;
-    const int bj0 = (tid / BN) * BJ;
-    const int c = col0 + brow_i;
-    const bool bvalid = c < ncols;
-    long brow = 0;
-    if (bvalid) {
-        const int p = c / a.nrhs, r = c % a.nrhs;
-        brow = ((long)a.in_cell[pair0 + p] * a.nrhs + r) * a.k_pad;
-    }
+    const int total = n_ctiles * m_tiles;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&tmem_slot)),
-                     "r"(4 * BN));
+                     "r"(Sh::TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int s = 0; s < TC_STAGES; s++)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[s])));
+        for (int s = 0; s < STAGES; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_bar[s])), "r"(TC_PRODUCERS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[s])));
+        }
+        for (int b = 0; b < 2; b++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&accf_bar[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_u32(&acce_bar[b])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&drain_bar)));
+        abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -213,104 +202,187 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a)
     const uint32_t tmem = tmem_slot;
     const uint32_t smem0 = smem_u32(smem);
 
-    auto load_stage = [&](int stage, int kc) {
-        const uint32_t st = smem0 + stage * TC_STAGE_BYTES;
-        const int k0 = kc * TC_BK;
-#pragma unroll
-        for (int t = 0; t < TC_TERMS; t++) {
-            stage_row_async<8>(st + t * TC_TILE_BYTES, tid, 0, a.A[t] + a_off + k0, true);
-            stage_row_async<BJ>(st + B_BASE + t * Sh::B_TILE, brow_i, bj0,
-                                bvalid ? a.B[t] + brow + k0 : a.B[t], bvalid);
+    // bounded wait that also gives up as soon as another role aborted
+    auto wait = [&](uint64_t* bar, uint32_t parity) -> bool {
+        const uint32_t b = smem_u32(bar);
+        const long long t0 = clock64();
+        while (!mbar_try(b, parity)) {
+            if (*reinterpret_cast<volatile int*>(&abort_flag)) return false;
+            if (clock64() - t0 > TC_WAIT_CYCLES) {
+                atomicExch(&abort_flag, 1);
+                return false;
+            }
         }
-        asm volatile("cp.async.commit_group;" ::: "memory");
+        return true;
     };
 
-    bool ok = true;
-    int issued = 0;  // chunks whose MMAs were committed
-    if (nk > 0) load_stage(0, 0);
-    for (int kc = 0; kc < nk; kc++) {
-        const int s = kc % TC_STAGES;
-        if (kc + 1 < nk) {
-            const int ns = (kc + 1) % TC_STAGES;
-            if (kc + 1 >= TC_STAGES) {
-                // stage ns is free once the MMAs of chunk kc + 1 - TC_STAGES completed;
-                // decided CTA-wide so that no thread is left at a barrier
-                const int prev = kc + 1 - TC_STAGES;
-                const bool w = mbar_wait(smem_u32(&mbar[ns]), (prev / TC_STAGES) & 1);
-                ok = __syncthreads_and(w);
+    bool mma_issued = false;
+    if (warp >= 4 && warp < 8) {
+        // ---------------- producers.  A plane tile is 128 rows of eight 16-byte
+        // pieces; piece e = pt + 128 i is row e / 8, piece e % 8, so one warp
+        // instruction copies four whole rows (full sectors, coalesced).
+        constexpr int A_PER = TC_BM * 8 / TC_PRODUCERS;  // 8 pieces of A per thread and plane
+        constexpr int B_PER = BN * 8 / TC_PRODUCERS;     // 8 (BN = 128) or 4 (BN = 64)
+        const int pt = tid - 128;
+        const int pj = pt % 8, prow = pt / 8;  // piece within a row; rows prow + 16 i
+        int j = 0;  // chunks issued (over all tiles of this CTA)
+        bool ok = true;
+        for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+            const int tile = t / m_tiles, m0 = (t % m_tiles) * TC_BM;
+            const int g = a.tile_group[tile];
+            const int col0 = a.tile_col0[tile];
+            const long pair0 = a.g_pair0[g];
+            const int ncols = a.g_npairs[g] * a.nrhs;
+            const long a_base = (long)a.g_op[g] * a.a_op_stride + (long)(m0 + prow) * a.k_pad + pj * 8;
+            long boff[B_PER];
+#pragma unroll
+            for (int i = 0; i < B_PER; i++) {
+                const int c = col0 + prow + 16 * i;
+                boff[i] = -1;
+                if (c < ncols) {
+                    const int p = c / a.nrhs, r = c % a.nrhs;
+                    boff[i] = ((long)a.in_cell[pair0 + p] * a.nrhs + r) * a.k_pad + pj * 8;
+                }
+            }
+            for (int kc = 0; kc < nk; kc++, j++) {
+                const int s = j % STAGES;
+                if (j >= STAGES && !wait(&empty_bar[s], ((j / STAGES) - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t st = smem0 + s * Sh::STAGE_BYTES;
+                const int k0 = kc * TC_BK;
+#pragma unroll
+                for (int q = 0; q < TC_TERMS; q++) {
+#pragma unroll
+                    for (int i = 0; i < A_PER; i++) {
+                        const int row = prow + 16 * i;
+                        const uint32_t dst = st + q * TC_TILE_BYTES + row * 128 + ((pj ^ (row & 7)) << 4);
+                        const __nv_bfloat16* src = a.A[q] + a_base + (long)16 * i * a.k_pad + k0;
+                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+                    }
+#pragma unroll
+                    for (int i = 0; i < B_PER; i++) {
+                        const int row = prow + 16 * i;
+                        const uint32_t dst = st + B_BASE + q * Sh::B_TILE + row * 128 + ((pj ^ (row & 7)) << 4);
+                        const bool v = boff[i] >= 0;
+                        // an invalid column is zero-filled (source size 0, nothing read)
+                        const __nv_bfloat16* src = v ? a.B[q] + boff[i] + k0 : a.B[q];
+                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
+                                     "r"(v ? 16u : 0u)
+                                     : "memory");
+                    }
+                }
+                asm volatile("cp.async.commit_group;" ::: "memory");
+                if (j >= 1) {
+                    // the previous chunk's copies have landed: hand its stage over
+                    asm volatile("cp.async.wait_group 1;" ::: "memory");
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_arrive(smem_u32(&full_bar[(j - 1) % STAGES]));
+                }
+            }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (ok && j >= 1) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(smem_u32(&full_bar[(j - 1) % STAGES]));
+        }
+    } else if (warp == 8) {
+        // ---------------- MMA issue (one thread)
+        if (lane == 0) {
+            int j = 0, tc = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < total && ok; t += gridDim.x, tc++) {
+                const int b = tc & 1, bu = tc >> 1;
+                if (bu >= 1 && !wait(&acce_bar[b], (bu - 1) & 1)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t big = tmem + b * 2 * BN, small = big + BN;
+                for (int kc = 0; kc < nk; kc++, j++) {
+                    const int s = j % STAGES;
+                    if (!wait(&full_bar[s], (j / STAGES) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t st = smem0 + s * Sh::STAGE_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < TC_BK / 16; kk++) {
+                        const uint32_t off = kk * 32;  // 16 bf16 along K inside the swizzle atom
+                        const uint32_t a0 = st + off, a1 = a0 + TC_TILE_BYTES, a2 = a0 + 2 * TC_TILE_BYTES;
+                        const uint32_t b0 = st + B_BASE + off, b1 = b0 + Sh::B_TILE, b2 = b0 + 2 * Sh::B_TILE;
+                        constexpr uint32_t ID = Sh::IDESC;
+                        const uint32_t acc = (kc | kk) != 0;
+                        mma_bf16(big, sw128_desc(a0), sw128_desc(b0), ID, acc);
+                        mma_bf16(small, sw128_desc(a0), sw128_desc(b1), ID, acc);
+                        mma_bf16(small, sw128_desc(a1), sw128_desc(b0), ID, 1);
+                        mma_bf16(small, sw128_desc(a0), sw128_desc(b2), ID, 1);
+                        mma_bf16(small, sw128_desc(a1), sw128_desc(b1), ID, 1);
+                        mma_bf16(small, sw128_desc(a2), sw128_desc(b0), ID, 1);
+                    }
+                    mma_issued = true;
+                    mma_commit(smem_u32(&empty_bar[s]));
+                }
                 if (!ok) break;
+                mma_commit(smem_u32(&accf_bar[b]));
             }
-            load_stage(ns, kc + 1);
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t st = smem0 + s * TC_STAGE_BYTES;
-#pragma unroll
-            for (int kk = 0; kk < TC_BK / 16; kk++) {
-                const uint32_t off = kk * 32;  // 16 bf16 along K inside the swizzle atom
-                const uint32_t a0 = st + off, a1 = a0 + TC_TILE_BYTES, a2 = a0 + 2 * TC_TILE_BYTES;
-                const uint32_t b0 = st + B_BASE + off, b1 = b0 + Sh::B_TILE, b2 = b0 + 2 * Sh::B_TILE;
-                constexpr uint32_t ID = Sh::IDESC;
-                const uint32_t big = tmem + (kc & 1) * BN;   // a0b0: even / odd chunks
-                const uint32_t small = tmem + 2 * BN;        // the five small products
-                mma_bf16(big, sw128_desc(a0), sw128_desc(b0), ID, (kc >= 2 || kk != 0) ? 1u : 0u);
-                mma_bf16(small, sw128_desc(a0), sw128_desc(b1), ID, (kc | kk) != 0);
-                mma_bf16(small, sw128_desc(a1), sw128_desc(b0), ID, 1);
-                mma_bf16(small, sw128_desc(a0), sw128_desc(b2), ID, 1);
-                mma_bf16(small, sw128_desc(a1), sw128_desc(b1), ID, 1);
-                mma_bf16(small, sw128_desc(a2), sw128_desc(b0), ID, 1);
-            }
-            mma_commit(smem_u32(&mbar[s]));
-        }
-        issued = kc + 1;
-    }
-    // no copy may still be in flight when the kernel leaves
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    // the commit of the last issued chunk covers every MMA issued before it;
-    // after a timeout this still drains what is in flight before TMEM is freed
-    if (issued > 0) {
-        const bool w = mbar_wait(smem_u32(&mbar[(issued - 1) % TC_STAGES]), ((issued - 1) / TC_STAGES) & 1);
-        ok = __syncthreads_and(w && ok);
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!ok) {
-        if (tid == 0) atomicExch(a.err, 1);
     } else {
-        const int row = m0 + warp * 32 + (tid % 32);
+        // ---------------- epilogue (warps 0-3)
+        int tc = 0;
+        for (int t = blockIdx.x; t < total; t += gridDim.x, tc++) {
+            const int b = tc & 1, bu = tc >> 1;
+            if (!wait(&accf_bar[b], bu & 1)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int tile = t / m_tiles, m0 = (t % m_tiles) * TC_BM;
+            const int g = a.tile_group[tile];
+            const int col0 = a.tile_col0[tile];
+            const long pair0 = a.g_pair0[g];
+            const int ncols = a.g_npairs[g] * a.nrhs;
+            const int row = m0 + warp * 32 + lane;
 #pragma unroll 1
-        for (int cc = 0; cc < BN / 32; cc++) {
-            float v[32], w[32];
-            const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + cc * 32;
-            tmem_ld32(lane_base + 2 * BN, v);  // small terms first
-            if (nk > 1) {
-                tmem_ld32(lane_base + BN, w);
+            for (int cc = 0; cc < BN / 32; cc++) {
+                float v[32], w[32];
+                const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + b * 2 * BN + cc * 32;
+                // lane q resolves column q's destination once; the stores below
+                // take it by shuffle instead of a load behind every store
+                long my_off = -1;
+                {
+                    const int col = col0 + cc * 32 + lane;
+                    if (col < ncols) {
+                        const int p = col / a.nrhs, r = col % a.nrhs;
+                        my_off = ((long)a.out_cell[pair0 + p] * a.nrhs + r) * a.n;
+                    }
+                }
+                tmem_ld32(lane_base + BN, v);  // small terms first
+                tmem_ld32(lane_base, w);
 #pragma unroll
-                for (int j = 0; j < 32; j++) v[j] += w[j];
-            }
-            tmem_ld32(lane_base, w);
+                for (int q = 0; q < 32; q++) v[q] += w[q];
 #pragma unroll
-            for (int j = 0; j < 32; j++) v[j] += w[j];
-            if (row >= a.n) continue;
-#pragma unroll 4
-            for (int j = 0; j < 32; j++) {
-                const int col = col0 + cc * 32 + j;
-                if (col >= ncols) break;
-                const int p = col / a.nrhs, r = col % a.nrhs;
-                float* dst = a.D + ((long)a.out_cell[pair0 + p] * a.nrhs + r) * a.n + row;
-                if (a.atomic) atomicAdd(dst, v[j]);
-                else *dst += v[j];
+                for (int q = 0; q < 32; q++) {
+                    const long off = __shfl_sync(0xffffffffu, my_off, q);
+                    if (off >= 0 && row < a.n) {
+                        float* dst = a.D + off + row;
+                        if (a.atomic) atomicAdd(dst, v[q]);
+                        else *dst += v[q];
+                    }
+                }
             }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(smem_u32(&acce_bar[b]));
         }
+    }
+    __syncthreads();
+    // drain: every MMA this CTA issued has completed before tensor memory is
+    // released (bounded; after an abort the MMAs in flight still finish)
+    if (warp == 8 && lane == 0 && mma_issued) {
+        mma_commit(smem_u32(&drain_bar));
+        if (!mbar_wait(smem_u32(&drain_bar), 0)) atomicExch(&abort_flag, 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    if (tid == 0 && abort_flag) atomicExch(a.err, 1);
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(4 * BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Sh::TMEM_COLS));
 }
 
 // v -> three bf16 terms t0 + t1 + t2 (each the rounding of what is left)
@@ -444,9 +516,15 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
     a.nrhs = nrhs;
     a.atomic = atomic;
     a.err = P.err.p;
-    dim3 grid((unsigned)it->second.first.n, (unsigned)(P.m_pad / TC_BM));
-    if (bn == 64) tc_gemm_kernel<64><<<grid, TC_THREADS, TcShape<64>::SMEM_BYTES, s>>>(a);
-    else tc_gemm_kernel<128><<<grid, TC_THREADS, TcShape<128>::SMEM_BYTES, s>>>(a);
+    const int n_ctiles = (int)it->second.first.n, m_tiles = P.m_pad / TC_BM;
+    const long total = (long)n_ctiles * m_tiles;
+    if (total == 0) return;
+    int dev = 0, sms = 0;
+    TBEM_CK(cudaGetDevice(&dev));
+    TBEM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const unsigned grid = (unsigned)std::min<long>(total, std::max(sms, 1));
+    if (bn == 64) tc_gemm_kernel<64><<<grid, TC_THREADS_P, TcShape<64>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
+    else tc_gemm_kernel<128><<<grid, TC_THREADS_P, TcShape<128>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
     TBEM_CK(cudaGetLastError());
     if (launches) (*launches)++;
 }

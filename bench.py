@@ -13,9 +13,9 @@ operator to the slip (2 x 98,304 points x RHS).  ``value`` is whole-job
 points*RHS/s of the precision (mixed) form with inputs resident in HBM;
 ``e2e`` is the same through the public C ABI with host buffers (the host to
 device copy of the slip and the device to host copy of the result are inside
-the timed region).  The operator tables (1.4 GB of M2L operators, 1 GB of
-per-leaf L2P operators per kernel) are far larger than L2, so no L2 flush is
-needed between steps.
+the timed region).  The operator tables (0.6 GB of M2L operator planes and
+0.3 GB of per-leaf L2P operators per kernel) are far larger than the 129 MB
+L2, so no L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -129,11 +129,19 @@ def aggregate(seconds, units_per_rank, dist=None, device=None):
 
 
 def m2l_flops(op, n_rhs):
-    """Algorithmic M2L flops of one apply: every M2L pair is one dense
-    (R n_s) x (R n_s) product per right-hand side (2 flops per entry)."""
+    """M2L flops of one apply.
+
+    reference: the reference formulation's count, one dense (R n_s) x (R n_s)
+    product per M2L pair and right-hand side (2 flops per entry);
+    tensor: what the compressed form's tensor-core kernel executes, one
+    r_out x r_in product per pair and right-hand side, each as six bf16
+    products (the three-term split), 2 flops per multiply-add."""
     n = op.n_surface() * op.R
     pairs = len(op.list("m2l")[0])
-    return 2.0 * n * n * pairs * n_rhs
+    ri, ro = op.m2l_ranks()
+    return {"reference": 2.0 * n * n * pairs * n_rhs,
+            "tensor": 6 * 2.0 * ri * ro * pairs * n_rhs if ri else None,
+            "pairs": pairs}
 
 
 def cpu_baseline(locs, nrm, w, x, fraction, threads):
@@ -193,8 +201,9 @@ def config_dict(n_rhs):
             "fmm": {"order_requested": ORDER, "surface_points": 295, "mac": MAC,
                     "min_pts_per_cell": LEAF, "d": D, "account_for_small_cells": False},
             "n_points": 3 * 2 * N_GRID * N_GRID, "n_rhs": n_rhs,
-            "precision": "mixed (FP32 / 3xBF16 tensor M2L, FP32 P2P compensated)",
-            "l2": "operator tables >> 129 MB L2; no flush needed"}
+            "precision": "mixed: far field in the M2L SVD bases (FP32), M2L products on "
+                         "tcgen05 3xBF16, P2P FP32 compensated",
+            "l2": "operator tables (0.9 GB per kernel) >> 129 MB L2; no flush needed"}
 
 
 def main():
@@ -255,7 +264,11 @@ def main():
         step()
     torch.cuda.synchronize()
 
-    # -- device-resident timed region
+    # -- device-resident timed region (per-phase CUDA events recorded on the
+    # operators' stream inside it, read after it)
+    for op in ops:
+        op.phase_times()  # drop the warm-up marks
+        op.set_timing(True)
     with ClockSampler(local) as clk:
         if dist:
             dist.barrier()
@@ -270,6 +283,14 @@ def main():
             dist.barrier()
     ms = e0.elapsed_time(e1) / args.steps
     launches = sum(op.last_launches() for op in ops) * args.steps
+    phase = {}       # ms per step (both operators)
+    m2l_launch = []  # ms of the M2L kernel per launch, per operator
+    for op in ops:
+        for name, t in op.phase_times():
+            phase[name] = phase.get(name, 0.0) + t
+            if name == "m2l":
+                m2l_launch.append(t)
+        op.set_timing(False)
     value, sec = aggregate(ms / 1e3, len(ops) * N * n_rhs, dist, "cuda")
     ms = sec * 1e3
 
@@ -305,23 +326,23 @@ def main():
         got = y[0].numpy().reshape(3, N)[:, rows].reshape(-1)
         errs[type(K).__name__] = float(np.linalg.norm(got - exact) / np.linalg.norm(exact))
 
-    # -- per-phase times (CUDA events on the operator's stream) for the roofline
+    # -- roofline of the dominant kernel: the M2L products (one launch per
+    # operator and apply), timed by the events of the timed region
     hbm, bf16, peak_kind = peaks()
-    phase = {}
-    for op in ops:
-        op.set_timing(True)
-        op.apply(xd)
-        for name, t in op.phase_times():
-            phase[name] = phase.get(name, 0.0) + t
-        op.set_timing(False)
-    torch.cuda.synchronize()
-    m2l_ms = phase.get("m2l", float("nan"))
-    flops = sum(m2l_flops(op, n_rhs) for op in ops)
-    achieved = flops / (m2l_ms / 1e3) / 1e12
+    fl = [m2l_flops(op, n_rhs) for op in ops]
+    launch_s = float(np.mean(m2l_launch)) / 1e3
+    tensor = fl[0]["tensor"] is not None and all(op.tc_tile() > 0 for op in ops)
+    per_launch = float(np.mean([f["tensor" if tensor else "reference"] for f in fl]))
+    achieved = per_launch / launch_s / 1e12
+    ref_form = float(np.mean([f["reference"] for f in fl]))
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("m2l_bytes_per_launch")
+        # DRAM bytes per M2L pair of the tensor kernel, from an ncu capture of a
+        # smaller case (the traffic grows with the pairs processed)
+        per_pair = json.load(open(tpath)).get("m2l_tc_dram_bytes_per_pair")
+        if per_pair and tensor:
+            traffic = per_pair * float(np.mean([f["pairs"] for f in fl])) * n_rhs
 
     # -- the plain FP64 form on the same workload
     plain = None
@@ -368,11 +389,17 @@ def main():
                     "h2d_bytes_per_step": 2 * 8 * X.size,
                     "d2h_bytes_per_step": 8 * sum(y.numel() for y in yh)},
             "gpu_launches": launches,
-            "roofline": {"bound": "tensor", "kernel": "M2L grouped GEMM", "achieved": achieved,
-                         "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+            "roofline": {"bound": "tensor",
+                         "kernel": ("tc_gemm_kernel: compressed M2L products, tcgen05 3xBF16"
+                                    if tensor else "grouped_gemm_kernel: M2L products, FP32 SIMT"),
+                         "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                         "frac": achieved / bf16,
                          "peak_kind": peak_kind + " bf16 dense (burst)",
                          "traffic": traffic,
-                         "algorithmic_flops_per_step": flops},
+                         "flops_per_launch": per_launch,
+                         "launch_ms": launch_s * 1e3,
+                         "reference_form_flops_per_launch": ref_form,
+                         "reference_form_effective_tflops": ref_form / launch_s / 1e12},
             "phases_ms": phase,
             "rel_err_vs_direct": errs,
             "plain_fp64": plain,

@@ -64,7 +64,8 @@ typedef struct {
     int device;            /* CUDA device ordinal                                */
     double svd_threshold;  /* singular-value cutoff (reference: 1e-10, fmm.cpp:122) */
     int m2l_path;          /* precision form's dense translations:
-                              0 auto (= 4 where the M2L operators are precomputed),
+                              0 auto (= 5 where the M2L operators are precomputed
+                                and compress; SIMT FP32 otherwise),
                               1 SIMT FP32 for all (uncompressed M2L),
                               2 tcgen05 3xBF16 for the uncompressed M2L only,
                               3 tcgen05 3xBF16 for M2L, M2M and L2L,
@@ -138,9 +139,12 @@ long tbem_fmm_n_c2e_levels(const TbemFmm* h, int which);
 int tbem_fmm_get_c2e(const TbemFmm* h, int which, long level, double* out);
 int tbem_fmm_set_c2e(TbemFmm* h, int which, long level, const double* op);
 
-/* Per-phase device times (ms) of the last apply, measured with CUDA events
- * when timing is enabled (tbem_fmm_set_timing).  names/ms are NULL-able;
- * returns the number of phases. */
+/* Per-phase device times: with timing enabled (tbem_fmm_set_timing) every
+ * apply records CUDA events between its phases on its own stream, without
+ * synchronizing.  tbem_fmm_phase_times waits for them and returns the mean
+ * milliseconds per apply of every phase over the applies since the previous
+ * call (the same numbers again when no apply ran since).  names/ms are
+ * NULL-able; returns the number of phases. */
 int tbem_fmm_set_timing(TbemFmm* h, int enabled);
 int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int cap);
 

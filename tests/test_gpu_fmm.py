@@ -279,3 +279,24 @@ def test_torch_device_tensors():
     y_np = op.apply(x)
     y_t = op.apply(torch.tensor(x, device="cuda"))
     assert y_t.is_cuda and rel(y_t.cpu().numpy(), y_np) < 1e-12  # float atomics order
+
+
+def test_phase_timing_means_over_applies():
+    """tbem_fmm_phase_times: mean device ms per apply of every phase over the
+    applies since the previous read; no apply synchronizes for it."""
+    torch = pytest.importorskip("torch")
+    from tbempy import ThreeD, meshes
+    locs, nrm, w = meshes.sphere_points(3)
+    op = ThreeD.FMMOperator(ThreeD.ElasticDisplacement(1.0, 0.25), locs, nrm, locs, nrm, w,
+                            ThreeD.FMMConfig(0.3, 296, 40, 0.05, False), precision="mixed")
+    x = torch.rand(op.n_cols(), dtype=torch.float64, device="cuda")
+    op.set_timing(True)
+    for _ in range(3):
+        op.apply(x)
+    ph = dict(op.phase_times())
+    assert {"gather", "p2m", "m2m", "p2p", "m2l", "l2l", "l2p", "scatter"} <= set(ph)
+    assert all(t >= 0 for t in ph.values()) and ph["m2l"] > 0
+    assert dict(op.phase_times()) == ph  # nothing new: the same numbers
+    op.set_timing(False)
+    op.apply(x)
+    assert dict(op.phase_times()) == ph
