@@ -337,12 +337,10 @@ def main():
     ref_form = float(np.mean([f["reference"] for f in fl]))
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        # DRAM bytes per M2L pair of the tensor kernel, from an ncu capture of a
-        # smaller case (the traffic grows with the pairs processed)
-        per_pair = json.load(open(tpath)).get("m2l_tc_dram_bytes_per_pair")
-        if per_pair and tensor:
-            traffic = per_pair * float(np.mean([f["pairs"] for f in fl])) * n_rhs
+    if os.path.exists(tpath) and tensor and args.grid == N_GRID and n_rhs == 1:
+        # DRAM bytes of one launch of the tensor kernel on this workload, from a
+        # one-pass ncu capture (profiles/tc_gemm_dram_elastic_fault_98k.md)
+        traffic = json.load(open(tpath)).get("m2l_tc_dram_bytes_per_launch")
 
     # -- the plain FP64 form on the same workload
     plain = None
