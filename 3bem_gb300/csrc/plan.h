@@ -175,8 +175,12 @@ struct GemmSet {
                   cudaStream_t s, long* launches = nullptr);
     // tensor-core path (B taken from P's split planes; D columns of P.m rows);
     // nn = elements per operator in the pool the groups' offsets refer to
-    DBuf<int> d_op;
-    std::map<int, std::pair<DBuf<int>, DBuf<int>>> tc_tiles;
+    struct TcTiles {
+        DBuf<int> op;          // per column tile: operator index
+        DBuf<int> brow, drow;  // per column tile and column: B row / D column, -1 past the end
+        int n = 0;
+    };
+    std::map<int, TcTiles> tc_tiles;  // per (nrhs, N tile)
     int tc_bn = 128;  // N tile of the tensor-core path (128 or 64; autotuned)
     void run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn, cudaStream_t s,
                 long* launches);

@@ -65,17 +65,12 @@ struct TcArgs {
     const __nv_bfloat16* A[TC_TERMS];  // [op][m_pad][k_pad] per term
     long a_op_stride;                  // m_pad * k_pad
     int k_pad;
-    const int* g_op;                   // per group: operator index
-    const long* g_pair0;
-    const int* g_npairs;
-    const int* tile_group;
-    const int* tile_col0;
-    const int* in_cell;
-    const int* out_cell;
+    const int* tile_op;    // per column tile: operator index
+    const int* tile_brow;  // per column tile and column: B row (cell * nrhs + rhs), -1 past the end
+    const int* tile_drow;  // per column tile and column: D column (cell * nrhs + rhs), -1 past the end
     const __nv_bfloat16* B[TC_TERMS];  // [cell][rhs][k_pad] per term
     float* D;                          // [cell][rhs][n]
     int n;
-    int nrhs;
     int atomic;
     int* err;
 };
@@ -225,25 +220,25 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
         constexpr int B_PER = BN * 8 / TC_PRODUCERS;     // 8 (BN = 128) or 4 (BN = 64)
         const int pt = tid - 128;
         const int pj = pt % 8, prow = pt / 8;  // piece within a row; rows prow + 16 i
+        // the next tile's operator and B rows, loaded one tile ahead (plain
+        // independent loads: their latency hides behind the current tile)
+        int nop = 0, nb[B_PER];
+        auto prefetch = [&](int t) {
+            const int tile = t / m_tiles;
+            nop = a.tile_op[tile];
+#pragma unroll
+            for (int i = 0; i < B_PER; i++) nb[i] = a.tile_brow[(long)tile * BN + prow + 16 * i];
+        };
+        if (blockIdx.x < total) prefetch(blockIdx.x);
         int j = 0;  // chunks issued (over all tiles of this CTA)
         bool ok = true;
         for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
-            const int tile = t / m_tiles, m0 = (t % m_tiles) * TC_BM;
-            const int g = a.tile_group[tile];
-            const int col0 = a.tile_col0[tile];
-            const long pair0 = a.g_pair0[g];
-            const int ncols = a.g_npairs[g] * a.nrhs;
-            const long a_base = (long)a.g_op[g] * a.a_op_stride + (long)(m0 + prow) * a.k_pad + pj * 8;
+            const int m0 = (t % m_tiles) * TC_BM;
+            const long a_base = (long)nop * a.a_op_stride + (long)(m0 + prow) * a.k_pad + pj * 8;
             long boff[B_PER];
 #pragma unroll
-            for (int i = 0; i < B_PER; i++) {
-                const int c = col0 + prow + 16 * i;
-                boff[i] = -1;
-                if (c < ncols) {
-                    const int p = c / a.nrhs, r = c % a.nrhs;
-                    boff[i] = ((long)a.in_cell[pair0 + p] * a.nrhs + r) * a.k_pad + pj * 8;
-                }
-            }
+            for (int i = 0; i < B_PER; i++) boff[i] = nb[i] >= 0 ? (long)nb[i] * a.k_pad + pj * 8 : -1;
+            if (t + (int)gridDim.x < total) prefetch(t + gridDim.x);
             for (int kc = 0; kc < nk; kc++, j++) {
                 const int s = j % STAGES;
                 if (j >= STAGES && !wait(&empty_bar[s], ((j / STAGES) - 1) & 1)) {
@@ -328,31 +323,24 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
         }
     } else {
         // ---------------- epilogue (warps 0-3)
+        constexpr int NCC = BN / 32;
         int tc = 0;
         for (int t = blockIdx.x; t < total; t += gridDim.x, tc++) {
             const int b = tc & 1, bu = tc >> 1;
+            const int tile = t / m_tiles, m0 = (t % m_tiles) * TC_BM;
+            // lane q of a 32-column chunk resolves column q's destination; the
+            // loads overlap the wait for the accumulator
+            int drow[NCC];
+#pragma unroll
+            for (int cc = 0; cc < NCC; cc++) drow[cc] = a.tile_drow[(long)tile * BN + cc * 32 + lane];
             if (!wait(&accf_bar[b], bu & 1)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int tile = t / m_tiles, m0 = (t % m_tiles) * TC_BM;
-            const int g = a.tile_group[tile];
-            const int col0 = a.tile_col0[tile];
-            const long pair0 = a.g_pair0[g];
-            const int ncols = a.g_npairs[g] * a.nrhs;
             const int row = m0 + warp * 32 + lane;
-#pragma unroll 1
-            for (int cc = 0; cc < BN / 32; cc++) {
+#pragma unroll
+            for (int cc = 0; cc < NCC; cc++) {
                 float v[32], w[32];
                 const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + b * 2 * BN + cc * 32;
-                // lane q resolves column q's destination once; the stores below
-                // take it by shuffle instead of a load behind every store
-                long my_off = -1;
-                {
-                    const int col = col0 + cc * 32 + lane;
-                    if (col < ncols) {
-                        const int p = col / a.nrhs, r = col % a.nrhs;
-                        my_off = ((long)a.out_cell[pair0 + p] * a.nrhs + r) * a.n;
-                    }
-                }
+                const long my_off = drow[cc] >= 0 ? (long)drow[cc] * a.n : -1;
                 tmem_ld32(lane_base + BN, v);  // small terms first
                 tmem_ld32(lane_base, w);
 #pragma unroll
@@ -475,26 +463,35 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
                      long* launches)
 {
     if (empty()) return;
-    if (d_op.n == 0) {
-        std::vector<int> op(A_off.size());
-        for (size_t g = 0; g < A_off.size(); g++) op[g] = (int)(A_off[g] / nn);
-        d_op.upload(op);
-    }
     const int bn = tc_bn == 64 ? 64 : 128;
     const int key = nrhs * 1024 + bn;
     auto it = tc_tiles.find(key);
     if (it == tc_tiles.end()) {
-        std::vector<int> tg, tc;
+        // column tiles of every group, with each column's B row and D column
+        std::vector<int> op, brow, drow;
         for (size_t g = 0; g < npairs.size(); g++) {
             const int ncols = npairs[g] * nrhs;
             for (int c = 0; c < ncols; c += bn) {
-                tg.push_back((int)g);
-                tc.push_back(c);
+                op.push_back((int)(A_off[g] / nn));
+                for (int jj = 0; jj < bn; jj++) {
+                    const int col = c + jj;
+                    if (col < ncols) {
+                        const long p = pair0[g] + col / nrhs;
+                        const int r = col % nrhs;
+                        brow.push_back(in_cell[p] * nrhs + r);
+                        drow.push_back(out_cell[p] * nrhs + r);
+                    } else {
+                        brow.push_back(-1);
+                        drow.push_back(-1);
+                    }
+                }
             }
         }
-        auto& e = tc_tiles[key];
-        e.first.upload(tg);
-        e.second.upload(tc);
+        TcTiles& e = tc_tiles[key];
+        e.op.upload(op);
+        e.brow.upload(brow);
+        e.drow.upload(drow);
+        e.n = (int)op.size();
         it = tc_tiles.find(key);
     }
     TcArgs a;
@@ -504,19 +501,14 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
     }
     a.a_op_stride = (long)P.m_pad * P.k_pad;
     a.k_pad = P.k_pad;
-    a.g_op = d_op.p;
-    a.g_pair0 = d_pair0.p;
-    a.g_npairs = d_npairs.p;
-    a.tile_group = it->second.first.p;
-    a.tile_col0 = it->second.second.p;
-    a.in_cell = d_in.p;
-    a.out_cell = d_out.p;
+    a.tile_op = it->second.op.p;
+    a.tile_brow = it->second.brow.p;
+    a.tile_drow = it->second.drow.p;
     a.D = D;
     a.n = P.m;
-    a.nrhs = nrhs;
     a.atomic = atomic;
     a.err = P.err.p;
-    const int n_ctiles = (int)it->second.first.n, m_tiles = P.m_pad / TC_BM;
+    const int n_ctiles = it->second.n, m_tiles = P.m_pad / TC_BM;
     const long total = (long)n_ctiles * m_tiles;
     if (total == 0) return;
     int dev = 0, sms = 0;
