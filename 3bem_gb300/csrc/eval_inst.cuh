@@ -18,9 +18,12 @@ cudaError_t go(int nr, int n_items, int tpt, const void* args, cudaStream_t s)
 {
     const EvalArgs<T>& a = *static_cast<const EvalArgs<T>*>(args);
     if (n_items <= 0) return cudaSuccess;
-    // the point-to-point pass has autotuned variants; every other pass uses 4
+    // the point-to-point pass (2, 4, 8) and the points-to-check-surface pass
+    // (1, 2, 4) have autotuned variants; every other pass uses 4
     if (!TR && !TS && !SS && tpt == 2) go_tpt<T, TR, TS, SS, 2>(nr, n_items, a, s);
     else if (!TR && !TS && !SS && tpt == 8) go_tpt<T, TR, TS, SS, 8>(nr, n_items, a, s);
+    else if (!TR && TS && !SS && tpt == 1) go_tpt<T, TR, TS, SS, 1>(nr, n_items, a, s);
+    else if (!TR && TS && !SS && tpt == 2) go_tpt<T, TR, TS, SS, 2>(nr, n_items, a, s);
     else go_tpt<T, TR, TS, SS, 4>(nr, n_items, a, s);
     return cudaGetLastError();
 }
@@ -34,7 +37,7 @@ cudaError_t go_t(const EvalLaunch& L, const void* args, cudaStream_t s)
     switch (idx) {
     case 0: return go<T, false, false, false>(nr, L.n_items, L.tpt, args, s);
     case 1: return go<T, false, false, true>(nr, L.n_items, 4, args, s);
-    case 2: return go<T, false, true, false>(nr, L.n_items, 4, args, s);
+    case 2: return go<T, false, true, false>(nr, L.n_items, L.tpt, args, s);
     case 3: return go<T, false, true, true>(nr, L.n_items, 4, args, s);
     case 4: return go<T, true, false, false>(nr, L.n_items, 4, args, s);
     case 5: return go<T, true, false, true>(nr, L.n_items, 4, args, s);

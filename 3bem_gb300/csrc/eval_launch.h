@@ -11,7 +11,8 @@ struct EvalLaunch {
     bool tgt_surf;
     bool src_surf;
     int n_items;
-    int tpt = 4;  // threads per target (2, 4 or 8 for the point-to-point pass; 4 otherwise)
+    int tpt = 4;  // threads per target (2, 4 or 8 for the point-to-point pass, 1, 2 or 4
+                  // for points to a check surface; 4 otherwise)
 };
 
 // One function per kernel id (eval_k<id>.cu) so that the instantiations

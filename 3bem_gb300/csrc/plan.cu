@@ -378,23 +378,34 @@ __global__ void __launch_bounds__(256) l2p_mixed_kernel(const float* E, const lo
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
     const int rows = npts[t] * R;
     const float* c0 = cd + (long)leaf[t] * nrhs * n;
+    const float4* cv = reinterpret_cast<const float4*>(c);
     for (int r = 0; r < nrhs; r++) {
         __syncthreads();
         for (int k = threadIdx.x; k < ld; k += blockDim.x) c[k] = k < n ? c0[(long)r * n + k] : 0.f;
         __syncthreads();
-        for (int row = warp; row < rows; row += nw) {
-            const float4* e = reinterpret_cast<const float4*>(E + (row0[t] + row) * (long)ld);
-            const float4* cv = reinterpret_cast<const float4*>(c);
-            float acc = 0.f;
+        // four rows per warp at a time: their loads are in flight together; E
+        // is read once per apply, so it streams past L2 (evict-first loads)
+        for (int rb = warp * 4; rb < rows; rb += nw * 4) {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
             for (int k4 = lane; k4 < ld / 4; k4 += 32) {
-                const float4 a = __ldg(e + k4), b = cv[k4];
-                acc += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+                const float4 b = cv[k4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (rb + q < rows) {
+                        const float4 a = __ldcs(reinterpret_cast<const float4*>(E + (row0[t] + rb + q) * (long)ld) + k4);
+                        acc[q] += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+                    }
+                }
             }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) {
+            for (int q = 0; q < 4; q++)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+            if (lane < 4 && rb + lane < rows) {
+                const int row = rb + lane;
+                const float v = lane == 0 ? acc[0] : lane == 1 ? acc[1] : lane == 2 ? acc[2] : acc[3];
                 const int i = row / R, d = row % R;
-                y[((long)r * R + d) * y_n + pt0[t] + i] += (double)acc;
+                y[((long)r * R + d) * y_n + pt0[t] + i] += (double)v;
             }
         }
     }
@@ -540,6 +551,8 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     TBEM_CK(cudaStreamSynchronize(stream));
     if (opt.p2p_block == 2 || opt.p2p_block == 4 || opt.p2p_block == 8) p2p_tpt = opt.p2p_block;
     else autotune_p2p();
+    if (opt.p2m_block == 1 || opt.p2m_block == 2 || opt.p2m_block == 4) p2m_tpt = opt.p2m_block;
+    else autotune_p2m();
     autotune_tc();
 }
 
@@ -630,6 +643,47 @@ void Plan::autotune_p2p()
     p2p_tpt = best_tpt;
 }
 
+// Picks the points-to-check-surface pass's threads per target (1, 2 or 4)
+// the same way: each variant timed on this operator's own leaves.
+void Plan::autotune_p2m()
+{
+    if (p2m.n_items() == 0) return;
+    ensure_rhs(1);
+    const bool mixed = f.mixed;
+    if (mixed) TBEM_CK(cudaMemsetAsync(s32.p, 0, sizeof(float) * R * n_src, stream));
+    else TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * n_src, stream));
+    cudaEvent_t e0, e1;
+    TBEM_CK(cudaEventCreate(&e0));
+    TBEM_CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_tpt = 4;
+    for (int tpt : {4, 2, 1}) {
+        p2m_tpt = tpt;
+        float ms = 0.f;
+        for (int rep = 0; rep < 3; rep++) {
+            TBEM_CK(cudaEventRecord(e0, stream));
+            if (mixed)
+                eval<float>(p2m_set(), f.ks_kid, true, false, *stree, *dsrc, f.r_uc, *dsrc, 0, s32.p, n_src,
+                            nullptr, nullptr, 0, cu32.p, 0, 1, stream, false);
+            else
+                eval<double>(p2m_set(), f.ks_kid, true, false, *stree, *dsrc, f.r_uc, *dsrc, 0, s64.p, n_src,
+                             nullptr, nullptr, 0, cu64.p, 0, 1, stream, false);
+            TBEM_CK(cudaEventRecord(e1, stream));
+            TBEM_CK(cudaEventSynchronize(e1));
+            float t = 0.f;
+            TBEM_CK(cudaEventElapsedTime(&t, e0, e1));
+            if (rep > 0) ms += t;
+        }
+        if (ms < best) {
+            best = ms;
+            best_tpt = tpt;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p2m_tpt = best_tpt;
+}
+
 void Plan::build_tasks()
 {
     const Tree& O = otree;
@@ -639,6 +693,8 @@ void Plan::build_tasks()
     for (int c : L.p2m) {
         const Cell& cc = S.cells[c];
         p2m.add(c, ns, cc.center, {{cc.pt_begin, (int)cc.n_points()}}, TPB);
+        p2m_tpt1.add(c, ns, cc.center, {{cc.pt_begin, (int)cc.n_points()}}, EVAL_THREADS);
+        p2m_tpt2.add(c, ns, cc.center, {{cc.pt_begin, (int)cc.n_points()}}, EVAL_THREADS / 2);
     }
     std::vector<std::vector<int>> p2p_of(O.cells.size()), m2p_of(O.cells.size()),
         p2l_of(O.cells.size()), m2l_of(O.cells.size());
@@ -705,7 +761,9 @@ void Plan::build_tasks()
     }
     p2p_tpt2.tpt = 2;
     p2p_tpt8.tpt = 8;
-    for (TaskSet* t : {&p2m, &p2p, &p2p_tpt2, &p2p_tpt8, &m2p, &p2l, &l2p, &m2l_fly, &p2m_t, &p2p_t,
+    p2m_tpt1.tpt = 1;
+    p2m_tpt2.tpt = 2;
+    for (TaskSet* t : {&p2m, &p2m_tpt1, &p2m_tpt2, &p2p, &p2p_tpt2, &p2p_tpt8, &m2p, &p2l, &l2p, &m2l_fly, &p2m_t, &p2p_t,
                        &m2p_t, &p2l_t, &l2p_t, &m2l_fly_t})
         t->upload();
 
@@ -1659,7 +1717,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
         TBEM_CK(cudaMemsetAsync(cu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
         TBEM_CK(cudaMemsetAsync(cd64.p, 0, sizeof(double) * nco * nrhs * n, s));
         mark("gather", s);
-        eval<double>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cu64.p, 0, nrhs, s, false);
+        eval<double>(p2m_set(), F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s64.p, NS, nullptr, nullptr, 0, cu64.p, 0, nrhs, s, false);
         mark("p2m", s);
         for (int l = S.n_levels() - 1; l >= 0; l--) {
             if (l < (int)F.m2m.size()) F.m2m[l].run<double>(qu64.p, cu64.p, n, nrhs, 0, GEMM_WAVES, s, &launches);
@@ -1690,7 +1748,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
         TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
         TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
         mark("gather", s);
-        eval<float>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
+        eval<float>(p2m_set(), F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
         mark("p2m", s);
         for (int l = S.n_levels() - 1; l >= 0; l--) {
             if (l >= (int)F.m2m.size() || F.m2m[l].empty()) continue;
@@ -1865,7 +1923,7 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     TBEM_CK(cudaMemsetAsync(cdc32.p, 0, sizeof(float) * nco * nrhs * ro, s));
     mark("gather", s);
     // P2M into the leaves' check potentials, then u~ = P_l u
-    eval<float>(p2m, F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
+    eval<float>(p2m_set(), F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
     F.comp_p2m.run_rect<float>(cu32.p, cuc32.p, ri, n, n, nrhs, 0, GEMM_ATOMIC, s, &launches);  // into zeros
     mark("p2m", s);
     for (int l = S.n_levels() - 1; l >= 0; l--)

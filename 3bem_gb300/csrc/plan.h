@@ -267,6 +267,11 @@ struct Plan {
     // point-to-point variants for 2 and 8 threads per target (autotuned)
     TaskSet p2p_tpt2, p2p_tpt8;
     int p2p_tpt = 4;
+    // points-to-check-surface variants for 1 and 2 threads per target (autotuned)
+    TaskSet p2m_tpt1, p2m_tpt2;
+    int p2m_tpt = 4;
+    void autotune_p2m();
+    const TaskSet& p2m_set() const { return p2m_tpt == 1 ? p2m_tpt1 : p2m_tpt == 2 ? p2m_tpt2 : p2m; }
     void autotune_p2p();
     void autotune_tc();  // N tile (128 / 64) of the tensor-core translations
     const TaskSet& p2p_set() const { return p2p_tpt == 2 ? p2p_tpt2 : p2p_tpt == 8 ? p2p_tpt8 : p2p; }

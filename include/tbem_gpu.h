@@ -77,7 +77,9 @@ typedef struct {
     double m2l_rank_tol;   /* compressed M2L: singular values of the stacked M2L
                               operators kept down to this fraction of the largest
                               (0: 1e-7)                                           */
-    int reserved[2];
+    int p2m_block;         /* 0 auto; else threads per target in the points-to-
+                              check-surface kernel (1, 2, 4)                      */
+    int reserved[1];
 } TbemGpuOptions;
 
 typedef struct TbemFmm TbemFmm;

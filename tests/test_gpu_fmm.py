@@ -71,6 +71,22 @@ def test_plain_matches_oracle(name, small):
     assert rel(y, y_orc) < 1e-10
 
 
+@pytest.mark.parametrize("block", [1, 2, 4])
+def test_p2m_variants_match_oracle(block):
+    """Every threads-per-target variant of the points-to-check-surface pass
+    (the autotuner's candidates) gives the reference's plain-form result."""
+    from tbempy import ThreeD
+    locs, nrm, w = cloud(800, 1)
+    for name in ("LaplaceDouble", "ElasticTraction"):
+        order = 35 if name.startswith("Laplace") else 20
+        orc = oracle.OracleFMM(name, locs, nrm, locs, nrm, w, 0.3, order, 25, 0.05, False)
+        op = ThreeD.FMMOperator(kernel_obj(name), locs, nrm, locs, nrm, w,
+                                ThreeD.FMMConfig(0.3, order, 25, 0.05, False), p2m_block=block)
+        inject(op, orc)
+        x = np.random.default_rng(2).uniform(-1, 1, op.n_cols())
+        assert rel(op.apply(x), orc.apply(x)) < 1e-10
+
+
 @pytest.mark.parametrize("name", KERNELS)
 def test_trees_and_lists_match_oracle(name):
     locs, nrm, w = cloud(700, 3)
