@@ -13,9 +13,10 @@ operator to the slip (2 x 98,304 points x RHS).  ``value`` is whole-job
 points*RHS/s of the precision (mixed) form with inputs resident in HBM;
 ``e2e`` is the same through the public C ABI with host buffers (the host to
 device copy of the slip and the device to host copy of the result are inside
-the timed region).  The operator tables (0.6 GB of M2L operator planes and
-0.3 GB of per-leaf L2P operators per kernel) are far larger than the 129 MB
-L2, so no L2 flush is needed between steps.
+the timed region).  L2 is flushed (256 MB written) before every timed step,
+outside the step's timing: the per-leaf L2P operators (0.3 GB per kernel) are
+larger than the 129 MB L2, but the M2L operator planes (42 MB per kernel)
+alone would stay resident.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -203,7 +204,7 @@ def config_dict(n_rhs):
             "n_points": 3 * 2 * N_GRID * N_GRID, "n_rhs": n_rhs,
             "precision": "mixed: far field in the M2L SVD bases (FP32), M2L products on "
                          "tcgen05 3xBF16, P2P FP32 compensated",
-            "l2": "operator tables (0.9 GB per kernel) >> 129 MB L2; no flush needed"}
+            "l2": "flushed before every timed step (256 MB write, outside the step timing)"}
 
 
 def main():
@@ -262,6 +263,7 @@ def main():
 
     for _ in range(args.warmup):
         step()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
     torch.cuda.synchronize()
 
     # -- device-resident timed region (per-phase CUDA events recorded on the
@@ -273,15 +275,19 @@ def main():
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
+        # L2 flushed before every timed step (a 256 MB write, outside the
+        # step's events): the M2L operator planes alone would fit in L2
+        pairs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                 for _ in range(args.steps)]
+        for e0, e1 in pairs:
+            flush.fill_(1)
+            e0.record(stream)
             step()
-        e1.record(stream)
+            e1.record(stream)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in pairs) / args.steps
     launches = sum(op.last_launches() for op in ops) * args.steps
     phase = {}       # ms per step (both operators)
     m2l_launch = []  # ms of the M2L kernel per launch, per operator
@@ -310,10 +316,14 @@ def main():
         step_e2e()
     if dist:
         dist.barrier()
-    t0 = time.perf_counter()
+    e2e_s = 0.0
     for _ in range(args.steps):
-        step_e2e()
-    e2e_s = (time.perf_counter() - t0) / args.steps
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_e2e()  # ends with the device-to-host copies of the results
+        e2e_s += time.perf_counter() - t0
+    e2e_s /= args.steps
     e2e_value, e2e_s = aggregate(e2e_s, len(ops) * N * n_rhs, dist, "cuda")
 
     # -- accuracy against the FP64 direct sum on 4,096 random rows
