@@ -576,9 +576,14 @@ void Plan::autotune_tc()
     TBEM_CK(cudaEventCreate(&e0));
     TBEM_CK(cudaEventCreate(&e1));
     float best = 1e30f;
-    int best_bn = 128;
-    for (int bn : {128, 64}) {
-        G.tc_bn = bn;
+    int best_bn = 128, best_bk = 64;
+    const int shapes[3][2] = {{128, 64}, {64, 64}, {128, 32}};
+    const int fixed = opt.tc_shape >= 1 && opt.tc_shape <= 3 ? opt.tc_shape - 1 : -1;
+    for (int si = 0; si < 3; si++) {
+        const auto& sh = shapes[si];
+        if (fixed >= 0 && si != fixed) continue;
+        G.tc_bn = sh[0];
+        G.tc_bk = sh[1];
         float ms = 1e30f;  // best of five (the first also builds the tile tables)
         for (int rep = 0; rep < 6; rep++) {
             TBEM_CK(cudaEventRecord(e0, stream));
@@ -591,14 +596,16 @@ void Plan::autotune_tc()
         }
         if (ms < best) {
             best = ms;
-            best_bn = bn;
+            best_bn = sh[0];
+            best_bk = sh[1];
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     G.tc_bn = best_bn;
-    for (auto& g : f.m2m) g.tc_bn = best_bn;
-    for (auto& g : f.l2l) g.tc_bn = best_bn;
+    G.tc_bk = best_bk;
+    for (auto& g : f.m2m) { g.tc_bn = best_bn; g.tc_bk = best_bk; }
+    for (auto& g : f.l2l) { g.tc_bn = best_bn; g.tc_bk = best_bk; }
 }
 
 // Picks the point-to-point pass's threads per target (2, 4 or 8) by timing

@@ -182,6 +182,7 @@ struct GemmSet {
     };
     std::map<int, TcTiles> tc_tiles;  // per (nrhs, N tile)
     int tc_bn = 128;  // N tile of the tensor-core path (128 or 64; autotuned)
+    int tc_bk = 64;   // K chunk (64, or 32 with N = 128; autotuned)
     void run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn, cudaStream_t s,
                 long* launches);
 };

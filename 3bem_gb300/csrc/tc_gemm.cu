@@ -38,25 +38,30 @@
 
 namespace tbem {
 
-constexpr int TC_BM = 128, TC_BK = 64;
+constexpr int TC_BM = 128, TC_BK = 64;                       // TC_BK: the planes' K padding
 constexpr int TC_TERMS = 3;                                  // bf16 terms per operand
-constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;            // 16 KB: one 128 x 64 bf16 A plane tile
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
 
-// Tile shapes (the autotuner picks one per operator set): N = 128 columns
-// with a 2-stage ring, or N = 64 columns with a 3-stage ring.
-template <int BN>
+// Tile shapes (the autotuner picks one per operator set): N = 128 columns and
+// 64-deep K chunks (128-byte rows, 128B swizzle) in a 2-stage ring; N = 64,
+// 64-deep, 3 stages; N = 128 with 32-deep chunks (64-byte rows, 64B swizzle)
+// in a 4-stage ring, which keeps three chunks in flight.
+template <int BN, int BK>
 struct TcShape {
-    static constexpr int STAGES = BN == 128 ? 2 : 3;
-    static constexpr int B_TILE = BN * TC_BK * 2;                         // one B plane tile
-    static constexpr int STAGE_BYTES = TC_TERMS * (TC_TILE_BYTES + B_TILE);
+    static_assert(BK == 64 || BK == 32, "K chunk");
+    static constexpr int RB = BK * 2;                                     // bytes per tile row
+    static constexpr int STAGES = BK == 32 ? 4 : (BN == 128 ? 2 : 3);
+    static constexpr int A_TILE = TC_BM * RB;                             // one A plane tile
+    static constexpr int B_TILE = BN * RB;                                // one B plane tile
+    static constexpr int STAGE_BYTES = TC_TERMS * (A_TILE + B_TILE);
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
     static constexpr uint32_t TMEM_COLS = 4 * BN;  // 2 buffers x (big, small) accumulators
     // kind::f16, bf16 A/B, FP32 D, K-major A and B, M = 128, N = BN
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
                                       ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
 };
-static_assert(TcShape<128>::SMEM_BYTES <= 227 * 1024 && TcShape<64>::SMEM_BYTES <= 227 * 1024,
+static_assert(TcShape<128, 64>::SMEM_BYTES <= 227 * 1024 && TcShape<64, 64>::SMEM_BYTES <= 227 * 1024 &&
+                  TcShape<128, 32>::SMEM_BYTES <= 227 * 1024,
               "shared memory budget");
 constexpr int TC_PRODUCERS = 128;                      // producer threads (warps 4-7)
 constexpr int TC_THREADS_P = 128 + TC_PRODUCERS + 32;  // epilogue + producers + MMA warp
@@ -82,17 +87,27 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p)
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+// Shared-memory matrix descriptor: K-major rows of RB bytes with the RB-byte
+// swizzle (128 or 64), 8-row groups 8 * RB bytes apart.
+template <int RB>
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr)
 {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-    d |= (uint64_t)1 << 16;             // leading byte offset (unused with this swizzle)
-    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
-    d |= (uint64_t)1 << 46;             // descriptor version
-    d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+    d |= (uint64_t)1 << 16;                  // leading byte offset (unused with a swizzle)
+    d |= (uint64_t)((8 * RB) >> 4) << 32;    // stride byte offset
+    d |= (uint64_t)1 << 46;                  // descriptor version
+    d |= (uint64_t)(RB == 128 ? 2 : 4) << 61;  // SWIZZLE_128B / SWIZZLE_64B
     return d;
+}
+
+// Position of 16-byte piece j of tile row r under the RB-byte swizzle: the
+// piece index XOR the row's position inside the 1024-byte (128B) or
+// 512-byte (64B) swizzle atom.
+template <int RB>
+__device__ __forceinline__ uint32_t sw_piece(int row, int j)
+{
+    return RB == 128 ? (uint32_t)(j ^ (row & 7)) : (uint32_t)(j ^ ((row >> 1) & 3));
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
@@ -156,12 +171,15 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
 }
 
-template <int BN>
+template <int BN, int BK>
 __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a, int n_ctiles, int m_tiles)
 {
-    using Sh = TcShape<BN>;
+    using Sh = TcShape<BN, BK>;
+    constexpr int RB = Sh::RB;
     constexpr int STAGES = Sh::STAGES;
-    constexpr int B_BASE = TC_TERMS * TC_TILE_BYTES;  // B planes follow the A planes
+    constexpr int LAG = STAGES - 1;  // chunks a producer keeps in flight before a hand-over
+    static_assert(LAG >= 1 && LAG <= 3, "stage count");
+    constexpr int B_BASE = TC_TERMS * Sh::A_TILE;  // B planes follow the A planes
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accf_bar[2], acce_bar[2], drain_bar;
     __shared__ uint32_t tmem_slot;
@@ -169,7 +187,7 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
     uint8_t* smem = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    const int nk = a.k_pad / TC_BK;
+    const int nk = a.k_pad / BK;
     const int total = n_ctiles * m_tiles;
 
     if (warp == 0) {
@@ -213,13 +231,15 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
 
     bool mma_issued = false;
     if (warp >= 4 && warp < 8) {
-        // ---------------- producers.  A plane tile is 128 rows of eight 16-byte
-        // pieces; piece e = pt + 128 i is row e / 8, piece e % 8, so one warp
-        // instruction copies four whole rows (full sectors, coalesced).
-        constexpr int A_PER = TC_BM * 8 / TC_PRODUCERS;  // 8 pieces of A per thread and plane
-        constexpr int B_PER = BN * 8 / TC_PRODUCERS;     // 8 (BN = 128) or 4 (BN = 64)
+        // ---------------- producers.  A plane tile is 128 rows of PPR 16-byte
+        // pieces; piece e = pt + 128 i is row e / PPR, piece e % PPR, so one
+        // warp instruction copies whole rows (full sectors, coalesced).
+        constexpr int PPR = RB / 16;                       // pieces per row (8 or 4)
+        constexpr int RSTEP = TC_PRODUCERS / PPR;          // rows between a thread's pieces
+        constexpr int A_PER = TC_BM / RSTEP;               // pieces of A per thread and plane
+        constexpr int B_PER = BN / RSTEP;                  // pieces of B per thread and plane
         const int pt = tid - 128;
-        const int pj = pt % 8, prow = pt / 8;  // piece within a row; rows prow + 16 i
+        const int pj = pt % PPR, prow = pt / PPR;  // piece within a row; rows prow + RSTEP i
         // the next tile's operator and B rows, loaded one tile ahead (plain
         // independent loads: their latency hides behind the current tile)
         int nop = 0, nb[B_PER];
@@ -227,7 +247,7 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
             const int tile = t / m_tiles;
             nop = a.tile_op[tile];
 #pragma unroll
-            for (int i = 0; i < B_PER; i++) nb[i] = a.tile_brow[(long)tile * BN + prow + 16 * i];
+            for (int i = 0; i < B_PER; i++) nb[i] = a.tile_brow[(long)tile * BN + prow + RSTEP * i];
         };
         if (blockIdx.x < total) prefetch(blockIdx.x);
         int j = 0;  // chunks issued (over all tiles of this CTA)
@@ -246,20 +266,20 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
                     break;
                 }
                 const uint32_t st = smem0 + s * Sh::STAGE_BYTES;
-                const int k0 = kc * TC_BK;
+                const int k0 = kc * BK;
 #pragma unroll
                 for (int q = 0; q < TC_TERMS; q++) {
 #pragma unroll
                     for (int i = 0; i < A_PER; i++) {
-                        const int row = prow + 16 * i;
-                        const uint32_t dst = st + q * TC_TILE_BYTES + row * 128 + ((pj ^ (row & 7)) << 4);
-                        const __nv_bfloat16* src = a.A[q] + a_base + (long)16 * i * a.k_pad + k0;
+                        const int row = prow + RSTEP * i;
+                        const uint32_t dst = st + q * Sh::A_TILE + row * RB + (sw_piece<RB>(row, pj) << 4);
+                        const __nv_bfloat16* src = a.A[q] + a_base + (long)RSTEP * i * a.k_pad + k0;
                         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
                     }
 #pragma unroll
                     for (int i = 0; i < B_PER; i++) {
-                        const int row = prow + 16 * i;
-                        const uint32_t dst = st + B_BASE + q * Sh::B_TILE + row * 128 + ((pj ^ (row & 7)) << 4);
+                        const int row = prow + RSTEP * i;
+                        const uint32_t dst = st + B_BASE + q * Sh::B_TILE + row * RB + (sw_piece<RB>(row, pj) << 4);
                         const bool v = boff[i] >= 0;
                         // an invalid column is zero-filled (source size 0, nothing read)
                         const __nv_bfloat16* src = v ? a.B[q] + boff[i] + k0 : a.B[q];
@@ -269,18 +289,22 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
                     }
                 }
                 asm volatile("cp.async.commit_group;" ::: "memory");
-                if (j >= 1) {
-                    // the previous chunk's copies have landed: hand its stage over
-                    asm volatile("cp.async.wait_group 1;" ::: "memory");
+                if (j >= LAG) {
+                    // chunk j - LAG has landed: hand its stage over (LAG chunks
+                    // stay in flight behind it)
+                    if constexpr (LAG == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
+                    else if constexpr (LAG == 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
+                    else asm volatile("cp.async.wait_group 3;" ::: "memory");
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    mbar_arrive(smem_u32(&full_bar[(j - 1) % STAGES]));
+                    mbar_arrive(smem_u32(&full_bar[(j - LAG) % STAGES]));
                 }
             }
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
-        if (ok && j >= 1) {
+        if (ok) {
+            // hand over the chunks still held back
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(smem_u32(&full_bar[(j - 1) % STAGES]));
+            for (int q = max(0, j - LAG); q < j; q++) mbar_arrive(smem_u32(&full_bar[q % STAGES]));
         }
     } else if (warp == 8) {
         // ---------------- MMA issue (one thread)
@@ -301,18 +325,18 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t st = smem0 + s * Sh::STAGE_BYTES;
 #pragma unroll
-                    for (int kk = 0; kk < TC_BK / 16; kk++) {
+                    for (int kk = 0; kk < BK / 16; kk++) {
                         const uint32_t off = kk * 32;  // 16 bf16 along K inside the swizzle atom
-                        const uint32_t a0 = st + off, a1 = a0 + TC_TILE_BYTES, a2 = a0 + 2 * TC_TILE_BYTES;
+                        const uint32_t a0 = st + off, a1 = a0 + Sh::A_TILE, a2 = a0 + 2 * Sh::A_TILE;
                         const uint32_t b0 = st + B_BASE + off, b1 = b0 + Sh::B_TILE, b2 = b0 + 2 * Sh::B_TILE;
                         constexpr uint32_t ID = Sh::IDESC;
                         const uint32_t acc = (kc | kk) != 0;
-                        mma_bf16(big, sw128_desc(a0), sw128_desc(b0), ID, acc);
-                        mma_bf16(small, sw128_desc(a0), sw128_desc(b1), ID, acc);
-                        mma_bf16(small, sw128_desc(a1), sw128_desc(b0), ID, 1);
-                        mma_bf16(small, sw128_desc(a0), sw128_desc(b2), ID, 1);
-                        mma_bf16(small, sw128_desc(a1), sw128_desc(b1), ID, 1);
-                        mma_bf16(small, sw128_desc(a2), sw128_desc(b0), ID, 1);
+                        mma_bf16(big, sw_desc<RB>(a0), sw_desc<RB>(b0), ID, acc);
+                        mma_bf16(small, sw_desc<RB>(a0), sw_desc<RB>(b1), ID, acc);
+                        mma_bf16(small, sw_desc<RB>(a1), sw_desc<RB>(b0), ID, 1);
+                        mma_bf16(small, sw_desc<RB>(a0), sw_desc<RB>(b2), ID, 1);
+                        mma_bf16(small, sw_desc<RB>(a1), sw_desc<RB>(b1), ID, 1);
+                        mma_bf16(small, sw_desc<RB>(a2), sw_desc<RB>(b0), ID, 1);
                     }
                     mma_issued = true;
                     mma_commit(smem_u32(&empty_bar[s]));
@@ -429,10 +453,12 @@ void TcPlanes::build(const float* ops32, long n_ops, int m, int k, cudaStream_t 
     err.alloc(1);
     TBEM_CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
     // per device: set on every build (the plan's device is current)
-    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 TcShape<128>::SMEM_BYTES));
-    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 TcShape<64>::SMEM_BYTES));
+    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<128, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TcShape<128, 64>::SMEM_BYTES));
+    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TcShape<64, 64>::SMEM_BYTES));
+    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<128, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TcShape<128, 32>::SMEM_BYTES));
 }
 
 void TcPlanes::split_b(const float* cells, long rows, cudaStream_t s)
@@ -515,8 +541,12 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
     TBEM_CK(cudaGetDevice(&dev));
     TBEM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const unsigned grid = (unsigned)std::min<long>(total, std::max(sms, 1));
-    if (bn == 64) tc_gemm_kernel<64><<<grid, TC_THREADS_P, TcShape<64>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
-    else tc_gemm_kernel<128><<<grid, TC_THREADS_P, TcShape<128>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
+    if (bn == 64)
+        tc_gemm_kernel<64, 64><<<grid, TC_THREADS_P, TcShape<64, 64>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
+    else if (tc_bk == 32)
+        tc_gemm_kernel<128, 32><<<grid, TC_THREADS_P, TcShape<128, 32>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
+    else
+        tc_gemm_kernel<128, 64><<<grid, TC_THREADS_P, TcShape<128, 64>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
     TBEM_CK(cudaGetLastError());
     if (launches) (*launches)++;
 }

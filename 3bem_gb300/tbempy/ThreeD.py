@@ -168,7 +168,8 @@ class FMMOperator(OperatorI):
 
     def __init__(self, K, obs_locs, obs_normals, src_locs, src_normals, src_weights, config,
                  precision="fp64", device=0, svd_threshold=1e-10, host_only=False,
-                 m2l_path=0, m2l_rank_tol=1e-7, p2p_block=0, p2m_block=0, _handle=None):
+                 m2l_path=0, m2l_rank_tol=1e-7, p2p_block=0, p2m_block=0, tc_shape=0,
+                 _handle=None):
         self.K = K
         self.config = config
         self.precision = precision
@@ -191,6 +192,7 @@ class FMMOperator(OperatorI):
         opt.m2l_rank_tol = float(m2l_rank_tol)
         opt.p2p_block = int(p2p_block)
         opt.p2m_block = int(p2m_block)
+        opt.tc_shape = int(tc_shape)
         cfg = config._c()
         h = C.c_void_p()
         params = K.params()

@@ -24,7 +24,7 @@ class TbemFmmConfig(C.Structure):
 class TbemGpuOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("svd_threshold", C.c_double),
                 ("m2l_path", C.c_int), ("p2p_block", C.c_int), ("host_only", C.c_int),
-                ("m2l_rank_tol", C.c_double), ("p2m_block", C.c_int), ("reserved", C.c_int * 1)]
+                ("m2l_rank_tol", C.c_double), ("p2m_block", C.c_int), ("tc_shape", C.c_int)]
 
 
 class TbemError(RuntimeError):

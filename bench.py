@@ -414,6 +414,8 @@ def main():
             "cpu_baseline": cpu,
             "setup_s": setup_s,
             "m2l_ranks": [list(op.m2l_ranks()) for op in ops],
+            "tc_tiles": [op.tc_tile() for op in ops],
+            "p2p_threads_per_target": [op.p2p_block() for op in ops],
         }
         print(json.dumps(line), flush=True)
     if dist:
