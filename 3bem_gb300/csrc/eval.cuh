@@ -10,7 +10,9 @@
 // a fixed summation order.  TPT threads share a target and split its
 // sources; their partial sums meet in a warp-shuffle reduction.  Sources are
 // staged through shared memory in tiles of 128 that run across source-block
-// boundaries.  Coordinates are shifted to the task's origin (the target
+// boundaries (each source's position, normal and densities stored as
+// 4-vectors, one shared load each in the pair loop).  Coordinates are
+// shifted to the task's origin (the target
 // cell's centre) in FP64 before the pair arithmetic, so the FP32 variant
 // keeps full relative accuracy in the separations.  The FP32 variant sums
 // each tile in FP32 and folds the tile sums into a compensated (Kahan) pair.
@@ -65,6 +67,12 @@ struct EvalArgs {
     double scale;
 };
 
+// Four values of one source in shared memory, read with one vector load.
+template <typename T>
+struct alignas(4 * sizeof(T)) Vec4 {
+    T x, y, z, w;
+};
+
 template <typename T>
 __device__ __forceinline__ void kahan_add(T& hi, T& lo, T v)
 {
@@ -81,9 +89,10 @@ eval_kernel(const EvalArgs<T> a)
     constexpr int R = kernel_dim(KID);
     constexpr int TPB = EVAL_THREADS / TPT;  // targets per CTA
     constexpr bool COMP = sizeof(T) == 4;    // compensated accumulation in FP32
-    __shared__ T sx[EVAL_THREADS], sy[EVAL_THREADS], sz[EVAL_THREADS];
-    __shared__ T snx[EVAL_THREADS], sny[EVAL_THREADS], snz[EVAL_THREADS];
-    __shared__ T sv[NR * R][EVAL_THREADS];
+    // per source: position, normal, and the R density components of every
+    // right-hand side, each a 4-vector (one shared load in the pair loop)
+    __shared__ Vec4<T> sp[EVAL_THREADS], sn[EVAL_THREADS];
+    __shared__ Vec4<T> sv[NR][EVAL_THREADS];
 
     const int task = a.item_task[blockIdx.x];
     const int t0 = a.item_start[blockIdx.x];
@@ -140,44 +149,49 @@ eval_kernel(const EvalArgs<T> a)
                 nx = T(ux); ny = T(uy); nz = T(uz);
                 const int cn = R * a.ns;
 #pragma unroll
-                for (int r_ = 0; r_ < NR; r_++)
+                for (int r_ = 0; r_ < NR; r_++) {
+                    T vv[3] = {T(0), T(0), T(0)};
 #pragma unroll
                     for (int d = 0; d < R; d++)
-                        sv[r_ * R + d][threadIdx.x] =
-                            r_ < nr_here ? a.q[(sb * a.nrhs + a.rhs0 + r_) * cn + d * a.ns + li] : T(0);
+                        vv[d] = r_ < nr_here ? a.q[(sb * a.nrhs + a.rhs0 + r_) * cn + d * a.ns + li] : T(0);
+                    sv[r_][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                }
             } else {
                 const long p = sb + li;
                 qx = a.s_xyz[3 * p]; qy = a.s_xyz[3 * p + 1]; qz = a.s_xyz[3 * p + 2];
                 nx = a.s_nrm[3 * p]; ny = a.s_nrm[3 * p + 1]; nz = a.s_nrm[3 * p + 2];
 #pragma unroll
-                for (int r_ = 0; r_ < NR; r_++)
+                for (int r_ = 0; r_ < NR; r_++) {
+                    T vv[3] = {T(0), T(0), T(0)};
 #pragma unroll
                     for (int d = 0; d < R; d++)
-                        sv[r_ * R + d][threadIdx.x] =
-                            r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
+                        vv[d] = r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
+                    sv[r_][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                }
             }
-            sx[threadIdx.x] = T(qx - ox); sy[threadIdx.x] = T(qy - oy); sz[threadIdx.x] = T(qz - oz);
-            snx[threadIdx.x] = nx; sny[threadIdx.x] = ny; snz[threadIdx.x] = nz;
+            sp[threadIdx.x] = Vec4<T>{T(qx - ox), T(qy - oy), T(qz - oz), T(0)};
+            sn[threadIdx.x] = Vec4<T>{nx, ny, nz, T(0)};
         }
         __syncthreads();
         if (active) {
             const int n_here = min(EVAL_THREADS, total - tile);
             for (int j = lane; j < n_here; j += TPT) {
-                const T dx = sx[j] - px, dy = sy[j] - py, dz = sz[j] - pz;
-                T v[R];
+                const Vec4<T> q = sp[j];
+                const T dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                const Vec4<T> nq = sn[j];
 #pragma unroll
                 for (int r_ = 0; r_ < NR; r_++) {
-#pragma unroll
-                    for (int d = 0; d < R; d++) v[d] = sv[r_ * R + d][j];
+                    const Vec4<T> vq = sv[r_][j];
+                    const T v[3] = {vq.x, vq.y, vq.z};
                     // transposed apply: the target is the forward source and
                     // the source the forward observer, so the separation
                     // (forward src - forward obs) flips sign and the normals swap
                     if (TRANS)
-                        accumulate<KID, true, T>(-dx, -dy, -dz, snx[j], sny[j], snz[j], pnx,
-                                                 pny, pnz, a.c2, v, &part[r_ * R]);
+                        accumulate<KID, true, T>(-dx, -dy, -dz, nq.x, nq.y, nq.z, pnx, pny, pnz,
+                                                 a.c2, v, &part[r_ * R]);
                     else
-                        accumulate<KID, false, T>(dx, dy, dz, pnx, pny, pnz, snx[j], sny[j],
-                                                  snz[j], a.c2, v, &part[r_ * R]);
+                        accumulate<KID, false, T>(dx, dy, dz, pnx, pny, pnz, nq.x, nq.y, nq.z,
+                                                  a.c2, v, &part[r_ * R]);
                 }
             }
             if (COMP) {
