@@ -452,6 +452,9 @@ Plan::~Plan()
     if (h_err) cudaFreeHost(h_err);
     if (cublas) cublasDestroy(cublas);
     if (solver) cusolverDnDestroy(solver);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -521,6 +524,9 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     if (!opt.host_only) {
         TBEM_CK(cudaSetDevice(opt.device));
         TBEM_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        TBEM_CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        TBEM_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        TBEM_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
         TBEM_CKB(cublasCreate(&cublas));
         TBEM_CKB(cublasSetStream(cublas, stream));
         TBEM_CKS(cusolverDnCreate(&solver));
@@ -1957,6 +1963,11 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
     TBEM_CK(cudaMemsetAsync(cdc32.p, 0, sizeof(float) * nco * nrhs * ro, s));
     mark("gather", s);
+    // the near field on the side stream, beside the far-field passes below
+    TBEM_CK(cudaEventRecord(ev_fork, s));
+    TBEM_CK(cudaStreamWaitEvent(side, ev_fork, 0));
+    eval<float>(p2p_set(), kid, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, side, false);
+    TBEM_CK(cudaEventRecord(ev_join, side));
     // P2M into the leaves' check potentials, then u~ = P_l u
     eval<float>(p2m_set(), F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
     F.comp_p2m.run_rect<float>(cu32.p, cuc32.p, ri, n, n, nrhs, 0, GEMM_ATOMIC, s, &launches);  // into zeros
@@ -1964,16 +1975,6 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     for (int l = S.n_levels() - 1; l >= 0; l--)
         if (l < (int)F.m2m_c.size()) F.m2m_c[l].run_rect<float>(cuc32.p, cuc32.p, ri, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("m2m", s);
-    eval<float>(p2p_set(), kid, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, s, false);
-    mark("p2p", s);
-    if (!L.m2p.empty()) {
-        // equivalent densities 2^-l W u~ of the M2P sources, evaluated in FP64
-        F.decomp_m2p.run_rect<float>(cuc32.p, cu32.p, n, ri, ri, nrhs, 0, GEMM_STORE, s, &launches);
-        promote_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu32.p, qu64.p, ncs * nrhs * n);
-        TBEM_CK(cudaGetLastError());
-        launches++;
-        eval<double>(m2p, F.kt_kid, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
-    }
     if (!L.p2l.empty()) {
         TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
         eval<float>(p2l, F.ks_kid, true, false, O, dobs, F.r_dc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cd32.p, 1, nrhs, s, false);
@@ -1992,6 +1993,17 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     for (int l = 1; l < O.n_levels(); l++)
         if (l - 1 < (int)F.l2l_c.size()) F.l2l_c[l - 1].run_rect<float>(cdc32.p, cdc32.p, ro, ro, ro, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("l2l", s);
+    // join the near field: the passes below add into the same outputs
+    TBEM_CK(cudaStreamWaitEvent(s, ev_join, 0));
+    mark("p2p_wait", s);
+    if (!L.m2p.empty()) {
+        // equivalent densities 2^-l W u~ of the M2P sources, evaluated in FP64
+        F.decomp_m2p.run_rect<float>(cuc32.p, cu32.p, n, ri, ri, nrhs, 0, GEMM_STORE, s, &launches);
+        promote_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu32.p, qu64.p, ncs * nrhs * n);
+        TBEM_CK(cudaGetLastError());
+        launches++;
+        eval<double>(m2p, F.kt_kid, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+    }
     if (F.n_l2p > 0) {
         l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cdc32.p, ro, F.E_ld, R, nrhs, y64.p, NO);
         TBEM_CK(cudaGetLastError());

@@ -286,6 +286,11 @@ struct Plan {
     DBuf<float> cu32, cd32;
     DBuf<float> cuc32, cdc32;  // compressed M2L coefficients [cell][rhs][r_in | r_out]
     cudaStream_t stream = nullptr;
+    // second stream for the near field, which runs beside the far-field
+    // passes of the compressed form (forked after the gather, joined before
+    // the passes that add into the outputs)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t solver = nullptr;
     // tensor-core timeout flags copied to pinned memory after every apply;
