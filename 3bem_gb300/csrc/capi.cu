@@ -7,9 +7,7 @@
 
 #include "plan.h"
 
-struct TbemFmm {
-    tbem::Plan plan;
-};
+#include "handle.h"
 
 namespace {
 thread_local std::string g_last_error;
@@ -226,6 +224,29 @@ int tbem_fmm_m2l_ranks(const TbemFmm* h, long* r_in, long* r_out)
     if (r_out) *r_out = c ? h->plan.f.r_out : 0;
     return TBEM_OK;
 }
+
+int tbem_fmm_graph_create(TbemFmm* const* ops, int n_ops, const double* const* x, double* const* y,
+                          int n_rhs, int adjoint, TbemGraph** out)
+{
+    if (!out) return fail(TBEM_ERR_ARG, "null output handle");
+    *out = nullptr;
+    TbemGraph* g = tbem::graph_new();
+    int rc = guarded([&] { tbem::graph_build(*g, ops, n_ops, x, y, n_rhs, adjoint != 0); });
+    if (rc != TBEM_OK) {
+        tbem::graph_delete(g);
+        return rc;
+    }
+    *out = g;
+    return TBEM_OK;
+}
+
+int tbem_fmm_graph_launch(TbemGraph* g, void* stream)
+{
+    if (!g) return fail(TBEM_ERR_ARG, "null graph");
+    return guarded([&] { tbem::graph_launch(*g, (cudaStream_t)stream); });
+}
+
+void tbem_fmm_graph_destroy(TbemGraph* g) { tbem::graph_delete(g); }
 
 long tbem_fmm_last_launches(const TbemFmm* h) { return h ? h->plan.launches : TBEM_ERR_ARG; }
 

@@ -307,6 +307,37 @@ class FMMOperator(OperatorI):
         return [(names[i].decode(), float(ms[i])) for i in range(min(k, cap))]
 
 
+class FMMGraph:
+    """One CUDA graph replaying the applies of several operators (e.g. one per
+    mesh of a batch) between fixed float64 CUDA tensors (tbem_fmm_graph_*).
+
+    ops: FMMOperators; xs / ys: CUDA tensors, [n_cols] / [n_rows] (or
+    [n_rhs, n] with n_rhs given).  Building runs each apply once (writing ys).
+    launch() replays all of them with one graph launch (asynchronous; the
+    results are in ys after a device synchronization)."""
+
+    def __init__(self, ops, xs, ys, n_rhs=1, adjoint=False):
+        self.ops, self.xs, self.ys = list(ops), list(xs), list(ys)  # keep alive
+        n = len(self.ops)
+        handles = (C.c_void_p * n)(*[op._h.value if hasattr(op._h, "value") else op._h
+                                     for op in self.ops])
+        xp = (C.c_void_p * n)(*[t.data_ptr() for t in self.xs])
+        yp = (C.c_void_p * n)(*[t.data_ptr() for t in self.ys])
+        h = C.c_void_p()
+        check(_L.lib().tbem_fmm_graph_create(handles, n, xp, yp, int(n_rhs), int(bool(adjoint)),
+                                             C.byref(h)))
+        self._h = h
+
+    def launch(self, stream=None):
+        check(_L.lib().tbem_fmm_graph_launch(self._h, stream))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _L._lib is not None:
+            _L._lib.tbem_fmm_graph_destroy(h)
+            self._h = None
+
+
 class DirectOperator(OperatorI):
     """FP64 direct N-body operator on the GPU (make_direct_nbody_operator,
     cpp/nbody_operator.h:143-152, applied matrix-free like nbody_eval)."""

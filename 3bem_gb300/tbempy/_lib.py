@@ -58,6 +58,9 @@ SIGNATURES = {
     "tbem_fmm_p2p_block": (_L, [_P]),
     "tbem_fmm_tc_tile": (_L, [_P]),
     "tbem_fmm_m2l_ranks": (_I, [_P, _P, _P]),
+    "tbem_fmm_graph_create": (_I, [_P, _I, _P, _P, _I, _I, _P]),
+    "tbem_fmm_graph_launch": (_I, [_P, _P]),
+    "tbem_fmm_graph_destroy": (None, [_P]),
     "tbem_direct_apply": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _I, _P]),
     "tbem_direct_gradients": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P]),

@@ -162,6 +162,25 @@ long tbem_fmm_tc_tile(const TbemFmm* h);
  * the M2L is not compressed.  Returns 0 or a TBEM_ERR_* code. */
 int tbem_fmm_m2l_ranks(const TbemFmm* h, long* r_in, long* r_out);
 
+/* CUDA-graph capture (the batching form's single launch; no reference
+ * counterpart: the reference applies one operator per call).  Captures the
+ * applies (or, with adjoint != 0, the transposed applies) of n_ops operators
+ * -- e.g. one per mesh of a batch -- from x[i] into y[i], n_rhs right-hand
+ * sides each, spread over up to eight parallel branches.  x and y must be
+ * device memory: the graph replays these addresses.  Each operator first
+ * runs one ordinary apply (writing y[i]) that sizes its buffers; nothing is
+ * allocated while capturing.  An operator's buffers are shared by its
+ * applies and its graphs: do not run them concurrently.  Phase timing must be
+ * off. */
+typedef struct TbemGraph TbemGraph;
+int tbem_fmm_graph_create(TbemFmm* const* ops, int n_ops, const double* const* x,
+                          double* const* y, int n_rhs, int adjoint, TbemGraph** out);
+/* Replays every captured apply with one graph launch on stream (NULL: the
+ * graph's own stream); asynchronous.  Returns TBEM_ERR_TIMEOUT when a
+ * tensor-core pass of an earlier replay gave up waiting. */
+int tbem_fmm_graph_launch(TbemGraph* g, void* stream);
+void tbem_fmm_graph_destroy(TbemGraph* g);
+
 /* Number of kernel launches the last apply made on the device (no
  * reference counterpart; used to report the launch count of a timed run). */
 long tbem_fmm_last_launches(const TbemFmm* h);
