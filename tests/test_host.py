@@ -121,3 +121,28 @@ def test_csr_create_validates():
         ThreeD.SparseOperator(2, 2, [1.0], [5], [0, 1, 1])   # column out of range
     with pytest.raises(TbemError):
         ThreeD.SparseOperator(2, 2, [1.0, 2.0], [0, 1], [0, 2, 1])  # decreasing row_ptrs
+
+
+def test_graph_arguments_rejected_before_device_use():
+    """tbem_fmm_graph_create validates its arguments before any device call:
+    no operators, a null operator, a host_only operator or n_rhs <= 0 come
+    back as status codes with a message."""
+    import ctypes as C
+    from tbempy import ThreeD, _lib
+    L = _lib.lib()
+    h = C.c_void_p()
+    assert L.tbem_fmm_graph_create(None, 0, None, None, 1, 0, C.byref(h)) == -1
+    assert h.value is None and b"no operators" in L.tbem_last_error()
+    rng = np.random.default_rng(0)
+    locs = rng.uniform(0, 1, (100, 3))
+    nrm = np.tile([0.0, 0.0, 1.0], (100, 1))
+    op = ThreeD.FMMOperator(ThreeD.LaplaceSingle(), locs, nrm, locs, nrm, np.ones(100),
+                            ThreeD.FMMConfig(0.3, 20, 20, 0.05, False), host_only=True)
+    ops = (C.c_void_p * 1)(op._h.value)
+    ptrs = (C.c_void_p * 1)(0)
+    assert L.tbem_fmm_graph_create(ops, 1, ptrs, ptrs, 0, 0, C.byref(h)) == -1  # n_rhs
+    nulls = (C.c_void_p * 1)(None)
+    assert L.tbem_fmm_graph_create(nulls, 1, ptrs, ptrs, 1, 0, C.byref(h)) == -1
+    assert L.tbem_fmm_graph_create(ops, 1, ptrs, ptrs, 1, 0, C.byref(h)) == -4  # host_only
+    assert b"host_only" in L.tbem_last_error()
+    assert L.tbem_fmm_graph_launch(None, None) == -1
