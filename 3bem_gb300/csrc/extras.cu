@@ -4,7 +4,7 @@
 #include <string>
 #include <vector>
 
-#include "plan.h"
+#include "handle.h"
 
 namespace {
 
@@ -38,8 +38,9 @@ __global__ void weight_kernel(const double* x, const double* w, double* s, long 
         s[t] = w[t % N] * x[t];
 }
 
+// y = A x (add = 0) or y += A x (add = 1); one warp per row.
 __global__ void csr_kernel(const long* rowptr, const long* col, const double* val, const double* x,
-                           double* y, long n_rows, long n_cols, int nrhs)
+                           double* y, long n_rows, long n_cols, int nrhs, int add = 0)
 {
     const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x % 32;
@@ -51,7 +52,10 @@ __global__ void csr_kernel(const long* rowptr, const long* col, const double* va
         for (long k = b + lane; k < e; k += 32) acc += val[k] * xr[col[k]];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) y[(long)r * n_rows + warp] = acc;
+        if (lane == 0) {
+            double* d = y + (long)r * n_rows + warp;
+            *d = add ? *d + acc : acc;
+        }
     }
 }
 }  // namespace
@@ -201,5 +205,105 @@ int tbem_csr_apply(TbemCsr* h, const double* x, double* y, int n_rhs, void* stre
 long tbem_csr_nnz(const TbemCsr* h) { return h ? h->nnz : TBEM_ERR_ARG; }
 
 void tbem_csr_destroy(TbemCsr* h) { delete h; }
+
+
+// ---- IntegralOperator: y = G (F (I x)) + N x + C x on the device -------------
+
+}  // extern "C"
+
+struct TbemIntegral {
+    TbemCsr *near = nullptr, *corr = nullptr, *galerkin = nullptr, *interp = nullptr;
+    TbemFmm* far = nullptr;
+    long n_rows = 0, n_cols = 0;
+    tbem::DBuf<double> xi, xf, yf, yo;  // I x, F (I x), staged output
+};
+
+namespace {
+void csr_into(const TbemCsr* A, const double* x, double* y, int nrhs, int add, cudaStream_t s)
+{
+    if (A->n_rows == 0) return;
+    if (A->nnz == 0) {
+        if (!add) TBEM_CK(cudaMemsetAsync(y, 0, sizeof(double) * A->n_rows * nrhs, s));
+        return;
+    }
+    const long threads = A->n_rows * 32;
+    csr_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(A->rowptr.p, A->col.p, A->val.p, x, y,
+                                                                 A->n_rows, A->n_cols, nrhs, add);
+    TBEM_CK(cudaGetLastError());
+}
+}  // namespace
+
+extern "C" {
+
+int tbem_integral_create(TbemCsr* nearfield, TbemCsr* correction, TbemCsr* galerkin,
+                         TbemFmm* farfield, TbemCsr* interp, TbemIntegral** out)
+{
+    if (!out) return TBEM_ERR_ARG;
+    *out = nullptr;
+    if (!nearfield || !correction || !galerkin || !farfield || !interp) {
+        tbem::set_last_error("null operator");
+        return TBEM_ERR_ARG;
+    }
+    const long fr = tbem_fmm_n_rows(farfield), fc = tbem_fmm_n_cols(farfield);
+    const long n = nearfield->n_rows, m = nearfield->n_cols;
+    if (correction->n_rows != n || correction->n_cols != m || galerkin->n_rows != n ||
+        galerkin->n_cols != fr || interp->n_rows != fc || interp->n_cols != m) {
+        tbem::set_last_error("operator shapes do not chain: G (n x F rows), F, I (F cols x m), N and C (n x m)");
+        return TBEM_ERR_ARG;
+    }
+    TbemIntegral* h = new TbemIntegral();
+    h->near = nearfield;
+    h->corr = correction;
+    h->galerkin = galerkin;
+    h->far = farfield;
+    h->interp = interp;
+    h->n_rows = n;
+    h->n_cols = m;
+    *out = h;
+    return TBEM_OK;
+}
+
+int tbem_integral_apply(TbemIntegral* h, const double* x, double* y, int n_rhs, void* stream)
+{
+    using namespace tbem;
+    if (!h || !y || n_rhs <= 0 || (!x && h->n_cols > 0)) {
+        set_last_error("null argument or n_rhs <= 0");
+        return TBEM_ERR_ARG;
+    }
+    try {
+        // one stream for the whole chain: the caller's, else the farfield's own
+        // (the FMM apply would otherwise run on that one, unordered with the
+        // sparse steps)
+        cudaStream_t s = stream ? (cudaStream_t)stream : h->far->plan.stream;
+        if (h->n_rows == 0) return TBEM_OK;
+        const size_t ny = (size_t)h->n_rows * n_rhs;
+        const bool y_dev = is_device(y);
+        double* yd = y;
+        if (!y_dev) {
+            h->yo.ensure(ny);
+            yd = h->yo.p;
+        }
+        Staged xs;
+        stage(xs, x, (size_t)h->n_cols * n_rhs, s);
+        const long fr = tbem_fmm_n_rows(h->far), fc = tbem_fmm_n_cols(h->far);
+        h->xi.ensure(std::max<size_t>((size_t)fc * n_rhs, 1));
+        h->xf.ensure(std::max<size_t>((size_t)fr * n_rhs, 1));
+        csr_into(h->interp, xs.p, h->xi.p, n_rhs, 0, s);               // I x
+        h->far->plan.apply(h->xi.p, h->xf.p, n_rhs, s, false);        // F (I x)
+        csr_into(h->galerkin, h->xf.p, yd, n_rhs, 0, s);               // G F I x
+        csr_into(h->near, xs.p, yd, n_rhs, 1, s);                      // + N x
+        csr_into(h->corr, xs.p, yd, n_rhs, 1, s);                      // + C x
+        if (!y_dev) TBEM_CK(cudaMemcpyAsync(y, yd, ny * sizeof(double), cudaMemcpyDeviceToHost, s));
+        TBEM_CK(cudaStreamSynchronize(s));
+        return TBEM_OK;
+    } catch (const tbem::Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    }
+}
+
+long tbem_integral_n_rows(const TbemIntegral* h) { return h ? h->n_rows : TBEM_ERR_ARG; }
+long tbem_integral_n_cols(const TbemIntegral* h) { return h ? h->n_cols : TBEM_ERR_ARG; }
+void tbem_integral_destroy(TbemIntegral* h) { delete h; }
 
 }  // extern "C"

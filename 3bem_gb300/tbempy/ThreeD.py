@@ -477,7 +477,10 @@ class SparseOperator(OperatorI):
 class IntegralOperator(OperatorI):
     """A = G (F I) + N + C (cpp/integral_operator.h:13-63): galerkin,
     farfield (e.g. an FMMOperator), interpolation, nearfield and the
-    farfield correction, all applied on the GPU."""
+    farfield correction, all applied on the GPU.  With sparse operators and
+    an FMMOperator farfield the chain runs on the device in one call
+    (tbem_integral_apply); any other farfield (e.g. a DirectOperator) is
+    composed step by step."""
 
     def __init__(self, nearfield, farfield_correction, galerkin, farfield, interp):
         self.nearfield = nearfield
@@ -485,6 +488,19 @@ class IntegralOperator(OperatorI):
         self.galerkin = galerkin
         self.farfield = farfield
         self.interp = interp
+        self._h = None
+        if isinstance(farfield, FMMOperator) and all(
+                isinstance(o, SparseOperator) for o in (nearfield, farfield_correction, galerkin, interp)):
+            h = C.c_void_p()
+            check(_L.lib().tbem_integral_create(nearfield._h, farfield_correction._h, galerkin._h,
+                                                farfield._h, interp._h, C.byref(h)))
+            self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _L._lib is not None:
+            _L._lib.tbem_integral_destroy(h)
+            self._h = None
 
     def n_rows(self):
         return self.galerkin.n_rows()
@@ -493,6 +509,11 @@ class IntegralOperator(OperatorI):
         return self.nearfield.n_cols()
 
     def apply(self, x):
+        if self._h is not None:
+            xx, n_rhs, is_t, squeeze = _prep_in(x, self.n_cols())
+            y = _alloc_out(xx, is_t, n_rhs, self.n_rows())
+            check(_L.lib().tbem_integral_apply(self._h, _ptr(xx), _ptr(y), int(n_rhs), _stream_of(xx)))
+            return y.reshape(-1) if squeeze else y
         far = self.galerkin.apply(self.farfield.apply(self.interp.apply(x)))
         return self.nearfield.apply(x) + far + self.farfield_correction.apply(x)
 

@@ -69,6 +69,11 @@ SIGNATURES = {
     "tbem_csr_apply": (_I, [_P, _P, _P, _I, _P]),
     "tbem_csr_nnz": (_L, [_P]),
     "tbem_csr_destroy": (None, [_P]),
+    "tbem_integral_create": (_I, [_P, _P, _P, _P, _P, _P]),
+    "tbem_integral_apply": (_I, [_P, _P, _P, _I, _P]),
+    "tbem_integral_n_rows": (_L, [_P]),
+    "tbem_integral_n_cols": (_L, [_P]),
+    "tbem_integral_destroy": (None, [_P]),
     "tbem_last_error": (C.c_char_p, []),
 }
 

@@ -235,6 +235,21 @@ int tbem_csr_apply(TbemCsr* h, const double* x, double* y, int n_rhs, void* stre
 long tbem_csr_nnz(const TbemCsr* h);
 void tbem_csr_destroy(TbemCsr* h);
 
+/* Replaces IntegralOperator::apply (cpp/integral_operator.h:55-63):
+ * y = G (F (I x)) + N x + C x with the galerkin G, the farfield F (an FMM
+ * operator), the interpolation I, the nearfield N and the farfield
+ * correction C, chained on the device in one call (no host round trip between
+ * the steps).  The operators are borrowed and must outlive the handle; the
+ * shapes must chain (G: n x F.n_rows, I: F.n_cols x m, N and C: n x m), else
+ * TBEM_ERR_ARG.  x: m * n_rhs, y: n * n_rhs values, host or device. */
+typedef struct TbemIntegral TbemIntegral;
+int tbem_integral_create(TbemCsr* nearfield, TbemCsr* correction, TbemCsr* galerkin,
+                         TbemFmm* farfield, TbemCsr* interp, TbemIntegral** out);
+int tbem_integral_apply(TbemIntegral* h, const double* x, double* y, int n_rhs, void* stream);
+long tbem_integral_n_rows(const TbemIntegral* h);
+long tbem_integral_n_cols(const TbemIntegral* h);
+void tbem_integral_destroy(TbemIntegral* h);
+
 /* Last error message of the calling thread ("" if none). */
 const char* tbem_last_error(void);
 

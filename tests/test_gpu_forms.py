@@ -116,10 +116,23 @@ def test_integral_operator_composition():
     near, N = rand_csr(n_dof, n_dof, 800)
     corr, Cm = rand_csr(n_dof, n_dof, 800)
     op = ThreeD.IntegralOperator(near, corr, galerkin, far, interp)
+    assert op._h is not None  # the device-side chain (tbem_integral_apply)
     x = rng.normal(size=n_dof)
     expect = G @ far.apply(I @ x) + N @ x + Cm @ x
     assert np.linalg.norm(op.apply(x) - expect) <= 1e-12 * np.linalg.norm(expect)
     assert op.n_rows() == n_dof and op.n_cols() == n_dof
+    # several right-hand sides, device tensors in and out.  A batched apply
+    # sums in another order than single ones, and the plain form's
+    # pseudo-inverse (condition ~1e9) lifts that rounding to ~1e-12: 1e-10
+    torch = pytest.importorskip("torch")
+    X = rng.normal(size=(3, n_dof))
+    Y = op.apply(torch.tensor(X, device="cuda")).cpu().numpy()
+    for r in range(3):
+        e = G @ far.apply(I @ X[r]) + N @ X[r] + Cm @ X[r]
+        assert np.linalg.norm(Y[r] - e) <= 1e-10 * np.linalg.norm(e)
+    # shapes that do not chain are refused
+    with pytest.raises(Exception):
+        ThreeD.IntegralOperator(near, corr, galerkin, far, rand_csr(499, n_dof, 100)[0])
 
 
 @pytest.mark.parametrize("name", ["ElasticDisplacement", "ElasticTraction", "LaplaceDouble"])
