@@ -67,7 +67,7 @@ void graph_build(TbemGraph& g, TbemFmm* const* ops, int n_ops, const double* con
             throw Error(TBEM_ERR_ARG, "a graph replays fixed addresses: inputs and outputs must be device memory");
     }
     g.device = dev;
-    TBEM_CK(cudaSetDevice(dev));
+    DeviceGuard guard(dev);
     TBEM_CK(cudaStreamCreateWithFlags(&g.cap, cudaStreamNonBlocking));
     const int nb = std::min(n_ops, 8);
     g.branch.resize(nb);
@@ -110,7 +110,7 @@ void graph_launch(TbemGraph& g, cudaStream_t s)
         const int* e = op->plan.h_err;
         if (e && (e[0] || e[1])) throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
     }
-    TBEM_CK(cudaSetDevice(g.device));
+    DeviceGuard guard(g.device);
     TBEM_CK(cudaGraphLaunch(g.exec, s ? s : g.cap));
 }
 

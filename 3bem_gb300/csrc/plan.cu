@@ -175,12 +175,9 @@ void GemmSet::run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int tr
     const std::vector<int>& st = wave_tile_start[nrhs];
     const int nw = (int)st.size() - 1;
     if (!waves && nw != 1) throw Error(TBEM_ERR_STATE, "a wave-ordered GEMM set run without waves");
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        TBEM_CK(cudaGetDevice(&dev));
-        TBEM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    }
+    int dev = 0, sms = 0;
+    TBEM_CK(cudaGetDevice(&dev));
+    TBEM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     for (int w = 0; w < nw; w++) {
         const int nt = st[w + 1] - st[w];
         if (nt == 0) continue;
@@ -447,6 +444,11 @@ inline double hypot_ref(const double* v)
 
 Plan::~Plan()
 {
+    // the library handles are released on the device they were made on
+    int prev = -1;
+    const bool own = !opt.host_only && cudaGetDevice(&prev) == cudaSuccess && prev != opt.device &&
+                     cudaSetDevice(opt.device) == cudaSuccess;
+    cudaGetLastError();
     for (auto& m : marks) cudaEventDestroy(m.second);
     for (auto e : event_pool) cudaEventDestroy(e);
     if (h_err) cudaFreeHost(h_err);
@@ -456,6 +458,7 @@ Plan::~Plan()
     if (ev_join) cudaEventDestroy(ev_join);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
+    if (own) cudaSetDevice(prev);
 }
 
 void Plan::upload_tree(const Tree& t, const double* locs, const double* normals,
@@ -521,8 +524,9 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     h_src_normals.assign(src_normals, src_normals + 3 * n_src);
     h_src_weights.assign(src_weights, src_weights + n_src);
 
+    std::unique_ptr<DeviceGuard> guard;
     if (!opt.host_only) {
-        TBEM_CK(cudaSetDevice(opt.device));
+        guard.reset(new DeviceGuard(opt.device));
         TBEM_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         TBEM_CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
         TBEM_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
@@ -1609,6 +1613,7 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
 void Plan::set_c2e(int which, long level, const double* op)
 {
     if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
+    DeviceGuard guard(opt.device);
     if (f.mixed) throw Error(TBEM_ERR_STATE, "set_c2e is only valid for the FP64 form");
     const auto& offs = which == 0 ? f.c2e_up_off : f.c2e_dn_off;
     if (level < 0 || level >= (long)offs.size()) throw Error(TBEM_ERR_ARG, "level out of range");
@@ -1621,6 +1626,7 @@ void Plan::set_c2e(int which, long level, const double* op)
 void Plan::get_c2e(int which, long level, double* out) const
 {
     if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
+    DeviceGuard guard(opt.device);
     const auto& offs = which == 0 ? f.c2e_up_off : f.c2e_dn_off;
     if (level < 0 || level >= (long)offs.size()) throw Error(TBEM_ERR_ARG, "level out of range");
     TBEM_CK(cudaStreamSynchronize(stream));
@@ -1678,6 +1684,7 @@ void Plan::mark(const char* name, cudaStream_t s)
 void Plan::read_phases()
 {
     if (marks.empty()) return;
+    DeviceGuard guard(opt.device);
     TBEM_CK(cudaEventSynchronize(marks.back().second));
     std::vector<std::pair<std::string, double>> sum;
     int applies = 0;
@@ -2061,6 +2068,7 @@ void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
 {
     if (nrhs <= 0) throw Error(TBEM_ERR_ARG, "n_rhs must be > 0");
     if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
+    DeviceGuard guard(opt.device);
     if (!s) s = stream;
     const long n_in = adj ? (long)R * n_obs : (long)R * n_src;
     const long n_out = adj ? (long)R * n_src : (long)R * n_obs;

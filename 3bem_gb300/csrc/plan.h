@@ -35,6 +35,30 @@ void check_cusolver(cusolverStatus_t e, const char* what, const char* file, int 
 #define TBEM_CKB(x) ::tbem::check_cublas((x), #x, __FILE__, __LINE__)
 #define TBEM_CKS(x) ::tbem::check_cusolver((x), #x, __FILE__, __LINE__)
 
+// Makes dev current for a scope and gives the caller's device back after it,
+// so that operators on different GPUs can be used from one thread.
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            cudaGetLastError();
+            prev = -1;
+        }
+        if (prev != dev) {
+            check_cuda(cudaSetDevice(dev), "cudaSetDevice", __FILE__, __LINE__);
+            changed = true;
+        }
+    }
+    ~DeviceGuard()
+    {
+        if (changed && prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
 // Owning device buffer.
 template <typename T>
 struct DBuf {
