@@ -335,3 +335,41 @@ def test_phase_timing_means_over_applies():
     op.set_timing(False)
     op.apply(x)
     assert dict(op.phase_times()) == ph
+
+
+@pytest.mark.parametrize("name", KERNELS)
+def test_default_precision_form_transpose(name):
+    """The default precision form (compressed far field, tensor-core M2L) and
+    its transposed apply: <A x, z> = <x, A^T z> for every kernel."""
+    from tbempy import ThreeD, meshes
+    locs, nrm, w = meshes.sphere_points(3)
+    order = 152 if name.startswith("Laplace") else 296
+    op = ThreeD.FMMOperator(kernel_obj(name), locs, nrm, locs, nrm, w,
+                            ThreeD.FMMConfig(0.3, order, 40, 0.05, False), precision="mixed")
+    rng = np.random.default_rng(60)
+    X = rng.uniform(-1, 1, (2, op.n_cols()))
+    Z = rng.uniform(-1, 1, (2, op.n_rows()))
+    AX, AtZ = op.apply(X), op.apply_adjoint(Z)
+    for r in range(2):
+        lhs, rhs = AX[r] @ Z[r], X[r] @ AtZ[r]
+        assert abs(lhs - rhs) <= 1e-6 * np.linalg.norm(AX[r]) * np.linalg.norm(Z[r])
+
+
+@pytest.mark.parametrize("name", ["LaplaceDouble", "ElasticTraction"])
+def test_precision_form_distinct_point_sets(name):
+    """Observation points apart from the sources (a free surface above the
+    fault): the precision form's M2L between different trees runs in FP64
+    on the fly; against the FP64 direct sum."""
+    from tbempy import ThreeD, meshes
+    locs, nrm, w, uv = meshes.fault_points(16)
+    rng = np.random.default_rng(61)
+    obs = np.column_stack([rng.uniform(-2, 2, 3000), rng.uniform(-2, 2, 3000), np.zeros(3000)])
+    on = np.tile([0.0, 0.0, 1.0], (3000, 1))
+    K = kernel_obj(name)
+    order = 152 if name.startswith("Laplace") else 296
+    op = ThreeD.FMMOperator(K, obs, on, locs, nrm, w, ThreeD.FMMConfig(0.3, order, 40, 0.05, False),
+                            precision="mixed")
+    assert op.m2l_ranks() == (0, 0)  # no compression between different trees
+    x = rng.uniform(-1, 1, op.n_cols())
+    exact = ThreeD.DirectOperator(K, obs, on, locs, nrm, w).apply(x)
+    assert rel(op.apply(x), exact) < 2e-6
