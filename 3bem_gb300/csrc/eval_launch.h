@@ -23,6 +23,7 @@ cudaError_t launch_eval_k2(const EvalLaunch&, const void* args, bool fp32, cudaS
 cudaError_t launch_eval_k3(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
 cudaError_t launch_eval_k4(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
 cudaError_t launch_eval_k5(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k6(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
 
 // rhs chunk per launch (the kernel keeps NR x R accumulators per thread)
 constexpr int EVAL_NR = 4;
@@ -37,7 +38,8 @@ inline cudaError_t launch_eval(const EvalLaunch& L, const EvalArgs<T>& a, cudaSt
     case 2: return launch_eval_k2(L, &a, fp32, s);
     case 3: return launch_eval_k3(L, &a, fp32, s);
     case 4: return launch_eval_k4(L, &a, fp32, s);
-    default: return launch_eval_k5(L, &a, fp32, s);
+    case 5: return launch_eval_k5(L, &a, fp32, s);
+    default: return launch_eval_k6(L, &a, fp32, s);
     }
 }
 

@@ -75,7 +75,7 @@ int tbem_direct_apply(int kernel, const double* kernel_params, const double* obs
 {
     using namespace tbem;
     try {
-        if (kernel < 0 || kernel > 5 || n_obs < 0 || n_src < 0 || n_rhs <= 0 || !y)
+        if (kernel < 0 || kernel > 6 || n_obs < 0 || n_src < 0 || n_rhs <= 0 || !y)
             throw Error(TBEM_ERR_ARG, "bad argument");
         const int R = kernel_dim(kernel);
         const double mu = (kernel_params && R == 3) ? kernel_params[0] : 1.0;

@@ -93,7 +93,7 @@ __global__ void grad_src_kernel(int kid, KParams p, const double* ox, const doub
     const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n_src) return;
     const int R = kernel_dim(kid);
-    const bool use_ns = kid == LAP_D || kid == EL_TRAC;
+    const bool use_ns = kid == LAP_D || kid == EL_TRAC || kid == EL_HYP;
     double xv[3] = {0, 0, 0};
     for (int b = 0; b < R; b++) xv[b] = x[b * n_src + j];
     const double y[3] = {sx[3 * j], sx[3 * j + 1], sx[3 * j + 2]};
@@ -135,7 +135,7 @@ __global__ void grad_obs_kernel(int kid, KParams p, const double* ox, const doub
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_obs) return;
     const int R = kernel_dim(kid);
-    const bool use_no = kid == EL_ADJ;
+    const bool use_no = kid == EL_ADJ || kid == EL_HYP;
     double rv[3] = {0, 0, 0};
     for (int a = 0; a < R; a++) rv[a] = r[a * n_obs + i];
     const double o[3] = {ox[3 * i], ox[3 * i + 1], ox[3 * i + 2]};
@@ -215,7 +215,7 @@ extern "C" int tbem_direct_gradients(int kernel, const double* kernel_params,
 {
     using namespace tbem;
     try {
-        if (kernel < 0 || kernel > 5 || n_obs < 0 || n_src < 0) throw Error(TBEM_ERR_ARG, "bad argument");
+        if (kernel < 0 || kernel > 6 || n_obs < 0 || n_src < 0) throw Error(TBEM_ERR_ARG, "bad argument");
         const int R = kernel_dim(kernel);
         const double mu = (kernel_params && R == 3) ? kernel_params[0] : 1.0;
         const double nu = (kernel_params && R == 3) ? kernel_params[1] : 0.25;

@@ -4,8 +4,8 @@
 // delta = y - x and the reference's self-pair rule: zero when r^2 < 1e-12
 // (cpp/kernel.h:19-33).  Formulas: LaplaceSingle 1/(4 pi r)
 // (cpp/laplace_kernels.h:25), LaplaceDouble n_y.delta/(4 pi r^3) (:41),
-// ElasticDisplacement / Traction / AdjointTraction
-// (cpp/elastic_kernels.h:192-311), IdentityScalar (cpp/identity_kernels.h).
+// ElasticDisplacement / Traction / AdjointTraction / Hypersingular
+// (cpp/elastic_kernels.h:192-357), IdentityScalar (cpp/identity_kernels.h).
 //
 // accumulate<KID, TRANS>() adds K v (or K^T v for the transposed apply) for
 // one pair directly, without forming the tensor: the elastic kernels reduce
@@ -16,11 +16,11 @@
 
 namespace tbem {
 
-enum KernelId { LAP_S = 0, LAP_D = 1, EL_DISP = 2, EL_TRAC = 3, EL_ADJ = 4, IDENT = 5 };
+enum KernelId { LAP_S = 0, LAP_D = 1, EL_DISP = 2, EL_TRAC = 3, EL_ADJ = 4, IDENT = 5, EL_HYP = 6 };
 
 __host__ __device__ constexpr int kernel_dim(int kid)
 {
-    return (kid == EL_DISP || kid == EL_TRAC || kid == EL_ADJ) ? 3 : 1;
+    return (kid == EL_DISP || kid == EL_TRAC || kid == EL_ADJ || kid == EL_HYP) ? 3 : 1;
 }
 
 // Constants of a kernel instance (mu, nu enter through c1, c2).
@@ -39,6 +39,7 @@ inline KParams make_kparams(int kid, double mu, double nu)
     case EL_DISP: p.scale = 1.0 / (16 * pi * mu * (1 - nu)); p.c2 = 3 - 4 * nu; break;
     case EL_TRAC:
     case EL_ADJ: p.scale = 1.0 / (8 * pi * (1 - nu)); p.c2 = 1 - 2 * nu; break;
+    case EL_HYP: p.scale = mu / (4 * pi * (1 - nu)); p.c2 = 1 - 2 * nu; break;
     default: p.scale = 1.0; break;
     }
     return p;
@@ -50,6 +51,36 @@ template <>
 __device__ __forceinline__ double dev_rsqrt<double>(double x) { return rsqrt(x); }
 template <>
 __device__ __forceinline__ float dev_rsqrt<float>(float x) { return rsqrtf(x); }
+
+// Hypersingular tensor without the leading constant (cpp/elastic_kernels.h:
+// 333-357): the traction (observation normal m) of the displacement field of
+// a dislocation with normal n, r^-3 times a polynomial in e = d / r, m, n.
+// nu comes from c2 = 1 - 2 nu.
+template <typename T>
+__device__ __forceinline__ void hyp_tensor(T dx, T dy, T dz, T r2, T ir, T mx, T my, T mz, T nx,
+                                           T ny, T nz, T c2, T* H)
+{
+    const T nu = (T(1) - c2) * T(0.5);
+    const T c3 = T(3) * nu, c4 = T(4) * nu - T(1);
+    const T e[3] = {dx * ir, dy * ir, dz * ir};
+    const T m[3] = {mx, my, mz}, n[3] = {nx, ny, nz};
+    const T em = e[0] * mx + e[1] * my + e[2] * mz;
+    const T en = e[0] * nx + e[1] * ny + e[2] * nz;
+    const T nm = nx * mx + ny * my + nz * mz;
+    const T C = ir / r2;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const T dkj = k == j ? T(1) : T(0);
+            const T t1 = T(3) * en * (c2 * m[k] * e[j] + nu * (m[j] * e[k] + dkj * em) -
+                                      T(5) * e[k] * e[j] * em);
+            const T t2 = c2 * (T(3) * n[j] * e[k] * em + dkj * nm + n[k] * m[j]);
+            const T t3 = c3 * (n[k] * e[j] * em + nm * e[k] * e[j]);
+            const T t4 = c4 * n[j] * m[k];
+            H[3 * k + j] = C * (t1 + t2 + t3 + t4);
+        }
+}
 
 // u += K(x,y) v  (TRANS: u += K(x,y)^T v), without the leading constant.
 // d = y - x; no = n_x (observation normal), ns = n_y (source normal).
@@ -75,6 +106,16 @@ __device__ __forceinline__ void accumulate(T dx, T dy, T dz, T nox, T noy, T noz
         u[0] += ir * (c2 * v[0] + dx * t);
         u[1] += ir * (c2 * v[1] + dy * t);
         u[2] += ir * (c2 * v[2] + dz * t);
+    } else if (KID == EL_HYP) {
+        T H[9];
+        hyp_tensor<T>(dx, dy, dz, r2, ir, nox, noy, noz, nsx, nsy, nsz, c2, H);
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                if (!TRANS) u[k] += H[3 * k + j] * v[j];
+                else u[j] += H[3 * k + j] * v[k];
+            }
     } else if (KID == EL_TRAC || KID == EL_ADJ) {
         // K_kj = s/r^2 [ (c2 delta_kj + 3 d_k d_j / r^2) drdm + sgn c2 (m_j d_k - m_k d_j)/r ]
         // with m = n_y, s = -1, sgn = -1 for the traction kernel and m = n_x,
@@ -128,6 +169,10 @@ __device__ __forceinline__ void kernel_tensor(int kid, T dx, T dy, T dz, T nox, 
         for (int k = 0; k < 3; k++)
             for (int j = 0; j < 3; j++)
                 out[3 * k + j] = (T(p.scale) / r) * (T(p.c2) * (k == j) + d[k] * d[j] / r2);
+    } else if (kid == EL_HYP) {
+        T H[9];
+        hyp_tensor<T>(dx, dy, dz, r2, T(1) / r, nox, noy, noz, nsx, nsy, nsz, T(p.c2), H);
+        for (int i = 0; i < 9; i++) out[i] = T(p.scale) * H[i];
     } else {
         const bool trac = kid == EL_TRAC;
         const T m[3] = {trac ? nsx : nox, trac ? nsy : noy, trac ? nsz : noz};

@@ -135,7 +135,7 @@ extern "C" int tbem_direct_apply_noalloc(int kernel, const double* kernel_params
 {
     using namespace tbem;
     try {
-        if (kernel < 0 || kernel > 5 || n_obs < 0 || n_src < 0 || n_rhs <= 0)
+        if (kernel < 0 || kernel > 6 || n_obs < 0 || n_src < 0 || n_rhs <= 0)
             throw Error(TBEM_ERR_ARG, "bad kernel id, point count or n_rhs");
         if (n_obs == 0) return TBEM_OK;
         const int R = kernel_dim(kernel);

@@ -498,7 +498,7 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
                  const double* src_normals, const double* src_weights, long n_src_,
                  const TbemFmmConfig& cfg_, const TbemGpuOptions& opt_)
 {
-    if (kernel < 0 || kernel > 5) throw Error(TBEM_ERR_ARG, "unknown kernel id");
+    if (kernel < 0 || kernel > 6) throw Error(TBEM_ERR_ARG, "unknown kernel id");
     if (cfg_.min_pts_per_cell <= 0) throw Error(TBEM_ERR_ARG, "min_pts_per_cell must be > 0");
     if (cfg_.order <= 0) throw Error(TBEM_ERR_ARG, "order must be > 0");
     if (!(cfg_.mac > 0)) throw Error(TBEM_ERR_ARG, "mac must be > 0");
@@ -944,11 +944,13 @@ void Plan::build_form()
         F.r_uc = 2.9;
         F.r_dc = 1.1;
         F.r_de = 2.9;
-        const bool elastic = kid == EL_DISP || kid == EL_TRAC || kid == EL_ADJ;
+        const bool elastic = kid == EL_DISP || kid == EL_TRAC || kid == EL_ADJ || kid == EL_HYP;
         F.g_kid = kid == IDENT ? IDENT : (elastic ? EL_DISP : LAP_S);
-        // adjoint traction: point-force sources, traction observed at the targets
-        F.ks_kid = kid == EL_ADJ ? EL_DISP : kid;
-        F.kt_kid = kid == EL_ADJ ? EL_ADJ : F.g_kid;
+        // adjoint traction: point-force sources, traction observed at the
+        // targets; hypersingular: dislocation sources (the traction kernel's
+        // displacement field), traction observed at the targets
+        F.ks_kid = kid == EL_ADJ ? EL_DISP : kid == EL_HYP ? EL_TRAC : kid;
+        F.kt_kid = (kid == EL_ADJ || kid == EL_HYP) ? EL_ADJ : F.g_kid;
     }
     build_c2e(F);
     if (F.mixed) build_mixed_ops(F);

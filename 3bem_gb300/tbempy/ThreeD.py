@@ -95,6 +95,12 @@ class ElasticAdjointTraction(_Elastic):
     kernel_id = 4
 
 
+class ElasticHypersingular(_Elastic):
+    """Hypersingular kernel: traction of the displacement of a dislocation
+    (cpp/elastic_kernels.h:314-365)."""
+    kernel_id = 6
+
+
 def _f64(a, shape=None):
     a = np.ascontiguousarray(a, dtype=np.float64)
     if shape is not None:

@@ -43,6 +43,7 @@ extern "C" {
 #define TBEM_ELASTIC_TRACTION 3
 #define TBEM_ELASTIC_ADJOINT_TRACTION 4
 #define TBEM_IDENTITY_SCALAR 5
+#define TBEM_ELASTIC_HYPERSINGULAR 6  /* cpp/elastic_kernels.h:314-365 */
 
 /* precision forms */
 #define TBEM_PRECISION_FP64 0   /* plain: reference surfaces and formulation, FP64 */

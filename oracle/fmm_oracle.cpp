@@ -15,7 +15,8 @@
 // the reference's svd_pseudoinverse (cpp/blas_wrapper.cpp:67-127).
 //
 // Kernel ids: 0 LaplaceSingle, 1 LaplaceDouble, 2 ElasticDisplacement,
-// 3 ElasticTraction, 4 ElasticAdjointTraction, 5 IdentityScalar (all 3D).
+// 3 ElasticTraction, 4 ElasticAdjointTraction, 5 IdentityScalar,
+// 6 ElasticHypersingular (all 3D).
 #include <cmath>
 #include <cstring>
 #include <cstdint>
@@ -38,18 +39,23 @@ struct KernelSpec {
     int R;
     double mu, nu;
     // constants precomputed like the reference's constructors
-    double c1, c2;
+    double c1, c2, c3 = 0.0, c4 = 0.0;
 };
 
 KernelSpec make_kernel(int id, double mu, double nu)
 {
-    KernelSpec k{id, (id == 2 || id == 3 || id == 4) ? 3 : 1, mu, nu, 0.0, 0.0};
+    KernelSpec k{id, (id == 2 || id == 3 || id == 4 || id == 6) ? 3 : 1, mu, nu, 0.0, 0.0};
     if (id == 2) {  // cpp/elastic_kernels.h:198-203
         k.c1 = 1.0 / (16 * M_PI * mu * (1 - nu));
         k.c2 = 3 - 4 * nu;
     } else if (id == 3 || id == 4) {  // cpp/elastic_kernels.h:236-241, 278-283
         k.c1 = 1.0 / (8 * M_PI * (1 - nu));
         k.c2 = 1 - 2 * nu;
+    } else if (id == 6) {  // cpp/elastic_kernels.h:323-331
+        k.c1 = mu / (4 * M_PI * (1 - nu));
+        k.c2 = 1 - 2 * nu;
+        k.c3 = 3 * nu;
+        k.c4 = -1 + 4 * nu;
     }
     return k;
 }
@@ -101,6 +107,27 @@ inline void kernel_eval(const KernelSpec& K, const V3& obs, const V3& src, const
                 const double term1 = (K.c2 * (k == j ? 1.0 : 0.0) + 3 * d[k] * d[j] / r2);
                 const double term2 = K.c2 * (nobs[j] * d[k] - nobs[k] * d[j]) / r;
                 out[3 * k + j] = (K.c1 / r2) * (term1 * drdm + term2);
+            }
+        }
+        return;
+    }
+    case 6: {  // cpp/elastic_kernels.h:333-357: traction (observation normal m) of the
+               // displacement of a dislocation (source normal n)
+        const double r = std::sqrt(r2);
+        const V3 e{d[0] / r, d[1] / r, d[2] / r};
+        const double em = dot3(d, nobs) / r;
+        const double en = dot3(e, nsrc);
+        const double nm = dot3(nsrc, nobs);
+        const double C = K.c1 / (r2 * r);
+        for (int k = 0; k < 3; k++) {
+            for (int j = 0; j < 3; j++) {
+                const double dkj = k == j ? 1.0 : 0.0;
+                const double t1 = 3 * en * (K.c2 * nobs[k] * e[j] + K.nu * (nobs[j] * e[k] + dkj * em) -
+                                            5 * e[k] * e[j] * em);
+                const double t2 = K.c2 * (3 * nsrc[j] * e[k] * em + dkj * nm + nsrc[k] * nobs[j]);
+                const double t3 = K.c3 * (nsrc[k] * e[j] * em + nm * e[k] * e[j]);
+                const double t4 = K.c4 * nsrc[j] * nobs[k];
+                out[3 * k + j] = C * (t1 + t2 + t3 + t4);
             }
         }
         return;
@@ -687,7 +714,7 @@ void* oracle_create(int kernel, double mu, double nu, const double* obs_locs,
                     const double* src_normals, const double* src_weights, long n_src,
                     double mac, long order, long min_pts, double d, int small_cells)
 {
-    if (kernel < 0 || kernel > 5 || min_pts <= 0 || order <= 0) return nullptr;
+    if (kernel < 0 || kernel > 6 || min_pts <= 0 || order <= 0) return nullptr;
     auto o = new Oracle();
     o->K = make_kernel(kernel, mu, nu);
     read_pts(o->obs, obs_locs, obs_normals, nullptr, n_obs);
@@ -811,7 +838,7 @@ long oracle_surface(long order, double* pts)
 int oracle_kernel(int kernel, double mu, double nu, const double* obs, const double* src,
                   const double* nobs, const double* nsrc, double* out)
 {
-    if (kernel < 0 || kernel > 5) return -1;
+    if (kernel < 0 || kernel > 6) return -1;
     auto K = make_kernel(kernel, mu, nu);
     kernel_eval(K, {obs[0], obs[1], obs[2]}, {src[0], src[1], src[2]},
                 {nobs[0], nobs[1], nobs[2]}, {nsrc[0], nsrc[1], nsrc[2]}, out);
@@ -825,7 +852,7 @@ int oracle_direct(int kernel, double mu, double nu, const double* obs_locs,
                   const double* src_normals, const double* src_weights, long n_src,
                   const double* x, double* y)
 {
-    if (kernel < 0 || kernel > 5) return -1;
+    if (kernel < 0 || kernel > 6) return -1;
     auto K = make_kernel(kernel, mu, nu);
     const int R = K.R;
 #pragma omp parallel for schedule(static)

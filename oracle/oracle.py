@@ -25,8 +25,9 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libtbem_ref.so")
 
 KERNELS = {"LaplaceSingle": 0, "LaplaceDouble": 1, "ElasticDisplacement": 2,
-           "ElasticTraction": 3, "ElasticAdjointTraction": 4, "IdentityScalar": 5}
-TENSOR_KERNELS = (2, 3, 4)
+           "ElasticTraction": 3, "ElasticAdjointTraction": 4, "IdentityScalar": 5,
+           "ElasticHypersingular": 6}
+TENSOR_KERNELS = (2, 3, 4, 6)
 LISTS = ["p2m", "m2m", "p2p", "m2p", "p2l", "m2l", "l2l", "l2p"]
 
 

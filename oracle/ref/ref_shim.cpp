@@ -8,7 +8,8 @@
 //
 // Kernel ids follow include/tbem_gpu.h:
 //   0 LaplaceSingle<3>, 1 LaplaceDouble<3>, 2 ElasticDisplacement<3>,
-//   3 ElasticTraction<3>, 4 ElasticAdjointTraction<3>, 5 IdentityScalar<3>.
+//   3 ElasticTraction<3>, 4 ElasticAdjointTraction<3>, 5 IdentityScalar<3>,
+//   6 ElasticHypersingular<3>.
 #include <memory>
 #include <vector>
 #include <cstring>
@@ -70,6 +71,7 @@ std::unique_ptr<Kernel<3, 3, 3>> tensor_kernel(int id, double mu, double nu)
     if (id == 2) return std::unique_ptr<Kernel<3, 3, 3>>(new ElasticDisplacement<3>(mu, nu));
     if (id == 3) return std::unique_ptr<Kernel<3, 3, 3>>(new ElasticTraction<3>(mu, nu));
     if (id == 4) return std::unique_ptr<Kernel<3, 3, 3>>(new ElasticAdjointTraction<3>(mu, nu));
+    if (id == 6) return std::unique_ptr<Kernel<3, 3, 3>>(new ElasticHypersingular<3>(mu, nu));
     return nullptr;
 }
 

@@ -106,6 +106,20 @@ def kernel_vectors():
                                  1.0, 0.25, lib="ref")
         rows.append(np.concatenate([[k, 1.0, 0.25], p, p + 1e-7, [1, 0, 0], [0, 1, 0],
                                     np.pad(K.ravel(), (0, 9 - K.size))]))
+    # the hypersingular kernel (id 6), its own seed so the rows above stay put
+    rng6 = np.random.default_rng(43)
+    for _ in range(40):
+        obs, src = rng6.uniform(-1, 1, 3), rng6.uniform(-1, 1, 3)
+        no, ns = rng6.normal(size=3), rng6.normal(size=3)
+        no /= np.linalg.norm(no)
+        ns /= np.linalg.norm(ns)
+        mu, nu = rng6.uniform(0.5, 40.0), rng6.uniform(0.1, 0.45)
+        K = oracle.kernel_tensor(6, obs, src, no, ns, mu, nu, lib="ref")
+        rows.append(np.concatenate([[6, mu, nu], obs, src, no, ns, K.ravel()]))
+    p = rng6.uniform(-1, 1, 3)
+    K = oracle.kernel_tensor(6, p, p + 1e-7, np.array([1.0, 0, 0]), np.array([0, 1.0, 0]), 1.0, 0.25,
+                             lib="ref")
+    rows.append(np.concatenate([[6, 1.0, 0.25], p, p + 1e-7, [1, 0, 0], [0, 1, 0], K.ravel()]))
     return np.array(rows)
 
 

@@ -19,7 +19,7 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 KERNELS = ["LaplaceSingle", "LaplaceDouble", "ElasticDisplacement", "ElasticTraction",
-           "ElasticAdjointTraction"]
+           "ElasticAdjointTraction", "ElasticHypersingular"]
 
 
 def rel(a, b):

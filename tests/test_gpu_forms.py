@@ -135,7 +135,8 @@ def test_integral_operator_composition():
         ThreeD.IntegralOperator(near, corr, galerkin, far, rand_csr(499, n_dof, 100)[0])
 
 
-@pytest.mark.parametrize("name", ["ElasticDisplacement", "ElasticTraction", "LaplaceDouble"])
+@pytest.mark.parametrize("name", ["ElasticDisplacement", "ElasticTraction", "LaplaceDouble",
+                                  "ElasticHypersingular"])
 def test_vertex_gradients_match_central_differences(name):
     """Differentiated misfit L = 0.5 ||G(v) s - d||^2 over a bumpy fault's
     vertex coordinates v, observers on the free surface z = 0: the GPU
