@@ -25,12 +25,18 @@ struct TbemGraph {
     int device = 0;
     ~TbemGraph()
     {
+        // released on the device they were made on, the caller's given back
+        int prev = -1;
+        const bool own = cudaGetDevice(&prev) == cudaSuccess && prev != device &&
+                         cudaSetDevice(device) == cudaSuccess;
+        cudaGetLastError();
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         for (auto e : joins) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         for (auto b : branch) cudaStreamDestroy(b);
         if (cap) cudaStreamDestroy(cap);
+        if (own) cudaSetDevice(prev);
     }
 };
 
