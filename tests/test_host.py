@@ -146,3 +146,49 @@ def test_graph_arguments_rejected_before_device_use():
     assert L.tbem_fmm_graph_create(ops, 1, ptrs, ptrs, 1, 0, C.byref(h)) == -4  # host_only
     assert b"host_only" in L.tbem_last_error()
     assert L.tbem_fmm_graph_launch(None, None) == -1
+
+
+def test_header_and_library_from_plain_c(tmp_path):
+    """include/tbem_gpu.h is a C header: a C99 program compiles against it,
+    links with the library and builds a host-only operator through the ABI
+    (trees and lists only, no device use)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    from tbempy import _lib
+    lib_path = _lib.lib()._name
+    src = tmp_path / "abi.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include "tbem_gpu.h"
+int main(void) {
+    double locs[3 * 64], nrm[3 * 64], w[64];
+    for (int i = 0; i < 64; i++) {
+        locs[3 * i] = (i % 4) * 0.25; locs[3 * i + 1] = ((i / 4) % 4) * 0.25;
+        locs[3 * i + 2] = (i / 16) * 0.25;
+        nrm[3 * i] = 0; nrm[3 * i + 1] = 0; nrm[3 * i + 2] = 1; w[i] = 1.0;
+    }
+    TbemFmmConfig cfg = {0.3, 20, 8, 0.05, 0};
+    TbemGpuOptions opt;
+    tbem_default_options(&opt);
+    opt.host_only = 1;
+    TbemFmm* h = NULL;
+    int rc = tbem_fmm_create(TBEM_LAPLACE_SINGLE, NULL, locs, nrm, 64, locs, nrm, w, 64, &cfg, &opt, &h);
+    if (rc != TBEM_OK) { printf("create failed: %s\n", tbem_last_error()); return 1; }
+    long cells = tbem_fmm_tree_cells(h, 0, NULL, NULL, NULL, NULL, NULL, NULL);
+    double x[64], y[64];
+    int rc2 = tbem_fmm_apply(h, x, y, 1, NULL);   /* host_only: refused with a status */
+    printf("%ld %ld %ld %d\n", tbem_fmm_n_rows(h), tbem_fmm_n_cols(h), cells, rc2 == TBEM_ERR_STATE);
+    tbem_fmm_destroy(h);
+    return 0;
+}
+""")
+    exe = tmp_path / "abi"
+    inc = os.path.join(ROOT, "include")
+    libdir = os.path.dirname(lib_path)
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-I", inc, str(src), "-o", str(exe),
+                    "-L", libdir, "-ltbem_gpu", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert out[0] == "64" and out[1] == "64" and int(out[2]) > 1 and out[3] == "1"
