@@ -587,9 +587,9 @@ void Plan::autotune_tc()
     TBEM_CK(cudaEventCreate(&e1));
     float best = 1e30f;
     int best_bn = 128, best_bk = 64;
-    const int shapes[3][2] = {{128, 64}, {64, 64}, {128, 32}};
-    const int fixed = opt.tc_shape >= 1 && opt.tc_shape <= 3 ? opt.tc_shape - 1 : -1;
-    for (int si = 0; si < 3; si++) {
+    const int shapes[4][2] = {{128, 64}, {64, 64}, {128, 32}, {256, 32}};
+    const int fixed = opt.tc_shape >= 1 && opt.tc_shape <= 4 ? opt.tc_shape - 1 : -1;
+    for (int si = 0; si < 4; si++) {
         const auto& sh = shapes[si];
         if (fixed >= 0 && si != fixed) continue;
         G.tc_bn = sh[0];

@@ -45,24 +45,30 @@ constexpr long long TC_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
 // Tile shapes (the autotuner picks one per operator set): N = 128 columns and
 // 64-deep K chunks (128-byte rows, 128B swizzle) in a 2-stage ring; N = 64,
 // 64-deep, 3 stages; N = 128 with 32-deep chunks (64-byte rows, 64B swizzle)
-// in a 4-stage ring, which keeps three chunks in flight.
+// in a 4-stage ring, which keeps three chunks in flight; N = 256, 32-deep,
+// 3 stages (each A chunk serves twice the columns: less shared-memory
+// traffic per MMA), one accumulator buffer.
 template <int BN, int BK>
 struct TcShape {
     static_assert(BK == 64 || BK == 32, "K chunk");
     static constexpr int RB = BK * 2;                                     // bytes per tile row
-    static constexpr int STAGES = BK == 32 ? 4 : (BN == 128 ? 2 : 3);
+    static constexpr int STAGES = BK == 32 ? (BN == 256 ? 3 : 4) : (BN == 128 ? 2 : 3);
     static constexpr int A_TILE = TC_BM * RB;                             // one A plane tile
     static constexpr int B_TILE = BN * RB;                                // one B plane tile
     static constexpr int STAGE_BYTES = TC_TERMS * (A_TILE + B_TILE);
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
-    static constexpr uint32_t TMEM_COLS = 4 * BN;  // 2 buffers x (big, small) accumulators
+    // accumulator buffers of (big, small): two while they fit in the 512
+    // tensor-memory columns (the epilogue overlaps the next tile), else one
+    static constexpr int NBUF = 4 * BN <= 512 ? 2 : 1;
+    static constexpr uint32_t TMEM_COLS = NBUF * 2 * BN;
     // kind::f16, bf16 A/B, FP32 D, K-major A and B, M = 128, N = BN
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
                                       ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
 };
 static_assert(TcShape<128, 64>::SMEM_BYTES <= 227 * 1024 && TcShape<64, 64>::SMEM_BYTES <= 227 * 1024 &&
-                  TcShape<128, 32>::SMEM_BYTES <= 227 * 1024,
+                  TcShape<128, 32>::SMEM_BYTES <= 227 * 1024 && TcShape<256, 32>::SMEM_BYTES <= 227 * 1024,
               "shared memory budget");
+static_assert(TcShape<256, 32>::TMEM_COLS == 512 && TcShape<128, 64>::TMEM_COLS == 512, "tensor memory");
 constexpr int TC_PRODUCERS = 128;                      // producer threads (warps 4-7)
 constexpr int TC_THREADS_P = 128 + TC_PRODUCERS + 32;  // epilogue + producers + MMA warp
 
@@ -312,7 +318,7 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
             int j = 0, tc = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < total && ok; t += gridDim.x, tc++) {
-                const int b = tc & 1, bu = tc >> 1;
+                const int b = tc % Sh::NBUF, bu = tc / Sh::NBUF;
                 if (bu >= 1 && !wait(&acce_bar[b], (bu - 1) & 1)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t big = tmem + b * 2 * BN, small = big + BN;
@@ -350,7 +356,7 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
         constexpr int NCC = BN / 32;
         int tc = 0;
         for (int t = blockIdx.x; t < total; t += gridDim.x, tc++) {
-            const int b = tc & 1, bu = tc >> 1;
+            const int b = tc % Sh::NBUF, bu = tc / Sh::NBUF;
             const int tile = t / m_tiles, m0 = (t % m_tiles) * TC_BM;
             // lane q of a 32-column chunk resolves column q's destination; the
             // loads overlap the wait for the accumulator
@@ -459,6 +465,8 @@ void TcPlanes::build(const float* ops32, long n_ops, int m, int k, cudaStream_t 
                                  TcShape<64, 64>::SMEM_BYTES));
     TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<128, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  TcShape<128, 32>::SMEM_BYTES));
+    TBEM_CK(cudaFuncSetAttribute(tc_gemm_kernel<256, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TcShape<256, 32>::SMEM_BYTES));
 }
 
 void TcPlanes::split_b(const float* cells, long rows, cudaStream_t s)
@@ -489,7 +497,7 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
                      long* launches)
 {
     if (empty()) return;
-    const int bn = tc_bn == 64 ? 64 : 128;
+    const int bn = tc_bn == 64 ? 64 : tc_bn == 256 ? 256 : 128;
     const int key = nrhs * 1024 + bn;
     auto it = tc_tiles.find(key);
     if (it == tc_tiles.end()) {
@@ -543,6 +551,8 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
     const unsigned grid = (unsigned)std::min<long>(total, std::max(sms, 1));
     if (bn == 64)
         tc_gemm_kernel<64, 64><<<grid, TC_THREADS_P, TcShape<64, 64>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
+    else if (bn == 256)
+        tc_gemm_kernel<256, 32><<<grid, TC_THREADS_P, TcShape<256, 32>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
     else if (tc_bk == 32)
         tc_gemm_kernel<128, 32><<<grid, TC_THREADS_P, TcShape<128, 32>::SMEM_BYTES, s>>>(a, n_ctiles, m_tiles);
     else

@@ -81,7 +81,7 @@ typedef struct {
     int p2m_block;         /* 0 auto; else threads per target in the points-to-
                               check-surface kernel (1, 2, 4)                      */
     int tc_shape;          /* tensor-core tile: 0 auto (timed at creation); 1 N 128 x
-                              K chunk 64, 2 N 64 x 64, 3 N 128 x 32               */
+                              K chunk 64, 2 N 64 x 64, 3 N 128 x 32, 4 N 256 x 32 */
 } TbemGpuOptions;
 
 typedef struct TbemFmm TbemFmm;

@@ -193,7 +193,7 @@ def test_compressed_m2l(name, order):
         assert abs(lhs - rhs) <= 1e-6 * np.linalg.norm(AX[r]) * np.linalg.norm(Z[r])
 
 
-@pytest.mark.parametrize("shape", [1, 2, 3])
+@pytest.mark.parametrize("shape", [1, 2, 3, 4])
 def test_tensor_core_tile_shapes(shape):
     """Every tile shape the tensor-core autotuner can pick (N 128 / 64 columns,
     64- or 32-deep K chunks with 128- or 64-byte swizzle) against the FP32
@@ -205,7 +205,7 @@ def test_tensor_core_tile_shapes(shape):
     tcs = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed", m2l_path=5,
                              tc_shape=shape)
     simt = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed", m2l_path=4)
-    assert tcs.tc_tile() == (64 if shape == 2 else 128)
+    assert tcs.tc_tile() == {1: 128, 2: 64, 3: 128, 4: 256}[shape]
     X = np.random.default_rng(40).uniform(-1, 1, (2, tcs.n_cols()))
     assert rel(tcs.apply(X), simt.apply(X)) < 2e-6
 
