@@ -16,7 +16,12 @@
 //
 // Kernel ids: 0 LaplaceSingle, 1 LaplaceDouble, 2 ElasticDisplacement,
 // 3 ElasticTraction, 4 ElasticAdjointTraction, 5 IdentityScalar,
-// 6 ElasticHypersingular (all 3D).
+// 6 ElasticHypersingular (3D); 16 LaplaceSingle, 17 LaplaceDouble,
+// 18 LaplaceHypersingular, 19 ElasticDisplacement, 20 ElasticTraction,
+// 21 ElasticAdjointTraction, 22 ElasticHypersingular, 23 IdentityScalar (2D:
+// FMMOperator<2,1,1> and <2,2,2>, cpp/fmm.cpp:651-652).  Points are passed as
+// [n][3] for both; a 2D operator reads x and y and keeps z = 0, which leaves
+// every sum, product and square root of the 2D arithmetic unchanged.
 #include <cmath>
 #include <cstring>
 #include <cstdint>
@@ -31,6 +36,10 @@ namespace {
 typedef std::array<double, 3> V3;
 
 inline double dot3(const V3& a, const V3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline double dot2(const V3& a, const V3& b) { return a[0] * b[0] + a[1] * b[1]; }
+
+inline bool valid_kernel(int id) { return (id >= 0 && id <= 6) || (id >= 16 && id <= 23); }
+inline int space_dim(int id) { return id >= 16 ? 2 : 3; }
 
 // ---------------------------------------------------------------- kernels
 // cpp/kernel.h:19-33: delta = src - obs, zero tensor when r2 < 1e-12.
@@ -44,7 +53,17 @@ struct KernelSpec {
 
 KernelSpec make_kernel(int id, double mu, double nu)
 {
-    KernelSpec k{id, (id == 2 || id == 3 || id == 4 || id == 6) ? 3 : 1, mu, nu, 0.0, 0.0};
+    const int R = (id == 2 || id == 3 || id == 4 || id == 6) ? 3 : (id >= 19 && id <= 22) ? 2 : 1;
+    KernelSpec k{id, R, mu, nu, 0.0, 0.0};
+    if (id == 19) {  // cpp/elastic_kernels.h:29-34
+        k.c1 = 1.0 / (8 * M_PI * mu * (1 - nu));
+        k.c2 = 3 - 4 * nu;
+    } else if (id == 20 || id == 21) {  // cpp/elastic_kernels.h:67-72, 109-114
+        k.c1 = 1.0 / (4 * M_PI * (1 - nu));
+        k.c2 = 1 - 2 * nu;
+    } else if (id == 22) {  // cpp/elastic_kernels.h:150-155
+        k.c2 = 1 - 2 * nu;
+    }
     if (id == 2) {  // cpp/elastic_kernels.h:198-203
         k.c1 = 1.0 / (16 * M_PI * mu * (1 - nu));
         k.c2 = 3 - 4 * nu;
@@ -114,7 +133,9 @@ inline void kernel_eval(const KernelSpec& K, const V3& obs, const V3& src, const
     case 6: {  // cpp/elastic_kernels.h:333-357: traction (observation normal m) of the
                // displacement of a dislocation (source normal n)
         const double r = std::sqrt(r2);
-        const V3 e{d[0] / r, d[1] / r, d[2] / r};
+        // Vec / scalar multiplies by the reciprocal (cpp/vec_ops.h:151-155)
+        const double ir = 1 / r;
+        const V3 e{d[0] * ir, d[1] * ir, d[2] * ir};
         const double em = dot3(d, nobs) / r;
         const double en = dot3(e, nsrc);
         const double nm = dot3(nsrc, nobs);
@@ -132,7 +153,69 @@ inline void kernel_eval(const KernelSpec& K, const V3& obs, const V3& src, const
         }
         return;
     }
-    default:  // IdentityScalar, cpp/identity_kernels.h:13-30
+    case 16:  // cpp/laplace_kernels.h:70
+        out[0] = std::log(std::sqrt(r2)) / (2 * M_PI);
+        return;
+    case 17:  // cpp/laplace_kernels.h:89
+        out[0] = dot2(nsrc, d) / (2 * M_PI * r2);
+        return;
+    case 18:  // cpp/laplace_kernels.h:104-106
+        out[0] = ((-dot2(nobs, nsrc) / r2) + ((2 * dot2(nsrc, d) * dot2(nobs, d)) / (r2 * r2))) /
+                 (2 * M_PI);
+        return;
+    case 19: {  // cpp/elastic_kernels.h:36-49
+        const double r = std::sqrt(r2);
+        for (int k = 0; k < 2; k++)
+            for (int j = 0; j < 2; j++)
+                out[2 * k + j] =
+                    K.c1 * (-K.c2 * (k == j ? 1.0 : 0.0) * std::log(r) + d[k] * d[j] / r2);
+        return;
+    }
+    case 20: {  // cpp/elastic_kernels.h:74-91
+        const double r = std::sqrt(r2);
+        const double drdn = dot2(d, nsrc) / r;
+        for (int k = 0; k < 2; k++)
+            for (int j = 0; j < 2; j++) {
+                const double term1 = (K.c2 * (k == j ? 1.0 : 0.0) + 2 * d[k] * d[j] / r2);
+                const double term2 = K.c2 * (nsrc[j] * d[k] - nsrc[k] * d[j]) / r;
+                out[2 * k + j] = -(K.c1 / r) * (term1 * drdn - term2);
+            }
+        return;
+    }
+    case 21: {  // cpp/elastic_kernels.h:116-133
+        const double r = std::sqrt(r2);
+        const double drdm = dot2(d, nobs) / r;
+        for (int k = 0; k < 2; k++)
+            for (int j = 0; j < 2; j++) {
+                const double term1 = (K.c2 * (k == j ? 1.0 : 0.0) + 2 * d[k] * d[j] / r2);
+                const double term2 = K.c2 * (nobs[j] * d[k] - nobs[k] * d[j]) / r;
+                out[2 * k + j] = (K.c1 / r) * (term1 * drdm + term2);
+            }
+        return;
+    }
+    case 22: {  // cpp/elastic_kernels.h:157-181
+        const double r = std::sqrt(r2);
+        const double ir = 1 / r;  // Vec / scalar, cpp/vec_ops.h:151-155
+        const V3 e{d[0] * ir, d[1] * ir, 0.0};
+        const double drdn = dot2(e, nsrc);
+        const double drdm = dot2(e, nobs);
+        const double nm = dot2(nsrc, nobs);
+        const double nu = K.nu;
+        for (int k = 0; k < 2; k++)
+            for (int j = 0; j < 2; j++) {
+                const double dkj = k == j ? 1.0 : 0.0;
+                const double line1 = 2 * drdn * (K.c2 * nobs[k] * e[j] +
+                                                 nu * (nobs[j] * e[k] + dkj * drdm) -
+                                                 4 * e[k] * e[j] * drdm);
+                const double line2 = K.c2 * (2 * nsrc[j] * e[k] * drdm + dkj * nm + nsrc[k] * nobs[j]);
+                const double line3 = 2 * nu * (nsrc[k] * e[j] * drdm + nm * e[k] * e[j]);
+                const double line4 = -(1 - 4 * nu) * nsrc[j] * nobs[k];
+                const double C = (K.mu / (2 * M_PI * (1 - nu) * r2));
+                out[2 * k + j] = C * (line1 + line2 + line3 + line4);
+            }
+        return;
+    }
+    default:  // IdentityScalar, cpp/identity_kernels.h:13-30 (ids 5 and 23)
         out[0] = 1.0;
         return;
     }
@@ -232,34 +315,37 @@ Box bounding_box(const std::vector<V3>& pts, const std::vector<size_t>& idx)
     return b;
 }
 
-// expand_by_max_axis_multiple (cpp/geometry.cpp:13-17).
-Box expand(const Box& b, double factor)
+// expand_by_max_axis_multiple (cpp/geometry.cpp:13-17) over the first dim axes.
+Box expand(const Box& b, double factor, int dim)
 {
-    double m = std::max(b.hw[0], std::max(b.hw[1], b.hw[2]));
+    double m = b.hw[0];
+    for (int d = 1; d < dim; d++) m = std::max(m, b.hw[d]);
     double e = factor * m;
-    return Box{b.center, {b.hw[0] + e, b.hw[1] + e, b.hw[2] + e}};
+    Box out = b;
+    for (int d = 0; d < dim; d++) out.hw[d] = b.hw[d] + e;
+    return out;
 }
 
-// get_subcell with make_child_idx bit order: bit 2 of i is x (cpp/geometry.cpp:20-28,
-// cpp/octree.cpp:45-55).
-Box subcell(const Box& b, int i)
+// get_subcell with make_child_idx bit order: the last axis is bit 0, the
+// first axis bit dim - 1 (cpp/geometry.cpp:20-28, cpp/octree.cpp:65-75).
+Box subcell(const Box& b, int i, int dim)
 {
-    int idx[3] = {(i >> 2) & 1, (i >> 1) & 1, i & 1};
-    Box out;
-    for (int d = 0; d < 3; d++) {
+    Box out = b;
+    for (int d = 0; d < dim; d++) {
+        const int idx = (i >> (dim - 1 - d)) & 1;
         out.hw[d] = b.hw[d] / 2.0;
-        out.center[d] = b.center[d] + ((static_cast<double>(idx[d]) * 2) - 1) * out.hw[d];
+        out.center[d] = b.center[d] + ((static_cast<double>(idx) * 2) - 1) * out.hw[d];
     }
     return out;
 }
 
 // find_containing_subcell (cpp/geometry.cpp:83-95): '>' sends ties to the low child.
-int containing_subcell(const Box& b, const V3& p)
+int containing_subcell(const Box& b, const V3& p, int dim)
 {
     int c = 0;
-    for (int d = 0; d < 3; d++) {
+    for (int d = 0; d < dim; d++) {
         if (p[d] > b.center[d]) c++;
-        if (d < 2) c <<= 1;
+        if (d < dim - 1) c <<= 1;
     }
     return c;
 }
@@ -293,21 +379,22 @@ struct Cell {
 std::array<std::unique_ptr<Cell>, 8> build_children(const Box& bounds, const std::vector<V3>& pts,
                                                     const std::vector<size_t>& indices,
                                                     size_t level, size_t min_pts,
-                                                    size_t& next_index)
+                                                    size_t& next_index, int dim)
 {
     std::array<std::unique_ptr<Cell>, 8> children;
     if (indices.size() <= min_pts) return children;
     std::array<std::vector<size_t>, 8> child_idx;
     for (size_t i = 0; i < indices.size(); i++)
-        child_idx[containing_subcell(bounds, pts[indices[i]])].push_back(indices[i]);
-    for (int i = 0; i < 8; i++) {
+        child_idx[containing_subcell(bounds, pts[indices[i]], dim)].push_back(indices[i]);
+    for (int i = 0; i < (1 << dim); i++) {
         if (child_idx[i].empty()) continue;
-        Box cb = subcell(bounds, i);
+        Box cb = subcell(bounds, i, dim);
         Box tight = bounding_box(pts, child_idx[i]);
         std::array<std::unique_ptr<Cell>, 8> sub;
-        // recurse unless every point coincides (all half widths equal the zero radius)
+        // recurse unless every point coincides (all half widths equal the zero
+        // radius; a 2D operator's z half width is always zero)
         if (tight.hw[0] != 0.0 || tight.hw[1] != 0.0 || tight.hw[2] != 0.0)
-            sub = build_children(cb, pts, child_idx[i], level + 1, min_pts, next_index);
+            sub = build_children(cb, pts, child_idx[i], level + 1, min_pts, next_index, dim);
         size_t my_index = next_index++;
         children[i].reset(new Cell{cb, child_idx[i], level + 1, my_index, {}});
         children[i]->children = std::move(sub);
@@ -317,14 +404,14 @@ std::array<std::unique_ptr<Cell>, 8> build_children(const Box& bounds, const std
 
 // make_octree (cpp/octree.cpp:156-171): root bounds are the expanded box, the
 // children are cut from the unexpanded one.
-std::unique_ptr<Cell> make_octree(const std::vector<V3>& pts, size_t min_pts)
+std::unique_ptr<Cell> make_octree(const std::vector<V3>& pts, size_t min_pts, int dim)
 {
     std::vector<size_t> all(pts.size());
     for (size_t i = 0; i < all.size(); i++) all[i] = i;
     Box box = bounding_box(pts, all);
-    Box ebox = expand(box, 1e-5);
+    Box ebox = expand(box, 1e-5, dim);
     size_t next_index = 1;
-    auto ch = build_children(box, pts, all, 0, min_pts, next_index);
+    auto ch = build_children(box, pts, all, 0, min_pts, next_index, dim);
     std::unique_ptr<Cell> root(new Cell{ebox, all, 0, 0, {}});
     root->children = std::move(ch);
     return root;
@@ -367,6 +454,26 @@ std::vector<V3> sphere_surface(size_t order)
     return pts;
 }
 
+// TranslationSurface<2>::make_surrounding_surface (cpp/fmm.cpp:7-20): order
+// points on the unit circle at theta_i = linspace(0, 2 pi, order + 1)[i]
+// (cpp/numbers.cpp:5-12).
+std::vector<V3> circle_surface(size_t order)
+{
+    std::vector<V3> pts;
+    const double a = 0, b = 2 * M_PI;
+    const size_t count = order + 1;
+    for (size_t i = 0; i < order; i++) {
+        const double theta = a + i * (b - a) / ((double)count - 1);
+        pts.push_back({std::cos(theta), std::sin(theta), 0.0});
+    }
+    return pts;
+}
+
+std::vector<V3> unit_surface(size_t order, int dim)
+{
+    return dim == 2 ? circle_surface(order) : sphere_surface(order);
+}
+
 struct Surface {
     std::vector<V3> pts;      // scaled by r_ref (TranslationSurface::scale)
     std::vector<V3> normals;  // the unscaled unit points
@@ -381,10 +488,10 @@ struct Surface {
     }
 };
 
-Surface make_surface(size_t order, double r_ref)
+Surface make_surface(size_t order, double r_ref, int dim)
 {
     Surface s;
-    s.normals = sphere_surface(order);
+    s.normals = unit_surface(order, dim);
     s.pts.resize(s.normals.size());
     for (size_t i = 0; i < s.pts.size(); i++)
         for (int d = 0; d < 3; d++) s.pts[i][d] = r_ref * s.normals[i][d];
@@ -714,7 +821,8 @@ void* oracle_create(int kernel, double mu, double nu, const double* obs_locs,
                     const double* src_normals, const double* src_weights, long n_src,
                     double mac, long order, long min_pts, double d, int small_cells)
 {
-    if (kernel < 0 || kernel > 6 || min_pts <= 0 || order <= 0) return nullptr;
+    if (!valid_kernel(kernel) || min_pts <= 0 || order <= 0) return nullptr;
+    const int dim = space_dim(kernel);
     auto o = new Oracle();
     o->K = make_kernel(kernel, mu, nu);
     read_pts(o->obs, obs_locs, obs_normals, nullptr, n_obs);
@@ -725,12 +833,12 @@ void* oracle_create(int kernel, double mu, double nu, const double* obs_locs,
     o->dd = d;
     o->small_cells = small_cells != 0;
     double r_far = 4.0 - std::sqrt(2) - 2 * d;  // cpp/fmm.h:44,64
-    o->up_check = make_surface(order, r_far);
-    o->up_equiv = make_surface(order, 0.3);     // cpp/fmm.h:51
-    o->down_check = make_surface(order, 0.3);   // cpp/fmm.h:58
-    o->down_equiv = make_surface(order, r_far);
-    o->src_oct = make_octree(o->src.locs, min_pts);
-    o->obs_oct = make_octree(o->obs.locs, min_pts);
+    o->up_check = make_surface(order, r_far, dim);
+    o->up_equiv = make_surface(order, 0.3, dim);     // cpp/fmm.h:51
+    o->down_check = make_surface(order, 0.3, dim);   // cpp/fmm.h:58
+    o->down_equiv = make_surface(order, r_far, dim);
+    o->src_oct = make_octree(o->src.locs, min_pts, dim);
+    o->obs_oct = make_octree(o->obs.locs, min_pts, dim);
     Oracle::first_at_level(*o->src_oct, o->src_first_at_level);
     Oracle::first_at_level(*o->obs_oct, o->obs_first_at_level);
     o->up_c2e.resize(o->src_first_at_level.size());
@@ -826,9 +934,10 @@ long oracle_list(void* p, int kind, long* a, long* b)
     return (long)v.size();
 }
 
-long oracle_surface(long order, double* pts)
+// Unit translation-surface points ([n][3]; z = 0 for dim 2).
+long oracle_surface(long order, int dim, double* pts)
 {
-    auto s = sphere_surface((size_t)order);
+    auto s = unit_surface((size_t)order, dim);
     if (pts)
         for (size_t i = 0; i < s.size(); i++)
             for (int d = 0; d < 3; d++) pts[3 * i + d] = s[i][d];
@@ -838,7 +947,7 @@ long oracle_surface(long order, double* pts)
 int oracle_kernel(int kernel, double mu, double nu, const double* obs, const double* src,
                   const double* nobs, const double* nsrc, double* out)
 {
-    if (kernel < 0 || kernel > 6) return -1;
+    if (!valid_kernel(kernel)) return -1;
     auto K = make_kernel(kernel, mu, nu);
     kernel_eval(K, {obs[0], obs[1], obs[2]}, {src[0], src[1], src[2]},
                 {nobs[0], nobs[1], nobs[2]}, {nsrc[0], nsrc[1], nsrc[2]}, out);
@@ -852,7 +961,7 @@ int oracle_direct(int kernel, double mu, double nu, const double* obs_locs,
                   const double* src_normals, const double* src_weights, long n_src,
                   const double* x, double* y)
 {
-    if (kernel < 0 || kernel > 6) return -1;
+    if (!valid_kernel(kernel)) return -1;
     auto K = make_kernel(kernel, mu, nu);
     const int R = K.R;
 #pragma omp parallel for schedule(static)

@@ -27,7 +27,28 @@ REF_LIB_PATH = os.path.join(HERE, "_ref", "libtbem_ref.so")
 KERNELS = {"LaplaceSingle": 0, "LaplaceDouble": 1, "ElasticDisplacement": 2,
            "ElasticTraction": 3, "ElasticAdjointTraction": 4, "IdentityScalar": 5,
            "ElasticHypersingular": 6}
+# 2D kernels (FMMOperator<2,1,1> / <2,2,2>); their points are [n][2] or [n][3]
+# with z ignored
+KERNELS_2D = {"LaplaceSingle": 16, "LaplaceDouble": 17, "LaplaceHypersingular": 18,
+              "ElasticDisplacement": 19, "ElasticTraction": 20, "ElasticAdjointTraction": 21,
+              "ElasticHypersingular": 22, "IdentityScalar": 23}
 TENSOR_KERNELS = (2, 3, 4, 6)
+TENSOR_KERNELS_2D = (19, 20, 21, 22)
+
+
+def kernel_id(kernel, dim=3):
+    if isinstance(kernel, str):
+        return (KERNELS_2D if dim == 2 else KERNELS)[kernel]
+    return int(kernel)
+
+
+def kernel_components(k):
+    """R (= C) of kernel id k."""
+    return 3 if k in TENSOR_KERNELS else 2 if k in TENSOR_KERNELS_2D else 1
+
+
+def space_dim(k):
+    return 2 if k >= 16 else 3
 LISTS = ["p2m", "m2m", "p2p", "m2p", "p2l", "m2l", "l2l", "l2p"]
 
 
@@ -65,6 +86,14 @@ def _ptr(a):
 
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _pts3(a):
+    """[n][2] or [n][3] points as [n][3] (z = 0 added to 2D points)."""
+    a = np.asarray(a, dtype=np.float64).reshape(len(a), -1)
+    if a.shape[1] == 2:
+        a = np.concatenate([a, np.zeros((len(a), 1))], axis=1)
+    return np.ascontiguousarray(a)
 
 
 def pinv_reference(A, threshold=1e-10):
@@ -105,10 +134,11 @@ class _FMMBase:
     def _setup(self, L, kernel, obs_locs, obs_normals, src_locs, src_normals,
                src_weights, mac, order, min_pts, d, small_cells, mu, nu):
         self.L = L
-        self.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
-        self.R = 3 if self.kernel in TENSOR_KERNELS else 1
-        self.obs_locs, self.obs_normals = _f64(obs_locs), _f64(obs_normals)
-        self.src_locs, self.src_normals = _f64(src_locs), _f64(src_normals)
+        dim = np.asarray(obs_locs).reshape(len(obs_locs), -1).shape[1] if len(obs_locs) else 3
+        self.kernel = kernel_id(kernel, dim)
+        self.R = kernel_components(self.kernel)
+        self.obs_locs, self.obs_normals = _pts3(obs_locs), _pts3(obs_normals)
+        self.src_locs, self.src_normals = _pts3(src_locs), _pts3(src_normals)
         self.src_weights = _f64(src_weights)
         self.n_obs, self.n_src = len(self.obs_locs), len(self.src_locs)
         create = L.fn("fmm_create" if L.prefix == "ref_" else "create", _P,
@@ -153,7 +183,9 @@ class _FMMBase:
 
 
 class OracleFMM(_FMMBase):
-    """The oracle restatement of FMMOperator<3,R,C> (cpp/fmm.h:131-237)."""
+    """The oracle restatement of FMMOperator<dim,R,C> (cpp/fmm.h:131-237).
+
+    kernel: an id, or a name resolved in 2D when the points are [n][2]."""
 
     def __init__(self, kernel, obs_locs, obs_normals, src_locs, src_normals, src_weights,
                  mac, order, min_pts, d=0.05, small_cells=False, mu=1.0, nu=0.25):
@@ -232,10 +264,11 @@ def ref_available():
 def direct(kernel, obs_locs, obs_normals, src_locs, src_normals, src_weights, x,
            mu=1.0, nu=0.25):
     """FP64 direct N-body sum (the reference's nbody_eval over all pairs)."""
-    k = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
-    R = 3 if k in TENSOR_KERNELS else 1
-    ol, on = _f64(obs_locs), _f64(obs_normals)
-    sl, sn, sw = _f64(src_locs), _f64(src_normals), _f64(src_weights)
+    dim = np.asarray(obs_locs).reshape(len(obs_locs), -1).shape[1] if len(obs_locs) else 3
+    k = kernel_id(kernel, dim)
+    R = kernel_components(k)
+    ol, on = _pts3(obs_locs), _pts3(obs_normals)
+    sl, sn, sw = _pts3(src_locs), _pts3(src_normals), _f64(src_weights)
     x = _f64(x)
     y = np.zeros(R * len(ol))
     f = _lib().fn("direct", _I, [_I, _D, _D, _P, _P, _L, _P, _P, _P, _L, _P, _P])
@@ -246,21 +279,23 @@ def direct(kernel, obs_locs, obs_normals, src_locs, src_normals, src_weights, x,
 
 def kernel_tensor(kernel, obs, src, nobs, nsrc, mu=1.0, nu=0.25, lib="oracle"):
     """One kernel tensor K(obs, src, nobs, nsrc) as an R x C array."""
-    k = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+    k = kernel_id(kernel, len(obs))
     L = _lib() if lib == "oracle" else _Lib._cache.setdefault("ref", _Lib(REF_LIB_PATH, "ref_"))
     f = L.fn("kernel", _I, [_I, _D, _D, _P, _P, _P, _P, _P])
     out = np.zeros(9)
-    args = [_f64(a) for a in (obs, src, nobs, nsrc)]
+    args = [_pts3(np.reshape(a, (1, -1)))[0] for a in (obs, src, nobs, nsrc)]
     n = f(k, mu, nu, *[_ptr(a) for a in args], _ptr(out))
-    R = 3 if n == 9 else 1
+    R = {9: 3, 4: 2}.get(n, 1)
     return out[:n].reshape(R, R)
 
 
-def surface(order):
-    f = _lib().fn("surface", _L, [_L, _P])
-    n = f(int(order), None)
+def surface(order, dim=3, lib="oracle"):
+    """Unit translation-surface points, [n][3] (z = 0 in 2D)."""
+    L = _lib() if lib == "oracle" else _Lib._cache.setdefault("ref", _Lib(REF_LIB_PATH, "ref_"))
+    f = L.fn("surface", _L, [_L, _I, _P])
+    n = f(int(order), int(dim), None)
     p = np.zeros((n, 3))
-    f(int(order), _ptr(p))
+    f(int(order), int(dim), _ptr(p))
     return p
 
 

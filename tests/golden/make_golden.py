@@ -6,7 +6,9 @@ small seeded inputs, and stores inputs, reference outputs, the reference's
 check-to-equivalent operators, trees and task lists.  The GPU tests compare
 the product against these without needing the reference checkout.
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py [/root/reference] [all|2d]
+
+("2d" writes only the 2D fixtures: fmm_*2_*.npz and kernels_2d.npz.)
 
 The reference's LAPACK (scipy's OpenBLAS) is run single-threaded so that
 the stored operators are reproducible.
@@ -40,9 +42,32 @@ CASES = [
     ("eldisp_fault", "ElasticDisplacement", 1536, 0, 12, 64, False, 9, "fault16"),
 ]
 
+# 2D operators (FMMOperator<2,1,1> / <2,2,2>): points [n][2]
+CASES_2D = [
+    ("laps2_square", "LaplaceSingle", 600, 0, 20, 20, False, 11, "square"),
+    ("lapd2_square_small", "LaplaceDouble", 600, 0, 20, 20, True, 12, "square"),
+    ("laph2_two_sets", "LaplaceHypersingular", 500, 300, 20, 20, False, 13, "square"),
+    ("eldisp2_square", "ElasticDisplacement", 400, 0, 12, 20, False, 14, "square"),
+    ("eltrac2_square_small", "ElasticTraction", 400, 0, 12, 20, True, 15, "square"),
+    ("eladj2_square", "ElasticAdjointTraction", 400, 0, 12, 20, False, 16, "square"),
+    ("elhyp2_square", "ElasticHypersingular", 400, 0, 16, 20, False, 17, "square"),
+    ("laps2_circle", "LaplaceSingle", 1024, 0, 20, 30, False, 18, "circle"),
+]
+
 
 def points(geom, n, seed):
     rng = np.random.default_rng(seed)
+    if geom == "square":
+        locs = rng.uniform(0, 1, (n, 2))
+        nrm = rng.normal(size=(n, 2))
+        nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+        w = rng.uniform(0.5, 1.0, n)
+        return locs, nrm, w
+    if geom == "circle":
+        # midpoints of n equal segments of the unit circle, outward normals
+        t = 2 * np.pi * (np.arange(n) + 0.5) / n
+        nrm = np.stack([np.cos(t), np.sin(t)], axis=1)
+        return nrm.copy(), nrm, np.full(n, 2 * np.pi / n)
     if geom == "cube":
         locs = rng.uniform(0, 1, (n, 3))
         nrm = rng.normal(size=(n, 3))
@@ -60,7 +85,7 @@ def points(geom, n, seed):
 def make_case(name, kernel, n_src, n_obs, order, leaf, small, seed, geom):
     locs, nrm, w = points(geom, n_src, seed)
     if n_obs:
-        ol, on, _ = points("cube", n_obs, seed + 100)
+        ol, on, _ = points("square" if locs.shape[1] == 2 else "cube", n_obs, seed + 100)
     else:
         ol, on = locs, nrm
     ref = oracle.RefFMM(kernel, ol, on, locs, nrm, w, 0.3, order, leaf, 0.05, small)
@@ -123,10 +148,47 @@ def kernel_vectors():
     return np.array(rows)
 
 
-def main(ref_root="/root/reference"):
+def kernel_vectors_2d():
+    """Reference 2D kernel tensors (ids 16-23) at seeded random configurations,
+    the same row layout as kernel_vectors with z = 0 everywhere."""
+    rng = np.random.default_rng(44)
+    rows = []
+    for k in range(16, 24):
+        for _ in range(40):
+            obs, src = rng.uniform(-1, 1, 2), rng.uniform(-1, 1, 2)
+            no, ns = rng.normal(size=2), rng.normal(size=2)
+            no /= np.linalg.norm(no)
+            ns /= np.linalg.norm(ns)
+            mu, nu = rng.uniform(0.5, 40.0), rng.uniform(0.1, 0.45)
+            K = oracle.kernel_tensor(k, obs, src, no, ns, mu, nu, lib="ref")
+            z = [0.0]
+            rows.append(np.concatenate([[k, mu, nu], obs, z, src, z, no, z, ns, z,
+                                        np.pad(K.ravel(), (0, 9 - K.size))]))
+        p = rng.uniform(-1, 1, 2)
+        K = oracle.kernel_tensor(k, p, p + 1e-7, np.array([1.0, 0]), np.array([0, 1.0]), 1.0, 0.25,
+                                 lib="ref")
+        rows.append(np.concatenate([[k, 1.0, 0.25], p, [0], p + 1e-7, [0], [1, 0, 0], [0, 1, 0],
+                                    np.pad(K.ravel(), (0, 9 - K.size))]))
+    return np.array(rows)
+
+
+def main(ref_root="/root/reference", which="all"):
     oracle.build()
     if oracle.build_ref(ref_root) is None:
         raise SystemExit("the reference checkout is needed to regenerate the fixtures")
+    for case in CASES_2D:
+        data = make_case(*case)
+        np.savez_compressed(os.path.join(HERE, "fmm_%s.npz" % case[0]), **data)
+        print("wrote", case[0], {k: v.shape for k, v in data.items() if hasattr(v, "shape") and v.ndim})
+    circ = {str(o): oracle.RefFMM("LaplaceSingle", np.zeros((1, 2)), np.zeros((1, 2)),
+                                  np.zeros((1, 2)), np.zeros((1, 2)), np.ones(1), 0.3, o, 1,
+                                  0.05, False).n_surf() for o in (1, 4, 12, 20, 64)}
+    np.savez_compressed(os.path.join(HERE, "kernels_2d.npz"), rows=kernel_vectors_2d(),
+                        surf_orders=np.array([int(k) for k in circ]),
+                        surf_counts=np.array(list(circ.values())),
+                        surf4=oracle.surface(4, 2, lib="ref"))
+    if which == "2d":
+        return
     for case in CASES:
         data = make_case(*case)
         np.savez_compressed(os.path.join(HERE, "fmm_%s.npz" % case[0]), **data)

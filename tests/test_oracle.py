@@ -72,12 +72,30 @@ def test_kernel_golden_vectors():
         k, mu, nu = int(r[0]), r[1], r[2]
         K = oracle.kernel_tensor(k, r[3:6], r[6:9], r[9:12], r[12:15], mu, nu)
         ref = r[15:15 + K.size].reshape(K.shape)
-        if k == 6:
-            # the hypersingular restatement keeps the reference's terms but not
-            # every rounding step: equal to a few ulps of the largest entry
-            assert np.abs(K - ref).max() <= 1e-14 * max(np.abs(ref).max(), 1e-300), (k, K, ref)
-        else:
-            assert np.allclose(K, ref, rtol=1e-14, atol=0), (k, K, ref)
+        assert np.allclose(K, ref, rtol=1e-14, atol=0), (k, K, ref)
+
+
+def test_kernel_golden_vectors_2d():
+    """The 2D kernels (ids 16-23) against the reference's own tensors, bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "kernels_2d.npz"))
+    rows = g["rows"]
+    assert sorted(set(rows[:, 0].astype(int))) == list(range(16, 24))
+    for r in rows:
+        k, mu, nu = int(r[0]), r[1], r[2]
+        K = oracle.kernel_tensor(k, r[3:5], r[6:8], r[9:11], r[12:14], mu, nu)
+        assert K.shape == ((2, 2) if 19 <= k <= 22 else (1, 1))
+        assert np.array_equal(K, r[15:15 + K.size].reshape(K.shape)), (k, K)
+
+
+def test_circle_surface_known_values():
+    """unit_tests/test_fmm.cpp:21-29 (order 4) and the reference's point counts."""
+    g = np.load(os.path.join(GOLDEN, "kernels_2d.npz"))
+    s = oracle.surface(4, 2)
+    assert np.array_equal(s, g["surf4"])
+    assert np.allclose(s[0, :2], [1, 0], atol=1e-12) and np.allclose(s[1, :2], [0, 1], atol=1e-12)
+    assert np.allclose(s[3, :2], [0, -1], atol=1e-12)
+    for o, c in zip(g["surf_orders"], g["surf_counts"]):
+        assert len(oracle.surface(int(o), 2)) == c == o
 
 
 REF_ELASTIC = "/root/reference/unit_tests/test_data_elastic3"
@@ -105,6 +123,33 @@ def test_elastic_kernels_against_reference_sympy_data():
                 assert K[k, j] == 0.0
             n += 1
     assert n == 360
+
+
+REF_ELASTIC_2D = "/root/reference/unit_tests/test_data_elastic2"
+
+
+@pytest.mark.skipif(not os.path.exists(REF_ELASTIC_2D), reason="reference checkout absent")
+def test_elastic_kernels_2d_against_reference_sympy_data():
+    """unit_tests/test_data_elastic2 through unit_tests/test_elastic_kernels.cpp:54-119
+    (2D: the first two of each coordinate triple, 1e-8)."""
+    ids = {"disp": 19, "trac": 20, "adj_trac": 21, "hyp": 22}
+    n = 0
+    with open(REF_ELASTIC_2D) as f:
+        for line in f:
+            e = line.strip().split(",")
+            if e[1] not in ids:
+                continue
+            k, j = int(e[2]), int(e[3])
+            v = [float(t) for t in e[8:20]]
+            K = oracle.kernel_tensor(ids[e[1]], v[3:5], v[0:2], v[9:11], v[6:8], float(e[4]),
+                                     float(e[5]))
+            exact = float(e[0])
+            if exact != 0.0:
+                assert abs(exact - K[k, j]) / ((abs(exact) + abs(K[k, j])) / 2) < 1e-8
+            else:
+                assert K[k, j] == 0.0
+            n += 1
+    assert n == 160
 
 
 def test_laplace_nbody_known_values():
@@ -188,6 +233,45 @@ def test_oracle_fmm_accuracy_reference_cases(name, order):
     assert np.all(_ref_error(o.apply(x), exact) <= 1e-4)
 
 
+@pytest.mark.parametrize("name,order,tol,mu", [
+    ("IdentityScalar", 1, 1e-4, 1.0), ("LaplaceSingle", 5, 1e-2, 1.0),
+    ("LaplaceDouble", 20, 1e-4, 1.0), ("LaplaceHypersingular", 20, 1e-4, 1.0),
+    ("ElasticDisplacement", 20, 1e-4, 30e9), ("ElasticTraction", 20, 1e-4, 30e9),
+    ("ElasticHypersingular", 30, 1e-4, 30e9)])
+def test_oracle_fmm_accuracy_reference_cases_2d(name, order, tol, mu):
+    """unit_tests/test_fmm.cpp:109-149 (2D): 100 random points in the unit
+    square, unit weights, mac 0.35, one point per cell, d = 0.05."""
+    rng = np.random.default_rng(4)
+    src, obs, nrm = rng.uniform(0, 1, (100, 2)), rng.uniform(0, 1, (100, 2)), rng.uniform(0, 1, (100, 2))
+    o = oracle.OracleFMM(name, obs, nrm, src, nrm, np.ones(100), 0.35, order, 1, 0.05, False,
+                         mu=mu, nu=0.25)
+    x = np.ones(o.R * 100)
+    exact = oracle.direct(name, obs, nrm, src, nrm, np.ones(100), x, mu=mu, nu=0.25)
+    assert np.all(_ref_error(o.apply(x), exact) <= tol)
+
+
+def test_quadtree_known_answers():
+    """unit_tests/test_octree.cpp:16-20, 54-62, 102-111: child order (x is the
+    high bit), the degenerate 2D line splits, and points are conserved."""
+    # child index 1 = (x low, y high), 3 = (high, high): place one point per quadrant
+    pts = np.array([[-1.0, -1.0], [-1.0, 1.0], [1.0, -1.0], [1.0, 1.0]])
+    o = oracle.OracleFMM("LaplaceSingle", pts, pts, pts, pts, np.ones(4), 0.3, 4, 1, 0.05, False)
+    t = o.tree(0)
+    kids = np.where(t["level"] == 1)[0]
+    assert [int(t["indices"][c][0]) for c in kids] == [0, 1, 2, 3]
+    line = np.array([[float(i), 0.0] for i in range(100)])
+    for leaf in (1, 26):
+        o = oracle.OracleFMM("LaplaceSingle", line, line, line, line, np.ones(100), 0.3, 4, leaf,
+                             0.05, False)
+        t = o.tree(0)
+        assert t["n_children"][0] > 0
+        leaves = np.where(t["n_children"] == 0)[0]
+        assert np.array_equal(np.sort(np.concatenate([t["indices"][i] for i in leaves])),
+                              np.arange(100))
+        # a quadtree: at most four children, z untouched
+        assert t["n_children"].max() <= 4 and not t["center"][:, 2].any() and not t["hw"][:, 2].any()
+
+
 def test_identity_fmm_known_answer():
     rng = np.random.default_rng(2)
     pts = rng.uniform(0, 1, (300, 3))
@@ -210,6 +294,34 @@ def test_oracle_vs_reference_library(small):
                 a.set_c2e(which, lev, b.c2e(which, lev))
         x = rng.uniform(-1, 1, a.R * 1500)
         assert rel(a.apply(x), b.apply(x)) < 1e-12
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference library not built here")
+@pytest.mark.parametrize("small", [False, True])
+def test_oracle_vs_reference_library_2d(small):
+    """Every 2D kernel: identical trees and lists, and with the reference's
+    own pseudo-inverses installed, the same apply to rounding (bit for bit
+    with one thread; both sides scatter with OpenMP atomics otherwise)."""
+    rng = np.random.default_rng(6)
+    pts = rng.uniform(-1, 1, (800, 2))
+    obs = rng.uniform(-1, 1, (700, 2)) + np.array([0.4, 0.1])
+    nrm = rng.normal(size=(800, 2))
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    w = rng.uniform(0.5, 1.5, 800)
+    for k in range(16, 24):
+        a = oracle.OracleFMM(k, obs, nrm[:700], pts, nrm, w, 0.3, 16, 12, 0.05, small, mu=1.3, nu=0.27)
+        b = oracle.RefFMM(k, obs, nrm[:700], pts, nrm, w, 0.3, 16, 12, 0.05, small, mu=1.3, nu=0.27)
+        for which in (0, 1):
+            ta, tb = a.tree(which), b.tree(which)
+            for key in ("level", "index", "center", "hw", "n_idx", "n_children"):
+                assert np.array_equal(ta[key], tb[key]), (k, key)
+        for kind in oracle.LISTS:
+            assert all(np.array_equal(u, v) for u, v in zip(a.list(kind), b.list(kind))), (k, kind)
+        for which in (0, 1):
+            for lev in range(b.n_levels(which)):
+                a.set_c2e(which, lev, b.c2e(which, lev))
+        x = rng.uniform(-1, 1, a.R * 800)
+        assert rel(a.apply(x), b.apply(x)) < 1e-13, k
 
 
 def test_hypersingular_is_the_traction_of_the_dislocation_field():
