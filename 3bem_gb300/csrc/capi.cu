@@ -97,9 +97,17 @@ int tbem_fmm_clone(const TbemFmm* h, TbemFmm** out)
     if (!h || !out) return fail(TBEM_ERR_ARG, "null argument");
     const tbem::Plan& p = h->plan;
     double params[2] = {p.mu, p.nu};
-    int rc = tbem_fmm_create(p.kid, params, p.h_obs_locs.data(), p.h_obs_normals.data(), p.n_obs,
-                             p.h_src_locs.data(), p.h_src_normals.data(), p.h_src_weights.data(),
-                             p.n_src, &p.cfg, &p.opt, out);
+    // the plan keeps [n][3] points; the create call takes [n][sdim]
+    auto narrow = [&](const std::vector<double>& v) {
+        std::vector<double> o(v.size() / 3 * p.sdim);
+        for (size_t i = 0; i < v.size() / 3; i++)
+            for (int d = 0; d < p.sdim; d++) o[p.sdim * i + d] = v[3 * i + d];
+        return o;
+    };
+    const std::vector<double> ol = narrow(p.h_obs_locs), on = narrow(p.h_obs_normals),
+                              sl = narrow(p.h_src_locs), sn = narrow(p.h_src_normals);
+    int rc = tbem_fmm_create(p.kid, params, ol.data(), on.data(), p.n_obs, sl.data(), sn.data(),
+                             p.h_src_weights.data(), p.n_src, &p.cfg, &p.opt, out);
     if (rc != TBEM_OK) return rc;
     if (!p.f.mixed) {
         // carry over installed check-to-equivalent operators

@@ -1,4 +1,6 @@
-// Instantiates the evaluation kernels of one kernel id (EVAL_KID).
+// Instantiates the evaluation kernels of one kernel id (EVAL_KID); with
+// EVAL_FP64_ONLY (the 2D kernels, which have the plain FP64 form only) the
+// FP32 variants are not built and asking for them is an error.
 #include "eval_launch.h"
 
 namespace tbem {
@@ -52,7 +54,12 @@ cudaError_t go_t(const EvalLaunch& L, const void* args, cudaStream_t s)
 cudaError_t TBEM_CAT(launch_eval_k, EVAL_KID)(const EvalLaunch& L, const void* args, bool fp32,
                                               cudaStream_t s)
 {
+#ifdef EVAL_FP64_ONLY
+    if (fp32) return cudaErrorInvalidValue;
+    return go_t<double>(L, args, s);
+#else
     return fp32 ? go_t<float>(L, args, s) : go_t<double>(L, args, s);
+#endif
 }
 
 }  // namespace tbem

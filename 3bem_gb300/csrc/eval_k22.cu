@@ -1,0 +1,3 @@
+#define EVAL_KID 22
+#define EVAL_FP64_ONLY 1
+#include "eval_inst.cuh"

@@ -24,6 +24,15 @@ cudaError_t launch_eval_k3(const EvalLaunch&, const void* args, bool fp32, cudaS
 cudaError_t launch_eval_k4(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
 cudaError_t launch_eval_k5(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
 cudaError_t launch_eval_k6(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+// 2D kernels (FP64 only)
+cudaError_t launch_eval_k16(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k17(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k18(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k19(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k20(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k21(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k22(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
+cudaError_t launch_eval_k23(const EvalLaunch&, const void* args, bool fp32, cudaStream_t);
 
 // rhs chunk per launch (the kernel keeps NR x R accumulators per thread)
 constexpr int EVAL_NR = 4;
@@ -39,7 +48,16 @@ inline cudaError_t launch_eval(const EvalLaunch& L, const EvalArgs<T>& a, cudaSt
     case 3: return launch_eval_k3(L, &a, fp32, s);
     case 4: return launch_eval_k4(L, &a, fp32, s);
     case 5: return launch_eval_k5(L, &a, fp32, s);
-    default: return launch_eval_k6(L, &a, fp32, s);
+    case 6: return launch_eval_k6(L, &a, fp32, s);
+    case 16: return launch_eval_k16(L, &a, fp32, s);
+    case 17: return launch_eval_k17(L, &a, fp32, s);
+    case 18: return launch_eval_k18(L, &a, fp32, s);
+    case 19: return launch_eval_k19(L, &a, fp32, s);
+    case 20: return launch_eval_k20(L, &a, fp32, s);
+    case 21: return launch_eval_k21(L, &a, fp32, s);
+    case 22: return launch_eval_k22(L, &a, fp32, s);
+    case 23: return launch_eval_k23(L, &a, fp32, s);
+    default: return cudaErrorInvalidValue;
     }
 }
 

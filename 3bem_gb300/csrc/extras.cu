@@ -32,6 +32,33 @@ void stage(Staged& s, const double* p, size_t n, cudaStream_t st)
     s.p = s.own.p;
 }
 
+__global__ void widen_kernel(const double* in, double* out, long n)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        out[3 * i] = in[2 * i];
+        out[3 * i + 1] = in[2 * i + 1];
+        out[3 * i + 2] = 0.0;
+    }
+}
+
+// Device view of caller points [n][sdim] as [n][3] (2D points get z = 0).
+void stage_points(Staged& s, const double* p, long n, int sdim, cudaStream_t st)
+{
+    if (sdim == 3) {
+        stage(s, p, 3 * (size_t)n, st);
+        return;
+    }
+    Staged raw;
+    stage(raw, p, 2 * (size_t)n, st);
+    s.own.alloc(3 * (size_t)n);
+    widen_kernel<<<(unsigned)std::max<long>(1, std::min<long>((n + 255) / 256, 9728)), 256, 0, st>>>(
+        raw.p, s.own.p, n);
+    TBEM_CK(cudaGetLastError());
+    // raw's own buffer (if any) is freed on return: finish the copy first
+    TBEM_CK(cudaStreamSynchronize(st));
+    s.p = s.own.p;
+}
+
 __global__ void weight_kernel(const double* x, const double* w, double* s, long N, long total)
 {
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x)
@@ -75,11 +102,12 @@ int tbem_direct_apply(int kernel, const double* kernel_params, const double* obs
 {
     using namespace tbem;
     try {
-        if (kernel < 0 || kernel > 6 || n_obs < 0 || n_src < 0 || n_rhs <= 0 || !y)
+        if (!kernel_valid(kernel) || n_obs < 0 || n_src < 0 || n_rhs <= 0 || !y)
             throw Error(TBEM_ERR_ARG, "bad argument");
         const int R = kernel_dim(kernel);
-        const double mu = (kernel_params && R == 3) ? kernel_params[0] : 1.0;
-        const double nu = (kernel_params && R == 3) ? kernel_params[1] : 0.25;
+        const int sdim = kernel_space_dim(kernel);
+        const double mu = (kernel_params && R > 1) ? kernel_params[0] : 1.0;
+        const double nu = (kernel_params && R > 1) ? kernel_params[1] : 0.25;
         const KParams kp = make_kparams(kernel, mu, nu);
         cudaStream_t s = (cudaStream_t)stream;
         const bool y_dev = is_device(y);
@@ -92,10 +120,10 @@ int tbem_direct_apply(int kernel, const double* kernel_params, const double* obs
             TBEM_CK(cudaMemsetAsync(yd, 0, ny * sizeof(double), s));
         } else {
             Staged ol, on, sl, sn, sw, xs;
-            stage(ol, obs_locs, 3 * n_obs, s);
-            stage(on, obs_normals, 3 * n_obs, s);
-            stage(sl, src_locs, 3 * n_src, s);
-            stage(sn, src_normals, 3 * n_src, s);
+            stage_points(ol, obs_locs, n_obs, sdim, s);
+            stage_points(on, obs_normals, n_obs, sdim, s);
+            stage_points(sl, src_locs, n_src, sdim, s);
+            stage_points(sn, src_normals, n_src, sdim, s);
             stage(sw, src_weights, n_src, s);
             stage(xs, x, (size_t)R * n_src * n_rhs, s);
             DBuf<double> str;

@@ -244,7 +244,7 @@ __global__ void surf_matrix_kernel(const SurfJob* jobs, const double* unit, int 
     const double sy = surf_coord(J.sr, J.srref, vy, J.sc[1]);
     const double sz = surf_coord(J.sr, J.srref, vz, J.sc[2]);
     double k[9];
-    kernel_tensor<double>(kid, sx - tx, sy - ty, sz - tz, ux, uy, uz, vx, vy, vz, kp, k);
+    kernel_tensor_any<double>(kid, sx - tx, sy - ty, sz - tz, ux, uy, uz, vx, vy, vz, kp, k);
     const long ld = (long)R * ns;
     double* o = out + J.out_off;
     for (int d1 = 0; d1 < R; d1++)
@@ -272,7 +272,7 @@ __global__ void pts_surf_matrix_kernel(const long* pt0, const int* npts, const i
     const double sy = surf_coord(rad[c], rref, vy, center[3 * c + 1]);
     const double sz = surf_coord(rad[c], rref, vz, center[3 * c + 2]);
     double k[9];
-    kernel_tensor<double>(kid, sx - xyz[3 * p], sy - xyz[3 * p + 1], sz - xyz[3 * p + 2],
+    kernel_tensor_any<double>(kid, sx - xyz[3 * p], sy - xyz[3 * p + 1], sz - xyz[3 * p + 2],
                           nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2], vx, vy, vz, kp, k);
     const long ld = (long)R * ns;
     double* o = out + (row0[t] - out_row_base) * ld;
@@ -498,7 +498,7 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
                  const double* src_normals, const double* src_weights, long n_src_,
                  const TbemFmmConfig& cfg_, const TbemGpuOptions& opt_)
 {
-    if (kernel < 0 || kernel > 6) throw Error(TBEM_ERR_ARG, "unknown kernel id");
+    if (!kernel_valid(kernel)) throw Error(TBEM_ERR_ARG, "unknown kernel id");
     if (cfg_.min_pts_per_cell <= 0) throw Error(TBEM_ERR_ARG, "min_pts_per_cell must be > 0");
     if (cfg_.order <= 0) throw Error(TBEM_ERR_ARG, "order must be > 0");
     if (!(cfg_.mac > 0)) throw Error(TBEM_ERR_ARG, "mac must be > 0");
@@ -510,18 +510,28 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
         throw Error(TBEM_ERR_ARG, "unknown precision form");
     kid = kernel;
     R = kernel_dim(kid);
-    mu = (params && R == 3) ? params[0] : 1.0;
-    nu = (params && R == 3) ? params[1] : 0.25;
+    sdim = kernel_space_dim(kid);
+    if (sdim == 2 && opt_.precision != TBEM_PRECISION_FP64)
+        throw Error(TBEM_ERR_ARG, "2D kernels run in the plain FP64 form only (the precision "
+                                  "form's operator reuse needs the 3D kernels' homogeneity)");
+    mu = (params && R > 1) ? params[0] : 1.0;
+    nu = (params && R > 1) ? params[1] : 0.25;
     kp = make_kparams(kid, mu, nu);
     cfg = cfg_;
     opt = opt_;
     if (!(opt.svd_threshold > 0)) opt.svd_threshold = 1e-10;
     n_obs = n_obs_;
     n_src = n_src_;
-    h_obs_locs.assign(obs_locs, obs_locs + 3 * n_obs);
-    h_obs_normals.assign(obs_normals, obs_normals + 3 * n_obs);
-    h_src_locs.assign(src_locs, src_locs + 3 * n_src);
-    h_src_normals.assign(src_normals, src_normals + 3 * n_src);
+    // points are [n][sdim]; kept as [n][3] (z = 0 in 2D)
+    auto widen = [&](std::vector<double>& dst, const double* p, long n) {
+        dst.assign(3 * n, 0.0);
+        for (long i = 0; i < n; i++)
+            for (int d = 0; d < sdim; d++) dst[3 * i + d] = p[sdim * i + d];
+    };
+    widen(h_obs_locs, obs_locs, n_obs);
+    widen(h_obs_normals, obs_normals, n_obs);
+    widen(h_src_locs, src_locs, n_src);
+    widen(h_src_normals, src_normals, n_src);
     h_src_weights.assign(src_weights, src_weights + n_src);
 
     std::unique_ptr<DeviceGuard> guard;
@@ -537,17 +547,17 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
         TBEM_CKS(cusolverDnSetStream(solver, stream));
     }
 
-    otree = build_tree(h_obs_locs.data(), n_obs, cfg.min_pts_per_cell);
+    otree = build_tree(h_obs_locs.data(), n_obs, cfg.min_pts_per_cell, sdim);
     same_tree = n_obs == n_src &&
                 (n_obs == 0 || std::memcmp(h_obs_locs.data(), h_src_locs.data(),
                                            3 * n_obs * sizeof(double)) == 0);
     if (same_tree) {
         stree = &otree;
     } else {
-        stree_own = build_tree(h_src_locs.data(), n_src, cfg.min_pts_per_cell);
+        stree_own = build_tree(h_src_locs.data(), n_src, cfg.min_pts_per_cell, sdim);
         stree = &stree_own;
     }
-    unit = sphere_surface(cfg.order);
+    unit = sdim == 2 ? circle_surface(cfg.order) : sphere_surface(cfg.order);
     ns = (int)(unit.size() / 3);
     n = R * ns;
     L = build_lists(otree, *stree, cfg.mac, ns, cfg.account_for_small_cells != 0);

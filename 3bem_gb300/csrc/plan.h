@@ -272,6 +272,7 @@ struct Form {
 
 struct Plan {
     int kid = 0, R = 1;
+    int sdim = 3;  // space dimension of the kernel (2: the reference's FMMOperator<2,R,C>)
     double mu = 1.0, nu = 0.25;
     KParams kp{};
     TbemFmmConfig cfg{};

@@ -33,33 +33,38 @@ Box bounding_box(const double* pts, const std::vector<long>& idx)
     return b;
 }
 
-// expand_by_max_axis_multiple (cpp/geometry.cpp:13-17)
-Box expand(const Box& b, double f)
+// expand_by_max_axis_multiple (cpp/geometry.cpp:13-17) over the first dim
+// axes (a 2D box keeps z = 0)
+Box expand(const Box& b, double f, int dim)
 {
-    double m = std::max(b.h[0], std::max(b.h[1], b.h[2]));
+    double m = b.h[0];
+    for (int d = 1; d < dim; d++) m = std::max(m, b.h[d]);
     double e = f * m;
-    return Box{{b.c[0], b.c[1], b.c[2]}, {b.h[0] + e, b.h[1] + e, b.h[2] + e}};
+    Box o = b;
+    for (int d = 0; d < dim; d++) o.h[d] = b.h[d] + e;
+    return o;
 }
 
-// get_subcell with make_child_idx's bit order (x is bit 2), cpp/geometry.cpp:20-28
-Box subcell(const Box& b, int oct)
+// get_subcell with make_child_idx's bit order: the first axis is the high bit
+// (bit dim - 1), cpp/geometry.cpp:20-28, cpp/octree.cpp:65-75
+Box subcell(const Box& b, int oct, int dim)
 {
-    int idx[3] = {(oct >> 2) & 1, (oct >> 1) & 1, oct & 1};
-    Box o;
-    for (int d = 0; d < 3; d++) {
+    Box o = b;
+    for (int d = 0; d < dim; d++) {
+        const int idx = (oct >> (dim - 1 - d)) & 1;
         o.h[d] = b.h[d] / 2.0;
-        o.c[d] = b.c[d] + ((static_cast<double>(idx[d]) * 2) - 1) * o.h[d];
+        o.c[d] = b.c[d] + ((static_cast<double>(idx) * 2) - 1) * o.h[d];
     }
     return o;
 }
 
 // find_containing_subcell: strict '>' (cpp/geometry.cpp:83-95)
-int containing(const Box& b, const double* p)
+int containing(const Box& b, const double* p, int dim)
 {
     int c = 0;
-    for (int d = 0; d < 3; d++) {
+    for (int d = 0; d < dim; d++) {
         if (p[d] > b.c[d]) c++;
-        if (d < 2) c <<= 1;
+        if (d < dim - 1) c <<= 1;
     }
     return c;
 }
@@ -76,6 +81,7 @@ struct Node {
 struct Builder {
     const double* pts;
     long min_pts;
+    int dim;
     std::vector<Node> nodes;
     long next_index = 1;
 
@@ -86,10 +92,10 @@ struct Builder {
         const std::vector<long> idx = nodes[node].idx;  // copy: nodes may reallocate
         if ((long)idx.size() <= min_pts) return;
         std::vector<long> part[8];
-        for (long i : idx) part[containing(bounds, &pts[3 * i])].push_back(i);
-        for (int o = 0; o < 8; o++) {
+        for (long i : idx) part[containing(bounds, &pts[3 * i], dim)].push_back(i);
+        for (int o = 0; o < (1 << dim); o++) {
             if (part[o].empty()) continue;
-            Box cb = subcell(bounds, o);
+            Box cb = subcell(bounds, o, dim);
             Box tight = bounding_box(pts, part[o]);
             Node n;
             n.b = cb;
@@ -110,16 +116,17 @@ struct Builder {
 
 }  // namespace
 
-Tree build_tree(const double* pts, long n, long min_pts)
+Tree build_tree(const double* pts, long n, long min_pts, int dim)
 {
     Builder B;
     B.pts = pts;
     B.min_pts = min_pts;
+    B.dim = dim;
     std::vector<long> all(n);
     for (long i = 0; i < n; i++) all[i] = i;
     Box box = bounding_box(pts, all);
     Node root;
-    root.b = expand(box, 1e-5);  // the root's bounds are the expanded box ...
+    root.b = expand(box, 1e-5, dim);  // the root's bounds are the expanded box ...
     root.idx = all;
     root.level = 0;
     root.ref_index = 0;
@@ -288,6 +295,23 @@ TaskLists build_lists(const Tree& obs, const Tree& src, double mac, long n_surf,
     if (obs.n_points() > 0 && src.n_points() > 0) B.dual(0, 0);
     if (obs.n_points() > 0) B.downward(0);
     return std::move(B.L);
+}
+
+// TranslationSurface<2>::make_surrounding_surface (cpp/fmm.cpp:7-20): order
+// points on the unit circle at linspace(0, 2 pi, order + 1)'s first order
+// angles (cpp/numbers.cpp:5-12), z = 0.
+std::vector<double> circle_surface(long order)
+{
+    std::vector<double> pts;
+    const double a = 0, b = 2 * M_PI;
+    const size_t count = (size_t)order + 1;
+    for (size_t i = 0; i < (size_t)order; i++) {
+        const double theta = a + i * (b - a) / ((double)count - 1);
+        pts.push_back(std::cos(theta));
+        pts.push_back(std::sin(theta));
+        pts.push_back(0.0);
+    }
+    return pts;
 }
 
 std::vector<double> sphere_surface(long order)

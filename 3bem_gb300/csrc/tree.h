@@ -22,7 +22,7 @@ struct Cell {
     int parent;       // flat id, -1 for the root
     int first_child;  // flat id of the first child, -1 for a leaf
     int n_children;
-    int octant;       // octant within the parent (bit 2 = x), -1 for the root
+    int octant;       // child slot within the parent (make_child_idx order), -1 for the root
     long pt_begin;    // permuted point range [pt_begin, pt_end)
     long pt_end;
     long ref_index;   // the reference's post-order index
@@ -40,8 +40,9 @@ struct Tree {
     long n_points() const { return (long)perm.size(); }
 };
 
-// pts: row-major [n][3].
-Tree build_tree(const double* pts, long n, long min_pts);
+// pts: row-major [n][3]; dim 2 builds the reference's quadtree
+// (Octree<2>) over x and y, with z = 0 in every point and cell.
+Tree build_tree(const double* pts, long n, long min_pts, int dim = 3);
 
 struct CellPair {
     int obs;
@@ -60,5 +61,7 @@ TaskLists build_lists(const Tree& obs, const Tree& src, double mac, long n_surf,
 
 // Unit points of surrounding_surface_sphere(order) (cpp/fmm.cpp:22-45).
 std::vector<double> sphere_surface(long order);
+// The 2D surface of order points on the unit circle (cpp/fmm.cpp:7-20), [n][3].
+std::vector<double> circle_surface(long order);
 
 }  // namespace tbem

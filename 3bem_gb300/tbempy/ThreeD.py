@@ -49,6 +49,7 @@ class FMMConfig:
 class Kernel:
     kernel_id = -1
     tensor_dim = 1
+    space_dim = 3
 
     def params(self):
         return None
@@ -183,10 +184,11 @@ class FMMOperator(OperatorI):
         if _handle is not None:
             self._h = _handle
             return
-        self._obs_locs = _f64(obs_locs, (-1, 3))
-        self._obs_normals = _f64(obs_normals, (-1, 3))
-        self._src_locs = _f64(src_locs, (-1, 3))
-        self._src_normals = _f64(src_normals, (-1, 3))
+        dim = K.space_dim
+        self._obs_locs = _f64(obs_locs, (-1, dim))
+        self._obs_normals = _f64(obs_normals, (-1, dim))
+        self._src_locs = _f64(src_locs, (-1, dim))
+        self._src_normals = _f64(src_normals, (-1, dim))
         self._src_weights = _f64(src_weights, (-1,))
         opt = _L.TbemGpuOptions()
         _L.lib().tbem_default_options(C.byref(opt))
@@ -246,7 +248,8 @@ class FMMOperator(OperatorI):
         return check(_L.lib().tbem_fmm_n_surface(self._h))
 
     def tree(self, which):
-        """Cells in pre-order (which: 0 source tree, 1 observation tree)."""
+        """Cells in pre-order (which: 0 source tree, 1 observation tree);
+        centers and half widths are [n][3] (z = 0 for a 2D operator)."""
         f = _L.lib().tbem_fmm_tree_cells
         n = check(f(self._h, which, None, None, None, None, None, None))
         out = {k: np.zeros(n, dtype=np.int64) for k in ("level", "index", "n_idx", "n_children")}
@@ -351,10 +354,11 @@ class DirectOperator(OperatorI):
     def __init__(self, K, obs_locs, obs_normals, src_locs, src_normals, src_weights):
         self.K = K
         self.R = K.tensor_dim
-        self._obs_locs = _f64(obs_locs, (-1, 3))
-        self._obs_normals = _f64(obs_normals, (-1, 3))
-        self._src_locs = _f64(src_locs, (-1, 3))
-        self._src_normals = _f64(src_normals, (-1, 3))
+        dim = K.space_dim
+        self._obs_locs = _f64(obs_locs, (-1, dim))
+        self._obs_normals = _f64(obs_normals, (-1, dim))
+        self._src_locs = _f64(src_locs, (-1, dim))
+        self._src_normals = _f64(src_normals, (-1, dim))
         self._src_weights = _f64(src_weights, (-1,))
         self._params = K.params()
 
@@ -384,6 +388,8 @@ def direct_gradients(K, obs_locs, obs_normals, src_locs, src_normals, src_weight
     operator) with respect to every point position, normal and weight and to
     x.  Arrays may be numpy (host) or float64 CUDA tensors; returns the same
     kind, keyed obs_locs, obs_normals, src_locs, src_normals, src_weights, x."""
+    if K.space_dim != 3:
+        raise ValueError("the kernel-gradient pass takes the 3D kernels")
     is_t = torch is not None and isinstance(obs_locs, torch.Tensor)
 
     def prep(a, shape):

@@ -1,7 +1,8 @@
 """tbempy: GPU (sm_103a) BEM operator apply with the reference's Python names.
 
-Submodules: ``ThreeD`` (operators over lib/libtbem_gpu.so), ``meshes``
+Submodules: ``ThreeD`` (operators over lib/libtbem_gpu.so), ``TwoD`` (the
+2D kernels on the same operators), ``meshes``
 (seeded synthetic meshes), ``autograd`` (torch.autograd wrapper), ``solve``
 (GMRES with FP64 iterative refinement).
 """
-from . import ThreeD, meshes  # noqa: F401
+from . import ThreeD, TwoD, meshes  # noqa: F401

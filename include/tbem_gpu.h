@@ -3,13 +3,15 @@
  * Drop-in for the reference's operator interface on the hot path
  * (tbenthompson/3bem):
  *   struct OperatorI { n_rows(); n_cols(); apply(x); clone(); }   cpp/operator.h:14-19
- *   FMMOperator<3,R,C>(Kernel, NBodyData, FMMConfig)              cpp/fmm.h:131-147
+ *   FMMOperator<dim,R,C>(Kernel, NBodyData, FMMConfig)            cpp/fmm.h:131-147
+ *     (dim 3: <3,1,1>, <3,3,3>; dim 2: <2,1,1>, <2,2,2>, cpp/fmm.cpp:651-654)
  *   FMMConfig(mac, order, min_pts_per_cell, d, account_for_small_cells)  cpp/fmm.h:73-96
  *   SparseOperator::apply (CSR SpMV)                              cpp/sparse_operator.cpp:19-28
  *   make_direct_nbody_operator / nbody_eval (direct sum)          cpp/nbody_operator.h:117-152
  *
  * Conventions (those of the reference):
- *   - points are row-major float64 [n][3]; weights float64 [n];
+ *   - points and normals are row-major float64 [n][dim] (dim = 3, or 2 for
+ *     the 2D kernel ids); weights float64 [n];
  *   - densities are component-major per right-hand side: x[r][d][j] =
  *     x[(r*C + d)*n_src + j] (cpp/fmm.cpp:189-190); outputs likewise
  *     y[(r*R + d)*n_obs + i];
@@ -44,6 +46,18 @@ extern "C" {
 #define TBEM_ELASTIC_ADJOINT_TRACTION 4
 #define TBEM_IDENTITY_SCALAR 5
 #define TBEM_ELASTIC_HYPERSINGULAR 6  /* cpp/elastic_kernels.h:314-365 */
+/* 2D kernels (cpp/laplace_kernels.h:66-110, cpp/elastic_kernels.h:21-189,
+ * cpp/identity_kernels.h): points [n][2]; the plain FP64 form only (the
+ * precision form is refused with TBEM_ERR_ARG); the gradient pass and the
+ * allocation-free direct apply take 3D kernels only. */
+#define TBEM_LAPLACE_SINGLE_2D 16          /* log(r) / (2 pi)                 */
+#define TBEM_LAPLACE_DOUBLE_2D 17          /* n_src . d / (2 pi r^2)          */
+#define TBEM_LAPLACE_HYPERSINGULAR_2D 18
+#define TBEM_ELASTIC_DISPLACEMENT_2D 19    /* 2 x 2 tensors from here          */
+#define TBEM_ELASTIC_TRACTION_2D 20
+#define TBEM_ELASTIC_ADJOINT_TRACTION_2D 21
+#define TBEM_ELASTIC_HYPERSINGULAR_2D 22
+#define TBEM_IDENTITY_SCALAR_2D 23
 
 /* precision forms */
 #define TBEM_PRECISION_FP64 0   /* plain: reference surfaces and formulation, FP64 */
@@ -89,8 +103,9 @@ typedef struct TbemFmm TbemFmm;
 /* Fill *opt with defaults (FP64, device 0, threshold 1e-10, auto paths). */
 void tbem_default_options(TbemGpuOptions* opt);
 
-/* Replaces FMMOperator<3,R,C>::FMMOperator(K, NBodyData, FMMConfig)
- * (cpp/fmm.cpp:72-101): builds both octrees, the task lists, the translation
+/* Replaces FMMOperator<dim,R,C>::FMMOperator(K, NBodyData, FMMConfig)
+ * (cpp/fmm.cpp:72-101): builds both octrees (quadtrees for the 2D kernels,
+ * with circle translation surfaces, cpp/fmm.cpp:7-20), the task lists, the translation
  * surfaces and the per-level check-to-equivalent operators, and uploads
  * everything to the device.  kernel_params = {shear_modulus, poisson_ratio}
  * for the elastic kernels (may be NULL for the scalar ones). */
@@ -123,8 +138,9 @@ void tbem_fmm_destroy(TbemFmm* h);
 /* Introspection for bit-exact checks against the reference octree
  * (cpp/octree.h:14-25) and task lists (FMMTasks, cpp/fmm.h:98-120).
  * which: 0 = source tree, 1 = observation tree.  Cells are reported in
- * pre-order with the reference's post-order `index`; any output pointer may
- * be NULL; returns the number of cells (or a negative status). */
+ * pre-order with the reference's post-order `index`; center and half_width
+ * are [n][3] (z = 0 for a 2D operator); any output pointer may be NULL;
+ * returns the number of cells (or a negative status). */
 long tbem_fmm_tree_cells(const TbemFmm* h, int which, long* level, long* index,
                          double* center, double* half_width, long* n_points,
                          long* n_children);

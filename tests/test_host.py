@@ -32,9 +32,9 @@ def test_library_exports_every_declared_symbol():
     assert sorted(_lib.SIGNATURES) == names
 
 
-def kernel_from_name(name):
-    from tbempy import ThreeD
-    k = getattr(ThreeD, name)
+def kernel_from_name(name, dim=3):
+    from tbempy import ThreeD, TwoD
+    k = getattr(TwoD if dim == 2 else ThreeD, name)
     return k(1.0, 0.25) if name.startswith("Elastic") else k()
 
 
@@ -44,8 +44,10 @@ def test_host_tree_and_lists_match_reference(path):
     g = dict(np.load(path))
     cfg = ThreeD.FMMConfig(float(g["mac"]), int(g["order"]), int(g["leaf"]), float(g["d"]),
                            bool(g["small"]))
-    op = ThreeD.FMMOperator(kernel_from_name(str(g["kernel"])), g["obs_locs"], g["obs_normals"],
-                            g["src_locs"], g["src_normals"], g["src_weights"], cfg, host_only=True)
+    dim = g["src_locs"].shape[1]
+    op = ThreeD.FMMOperator(kernel_from_name(str(g["kernel"]), dim), g["obs_locs"],
+                            g["obs_normals"], g["src_locs"], g["src_normals"], g["src_weights"],
+                            cfg, host_only=True)
     assert op.n_surface() == int(g["n_surf"])
     for which in (0, 1):
         t = op.tree(which)
@@ -112,6 +114,49 @@ def test_argument_errors_are_status_codes():
     with pytest.raises(TbemError) as e:
         op.apply(np.ones(10))
     assert e.value.code == -4
+
+
+def test_2d_operators_build_quadtrees_and_refuse_the_precision_form():
+    """2D kernels: quadtrees over x and y with the reference's lists (checked
+    against the oracle, itself pinned to the reference), n_rows = R n_obs,
+    empty and coincident inputs, and the precision form refused with a
+    status (it rests on the 3D kernels' homogeneity)."""
+    from oracle import oracle
+    from tbempy import ThreeD, TwoD
+    from tbempy._lib import TbemError
+    rng = np.random.default_rng(9)
+    src, obs = rng.uniform(-1, 1, (900, 2)), rng.uniform(-1, 1, (500, 2)) * 0.7
+    ns = rng.normal(size=(900, 2))
+    no = rng.normal(size=(500, 2))
+    w = rng.uniform(0.5, 1, 900)
+    for small in (False, True):
+        cfg = ThreeD.FMMConfig(0.3, 16, 12, 0.05, small)
+        for K in (TwoD.LaplaceHypersingular(), TwoD.ElasticTraction(1.0, 0.25)):
+            op = TwoD.FMMOperator(K, obs, no, src, ns, w, cfg, host_only=True)
+            assert op.n_rows() == K.tensor_dim * 500 and op.n_cols() == K.tensor_dim * 900
+            assert op.n_surface() == 16
+            orc = oracle.OracleFMM(K.kernel_id, obs, no, src, ns, w, 0.3, 16, 12, 0.05, small)
+            for which in (0, 1):
+                t, u = op.tree(which), orc.tree(which)
+                assert t["n_children"].max() <= 4
+                for k in ("level", "index", "center", "hw", "n_idx", "n_children"):
+                    assert np.array_equal(t[k], u[k]), k
+            for kind in LISTS:
+                for a, b in zip(op.list(kind), orc.list(kind)):
+                    assert np.array_equal(a, b), kind
+    e = np.zeros((0, 2))
+    op = TwoD.FMMOperator(TwoD.LaplaceSingle(), e, e, e, e, np.zeros(0),
+                          ThreeD.FMMConfig(0.3, 8, 10, 0.05, False), host_only=True)
+    assert op.n_rows() == 0
+    same = np.array([[1.0, 2.0], [1.0, 2.0], [0.0, 0.0]])
+    op = TwoD.FMMOperator(TwoD.LaplaceSingle(), same, same, same, same, np.ones(3),
+                          ThreeD.FMMConfig(0.3, 8, 1, 0.05, False), host_only=True)
+    assert op.tree(0)["n_idx"][0] == 3
+    with pytest.raises(TbemError) as err:
+        TwoD.FMMOperator(TwoD.LaplaceSingle(), src, ns, src, ns, w,
+                         ThreeD.FMMConfig(0.3, 16, 12, 0.05, False), precision="mixed",
+                         host_only=True)
+    assert err.value.code == -1 and "2D" in str(err.value)
 
 
 def test_csr_create_validates():
