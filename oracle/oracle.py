@@ -206,6 +206,33 @@ class OracleFMM(_FMMBase):
                 setf(self.h, which, lev, _ptr(P))
         self._apply = L.fn("apply", None, [_P, _P, _P, _I, _D])
 
+    def c2e_system(self, which, level):
+        """The (R n_s) x (C n_s) system whose pseudo-inverse is the operator."""
+        n = self.n_surf() * self.R
+        A = np.zeros((n, n))
+        self.L.fn("c2e_system", _L, [_P, _I, _L, _P])(self.h, which, level, _ptr(A))
+        return A
+
+    def ulp_floor(self, x, seed=0):
+        """Relative change of this apply when every check-to-equivalent system
+        is perturbed by one ulp (relative 2^-52 of each entry, random sign)
+        before its pseudo-inverse: the agreement two correct FP64 evaluations
+        of the plain form can be expected to reach (its pseudo-inverses keep
+        singular values down to 1e-10 of the largest)."""
+        y0 = self.apply(x)
+        saved = {w: list(self.c2e[w]) for w in (0, 1)}
+        rng = np.random.default_rng(seed)
+        for which in (0, 1):
+            for lev in range(len(saved[which])):
+                A = self.c2e_system(which, lev)
+                A = A * (1 + 2.0 ** -52 * rng.choice([-1.0, 1.0], size=A.shape))
+                self.set_c2e(which, lev, pinv_reference(A))
+        y1 = self.apply(x)
+        for which in (0, 1):
+            for lev, op in enumerate(saved[which]):
+                self.set_c2e(which, lev, op)
+        return float(np.linalg.norm(y1 - y0) / max(np.linalg.norm(y0), 1e-300))
+
     def set_c2e(self, which, level, op):
         """Install a check-to-equivalent operator (e.g. the reference's own)."""
         op = _f64(op)
