@@ -232,6 +232,32 @@ int tbem_csr_apply(TbemCsr* h, const double* x, double* y, int n_rhs, void* stre
 
 long tbem_csr_nnz(const TbemCsr* h) { return h ? h->nnz : TBEM_ERR_ARG; }
 
+int tbem_csr_shape(const TbemCsr* h, long* n_rows, long* n_cols)
+{
+    if (!h) return TBEM_ERR_ARG;
+    if (n_rows) *n_rows = h->n_rows;
+    if (n_cols) *n_cols = h->n_cols;
+    return TBEM_OK;
+}
+
+int tbem_csr_download(const TbemCsr* h, double* values, long* column_indices, long* row_ptrs)
+{
+    using namespace tbem;
+    if (!h) return TBEM_ERR_ARG;
+    try {
+        if (row_ptrs)
+            TBEM_CK(cudaMemcpy(row_ptrs, h->rowptr.p, sizeof(long) * (h->n_rows + 1), cudaMemcpyDeviceToHost));
+        if (h->nnz > 0 && values)
+            TBEM_CK(cudaMemcpy(values, h->val.p, sizeof(double) * h->nnz, cudaMemcpyDeviceToHost));
+        if (h->nnz > 0 && column_indices)
+            TBEM_CK(cudaMemcpy(column_indices, h->col.p, sizeof(long) * h->nnz, cudaMemcpyDeviceToHost));
+        return TBEM_OK;
+    } catch (const tbem::Error& e) {
+        tbem::set_last_error(e.what());
+        return e.code;
+    }
+}
+
 void tbem_csr_destroy(TbemCsr* h) { delete h; }
 
 

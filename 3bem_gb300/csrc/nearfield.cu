@@ -1,0 +1,543 @@
+// Nearfield / farfield-correction matrix construction on the GPU.
+//
+// The reference builds these sparse matrices term by term on the host
+// (make_nearfield_operator / make_farfield_correction_operator,
+// cpp/nearfield_operator.h:48-117): for every Galerkin observation point and
+// every source facet near it, IntegrationStrategy::compute_term
+// (cpp/integral_term.cpp:33-92) integrates the kernel times the facet's
+// linear basis by one of three rules -- a fixed Gauss rule far away, a
+// sinh-transformed Gauss rule nearby (SinhIntegrator,
+// cpp/integral_term.cpp:155-203, with the transforms of cpp/gauss_quad.cpp:
+// 54-90 and cpp/sinh_quad.cpp), and, for observation points on the surface,
+// Richardson extrapolation (cpp/richardson.h) of nearby integrals taken at
+// points stepped back along the limit direction.
+//
+// Here the host finds the terms (nearfield_host.cpp) and the GPU integrates
+// them: one warp per term, the lanes striding over the term's quadrature
+// points (every node generated on the fly from a table of Gauss rules) and
+// meeting in a butterfly reduction; each Richardson step is reduced before
+// the next, and lane e extrapolates entry e.  The values come back to the
+// host, which lays them out as the reference's COO entries and compresses
+// them to CSR (csr_from_coo's stable row order).
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "handle.h"
+#include "nearfield.h"
+
+namespace tbem {
+namespace {
+
+constexpr int NF_GMAX = 512;  // largest Gauss rule the device table holds
+constexpr int NF_WARPS = 4;   // terms per CTA
+
+struct NfArgs {
+    int kid;
+    KParams kp;
+    int mode;  // 0: compute_term; 1: -compute_farfield (the farfield correction)
+    int sinh_order;
+    int n_steps;
+    double far_threshold;
+    const double* gx;  // Gauss rule n (n = 1..NF_GMAX) at offset n (n - 1) / 2
+    const double* gw;
+    const double* fx;  // source farfield rule: [n_far][2] reference points
+    const double* fw;
+    int n_far;
+    const double* loc;  // observation points [n][3]
+    const double* nrm;
+    const double* dir;  // Richardson directions
+    const double* fac;  // source facets [n][3 corners][3]
+    const double* ls;   // length scale
+    const double* jac;  // jacobian
+    const double* fn;   // facet normal [n][3]
+    const int* t_obs;
+    const int* t_fac;
+    long n_terms;
+    double* out;  // [n_terms][dim][R][C]
+    int* err;     // bit 1: a point on a facet without a limit direction; bit 2: rule too large
+};
+
+__device__ __forceinline__ double gnode(const NfArgs& a, int n, int i) { return a.gx[n * (n - 1) / 2 + i]; }
+__device__ __forceinline__ double gweight(const NfArgs& a, int n, int i) { return a.gw[n * (n - 1) / 2 + i]; }
+
+struct DClosest {
+    double ref0, ref1, dist;
+};
+
+// nf::closest_point on the device, formula for formula.
+template <int DIM>
+__device__ DClosest d_closest(const double* p, const double* c)
+{
+    DClosest r{0.0, 0.0, 0.0};
+    if (DIM == 2) {
+        const double dx = c[3] - c[0], dy = c[4] - c[1];
+        const double L2 = dx * dx + dy * dy;
+        double t = 0.0;
+        if (L2 > 0.0) {
+            t = ((p[0] - c[0]) * dx + (p[1] - c[1]) * dy) / L2;
+            t = fmin(1.0, fmax(0.0, t));
+        }
+        double qx, qy;
+        if (t == 1.0) { qx = c[3]; qy = c[4]; }
+        else if (t == 0.0) { qx = c[0]; qy = c[1]; }
+        else { qx = c[0] + dx * t; qy = c[1] + dy * t; }
+        r.ref0 = 2 * t - 1;
+        r.dist = sqrt((p[0] - qx) * (p[0] - qx) + (p[1] - qy) * (p[1] - qy));
+        return r;
+    }
+    double ab[3], ac[3], ap[3], bp[3], cp[3];
+    for (int d = 0; d < 3; d++) {
+        ab[d] = c[3 + d] - c[d];
+        ac[d] = c[6 + d] - c[d];
+        ap[d] = p[d] - c[d];
+        bp[d] = p[d] - c[3 + d];
+        cp[d] = p[d] - c[6 + d];
+    }
+    auto dot = [](const double* u, const double* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
+    const double d1 = dot(ab, ap), d2 = dot(ac, ap), d3 = dot(ab, bp), d4 = dot(ac, bp);
+    const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    const double vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+    double v = 0.0, w = 0.0, q[3];
+    if (d1 <= 0.0 && d2 <= 0.0) {
+        for (int d = 0; d < 3; d++) q[d] = c[d];
+    } else if (d3 >= 0.0 && d4 <= d3) {
+        v = 1.0;
+        for (int d = 0; d < 3; d++) q[d] = c[3 + d];
+    } else if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+        v = d1 / (d1 - d3);
+        for (int d = 0; d < 3; d++) q[d] = c[d] + ab[d] * v;
+    } else if (d6 >= 0.0 && d5 <= d6) {
+        w = 1.0;
+        for (int d = 0; d < 3; d++) q[d] = c[6 + d];
+    } else if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+        w = d2 / (d2 - d6);
+        for (int d = 0; d < 3; d++) q[d] = c[d] + ac[d] * w;
+    } else if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0) {
+        w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        v = 1.0 - w;
+        for (int d = 0; d < 3; d++) q[d] = c[3 + d] + (c[6 + d] - c[3 + d]) * w;
+    } else {
+        const double inv = 1.0 / (va + vb + vc);
+        v = vb * inv;
+        w = vc * inv;
+        for (int d = 0; d < 3; d++) q[d] = c[d] + ab[d] * v + ac[d] * w;
+    }
+    r.ref0 = v;
+    r.ref1 = w;
+    r.dist = sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) +
+                  (p[2] - q[2]) * (p[2] - q[2]));
+    return r;
+}
+
+// One source quadrature point's influence (IntegralTerm::eval_point_influence,
+// cpp/integral_term.cpp:11-20): basis (x) K(obs, y(x_hat)) * jacobian * w.
+template <int DIM, int R>
+__device__ __forceinline__ void influence(const NfArgs& a, int f, const double* p, const double* pn,
+                                          double xh0, double xh1, double w, double* acc)
+{
+    const double* c = a.fac + 9 * f;
+    double y[3], bas[3];
+    if (DIM == 2) {
+        bas[0] = 0.5 - 0.5 * xh0;
+        bas[1] = 0.5 + 0.5 * xh0;
+        y[0] = bas[0] * c[0] + bas[1] * c[3];
+        y[1] = bas[0] * c[1] + bas[1] * c[4];
+        y[2] = 0.0;
+    } else {
+        bas[0] = 1 - xh0 - xh1;
+        bas[1] = xh0;
+        bas[2] = xh1;
+        for (int d = 0; d < 3; d++) y[d] = bas[0] * c[d] + bas[1] * c[3 + d] + bas[2] * c[6 + d];
+    }
+    double K[9];
+    const double* n = a.fn + 3 * f;
+    kernel_tensor_any<double>(a.kid, y[0] - p[0], y[1] - p[1], y[2] - p[2], pn[0], pn[1], pn[2], n[0],
+                              n[1], n[2], a.kp, K);
+    const double J = a.jac[f];
+#pragma unroll
+    for (int b = 0; b < DIM; b++)
+#pragma unroll
+        for (int k = 0; k < R * R; k++) acc[b * R * R + k] += bas[b] * (K[k] * J) * w;
+}
+
+// The sinh-transformed rule around the closest point (choose_sinh_quad +
+// sinh_transform / sinh_sigmoidal_transform), this lane's share.  Returns
+// false (and flags) when the point lies on the facet or the rule is too big.
+template <int DIM, int R>
+__device__ bool sinh_near(const NfArgs& a, int f, const double* p, const double* pn, double* acc)
+{
+    const int lane = threadIdx.x & 31;
+    const DClosest cp = d_closest<DIM>(p, a.fac + 9 * f);
+    const double l = cp.dist, S = a.ls[f];
+    if (!(l > 0.0)) {
+        if (lane == 0) atomicOr(a.err, 1);
+        return false;
+    }
+    const double scaled = l / S;
+    int n = (int)(a.sinh_order + (a.sinh_order * (-log(scaled))));
+    n = max(n, a.sinh_order);
+    if ((DIM == 3 ? 2 * n : n) > NF_GMAX) {
+        if (lane == 0) atomicOr(a.err, 2);
+        return false;
+    }
+    const double sa = DIM == 3 ? -1.0 : cp.ref0, b = scaled;
+    const double mu0 = 0.5 * (asinh((1.0 + sa) / b) + asinh((1.0 - sa) / b));
+    const double eta0 = 0.5 * (asinh((1.0 + sa) / b) - asinh((1.0 - sa) / b));
+    if (DIM == 2) {
+        for (int q = lane; q < n; q += 32) {
+            const double s = gnode(a, n, q);
+            const double x = sa + b * sinh(mu0 * s - eta0);
+            const double jw = b * mu0 * cosh(mu0 * s - eta0);
+            influence<DIM, R>(a, f, p, pn, x, 0.0, gweight(a, n, q) * jw, acc);
+        }
+        return true;
+    }
+    // three sub-triangles around the singular point (x0, y0): {sp, p0, p2},
+    // {sp, p2, p1}, {sp, p0, p1} with p0 = (0,0), p1 = (1,0), p2 = (0,1)
+    const double x0 = cp.ref0, y0 = cp.ref1;
+    const double tx[3][3] = {{x0, 0.0, 0.0}, {x0, 0.0, 1.0}, {x0, 0.0, 1.0}};
+    const double ty[3][3] = {{y0, 0.0, 1.0}, {y0, 1.0, 0.0}, {y0, 0.0, 0.0}};
+    double tj[3];
+#pragma unroll
+    for (int t = 0; t < 3; t++) {  // 2 * tri_area = |cross(c2 - c0, c2 - c1)_z|
+        const double ux = tx[t][2] - tx[t][0], uy = ty[t][2] - ty[t][0];
+        const double vx = tx[t][2] - tx[t][1], vy = ty[t][2] - ty[t][1];
+        tj[t] = 2.0 * (0.5 * fabs(ux * vy - uy * vx));
+    }
+    const int nt = 2 * n, per = nt * n;
+    const double hp = M_PI / 2.0, s45 = sin(M_PI / 4.0);
+    for (int q = lane; q < 3 * per; q += 32) {
+        const int t = q / per, rem = q - t * per, i = rem / n, j = rem - i * n;
+        const double u = gnode(a, nt, i);
+        const double sigma = (u + 1.0) / 2.0;
+        const double s2 = sigma * sigma, c2 = (1 - sigma) * (1 - sigma);
+        const double theta = s2 / (s2 + c2) * hp;
+        const double theta_j = hp * sigma * (1 - sigma) / ((s2 + c2) * (s2 + c2));
+        const double Rt = s45 / sin(theta + M_PI / 4.0);
+        const double s = gnode(a, n, j);
+        const double xs = sa + b * sinh(mu0 * s - eta0);
+        const double ws = gweight(a, n, j) * (b * mu0 * cosh(mu0 * s - eta0));
+        const double r = Rt * (xs + 1.0) / 2.0;
+        const double rj = r * (Rt / 2.0);
+        const double w = theta_j * rj * ws * gweight(a, nt, i);
+        const double ux = r * cos(theta), uy = r * sin(theta);
+        const double b0 = 1 - ux - uy;
+        const double px = b0 * tx[t][0] + ux * tx[t][1] + uy * tx[t][2];
+        const double py = b0 * ty[t][0] + ux * ty[t][1] + uy * ty[t][2];
+        influence<DIM, R>(a, f, p, pn, px, py, w * tj[t], acc);
+    }
+    return true;
+}
+
+template <int E>
+__device__ __forceinline__ void warp_sum(double* acc)
+{
+#pragma unroll
+    for (int e = 0; e < E; e++)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc[e] += __shfl_xor_sync(0xffffffffu, acc[e], off);
+}
+
+template <int DIM, int R>
+__global__ void __launch_bounds__(32 * NF_WARPS) nearfield_kernel(const NfArgs a)
+{
+    constexpr int E = DIM * R * R;
+    const long t = (long)blockIdx.x * NF_WARPS + threadIdx.x / 32;
+    if (t >= a.n_terms) return;  // whole warps leave together
+    const int lane = threadIdx.x & 31;
+    const int o = a.t_obs[t], f = a.t_fac[t];
+    const double* p = a.loc + 3 * o;
+    const double* pn = a.nrm + 3 * o;
+    const double* dir = a.dir + 3 * o;
+    double acc[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) acc[e] = 0.0;
+    double result = 0.0;  // entry `lane` of the term (lanes < E)
+
+    const double ls = a.ls[f];
+    const DClosest cp = d_closest<DIM>(p, a.fac + 9 * f);
+    const bool near = a.mode == 0 && cp.dist < a.far_threshold * ls;
+    double d2 = 0.0;
+    for (int d = 0; d < DIM; d++) d2 += dir[d] * dir[d];
+    const bool singular = near && cp.dist < 1.0 * ls && d2 > 1e-10 * ls;
+    if (singular) {
+        // Richardson extrapolation over points stepped back along the limit
+        // direction, steps 1, 1/2, 1/4, ... (make_singular_steps, get_step_loc)
+        double vals[32];
+        for (int k = 0; k < a.n_steps; k++) {
+            const double step = 1.0 / pow(2.0, (double)k);
+            const double ps[3] = {p[0] + (1.0 * step) * dir[0], p[1] + (1.0 * step) * dir[1],
+                                  p[2] + (1.0 * step) * dir[2]};
+#pragma unroll
+            for (int e = 0; e < E; e++) acc[e] = 0.0;
+            sinh_near<DIM, R>(a, f, ps, pn, acc);
+            warp_sum<E>(acc);
+            double mine = 0.0;
+#pragma unroll
+            for (int e = 0; e < E; e++)
+                if (e == lane) mine = acc[e];
+            vals[k] = mine;
+        }
+        // richardson_limit(2, steps) (cpp/richardson.h:10-34)
+        for (int m = 1; m < a.n_steps; m++) {
+            const double mult = pow(2.0, (double)m);
+            const double factor = 1.0 / (mult - 1.0);
+            for (int i = 0; i < a.n_steps - m; i++) vals[i] = factor * (mult * vals[i + 1] - vals[i]);
+        }
+        result = vals[0];
+    } else {
+        if (near) {
+            sinh_near<DIM, R>(a, f, p, pn, acc);
+        } else {
+            for (int q = lane; q < a.n_far; q += 32)
+                influence<DIM, R>(a, f, p, pn, a.fx[2 * q], a.fx[2 * q + 1], a.fw[q], acc);
+        }
+        warp_sum<E>(acc);
+#pragma unroll
+        for (int e = 0; e < E; e++)
+            if (e == lane) result = acc[e];
+        if (a.mode == 1) result = -result;
+    }
+    if (lane < E) a.out[t * E + lane] = result;
+}
+
+// Gauss rules 1..NF_GMAX, computed once per process.
+const std::vector<double>& gauss_table(int which)
+{
+    static std::vector<double> x, w;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        x.reserve((size_t)NF_GMAX * (NF_GMAX + 1) / 2);
+        w.reserve(x.capacity());
+        std::vector<double> gx, gw;
+        for (int n = 1; n <= NF_GMAX; n++) {
+            nf::gauss_rule(n, gx, gw);
+            x.insert(x.end(), gx.begin(), gx.end());
+            w.insert(w.end(), gw.begin(), gw.end());
+        }
+    });
+    return which == 0 ? x : w;
+}
+
+std::vector<nf::Facet> read_facets(const double* verts, long n_verts, const long* idx, long n, int dim)
+{
+    std::vector<nf::Facet> out((size_t)n);
+    for (long i = 0; i < n; i++) {
+        nf::Facet f{};
+        for (int v = 0; v < dim; v++) {
+            const long k = idx[dim * i + v];
+            if (k < 0 || k >= n_verts) throw Error(TBEM_ERR_ARG, "facet vertex index out of range");
+            for (int d = 0; d < dim; d++) f.c[v][d] = verts[dim * k + d];
+        }
+        out[i] = f;
+    }
+    return out;
+}
+
+template <int DIM, int R>
+void launch(const NfArgs& a)
+{
+    const long blocks = (a.n_terms + NF_WARPS - 1) / NF_WARPS;
+    nearfield_kernel<DIM, R><<<(unsigned)blocks, 32 * NF_WARPS>>>(a);
+    TBEM_CK(cudaGetLastError());
+}
+
+}  // namespace
+}  // namespace tbem
+
+extern "C" {
+
+long tbem_gauss_facet(int dim, long n, double* x, double* w)
+{
+    if ((dim != 2 && dim != 3) || n <= 0 || n > 4096) return TBEM_ERR_ARG;
+    std::vector<double> qx, qw;
+    tbem::nf::gauss_facet(dim, (int)n, qx, qw);
+    if (x)
+        for (size_t i = 0; i < qw.size(); i++) {
+            x[(dim - 1) * i] = qx[2 * i];
+            if (dim == 3) x[2 * i + 1] = qx[2 * i + 1];
+        }
+    if (w) std::copy(qw.begin(), qw.end(), w);
+    return (long)qw.size();
+}
+
+long tbem_galerkin_obs_points(int dim, const double* vertices, long n_vertices,
+                              const long* obs_facets, long n_obs_facets, const long* all_facets,
+                              long n_all_facets, long order, double* locs, double* normals,
+                              double* dirs)
+{
+    using namespace tbem;
+    try {
+        if ((dim != 2 && dim != 3) || order <= 0 || n_vertices < 0 || n_obs_facets < 0 || n_all_facets < 0)
+            throw Error(TBEM_ERR_ARG, "bad argument");
+        const auto obs = read_facets(vertices, n_vertices, obs_facets, n_obs_facets, dim);
+        const auto all = read_facets(vertices, n_vertices, all_facets, n_all_facets, dim);
+        nf::FacetSet all_set(all, dim);
+        const nf::ObsPoints pts = nf::galerkin_obs_points(obs, all_set, (int)order, dim);
+        for (size_t i = 0; i < pts.loc.size(); i++)
+            for (int d = 0; d < dim; d++) {
+                if (locs) locs[dim * i + d] = pts.loc[i][d];
+                if (normals) normals[dim * i + d] = pts.normal[i][d];
+                if (dirs) dirs[dim * i + d] = pts.dir[i][d];
+            }
+        return (long)pts.loc.size();
+    } catch (const tbem::Error& e) {
+        tbem::set_last_error(e.what());
+        return e.code;
+    }
+}
+
+int tbem_nearfield_create(int kernel, const double* kernel_params, const double* vertices,
+                          long n_vertices, const long* obs_facets, long n_obs_facets,
+                          const long* src_facets, long n_src_facets, const long* all_facets,
+                          long n_all_facets, const TbemSinhIntegrator* mthd, int which,
+                          TbemCsr** out)
+{
+    using namespace tbem;
+    if (!out || !mthd) return TBEM_ERR_ARG;
+    *out = nullptr;
+    try {
+        if (!kernel_valid(kernel)) throw Error(TBEM_ERR_ARG, "unknown kernel id");
+        if (which != 0 && which != 1) throw Error(TBEM_ERR_ARG, "which must be 0 or 1");
+        if (n_vertices < 0 || n_obs_facets < 0 || n_src_facets < 0 || n_all_facets < 0)
+            throw Error(TBEM_ERR_ARG, "negative count");
+        if (mthd->sinh_order <= 0 || mthd->obs_near_order <= 0 || mthd->obs_far_order <= 0 ||
+            mthd->src_far_order <= 0 || mthd->n_singular_steps < 2 || mthd->n_singular_steps > 32 ||
+            !(mthd->far_threshold > 0))
+            throw Error(TBEM_ERR_ARG, "bad integrator parameters");
+        const int dim = kernel_space_dim(kernel), R = kernel_dim(kernel);
+        const double mu = (kernel_params && R > 1) ? kernel_params[0] : 1.0;
+        const double nu = (kernel_params && R > 1) ? kernel_params[1] : 0.25;
+        const auto obs = read_facets(vertices, n_vertices, obs_facets, n_obs_facets, dim);
+        const auto src = read_facets(vertices, n_vertices, src_facets, n_src_facets, dim);
+        const auto all = read_facets(vertices, n_vertices, all_facets, n_all_facets, dim);
+        nf::FacetSet all_set(all, dim), src_set(src, dim);
+        const int order = (int)(which == 0 ? mthd->obs_near_order : mthd->obs_far_order);
+        const nf::ObsPoints pts = nf::galerkin_obs_points(obs, all_set, order, dim);
+        const long n_pts = (long)pts.loc.size();
+
+        // terms: every observation point against its nearfield source facets,
+        // in the reference's loop order
+        std::vector<int> t_obs, t_fac;
+        std::vector<size_t> nearby;
+        size_t nearest = 0;
+        double dist = 0.0;
+        for (long i = 0; i < n_pts; i++) {
+            src_set.find(pts.loc[i], mthd->far_threshold, nearby, nearest, dist);
+            for (size_t f : nearby) {
+                t_obs.push_back((int)i);
+                t_fac.push_back((int)f);
+            }
+        }
+        const long n_terms = (long)t_obs.size();
+        const int E = dim * R * R;
+        std::vector<double> vals((size_t)n_terms * E);
+        if (n_terms > 0) {
+            std::vector<double> loc, nrm, dir, fac, ls, jac, fn;
+            for (long i = 0; i < n_pts; i++)
+                for (int d = 0; d < 3; d++) {
+                    loc.push_back(pts.loc[i][d]);
+                    nrm.push_back(pts.normal[i][d]);
+                    dir.push_back(pts.dir[i][d]);
+                }
+            for (size_t f = 0; f < src.size(); f++) {
+                for (int v = 0; v < 3; v++)
+                    for (int d = 0; d < 3; d++) fac.push_back(src[f].c[v][d]);
+                const nf::FacetInfo& fi = src_set.info(f);
+                ls.push_back(fi.length_scale);
+                jac.push_back(fi.jacobian);
+                for (int d = 0; d < 3; d++) fn.push_back(fi.normal[d]);
+            }
+            std::vector<double> fx, fw;
+            nf::gauss_facet(dim, (int)mthd->src_far_order, fx, fw);
+            DBuf<double> d_gx, d_gw, d_fx, d_fw, d_loc, d_nrm, d_dir, d_fac, d_ls, d_jac, d_fn, d_out;
+            DBuf<int> d_to, d_tf, d_err;
+            d_gx.upload(gauss_table(0));
+            d_gw.upload(gauss_table(1));
+            d_fx.upload(fx);
+            d_fw.upload(fw);
+            d_loc.upload(loc);
+            d_nrm.upload(nrm);
+            d_dir.upload(dir);
+            d_fac.upload(fac);
+            d_ls.upload(ls);
+            d_jac.upload(jac);
+            d_fn.upload(fn);
+            d_to.upload(t_obs);
+            d_tf.upload(t_fac);
+            d_err.upload(std::vector<int>(1, 0));
+            d_out.alloc(vals.size());
+            NfArgs a{};
+            a.kid = kernel;
+            a.kp = make_kparams(kernel, mu, nu);
+            a.mode = which;
+            a.sinh_order = (int)mthd->sinh_order;
+            a.n_steps = (int)mthd->n_singular_steps;
+            a.far_threshold = mthd->far_threshold;
+            a.gx = d_gx.p;
+            a.gw = d_gw.p;
+            a.fx = d_fx.p;
+            a.fw = d_fw.p;
+            a.n_far = (int)fw.size();
+            a.loc = d_loc.p;
+            a.nrm = d_nrm.p;
+            a.dir = d_dir.p;
+            a.fac = d_fac.p;
+            a.ls = d_ls.p;
+            a.jac = d_jac.p;
+            a.fn = d_fn.p;
+            a.t_obs = d_to.p;
+            a.t_fac = d_tf.p;
+            a.n_terms = n_terms;
+            a.out = d_out.p;
+            a.err = d_err.p;
+            if (dim == 2 && R == 1) launch<2, 1>(a);
+            else if (dim == 2) launch<2, 2>(a);
+            else if (R == 1) launch<3, 1>(a);
+            else launch<3, 3>(a);
+            TBEM_CK(cudaDeviceSynchronize());
+            int err = 0;
+            TBEM_CK(cudaMemcpy(&err, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (err & 1)
+                throw Error(TBEM_ERR_ARG, "an observation point lies on a source facet without a "
+                                          "limit direction (the reference asserts here)");
+            if (err & 2)
+                throw Error(TBEM_ERR_ARG, "a sinh rule needs more than 512 Gauss points "
+                                          "(observation point too close to a facet)");
+            TBEM_CK(cudaMemcpy(vals.data(), d_out.p, vals.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost));
+        }
+        // COO entries in the reference's order (cpp/nearfield_operator.h:59-84),
+        // rows d1 * n_pts + point, columns d2 * n_dofs + facet * dim + basis;
+        // a stable sort by row gives csr_from_coo's layout
+        const long n_dofs = (long)src.size() * dim;
+        const long n_rows = R * n_pts, n_cols = R * n_dofs;
+        std::vector<long> count(n_rows + 1, 0);
+        for (long t = 0; t < n_terms; t++)
+            for (int d1 = 0; d1 < R; d1++) count[d1 * n_pts + t_obs[t] + 1] += dim * R;
+        for (long r = 0; r < n_rows; r++) count[r + 1] += count[r];
+        std::vector<long> fill(count.begin(), count.end() - 1), cols(count[n_rows]);
+        std::vector<double> v(count[n_rows]);
+        for (long t = 0; t < n_terms; t++)
+            for (int b = 0; b < dim; b++)
+                for (int d1 = 0; d1 < R; d1++)
+                    for (int d2 = 0; d2 < R; d2++) {
+                        const long row = d1 * n_pts + t_obs[t];
+                        const long k = fill[row]++;
+                        cols[k] = d2 * n_dofs + (long)t_fac[t] * dim + b;
+                        v[k] = vals[(size_t)t * E + (b * R + d1) * R + d2];
+                    }
+        return tbem_csr_create(n_rows, n_cols, v.data(), cols.data(), count.data(), out);
+    } catch (const tbem::Error& e) {
+        tbem::set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        tbem::set_last_error("host allocation failed");
+        return TBEM_ERR_ALLOC;
+    }
+}
+
+}  // extern "C"

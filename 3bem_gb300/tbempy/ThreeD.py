@@ -432,6 +432,22 @@ class SparseOperator(OperatorI):
                                        _ptr(self._cols), _ptr(self._rows), C.byref(h)))
         self._h = h
 
+    @classmethod
+    def _from_handle(cls, h):
+        """Wrap a CSR operator the library built (its arrays read back once)."""
+        self = cls.__new__(cls)
+        L = _L.lib()
+        nr, nc = C.c_long(), C.c_long()
+        check(L.tbem_csr_shape(h, C.byref(nr), C.byref(nc)))
+        nnz = check(L.tbem_csr_nnz(h))
+        self._shape = (nr.value, nc.value)
+        self._values = np.zeros(nnz)
+        self._cols = np.zeros(nnz, dtype=np.int64)
+        self._rows = np.zeros(nr.value + 1, dtype=np.int64)
+        check(L.tbem_csr_download(h, _ptr(self._values), _ptr(self._cols), _ptr(self._rows)))
+        self._h = h
+        return self
+
     @staticmethod
     def csr_from_coo(n_rows, n_cols, rows, cols, values):
         """csr_from_coo (cpp/sparse_operator.cpp:140-172): entries keep their
@@ -532,3 +548,11 @@ class IntegralOperator(OperatorI):
     def clone(self):
         return IntegralOperator(self.nearfield.clone(), self.farfield_correction.clone(),
                                 self.galerkin.clone(), self.farfield.clone(), self.interp.clone())
+
+
+# boundary-operator assembly (nearfield / correction matrices on the GPU,
+# Galerkin and interpolation operators, boundary_operator)
+from .bem import (Mesh, IntegrationStrategy, boundary_operator, farfield_correction_operator,  # noqa: E402,F401
+                  galerkin_obs_points, galerkin_operator, gauss_facet, interpolation_operator,
+                  make_adaptive_integrator, make_sinh_integrator, nearfield_operator,
+                  quadrature_points)

@@ -11,7 +11,11 @@ operators run in the plain FP64 form.
 import numpy as np
 
 from .ThreeD import (DirectOperator, FMMConfig, FMMGraph, FMMOperator,  # noqa: F401
-                     IntegralOperator, Kernel, OperatorI, SparseOperator)
+                     IntegralOperator, IntegrationStrategy, Kernel, Mesh, OperatorI,
+                     SparseOperator, boundary_operator, farfield_correction_operator,
+                     galerkin_obs_points, galerkin_operator, gauss_facet,
+                     interpolation_operator, make_adaptive_integrator, make_sinh_integrator,
+                     nearfield_operator, quadrature_points)
 
 
 class _Kernel2D(Kernel):

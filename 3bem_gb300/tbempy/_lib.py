@@ -27,6 +27,12 @@ class TbemGpuOptions(C.Structure):
                 ("m2l_rank_tol", C.c_double), ("p2m_block", C.c_int), ("tc_shape", C.c_int)]
 
 
+class TbemSinhIntegrator(C.Structure):
+    _fields_ = [("sinh_order", C.c_long), ("obs_near_order", C.c_long),
+                ("obs_far_order", C.c_long), ("src_far_order", C.c_long),
+                ("n_singular_steps", C.c_long), ("far_threshold", C.c_double)]
+
+
 class TbemError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s (%d): %s" % (ERRORS.get(code, "error"), code, msg))
@@ -68,6 +74,11 @@ SIGNATURES = {
     "tbem_csr_create": (_I, [_L, _L, _P, _P, _P, _P]),
     "tbem_csr_apply": (_I, [_P, _P, _P, _I, _P]),
     "tbem_csr_nnz": (_L, [_P]),
+    "tbem_csr_shape": (_I, [_P, _P, _P]),
+    "tbem_csr_download": (_I, [_P, _P, _P, _P]),
+    "tbem_nearfield_create": (_I, [_I, _P, _P, _L, _P, _L, _P, _L, _P, _L, _P, _I, _P]),
+    "tbem_gauss_facet": (_L, [_I, _L, _P, _P]),
+    "tbem_galerkin_obs_points": (_L, [_I, _P, _L, _P, _L, _P, _L, _L, _P, _P, _P]),
     "tbem_csr_destroy": (None, [_P]),
     "tbem_integral_create": (_I, [_P, _P, _P, _P, _P, _P]),
     "tbem_integral_apply": (_I, [_P, _P, _P, _I, _P]),

@@ -250,6 +250,11 @@ int tbem_csr_create(long n_rows, long n_cols, const double* values,
                     const long* column_indices, const long* row_ptrs, TbemCsr** out);
 int tbem_csr_apply(TbemCsr* h, const double* x, double* y, int n_rhs, void* stream);
 long tbem_csr_nnz(const TbemCsr* h);
+/* Shape and a host copy of the arrays (SparseOperator's n_rows / n_cols /
+ * values / column_indices / row_ptrs, python_wrapper/linalg.cpp:15-38); any
+ * output pointer may be NULL. */
+int tbem_csr_shape(const TbemCsr* h, long* n_rows, long* n_cols);
+int tbem_csr_download(const TbemCsr* h, double* values, long* column_indices, long* row_ptrs);
 void tbem_csr_destroy(TbemCsr* h);
 
 /* Replaces IntegralOperator::apply (cpp/integral_operator.h:55-63):
@@ -269,6 +274,47 @@ void tbem_integral_destroy(TbemIntegral* h);
 
 /* Last error message of the calling thread ("" if none). */
 const char* tbem_last_error(void);
+
+/* Nearfield and farfield-correction matrices (make_nearfield_operator /
+ * make_farfield_correction_operator, cpp/nearfield_operator.h:12-117, with the
+ * sinh integration strategy, make_sinh_integrator, cpp/integral_term.h:
+ * 129-150, and IntegrationStrategy::compute_term, cpp/integral_term.cpp:
+ * 33-92).  The host finds every (Galerkin observation point, nearby source
+ * facet) term and the point's Richardson direction; the GPU integrates the
+ * terms.  Meshes share one vertex array [n_vertices][dim] (dim from the
+ * kernel id); obs / src / all facets are [n][dim] vertex indices (the
+ * reference's boundary_operator(obs_mesh, src_mesh, mthd, fmm_config,
+ * all_mesh), cpp/integral_operator.h:66-99).  which: 0 the nearfield
+ * operator (observation points from obs_near_order), 1 the farfield
+ * correction (obs_far_order).  The result is a CSR operator with rows
+ * R * n_obs_facets * n_obs_quad and columns C * dim * n_src_facets. */
+typedef struct {
+    long sinh_order;       /* sinh rules: order + order * log(facet size / distance) points */
+    long obs_near_order;   /* Gauss rule of the nearfield observation points */
+    long obs_far_order;    /* Gauss rule of the farfield observation points */
+    long src_far_order;    /* Gauss rule of far source facets */
+    long n_singular_steps; /* Richardson steps (2..32) */
+    double far_threshold;  /* facets nearer than far_threshold x facet size are "near" */
+} TbemSinhIntegrator;
+
+/* Gauss rule on the reference facet (gauss_facet, cpp/gauss_quad.cpp:155-165):
+ * points [n][dim - 1] on [-1, 1] (dim 2) or the triangle (0,0)-(1,0)-(0,1)
+ * (dim 3), weights [n]; returns n (host only). */
+long tbem_gauss_facet(int dim, long n, double* x, double* w);
+
+/* Galerkin observation points of obs_facets with their Richardson (limit)
+ * directions against all_facets (galerkin_obs_pts, cpp/nearfield_operator.h:
+ * 12-40); outputs [n][dim] (NULL-able); returns n (host only). */
+long tbem_galerkin_obs_points(int dim, const double* vertices, long n_vertices,
+                              const long* obs_facets, long n_obs_facets, const long* all_facets,
+                              long n_all_facets, long order, double* locs, double* normals,
+                              double* dirs);
+
+int tbem_nearfield_create(int kernel, const double* kernel_params, const double* vertices,
+                          long n_vertices, const long* obs_facets, long n_obs_facets,
+                          const long* src_facets, long n_src_facets, const long* all_facets,
+                          long n_all_facets, const TbemSinhIntegrator* mthd, int which,
+                          TbemCsr** out);
 
 #ifdef __cplusplus
 }

@@ -328,3 +328,76 @@ def surface(order, dim=3, lib="oracle"):
 
 def max_threads():
     return _lib().fn("max_threads", _I, [])()
+
+
+# ---- the reference's nearfield construction (oracle/ref/nearfield_shim.cpp)
+
+def _ref():
+    return _Lib._cache.setdefault("ref", _Lib(REF_LIB_PATH, "ref_"))
+
+
+def _mesh_args(vertices, facets):
+    v = _pts3(vertices)
+    f = np.ascontiguousarray(facets, dtype=np.int64)
+    return v, f
+
+
+def ref_nearfield(kernel, vertices, facets, strategy="sinh", near_tol=1e-4, sinh_order=5,
+                  obs_near_order=2, obs_far_order=2, src_far_order=2, n_singular_steps=8,
+                  far_threshold=3.0, which=0, mu=1.0, nu=0.25):
+    """The reference's nearfield (which 0) or farfield-correction (which 1)
+    CSR matrix of a mesh against itself: (n_rows, n_cols, values, cols, rowptr)."""
+    dim = np.asarray(vertices).shape[1]
+    k = kernel_id(kernel, dim)
+    v, f = _mesh_args(vertices, facets)
+    fn = _ref().fn("nearfield", _L, [_I, _D, _D, _I, _P, _L, _P, _L, _I, _D, _L, _L, _L, _L, _L,
+                                     _D, _I, _P, _P, _P, _P, _L])
+    shape = np.zeros(2, dtype=np.int64)
+    args = [k, mu, nu, dim, _ptr(v), len(v), _ptr(f), len(f), 0 if strategy == "adaptive" else 1,
+            near_tol, sinh_order, obs_near_order, obs_far_order, src_far_order, n_singular_steps,
+            far_threshold, which, _ptr(shape)]
+    nnz = fn(*args, None, None, None, 0)
+    if nnz < 0:
+        raise ValueError("reference nearfield failed")
+    vals = np.zeros(nnz)
+    cols = np.zeros(nnz, dtype=np.int64)
+    rows = np.zeros(shape[0] + 1, dtype=np.int64)
+    fn(*args, _ptr(vals), _ptr(cols), _ptr(rows), nnz)
+    return int(shape[0]), int(shape[1]), vals, cols, rows
+
+
+def ref_obs_points(vertices, facets, order):
+    """The reference's Galerkin observation points: (locs, normals, dirs) [n][3]."""
+    dim = np.asarray(vertices).shape[1]
+    v, f = _mesh_args(vertices, facets)
+    fn = _ref().fn("obs_points", _L, [_I, _P, _L, _P, _L, _L, _P, _P, _P])
+    n = fn(dim, _ptr(v), len(v), _ptr(f), len(f), order, None, None, None)
+    out = [np.zeros((n, 3)) for _ in range(3)]
+    fn(dim, _ptr(v), len(v), _ptr(f), len(f), order, *[_ptr(a) for a in out])
+    return tuple(out)
+
+
+def ref_gauss_facet(dim, n):
+    fn = _ref().fn("gauss_facet", _L, [_I, _L, _P, _P])
+    k = fn(dim, n, None, None)
+    x = np.zeros((k, dim - 1))
+    w = np.zeros(k)
+    fn(dim, n, _ptr(x), _ptr(w))
+    return x, w
+
+
+def ref_term(kernel, loc, normal, direction, facet, strategy="sinh", near_tol=1e-4, sinh_order=5,
+             obs_near_order=2, obs_far_order=2, src_far_order=2, n_singular_steps=8,
+             far_threshold=3.0, mu=1.0, nu=0.25):
+    """One compute_term of the reference: [dim][R][C]."""
+    dim = len(loc)
+    k = kernel_id(kernel, dim)
+    R = kernel_components(k)
+    fn = _ref().fn("term", _L, [_I, _D, _D, _I, _D, _L, _L, _L, _L, _L, _D, _P, _P, _P, _P, _P])
+    vec = [_pts3(np.reshape(a, (1, -1)))[0] for a in (loc, normal, direction)]
+    fac = _pts3(np.reshape(facet, (dim, -1)))
+    out = np.zeros(dim * R * R)
+    fn(k, mu, nu, 0 if strategy == "adaptive" else 1, near_tol, sinh_order, obs_near_order,
+       obs_far_order, src_far_order, n_singular_steps, far_threshold, *[_ptr(a) for a in vec],
+       _ptr(fac), _ptr(out))
+    return out.reshape(dim, R, R)

@@ -6,9 +6,12 @@ small seeded inputs, and stores inputs, reference outputs, the reference's
 check-to-equivalent operators, trees and task lists.  The GPU tests compare
 the product against these without needing the reference checkout.
 
-    python tests/golden/make_golden.py [/root/reference] [all|2d]
+    python tests/golden/make_golden.py [/root/reference] [all|2d|nearfield]
 
-("2d" writes only the 2D fixtures: fmm_*2_*.npz and kernels_2d.npz.)
+("2d" writes only the 2D fixtures: fmm_*2_*.npz and kernels_2d.npz;
+"nearfield" only the nearfield / farfield-correction matrices,
+nearfield_*.npz, made by the reference's own construction with the
+restated GTEngine queries of oracle/ref/gte_restated.cpp.)
 
 The reference's LAPACK (scipy's OpenBLAS) is run single-threaded so that
 the stored operators are reproducible.
@@ -172,10 +175,73 @@ def kernel_vectors_2d():
     return np.array(rows)
 
 
+def nearfield_meshes():
+    """Small seeded meshes for the nearfield fixtures: an icosphere, a dipping
+    fault, a folded wedge (3D), a circle and a V-shaped wedge (2D)."""
+    ico_v, ico_f = meshes.icosphere(1)
+    flt_v, flt_f, _ = meshes.dipping_fault(4)
+    wedge_v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0], [0, 0.1, 0.2], [1, 0.1, 0.2]], float)
+    wedge_f = np.array([[0, 1, 2], [1, 3, 2], [0, 4, 1], [1, 4, 5]])
+    n = 40
+    t = 2 * np.pi * np.arange(n) / n
+    circ_v = np.stack([np.cos(t), np.sin(t)], axis=1)
+    circ_f = np.stack([np.arange(n), (np.arange(n) + 1) % n], axis=1)
+    vw_v = np.array([[-1, 1], [-0.5, 0.5], [0, 0], [0.5, 0.5], [1, 1], [0.2, 0.05]], float)
+    vw_f = np.array([[0, 1], [1, 2], [2, 3], [3, 4], [2, 5]])
+    return {"ico": (ico_v, ico_f), "fault": (flt_v, flt_f), "wedge": (wedge_v, wedge_f),
+            "circle": (circ_v, circ_f), "vwedge": (vw_v, vw_f)}
+
+
+# (name, mesh, kernel, mu, nu, sinh_order, obs_near, obs_far, src_far, steps, far_threshold)
+NEARFIELD_CASES = [
+    ("lapd_ico", "ico", "LaplaceDouble", 1.0, 0.25, 5, 2, 2, 2, 8, 3.0),
+    ("laps_wedge", "wedge", "LaplaceSingle", 1.0, 0.25, 4, 3, 2, 3, 6, 3.0),
+    ("eltrac_fault", "fault", "ElasticTraction", 1.0, 0.25, 4, 2, 2, 3, 6, 3.0),
+    ("elhyp_fault", "fault", "ElasticHypersingular", 30.0, 0.25, 4, 2, 2, 2, 6, 3.0),
+    ("laps2_circle", "circle", "LaplaceSingle", 1.0, 0.25, 12, 3, 3, 3, 8, 3.0),
+    ("eldisp2_vwedge", "vwedge", "ElasticDisplacement", 1.0, 0.25, 8, 3, 2, 3, 8, 3.0),
+    ("elhyp2_circle", "circle", "ElasticHypersingular", 1.0, 0.3, 10, 2, 2, 3, 8, 3.0),
+]
+
+
+def make_nearfield_cases():
+    ms = nearfield_meshes()
+    for name, mesh, kernel, mu, nu, so, on, of, sf, st, ft in NEARFIELD_CASES:
+        v, f = ms[mesh]
+        out = dict(kernel=kernel, mu=mu, nu=nu, vertices=v, facets=f, sinh_order=so,
+                   obs_near_order=on, obs_far_order=of, src_far_order=sf, n_singular_steps=st,
+                   far_threshold=ft)
+        # the reference's own sensitivity: its matrix again with every vertex
+        # coordinate moved by one ulp (random sign), max |change| / max |entry|
+        vp = v * (1 + 2.0 ** -52 * np.random.default_rng(0).choice([-1, 1], size=v.shape))
+        for which in (0, 1):
+            nr, nc, vals, cols, rows = oracle.ref_nearfield(
+                kernel, v, f, "sinh", 0.0, so, on, of, sf, st, ft, which, mu, nu)
+            out["shape%d" % which] = np.array([nr, nc])
+            out["values%d" % which] = vals
+            out["cols%d" % which] = cols
+            out["rowptr%d" % which] = rows
+            pr, pc, pv, pcols, prows = oracle.ref_nearfield(
+                kernel, vp, f, "sinh", 0.0, so, on, of, sf, st, ft, which, mu, nu)
+            a = np.zeros((nr, nc))
+            b = np.zeros((pr, pc))
+            for r in range(nr):
+                np.add.at(a[r], cols[rows[r]:rows[r + 1]], vals[rows[r]:rows[r + 1]])
+                np.add.at(b[r], pcols[prows[r]:prows[r + 1]], pv[prows[r]:prows[r + 1]])
+            out["ulp_floor%d" % which] = np.abs(a - b).max() / np.abs(a).max()
+        loc, nrm, dirs = oracle.ref_obs_points(v, f, on)
+        out["obs_loc"], out["obs_dir"] = loc, dirs
+        np.savez_compressed(os.path.join(HERE, "nearfield_%s.npz" % name), **out)
+        print("wrote nearfield", name, out["shape0"], len(out["values0"]), len(out["values1"]))
+
+
 def main(ref_root="/root/reference", which="all"):
     oracle.build()
     if oracle.build_ref(ref_root) is None:
         raise SystemExit("the reference checkout is needed to regenerate the fixtures")
+    if which == "nearfield":
+        make_nearfield_cases()
+        return
     for case in CASES_2D:
         data = make_case(*case)
         np.savez_compressed(os.path.join(HERE, "fmm_%s.npz" % case[0]), **data)

@@ -1,0 +1,84 @@
+"""GPU parity of the nearfield and farfield-correction matrices with the
+reference's own construction (tests/golden/nearfield_*.npz: 3D and 2D
+meshes, Laplace and elastic kernels including the hypersingular ones,
+Richardson extrapolation for the on-surface observation points).
+
+Tolerance (written here, checked below): max |GPU - reference| <= max(1e-10,
+100 x floor) x max |reference entry|, with floor the reference's own change
+when every vertex moves by one ulp (stored in the fixture: <= 1e-13 for the
+3D cases, 1.4e-10 for the 2D cases whose Richardson extrapolation cancels
+the most).  Same layout: identical row pointers and column indices (the
+reference's facet order is reproduced).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CASES = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "nearfield_*.npz")))
+
+
+def dense(shape, vals, cols, rows):
+    a = np.zeros(tuple(shape))
+    for r in range(shape[0]):
+        np.add.at(a[r], cols[rows[r]:rows[r + 1]], vals[rows[r]:rows[r + 1]])
+    return a
+
+
+def kernel_of(g, dim):
+    from tbempy import ThreeD, TwoD
+    k = getattr(TwoD if dim == 2 else ThreeD, str(g["kernel"]))
+    return k(float(g["mu"]), float(g["nu"])) if str(g["kernel"]).startswith("Elastic") else k()
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(p)[10:-4] for p in CASES])
+def test_nearfield_matrices_match_reference(path):
+    from tbempy import ThreeD
+    g = dict(np.load(path))
+    m = ThreeD.Mesh(g["vertices"], g["facets"])
+    mthd = ThreeD.make_sinh_integrator(int(g["sinh_order"]), int(g["obs_near_order"]),
+                                       int(g["obs_far_order"]), int(g["src_far_order"]),
+                                       int(g["n_singular_steps"]), float(g["far_threshold"]),
+                                       kernel_of(g, m.dim))
+    for which, build in ((0, ThreeD.nearfield_operator), (1, ThreeD.farfield_correction_operator)):
+        op = build(m, m, mthd, m)
+        assert (op.n_rows(), op.n_cols()) == tuple(g["shape%d" % which])
+        assert np.array_equal(op.row_ptrs(), g["rowptr%d" % which])
+        assert np.array_equal(op.column_indices(), g["cols%d" % which])
+        ref = g["values%d" % which]
+        tol = max(1e-10, 100 * float(g["ulp_floor%d" % which])) * np.abs(ref).max()
+        assert np.abs(op.values() - ref).max() <= tol
+        # the device CSR applies the same matrix
+        x = np.random.default_rng(1).uniform(-1, 1, op.n_cols())
+        A = dense(g["shape%d" % which], ref, g["cols%d" % which], g["rowptr%d" % which])
+        assert np.linalg.norm(op.apply(x) - A @ x) <= 1e-8 * np.linalg.norm(A @ x) + 1e-300
+
+
+def test_boundary_operator_assembles_and_matches_dense_chain():
+    """boundary_operator: the device chain G_near N + G_far C + G_far F I with
+    the FMM farfield equals the same chain with the direct farfield."""
+    from tbempy import ThreeD, meshes
+    v, f = meshes.icosphere(2)
+    m = ThreeD.Mesh(v, f)
+    K = ThreeD.LaplaceDouble()
+    mthd = ThreeD.make_sinh_integrator(5, 3, 3, 3, 8, 3.0, K)
+    A = ThreeD.boundary_operator(m, m, mthd, ThreeD.FMMConfig(0.3, 75, 20, 0.05, False), m)
+    assert A.n_rows() == m.n_dofs() and A.n_cols() == m.n_dofs()
+    x = np.random.default_rng(2).uniform(-1, 1, m.n_dofs())
+    y = A.apply(x)
+    ol, on, _ = ThreeD.quadrature_points(m, 3)
+    sl, sn, sw = ThreeD.quadrature_points(m, 3)
+    D = ThreeD.DirectOperator(K, ol, on, sl, sn, sw)
+    chain = ThreeD.IntegralOperator(A.nearfield, A.farfield_correction, A.galerkin, D, A.interp)
+    yd = chain.apply(x)
+    assert np.linalg.norm(y - yd) <= 1e-6 * np.linalg.norm(yd)
+    # the double layer of a constant density on a closed surface, its limit
+    # taken along the facet normals (outward here): the exterior value 0 (the
+    # reference's own matrices give |A 1| <= 2.4e-3 of the basis integrals)
+    ones = np.ones(m.n_dofs())
+    g = A.galerkin.apply(np.ones(A.galerkin.n_cols()))  # integrals of the basis functions
+    assert np.abs(A.apply(ones)).max() <= 5e-3 * np.abs(g).max()

@@ -1,0 +1,73 @@
+"""CPU tests of the nearfield construction's host side against the
+reference's own outputs (tests/golden/nearfield_*.npz, made by the
+reference's construction with oracle/ref/gte_restated.cpp standing in for the
+absent GTEngine): the Galerkin observation points and their Richardson
+(limit) directions bit for bit, the Gauss rules, and the argument checks.
+No device compute happens here."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CASES = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "nearfield_*.npz")))
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(p)[10:-4] for p in CASES])
+def test_obs_points_and_limit_directions_match_reference(path):
+    from tbempy import ThreeD
+    g = dict(np.load(path))
+    m = ThreeD.Mesh(g["vertices"], g["facets"])
+    loc, nrm, dirs = ThreeD.galerkin_obs_points(m, m, int(g["obs_near_order"]))
+    dim = m.dim
+    assert np.array_equal(loc, g["obs_loc"][:, :dim])
+    assert np.array_equal(dirs, g["obs_dir"][:, :dim])
+    # points on the surface step off it: every direction is non-zero
+    assert np.all(np.abs(dirs).sum(axis=1) > 0)
+
+
+def test_gauss_rules_integrate_polynomials():
+    """gauss_facet: degree 2n - 1 on [-1, 1]; the collapsed tensor rule on
+    the unit triangle integrates x^a y^b exactly (a + b <= 2n - 2) -- to the
+    1e-12 the reference's Newton iteration leaves (its weights for n = 20 sum
+    to 2 - 2e-13)."""
+    from math import factorial
+    from tbempy import ThreeD
+    for n in (1, 3, 7, 20):
+        x, w = ThreeD.gauss_facet(2, n)
+        for k in range(2 * n):
+            exact = 0.0 if k % 2 else 2.0 / (k + 1)
+            assert abs((w * x[:, 0] ** k).sum() - exact) < 1e-12
+        x, w = ThreeD.gauss_facet(3, n)
+        assert len(w) == n * n
+        for a in range(n):
+            for b in range(n - 1 - a + 1):
+                if a + b > 2 * n - 2:
+                    continue
+                exact = factorial(a) * factorial(b) / factorial(a + b + 2)
+                assert abs((w * x[:, 0] ** a * x[:, 1] ** b).sum() - exact) < 1e-12
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/cpp"), reason="reference checkout absent")
+def test_gauss_rules_match_reference():
+    from oracle import oracle
+    from tbempy import ThreeD
+    if not oracle.ref_available():
+        pytest.skip("reference library not built here")
+    for dim in (2, 3):
+        for n in (1, 2, 5, 12, 33):
+            a, b = ThreeD.gauss_facet(dim, n), oracle.ref_gauss_facet(dim, n)
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_adaptive_strategy_and_bad_arguments_refused():
+    from tbempy import ThreeD, TwoD
+    from tbempy._lib import TbemError
+    g = dict(np.load(CASES[0]))
+    m = ThreeD.Mesh(g["vertices"], g["facets"])
+    K = ThreeD.LaplaceDouble() if m.dim == 3 else TwoD.LaplaceDouble()
+    with pytest.raises(NotImplementedError):
+        ThreeD.nearfield_operator(m, m, ThreeD.make_adaptive_integrator(1e-4, 2, 2, 2, 8, 3.0, K), m)
+    with pytest.raises(TbemError):
+        ThreeD.galerkin_obs_points(ThreeD.Mesh(m.vertices, m.facets + 10 * len(m.vertices)), m, 2)
