@@ -12,13 +12,16 @@
 // Richardson extrapolation (cpp/richardson.h) of nearby integrals taken at
 // points stepped back along the limit direction.
 //
-// Here the host finds the terms (nearfield_host.cpp) and the GPU integrates
-// them: one warp per term, the lanes striding over the term's quadrature
-// points (every node generated on the fly from a table of Gauss rules) and
-// meeting in a butterfly reduction; each Richardson step is reduced before
-// the next, and lane e extrapolates entry e.  The values come back to the
-// host, which lays them out as the reference's COO entries and compresses
-// them to CSR (csr_from_coo's stable row order).
+// Here the host finds the terms (nearfield_host.cpp) and classifies each one
+// exactly as compute_term does (closest point, far / near / singular); a
+// singular term becomes one near evaluation per Richardson step at the
+// stepped-back point, computed on the host like the reference's
+// get_step_loc.  The GPU integrates every evaluation: one warp per
+// evaluation, the lanes striding over its quadrature points (every node
+// generated on the fly from a table of Gauss rules) and meeting in a
+// butterfly reduction.  The host extrapolates the singular terms
+// (richardson_limit), lays the values out as the reference's COO entries and
+// compresses them to CSR (csr_from_coo's stable row order).
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -37,27 +40,24 @@ constexpr int NF_WARPS = 4;   // terms per CTA
 struct NfArgs {
     int kid;
     KParams kp;
-    int mode;  // 0: compute_term; 1: -compute_farfield (the farfield correction)
     int sinh_order;
-    int n_steps;
-    double far_threshold;
     const double* gx;  // Gauss rule n (n = 1..NF_GMAX) at offset n (n - 1) / 2
     const double* gw;
     const double* fx;  // source farfield rule: [n_far][2] reference points
     const double* fw;
     int n_far;
-    const double* loc;  // observation points [n][3]
-    const double* nrm;
-    const double* dir;  // Richardson directions
+    const double* loc;  // evaluation points [n_items][3]
+    const double* nrm;  // observation normals [n_obs][3]
     const double* fac;  // source facets [n][3 corners][3]
     const double* ls;   // length scale
     const double* jac;  // jacobian
     const double* fn;   // facet normal [n][3]
-    const int* t_obs;
-    const int* t_fac;
-    long n_terms;
-    double* out;  // [n_terms][dim][R][C]
-    int* err;     // bit 1: a point on a facet without a limit direction; bit 2: rule too large
+    const int* i_obs;   // per evaluation: observation point (for its normal),
+    const int* i_fac;   // source facet,
+    const int* i_near;  // 1: sinh rule at the point, 0: the farfield rule
+    long n_items;
+    double* out;  // [n_items][dim][R][C]
+    int* err;     // bit 1: a point on a facet; bit 2: rule too large
 };
 
 __device__ __forceinline__ double gnode(const NfArgs& a, int n, int i) { return a.gx[n * (n - 1) / 2 + i]; }
@@ -245,63 +245,27 @@ template <int DIM, int R>
 __global__ void __launch_bounds__(32 * NF_WARPS) nearfield_kernel(const NfArgs a)
 {
     constexpr int E = DIM * R * R;
-    const long t = (long)blockIdx.x * NF_WARPS + threadIdx.x / 32;
-    if (t >= a.n_terms) return;  // whole warps leave together
+    const long i = (long)blockIdx.x * NF_WARPS + threadIdx.x / 32;
+    if (i >= a.n_items) return;  // whole warps leave together
     const int lane = threadIdx.x & 31;
-    const int o = a.t_obs[t], f = a.t_fac[t];
-    const double* p = a.loc + 3 * o;
-    const double* pn = a.nrm + 3 * o;
-    const double* dir = a.dir + 3 * o;
+    const int f = a.i_fac[i];
+    const double* p = a.loc + 3 * i;
+    const double* pn = a.nrm + 3 * a.i_obs[i];
     double acc[E];
 #pragma unroll
     for (int e = 0; e < E; e++) acc[e] = 0.0;
-    double result = 0.0;  // entry `lane` of the term (lanes < E)
-
-    const double ls = a.ls[f];
-    const DClosest cp = d_closest<DIM>(p, a.fac + 9 * f);
-    const bool near = a.mode == 0 && cp.dist < a.far_threshold * ls;
-    double d2 = 0.0;
-    for (int d = 0; d < DIM; d++) d2 += dir[d] * dir[d];
-    const bool singular = near && cp.dist < 1.0 * ls && d2 > 1e-10 * ls;
-    if (singular) {
-        // Richardson extrapolation over points stepped back along the limit
-        // direction, steps 1, 1/2, 1/4, ... (make_singular_steps, get_step_loc)
-        double vals[32];
-        for (int k = 0; k < a.n_steps; k++) {
-            const double step = 1.0 / pow(2.0, (double)k);
-            const double ps[3] = {p[0] + (1.0 * step) * dir[0], p[1] + (1.0 * step) * dir[1],
-                                  p[2] + (1.0 * step) * dir[2]};
-#pragma unroll
-            for (int e = 0; e < E; e++) acc[e] = 0.0;
-            sinh_near<DIM, R>(a, f, ps, pn, acc);
-            warp_sum<E>(acc);
-            double mine = 0.0;
-#pragma unroll
-            for (int e = 0; e < E; e++)
-                if (e == lane) mine = acc[e];
-            vals[k] = mine;
-        }
-        // richardson_limit(2, steps) (cpp/richardson.h:10-34)
-        for (int m = 1; m < a.n_steps; m++) {
-            const double mult = pow(2.0, (double)m);
-            const double factor = 1.0 / (mult - 1.0);
-            for (int i = 0; i < a.n_steps - m; i++) vals[i] = factor * (mult * vals[i + 1] - vals[i]);
-        }
-        result = vals[0];
+    if (a.i_near[i]) {
+        sinh_near<DIM, R>(a, f, p, pn, acc);
     } else {
-        if (near) {
-            sinh_near<DIM, R>(a, f, p, pn, acc);
-        } else {
-            for (int q = lane; q < a.n_far; q += 32)
-                influence<DIM, R>(a, f, p, pn, a.fx[2 * q], a.fx[2 * q + 1], a.fw[q], acc);
-        }
-        warp_sum<E>(acc);
-#pragma unroll
-        for (int e = 0; e < E; e++)
-            if (e == lane) result = acc[e];
-        if (a.mode == 1) result = -result;
+        for (int q = lane; q < a.n_far; q += 32)
+            influence<DIM, R>(a, f, p, pn, a.fx[2 * q], a.fx[2 * q + 1], a.fw[q], acc);
     }
-    if (lane < E) a.out[t * E + lane] = result;
+    warp_sum<E>(acc);
+    double result = 0.0;  // entry `lane` of the evaluation (lanes < E)
+#pragma unroll
+    for (int e = 0; e < E; e++)
+        if (e == lane) result = acc[e];
+    if (lane < E) a.out[i * E + lane] = result;
 }
 
 // Gauss rules 1..NF_GMAX, computed once per process.
@@ -340,7 +304,7 @@ std::vector<nf::Facet> read_facets(const double* verts, long n_verts, const long
 template <int DIM, int R>
 void launch(const NfArgs& a)
 {
-    const long blocks = (a.n_terms + NF_WARPS - 1) / NF_WARPS;
+    const long blocks = (a.n_items + NF_WARPS - 1) / NF_WARPS;
     nearfield_kernel<DIM, R><<<(unsigned)blocks, 32 * NF_WARPS>>>(a);
     TBEM_CK(cudaGetLastError());
 }
@@ -434,15 +398,59 @@ int tbem_nearfield_create(int kernel, const double* kernel_params, const double*
         }
         const long n_terms = (long)t_obs.size();
         const int E = dim * R * R;
-        std::vector<double> vals((size_t)n_terms * E);
-        if (n_terms > 0) {
-            std::vector<double> loc, nrm, dir, fac, ls, jac, fn;
-            for (long i = 0; i < n_pts; i++)
-                for (int d = 0; d < 3; d++) {
-                    loc.push_back(pts.loc[i][d]);
-                    nrm.push_back(pts.normal[i][d]);
-                    dir.push_back(pts.dir[i][d]);
+        // classify every term as IntegrationStrategy::compute_term does
+        // (cpp/integral_term.cpp:33-53) and list its evaluations: one for a far
+        // or near term, n_steps (at the stepped-back points, get_step_loc,
+        // cpp/integral_term.cpp:55-60) for a singular one
+        const int n_steps = (int)mthd->n_singular_steps;
+        std::vector<long> first(n_terms);
+        std::vector<char> sing(n_terms, 0);
+        std::vector<int> i_obs, i_fac, i_near;
+        std::vector<double> iloc;
+        auto add_item = [&](long o, long f, int nearflag, const nf::V3& at) {
+            i_obs.push_back((int)o);
+            i_fac.push_back((int)f);
+            i_near.push_back(nearflag);
+            for (int d = 0; d < 3; d++) iloc.push_back(at[d]);
+        };
+        for (long t = 0; t < n_terms; t++) {
+            const long o = t_obs[t], f = t_fac[t];
+            first[t] = (long)i_obs.size();
+            const nf::V3& p = pts.loc[o];
+            if (which == 1) {  // -compute_farfield for every term
+                add_item(o, f, 0, p);
+                continue;
+            }
+            const double dist = nf::closest_point(p, src[f], dim).dist;
+            const double ls = src_set.info(f).length_scale;
+            if (dist < mthd->far_threshold * ls) {
+                double d2 = 0.0;
+                for (int d = 0; d < dim; d++) d2 += pts.dir[o][d] * pts.dir[o][d];
+                if (dist < 1.0 * ls && d2 > 1e-10 * ls) {
+                    sing[t] = 1;
+                    for (int k = 0; k < n_steps; k++) {
+                        const double step = 1.0 / std::pow(2.0, (double)k);
+                        const double sd = 1.0 * step;
+                        nf::V3 q;
+                        for (int d = 0; d < 3; d++) q[d] = p[d] + sd * pts.dir[o][d];
+                        add_item(o, f, 1, q);
+                    }
+                } else {
+                    if (!(dist > 0.0))
+                        throw Error(TBEM_ERR_ARG, "an observation point lies on a source facet without a "
+                                                  "limit direction (the reference asserts here)");
+                    add_item(o, f, 1, p);
                 }
+            } else {
+                add_item(o, f, 0, p);
+            }
+        }
+        const long n_items = (long)i_obs.size();
+        std::vector<double> ivals((size_t)n_items * E);
+        if (n_items > 0) {
+            std::vector<double> nrm, fac, ls, jac, fn;
+            for (long i = 0; i < n_pts; i++)
+                for (int d = 0; d < 3; d++) nrm.push_back(pts.normal[i][d]);
             for (size_t f = 0; f < src.size(); f++) {
                 for (int v = 0; v < 3; v++)
                     for (int d = 0; d < 3; d++) fac.push_back(src[f].c[v][d]);
@@ -453,30 +461,27 @@ int tbem_nearfield_create(int kernel, const double* kernel_params, const double*
             }
             std::vector<double> fx, fw;
             nf::gauss_facet(dim, (int)mthd->src_far_order, fx, fw);
-            DBuf<double> d_gx, d_gw, d_fx, d_fw, d_loc, d_nrm, d_dir, d_fac, d_ls, d_jac, d_fn, d_out;
-            DBuf<int> d_to, d_tf, d_err;
+            DBuf<double> d_gx, d_gw, d_fx, d_fw, d_loc, d_nrm, d_fac, d_ls, d_jac, d_fn, d_out;
+            DBuf<int> d_io, d_if, d_in, d_err;
             d_gx.upload(gauss_table(0));
             d_gw.upload(gauss_table(1));
             d_fx.upload(fx);
             d_fw.upload(fw);
-            d_loc.upload(loc);
+            d_loc.upload(iloc);
             d_nrm.upload(nrm);
-            d_dir.upload(dir);
             d_fac.upload(fac);
             d_ls.upload(ls);
             d_jac.upload(jac);
             d_fn.upload(fn);
-            d_to.upload(t_obs);
-            d_tf.upload(t_fac);
+            d_io.upload(i_obs);
+            d_if.upload(i_fac);
+            d_in.upload(i_near);
             d_err.upload(std::vector<int>(1, 0));
-            d_out.alloc(vals.size());
+            d_out.alloc(ivals.size());
             NfArgs a{};
             a.kid = kernel;
             a.kp = make_kparams(kernel, mu, nu);
-            a.mode = which;
             a.sinh_order = (int)mthd->sinh_order;
-            a.n_steps = (int)mthd->n_singular_steps;
-            a.far_threshold = mthd->far_threshold;
             a.gx = d_gx.p;
             a.gw = d_gw.p;
             a.fx = d_fx.p;
@@ -484,14 +489,14 @@ int tbem_nearfield_create(int kernel, const double* kernel_params, const double*
             a.n_far = (int)fw.size();
             a.loc = d_loc.p;
             a.nrm = d_nrm.p;
-            a.dir = d_dir.p;
             a.fac = d_fac.p;
             a.ls = d_ls.p;
             a.jac = d_jac.p;
             a.fn = d_fn.p;
-            a.t_obs = d_to.p;
-            a.t_fac = d_tf.p;
-            a.n_terms = n_terms;
+            a.i_obs = d_io.p;
+            a.i_fac = d_if.p;
+            a.i_near = d_in.p;
+            a.n_items = n_items;
             a.out = d_out.p;
             a.err = d_err.p;
             if (dim == 2 && R == 1) launch<2, 1>(a);
@@ -502,13 +507,33 @@ int tbem_nearfield_create(int kernel, const double* kernel_params, const double*
             int err = 0;
             TBEM_CK(cudaMemcpy(&err, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
             if (err & 1)
-                throw Error(TBEM_ERR_ARG, "an observation point lies on a source facet without a "
-                                          "limit direction (the reference asserts here)");
+                throw Error(TBEM_ERR_ARG, "a stepped-back Richardson point lies on a source facet");
             if (err & 2)
                 throw Error(TBEM_ERR_ARG, "a sinh rule needs more than 512 Gauss points "
                                           "(observation point too close to a facet)");
-            TBEM_CK(cudaMemcpy(vals.data(), d_out.p, vals.size() * sizeof(double),
+            TBEM_CK(cudaMemcpy(ivals.data(), d_out.p, ivals.size() * sizeof(double),
                                cudaMemcpyDeviceToHost));
+        }
+        // per term: the evaluation, its negation (farfield correction) or the
+        // Richardson limit of its steps (richardson_limit, cpp/richardson.h:10-34)
+        std::vector<double> vals((size_t)n_terms * E);
+        std::vector<double> tab(n_steps);
+        for (long t = 0; t < n_terms; t++) {
+            for (int e = 0; e < E; e++) {
+                double v;
+                if (sing[t]) {
+                    for (int k = 0; k < n_steps; k++) tab[k] = ivals[(size_t)(first[t] + k) * E + e];
+                    for (int m = 1; m < n_steps; m++) {
+                        const double mult = std::pow(2.0, m);
+                        const double factor = 1.0 / (mult - 1.0);
+                        for (int i = 0; i < n_steps - m; i++) tab[i] = factor * (mult * tab[i + 1] - tab[i]);
+                    }
+                    v = tab[0];
+                } else {
+                    v = ivals[(size_t)first[t] * E + e];
+                }
+                vals[(size_t)t * E + e] = which == 1 ? -v : v;
+            }
         }
         // COO entries in the reference's order (cpp/nearfield_operator.h:59-84),
         // rows d1 * n_pts + point, columns d2 * n_dofs + facet * dim + basis;
