@@ -553,6 +553,7 @@ class IntegralOperator(OperatorI):
 # boundary-operator assembly (nearfield / correction matrices on the GPU,
 # Galerkin and interpolation operators, boundary_operator)
 from .bem import (Mesh, IntegrationStrategy, boundary_operator, farfield_correction_operator,  # noqa: E402,F401
-                  galerkin_obs_points, galerkin_operator, gauss_facet, interpolation_operator,
+                  galerkin_csr, galerkin_obs_points, galerkin_operator, gauss_facet,
+                  interpolation_csr, interpolation_operator,
                   make_adaptive_integrator, make_sinh_integrator, nearfield_operator,
                   quadrature_points)

@@ -13,8 +13,8 @@ import numpy as np
 from .ThreeD import (DirectOperator, FMMConfig, FMMGraph, FMMOperator,  # noqa: F401
                      IntegralOperator, IntegrationStrategy, Kernel, Mesh, OperatorI,
                      SparseOperator, boundary_operator, farfield_correction_operator,
-                     galerkin_obs_points, galerkin_operator, gauss_facet,
-                     interpolation_operator, make_adaptive_integrator, make_sinh_integrator,
+                     galerkin_csr, galerkin_obs_points, galerkin_operator, gauss_facet,
+                     interpolation_csr, interpolation_operator, make_adaptive_integrator, make_sinh_integrator,
                      nearfield_operator, quadrature_points)
 
 

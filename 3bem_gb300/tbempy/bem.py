@@ -159,17 +159,19 @@ def _basis(x, dim):
     return np.stack([1 - x[:, 0] - x[:, 1], x[:, 0], x[:, 1]], axis=1)
 
 
-def _csr(n_rows, n_cols, rows, cols, vals):
-    order = np.argsort(rows, kind="stable")  # csr_from_coo keeps input order in a row
+def _csr_arrays(n_rows, n_cols, rows, cols, vals):
+    """csr_from_coo (cpp/sparse_operator.cpp:140-172): entries keep their input
+    order inside a row.  Returns (n_rows, n_cols, values, column_indices, row_ptrs)."""
+    order = np.argsort(rows, kind="stable")
     counts = np.bincount(rows, minlength=n_rows)
-    return SparseOperator(n_rows, n_cols, vals[order], cols[order],
-                          np.concatenate([[0], np.cumsum(counts)]))
+    return (n_rows, n_cols, vals[order], cols[order].astype(np.int64),
+            np.concatenate([[0], np.cumsum(counts)]).astype(np.int64))
 
 
-def galerkin_operator(n_components, obs_mesh, order):
-    """make_galerkin_operator (cpp/galerkin_operator.cpp:9-44): rows
-    d * n_dofs + dof, columns d * n_quad_points + quad point, values
-    basis * jacobian * weight."""
+def galerkin_csr(n_components, obs_mesh, order):
+    """make_galerkin_operator (cpp/galerkin_operator.cpp:9-44) as host CSR
+    arrays: rows d * n_dofs + dof, columns d * n_quad_points + quad point,
+    values basis * (jacobian * weight)."""
     dim = obs_mesh.dim
     x, w = gauss_facet(dim, order)
     nq, nf = len(w), obs_mesh.n_facets()
@@ -180,12 +182,18 @@ def galerkin_operator(n_components, obs_mesh, order):
     rows = d * obs_mesh.n_dofs() + dim * f + b
     cols = d * (nf * nq) + f * nq + q
     vals = bas[q, b] * (jac[f] * w[q])
-    return _csr(n_components * obs_mesh.n_dofs(), n_components * nf * nq, rows.ravel(),
-                cols.ravel(), vals.ravel())
+    return _csr_arrays(n_components * obs_mesh.n_dofs(), n_components * nf * nq, rows.ravel(),
+                       cols.ravel(), vals.ravel())
 
 
-def interpolation_operator(n_components, src_mesh, order):
-    """make_interpolation_operator (cpp/interpolation_operator.cpp:9-39)."""
+def galerkin_operator(n_components, obs_mesh, order):
+    """make_galerkin_operator as a GPU SparseOperator."""
+    return SparseOperator(*galerkin_csr(n_components, obs_mesh, order))
+
+
+def interpolation_csr(n_components, src_mesh, order):
+    """make_interpolation_operator (cpp/interpolation_operator.cpp:9-39) as
+    host CSR arrays."""
     dim = src_mesh.dim
     x, w = gauss_facet(dim, order)
     nq, nf = len(w), src_mesh.n_facets()
@@ -195,8 +203,13 @@ def interpolation_operator(n_components, src_mesh, order):
     rows = d * (nf * nq) + f * nq + q
     cols = d * src_mesh.n_dofs() + dim * f + b
     vals = bas[q, b]
-    return _csr(n_components * nf * nq, n_components * src_mesh.n_dofs(), rows.ravel(),
-                cols.ravel(), vals.ravel())
+    return _csr_arrays(n_components * nf * nq, n_components * src_mesh.n_dofs(), rows.ravel(),
+                       cols.ravel(), vals.ravel())
+
+
+def interpolation_operator(n_components, src_mesh, order):
+    """make_interpolation_operator as a GPU SparseOperator."""
+    return SparseOperator(*interpolation_csr(n_components, src_mesh, order))
 
 
 def quadrature_points(mesh, order):

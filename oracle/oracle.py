@@ -401,3 +401,19 @@ def ref_term(kernel, loc, normal, direction, facet, strategy="sinh", near_tol=1e
        obs_far_order, src_far_order, n_singular_steps, far_threshold, *[_ptr(a) for a in vec],
        _ptr(fac), _ptr(out))
     return out.reshape(dim, R, R)
+
+
+def ref_galerkin_interp(which, vertices, facets, n_components, order):
+    """The reference's Galerkin (which 0) or interpolation (which 1) CSR
+    operator: (n_rows, n_cols, values, cols, rowptr)."""
+    dim = np.asarray(vertices).shape[1]
+    v, f = _mesh_args(vertices, facets)
+    fn = _ref().fn("galerkin_interp", _L, [_I, _I, _L, _P, _L, _P, _L, _L, _P, _P, _P, _P, _L])
+    shape = np.zeros(2, dtype=np.int64)
+    args = [which, dim, n_components, _ptr(v), len(v), _ptr(f), len(f), order, _ptr(shape)]
+    nnz = fn(*args, None, None, None, 0)
+    vals = np.zeros(nnz)
+    cols = np.zeros(nnz, dtype=np.int64)
+    rows = np.zeros(shape[0] + 1, dtype=np.int64)
+    fn(*args, _ptr(vals), _ptr(cols), _ptr(rows), nnz)
+    return int(shape[0]), int(shape[1]), vals, cols, rows

@@ -14,6 +14,8 @@
 #include <omp.h>
 
 #include "elastic_kernels.h"
+#include "galerkin_operator.h"
+#include "interpolation_operator.h"
 #include "identity_kernels.h"
 #include "integral_term.h"
 #include "laplace_kernels.h"
@@ -215,6 +217,30 @@ long ref_term(int kernel, double mu, double nu, int strategy, double near_tol, l
     case 23: return term(IdentityScalar<2>(), s, loc, nrm, dir, facet, out);
     }
     return -1;
+}
+
+// make_galerkin_operator (which 0, cpp/galerkin_operator.cpp:9-44) or
+// make_interpolation_operator (which 1, cpp/interpolation_operator.cpp:9-39)
+// with gauss_facet(order); CSR written when cap >= nnz; returns nnz.
+long ref_galerkin_interp(int which, int dim, long n_components, const double* verts, long n_verts,
+                         const long* facets, long n_facets, long order, long* shape,
+                         double* values, long* cols, long* rowptr, long cap)
+{
+    auto build = [&](auto m, auto q) {
+        return which == 0 ? make_galerkin_operator(n_components, m, q)
+                          : make_interpolation_operator(n_components, m, q);
+    };
+    SparseOperator op = dim == 2
+        ? build(make_mesh<2>(verts, n_verts, facets, n_facets), gauss_facet<2>((size_t)order))
+        : build(make_mesh<3>(verts, n_verts, facets, n_facets), gauss_facet<3>((size_t)order));
+    const long nnz = (long)op.values.size();
+    if (shape) { shape[0] = (long)op.n_rows(); shape[1] = (long)op.n_cols(); }
+    if (cap >= nnz && values) {
+        std::memcpy(values, op.values.data(), nnz * sizeof(double));
+        for (long k = 0; k < nnz; k++) cols[k] = (long)op.column_indices[k];
+        for (size_t r = 0; r < op.row_ptrs.size(); r++) rowptr[r] = (long)op.row_ptrs[r];
+    }
+    return nnz;
 }
 
 // Gauss rule on the reference facet (gauss_facet, cpp/gauss_quad.cpp:155-165):

@@ -71,3 +71,25 @@ def test_adaptive_strategy_and_bad_arguments_refused():
         ThreeD.nearfield_operator(m, m, ThreeD.make_adaptive_integrator(1e-4, 2, 2, 2, 8, 3.0, K), m)
     with pytest.raises(TbemError):
         ThreeD.galerkin_obs_points(ThreeD.Mesh(m.vertices, m.facets + 10 * len(m.vertices)), m, 2)
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(p)[10:-4] for p in CASES])
+def test_galerkin_and_interpolation_operators_match_reference(path):
+    """The host assembly of the Galerkin and interpolation operators against
+    the reference's make_galerkin_operator / make_interpolation_operator
+    (same layout; values to the last bit or one rounding)."""
+    from oracle import oracle
+    from tbempy import ThreeD
+    if not oracle.ref_available():
+        pytest.skip("reference library not built here")
+    g = dict(np.load(path))
+    m = ThreeD.Mesh(g["vertices"], g["facets"])
+    for ncomp in (1, m.dim):
+        for order in (2, 3):
+            for which, fn in ((0, ThreeD.galerkin_csr), (1, ThreeD.interpolation_csr)):
+                nr, nc, vals, cols, rows = fn(ncomp, m, order)
+                rr, rc, rv, rcols, rrows = oracle.ref_galerkin_interp(which, g["vertices"], g["facets"],
+                                                                      ncomp, order)
+                assert (nr, nc) == (rr, rc)
+                assert np.array_equal(rows, rrows) and np.array_equal(cols, rcols)
+                assert np.allclose(vals, rv, rtol=2e-16, atol=0)
