@@ -93,3 +93,33 @@ def test_galerkin_and_interpolation_operators_match_reference(path):
                 assert (nr, nc) == (rr, rc)
                 assert np.array_equal(rows, rrows) and np.array_equal(cols, rcols)
                 assert np.allclose(vals, rv, rtol=2e-16, atol=0)
+
+
+def test_nearfield_create_validates_before_device_use():
+    """Bad kernel ids, integrator parameters, `which` and facet indices come
+    back as TBEM_ERR_ARG with a message, before anything touches the device."""
+    import ctypes as C
+    from tbempy import _lib
+    L = _lib.lib()
+    v = np.ascontiguousarray([[0, 0, 0], [1, 0, 0], [0, 1, 0]], dtype=np.float64)
+    f = np.ascontiguousarray([[0, 1, 2]], dtype=np.int64)
+    bad_f = np.ascontiguousarray([[0, 1, 7]], dtype=np.int64)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    good = _lib.TbemSinhIntegrator(5, 2, 2, 2, 8, 3.0)
+    cases = [
+        (42, f, good, 0, "kernel"),                                        # unknown kernel
+        (1, f, good, 5, "which"),                                          # bad which
+        (1, f, _lib.TbemSinhIntegrator(0, 2, 2, 2, 8, 3.0), 0, "integrator"),
+        (1, f, _lib.TbemSinhIntegrator(5, 2, 2, 2, 1, 3.0), 0, "integrator"),  # < 2 steps
+        (1, f, _lib.TbemSinhIntegrator(5, 2, 2, 2, 8, -1.0), 0, "integrator"),
+        (1, bad_f, good, 0, "index"),                                      # vertex out of range
+    ]
+    for kid, fac, cfg, which, word in cases:
+        h = C.c_void_p()
+        rc = L.tbem_nearfield_create(kid, None, P(v), 3, P(fac), 1, P(fac), 1, P(fac), 1,
+                                     C.byref(cfg), which, C.byref(h))
+        assert rc == -1, (kid, which)
+        assert word in L.tbem_last_error().decode(), L.tbem_last_error()
+        assert not h.value
+    assert L.tbem_gauss_facet(4, 3, None, None) == -1
+    assert L.tbem_gauss_facet(3, 0, None, None) == -1
