@@ -309,6 +309,200 @@ void launch(const NfArgs& a)
     TBEM_CK(cudaGetLastError());
 }
 
+// The nearfield (which 0) or farfield-correction (which 1) CSR of the
+// observation points pts against the source facets (the body of
+// nearfield_inner_integral, cpp/nearfield_operator.h:48-95).
+int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const nf::ObsPoints& pts,
+                        const std::vector<nf::Facet>& src, const nf::FacetSet& src_set,
+                        const TbemSinhIntegrator* mthd, int which, TbemCsr** out)
+{
+    const long n_pts = (long)pts.loc.size();
+
+    // terms: every observation point against its nearfield source facets,
+    // in the reference's loop order
+    std::vector<int> t_obs, t_fac;
+    std::vector<size_t> nearby;
+    size_t nearest = 0;
+    double dist = 0.0;
+    for (long i = 0; i < n_pts; i++) {
+        src_set.find(pts.loc[i], mthd->far_threshold, nearby, nearest, dist);
+        for (size_t f : nearby) {
+            t_obs.push_back((int)i);
+            t_fac.push_back((int)f);
+        }
+    }
+    const long n_terms = (long)t_obs.size();
+    const int E = dim * R * R;
+    // classify every term as IntegrationStrategy::compute_term does
+    // (cpp/integral_term.cpp:33-53) and list its evaluations: one for a far
+    // or near term, n_steps (at the stepped-back points, get_step_loc,
+    // cpp/integral_term.cpp:55-60) for a singular one
+    const int n_steps = (int)mthd->n_singular_steps;
+    std::vector<long> first(n_terms);
+    std::vector<char> sing(n_terms, 0);
+    std::vector<int> i_obs, i_fac, i_near;
+    std::vector<double> iloc;
+    auto add_item = [&](long o, long f, int nearflag, const nf::V3& at) {
+        i_obs.push_back((int)o);
+        i_fac.push_back((int)f);
+        i_near.push_back(nearflag);
+        for (int d = 0; d < 3; d++) iloc.push_back(at[d]);
+    };
+    for (long t = 0; t < n_terms; t++) {
+        const long o = t_obs[t], f = t_fac[t];
+        first[t] = (long)i_obs.size();
+        const nf::V3& p = pts.loc[o];
+        if (which == 1) {  // -compute_farfield for every term
+            add_item(o, f, 0, p);
+            continue;
+        }
+        const double dist = nf::closest_point(p, src[f], dim).dist;
+        const double ls = src_set.info(f).length_scale;
+        if (dist < mthd->far_threshold * ls) {
+            double d2 = 0.0;
+            for (int d = 0; d < dim; d++) d2 += pts.dir[o][d] * pts.dir[o][d];
+            if (dist < 1.0 * ls && d2 > 1e-10 * ls) {
+                sing[t] = 1;
+                for (int k = 0; k < n_steps; k++) {
+                    const double step = 1.0 / std::pow(2.0, (double)k);
+                    const double sd = 1.0 * step;
+                    nf::V3 q;
+                    for (int d = 0; d < 3; d++) q[d] = p[d] + sd * pts.dir[o][d];
+                    add_item(o, f, 1, q);
+                }
+            } else {
+                if (!(dist > 0.0))
+                    throw Error(TBEM_ERR_ARG, "an observation point lies on a source facet without a "
+                                              "limit direction (the reference asserts here)");
+                add_item(o, f, 1, p);
+            }
+        } else {
+            add_item(o, f, 0, p);
+        }
+    }
+    const long n_items = (long)i_obs.size();
+    std::vector<double> ivals((size_t)n_items * E);
+    if (n_items > 0) {
+        std::vector<double> nrm, fac, ls, jac, fn;
+        for (long i = 0; i < n_pts; i++)
+            for (int d = 0; d < 3; d++) nrm.push_back(pts.normal[i][d]);
+        for (size_t f = 0; f < src.size(); f++) {
+            for (int v = 0; v < 3; v++)
+                for (int d = 0; d < 3; d++) fac.push_back(src[f].c[v][d]);
+            const nf::FacetInfo& fi = src_set.info(f);
+            ls.push_back(fi.length_scale);
+            jac.push_back(fi.jacobian);
+            for (int d = 0; d < 3; d++) fn.push_back(fi.normal[d]);
+        }
+        std::vector<double> fx, fw;
+        nf::gauss_facet(dim, (int)mthd->src_far_order, fx, fw);
+        DBuf<double> d_gx, d_gw, d_fx, d_fw, d_loc, d_nrm, d_fac, d_ls, d_jac, d_fn, d_out;
+        DBuf<int> d_io, d_if, d_in, d_err;
+        d_gx.upload(gauss_table(0));
+        d_gw.upload(gauss_table(1));
+        d_fx.upload(fx);
+        d_fw.upload(fw);
+        d_loc.upload(iloc);
+        d_nrm.upload(nrm);
+        d_fac.upload(fac);
+        d_ls.upload(ls);
+        d_jac.upload(jac);
+        d_fn.upload(fn);
+        d_io.upload(i_obs);
+        d_if.upload(i_fac);
+        d_in.upload(i_near);
+        d_err.upload(std::vector<int>(1, 0));
+        d_out.alloc(ivals.size());
+        NfArgs a{};
+        a.kid = kernel;
+        a.kp = make_kparams(kernel, mu, nu);
+        a.sinh_order = (int)mthd->sinh_order;
+        a.gx = d_gx.p;
+        a.gw = d_gw.p;
+        a.fx = d_fx.p;
+        a.fw = d_fw.p;
+        a.n_far = (int)fw.size();
+        a.loc = d_loc.p;
+        a.nrm = d_nrm.p;
+        a.fac = d_fac.p;
+        a.ls = d_ls.p;
+        a.jac = d_jac.p;
+        a.fn = d_fn.p;
+        a.i_obs = d_io.p;
+        a.i_fac = d_if.p;
+        a.i_near = d_in.p;
+        a.n_items = n_items;
+        a.out = d_out.p;
+        a.err = d_err.p;
+        if (dim == 2 && R == 1) launch<2, 1>(a);
+        else if (dim == 2) launch<2, 2>(a);
+        else if (R == 1) launch<3, 1>(a);
+        else launch<3, 3>(a);
+        TBEM_CK(cudaDeviceSynchronize());
+        int err = 0;
+        TBEM_CK(cudaMemcpy(&err, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err & 1)
+            throw Error(TBEM_ERR_ARG, "a stepped-back Richardson point lies on a source facet");
+        if (err & 2)
+            throw Error(TBEM_ERR_ARG, "a sinh rule needs more than 512 Gauss points "
+                                      "(observation point too close to a facet)");
+        TBEM_CK(cudaMemcpy(ivals.data(), d_out.p, ivals.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost));
+    }
+    // per term: the evaluation, its negation (farfield correction) or the
+    // Richardson limit of its steps (richardson_limit, cpp/richardson.h:10-34)
+    std::vector<double> vals((size_t)n_terms * E);
+    std::vector<double> tab(n_steps);
+    for (long t = 0; t < n_terms; t++) {
+        for (int e = 0; e < E; e++) {
+            double v;
+            if (sing[t]) {
+                for (int k = 0; k < n_steps; k++) tab[k] = ivals[(size_t)(first[t] + k) * E + e];
+                for (int m = 1; m < n_steps; m++) {
+                    const double mult = std::pow(2.0, m);
+                    const double factor = 1.0 / (mult - 1.0);
+                    for (int i = 0; i < n_steps - m; i++) tab[i] = factor * (mult * tab[i + 1] - tab[i]);
+                }
+                v = tab[0];
+            } else {
+                v = ivals[(size_t)first[t] * E + e];
+            }
+            vals[(size_t)t * E + e] = which == 1 ? -v : v;
+        }
+    }
+    // COO entries in the reference's order (cpp/nearfield_operator.h:59-84),
+    // rows d1 * n_pts + point, columns d2 * n_dofs + facet * dim + basis;
+    // a stable sort by row gives csr_from_coo's layout
+    const long n_dofs = (long)src.size() * dim;
+    const long n_rows = R * n_pts, n_cols = R * n_dofs;
+    std::vector<long> count(n_rows + 1, 0);
+    for (long t = 0; t < n_terms; t++)
+        for (int d1 = 0; d1 < R; d1++) count[d1 * n_pts + t_obs[t] + 1] += dim * R;
+    for (long r = 0; r < n_rows; r++) count[r + 1] += count[r];
+    std::vector<long> fill(count.begin(), count.end() - 1), cols(count[n_rows]);
+    std::vector<double> v(count[n_rows]);
+    for (long t = 0; t < n_terms; t++)
+        for (int b = 0; b < dim; b++)
+            for (int d1 = 0; d1 < R; d1++)
+                for (int d2 = 0; d2 < R; d2++) {
+                    const long row = d1 * n_pts + t_obs[t];
+                    const long k = fill[row]++;
+                    cols[k] = d2 * n_dofs + (long)t_fac[t] * dim + b;
+                    v[k] = vals[(size_t)t * E + (b * R + d1) * R + d2];
+                }
+    return tbem_csr_create(n_rows, n_cols, v.data(), cols.data(), count.data(), out);
+}
+
+void validate(int kernel, int which, const TbemSinhIntegrator* mthd)
+{
+    if (!kernel_valid(kernel)) throw Error(TBEM_ERR_ARG, "unknown kernel id");
+    if (which != 0 && which != 1) throw Error(TBEM_ERR_ARG, "which must be 0 or 1");
+    if (mthd->sinh_order <= 0 || mthd->obs_near_order <= 0 || mthd->obs_far_order <= 0 ||
+        mthd->src_far_order <= 0 || mthd->n_singular_steps < 2 || mthd->n_singular_steps > 32 ||
+        !(mthd->far_threshold > 0))
+        throw Error(TBEM_ERR_ARG, "bad integrator parameters");
+}
+
 }  // namespace
 }  // namespace tbem
 
@@ -364,14 +558,9 @@ int tbem_nearfield_create(int kernel, const double* kernel_params, const double*
     if (!out || !mthd) return TBEM_ERR_ARG;
     *out = nullptr;
     try {
-        if (!kernel_valid(kernel)) throw Error(TBEM_ERR_ARG, "unknown kernel id");
-        if (which != 0 && which != 1) throw Error(TBEM_ERR_ARG, "which must be 0 or 1");
+        validate(kernel, which, mthd);
         if (n_vertices < 0 || n_obs_facets < 0 || n_src_facets < 0 || n_all_facets < 0)
             throw Error(TBEM_ERR_ARG, "negative count");
-        if (mthd->sinh_order <= 0 || mthd->obs_near_order <= 0 || mthd->obs_far_order <= 0 ||
-            mthd->src_far_order <= 0 || mthd->n_singular_steps < 2 || mthd->n_singular_steps > 32 ||
-            !(mthd->far_threshold > 0))
-            throw Error(TBEM_ERR_ARG, "bad integrator parameters");
         const int dim = kernel_space_dim(kernel), R = kernel_dim(kernel);
         const double mu = (kernel_params && R > 1) ? kernel_params[0] : 1.0;
         const double nu = (kernel_params && R > 1) ? kernel_params[1] : 0.25;
@@ -381,181 +570,74 @@ int tbem_nearfield_create(int kernel, const double* kernel_params, const double*
         nf::FacetSet all_set(all, dim), src_set(src, dim);
         const int order = (int)(which == 0 ? mthd->obs_near_order : mthd->obs_far_order);
         const nf::ObsPoints pts = nf::galerkin_obs_points(obs, all_set, order, dim);
-        const long n_pts = (long)pts.loc.size();
+        return build_nearfield_csr(kernel, dim, R, mu, nu, pts, src, src_set, mthd, which, out);
+    } catch (const tbem::Error& e) {
+        tbem::set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        tbem::set_last_error("host allocation failed");
+        return TBEM_ERR_ALLOC;
+    }
+}
 
-        // terms: every observation point against its nearfield source facets,
-        // in the reference's loop order
-        std::vector<int> t_obs, t_fac;
-        std::vector<size_t> nearby;
-        size_t nearest = 0;
-        double dist = 0.0;
-        for (long i = 0; i < n_pts; i++) {
-            src_set.find(pts.loc[i], mthd->far_threshold, nearby, nearest, dist);
-            for (size_t f : nearby) {
-                t_obs.push_back((int)i);
-                t_fac.push_back((int)f);
-            }
+long tbem_interior_obs_points(int dim, const double* locs, long n, const double* vertices,
+                              long n_vertices, const long* all_facets, long n_all_facets,
+                              double* dirs)
+{
+    using namespace tbem;
+    try {
+        if ((dim != 2 && dim != 3) || n < 0 || n_vertices < 0 || n_all_facets < 0 || (n > 0 && !locs))
+            throw Error(TBEM_ERR_ARG, "bad argument");
+        const auto all = read_facets(vertices, n_vertices, all_facets, n_all_facets, dim);
+        nf::FacetSet all_set(all, dim);
+        for (long i = 0; i < n; i++) {
+            nf::V3 p{{0, 0, 0}};
+            for (int d = 0; d < dim; d++) p[d] = locs[dim * i + d];
+            const nf::V3 r = nf::limit_direction(p, all_set, dim);
+            if (dirs)
+                for (int d = 0; d < dim; d++) dirs[dim * i + d] = r[d];
         }
-        const long n_terms = (long)t_obs.size();
-        const int E = dim * R * R;
-        // classify every term as IntegrationStrategy::compute_term does
-        // (cpp/integral_term.cpp:33-53) and list its evaluations: one for a far
-        // or near term, n_steps (at the stepped-back points, get_step_loc,
-        // cpp/integral_term.cpp:55-60) for a singular one
-        const int n_steps = (int)mthd->n_singular_steps;
-        std::vector<long> first(n_terms);
-        std::vector<char> sing(n_terms, 0);
-        std::vector<int> i_obs, i_fac, i_near;
-        std::vector<double> iloc;
-        auto add_item = [&](long o, long f, int nearflag, const nf::V3& at) {
-            i_obs.push_back((int)o);
-            i_fac.push_back((int)f);
-            i_near.push_back(nearflag);
-            for (int d = 0; d < 3; d++) iloc.push_back(at[d]);
-        };
-        for (long t = 0; t < n_terms; t++) {
-            const long o = t_obs[t], f = t_fac[t];
-            first[t] = (long)i_obs.size();
-            const nf::V3& p = pts.loc[o];
-            if (which == 1) {  // -compute_farfield for every term
-                add_item(o, f, 0, p);
-                continue;
+        return n;
+    } catch (const tbem::Error& e) {
+        tbem::set_last_error(e.what());
+        return e.code;
+    }
+}
+
+int tbem_nearfield_points_create(int kernel, const double* kernel_params, const double* obs_locs,
+                                 const double* obs_normals, long n_obs, const double* vertices,
+                                 long n_vertices, const long* src_facets, long n_src_facets,
+                                 const long* all_facets, long n_all_facets,
+                                 const TbemSinhIntegrator* mthd, int which, TbemCsr** out)
+{
+    using namespace tbem;
+    if (!out || !mthd) return TBEM_ERR_ARG;
+    *out = nullptr;
+    try {
+        validate(kernel, which, mthd);
+        if (n_obs < 0 || n_vertices < 0 || n_src_facets < 0 || n_all_facets < 0)
+            throw Error(TBEM_ERR_ARG, "negative count");
+        if (n_obs > 0 && (!obs_locs || !obs_normals)) throw Error(TBEM_ERR_ARG, "null point array");
+        const int dim = kernel_space_dim(kernel), R = kernel_dim(kernel);
+        const double mu = (kernel_params && R > 1) ? kernel_params[0] : 1.0;
+        const double nu = (kernel_params && R > 1) ? kernel_params[1] : 0.25;
+        const auto src = read_facets(vertices, n_vertices, src_facets, n_src_facets, dim);
+        const auto all = read_facets(vertices, n_vertices, all_facets, n_all_facets, dim);
+        nf::FacetSet all_set(all, dim), src_set(src, dim);
+        // interior_obs_pts (cpp/nearfield_operator.h:27-40): the given points and
+        // normals with their limit directions against all_facets
+        nf::ObsPoints pts;
+        for (long i = 0; i < n_obs; i++) {
+            nf::V3 p{{0, 0, 0}}, nn{{0, 0, 0}};
+            for (int d = 0; d < dim; d++) {
+                p[d] = obs_locs[dim * i + d];
+                nn[d] = obs_normals[dim * i + d];
             }
-            const double dist = nf::closest_point(p, src[f], dim).dist;
-            const double ls = src_set.info(f).length_scale;
-            if (dist < mthd->far_threshold * ls) {
-                double d2 = 0.0;
-                for (int d = 0; d < dim; d++) d2 += pts.dir[o][d] * pts.dir[o][d];
-                if (dist < 1.0 * ls && d2 > 1e-10 * ls) {
-                    sing[t] = 1;
-                    for (int k = 0; k < n_steps; k++) {
-                        const double step = 1.0 / std::pow(2.0, (double)k);
-                        const double sd = 1.0 * step;
-                        nf::V3 q;
-                        for (int d = 0; d < 3; d++) q[d] = p[d] + sd * pts.dir[o][d];
-                        add_item(o, f, 1, q);
-                    }
-                } else {
-                    if (!(dist > 0.0))
-                        throw Error(TBEM_ERR_ARG, "an observation point lies on a source facet without a "
-                                                  "limit direction (the reference asserts here)");
-                    add_item(o, f, 1, p);
-                }
-            } else {
-                add_item(o, f, 0, p);
-            }
+            pts.loc.push_back(p);
+            pts.normal.push_back(nn);
+            pts.dir.push_back(nf::limit_direction(p, all_set, dim));
         }
-        const long n_items = (long)i_obs.size();
-        std::vector<double> ivals((size_t)n_items * E);
-        if (n_items > 0) {
-            std::vector<double> nrm, fac, ls, jac, fn;
-            for (long i = 0; i < n_pts; i++)
-                for (int d = 0; d < 3; d++) nrm.push_back(pts.normal[i][d]);
-            for (size_t f = 0; f < src.size(); f++) {
-                for (int v = 0; v < 3; v++)
-                    for (int d = 0; d < 3; d++) fac.push_back(src[f].c[v][d]);
-                const nf::FacetInfo& fi = src_set.info(f);
-                ls.push_back(fi.length_scale);
-                jac.push_back(fi.jacobian);
-                for (int d = 0; d < 3; d++) fn.push_back(fi.normal[d]);
-            }
-            std::vector<double> fx, fw;
-            nf::gauss_facet(dim, (int)mthd->src_far_order, fx, fw);
-            DBuf<double> d_gx, d_gw, d_fx, d_fw, d_loc, d_nrm, d_fac, d_ls, d_jac, d_fn, d_out;
-            DBuf<int> d_io, d_if, d_in, d_err;
-            d_gx.upload(gauss_table(0));
-            d_gw.upload(gauss_table(1));
-            d_fx.upload(fx);
-            d_fw.upload(fw);
-            d_loc.upload(iloc);
-            d_nrm.upload(nrm);
-            d_fac.upload(fac);
-            d_ls.upload(ls);
-            d_jac.upload(jac);
-            d_fn.upload(fn);
-            d_io.upload(i_obs);
-            d_if.upload(i_fac);
-            d_in.upload(i_near);
-            d_err.upload(std::vector<int>(1, 0));
-            d_out.alloc(ivals.size());
-            NfArgs a{};
-            a.kid = kernel;
-            a.kp = make_kparams(kernel, mu, nu);
-            a.sinh_order = (int)mthd->sinh_order;
-            a.gx = d_gx.p;
-            a.gw = d_gw.p;
-            a.fx = d_fx.p;
-            a.fw = d_fw.p;
-            a.n_far = (int)fw.size();
-            a.loc = d_loc.p;
-            a.nrm = d_nrm.p;
-            a.fac = d_fac.p;
-            a.ls = d_ls.p;
-            a.jac = d_jac.p;
-            a.fn = d_fn.p;
-            a.i_obs = d_io.p;
-            a.i_fac = d_if.p;
-            a.i_near = d_in.p;
-            a.n_items = n_items;
-            a.out = d_out.p;
-            a.err = d_err.p;
-            if (dim == 2 && R == 1) launch<2, 1>(a);
-            else if (dim == 2) launch<2, 2>(a);
-            else if (R == 1) launch<3, 1>(a);
-            else launch<3, 3>(a);
-            TBEM_CK(cudaDeviceSynchronize());
-            int err = 0;
-            TBEM_CK(cudaMemcpy(&err, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
-            if (err & 1)
-                throw Error(TBEM_ERR_ARG, "a stepped-back Richardson point lies on a source facet");
-            if (err & 2)
-                throw Error(TBEM_ERR_ARG, "a sinh rule needs more than 512 Gauss points "
-                                          "(observation point too close to a facet)");
-            TBEM_CK(cudaMemcpy(ivals.data(), d_out.p, ivals.size() * sizeof(double),
-                               cudaMemcpyDeviceToHost));
-        }
-        // per term: the evaluation, its negation (farfield correction) or the
-        // Richardson limit of its steps (richardson_limit, cpp/richardson.h:10-34)
-        std::vector<double> vals((size_t)n_terms * E);
-        std::vector<double> tab(n_steps);
-        for (long t = 0; t < n_terms; t++) {
-            for (int e = 0; e < E; e++) {
-                double v;
-                if (sing[t]) {
-                    for (int k = 0; k < n_steps; k++) tab[k] = ivals[(size_t)(first[t] + k) * E + e];
-                    for (int m = 1; m < n_steps; m++) {
-                        const double mult = std::pow(2.0, m);
-                        const double factor = 1.0 / (mult - 1.0);
-                        for (int i = 0; i < n_steps - m; i++) tab[i] = factor * (mult * tab[i + 1] - tab[i]);
-                    }
-                    v = tab[0];
-                } else {
-                    v = ivals[(size_t)first[t] * E + e];
-                }
-                vals[(size_t)t * E + e] = which == 1 ? -v : v;
-            }
-        }
-        // COO entries in the reference's order (cpp/nearfield_operator.h:59-84),
-        // rows d1 * n_pts + point, columns d2 * n_dofs + facet * dim + basis;
-        // a stable sort by row gives csr_from_coo's layout
-        const long n_dofs = (long)src.size() * dim;
-        const long n_rows = R * n_pts, n_cols = R * n_dofs;
-        std::vector<long> count(n_rows + 1, 0);
-        for (long t = 0; t < n_terms; t++)
-            for (int d1 = 0; d1 < R; d1++) count[d1 * n_pts + t_obs[t] + 1] += dim * R;
-        for (long r = 0; r < n_rows; r++) count[r + 1] += count[r];
-        std::vector<long> fill(count.begin(), count.end() - 1), cols(count[n_rows]);
-        std::vector<double> v(count[n_rows]);
-        for (long t = 0; t < n_terms; t++)
-            for (int b = 0; b < dim; b++)
-                for (int d1 = 0; d1 < R; d1++)
-                    for (int d2 = 0; d2 < R; d2++) {
-                        const long row = d1 * n_pts + t_obs[t];
-                        const long k = fill[row]++;
-                        cols[k] = d2 * n_dofs + (long)t_fac[t] * dim + b;
-                        v[k] = vals[(size_t)t * E + (b * R + d1) * R + d2];
-                    }
-        return tbem_csr_create(n_rows, n_cols, v.data(), cols.data(), count.data(), out);
+        return build_nearfield_csr(kernel, dim, R, mu, nu, pts, src, src_set, mthd, which, out);
     } catch (const tbem::Error& e) {
         tbem::set_last_error(e.what());
         return e.code;

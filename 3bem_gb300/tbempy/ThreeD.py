@@ -554,6 +554,7 @@ class IntegralOperator(OperatorI):
 # Galerkin and interpolation operators, boundary_operator)
 from .bem import (Mesh, IntegrationStrategy, boundary_operator, farfield_correction_operator,  # noqa: E402,F401
                   galerkin_csr, galerkin_obs_points, galerkin_operator, gauss_facet,
-                  interpolation_csr, interpolation_operator,
+                  interpolation_csr, interpolation_operator, dense_interior_operator,
+                  interior_limit_directions, mass_csr, mass_operator_scalar, mass_operator_tensor,
                   make_adaptive_integrator, make_sinh_integrator, nearfield_operator,
                   quadrature_points)

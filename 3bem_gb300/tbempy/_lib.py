@@ -79,6 +79,8 @@ SIGNATURES = {
     "tbem_nearfield_create": (_I, [_I, _P, _P, _L, _P, _L, _P, _L, _P, _L, _P, _I, _P]),
     "tbem_gauss_facet": (_L, [_I, _L, _P, _P]),
     "tbem_galerkin_obs_points": (_L, [_I, _P, _L, _P, _L, _P, _L, _L, _P, _P, _P]),
+    "tbem_nearfield_points_create": (_I, [_I, _P, _P, _P, _L, _P, _L, _P, _L, _P, _L, _P, _I, _P]),
+    "tbem_interior_obs_points": (_L, [_I, _P, _L, _P, _L, _P, _L, _P]),
     "tbem_csr_destroy": (None, [_P]),
     "tbem_integral_create": (_I, [_P, _P, _P, _P, _P, _P]),
     "tbem_integral_apply": (_I, [_P, _P, _P, _I, _P]),

@@ -257,3 +257,83 @@ def boundary_operator(obs_mesh, src_mesh, mthd, fmm_config, all_mesh, precision=
     sl, sn, sw = quadrature_points(src_mesh, mthd.src_far_order)
     far = FMMOperator(K, ol, on, sl, sn, sw, fmm_config, precision=precision)
     return IntegralOperator(_product(g_near, near), _product(g_far, corr), g_far, far, interp)
+
+
+def interior_limit_directions(locs, all_mesh):
+    """Limit (Richardson) directions of given points against a mesh, as
+    interior_obs_pts computes them (cpp/nearfield_operator.h:27-40); [n, dim]."""
+    dim = all_mesh.dim
+    locs = np.ascontiguousarray(locs, dtype=np.float64).reshape(-1, dim)
+    af = np.ascontiguousarray(all_mesh.facets)
+    dirs = np.zeros_like(locs)
+    check(_L.lib().tbem_interior_obs_points(dim, _ptr(locs), len(locs), _ptr(all_mesh.vertices),
+                                            len(all_mesh.vertices), _ptr(af), len(af), _ptr(dirs)))
+    return dirs
+
+
+def _nearfield_points(locs, normals, src_mesh, mthd, all_mesh, which):
+    if mthd.kind != "sinh":
+        raise NotImplementedError("adaptive Gauss-Lobatto nearfield quadrature is not built on "
+                                  "the device; use make_sinh_integrator")
+    dim = src_mesh.dim
+    locs = np.ascontiguousarray(locs, dtype=np.float64).reshape(-1, dim)
+    normals = np.ascontiguousarray(normals, dtype=np.float64).reshape(-1, dim)
+    v, (sf, af) = _merge(src_mesh, all_mesh)
+    h = C.c_void_p()
+    cfg = mthd._c()
+    check(_L.lib().tbem_nearfield_points_create(
+        mthd.K.kernel_id, _ptr(mthd.K.params()), _ptr(locs), _ptr(normals), len(locs), _ptr(v),
+        len(v), _ptr(sf), len(sf), _ptr(af), len(af), C.byref(cfg), int(which), C.byref(h)))
+    return SparseOperator._from_handle(h)
+
+
+def _identity(n):
+    return SparseOperator(n, n, np.ones(n), np.arange(n, dtype=np.int64),
+                          np.arange(n + 1, dtype=np.int64))
+
+
+def dense_interior_operator(locs, normals, src_mesh, mthd, all_mesh, fmm_config=None):
+    """The field of a boundary density at given points
+    (dense_interior_operator, cpp/integral_operator.h:132-158):
+    A = N + C + F I, with N and C integrated on the GPU for the points (their
+    limit directions taken against all_mesh) and F the direct N-body operator
+    over the source quadrature points -- or the GPU FMM when fmm_config is
+    given.  Applied matrix-free on the device (the name is the reference's;
+    the reference returns the assembled dense matrix)."""
+    K = mthd.K
+    locs = np.ascontiguousarray(locs, dtype=np.float64).reshape(-1, src_mesh.dim)
+    normals = np.ascontiguousarray(normals, dtype=np.float64).reshape(-1, src_mesh.dim)
+    near = _nearfield_points(locs, normals, src_mesh, mthd, all_mesh, 0)
+    corr = _nearfield_points(locs, normals, src_mesh, mthd, all_mesh, 1)
+    interp = interpolation_operator(K.tensor_dim, src_mesh, mthd.src_far_order)
+    sl, sn, sw = quadrature_points(src_mesh, mthd.src_far_order)
+    if fmm_config is None:
+        from .ThreeD import DirectOperator
+        far = DirectOperator(K, locs, normals, sl, sn, sw)
+    else:
+        far = FMMOperator(K, locs, normals, sl, sn, sw, fmm_config)
+    return IntegralOperator(near, corr, _identity(K.tensor_dim * len(locs)), far, interp)
+
+
+def mass_csr(n_components, mesh, n_q):
+    """mass_operator (cpp/mass_operator.h:10-19): the Galerkin operator times
+    the interpolation operator on the same Gauss rule, as host CSR arrays."""
+    import scipy.sparse as sp
+    g = galerkin_csr(n_components, mesh, n_q)
+    i = interpolation_csr(n_components, mesh, n_q)
+    a = sp.csr_matrix((g[2], g[3], g[4]), shape=(g[0], g[1]))
+    b = sp.csr_matrix((i[2], i[3], i[4]), shape=(i[0], i[1]))
+    p = (a @ b).tocsr()
+    p.sort_indices()
+    return (p.shape[0], p.shape[1], p.data, p.indices.astype(np.int64), p.indptr.astype(np.int64))
+
+
+def mass_operator_scalar(mesh, n_q):
+    """mass_operator<dim,1,1> (python_wrapper/dimension.cpp:93)."""
+    return SparseOperator(*mass_csr(1, mesh, n_q))
+
+
+def mass_operator_tensor(mesh, n_q):
+    """mass_operator<dim,dim,dim> (python_wrapper/dimension.cpp:94)."""
+    return SparseOperator(*mass_csr(mesh.dim, mesh, n_q))
+

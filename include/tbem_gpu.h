@@ -316,6 +316,24 @@ int tbem_nearfield_create(int kernel, const double* kernel_params, const double*
                           long n_all_facets, const TbemSinhIntegrator* mthd, int which,
                           TbemCsr** out);
 
+/* The same matrices for given observation points (the reference's
+ * interior_obs_pts, cpp/nearfield_operator.h:27-40, as dense_interior_operator
+ * uses them, cpp/integral_operator.h:132-158): obs_locs / obs_normals
+ * [n_obs][dim], their limit directions found against all_facets.  Rows
+ * R * n_obs. */
+int tbem_nearfield_points_create(int kernel, const double* kernel_params, const double* obs_locs,
+                                 const double* obs_normals, long n_obs, const double* vertices,
+                                 long n_vertices, const long* src_facets, long n_src_facets,
+                                 const long* all_facets, long n_all_facets,
+                                 const TbemSinhIntegrator* mthd, int which, TbemCsr** out);
+
+/* Limit (Richardson) directions of given points against all_facets
+ * (decide_limit_dir, cpp/limit_direction.cpp:87-147, with the constants
+ * interior_obs_pts passes); dirs [n][dim]; returns n (host only). */
+long tbem_interior_obs_points(int dim, const double* locs, long n, const double* vertices,
+                              long n_vertices, const long* all_facets, long n_all_facets,
+                              double* dirs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -417,3 +417,53 @@ def ref_galerkin_interp(which, vertices, facets, n_components, order):
     rows = np.zeros(shape[0] + 1, dtype=np.int64)
     fn(*args, _ptr(vals), _ptr(cols), _ptr(rows), nnz)
     return int(shape[0]), int(shape[1]), vals, cols, rows
+
+
+def ref_interior_dirs(locs, vertices, facets):
+    """The reference's interior_obs_pts limit directions, [n][3]."""
+    dim = np.asarray(vertices).shape[1]
+    v, f = _mesh_args(vertices, facets)
+    l = _pts3(locs)
+    fn = _ref().fn("interior_dirs", _L, [_I, _P, _L, _P, _L, _P, _L, _P])
+    out = np.zeros((len(l), 3))
+    fn(dim, _ptr(l), len(l), _ptr(v), len(v), _ptr(f), len(f), _ptr(out))
+    return out
+
+
+def ref_mass(vertices, facets, R, n_q):
+    """The reference's mass_operator<dim,R,R>: (n_rows, n_cols, values, cols, rowptr)."""
+    dim = np.asarray(vertices).shape[1]
+    v, f = _mesh_args(vertices, facets)
+    fn = _ref().fn("mass", _L, [_I, _L, _P, _L, _P, _L, _L, _P, _P, _P, _P, _L])
+    shape = np.zeros(2, dtype=np.int64)
+    args = [dim, R, _ptr(v), len(v), _ptr(f), len(f), n_q, _ptr(shape)]
+    nnz = fn(*args, None, None, None, 0)
+    vals = np.zeros(nnz)
+    cols = np.zeros(nnz, dtype=np.int64)
+    rows = np.zeros(shape[0] + 1, dtype=np.int64)
+    fn(*args, _ptr(vals), _ptr(cols), _ptr(rows), nnz)
+    return int(shape[0]), int(shape[1]), vals, cols, rows
+
+
+def ref_nearfield_points(kernel, vertices, facets, locs, normals, sinh_order=5, obs_near_order=2,
+                         obs_far_order=2, src_far_order=2, n_singular_steps=8, far_threshold=3.0,
+                         which=0, mu=1.0, nu=0.25):
+    """The reference's nearfield (which 0) / correction (1) CSR for given points."""
+    dim = np.asarray(vertices).shape[1]
+    k = kernel_id(kernel, dim)
+    v, f = _mesh_args(vertices, facets)
+    l, n = _pts3(locs), _pts3(normals)
+    fn = _ref().fn("nearfield_points", _L, [_I, _D, _D, _I, _P, _L, _P, _L, _P, _P, _L, _L, _L, _L,
+                                            _L, _L, _D, _I, _P, _P, _P, _P, _L])
+    shape = np.zeros(2, dtype=np.int64)
+    args = [k, mu, nu, dim, _ptr(v), len(v), _ptr(f), len(f), _ptr(l), _ptr(n), len(l), sinh_order,
+            obs_near_order, obs_far_order, src_far_order, n_singular_steps, far_threshold, which,
+            _ptr(shape)]
+    nnz = fn(*args, None, None, None, 0)
+    if nnz < 0:
+        raise ValueError("reference nearfield failed")
+    vals = np.zeros(nnz)
+    cols = np.zeros(nnz, dtype=np.int64)
+    rows = np.zeros(shape[0] + 1, dtype=np.int64)
+    fn(*args, _ptr(vals), _ptr(cols), _ptr(rows), nnz)
+    return int(shape[0]), int(shape[1]), vals, cols, rows

@@ -16,6 +16,7 @@
 #include "elastic_kernels.h"
 #include "galerkin_operator.h"
 #include "interpolation_operator.h"
+#include "mass_operator.h"
 #include "identity_kernels.h"
 #include "integral_term.h"
 #include "laplace_kernels.h"
@@ -66,6 +67,27 @@ Csr build(const Kernel<dim, R, C>& K, const Mesh<dim>& m, const Strategy& s, int
 {
     auto mthd = make_strategy(s, K);
     auto obs = galerkin_obs_pts(m, which == 0 ? mthd.obs_near_quad : mthd.obs_far_quad, m);
+    SparseOperator op = which == 0 ? make_nearfield_operator(obs, m, mthd)
+                                   : make_farfield_correction_operator(obs, m, mthd);
+    Csr c;
+    c.n_rows = (long)op.n_rows();
+    c.n_cols = (long)op.n_cols();
+    c.values = op.values;
+    c.cols.assign(op.column_indices.begin(), op.column_indices.end());
+    c.rowptr.assign(op.row_ptrs.begin(), op.row_ptrs.end());
+    return c;
+}
+
+// the same for given points (interior_obs_pts) against the mesh
+template <size_t dim, size_t R, size_t C>
+Csr build_points(const Kernel<dim, R, C>& K, const Mesh<dim>& m, const Strategy& s, int which,
+                 const double* locs, const double* nrms, long n)
+{
+    auto mthd = make_strategy(s, K);
+    std::vector<Vec<double, dim>> l(n), nn(n);
+    for (long i = 0; i < n; i++)
+        for (size_t d = 0; d < dim; d++) { l[i][d] = locs[3 * i + d]; nn[i][d] = nrms[3 * i + d]; }
+    auto obs = interior_obs_pts(l, nn, m);
     SparseOperator op = which == 0 ? make_nearfield_operator(obs, m, mthd)
                                    : make_farfield_correction_operator(obs, m, mthd);
     Csr c;
@@ -189,6 +211,49 @@ long ref_obs_points(int dim, const double* verts, long n_verts, const long* face
                     : obs_points(make_mesh<3>(verts, n_verts, facets, n_facets), order, locs, normals, dirs);
 }
 
+// The nearfield / correction operator for given points [n][3] (the
+// interior_obs_pts path of dense_interior_operator,
+// cpp/integral_operator.h:132-158); CSR when cap >= nnz; returns nnz.
+long ref_nearfield_points(int kernel, double mu, double nu, int dim, const double* verts,
+                          long n_verts, const long* facets, long n_facets, const double* locs,
+                          const double* nrms, long n, long sinh_order, long obs_near_order,
+                          long obs_far_order, long src_far_order, long n_singular_steps,
+                          double far_threshold, int which, long* shape, double* values,
+                          long* cols, long* rowptr, long cap)
+{
+    Strategy s{1, 0.0, sinh_order, obs_near_order, obs_far_order, src_far_order, n_singular_steps,
+               far_threshold};
+    int saved = omp_get_max_threads();
+    omp_set_num_threads(1);
+    Csr c{-1};
+    if (dim == 3) {
+        auto m = make_mesh<3>(verts, n_verts, facets, n_facets);
+        switch (kernel) {
+        case 0: c = build_points(LaplaceSingle<3>(), m, s, which, locs, nrms, n); break;
+        case 1: c = build_points(LaplaceDouble<3>(), m, s, which, locs, nrms, n); break;
+        case 2: c = build_points(ElasticDisplacement<3>(mu, nu), m, s, which, locs, nrms, n); break;
+        case 3: c = build_points(ElasticTraction<3>(mu, nu), m, s, which, locs, nrms, n); break;
+        }
+    } else {
+        auto m = make_mesh<2>(verts, n_verts, facets, n_facets);
+        switch (kernel) {
+        case 16: c = build_points(LaplaceSingle<2>(), m, s, which, locs, nrms, n); break;
+        case 17: c = build_points(LaplaceDouble<2>(), m, s, which, locs, nrms, n); break;
+        case 19: c = build_points(ElasticDisplacement<2>(mu, nu), m, s, which, locs, nrms, n); break;
+        }
+    }
+    omp_set_num_threads(saved);
+    if (c.n_rows < 0) return -1;
+    const long nnz = (long)c.values.size();
+    if (shape) { shape[0] = c.n_rows; shape[1] = c.n_cols; }
+    if (cap >= nnz && values) {
+        std::memcpy(values, c.values.data(), nnz * sizeof(double));
+        std::memcpy(cols, c.cols.data(), nnz * sizeof(long));
+        std::memcpy(rowptr, c.rowptr.data(), (c.n_rows + 1) * sizeof(long));
+    }
+    return nnz;
+}
+
 // One IntegrationStrategy::compute_term (cpp/integral_term.cpp:33-53) for an
 // observation point (loc, normal, Richardson direction, 3-vectors) against
 // one facet ([dim][3]); out [dim basis][R][C].  Returns dim * R * C or -1.
@@ -233,6 +298,45 @@ long ref_galerkin_interp(int which, int dim, long n_components, const double* ve
     SparseOperator op = dim == 2
         ? build(make_mesh<2>(verts, n_verts, facets, n_facets), gauss_facet<2>((size_t)order))
         : build(make_mesh<3>(verts, n_verts, facets, n_facets), gauss_facet<3>((size_t)order));
+    const long nnz = (long)op.values.size();
+    if (shape) { shape[0] = (long)op.n_rows(); shape[1] = (long)op.n_cols(); }
+    if (cap >= nnz && values) {
+        std::memcpy(values, op.values.data(), nnz * sizeof(double));
+        for (long k = 0; k < nnz; k++) cols[k] = (long)op.column_indices[k];
+        for (size_t r = 0; r < op.row_ptrs.size(); r++) rowptr[r] = (long)op.row_ptrs[r];
+    }
+    return nnz;
+}
+
+// interior_obs_pts' limit directions (cpp/nearfield_operator.h:27-40) for
+// given points [n][3] against a mesh; dirs [n][3].
+long ref_interior_dirs(int dim, const double* locs, long n, const double* verts, long n_verts,
+                       const long* facets, long n_facets, double* dirs)
+{
+    auto run = [&](auto m, auto tag) {
+        constexpr size_t D = decltype(tag)::value;
+        std::vector<Vec<double, D>> l(n), nn(n);
+        for (long i = 0; i < n; i++)
+            for (size_t d = 0; d < D; d++) { l[i][d] = locs[3 * i + d]; nn[i][d] = 0.0; }
+        auto pts = interior_obs_pts(l, nn, m);
+        for (long i = 0; i < n; i++)
+            for (size_t d = 0; d < 3; d++) dirs[3 * i + d] = d < D ? pts[i].richardson_dir[d] : 0.0;
+    };
+    if (dim == 2) run(make_mesh<2>(verts, n_verts, facets, n_facets), std::integral_constant<size_t, 2>());
+    else run(make_mesh<3>(verts, n_verts, facets, n_facets), std::integral_constant<size_t, 3>());
+    return n;
+}
+
+// mass_operator<dim,R,R> (cpp/mass_operator.h:10-19); CSR when cap >= nnz.
+long ref_mass(int dim, long R, const double* verts, long n_verts, const long* facets,
+              long n_facets, long n_q, long* shape, double* values, long* cols, long* rowptr,
+              long cap)
+{
+    SparseOperator op = dim == 2
+        ? (R == 1 ? mass_operator<2, 1, 1>(make_mesh<2>(verts, n_verts, facets, n_facets), n_q)
+                  : mass_operator<2, 2, 2>(make_mesh<2>(verts, n_verts, facets, n_facets), n_q))
+        : (R == 1 ? mass_operator<3, 1, 1>(make_mesh<3>(verts, n_verts, facets, n_facets), n_q)
+                  : mass_operator<3, 3, 3>(make_mesh<3>(verts, n_verts, facets, n_facets), n_q));
     const long nnz = (long)op.values.size();
     if (shape) { shape[0] = (long)op.n_rows(); shape[1] = (long)op.n_cols(); }
     if (cap >= nnz && values) {

@@ -235,12 +235,60 @@ def make_nearfield_cases():
         print("wrote nearfield", name, out["shape0"], len(out["values0"]), len(out["values1"]))
 
 
+def _dense(nr, nc, vals, cols, rows):
+    a = np.zeros((nr, nc))
+    for r in range(nr):
+        np.add.at(a[r], cols[rows[r]:rows[r + 1]], vals[rows[r]:rows[r + 1]])
+    return a
+
+
+def make_interior_cases():
+    """dense_interior_operator's nearfield / correction for given points (on the
+    surface, just off it, inside, far) and the mass operators, from the
+    reference; plus the reference's one-ulp sensitivity as for the nearfield."""
+    ms = nearfield_meshes()
+    rng = np.random.default_rng(21)
+    cases = [("lapd_ico", "ico", "LaplaceDouble", 1.0, 0.25, 5, 2, 2, 2, 8, 3.0),
+             ("laps2_circle", "circle", "LaplaceSingle", 1.0, 0.25, 10, 2, 2, 3, 8, 3.0)]
+    for name, mesh, kernel, mu, nu, so, on, of, sf, st, ft in cases:
+        v, f = ms[mesh]
+        dim = v.shape[1]
+        loc, nrm, _ = oracle.ref_obs_points(v, f, 2)
+        loc, nrm = loc[:, :dim], nrm[:, :dim]
+        pts = np.concatenate([loc[:8], loc[8:16] * (1 + 1e-4), loc[16:24] * 0.97,
+                              rng.normal(size=(6, dim)) * 0.3, rng.normal(size=(4, dim)) * 3])
+        nrms = np.concatenate([nrm[:24], np.tile(np.eye(dim)[:1], (10, 1))])
+        out = dict(kernel=kernel, mu=mu, nu=nu, vertices=v, facets=f, sinh_order=so,
+                   obs_near_order=on, obs_far_order=of, src_far_order=sf, n_singular_steps=st,
+                   far_threshold=ft, locs=pts, normals=nrms,
+                   dirs=oracle.ref_interior_dirs(pts, v, f)[:, :dim])
+        vp = v * (1 + 2.0 ** -52 * np.random.default_rng(0).choice([-1, 1], size=v.shape))
+        for which in (0, 1):
+            res = oracle.ref_nearfield_points(kernel, v, f, pts, nrms, so, on, of, sf, st, ft, which,
+                                              mu, nu)
+            out["shape%d" % which] = np.array(res[:2])
+            out["values%d" % which], out["cols%d" % which], out["rowptr%d" % which] = res[2:]
+            pr = oracle.ref_nearfield_points(kernel, vp, f, pts, nrms, so, on, of, sf, st, ft, which,
+                                             mu, nu)
+            a, b = _dense(*res), _dense(*pr)
+            out["ulp_floor%d" % which] = np.abs(a - b).max() / max(np.abs(a).max(), 1e-300)
+        for R in sorted({1, dim}):
+            for nq in (2, 3):
+                res = oracle.ref_mass(v, f, R, nq)
+                out["mass_%d_%d_shape" % (R, nq)] = np.array(res[:2])
+                (out["mass_%d_%d_values" % (R, nq)], out["mass_%d_%d_cols" % (R, nq)],
+                 out["mass_%d_%d_rowptr" % (R, nq)]) = res[2:]
+        np.savez_compressed(os.path.join(HERE, "interior_%s.npz" % name), **out)
+        print("wrote interior", name, out["shape0"], len(out["values0"]), out["ulp_floor0"])
+
+
 def main(ref_root="/root/reference", which="all"):
     oracle.build()
     if oracle.build_ref(ref_root) is None:
         raise SystemExit("the reference checkout is needed to regenerate the fixtures")
     if which == "nearfield":
         make_nearfield_cases()
+        make_interior_cases()
         return
     for case in CASES_2D:
         data = make_case(*case)

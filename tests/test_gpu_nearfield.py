@@ -82,3 +82,39 @@ def test_boundary_operator_assembles_and_matches_dense_chain():
     ones = np.ones(m.n_dofs())
     g = A.galerkin.apply(np.ones(A.galerkin.n_cols()))  # integrals of the basis functions
     assert np.abs(A.apply(ones)).max() <= 5e-3 * np.abs(g).max()
+
+
+INTERIOR = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "interior_*.npz")))
+
+
+@pytest.mark.parametrize("path", INTERIOR, ids=[os.path.basename(p)[9:-4] for p in INTERIOR])
+def test_interior_operator_matches_reference(path):
+    """dense_interior_operator: its nearfield and correction matrices against
+    the reference's (same tolerance as above), and its apply against
+    N x + C x + F (I x) with F the FP64 direct sum of the oracle."""
+    from oracle import oracle
+    from tbempy import ThreeD
+    g = dict(np.load(path))
+    m = ThreeD.Mesh(g["vertices"], g["facets"])
+    K = kernel_of(g, m.dim)
+    mthd = ThreeD.make_sinh_integrator(int(g["sinh_order"]), int(g["obs_near_order"]),
+                                       int(g["obs_far_order"]), int(g["src_far_order"]),
+                                       int(g["n_singular_steps"]), float(g["far_threshold"]), K)
+    A = ThreeD.dense_interior_operator(g["locs"], g["normals"], m, mthd, m)
+    for which, op in ((0, A.nearfield), (1, A.farfield_correction)):
+        assert (op.n_rows(), op.n_cols()) == tuple(g["shape%d" % which])
+        assert np.array_equal(op.row_ptrs(), g["rowptr%d" % which])
+        assert np.array_equal(op.column_indices(), g["cols%d" % which])
+        ref = g["values%d" % which]
+        tol = max(1e-10, 100 * float(g["ulp_floor%d" % which])) * np.abs(ref).max()
+        assert np.abs(op.values() - ref).max() <= tol
+    x = np.random.default_rng(3).uniform(-1, 1, A.n_cols())
+    N = dense(g["shape0"], g["values0"], g["cols0"], g["rowptr0"])
+    Cc = dense(g["shape1"], g["values1"], g["cols1"], g["rowptr1"])
+    I = A.interp
+    Id = dense((I.n_rows(), I.n_cols()), I.values(), I.column_indices(), I.row_ptrs())
+    sl, sn, sw = ThreeD.quadrature_points(m, int(g["src_far_order"]))
+    far = oracle.direct(K.kernel_id, g["locs"], g["normals"], sl, sn, sw, Id @ x,
+                        mu=float(g["mu"]), nu=float(g["nu"]))
+    expect = N @ x + Cc @ x + far
+    assert np.linalg.norm(A.apply(x) - expect) <= 1e-10 * np.linalg.norm(expect)

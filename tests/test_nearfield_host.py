@@ -123,3 +123,25 @@ def test_nearfield_create_validates_before_device_use():
         assert not h.value
     assert L.tbem_gauss_facet(4, 3, None, None) == -1
     assert L.tbem_gauss_facet(3, 0, None, None) == -1
+
+
+INTERIOR = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "interior_*.npz")))
+
+
+@pytest.mark.parametrize("path", INTERIOR, ids=[os.path.basename(p)[9:-4] for p in INTERIOR])
+def test_interior_limit_directions_and_mass_operator_match_reference(path):
+    """dense_interior_operator's observation points (interior_obs_pts: points
+    on the surface, just off it, inside and far) get the reference's limit
+    directions bit for bit; mass_operator_scalar / _tensor equal the
+    reference's (cpp/mass_operator.h) in layout and value."""
+    from tbempy import ThreeD
+    g = dict(np.load(path))
+    m = ThreeD.Mesh(g["vertices"], g["facets"])
+    assert np.array_equal(ThreeD.interior_limit_directions(g["locs"], m), g["dirs"])
+    for R in sorted({1, m.dim}):
+        for nq in (2, 3):
+            nr, nc, vals, cols, rows = ThreeD.mass_csr(R, m, nq)
+            key = "mass_%d_%d_" % (R, nq)
+            assert (nr, nc) == tuple(g[key + "shape"])
+            assert np.array_equal(rows, g[key + "rowptr"]) and np.array_equal(cols, g[key + "cols"])
+            assert np.allclose(vals, g[key + "values"], rtol=1e-15, atol=0)
