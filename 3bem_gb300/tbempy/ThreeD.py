@@ -419,6 +419,45 @@ def direct_gradients(K, obs_locs, obs_normals, src_locs, src_normals, src_weight
     return g
 
 
+class DenseOperator(OperatorI):
+    """A dense matrix operator (DenseOperator, cpp/dense_operator.h:11-40;
+    python_wrapper/linalg.cpp:15-20): row-major data of n_rows x n_cols,
+    ``data()`` the flat copy, applied on the GPU (through the CSR kernel, built
+    on the first apply)."""
+
+    def __init__(self, n_rows, n_cols, data):
+        self._shape = (int(n_rows), int(n_cols))
+        self._data = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+        if self._data.size != self._shape[0] * self._shape[1]:
+            raise ValueError("data must hold n_rows * n_cols values")
+        self._op = None
+
+    def n_rows(self):
+        return self._shape[0]
+
+    def n_cols(self):
+        return self._shape[1]
+
+    def n_elements(self):
+        return self._data.size
+
+    def data(self):
+        return self._data.copy()
+
+    def to_dense(self):
+        return self._data.reshape(self._shape).copy()
+
+    def apply(self, x):
+        if self._op is None:
+            nr, nc = self._shape
+            self._op = SparseOperator(nr, nc, self._data, np.tile(np.arange(nc, dtype=np.int64), nr),
+                                      np.arange(nr + 1, dtype=np.int64) * nc)
+        return self._op.apply(x)
+
+    def clone(self):
+        return DenseOperator(self._shape[0], self._shape[1], self._data)
+
+
 class SparseOperator(OperatorI):
     """CSR operator (cpp/sparse_operator.h:44-83) with a GPU apply."""
 
@@ -555,6 +594,7 @@ class IntegralOperator(OperatorI):
 from .bem import (Mesh, IntegrationStrategy, boundary_operator, farfield_correction_operator,  # noqa: E402,F401
                   galerkin_csr, galerkin_obs_points, galerkin_operator, gauss_facet,
                   interpolation_csr, interpolation_operator, dense_interior_operator,
+                  dense_boundary_operator,
                   interior_limit_directions, mass_csr, mass_operator_scalar, mass_operator_tensor,
                   make_adaptive_integrator, make_sinh_integrator, nearfield_operator,
                   quadrature_points)

@@ -10,11 +10,12 @@ operators run in the plain FP64 form.
 """
 import numpy as np
 
-from .ThreeD import (DirectOperator, FMMConfig, FMMGraph, FMMOperator,  # noqa: F401
+from .ThreeD import (DenseOperator, DirectOperator, FMMConfig, FMMGraph, FMMOperator,  # noqa: F401
                      IntegralOperator, IntegrationStrategy, Kernel, Mesh, OperatorI,
                      SparseOperator, boundary_operator, farfield_correction_operator,
                      galerkin_csr, galerkin_obs_points, galerkin_operator, gauss_facet,
                      interpolation_csr, interpolation_operator, dense_interior_operator,
+                     dense_boundary_operator,
                      interior_limit_directions, mass_csr, mass_operator_scalar,
                      mass_operator_tensor, make_adaptive_integrator, make_sinh_integrator,
                      nearfield_operator, quadrature_points)

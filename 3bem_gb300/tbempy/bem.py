@@ -337,3 +337,36 @@ def mass_operator_tensor(mesh, n_q):
     """mass_operator<dim,dim,dim> (python_wrapper/dimension.cpp:94)."""
     return SparseOperator(*mass_csr(mesh.dim, mesh, n_q))
 
+
+def _dense(csr):
+    nr, nc, vals, cols, rows = csr
+    out = np.zeros((nr, nc))
+    for r in range(nr):
+        np.add.at(out[r], cols[rows[r]:rows[r + 1]], vals[rows[r]:rows[r + 1]])
+    return out
+
+
+def dense_boundary_operator(obs_mesh, src_mesh, mthd, all_mesh):
+    """The boundary operator assembled densely with the exact farfield
+    (dense_boundary_operator, cpp/integral_operator.h:100-130):
+    G_far (C + F I) + G_near N, F the direct N-body matrix over the
+    quadrature points.  N and C are integrated on the GPU, F I is the GPU
+    direct sum applied to the columns of I; the products are formed on the
+    host.  Returns a DenseOperator (for small meshes, as in the reference)."""
+    from .ThreeD import DenseOperator, DirectOperator
+    K = mthd.K
+    R = K.tensor_dim
+    near = nearfield_operator(obs_mesh, src_mesh, mthd, all_mesh)
+    corr = farfield_correction_operator(obs_mesh, src_mesh, mthd, all_mesh)
+    g_near = _dense(galerkin_csr(R, obs_mesh, mthd.obs_near_order))
+    g_far = _dense(galerkin_csr(R, obs_mesh, mthd.obs_far_order))
+    interp = _dense(interpolation_csr(R, src_mesh, mthd.src_far_order))
+    ol, on, _ = quadrature_points(obs_mesh, mthd.obs_far_order)
+    sl, sn, sw = quadrature_points(src_mesh, mthd.src_far_order)
+    F = DirectOperator(K, ol, on, sl, sn, sw)
+    FI = np.asarray(F.apply(np.ascontiguousarray(interp.T))).T  # F applied to every column of I
+    near_d = _dense((near.n_rows(), near.n_cols(), near.values(), near.column_indices(), near.row_ptrs()))
+    corr_d = _dense((corr.n_rows(), corr.n_cols(), corr.values(), corr.column_indices(), corr.row_ptrs()))
+    out = g_far @ (corr_d + FI) + g_near @ near_d
+    return DenseOperator(out.shape[0], out.shape[1], out.ravel())
+

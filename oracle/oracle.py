@@ -467,3 +467,21 @@ def ref_nearfield_points(kernel, vertices, facets, locs, normals, sinh_order=5, 
     rows = np.zeros(shape[0] + 1, dtype=np.int64)
     fn(*args, _ptr(vals), _ptr(cols), _ptr(rows), nnz)
     return int(shape[0]), int(shape[1]), vals, cols, rows
+
+
+def ref_dense_boundary(kernel, vertices, facets, sinh_order=5, obs_near_order=2, obs_far_order=2,
+                       src_far_order=2, n_singular_steps=8, far_threshold=3.0, mu=1.0, nu=0.25):
+    """The reference's dense_boundary_operator (sinh strategy) of a mesh against
+    itself: the dense matrix [R n_dofs, C n_dofs]."""
+    dim = np.asarray(vertices).shape[1]
+    k = kernel_id(kernel, dim)
+    v, f = _mesh_args(vertices, facets)
+    fn = _ref().fn("dense_boundary", _L, [_I, _D, _D, _I, _P, _L, _P, _L, _L, _L, _L, _L, _L, _D, _P])
+    args = [k, mu, nu, dim, _ptr(v), len(v), _ptr(f), len(f), sinh_order, obs_near_order,
+            obs_far_order, src_far_order, n_singular_steps, far_threshold]
+    n = fn(*args, None)
+    out = np.zeros(n)
+    fn(*args, _ptr(out))
+    R = kernel_components(k)
+    rows = R * dim * len(f)
+    return out.reshape(rows, -1)

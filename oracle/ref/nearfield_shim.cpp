@@ -17,6 +17,7 @@
 #include "galerkin_operator.h"
 #include "interpolation_operator.h"
 #include "mass_operator.h"
+#include "integral_operator.h"
 #include "identity_kernels.h"
 #include "integral_term.h"
 #include "laplace_kernels.h"
@@ -252,6 +253,42 @@ long ref_nearfield_points(int kernel, double mu, double nu, int dim, const doubl
         std::memcpy(rowptr, c.rowptr.data(), (c.n_rows + 1) * sizeof(long));
     }
     return nnz;
+}
+
+// dense_boundary_operator (cpp/integral_operator.h:100-130) of a mesh against
+// itself with the sinh strategy: the dense (R n_dofs) x (C n_dofs) matrix,
+// row-major, written when out != NULL; returns the number of entries.
+long ref_dense_boundary(int kernel, double mu, double nu, int dim, const double* verts,
+                        long n_verts, const long* facets, long n_facets, long sinh_order,
+                        long obs_near_order, long obs_far_order, long src_far_order,
+                        long n_singular_steps, double far_threshold, double* out)
+{
+    Strategy s{1, 0.0, sinh_order, obs_near_order, obs_far_order, src_far_order, n_singular_steps,
+               far_threshold};
+    int saved = omp_get_max_threads();
+    omp_set_num_threads(1);
+    std::vector<double> data;
+    auto run = [&](const auto& K, const auto& m) {
+        auto mthd = make_strategy(s, K);
+        auto op = dense_boundary_operator(m, m, mthd, m);
+        data = op.data();
+    };
+    if (dim == 3) {
+        auto m = make_mesh<3>(verts, n_verts, facets, n_facets);
+        if (kernel == 0) run(LaplaceSingle<3>(), m);
+        else if (kernel == 1) run(LaplaceDouble<3>(), m);
+        else if (kernel == 2) run(ElasticDisplacement<3>(mu, nu), m);
+        else if (kernel == 3) run(ElasticTraction<3>(mu, nu), m);
+    } else {
+        auto m = make_mesh<2>(verts, n_verts, facets, n_facets);
+        if (kernel == 16) run(LaplaceSingle<2>(), m);
+        else if (kernel == 17) run(LaplaceDouble<2>(), m);
+        else if (kernel == 19) run(ElasticDisplacement<2>(mu, nu), m);
+        else if (kernel == 20) run(ElasticTraction<2>(mu, nu), m);
+    }
+    omp_set_num_threads(saved);
+    if (out) std::memcpy(out, data.data(), data.size() * sizeof(double));
+    return (long)data.size();
 }
 
 // One IntegrationStrategy::compute_term (cpp/integral_term.cpp:33-53) for an

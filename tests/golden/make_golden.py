@@ -282,6 +282,25 @@ def make_interior_cases():
         print("wrote interior", name, out["shape0"], len(out["values0"]), out["ulp_floor0"])
 
 
+def make_dense_boundary_cases():
+    """The reference's dense_boundary_operator (sinh strategy) of two small
+    meshes, with its one-ulp sensitivity."""
+    ms = nearfield_meshes()
+    cases = [("lapd_ico", "ico", "LaplaceDouble", 1.0, 0.25, 5, 3, 3, 3, 8, 3.0),
+             ("eltrac2_circle", "circle", "ElasticTraction", 1.0, 0.25, 8, 3, 3, 3, 8, 3.0)]
+    for name, mesh, kernel, mu, nu, so, on, of, sf, st, ft in cases:
+        v, f = ms[mesh]
+        A = oracle.ref_dense_boundary(kernel, v, f, so, on, of, sf, st, ft, mu, nu)
+        vp = v * (1 + 2.0 ** -52 * np.random.default_rng(0).choice([-1, 1], size=v.shape))
+        B = oracle.ref_dense_boundary(kernel, vp, f, so, on, of, sf, st, ft, mu, nu)
+        np.savez_compressed(os.path.join(HERE, "dense_boundary_%s.npz" % name), kernel=kernel, mu=mu,
+                            nu=nu, vertices=v, facets=f, sinh_order=so, obs_near_order=on,
+                            obs_far_order=of, src_far_order=sf, n_singular_steps=st,
+                            far_threshold=ft, matrix=A,
+                            ulp_floor=np.abs(A - B).max() / np.abs(A).max())
+        print("wrote dense boundary", name, A.shape, np.abs(A - B).max() / np.abs(A).max())
+
+
 def main(ref_root="/root/reference", which="all"):
     oracle.build()
     if oracle.build_ref(ref_root) is None:
@@ -289,6 +308,7 @@ def main(ref_root="/root/reference", which="all"):
     if which == "nearfield":
         make_nearfield_cases()
         make_interior_cases()
+        make_dense_boundary_cases()
         return
     for case in CASES_2D:
         data = make_case(*case)

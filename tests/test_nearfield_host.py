@@ -145,3 +145,16 @@ def test_interior_limit_directions_and_mass_operator_match_reference(path):
             assert (nr, nc) == tuple(g[key + "shape"])
             assert np.array_equal(rows, g[key + "rowptr"]) and np.array_equal(cols, g[key + "cols"])
             assert np.allclose(vals, g[key + "values"], rtol=1e-15, atol=0)
+
+
+def test_dense_operator_host_side():
+    """DenseOperator (cpp/dense_operator.h:11-40): shape, data(), to_dense,
+    clone, size check; nothing reaches the device before an apply."""
+    from tbempy import ThreeD
+    d = np.arange(12.0)
+    A = ThreeD.DenseOperator(3, 4, d)
+    assert (A.n_rows(), A.n_cols(), A.n_elements()) == (3, 4, 12)
+    assert np.array_equal(A.data(), d) and np.array_equal(A.to_dense(), d.reshape(3, 4))
+    assert np.array_equal(A.clone().data(), d)
+    with pytest.raises(ValueError):
+        ThreeD.DenseOperator(3, 5, d)
