@@ -287,7 +287,8 @@ const char* tbem_last_error(void);
  * all_mesh), cpp/integral_operator.h:66-99).  which: 0 the nearfield
  * operator (observation points from obs_near_order), 1 the farfield
  * correction (obs_far_order).  The result is a CSR operator with rows
- * R * n_obs_facets * n_obs_quad and columns C * dim * n_src_facets. */
+ * R * n_obs_facets * n_obs_quad and columns C * dim * n_src_facets.  Runs
+ * on the current CUDA device and synchronizes it before returning. */
 typedef struct {
     long sinh_order;       /* sinh rules: order + order * log(facet size / distance) points */
     long obs_near_order;   /* Gauss rule of the nearfield observation points */
