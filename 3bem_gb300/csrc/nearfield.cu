@@ -54,7 +54,7 @@ struct NfArgs {
     const double* fn;   // facet normal [n][3]
     const int* i_obs;   // per evaluation: observation point (for its normal),
     const int* i_fac;   // source facet,
-    const int* i_near;  // 1: sinh rule at the point, 0: the farfield rule
+    const int* i_near;  // 1: sinh rule at the point, 0: the farfield rule, 2: skipped here
     long n_items;
     double* out;  // [n_items][dim][R][C]
     int* err;     // bit 1: a point on a facet; bit 2: rule too large
@@ -247,6 +247,7 @@ __global__ void __launch_bounds__(32 * NF_WARPS) nearfield_kernel(const NfArgs a
     constexpr int E = DIM * R * R;
     const long i = (long)blockIdx.x * NF_WARPS + threadIdx.x / 32;
     if (i >= a.n_items) return;  // whole warps leave together
+    if (a.i_near[i] == 2) return;  // integrated by the adaptive rule instead
     const int lane = threadIdx.x & 31;
     const int f = a.i_fac[i];
     const double* p = a.loc + 3 * i;
@@ -266,6 +267,34 @@ __global__ void __launch_bounds__(32 * NF_WARPS) nearfield_kernel(const NfArgs a
     for (int e = 0; e < E; e++)
         if (e == lane) result = acc[e];
     if (lane < E) a.out[i * E + lane] = result;
+}
+
+// The adaptive rule's points: one thread per point, the term's basis x
+// kernel x jacobian at the reference point (eval_point_influence,
+// cpp/integral_term.cpp:11-20).
+template <int DIM, int R>
+__global__ void point_influence_kernel(const NfArgs a, const int* p_item, const double* p_x0,
+                                       const double* p_x1, long n, double* out)
+{
+    constexpr int E = DIM * R * R;
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = p_item[k];
+    double acc[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) acc[e] = 0.0;
+    influence<DIM, R>(a, a.i_fac[i], a.loc + 3 * i, a.nrm + 3 * a.i_obs[i], p_x0[k], p_x1[k], 1.0, acc);
+#pragma unroll
+    for (int e = 0; e < E; e++) out[k * E + e] = acc[e];
+}
+
+template <int DIM, int R>
+void launch_points(const NfArgs& a, const int* item, const double* x0, const double* x1, long n,
+                   double* out)
+{
+    if (n <= 0) return;
+    point_influence_kernel<DIM, R><<<(unsigned)((n + 127) / 128), 128>>>(a, item, x0, x1, n, out);
+    TBEM_CK(cudaGetLastError());
 }
 
 // Gauss rules 1..NF_GMAX, computed once per process.
@@ -314,7 +343,7 @@ void launch(const NfArgs& a)
 // nearfield_inner_integral, cpp/nearfield_operator.h:48-95).
 int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const nf::ObsPoints& pts,
                         const std::vector<nf::Facet>& src, const nf::FacetSet& src_set,
-                        const TbemSinhIntegrator* mthd, int which, TbemCsr** out)
+                        const TbemIntegrator* mthd, int which, TbemCsr** out)
 {
     const long n_pts = (long)pts.loc.size();
 
@@ -371,9 +400,9 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
                     add_item(o, f, 1, q);
                 }
             } else {
-                if (!(dist > 0.0))
+                if (!(dist > 0.0) && mthd->strategy == TBEM_QUAD_SINH)
                     throw Error(TBEM_ERR_ARG, "an observation point lies on a source facet without a "
-                                              "limit direction (the reference asserts here)");
+                                              "limit direction (the reference's sinh rule asserts here)");
                 add_item(o, f, 1, p);
             }
         } else {
@@ -381,6 +410,14 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
         }
     }
     const long n_items = (long)i_obs.size();
+    const bool adaptive = mthd->strategy == TBEM_QUAD_ADAPTIVE;
+    std::vector<long> adaptive_items;  // near evaluations done by the adaptive rule
+    if (adaptive)
+        for (long i = 0; i < n_items; i++)
+            if (i_near[i] == 1) {
+                i_near[i] = 2;
+                adaptive_items.push_back(i);
+            }
     std::vector<double> ivals((size_t)n_items * E);
     if (n_items > 0) {
         std::vector<double> nrm, fac, ls, jac, fn;
@@ -448,6 +485,35 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
                                       "(observation point too close to a facet)");
         TBEM_CK(cudaMemcpy(ivals.data(), d_out.p, ivals.size() * sizeof(double),
                            cudaMemcpyDeviceToHost));
+        if (!adaptive_items.empty()) {
+            // the adaptive Gauss-Lobatto rule: subdivision on the host,
+            // every level's points on the GPU
+            DBuf<int> d_pi;
+            DBuf<double> d_x0, d_x1, d_pv;
+            nf::InfluenceEval eval = [&](const std::vector<long>& item, const std::vector<double>& x0,
+                                         const std::vector<double>& x1, std::vector<double>& out) {
+                const long n = (long)item.size();
+                out.assign((size_t)n * E, 0.0);
+                if (n == 0) return;
+                std::vector<int> it(n);
+                for (long k = 0; k < n; k++) it[k] = (int)adaptive_items[item[k]];
+                d_pi.upload(it);
+                d_x0.upload(x0);
+                d_x1.upload(x1);
+                d_pv.alloc((size_t)n * E);
+                if (dim == 2 && R == 1) launch_points<2, 1>(a, d_pi.p, d_x0.p, d_x1.p, n, d_pv.p);
+                else if (dim == 2) launch_points<2, 2>(a, d_pi.p, d_x0.p, d_x1.p, n, d_pv.p);
+                else if (R == 1) launch_points<3, 1>(a, d_pi.p, d_x0.p, d_x1.p, n, d_pv.p);
+                else launch_points<3, 3>(a, d_pi.p, d_x0.p, d_x1.p, n, d_pv.p);
+                TBEM_CK(cudaMemcpy(out.data(), d_pv.p, out.size() * sizeof(double),
+                                   cudaMemcpyDeviceToHost));
+            };
+            const std::vector<double> v = nf::adaptive_facet_integrals(
+                dim, E, (long)adaptive_items.size(), mthd->near_tol, eval);
+            for (size_t k = 0; k < adaptive_items.size(); k++)
+                for (int e = 0; e < E; e++)
+                    ivals[(size_t)adaptive_items[k] * E + e] = v[k * E + e];
+        }
     }
     // per term: the evaluation, its negation (farfield correction) or the
     // Richardson limit of its steps (richardson_limit, cpp/richardson.h:10-34)
@@ -493,13 +559,16 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
     return tbem_csr_create(n_rows, n_cols, v.data(), cols.data(), count.data(), out);
 }
 
-void validate(int kernel, int which, const TbemSinhIntegrator* mthd)
+void validate(int kernel, int which, const TbemIntegrator* mthd)
 {
     if (!kernel_valid(kernel)) throw Error(TBEM_ERR_ARG, "unknown kernel id");
     if (which != 0 && which != 1) throw Error(TBEM_ERR_ARG, "which must be 0 or 1");
-    if (mthd->sinh_order <= 0 || mthd->obs_near_order <= 0 || mthd->obs_far_order <= 0 ||
-        mthd->src_far_order <= 0 || mthd->n_singular_steps < 2 || mthd->n_singular_steps > 32 ||
-        !(mthd->far_threshold > 0))
+    if (mthd->strategy != TBEM_QUAD_SINH && mthd->strategy != TBEM_QUAD_ADAPTIVE)
+        throw Error(TBEM_ERR_ARG, "bad integrator parameters: unknown strategy");
+    if ((mthd->strategy == TBEM_QUAD_SINH && mthd->sinh_order <= 0) ||
+        (mthd->strategy == TBEM_QUAD_ADAPTIVE && !(mthd->near_tol > 0)) ||
+        mthd->obs_near_order <= 0 || mthd->obs_far_order <= 0 || mthd->src_far_order <= 0 ||
+        mthd->n_singular_steps < 2 || mthd->n_singular_steps > 32 || !(mthd->far_threshold > 0))
         throw Error(TBEM_ERR_ARG, "bad integrator parameters");
 }
 
@@ -551,7 +620,7 @@ long tbem_galerkin_obs_points(int dim, const double* vertices, long n_vertices,
 int tbem_nearfield_create(int kernel, const double* kernel_params, const double* vertices,
                           long n_vertices, const long* obs_facets, long n_obs_facets,
                           const long* src_facets, long n_src_facets, const long* all_facets,
-                          long n_all_facets, const TbemSinhIntegrator* mthd, int which,
+                          long n_all_facets, const TbemIntegrator* mthd, int which,
                           TbemCsr** out)
 {
     using namespace tbem;
@@ -608,7 +677,7 @@ int tbem_nearfield_points_create(int kernel, const double* kernel_params, const 
                                  const double* obs_normals, long n_obs, const double* vertices,
                                  long n_vertices, const long* src_facets, long n_src_facets,
                                  const long* all_facets, long n_all_facets,
-                                 const TbemSinhIntegrator* mthd, int which, TbemCsr** out)
+                                 const TbemIntegrator* mthd, int which, TbemCsr** out)
 {
     using namespace tbem;
     if (!out || !mthd) return TBEM_ERR_ARG;

@@ -10,6 +10,7 @@
 // (nearfield.cu): every term's quadrature on the GPU, one warp per term.
 // Points and facets are stored as 3-vectors (z = 0 in 2D).
 #pragma once
+#include <functional>
 #include <vector>
 
 namespace tbem {
@@ -96,6 +97,29 @@ V3 limit_direction(const V3& p, const FacetSet& all, int dim);
 
 ObsPoints galerkin_obs_points(const std::vector<Facet>& obs, const FacetSet& all, int order,
                               int dim);
+
+// Batched evaluation of the functions being integrated: for point k, the
+// value (E numbers) of job[k]'s function at t[k], written to out[k * E ...].
+using AdaptiveEval = std::function<void(const std::vector<long>& job, const std::vector<double>& t,
+                                        std::vector<double>& out)>;
+
+// Adaptive Gauss-Lobatto integrals of job j's function over [a[j], b[j]]
+// (adaptive_integrate, cpp/adaptive_quad.h:128-174), all jobs level by level;
+// returns [n][E] (nearfield_adaptive.cpp).
+std::vector<double> adaptive_batch(int E, const std::vector<double>& a, const std::vector<double>& b,
+                                   double p_tol, const AdaptiveEval& eval);
+
+// Batched point influences of the terms being integrated: for point k, term
+// item[k]'s basis x kernel x jacobian at the reference point (x0[k], x1[k]).
+using InfluenceEval = std::function<void(const std::vector<long>& item, const std::vector<double>& x0,
+                                         const std::vector<double>& x1, std::vector<double>& out)>;
+
+// The facet integral of every item by the adaptive rule
+// (UnitFacetAdaptiveIntegrator, cpp/integral_term.cpp:96-128): over
+// x_hat in [-1, 1] in 2D; over x in [0, 1] of the integral over y in
+// [0, 1 - x] in 3D (zero at x = 1).  Returns [n_items][E].
+std::vector<double> adaptive_facet_integrals(int dim, int E, long n_items, double tol,
+                                             const InfluenceEval& eval);
 
 }  // namespace nf
 }  // namespace tbem

@@ -27,8 +27,9 @@ class TbemGpuOptions(C.Structure):
                 ("m2l_rank_tol", C.c_double), ("p2m_block", C.c_int), ("tc_shape", C.c_int)]
 
 
-class TbemSinhIntegrator(C.Structure):
-    _fields_ = [("sinh_order", C.c_long), ("obs_near_order", C.c_long),
+class TbemIntegrator(C.Structure):
+    _fields_ = [("strategy", C.c_int), ("near_tol", C.c_double),
+                ("sinh_order", C.c_long), ("obs_near_order", C.c_long),
                 ("obs_far_order", C.c_long), ("src_far_order", C.c_long),
                 ("n_singular_steps", C.c_long), ("far_threshold", C.c_double)]
 

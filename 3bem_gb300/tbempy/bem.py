@@ -17,10 +17,10 @@ farfield commented out and applied a dense operator), and the whole chain
 is applied on the device by ``IntegralOperator``.
 
 Meshes are ``Mesh(vertices [n, dim], facets [m, dim])``; the strategy comes
-from ``make_sinh_integrator`` (cpp/integral_term.h:129-150).  The reference's
-other strategy, ``make_adaptive_integrator`` (adaptive Gauss-Lobatto
-quadrature, cpp/adaptive_quad.h), is accepted by name but refused at
-construction: it is not built on the device.
+from ``make_sinh_integrator`` or ``make_adaptive_integrator``
+(cpp/integral_term.h:53-150): sinh-transformed Gauss rules, or the adaptive
+Gauss-Lobatto rule (cpp/adaptive_quad.h) whose subdivision the host decides
+level by level while the GPU evaluates every level's points.
 """
 import ctypes as C
 
@@ -68,8 +68,9 @@ class IntegrationStrategy:
         self.far_threshold = float(far_threshold)
 
     def _c(self):
-        return _L.TbemSinhIntegrator(self.sinh_order, self.obs_near_order, self.obs_far_order,
-                                     self.src_far_order, self.n_singular_steps, self.far_threshold)
+        return _L.TbemIntegrator(1 if self.kind == "adaptive" else 0, float(self.near_tol or 0.0),
+                                 self.sinh_order, self.obs_near_order, self.obs_far_order,
+                                 self.src_far_order, self.n_singular_steps, self.far_threshold)
 
 
 def make_sinh_integrator(sinh_order, obs_near_order, obs_far_order, src_far_order,
@@ -118,9 +119,6 @@ def galerkin_obs_points(obs_mesh, all_mesh, order):
 
 
 def _nearfield(obs_mesh, src_mesh, mthd, all_mesh, which):
-    if mthd.kind != "sinh":
-        raise NotImplementedError("adaptive Gauss-Lobatto nearfield quadrature is not built on "
-                                  "the device; use make_sinh_integrator")
     if mthd.K.space_dim != obs_mesh.dim:
         raise ValueError("the kernel's dimension does not match the mesh's")
     v, (of, sf, af) = _merge(obs_mesh, src_mesh, all_mesh)
@@ -272,9 +270,6 @@ def interior_limit_directions(locs, all_mesh):
 
 
 def _nearfield_points(locs, normals, src_mesh, mthd, all_mesh, which):
-    if mthd.kind != "sinh":
-        raise NotImplementedError("adaptive Gauss-Lobatto nearfield quadrature is not built on "
-                                  "the device; use make_sinh_integrator")
     dim = src_mesh.dim
     locs = np.ascontiguousarray(locs, dtype=np.float64).reshape(-1, dim)
     normals = np.ascontiguousarray(normals, dtype=np.float64).reshape(-1, dim)

@@ -276,12 +276,14 @@ void tbem_integral_destroy(TbemIntegral* h);
 const char* tbem_last_error(void);
 
 /* Nearfield and farfield-correction matrices (make_nearfield_operator /
- * make_farfield_correction_operator, cpp/nearfield_operator.h:12-117, with the
- * sinh integration strategy, make_sinh_integrator, cpp/integral_term.h:
- * 129-150, and IntegrationStrategy::compute_term, cpp/integral_term.cpp:
- * 33-92).  The host finds every (Galerkin observation point, nearby source
- * facet) term and the point's Richardson direction; the GPU integrates the
- * terms.  Meshes share one vertex array [n_vertices][dim] (dim from the
+ * make_farfield_correction_operator, cpp/nearfield_operator.h:12-117, with
+ * either integration strategy -- make_sinh_integrator or
+ * make_adaptive_integrator, cpp/integral_term.h:53-150 -- and
+ * IntegrationStrategy::compute_term, cpp/integral_term.cpp:33-92).  The host
+ * finds every (Galerkin observation point, nearby source facet) term and the
+ * point's Richardson direction; the GPU evaluates the quadratures (the
+ * adaptive rule's subdivision is decided on the host, level by level, with
+ * every level's points evaluated on the GPU).  Meshes share one vertex array [n_vertices][dim] (dim from the
  * kernel id); obs / src / all facets are [n][dim] vertex indices (the
  * reference's boundary_operator(obs_mesh, src_mesh, mthd, fmm_config,
  * all_mesh), cpp/integral_operator.h:66-99).  which: 0 the nearfield
@@ -289,14 +291,19 @@ const char* tbem_last_error(void);
  * correction (obs_far_order).  The result is a CSR operator with rows
  * R * n_obs_facets * n_obs_quad and columns C * dim * n_src_facets.  Runs
  * on the current CUDA device and synchronizes it before returning. */
+#define TBEM_QUAD_SINH 0      /* make_sinh_integrator */
+#define TBEM_QUAD_ADAPTIVE 1  /* make_adaptive_integrator (Gauss-Lobatto, near_tol) */
+
 typedef struct {
+    int strategy;          /* TBEM_QUAD_SINH or TBEM_QUAD_ADAPTIVE */
+    double near_tol;       /* adaptive rule's tolerance */
     long sinh_order;       /* sinh rules: order + order * log(facet size / distance) points */
     long obs_near_order;   /* Gauss rule of the nearfield observation points */
     long obs_far_order;    /* Gauss rule of the farfield observation points */
     long src_far_order;    /* Gauss rule of far source facets */
     long n_singular_steps; /* Richardson steps (2..32) */
     double far_threshold;  /* facets nearer than far_threshold x facet size are "near" */
-} TbemSinhIntegrator;
+} TbemIntegrator;
 
 /* Gauss rule on the reference facet (gauss_facet, cpp/gauss_quad.cpp:155-165):
  * points [n][dim - 1] on [-1, 1] (dim 2) or the triangle (0,0)-(1,0)-(0,1)
@@ -314,7 +321,7 @@ long tbem_galerkin_obs_points(int dim, const double* vertices, long n_vertices,
 int tbem_nearfield_create(int kernel, const double* kernel_params, const double* vertices,
                           long n_vertices, const long* obs_facets, long n_obs_facets,
                           const long* src_facets, long n_src_facets, const long* all_facets,
-                          long n_all_facets, const TbemSinhIntegrator* mthd, int which,
+                          long n_all_facets, const TbemIntegrator* mthd, int which,
                           TbemCsr** out);
 
 /* The same matrices for given observation points (the reference's
@@ -326,7 +333,7 @@ int tbem_nearfield_points_create(int kernel, const double* kernel_params, const 
                                  const double* obs_normals, long n_obs, const double* vertices,
                                  long n_vertices, const long* src_facets, long n_src_facets,
                                  const long* all_facets, long n_all_facets,
-                                 const TbemSinhIntegrator* mthd, int which, TbemCsr** out);
+                                 const TbemIntegrator* mthd, int which, TbemCsr** out);
 
 /* Limit (Richardson) directions of given points against all_facets
  * (decide_limit_dir, cpp/limit_direction.cpp:87-147, with the constants

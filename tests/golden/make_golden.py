@@ -204,25 +204,39 @@ NEARFIELD_CASES = [
 ]
 
 
+# the adaptive Gauss-Lobatto strategy (make_adaptive_integrator): (name, mesh,
+# kernel, mu, nu, near_tol, obs_near, obs_far, src_far, steps, far_threshold)
+ADAPTIVE_CASES = [
+    ("adapt_laps_wedge", "wedge", "LaplaceSingle", 1.0, 0.25, 1e-4, 2, 2, 3, 6, 3.0),
+    ("adapt_lapd_ico", "ico", "LaplaceDouble", 1.0, 0.25, 1e-4, 2, 2, 3, 6, 3.0),
+    ("adapt_eltrac_fault", "fault", "ElasticTraction", 1.0, 0.25, 1e-4, 2, 2, 3, 6, 3.0),
+    ("adapt_laps2_circle", "circle", "LaplaceSingle", 1.0, 0.25, 1e-5, 2, 2, 3, 6, 3.0),
+    ("adapt_eldisp2_vwedge", "vwedge", "ElasticDisplacement", 1.0, 0.25, 1e-5, 2, 2, 3, 6, 3.0),
+]
+
+
 def make_nearfield_cases():
     ms = nearfield_meshes()
-    for name, mesh, kernel, mu, nu, so, on, of, sf, st, ft in NEARFIELD_CASES:
+    cases = [(c, "sinh", 0.0) for c in NEARFIELD_CASES]
+    cases += [((n, m, k, mu, nu, 0) + tuple(rest), "adaptive", tol)
+              for n, m, k, mu, nu, tol, *rest in ADAPTIVE_CASES]
+    for (name, mesh, kernel, mu, nu, so, on, of, sf, st, ft), strategy, tol in cases:
         v, f = ms[mesh]
         out = dict(kernel=kernel, mu=mu, nu=nu, vertices=v, facets=f, sinh_order=so,
                    obs_near_order=on, obs_far_order=of, src_far_order=sf, n_singular_steps=st,
-                   far_threshold=ft)
+                   far_threshold=ft, strategy=strategy, near_tol=tol)
         # the reference's own sensitivity: its matrix again with every vertex
         # coordinate moved by one ulp (random sign), max |change| / max |entry|
         vp = v * (1 + 2.0 ** -52 * np.random.default_rng(0).choice([-1, 1], size=v.shape))
         for which in (0, 1):
             nr, nc, vals, cols, rows = oracle.ref_nearfield(
-                kernel, v, f, "sinh", 0.0, so, on, of, sf, st, ft, which, mu, nu)
+                kernel, v, f, strategy, tol, so, on, of, sf, st, ft, which, mu, nu)
             out["shape%d" % which] = np.array([nr, nc])
             out["values%d" % which] = vals
             out["cols%d" % which] = cols
             out["rowptr%d" % which] = rows
             pr, pc, pv, pcols, prows = oracle.ref_nearfield(
-                kernel, vp, f, "sinh", 0.0, so, on, of, sf, st, ft, which, mu, nu)
+                kernel, vp, f, strategy, tol, so, on, of, sf, st, ft, which, mu, nu)
             a = np.zeros((nr, nc))
             b = np.zeros((pr, pc))
             for r in range(nr):

@@ -1,7 +1,8 @@
 """GPU parity of the nearfield and farfield-correction matrices with the
 reference's own construction (tests/golden/nearfield_*.npz: 3D and 2D
 meshes, Laplace and elastic kernels including the hypersingular ones,
-Richardson extrapolation for the on-surface observation points).
+Richardson extrapolation for the on-surface observation points; the sinh
+strategy and the adaptive Gauss-Lobatto one).
 
 Tolerance (written here, checked below): max |GPU - reference| <= max(1e-10,
 100 x floor) x max |reference entry|, with floor the reference's own change
@@ -40,10 +41,12 @@ def test_nearfield_matrices_match_reference(path):
     from tbempy import ThreeD
     g = dict(np.load(path))
     m = ThreeD.Mesh(g["vertices"], g["facets"])
-    mthd = ThreeD.make_sinh_integrator(int(g["sinh_order"]), int(g["obs_near_order"]),
-                                       int(g["obs_far_order"]), int(g["src_far_order"]),
-                                       int(g["n_singular_steps"]), float(g["far_threshold"]),
-                                       kernel_of(g, m.dim))
+    rest = (int(g["obs_near_order"]), int(g["obs_far_order"]), int(g["src_far_order"]),
+            int(g["n_singular_steps"]), float(g["far_threshold"]), kernel_of(g, m.dim))
+    if str(g["strategy"]) == "adaptive":
+        mthd = ThreeD.make_adaptive_integrator(float(g["near_tol"]), *rest)
+    else:
+        mthd = ThreeD.make_sinh_integrator(int(g["sinh_order"]), *rest)
     for which, build in ((0, ThreeD.nearfield_operator), (1, ThreeD.farfield_correction_operator)):
         op = build(m, m, mthd, m)
         assert (op.n_rows(), op.n_cols()) == tuple(g["shape%d" % which])

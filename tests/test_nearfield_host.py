@@ -61,14 +61,11 @@ def test_gauss_rules_match_reference():
             assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
-def test_adaptive_strategy_and_bad_arguments_refused():
-    from tbempy import ThreeD, TwoD
+def test_bad_facet_indices_refused():
+    from tbempy import ThreeD
     from tbempy._lib import TbemError
     g = dict(np.load(CASES[0]))
     m = ThreeD.Mesh(g["vertices"], g["facets"])
-    K = ThreeD.LaplaceDouble() if m.dim == 3 else TwoD.LaplaceDouble()
-    with pytest.raises(NotImplementedError):
-        ThreeD.nearfield_operator(m, m, ThreeD.make_adaptive_integrator(1e-4, 2, 2, 2, 8, 3.0, K), m)
     with pytest.raises(TbemError):
         ThreeD.galerkin_obs_points(ThreeD.Mesh(m.vertices, m.facets + 10 * len(m.vertices)), m, 2)
 
@@ -105,13 +102,15 @@ def test_nearfield_create_validates_before_device_use():
     f = np.ascontiguousarray([[0, 1, 2]], dtype=np.int64)
     bad_f = np.ascontiguousarray([[0, 1, 7]], dtype=np.int64)
     P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
-    good = _lib.TbemSinhIntegrator(5, 2, 2, 2, 8, 3.0)
+    good = _lib.TbemIntegrator(0, 0.0, 5, 2, 2, 2, 8, 3.0)
     cases = [
         (42, f, good, 0, "kernel"),                                        # unknown kernel
         (1, f, good, 5, "which"),                                          # bad which
-        (1, f, _lib.TbemSinhIntegrator(0, 2, 2, 2, 8, 3.0), 0, "integrator"),
-        (1, f, _lib.TbemSinhIntegrator(5, 2, 2, 2, 1, 3.0), 0, "integrator"),  # < 2 steps
-        (1, f, _lib.TbemSinhIntegrator(5, 2, 2, 2, 8, -1.0), 0, "integrator"),
+        (1, f, _lib.TbemIntegrator(0, 0.0, 0, 2, 2, 2, 8, 3.0), 0, "integrator"),  # sinh order 0
+        (1, f, _lib.TbemIntegrator(1, 0.0, 0, 2, 2, 2, 8, 3.0), 0, "integrator"),  # adaptive tol 0
+        (1, f, _lib.TbemIntegrator(7, 1e-4, 5, 2, 2, 2, 8, 3.0), 0, "strategy"),
+        (1, f, _lib.TbemIntegrator(0, 0.0, 5, 2, 2, 2, 1, 3.0), 0, "integrator"),  # < 2 steps
+        (1, f, _lib.TbemIntegrator(0, 0.0, 5, 2, 2, 2, 8, -1.0), 0, "integrator"),
         (1, bad_f, good, 0, "index"),                                      # vertex out of range
     ]
     for kid, fac, cfg, which, word in cases:
@@ -158,3 +157,49 @@ def test_dense_operator_host_side():
     assert np.array_equal(A.clone().data(), d)
     with pytest.raises(ValueError):
         ThreeD.DenseOperator(3, 5, d)
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/cpp"), reason="reference checkout absent")
+@pytest.mark.parametrize("kernel,dim", [(0, 3), (1, 3), (3, 3), (6, 3), (16, 2), (19, 2), (22, 2)])
+def test_adaptive_engine_matches_reference(kernel, dim, tmp_path):
+    """The level-by-level adaptive Gauss-Lobatto engine the product drives
+    (3bem_gb300/csrc/nearfield_adaptive.cpp), run here with the oracle's CPU
+    kernels as its point evaluator (tests/cpp/adaptive_driver.cpp; the product
+    evaluates the same points on the GPU), equals the reference's recursive
+    integrator (cpp/adaptive_quad.h via compute_term) bit for bit on near
+    terms."""
+    import subprocess
+    from oracle import oracle
+    if not oracle.ref_available():
+        pytest.skip("reference library not built here")
+    exe = str(tmp_path / "adaptive_driver")
+    csrc = os.path.join(ROOT, "3bem_gb300", "csrc")
+    odir = os.path.join(ROOT, "oracle")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I" + csrc,
+                           "-I" + os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "cpp", "adaptive_driver.cpp"),
+                           os.path.join(csrc, "nearfield_adaptive.cpp"),
+                           os.path.join(csrc, "nearfield_host.cpp"), "-o", exe,
+                           os.path.join(odir, "liboracle.so"), "-Wl,-rpath," + odir])
+    rng = np.random.default_rng(kernel)
+    facet = (np.array([[0, 0, 0], [1.0, 0.1, 0], [0.2, 0.9, 0.1]]) if dim == 3
+             else np.array([[0, 0, 0], [1.0, 0.2, 0]]))
+    tol = 1e-5
+    terms = []
+    for _ in range(6):
+        obs = facet.mean(axis=0) + rng.normal(size=3) * 0.3
+        n = rng.normal(size=3)
+        if dim == 2:
+            obs[2] = n[2] = 0.0
+        terms.append((obs, n / np.linalg.norm(n)))
+    lines = ["%d %.17g %.17g %.17g %d" % (kernel, 1.3, 0.27, tol, dim)]
+    for obs, n in terms:
+        lines.append(" ".join("%.17g" % v for v in list(obs) + list(n) + list(facet.ravel())))
+    out = subprocess.run([exe], input="\n".join(lines) + "\n", capture_output=True, text=True,
+                         check=True).stdout.strip().split("\n")
+    for (obs, n), row in zip(terms, out):
+        mine = np.array([float(v) for v in row.split()])
+        ref = oracle.ref_term(kernel, obs[:dim], n[:dim], np.zeros(dim), facet[:, :dim], "adaptive",
+                              tol, 0, 2, 2, 2, 8, 1e9, 1.3, 0.27).ravel()
+        assert np.array_equal(mine, ref)
+
