@@ -67,7 +67,8 @@ def build(verbose=False, jobs=None):
                     print(out)
     if steps or not os.path.exists(LIB):
         tmp = LIB + ".tmp%d" % os.getpid()
-        _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcusolver", "-lcublas", "-lcudart"])
+        _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcusolver", "-lcublas", "-lcudart",
+                                                               "-lpthread"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -349,17 +349,18 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
 
     // terms: every observation point against its nearfield source facets,
     // in the reference's loop order
+    std::vector<std::vector<size_t>> near_of(n_pts);
+    nf::parallel_for(n_pts, [&](long i) {
+        size_t nearest = 0;
+        double dist = 0.0;
+        src_set.find(pts.loc[i], mthd->far_threshold, near_of[i], nearest, dist);
+    });
     std::vector<int> t_obs, t_fac;
-    std::vector<size_t> nearby;
-    size_t nearest = 0;
-    double dist = 0.0;
-    for (long i = 0; i < n_pts; i++) {
-        src_set.find(pts.loc[i], mthd->far_threshold, nearby, nearest, dist);
-        for (size_t f : nearby) {
+    for (long i = 0; i < n_pts; i++)
+        for (size_t f : near_of[i]) {
             t_obs.push_back((int)i);
             t_fac.push_back((int)f);
         }
-    }
     const long n_terms = (long)t_obs.size();
     const int E = dim * R * R;
     // classify every term as IntegrationStrategy::compute_term does
@@ -659,13 +660,13 @@ long tbem_interior_obs_points(int dim, const double* locs, long n, const double*
             throw Error(TBEM_ERR_ARG, "bad argument");
         const auto all = read_facets(vertices, n_vertices, all_facets, n_all_facets, dim);
         nf::FacetSet all_set(all, dim);
-        for (long i = 0; i < n; i++) {
+        nf::parallel_for(n, [&](long i) {
             nf::V3 p{{0, 0, 0}};
             for (int d = 0; d < dim; d++) p[d] = locs[dim * i + d];
             const nf::V3 r = nf::limit_direction(p, all_set, dim);
             if (dirs)
                 for (int d = 0; d < dim; d++) dirs[dim * i + d] = r[d];
-        }
+        });
         return n;
     } catch (const tbem::Error& e) {
         tbem::set_last_error(e.what());
@@ -704,8 +705,9 @@ int tbem_nearfield_points_create(int kernel, const double* kernel_params, const 
             }
             pts.loc.push_back(p);
             pts.normal.push_back(nn);
-            pts.dir.push_back(nf::limit_direction(p, all_set, dim));
         }
+        pts.dir.resize(n_obs);
+        nf::parallel_for(n_obs, [&](long i) { pts.dir[i] = nf::limit_direction(pts.loc[i], all_set, dim); });
         return build_nearfield_csr(kernel, dim, R, mu, nu, pts, src, src_set, mthd, which, out);
     } catch (const tbem::Error& e) {
         tbem::set_last_error(e.what());

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <thread>
 
 #include "nearfield.h"
 
@@ -590,6 +591,22 @@ V3 limit_direction(const V3& p, const FacetSet& all, int dim)
     return d;
 }
 
+void parallel_for(long n, const std::function<void(long)>& body)
+{
+    const long hw = (long)std::max(1u, std::thread::hardware_concurrency());
+    const long nt = std::min(hw, std::max(1L, n / 256));
+    if (nt <= 1) {
+        for (long i = 0; i < n; i++) body(i);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (long t = 0; t < nt; t++)
+        th.emplace_back([&, t] {
+            for (long i = n * t / nt; i < n * (t + 1) / nt; i++) body(i);
+        });
+    for (auto& x : th) x.join();
+}
+
 ObsPoints galerkin_obs_points(const std::vector<Facet>& obs, const FacetSet& all, int order, int dim)
 {
     std::vector<double> qx, qw;
@@ -598,12 +615,13 @@ ObsPoints galerkin_obs_points(const std::vector<Facet>& obs, const FacetSet& all
     for (const Facet& f : obs) {
         const FacetInfo fi = facet_info(f, dim);
         for (size_t q = 0; q < qw.size(); q++) {
-            const V3 loc = ref_to_real(&qx[2 * q], f, dim);
-            o.loc.push_back(loc);
+            o.loc.push_back(ref_to_real(&qx[2 * q], f, dim));
             o.normal.push_back(fi.normal);
-            o.dir.push_back(limit_direction(loc, all, dim));
         }
     }
+    // the limit directions, point by point (the reference's interior_obs_pts loop)
+    o.dir.resize(o.loc.size());
+    parallel_for((long)o.loc.size(), [&](long i) { o.dir[i] = limit_direction(o.loc[i], all, dim); });
     return o;
 }
 
