@@ -5,6 +5,8 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <exception>
+#include <mutex>
 #include <thread>
 
 #include "nearfield.h"
@@ -600,11 +602,19 @@ void parallel_for(long n, const std::function<void(long)>& body)
         return;
     }
     std::vector<std::thread> th;
+    std::exception_ptr failure;
+    std::mutex m;
     for (long t = 0; t < nt; t++)
         th.emplace_back([&, t] {
-            for (long i = n * t / nt; i < n * (t + 1) / nt; i++) body(i);
+            try {
+                for (long i = n * t / nt; i < n * (t + 1) / nt; i++) body(i);
+            } catch (...) {  // handed to the caller after the join
+                std::lock_guard<std::mutex> lock(m);
+                if (!failure) failure = std::current_exception();
+            }
         });
     for (auto& x : th) x.join();
+    if (failure) std::rethrow_exception(failure);
 }
 
 ObsPoints galerkin_obs_points(const std::vector<Facet>& obs, const FacetSet& all, int order, int dim)
