@@ -18,6 +18,28 @@ int fail(int code, const std::string& msg)
     return code;
 }
 
+}  // namespace
+
+namespace tbem {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+int api_status()
+{
+    try {
+        throw;
+    } catch (const Error& e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(TBEM_ERR_ALLOC, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(TBEM_ERR_ARG, e.what());
+    } catch (...) {
+        return fail(TBEM_ERR_ARG, "unknown error");
+    }
+}
+}  // namespace tbem
+
+namespace {
 template <typename F>
 int guarded(F&& f)
 {
@@ -25,19 +47,11 @@ int guarded(F&& f)
         g_last_error.clear();
         f();
         return TBEM_OK;
-    } catch (const tbem::Error& e) {
-        return fail(e.code, e.what());
-    } catch (const std::bad_alloc&) {
-        return fail(TBEM_ERR_ALLOC, "host allocation failed");
-    } catch (const std::exception& e) {
-        return fail(TBEM_ERR_ARG, e.what());
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 }  // namespace
-
-namespace tbem {
-void set_last_error(const std::string& msg) { g_last_error = msg; }
-}  // namespace tbem
 
 extern "C" {
 
@@ -95,33 +109,41 @@ long tbem_fmm_n_cols(const TbemFmm* h) { return h ? h->plan.R * h->plan.n_src : 
 int tbem_fmm_clone(const TbemFmm* h, TbemFmm** out)
 {
     if (!h || !out) return fail(TBEM_ERR_ARG, "null argument");
+    *out = nullptr;
     const tbem::Plan& p = h->plan;
-    double params[2] = {p.mu, p.nu};
-    // the plan keeps [n][3] points; the create call takes [n][sdim]
-    auto narrow = [&](const std::vector<double>& v) {
-        std::vector<double> o(v.size() / 3 * p.sdim);
-        for (size_t i = 0; i < v.size() / 3; i++)
-            for (int d = 0; d < p.sdim; d++) o[p.sdim * i + d] = v[3 * i + d];
-        return o;
-    };
-    const std::vector<double> ol = narrow(p.h_obs_locs), on = narrow(p.h_obs_normals),
-                              sl = narrow(p.h_src_locs), sn = narrow(p.h_src_normals);
-    int rc = tbem_fmm_create(p.kid, params, ol.data(), on.data(), p.n_obs, sl.data(), sn.data(),
-                             p.h_src_weights.data(), p.n_src, &p.cfg, &p.opt, out);
-    if (rc != TBEM_OK) return rc;
-    if (!p.f.mixed) {
-        // carry over installed check-to-equivalent operators
-        return guarded([&] {
+    TbemFmm* c = nullptr;
+    const int rc = guarded([&] {
+        double params[2] = {p.mu, p.nu};
+        // the plan keeps [n][3] points; the create call takes [n][sdim]
+        auto narrow = [&](const std::vector<double>& v) {
+            std::vector<double> o(v.size() / 3 * p.sdim);
+            for (size_t i = 0; i < v.size() / 3; i++)
+                for (int d = 0; d < p.sdim; d++) o[p.sdim * i + d] = v[3 * i + d];
+            return o;
+        };
+        const std::vector<double> ol = narrow(p.h_obs_locs), on = narrow(p.h_obs_normals),
+                                  sl = narrow(p.h_src_locs), sn = narrow(p.h_src_normals);
+        const int created = tbem_fmm_create(p.kid, params, ol.data(), on.data(), p.n_obs, sl.data(),
+                                            sn.data(), p.h_src_weights.data(), p.n_src, &p.cfg, &p.opt, &c);
+        if (created != TBEM_OK) throw tbem::Error(created, g_last_error);
+        if (!p.f.mixed && !p.opt.host_only) {
+            // carry over installed check-to-equivalent operators (a host-only
+            // operator has none)
             std::vector<double> buf((size_t)p.n * p.n);
             for (int w = 0; w < 2; w++) {
                 long nl = (long)(w == 0 ? p.f.c2e_up_off.size() : p.f.c2e_dn_off.size());
                 for (long l = 0; l < nl; l++) {
                     p.get_c2e(w, l, buf.data());
-                    (*out)->plan.set_c2e(w, l, buf.data());
+                    c->plan.set_c2e(w, l, buf.data());
                 }
             }
-        });
+        }
+    });
+    if (rc != TBEM_OK) {
+        delete c;
+        return rc;
     }
+    *out = c;
     return TBEM_OK;
 }
 
@@ -149,18 +171,20 @@ long tbem_fmm_tree_indices(const TbemFmm* h, int which, long* out)
     if (!h || (which != 0 && which != 1)) return fail(TBEM_ERR_ARG, "bad handle or tree");
     const tbem::Tree& t = which == 0 ? *h->plan.stree : h->plan.otree;
     long k = 0;
-    std::vector<long> tmp;
-    for (int f : t.preorder) {
-        const tbem::Cell& c = t.cells[f];
-        // the reference lists a cell's points in ascending original order
-        tmp.assign(t.perm.begin() + c.pt_begin, t.perm.begin() + c.pt_end);
-        std::sort(tmp.begin(), tmp.end());
-        for (long v : tmp) {
-            if (out) out[k] = v;
-            k++;
+    const int rc = guarded([&] {
+        std::vector<long> tmp;
+        for (int f : t.preorder) {
+            const tbem::Cell& c = t.cells[f];
+            // the reference lists a cell's points in ascending original order
+            tmp.assign(t.perm.begin() + c.pt_begin, t.perm.begin() + c.pt_end);
+            std::sort(tmp.begin(), tmp.end());
+            for (long v : tmp) {
+                if (out) out[k] = v;
+                k++;
+            }
         }
-    }
-    return k;
+    });
+    return rc != TBEM_OK ? rc : k;
 }
 
 long tbem_fmm_list(const TbemFmm* h, int kind, long* obs_index, long* src_index)
@@ -238,8 +262,11 @@ int tbem_fmm_graph_create(TbemFmm* const* ops, int n_ops, const double* const* x
 {
     if (!out) return fail(TBEM_ERR_ARG, "null output handle");
     *out = nullptr;
-    TbemGraph* g = tbem::graph_new();
-    int rc = guarded([&] { tbem::graph_build(*g, ops, n_ops, x, y, n_rhs, adjoint != 0); });
+    TbemGraph* g = nullptr;
+    int rc = guarded([&] {
+        g = tbem::graph_new();
+        tbem::graph_build(*g, ops, n_ops, x, y, n_rhs, adjoint != 0);
+    });
     if (rc != TBEM_OK) {
         tbem::graph_delete(g);
         return rc;

@@ -1,6 +1,7 @@
 // Direct FP64 N-body sum on the GPU and the CSR operator.
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -104,6 +105,10 @@ int tbem_direct_apply(int kernel, const double* kernel_params, const double* obs
     try {
         if (!kernel_valid(kernel) || n_obs < 0 || n_src < 0 || n_rhs <= 0 || !y)
             throw Error(TBEM_ERR_ARG, "bad argument");
+        if (n_src > (long)INT32_MAX) throw Error(TBEM_ERR_ARG, "too many sources");
+        if (n_obs > 0 && n_src > 0 && (!obs_locs || !obs_normals || !src_locs || !src_normals ||
+                                       !src_weights || !x))
+            throw Error(TBEM_ERR_ARG, "null point or input array");
         const int R = kernel_dim(kernel);
         const int sdim = kernel_space_dim(kernel);
         const double mu = (kernel_params && R > 1) ? kernel_params[0] : 1.0;
@@ -137,7 +142,6 @@ int tbem_direct_apply(int kernel, const double* kernel_params, const double* obs
             double org[3] = {0, 0, 0};
             for (long b = 0; b < n_obs; b += chunk)
                 ts.add(b, (int)std::min<long>(chunk, n_obs - b), org, {{0L, (int)n_src}}, EVAL_THREADS / 4);
-            if (n_src > (long)INT32_MAX) throw Error(TBEM_ERR_ARG, "too many sources");
             ts.upload();
             EvalArgs<double> a{};
             ts.fill(a);
@@ -162,9 +166,8 @@ int tbem_direct_apply(int kernel, const double* kernel_params, const double* obs
         if (!y_dev) TBEM_CK(cudaMemcpyAsync(y, yd, ny * sizeof(double), cudaMemcpyDeviceToHost, s));
         TBEM_CK(cudaStreamSynchronize(s));
         return TBEM_OK;
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 
@@ -183,7 +186,7 @@ int tbem_csr_create(long n_rows, long n_cols, const double* values, const long* 
         for (long k = 0; k < nnz; k++)
             if (column_indices[k] < 0 || column_indices[k] >= n_cols)
                 throw Error(TBEM_ERR_ARG, "column index out of range");
-        auto h = new TbemCsr();
+        auto h = std::make_unique<TbemCsr>();
         h->n_rows = n_rows;
         h->n_cols = n_cols;
         h->nnz = nnz;
@@ -192,18 +195,20 @@ int tbem_csr_create(long n_rows, long n_cols, const double* values, const long* 
             h->col.upload(std::vector<long>(column_indices, column_indices + nnz));
             h->val.upload(std::vector<double>(values, values + nnz));
         }
-        *out = h;
+        *out = h.release();
         return TBEM_OK;
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 
 int tbem_csr_apply(TbemCsr* h, const double* x, double* y, int n_rhs, void* stream)
 {
     using namespace tbem;
-    if (!h || !y || n_rhs <= 0) return TBEM_ERR_ARG;
+    if (!h || !y || n_rhs <= 0 || (!x && h->n_cols > 0)) {
+        tbem::set_last_error("null argument or n_rhs <= 0");
+        return TBEM_ERR_ARG;
+    }
     try {
         cudaStream_t s = (cudaStream_t)stream;
         if (h->n_rows == 0) return TBEM_OK;
@@ -224,9 +229,8 @@ int tbem_csr_apply(TbemCsr* h, const double* x, double* y, int n_rhs, void* stre
         if (!y_dev) TBEM_CK(cudaMemcpyAsync(y, yd, ny * sizeof(double), cudaMemcpyDeviceToHost, s));
         TBEM_CK(cudaStreamSynchronize(s));
         return TBEM_OK;
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 
@@ -252,9 +256,8 @@ int tbem_csr_download(const TbemCsr* h, double* values, long* column_indices, lo
         if (h->nnz > 0 && column_indices)
             TBEM_CK(cudaMemcpy(column_indices, h->col.p, sizeof(long) * h->nnz, cudaMemcpyDeviceToHost));
         return TBEM_OK;
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 
@@ -350,9 +353,8 @@ int tbem_integral_apply(TbemIntegral* h, const double* x, double* y, int n_rhs, 
         if (!y_dev) TBEM_CK(cudaMemcpyAsync(y, yd, ny * sizeof(double), cudaMemcpyDeviceToHost, s));
         TBEM_CK(cudaStreamSynchronize(s));
         return TBEM_OK;
-    } catch (const tbem::Error& e) {
-        set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return api_status();
     }
 }
 

@@ -260,8 +260,7 @@ extern "C" int tbem_direct_gradients(int kernel, const double* kernel_params,
         for (Out* o : {&go, &gno, &gs, &gns, &gw, &gx}) o->finish(s);
         TBEM_CK(cudaStreamSynchronize(s));
         return TBEM_OK;
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return tbem::api_status();
     }
 }

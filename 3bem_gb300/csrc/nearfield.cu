@@ -24,6 +24,7 @@
 // compresses them to CSR (csr_from_coo's stable row order).
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -317,6 +318,9 @@ const std::vector<double>& gauss_table(int which)
 
 std::vector<nf::Facet> read_facets(const double* verts, long n_verts, const long* idx, long n, int dim)
 {
+    if (n > 0 && (!idx || !verts)) throw Error(TBEM_ERR_ARG, "null vertex or facet array");
+    // facet and point numbers travel to the device as int
+    if (n > (long)INT32_MAX) throw Error(TBEM_ERR_ARG, "too many facets");
     std::vector<nf::Facet> out((size_t)n);
     for (long i = 0; i < n; i++) {
         nf::Facet f{};
@@ -346,6 +350,7 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
                         const TbemIntegrator* mthd, int which, TbemCsr** out)
 {
     const long n_pts = (long)pts.loc.size();
+    if (n_pts > (long)INT32_MAX) throw Error(TBEM_ERR_ARG, "too many observation points");
 
     // terms: every observation point against its nearfield source facets,
     // in the reference's loop order
@@ -411,6 +416,8 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
         }
     }
     const long n_items = (long)i_obs.size();
+    // the adaptive evaluations name their item as int on the device
+    if (n_items > (long)INT32_MAX) throw Error(TBEM_ERR_ARG, "too many nearfield terms");
     const bool adaptive = mthd->strategy == TBEM_QUAD_ADAPTIVE;
     std::vector<long> adaptive_items;  // near evaluations done by the adaptive rule
     if (adaptive)
@@ -580,16 +587,21 @@ extern "C" {
 
 long tbem_gauss_facet(int dim, long n, double* x, double* w)
 {
-    if ((dim != 2 && dim != 3) || n <= 0 || n > 4096) return TBEM_ERR_ARG;
-    std::vector<double> qx, qw;
-    tbem::nf::gauss_facet(dim, (int)n, qx, qw);
-    if (x)
-        for (size_t i = 0; i < qw.size(); i++) {
-            x[(dim - 1) * i] = qx[2 * i];
-            if (dim == 3) x[2 * i + 1] = qx[2 * i + 1];
-        }
-    if (w) std::copy(qw.begin(), qw.end(), w);
-    return (long)qw.size();
+    try {
+        if ((dim != 2 && dim != 3) || n <= 0 || n > 4096)
+            throw tbem::Error(TBEM_ERR_ARG, "dim must be 2 or 3 and n in [1, 4096]");
+        std::vector<double> qx, qw;
+        tbem::nf::gauss_facet(dim, (int)n, qx, qw);
+        if (x)
+            for (size_t i = 0; i < qw.size(); i++) {
+                x[(dim - 1) * i] = qx[2 * i];
+                if (dim == 3) x[2 * i + 1] = qx[2 * i + 1];
+            }
+        if (w) std::copy(qw.begin(), qw.end(), w);
+        return (long)qw.size();
+    } catch (...) {
+        return tbem::api_status();
+    }
 }
 
 long tbem_galerkin_obs_points(int dim, const double* vertices, long n_vertices,
@@ -612,9 +624,8 @@ long tbem_galerkin_obs_points(int dim, const double* vertices, long n_vertices,
                 if (dirs) dirs[dim * i + d] = pts.dir[i][d];
             }
         return (long)pts.loc.size();
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 
@@ -641,12 +652,8 @@ int tbem_nearfield_create(int kernel, const double* kernel_params, const double*
         const int order = (int)(which == 0 ? mthd->obs_near_order : mthd->obs_far_order);
         const nf::ObsPoints pts = nf::galerkin_obs_points(obs, all_set, order, dim);
         return build_nearfield_csr(kernel, dim, R, mu, nu, pts, src, src_set, mthd, which, out);
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        tbem::set_last_error("host allocation failed");
-        return TBEM_ERR_ALLOC;
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 
@@ -668,9 +675,8 @@ long tbem_interior_obs_points(int dim, const double* locs, long n, const double*
                 for (int d = 0; d < dim; d++) dirs[dim * i + d] = r[d];
         });
         return n;
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 
@@ -709,12 +715,8 @@ int tbem_nearfield_points_create(int kernel, const double* kernel_params, const 
         pts.dir.resize(n_obs);
         nf::parallel_for(n_obs, [&](long i) { pts.dir[i] = nf::limit_direction(pts.loc[i], all_set, dim); });
         return build_nearfield_csr(kernel, dim, R, mu, nu, pts, src, src_set, mthd, which, out);
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        tbem::set_last_error("host allocation failed");
-        return TBEM_ERR_ALLOC;
+    } catch (...) {
+        return tbem::api_status();
     }
 }
 

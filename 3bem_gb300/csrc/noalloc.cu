@@ -209,8 +209,7 @@ extern "C" int tbem_direct_apply_noalloc(int kernel, const double* kernel_params
             TBEM_CK(launch_eval<double>(L, a, s));
         }
         return TBEM_OK;
-    } catch (const tbem::Error& e) {
-        tbem::set_last_error(e.what());
-        return e.code;
+    } catch (...) {
+        return tbem::api_status();
     }
 }

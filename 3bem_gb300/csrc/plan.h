@@ -28,6 +28,12 @@ struct Error : std::runtime_error {
 // Records the message returned by tbem_last_error() on the calling thread.
 void set_last_error(const std::string& msg);
 
+// Inside a catch block of an extern "C" entry point: records the exception
+// being handled as the calling thread's last error and returns its status
+// (tbem::Error: its code; std::bad_alloc: TBEM_ERR_ALLOC; any other
+// exception: TBEM_ERR_ARG), so that no C++ exception crosses the C ABI.
+int api_status();
+
 void check_cuda(cudaError_t e, const char* what, const char* file, int line);
 void check_cublas(cublasStatus_t e, const char* what, const char* file, int line);
 void check_cusolver(cusolverStatus_t e, const char* what, const char* file, int line);

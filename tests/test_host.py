@@ -114,6 +114,23 @@ def test_argument_errors_are_status_codes():
     with pytest.raises(TbemError) as e:
         op.apply(np.ones(10))
     assert e.value.code == -4
+    # a clone rebuilds the same tree and lists
+    c = op.clone()
+    assert c.n_rows() == op.n_rows() and c.n_cols() == op.n_cols()
+    for kind in range(8):
+        assert all(np.array_equal(a, b) for a, b in zip(op.list(kind), c.list(kind)))
+    for which in (0, 1):
+        assert np.array_equal(op.tree(which)["center"], c.tree(which)["center"])
+
+    # the direct sum refuses null arrays before touching the device
+    import ctypes as C
+    from tbempy import _lib
+    L = _lib.lib()
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    y = np.zeros(10)
+    assert L.tbem_direct_apply(0, None, P(p), P(p), 10, P(p), P(p), None, 10, P(y), P(y), 1,
+                               None) == -1
+    assert "null" in L.tbem_last_error().decode()
 
 
 def test_2d_operators_build_quadtrees_and_refuse_the_precision_form():

@@ -120,7 +120,18 @@ def test_nearfield_create_validates_before_device_use():
         assert rc == -1, (kid, which)
         assert word in L.tbem_last_error().decode(), L.tbem_last_error()
         assert not h.value
+    # null vertex / facet arrays with a nonzero count are argument errors, not crashes
+    h = C.c_void_p()
+    rc = L.tbem_nearfield_create(1, None, None, 3, P(f), 1, P(f), 1, P(f), 1, C.byref(good), 0,
+                                 C.byref(h))
+    assert rc == -1 and "null" in L.tbem_last_error().decode()
+    rc = L.tbem_nearfield_create(1, None, P(v), 3, None, 1, P(f), 1, P(f), 1, C.byref(good), 0,
+                                 C.byref(h))
+    assert rc == -1 and "null" in L.tbem_last_error().decode() and not h.value
+    assert L.tbem_galerkin_obs_points(3, P(v), 3, None, 1, P(f), 1, 2, None, None, None) == -1
+    assert L.tbem_interior_obs_points(3, P(v), 1, P(v), 3, None, 1, None) == -1
     assert L.tbem_gauss_facet(4, 3, None, None) == -1
+    assert "dim" in L.tbem_last_error().decode()
     assert L.tbem_gauss_facet(3, 0, None, None) == -1
 
 
