@@ -592,9 +592,8 @@ void Plan::autotune_tc()
     const long nn = comp ? (long)f.r_out * f.r_in : (long)n * n;
     TBEM_CK(cudaMemsetAsync(in, 0, sizeof(float) * ncs * P.k, stream));
     P.split_b_rows(in, 0, ncs, std::max(ncs, nco), stream);
-    cudaEvent_t e0, e1;
-    TBEM_CK(cudaEventCreate(&e0));
-    TBEM_CK(cudaEventCreate(&e1));
+    ScopedEvent t0, t1;
+    const cudaEvent_t e0 = t0.e, e1 = t1.e;
     float best = 1e30f;
     int best_bn = 128, best_bk = 64;
     const int shapes[4][2] = {{128, 64}, {64, 64}, {128, 32}, {256, 32}};
@@ -620,8 +619,6 @@ void Plan::autotune_tc()
             best_bk = sh[1];
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     G.tc_bn = best_bn;
     G.tc_bk = best_bk;
     for (auto& g : f.m2m) { g.tc_bn = best_bn; g.tc_bk = best_bk; }
@@ -638,9 +635,8 @@ void Plan::autotune_p2p()
     const bool mixed = f.mixed;
     if (mixed) TBEM_CK(cudaMemsetAsync(s32.p, 0, sizeof(float) * R * n_src, stream));
     else TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * n_src, stream));
-    cudaEvent_t e0, e1;
-    TBEM_CK(cudaEventCreate(&e0));
-    TBEM_CK(cudaEventCreate(&e1));
+    ScopedEvent t0, t1;
+    const cudaEvent_t e0 = t0.e, e1 = t1.e;
     float best = 1e30f;
     int best_tpt = 4;
     for (int tpt : {4, 2, 8}) {
@@ -665,8 +661,6 @@ void Plan::autotune_p2p()
             best_tpt = tpt;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     p2p_tpt = best_tpt;
 }
 
@@ -679,9 +673,8 @@ void Plan::autotune_p2m()
     const bool mixed = f.mixed;
     if (mixed) TBEM_CK(cudaMemsetAsync(s32.p, 0, sizeof(float) * R * n_src, stream));
     else TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * n_src, stream));
-    cudaEvent_t e0, e1;
-    TBEM_CK(cudaEventCreate(&e0));
-    TBEM_CK(cudaEventCreate(&e1));
+    ScopedEvent t0, t1;
+    const cudaEvent_t e0 = t0.e, e1 = t1.e;
     float best = 1e30f;
     int best_tpt = 4;
     for (int tpt : {4, 2, 1}) {
@@ -706,8 +699,6 @@ void Plan::autotune_p2m()
             best_tpt = tpt;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     p2m_tpt = best_tpt;
 }
 

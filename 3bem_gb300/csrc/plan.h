@@ -126,6 +126,19 @@ struct DBuf {
     }
 };
 
+// A timing event destroyed on every exit path (the autotuners time
+// candidates between two of these).
+struct ScopedEvent {
+    cudaEvent_t e = nullptr;
+    ScopedEvent() { TBEM_CK(cudaEventCreate(&e)); }
+    ScopedEvent(const ScopedEvent&) = delete;
+    ScopedEvent& operator=(const ScopedEvent&) = delete;
+    ~ScopedEvent()
+    {
+        if (e) cudaEventDestroy(e);
+    }
+};
+
 // A set of obs-owner evaluation tasks (eval.cuh).
 struct TaskSet {
     std::vector<long> tgt;
