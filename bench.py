@@ -145,24 +145,27 @@ def m2l_flops(op, n_rhs):
             "pairs": pairs}
 
 
-def cpu_baseline(locs, nrm, w, x, fraction, threads):
-    """The oracle (CPU restatement of the reference FMM, OpenMP) on the same
-    workload, timed on a bounded sample: the leading `fraction` of every task
-    list, extrapolated to a full apply."""
+def cpu_operators(locs, nrm, w, threads):
+    """The oracle (CPU restatement of the reference FMM, OpenMP) built on the
+    same workload, both kernels.  Returns (operators, setup seconds, threads)."""
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
     from oracle import oracle
     oracle.build()
+    t0 = time.perf_counter()
+    ops = [oracle.OracleFMM(name, locs, nrm, locs, nrm, w, MAC, ORDER, LEAF, D, False, MU, NU)
+           for name in ("ElasticDisplacement", "ElasticTraction")]
+    return ops, time.perf_counter() - t0, oracle.max_threads()
+
+
+def cpu_apply_seconds(ops, x, fraction):
+    """One step of the oracle operators timed on a bounded sample: the leading
+    `fraction` of every task list, extrapolated to a full apply."""
     total = 0.0
-    setups = 0.0
-    for name in ("ElasticDisplacement", "ElasticTraction"):
-        t0 = time.perf_counter()
-        o = oracle.OracleFMM(name, locs, nrm, locs, nrm, w, MAC, ORDER, LEAF, D, False, MU, NU)
-        setups += time.perf_counter() - t0
+    for o in ops:
         t0 = time.perf_counter()
         o.apply(x, list_fraction=fraction)
         total += (time.perf_counter() - t0) / fraction
-        del o
-    return total, setups, oracle.max_threads()
+    return total
 
 
 def run_reference(args, rank, world):
@@ -173,9 +176,11 @@ def run_reference(args, rank, world):
     locs, nrm, w, x = workload()
     threads = os.cpu_count() or 1
     frac = args.cpu_fraction
+    # built once, like the operator of the GPU arm; each step is one apply
+    ops, setup, cores = cpu_operators(locs, nrm, w, threads)
     samples = []
     for i in range(args.warmup + args.steps):
-        t_full, setup, cores = cpu_baseline(locs, nrm, w, x, frac, threads)
+        t_full = cpu_apply_seconds(ops, x, frac)
         if i >= args.warmup:
             samples.append(t_full)
     t = float(np.median(samples))
@@ -191,6 +196,7 @@ def run_reference(args, rank, world):
                                    "extrapolated to a full apply" % frac},
         "e2e": {"value": value, "unit": "points*RHS/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "setup_s": setup,
     }
     print(json.dumps(line), flush=True)
 
@@ -379,7 +385,9 @@ def main():
     cpu = None
     if not args.no_cpu and rank == 0:
         threads = os.cpu_count() or 1
-        t_full, setup, cores = cpu_baseline(locs, nrm, w, x, args.cpu_fraction, threads)
+        cops, _, cores = cpu_operators(locs, nrm, w, threads)
+        t_full = cpu_apply_seconds(cops, x, args.cpu_fraction)
+        del cops
         cpu = {"value": 2 * N / t_full, "unit": "points*RHS/s", "cores": cores, "kind": "port",
                "sample": "oracle FMM apply of both kernels on the leading %.3g of every task "
                          "list, extrapolated to a full apply (%.1f s measured)"
