@@ -32,6 +32,52 @@ def test_library_exports_every_declared_symbol():
     assert sorted(_lib.SIGNATURES) == names
 
 
+def _header_source():
+    src = open(os.path.join(ROOT, "include", "tbem_gpu.h")).read()
+    return re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+
+
+def _ctype_of(decl):
+    """The ctypes class the binding must use for one C declaration (a return
+    type, or a parameter with its name)."""
+    import ctypes as C
+    decl = decl.strip()
+    if "*" in decl:
+        return C.c_char_p if re.fullmatch(r"const\s+char\s*\*", decl) else C.c_void_p
+    base = decl.split()[0] if decl.split()[0] != "const" else decl.split()[1]
+    return {"int": C.c_int, "long": C.c_long, "double": C.c_double, "void": None}[base]
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every function's return and parameter types in the ctypes table equal
+    the header's (int / long / double / pointer), so no argument is truncated
+    or widened at the boundary."""
+    from tbempy import _lib
+    decls = re.findall(r"(int|long|void|const\s+char\s*\*)\s+(tbem_\w+)\s*\(([^)]*)\)\s*;",
+                       _header_source())
+    assert len(decls) == len(_lib.SIGNATURES)
+    for ret, name, params in decls:
+        res, args = _lib.SIGNATURES[name]
+        params = [p for p in (q.strip() for q in params.split(",")) if p and p != "void"]
+        assert res is _ctype_of(ret), name
+        assert len(args) == len(params), name
+        for a, p in zip(args, params):
+            assert a is _ctype_of(p.rsplit(None, 1)[0] + (" *" if "*" in p.rsplit(None, 1)[-1]
+                                                          else "")), (name, p)
+
+
+def test_ctypes_structs_match_the_header():
+    """The option and configuration structs: same fields, same order, same
+    types as the header's typedefs."""
+    from tbempy import _lib
+    src = _header_source()
+    for cls in (_lib.TbemFmmConfig, _lib.TbemGpuOptions, _lib.TbemIntegrator):
+        body = re.search(r"typedef\s+struct\s*\{([^}]*)\}\s*%s\s*;" % cls.__name__, src).group(1)
+        fields = [f.strip().rsplit(None, 1) for f in body.split(";") if f.strip()]
+        assert [n for _, n in fields] == [n for n, _ in cls._fields_], cls.__name__
+        assert [_ctype_of(t) for t, _ in fields] == [t for _, t in cls._fields_], cls.__name__
+
+
 def kernel_from_name(name, dim=3):
     from tbempy import ThreeD, TwoD
     k = getattr(TwoD if dim == 2 else ThreeD, name)
