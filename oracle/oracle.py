@@ -65,7 +65,10 @@ def build(force=False):
     return LIB_PATH
 
 
-def build_ref(ref_root="/root/reference"):
+REF_ROOT = "/root/reference"  # the reference checkout, where one exists
+
+
+def build_ref(ref_root=REF_ROOT):
     """Compile the reference's own sources into oracle/_ref (needs the checkout)."""
     if not os.path.isdir(os.path.join(ref_root, "cpp")):
         return None

@@ -78,6 +78,34 @@ def test_ctypes_structs_match_the_header():
         assert [_ctype_of(t) for t, _ in fields] == [t for _, t in cls._fields_], cls.__name__
 
 
+def test_integration_adapters_compile_against_the_reference(tmp_path):
+    """The C++ adapters the integration guide gives a maintainer (an
+    OperatorI over the FMM handle, a SparseOperator from the nearfield
+    construction) compile against the reference's own headers and
+    include/tbem_gpu.h, templates instantiated."""
+    import shutil
+    import subprocess
+    from oracle import oracle
+    ref = os.path.join(oracle.REF_ROOT, "cpp")
+    gxx = shutil.which("g++")
+    if gxx is None or not os.path.isdir(ref):
+        pytest.skip("needs g++ and the reference checkout")
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```cpp\n(.*?)```", text, flags=re.S)
+    assert len(blocks) >= 2
+    for i, b in enumerate(blocks):
+        for m in re.finditer(r"template\s*<size_t R>\s*struct (\w+)", b):
+            b += "\ntemplate struct tbem::%s<1>;\ntemplate struct tbem::%s<3>;\n" % (m.group(1),
+                                                                                 m.group(1))
+        src = tmp_path / ("adapter%d.cpp" % i)
+        src.write_text(b)
+        r = subprocess.run([gxx, "-std=c++14", "-fsyntax-only", "-include", "cstddef", "-include",
+                            "stdexcept", "-include", "ostream", "-I", ref, "-I",
+                            os.path.join(ROOT, "include"), str(src)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-2000:]
+
+
 def kernel_from_name(name, dim=3):
     from tbempy import ThreeD, TwoD
     k = getattr(TwoD if dim == 2 else ThreeD, name)
