@@ -496,19 +496,21 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
         if (!adaptive_items.empty()) {
             // the adaptive Gauss-Lobatto rule: subdivision on the host,
             // every level's points on the GPU
+            // buffers kept across the levels (each level's batch has its own size)
             DBuf<int> d_pi;
             DBuf<double> d_x0, d_x1, d_pv;
+            std::vector<int> it;
             nf::InfluenceEval eval = [&](const std::vector<long>& item, const std::vector<double>& x0,
                                          const std::vector<double>& x1, std::vector<double>& out) {
                 const long n = (long)item.size();
-                out.assign((size_t)n * E, 0.0);
+                out.resize((size_t)n * E);  // every value is copied back below
                 if (n == 0) return;
-                std::vector<int> it(n);
-                for (long k = 0; k < n; k++) it[k] = (int)adaptive_items[item[k]];
-                d_pi.upload(it);
-                d_x0.upload(x0);
-                d_x1.upload(x1);
-                d_pv.alloc((size_t)n * E);
+                it.resize(n);
+                nf::parallel_for(n, [&](long k) { it[k] = (int)adaptive_items[item[k]]; }, 1 << 16);
+                d_pi.upload_grow(it);
+                d_x0.upload_grow(x0);
+                d_x1.upload_grow(x1);
+                d_pv.ensure((size_t)n * E);
                 if (dim == 2 && R == 1) launch_points<2, 1>(a, d_pi.p, d_x0.p, d_x1.p, n, d_pv.p);
                 else if (dim == 2) launch_points<2, 2>(a, d_pi.p, d_x0.p, d_x1.p, n, d_pv.p);
                 else if (R == 1) launch_points<3, 1>(a, d_pi.p, d_x0.p, d_x1.p, n, d_pv.p);

@@ -98,9 +98,10 @@ V3 limit_direction(const V3& p, const FacetSet& all, int dim);
 ObsPoints galerkin_obs_points(const std::vector<Facet>& obs, const FacetSet& all, int order,
                               int dim);
 
-// body(i) for i in [0, n) over the host's cores (contiguous chunks; each i
-// writes only its own outputs, so the results do not depend on the split).
-void parallel_for(long n, const std::function<void(long)>& body);
+// body(i) for i in [0, n) over the host's cores (contiguous chunks of at
+// least `grain` indices per thread; each i writes only its own outputs, so
+// the results do not depend on the split).
+void parallel_for(long n, const std::function<void(long)>& body, long grain = 256);
 
 // Batched evaluation of the functions being integrated: for point k, the
 // value (E numbers) of job[k]'s function at t[k], written to out[k * E ...].

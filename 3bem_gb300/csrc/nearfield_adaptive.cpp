@@ -11,8 +11,15 @@
 // the recursive rule decides; at the end every tree is summed in the
 // recursion's order.  In 3D the outer rule's function values are inner
 // integrals, computed the same way in one batch per outer level.
+//
+// The host work between the batches (emitting points, the stop rule, the
+// splits, the final sums) runs on all host cores: the terms are dealt to
+// chunks, each chunk keeps its own trees, and every term's arithmetic is the
+// recursion's, in its order, whichever chunk and thread it lands on.
+#include <algorithm>
 #include <cmath>
 #include <limits>
+#include <thread>
 
 #include "nearfield.h"
 
@@ -48,10 +55,234 @@ struct Node {
     long value = -1;  // slot of the leaf's estimate i1
 };
 
-struct Job {
-    long root = -1;
-    long err = -1;  // slot of the error target is (E values)
+// The jobs j = c, c + C, c + 2C, ... of chunk c (dealt round robin, so that
+// runs of hard terms spread over the chunks) with their trees and values.
+struct Chunk {
+    std::vector<long> job;        // job ids
+    std::vector<long> root, err;  // per local job: root node, error-target slot
+    std::vector<Node> nodes;
+    std::vector<double> pool;  // E values per slot
+    std::vector<long> open, open_job, next, next_job;  // open nodes, their local job
+    long offset = 0;  // this chunk's first point in the current batch
+    long slot(const double* v, int E)
+    {
+        const long s = (long)(pool.size() / E);
+        pool.insert(pool.end(), v, v + E);
+        return s;
+    }
+    void reset()  // empty, keeping the memory
+    {
+        for (auto* v : {&job, &root, &err, &open, &open_job, &next, &next_job}) v->clear();
+        nodes.clear();
+        pool.clear();
+    }
 };
+
+// The buffers of one batch driver, kept between its calls: the 3D inner
+// integrals run one batch per outer level, and reusing memory already
+// touched spares the page faults of fresh gigabyte-sized buffers.
+struct Work {
+    std::vector<Chunk> ch;
+    std::vector<long> pj;
+    std::vector<double> pt, y;
+};
+
+// adaptive_batch over a[0..n), b[0..n) into total ([n][E]), with w's buffers.
+void run_batch(int E, const double* a, const double* b, long n, double p_tol, const AdaptiveEval& eval,
+               Work& w, std::vector<double>& total)
+{
+    total.resize((size_t)n * E);
+    if (n == 0) return;
+    const long hw = (long)std::max(1u, std::thread::hardware_concurrency());
+    const long C = std::max(1L, std::min(4 * hw, n / 64));
+    if ((long)w.ch.size() < C) w.ch.resize(C);
+    std::vector<Chunk>& ch = w.ch;
+    for (Chunk& k : ch) k.reset();
+    for (long c = 0; c < C; c++)
+        for (long j = c; j < n; j += C) ch[c].job.push_back(j);
+    std::vector<long>& pj = w.pj;
+    std::vector<double>&pt = w.pt, &y = w.y;
+    // lays the chunks' points out one after the other: count(chunk) points each
+    auto layout = [&](long (*count)(const Chunk&)) {
+        long tot = 0;
+        for (Chunk& k : ch) {
+            k.offset = tot;
+            tot += count(k);
+        }
+        pj.resize(tot);
+        pt.resize(tot);
+        return tot;
+    };
+
+    // the initial 13-point stage (adaptive_integrate, cpp/adaptive_quad.h:128-171)
+    layout([](const Chunk& k) { return 13 * (long)k.job.size(); });
+    parallel_for(
+        C,
+        [&](long c) {
+            const Chunk& k = ch[c];
+            long o = k.offset;
+            for (long j : k.job) {
+                const double m = (a[j] + b[j]) / 2., h = (b[j] - a[j]) / 2.;
+                const double xs[13] = {a[j], m - kX1 * h, m - kAlpha * h, m - kX2 * h, m - kBeta * h,
+                                       m - kX3 * h, m, m + kX3 * h, m + kBeta * h, m + kX2 * h,
+                                       m + kAlpha * h, m + kX1 * h, b[j]};
+                for (double x : xs) {
+                    pj[o] = j;
+                    pt[o++] = x;
+                }
+            }
+        },
+        1);
+    eval(pj, pt, y);
+    parallel_for(
+        C,
+        [&](long c) {
+            Chunk& k = ch[c];
+            std::vector<double> i1(E), i2(E), is(E), err(E);
+            const long nj = (long)k.job.size();
+            k.root.resize(nj);
+            k.err.resize(nj);
+            for (long q = 0; q < nj; q++) {
+                const long j = k.job[q];
+                const double* Y = &y[(size_t)(k.offset + 13 * q) * E];
+                const double h = (b[j] - a[j]) / 2.;
+                for (int e = 0; e < E; e++) {
+                    auto v = [&](int i) { return Y[i * E + e]; };
+                    i2[e] = (h / 6.0) * (v(0) + v(12) + 5.0 * (v(4) + v(8)));
+                    i1[e] = (h / 1470.0) * (77.0 * (v(0) + v(12)) + 432.0 * (v(2) + v(10)) +
+                                            625.0 * (v(4) + v(8)) + 672.0 * v(6));
+                    is[e] = h * (kW[0] * (v(0) + v(12)) + kW[1] * (v(1) + v(11)) + kW[2] * (v(2) + v(10)) +
+                                 kW[3] * (v(3) + v(9)) + kW[4] * (v(4) + v(8)) + kW[5] * (v(5) + v(7)) +
+                                 kW[6] * v(6));
+                    err[e] = error_is(p_tol, std::fabs(i1[e] - is[e]), std::fabs(i2[e] - is[e]), is[e], a[j],
+                                      b[j]);
+                }
+                k.err[q] = k.slot(err.data(), E);
+                Node root;
+                root.a = a[j];
+                root.b = b[j];
+                root.fa = k.slot(Y, E);
+                root.fb = k.slot(Y + 12 * E, E);
+                k.root[q] = (long)k.nodes.size();
+                k.nodes.push_back(root);
+                k.open.push_back(k.root[q]);
+                k.open_job.push_back(q);
+            }
+        },
+        1);
+
+    // breadth-first adaptlobstp (cpp/adaptive_quad.h:40-79)
+    while (layout([](const Chunk& k) { return 5 * (long)k.open.size(); }) > 0) {
+        parallel_for(
+            C,
+            [&](long c) {
+                const Chunk& k = ch[c];
+                long o = k.offset;
+                for (size_t i = 0; i < k.open.size(); i++) {
+                    const Node& nd = k.nodes[k.open[i]];
+                    const double m = (nd.a + nd.b) / 2., h = (nd.b - nd.a) / 2.;
+                    const double xs[5] = {m - kAlpha * h, m - kBeta * h, m, m + kBeta * h, m + kAlpha * h};
+                    const long j = k.job[k.open_job[i]];
+                    for (double x : xs) {
+                        pj[o] = j;
+                        pt[o++] = x;
+                    }
+                }
+            },
+            1);
+        eval(pj, pt, y);
+        parallel_for(
+            C,
+            [&](long c) {
+                Chunk& k = ch[c];
+                std::vector<double> i1(E), i2(E);
+                k.next.clear();
+                k.next_job.clear();
+                for (size_t i = 0; i < k.open.size(); i++) {
+                    const long id = k.open[i];
+                    const long q = k.open_job[i];
+                    const double na = k.nodes[id].a, nb = k.nodes[id].b;
+                    const double m = (na + nb) / 2., h = (nb - na) / 2.;
+                    const double mll = m - kAlpha * h, ml = m - kBeta * h, mr = m + kBeta * h,
+                                 mrr = m + kAlpha * h;
+                    const double* Y = &y[(size_t)(k.offset + 5 * (long)i) * E];  // fmll, fml, fm, fmr, fmrr
+                    const double* fa = &k.pool[(size_t)k.nodes[id].fa * E];
+                    const double* fb = &k.pool[(size_t)k.nodes[id].fb * E];
+                    const double* target = &k.pool[(size_t)k.err[q] * E];
+                    bool converged = true;
+                    for (int e = 0; e < E; e++) {
+                        i2[e] = (h / 6.) * (fa[e] + fb[e] + 5.0 * (Y[E + e] + Y[3 * E + e]));
+                        i1[e] = (h / 1470.) * (77.0 * (fa[e] + fb[e]) + 432.0 * (Y[e] + Y[4 * E + e]) +
+                                               625.0 * (Y[E + e] + Y[3 * E + e]) + 672.0 * Y[2 * E + e]);
+                        converged = converged && (target[e] + (i1[e] - i2[e]) == target[e]);
+                    }
+                    if (converged || mll <= na || nb <= mrr) {
+                        const long v = k.slot(i1.data(), E);
+                        k.nodes[id].value = v;
+                        continue;
+                    }
+                    long s[5];
+                    for (int r = 0; r < 5; r++) s[r] = k.slot(Y + r * E, E);
+                    const double cut[7] = {na, mll, ml, m, mr, mrr, nb};
+                    const long fs[7] = {k.nodes[id].fa, s[0], s[1], s[2], s[3], s[4], k.nodes[id].fb};
+                    const long first = (long)k.nodes.size();
+                    for (int r = 0; r < 6; r++) {
+                        Node child;
+                        child.a = cut[r];
+                        child.b = cut[r + 1];
+                        child.fa = fs[r];
+                        child.fb = fs[r + 1];
+                        k.nodes.push_back(child);
+                        k.next.push_back(first + r);
+                        k.next_job.push_back(q);
+                    }
+                    k.nodes[id].first = first;
+                }
+                k.open.swap(k.next);
+                k.open_job.swap(k.next_job);
+            },
+            1);
+    }
+
+    // sum every tree in the recursion's order: ((((c1 + c2) + c3) + c4) + c5) + c6,
+    // post-order with an explicit stack and one partial sum per depth
+    parallel_for(
+        C,
+        [&](long c) {
+            const Chunk& k = ch[c];
+            std::vector<std::pair<long, int>> st;  // node, children entered
+            std::vector<double> part;
+            for (size_t q = 0; q < k.job.size(); q++) {
+                double* out = &total[(size_t)k.job[q] * E];
+                st.assign(1, {k.root[q], 0});
+                while (!st.empty()) {
+                    const Node& nd = k.nodes[st.back().first];
+                    const double* ret;
+                    if (nd.first < 0) {  // leaf: its estimate
+                        ret = &k.pool[(size_t)nd.value * E];
+                    } else if (st.back().second < 6) {
+                        const int r = st.back().second++;
+                        st.push_back({nd.first + r, 0});
+                        if (part.size() < st.size() * E) part.resize(st.size() * E);
+                        continue;
+                    } else {  // all six children summed
+                        ret = &part[(st.size() - 1) * E];
+                    }
+                    st.pop_back();
+                    if (st.empty()) {
+                        std::copy(ret, ret + E, out);
+                        break;
+                    }
+                    // fold ret into the parent: the first child starts the sum
+                    double* p = &part[(st.size() - 1) * E];
+                    if (st.back().second == 1) std::copy(ret, ret + E, p);
+                    else
+                        for (int e = 0; e < E; e++) p[e] = p[e] + ret[e];
+                }
+            }
+        },
+        1);
+}
 
 }  // namespace
 
@@ -61,172 +292,41 @@ struct Job {
 std::vector<double> adaptive_batch(int E, const std::vector<double>& a, const std::vector<double>& b,
                                    double p_tol, const AdaptiveEval& eval)
 {
-    const long n = (long)a.size();
-    std::vector<double> pool;  // E values per slot
-    auto slot = [&](const double* v) {
-        const long s = (long)(pool.size() / E);
-        pool.insert(pool.end(), v, v + E);
-        return s;
-    };
-    std::vector<Node> nodes;
-    std::vector<Job> jobs(n);
-    // the initial 13-point stage (adaptive_integrate, cpp/adaptive_quad.h:128-171)
-    {
-        std::vector<long> pj;
-        std::vector<double> pt;
-        for (long j = 0; j < n; j++) {
-            const double m = (a[j] + b[j]) / 2., h = (b[j] - a[j]) / 2.;
-            const double xs[13] = {a[j], m - kX1 * h, m - kAlpha * h, m - kX2 * h, m - kBeta * h,
-                                   m - kX3 * h, m, m + kX3 * h, m + kBeta * h, m + kX2 * h,
-                                   m + kAlpha * h, m + kX1 * h, b[j]};
-            for (double x : xs) {
-                pj.push_back(j);
-                pt.push_back(x);
-            }
-        }
-        std::vector<double> y;
-        if (!pj.empty()) eval(pj, pt, y);
-        std::vector<double> i1(E), i2(E), is(E), err(E);
-        for (long j = 0; j < n; j++) {
-            const double* Y = &y[(size_t)j * 13 * E];
-            const double h = (b[j] - a[j]) / 2.;
-            for (int e = 0; e < E; e++) {
-                auto v = [&](int k) { return Y[k * E + e]; };
-                i2[e] = (h / 6.0) * (v(0) + v(12) + 5.0 * (v(4) + v(8)));
-                i1[e] = (h / 1470.0) *
-                        (77.0 * (v(0) + v(12)) + 432.0 * (v(2) + v(10)) + 625.0 * (v(4) + v(8)) + 672.0 * v(6));
-                is[e] = h * (kW[0] * (v(0) + v(12)) + kW[1] * (v(1) + v(11)) + kW[2] * (v(2) + v(10)) +
-                             kW[3] * (v(3) + v(9)) + kW[4] * (v(4) + v(8)) + kW[5] * (v(5) + v(7)) +
-                             kW[6] * v(6));
-                err[e] = error_is(p_tol, std::fabs(i1[e] - is[e]), std::fabs(i2[e] - is[e]), is[e], a[j], b[j]);
-            }
-            jobs[j].err = slot(err.data());
-            Node root;
-            root.a = a[j];
-            root.b = b[j];
-            root.fa = slot(Y);
-            root.fb = slot(Y + 12 * E);
-            jobs[j].root = (long)nodes.size();
-            nodes.push_back(root);
-        }
-    }
-    // breadth-first adaptlobstp (cpp/adaptive_quad.h:40-79)
-    std::vector<long> open, open_job;
-    for (long j = 0; j < n; j++) {
-        open.push_back(jobs[j].root);
-        open_job.push_back(j);
-    }
-    std::vector<double> i1(E), i2(E);
-    while (!open.empty()) {
-        std::vector<long> pj;
-        std::vector<double> pt;
-        for (size_t k = 0; k < open.size(); k++) {
-            const Node& nd = nodes[open[k]];
-            const double m = (nd.a + nd.b) / 2., h = (nd.b - nd.a) / 2.;
-            const double xs[5] = {m - kAlpha * h, m - kBeta * h, m, m + kBeta * h, m + kAlpha * h};
-            for (double x : xs) {
-                pj.push_back(open_job[k]);
-                pt.push_back(x);
-            }
-        }
-        std::vector<double> y;
-        eval(pj, pt, y);
-        std::vector<long> next, next_job;
-        for (size_t k = 0; k < open.size(); k++) {
-            const long id = open[k];
-            const long j = open_job[k];
-            const double na = nodes[id].a, nb = nodes[id].b;
-            const double m = (na + nb) / 2., h = (nb - na) / 2.;
-            const double mll = m - kAlpha * h, ml = m - kBeta * h, mr = m + kBeta * h, mrr = m + kAlpha * h;
-            const double* Y = &y[k * 5 * E];  // fmll, fml, fm, fmr, fmrr
-            const double* fa = &pool[(size_t)nodes[id].fa * E];
-            const double* fb = &pool[(size_t)nodes[id].fb * E];
-            const double* target = &pool[(size_t)jobs[j].err * E];
-            bool converged = true;
-            for (int e = 0; e < E; e++) {
-                i2[e] = (h / 6.) * (fa[e] + fb[e] + 5.0 * (Y[E + e] + Y[3 * E + e]));
-                i1[e] = (h / 1470.) * (77.0 * (fa[e] + fb[e]) + 432.0 * (Y[e] + Y[4 * E + e]) +
-                                       625.0 * (Y[E + e] + Y[3 * E + e]) + 672.0 * Y[2 * E + e]);
-                converged = converged && (target[e] + (i1[e] - i2[e]) == target[e]);
-            }
-            if (converged || mll <= na || nb <= mrr) {
-                nodes[id].value = slot(i1.data());
-                continue;
-            }
-            long s[5];
-            for (int q = 0; q < 5; q++) s[q] = slot(Y + q * E);
-            const double cut[7] = {na, mll, ml, m, mr, mrr, nb};
-            const long fs[7] = {nodes[id].fa, s[0], s[1], s[2], s[3], s[4], nodes[id].fb};
-            const long first = (long)nodes.size();
-            for (int c = 0; c < 6; c++) {
-                Node ch;
-                ch.a = cut[c];
-                ch.b = cut[c + 1];
-                ch.fa = fs[c];
-                ch.fb = fs[c + 1];
-                nodes.push_back(ch);
-                next.push_back(first + c);
-                next_job.push_back(j);
-            }
-            nodes[id].first = first;
-        }
-        open.swap(next);
-        open_job.swap(next_job);
-    }
-    // sum every tree in the recursion's order: ((((c1 + c2) + c3) + c4) + c5) + c6
-    std::vector<double> total((size_t)n * E), acc;
-    std::vector<std::pair<long, int>> stack;
-    for (long j = 0; j < n; j++) {
-        // post-order with an explicit stack; acc holds partial sums per depth
-        std::vector<std::vector<double>> partial;
-        stack.clear();
-        stack.push_back({jobs[j].root, 0});
-        partial.push_back(std::vector<double>(E, 0.0));
-        std::vector<double> ret(E);
-        while (!stack.empty()) {
-            auto& top = stack.back();
-            const Node& nd = nodes[top.first];
-            if (nd.first < 0) {  // leaf: its estimate
-                for (int e = 0; e < E; e++) ret[e] = pool[(size_t)nd.value * E + e];
-            } else if (top.second < 6) {
-                const int c = top.second++;
-                stack.push_back({nd.first + c, 0});
-                partial.push_back(std::vector<double>(E, 0.0));
-                continue;
-            } else {
-                ret = partial.back();
-            }
-            stack.pop_back();
-            partial.pop_back();
-            if (stack.empty()) break;
-            // fold ret into the parent: the first child starts the sum
-            std::vector<double>& p = partial.back();
-            if (stack.back().second == 1) p = ret;
-            else
-                for (int e = 0; e < E; e++) p[e] = p[e] + ret[e];
-        }
-        for (int e = 0; e < E; e++) total[(size_t)j * E + e] = ret[e];
-    }
+    Work w;
+    std::vector<double> total;
+    run_batch(E, a.data(), b.data(), (long)a.size(), p_tol, eval, w, total);
     return total;
 }
 
 std::vector<double> adaptive_facet_integrals(int dim, int E, long n_items, double tol,
                                              const InfluenceEval& eval)
 {
+    Work outer;
+    std::vector<double> total;
     if (dim == 2) {
         const std::vector<double> a(n_items, -1.0), b(n_items, 1.0);
-        return adaptive_batch(E, a, b, tol, [&](const std::vector<long>& job, const std::vector<double>& t,
-                                                std::vector<double>& out) {
-            eval(job, t, std::vector<double>(t.size(), 0.0), out);
-        });
+        std::vector<double> zeros;
+        run_batch(
+            E, a.data(), b.data(), n_items, tol,
+            [&](const std::vector<long>& job, const std::vector<double>& t, std::vector<double>& out) {
+                zeros.assign(t.size(), 0.0);
+                eval(job, t, zeros, out);
+            },
+            outer, total);
+        return total;
     }
     const std::vector<double> a(n_items, 0.0), b(n_items, 1.0);
-    return adaptive_batch(E, a, b, tol, [&](const std::vector<long>& job, const std::vector<double>& xs,
-                                            std::vector<double>& out) {
+    // kept across the outer levels (each runs one inner batch)
+    Work inner;
+    std::vector<long> inner_item, inner_of, it;
+    std::vector<double> ia, ib, ix, x0, v;
+    run_batch(
+        E, a.data(), b.data(), n_items, tol,
+        [&](const std::vector<long>& job, const std::vector<double>& xs, std::vector<double>& out) {
         // the outer function at x: the inner integral over y in [0, 1 - x]
         out.assign(xs.size() * E, 0.0);
-        std::vector<long> inner_item, inner_of;
-        std::vector<double> ia, ib, ix;
+        for (auto* u : {&inner_item, &inner_of}) u->clear();
+        for (auto* u : {&ia, &ib, &ix}) u->clear();
         for (size_t k = 0; k < xs.size(); k++) {
             if (xs[k] == 1.0) continue;  // zero, as the reference's outer lambda returns
             inner_item.push_back(job[k]);
@@ -236,20 +336,26 @@ std::vector<double> adaptive_facet_integrals(int dim, int E, long n_items, doubl
             ix.push_back(xs[k]);
         }
         if (inner_item.empty()) return;
-        const std::vector<double> v =
-            adaptive_batch(E, ia, ib, tol, [&](const std::vector<long>& ij, const std::vector<double>& ys,
-                                               std::vector<double>& o) {
-                std::vector<long> it(ij.size());
-                std::vector<double> x0(ij.size());
-                for (size_t q = 0; q < ij.size(); q++) {
-                    it[q] = inner_item[ij[q]];
-                    x0[q] = ix[ij[q]];
-                }
+        run_batch(
+            E, ia.data(), ib.data(), (long)ia.size(), tol,
+            [&](const std::vector<long>& ij, const std::vector<double>& ys, std::vector<double>& o) {
+                it.resize(ij.size());
+                x0.resize(ij.size());
+                parallel_for(
+                    (long)ij.size(),
+                    [&](long q) {
+                        it[q] = inner_item[ij[q]];
+                        x0[q] = ix[ij[q]];
+                    },
+                    1 << 16);
                 eval(it, x0, ys, o);
-            });
+            },
+            inner, v);
         for (size_t q = 0; q < inner_of.size(); q++)
             for (int e = 0; e < E; e++) out[(size_t)inner_of[q] * E + e] = v[q * E + e];
-    });
+        },
+        outer, total);
+    return total;
 }
 
 }  // namespace nf

@@ -593,10 +593,10 @@ V3 limit_direction(const V3& p, const FacetSet& all, int dim)
     return d;
 }
 
-void parallel_for(long n, const std::function<void(long)>& body)
+void parallel_for(long n, const std::function<void(long)>& body, long grain)
 {
     const long hw = (long)std::max(1u, std::thread::hardware_concurrency());
-    const long nt = std::min(hw, std::max(1L, n / 256));
+    const long nt = std::min(hw, std::max(1L, n / std::max(1L, grain)));
     if (nt <= 1) {
         for (long i = 0; i < n; i++) body(i);
         return;

@@ -115,6 +115,16 @@ struct DBuf {
             TBEM_CK(cudaStreamSynchronize(cudaStreamLegacy));
         }
     }
+    // The same into the first v.size() elements, growing the buffer only when
+    // it is too small: repeated uploads of varying sizes keep one allocation.
+    void upload_grow(const std::vector<T>& v)
+    {
+        ensure(v.size());
+        if (!v.empty()) {
+            TBEM_CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+            TBEM_CK(cudaStreamSynchronize(cudaStreamLegacy));
+        }
+    }
     std::vector<T> download() const
     {
         std::vector<T> v(n);

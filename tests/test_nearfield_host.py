@@ -49,10 +49,11 @@ def test_gauss_rules_integrate_polynomials():
                 assert abs((w * x[:, 0] ** a * x[:, 1] ** b).sum() - exact) < 1e-12
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/cpp"), reason="reference checkout absent")
 def test_gauss_rules_match_reference():
     from oracle import oracle
     from tbempy import ThreeD
+    if not os.path.isdir(os.path.join(oracle.REF_ROOT, "cpp")):
+        pytest.skip("reference checkout absent")
     if not oracle.ref_available():
         pytest.skip("reference library not built here")
     for dim in (2, 3):
@@ -170,17 +171,20 @@ def test_dense_operator_host_side():
         ThreeD.DenseOperator(3, 5, d)
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/cpp"), reason="reference checkout absent")
-@pytest.mark.parametrize("kernel,dim", [(0, 3), (1, 3), (3, 3), (6, 3), (16, 2), (19, 2), (22, 2)])
-def test_adaptive_engine_matches_reference(kernel, dim, tmp_path):
+@pytest.mark.parametrize("kernel,dim,n_terms", [(0, 3, 6), (1, 3, 6), (3, 3, 6), (6, 3, 6),
+                                                (16, 2, 6), (19, 2, 6), (22, 2, 6),
+                                                (1, 3, 160), (17, 2, 600)])
+def test_adaptive_engine_matches_reference(kernel, dim, n_terms, tmp_path):
     """The level-by-level adaptive Gauss-Lobatto engine the product drives
     (3bem_gb300/csrc/nearfield_adaptive.cpp), run here with the oracle's CPU
     kernels as its point evaluator (tests/cpp/adaptive_driver.cpp; the product
     evaluates the same points on the GPU), equals the reference's recursive
     integrator (cpp/adaptive_quad.h via compute_term) bit for bit on near
-    terms."""
+    terms; the larger cases spread the terms over several host chunks."""
     import subprocess
     from oracle import oracle
+    if not os.path.isdir(os.path.join(oracle.REF_ROOT, "cpp")):
+        pytest.skip("reference checkout absent")
     if not oracle.ref_available():
         pytest.skip("reference library not built here")
     exe = str(tmp_path / "adaptive_driver")
@@ -197,7 +201,7 @@ def test_adaptive_engine_matches_reference(kernel, dim, tmp_path):
              else np.array([[0, 0, 0], [1.0, 0.2, 0]]))
     tol = 1e-5
     terms = []
-    for _ in range(6):
+    for _ in range(n_terms):
         obs = facet.mean(axis=0) + rng.normal(size=3) * 0.3
         n = rng.normal(size=3)
         if dim == 2:

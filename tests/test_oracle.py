@@ -98,7 +98,7 @@ def test_circle_surface_known_values():
         assert len(oracle.surface(int(o), 2)) == c == o
 
 
-REF_ELASTIC = "/root/reference/unit_tests/test_data_elastic3"
+REF_ELASTIC = os.path.join(oracle.REF_ROOT, "unit_tests", "test_data_elastic3")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_ELASTIC), reason="reference checkout absent")
@@ -125,7 +125,7 @@ def test_elastic_kernels_against_reference_sympy_data():
     assert n == 360
 
 
-REF_ELASTIC_2D = "/root/reference/unit_tests/test_data_elastic2"
+REF_ELASTIC_2D = os.path.join(oracle.REF_ROOT, "unit_tests", "test_data_elastic2")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_ELASTIC_2D), reason="reference checkout absent")
