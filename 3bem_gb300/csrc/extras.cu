@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "handle.h"
+#include "nearfield.h"
 
 namespace {
 
@@ -183,17 +184,26 @@ int tbem_csr_create(long n_rows, long n_cols, const double* values, const long* 
             if (row_ptrs[i + 1] < row_ptrs[i]) throw Error(TBEM_ERR_ARG, "row_ptrs must not decrease");
         const long nnz = row_ptrs[n_rows];
         if (nnz > 0 && (!values || !column_indices)) throw Error(TBEM_ERR_ARG, "null values");
-        for (long k = 0; k < nnz; k++)
-            if (column_indices[k] < 0 || column_indices[k] >= n_cols)
-                throw Error(TBEM_ERR_ARG, "column index out of range");
+        // column check on all host cores, in blocks (one flag per block)
+        const long block = 1 << 20, n_blocks = (nnz + block - 1) / block;
+        std::vector<char> bad(n_blocks, 0);
+        nf::parallel_for(
+            n_blocks,
+            [&](long b) {
+                for (long k = b * block; k < std::min(nnz, (b + 1) * block); k++)
+                    if (column_indices[k] < 0 || column_indices[k] >= n_cols) bad[b] = 1;
+            },
+            1);
+        if (std::find(bad.begin(), bad.end(), 1) != bad.end())
+            throw Error(TBEM_ERR_ARG, "column index out of range");
         auto h = std::make_unique<TbemCsr>();
         h->n_rows = n_rows;
         h->n_cols = n_cols;
         h->nnz = nnz;
-        h->rowptr.upload(std::vector<long>(row_ptrs, row_ptrs + n_rows + 1));
+        h->rowptr.upload(row_ptrs, (size_t)n_rows + 1);
         if (nnz > 0) {
-            h->col.upload(std::vector<long>(column_indices, column_indices + nnz));
-            h->val.upload(std::vector<double>(values, values + nnz));
+            h->col.upload(column_indices, (size_t)nnz);
+            h->val.upload(values, (size_t)nnz);
         }
         *out = h.release();
         return TBEM_OK;

@@ -352,69 +352,20 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
     const long n_pts = (long)pts.loc.size();
     if (n_pts > (long)INT32_MAX) throw Error(TBEM_ERR_ARG, "too many observation points");
 
-    // terms: every observation point against its nearfield source facets,
-    // in the reference's loop order
-    std::vector<std::vector<size_t>> near_of(n_pts);
-    nf::parallel_for(n_pts, [&](long i) {
-        size_t nearest = 0;
-        double dist = 0.0;
-        src_set.find(pts.loc[i], mthd->far_threshold, near_of[i], nearest, dist);
-    });
-    std::vector<int> t_obs, t_fac;
-    for (long i = 0; i < n_pts; i++)
-        for (size_t f : near_of[i]) {
-            t_obs.push_back((int)i);
-            t_fac.push_back((int)f);
-        }
-    const long n_terms = (long)t_obs.size();
+    // every (point, nearfield facet) term in the reference's order, classified
+    // as IntegrationStrategy::compute_term does (far / near / singular), with
+    // its evaluations: one for a far or near term, n_steps at the stepped-back
+    // points for a singular one; the correction matrix (which 1) is
+    // -compute_farfield of every term (host, all cores)
     const int E = dim * R * R;
-    // classify every term as IntegrationStrategy::compute_term does
-    // (cpp/integral_term.cpp:33-53) and list its evaluations: one for a far
-    // or near term, n_steps (at the stepped-back points, get_step_loc,
-    // cpp/integral_term.cpp:55-60) for a singular one
     const int n_steps = (int)mthd->n_singular_steps;
-    std::vector<long> first(n_terms);
-    std::vector<char> sing(n_terms, 0);
-    std::vector<int> i_obs, i_fac, i_near;
-    std::vector<double> iloc;
-    auto add_item = [&](long o, long f, int nearflag, const nf::V3& at) {
-        i_obs.push_back((int)o);
-        i_fac.push_back((int)f);
-        i_near.push_back(nearflag);
-        for (int d = 0; d < 3; d++) iloc.push_back(at[d]);
-    };
-    for (long t = 0; t < n_terms; t++) {
-        const long o = t_obs[t], f = t_fac[t];
-        first[t] = (long)i_obs.size();
-        const nf::V3& p = pts.loc[o];
-        if (which == 1) {  // -compute_farfield for every term
-            add_item(o, f, 0, p);
-            continue;
-        }
-        const double dist = nf::closest_point(p, src[f], dim).dist;
-        const double ls = src_set.info(f).length_scale;
-        if (dist < mthd->far_threshold * ls) {
-            double d2 = 0.0;
-            for (int d = 0; d < dim; d++) d2 += pts.dir[o][d] * pts.dir[o][d];
-            if (dist < 1.0 * ls && d2 > 1e-10 * ls) {
-                sing[t] = 1;
-                for (int k = 0; k < n_steps; k++) {
-                    const double step = 1.0 / std::pow(2.0, (double)k);
-                    const double sd = 1.0 * step;
-                    nf::V3 q;
-                    for (int d = 0; d < 3; d++) q[d] = p[d] + sd * pts.dir[o][d];
-                    add_item(o, f, 1, q);
-                }
-            } else {
-                if (!(dist > 0.0) && mthd->strategy == TBEM_QUAD_SINH)
-                    throw Error(TBEM_ERR_ARG, "an observation point lies on a source facet without a "
-                                              "limit direction (the reference's sinh rule asserts here)");
-                add_item(o, f, 1, p);
-            }
-        } else {
-            add_item(o, f, 0, p);
-        }
-    }
+    nf::TermPlan tp = nf::plan_terms(pts, src, src_set, mthd->far_threshold, n_steps, dim, which == 1);
+    if (tp.on_facet && mthd->strategy == TBEM_QUAD_SINH)
+        throw Error(TBEM_ERR_ARG, "an observation point lies on a source facet without a "
+                                  "limit direction (the reference's sinh rule asserts here)");
+    const std::vector<int>&i_obs = tp.i_obs, &i_fac = tp.i_fac;
+    std::vector<int>& i_near = tp.i_near;
+    const std::vector<double>& iloc = tp.iloc;
     const long n_items = (long)i_obs.size();
     // the adaptive evaluations name their item as int on the device
     if (n_items > (long)INT32_MAX) throw Error(TBEM_ERR_ARG, "too many nearfield terms");
@@ -525,48 +476,12 @@ int build_nearfield_csr(int kernel, int dim, int R, double mu, double nu, const 
                     ivals[(size_t)adaptive_items[k] * E + e] = v[k * E + e];
         }
     }
-    // per term: the evaluation, its negation (farfield correction) or the
-    // Richardson limit of its steps (richardson_limit, cpp/richardson.h:10-34)
-    std::vector<double> vals((size_t)n_terms * E);
-    std::vector<double> tab(n_steps);
-    for (long t = 0; t < n_terms; t++) {
-        for (int e = 0; e < E; e++) {
-            double v;
-            if (sing[t]) {
-                for (int k = 0; k < n_steps; k++) tab[k] = ivals[(size_t)(first[t] + k) * E + e];
-                for (int m = 1; m < n_steps; m++) {
-                    const double mult = std::pow(2.0, m);
-                    const double factor = 1.0 / (mult - 1.0);
-                    for (int i = 0; i < n_steps - m; i++) tab[i] = factor * (mult * tab[i + 1] - tab[i]);
-                }
-                v = tab[0];
-            } else {
-                v = ivals[(size_t)first[t] * E + e];
-            }
-            vals[(size_t)t * E + e] = which == 1 ? -v : v;
-        }
-    }
-    // COO entries in the reference's order (cpp/nearfield_operator.h:59-84),
-    // rows d1 * n_pts + point, columns d2 * n_dofs + facet * dim + basis;
-    // a stable sort by row gives csr_from_coo's layout
-    const long n_dofs = (long)src.size() * dim;
-    const long n_rows = R * n_pts, n_cols = R * n_dofs;
-    std::vector<long> count(n_rows + 1, 0);
-    for (long t = 0; t < n_terms; t++)
-        for (int d1 = 0; d1 < R; d1++) count[d1 * n_pts + t_obs[t] + 1] += dim * R;
-    for (long r = 0; r < n_rows; r++) count[r + 1] += count[r];
-    std::vector<long> fill(count.begin(), count.end() - 1), cols(count[n_rows]);
-    std::vector<double> v(count[n_rows]);
-    for (long t = 0; t < n_terms; t++)
-        for (int b = 0; b < dim; b++)
-            for (int d1 = 0; d1 < R; d1++)
-                for (int d2 = 0; d2 < R; d2++) {
-                    const long row = d1 * n_pts + t_obs[t];
-                    const long k = fill[row]++;
-                    cols[k] = d2 * n_dofs + (long)t_fac[t] * dim + b;
-                    v[k] = vals[(size_t)t * E + (b * R + d1) * R + d2];
-                }
-    return tbem_csr_create(n_rows, n_cols, v.data(), cols.data(), count.data(), out);
+    // Richardson limits / negation and the reference's CSR layout (host, all cores)
+    std::vector<double> v;
+    std::vector<long> cols, row_ptr;
+    nf::assemble_csr(tp, ivals, n_pts, (long)src.size(), dim, R, n_steps, which == 1, v, cols, row_ptr);
+    return tbem_csr_create(R * n_pts, R * (long)src.size() * dim, v.data(), cols.data(), row_ptr.data(),
+                           out);
 }
 
 void validate(int kernel, int which, const TbemIntegrator* mthd)

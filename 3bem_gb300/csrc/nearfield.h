@@ -103,6 +103,38 @@ ObsPoints galerkin_obs_points(const std::vector<Facet>& obs, const FacetSet& all
 // the results do not depend on the split).
 void parallel_for(long n, const std::function<void(long)>& body, long grain = 256);
 
+// The terms of one nearfield (or farfield-correction) matrix and the
+// evaluations they need (IntegrationStrategy::compute_term's split,
+// cpp/integral_term.cpp:33-60): every (observation point, source facet) pair
+// the facet search returns, point by point in the reference's loop order
+// (cpp/nearfield_operator.h:59-84); a far term is one evaluation of the
+// source facet's Gauss rule at the point, a near term one sinh-rule
+// evaluation, a singular term n_steps sinh-rule evaluations at the points
+// stepped back along the limit direction (get_step_loc).
+struct TermPlan {
+    std::vector<int> t_obs, t_fac;          // per term
+    std::vector<long> first;                // per term (+1): its first evaluation
+    std::vector<char> sing;                 // per term: 1 = Richardson over its steps
+    std::vector<int> i_obs, i_fac, i_near;  // per evaluation (i_near: 1 sinh, 0 far)
+    std::vector<double> iloc;               // per evaluation: its point [3]
+    bool on_facet = false;  // a near (not singular) term's point lies on its facet
+};
+
+// Builds the plan on all host cores (farfield_only: the correction matrix,
+// every term one far evaluation at its point).
+TermPlan plan_terms(const ObsPoints& pts, const std::vector<Facet>& src, const FacetSet& src_set,
+                    double far_threshold, int n_steps, int dim, bool farfield_only);
+
+// The matrix from the evaluations' values ([n_evaluations][dim][R][R]):
+// per term its value, its Richardson limit (richardson_limit,
+// cpp/richardson.h:10-34) or (negate) its negation, laid out as the
+// reference's COO entries compressed to CSR (csr_from_coo's stable row
+// order): rows d1 * n_pts + point, columns d2 * dim * n_src + facet * dim +
+// basis.
+void assemble_csr(const TermPlan& tp, const std::vector<double>& ivals, long n_pts, long n_src, int dim,
+                  int R, int n_steps, bool negate, std::vector<double>& vals, std::vector<long>& cols,
+                  std::vector<long>& row_ptr);
+
 // Batched evaluation of the functions being integrated: for point k, the
 // value (E numbers) of job[k]'s function at t[k], written to out[k * E ...].
 using AdaptiveEval = std::function<void(const std::vector<long>& job, const std::vector<double>& t,

@@ -635,5 +635,135 @@ ObsPoints galerkin_obs_points(const std::vector<Facet>& obs, const FacetSet& all
     return o;
 }
 
+TermPlan plan_terms(const ObsPoints& pts, const std::vector<Facet>& src, const FacetSet& src_set,
+                    double far_threshold, int n_steps, int dim, bool farfield_only)
+{
+    TermPlan tp;
+    const long n_pts = (long)pts.loc.size();
+    // the nearfield facets of every point (NearfieldFacetFinder), then the
+    // terms point by point
+    std::vector<std::vector<size_t>> near_of(n_pts);
+    parallel_for(n_pts, [&](long i) {
+        size_t nearest = 0;
+        double dist = 0.0;
+        src_set.find(pts.loc[i], far_threshold, near_of[i], nearest, dist);
+    });
+    std::vector<long> tb(n_pts + 1, 0);
+    for (long i = 0; i < n_pts; i++) tb[i + 1] = tb[i] + (long)near_of[i].size();
+    const long n_terms = tb[n_pts];
+    tp.t_obs.resize(n_terms);
+    tp.t_fac.resize(n_terms);
+    parallel_for(n_pts, [&](long i) {
+        long t = tb[i];
+        for (size_t f : near_of[i]) {
+            tp.t_obs[t] = (int)i;
+            tp.t_fac[t++] = (int)f;
+        }
+        std::vector<size_t>().swap(near_of[i]);
+    });
+    // each term's category as compute_term decides it (cpp/integral_term.cpp:
+    // 33-53): 0 far, 1 near, 2 singular (near the facet with a limit direction)
+    std::vector<char> cat(n_terms, 0), on_facet(n_terms, 0);
+    if (!farfield_only)
+        parallel_for(n_terms, [&](long t) {
+            const long o = tp.t_obs[t], f = tp.t_fac[t];
+            const double dist = closest_point(pts.loc[o], src[f], dim).dist;
+            const double ls = src_set.info(f).length_scale;
+            if (!(dist < far_threshold * ls)) return;
+            double d2 = 0.0;
+            for (int d = 0; d < dim; d++) d2 += pts.dir[o][d] * pts.dir[o][d];
+            if (dist < 1.0 * ls && d2 > 1e-10 * ls) {
+                cat[t] = 2;
+            } else {
+                cat[t] = 1;
+                on_facet[t] = !(dist > 0.0);
+            }
+        });
+    tp.on_facet = std::find(on_facet.begin(), on_facet.end(), 1) != on_facet.end();
+    tp.first.resize(n_terms + 1);
+    tp.first[0] = 0;
+    for (long t = 0; t < n_terms; t++) tp.first[t + 1] = tp.first[t] + (cat[t] == 2 ? n_steps : 1);
+    const long n_items = tp.first[n_terms];
+    tp.sing.assign(n_terms, 0);
+    tp.i_obs.resize(n_items);
+    tp.i_fac.resize(n_items);
+    tp.i_near.resize(n_items);
+    tp.iloc.resize(3 * n_items);
+    parallel_for(n_terms, [&](long t) {
+        const long o = tp.t_obs[t], f = tp.t_fac[t];
+        const V3& p = pts.loc[o];
+        long i = tp.first[t];
+        auto put = [&](int nearflag, const V3& at) {
+            tp.i_obs[i] = (int)o;
+            tp.i_fac[i] = (int)f;
+            tp.i_near[i] = nearflag;
+            for (int d = 0; d < 3; d++) tp.iloc[3 * i + d] = at[d];
+            i++;
+        };
+        if (cat[t] != 2) {
+            put(cat[t], p);
+            return;
+        }
+        tp.sing[t] = 1;
+        for (int k = 0; k < n_steps; k++) {  // get_step_loc (cpp/integral_term.cpp:55-60)
+            const double step = 1.0 / std::pow(2.0, (double)k);
+            const double sd = 1.0 * step;
+            V3 q;
+            for (int d = 0; d < 3; d++) q[d] = p[d] + sd * pts.dir[o][d];
+            put(1, q);
+        }
+    });
+    return tp;
+}
+
+void assemble_csr(const TermPlan& tp, const std::vector<double>& ivals, long n_pts, long n_src, int dim,
+                  int R, int n_steps, bool negate, std::vector<double>& vals, std::vector<long>& cols,
+                  std::vector<long>& row_ptr)
+{
+    const int E = dim * R * R;
+    const long n_terms = (long)tp.t_obs.size();
+    // the terms of point o are [tb[o], tb[o + 1]) (planned point by point)
+    std::vector<long> tb(n_pts + 1, 0);
+    for (long t = 0; t < n_terms; t++) tb[tp.t_obs[t] + 1]++;
+    for (long o = 0; o < n_pts; o++) tb[o + 1] += tb[o];
+    // row d1 * n_pts + o: the dim * R entries (basis b, component d2) of each
+    // of o's terms, term after term -- where the reference's COO loop
+    // (cpp/nearfield_operator.h:59-84) and csr_from_coo's stable order put them
+    const long n_rows = R * n_pts, n_dofs = n_src * dim;
+    row_ptr.assign(n_rows + 1, 0);
+    for (long r = 0; r < n_rows; r++) {
+        const long o = r % n_pts;
+        row_ptr[r + 1] = row_ptr[r] + (tb[o + 1] - tb[o]) * dim * R;
+    }
+    vals.resize(row_ptr[n_rows]);
+    cols.resize(row_ptr[n_rows]);
+    parallel_for(n_pts, [&](long o) {
+        std::vector<double> tab(n_steps), v(E);
+        for (long t = tb[o]; t < tb[o + 1]; t++) {
+            const double* x = &ivals[(size_t)tp.first[t] * E];
+            for (int e = 0; e < E; e++) {
+                double r = x[e];
+                if (tp.sing[t]) {  // richardson_limit (cpp/richardson.h:10-34), step ratio 2
+                    for (int k = 0; k < n_steps; k++) tab[k] = x[k * E + e];
+                    for (int m = 1; m < n_steps; m++) {
+                        const double mult = std::pow(2.0, m);
+                        const double factor = 1.0 / (mult - 1.0);
+                        for (int i = 0; i < n_steps - m; i++) tab[i] = factor * (mult * tab[i + 1] - tab[i]);
+                    }
+                    r = tab[0];
+                }
+                v[e] = negate ? -r : r;
+            }
+            for (int b = 0; b < dim; b++)
+                for (int d1 = 0; d1 < R; d1++)
+                    for (int d2 = 0; d2 < R; d2++) {
+                        const long k = row_ptr[d1 * n_pts + o] + (t - tb[o]) * dim * R + b * R + d2;
+                        cols[k] = d2 * n_dofs + (long)tp.t_fac[t] * dim + b;
+                        vals[k] = v[(b * R + d1) * R + d2];
+                    }
+        }
+    });
+}
+
 }  // namespace nf
 }  // namespace tbem

@@ -107,11 +107,12 @@ struct DBuf {
     // Setup-time copies.  The plans compute on non-blocking streams, which a
     // plain cudaMemcpy (legacy default stream) does not order against: an
     // upload waits for its DMA to land, a download for all device work.
-    void upload(const std::vector<T>& v)
+    void upload(const std::vector<T>& v) { upload(v.data(), v.size()); }
+    void upload(const T* src, size_t count)
     {
-        alloc(v.size());
-        if (!v.empty()) {
-            TBEM_CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        alloc(count);
+        if (count) {
+            TBEM_CK(cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice));
             TBEM_CK(cudaStreamSynchronize(cudaStreamLegacy));
         }
     }

@@ -218,3 +218,52 @@ def test_adaptive_engine_matches_reference(kernel, dim, n_terms, tmp_path):
                               tol, 0, 2, 2, 2, 8, 1e9, 1.3, 0.27).ravel()
         assert np.array_equal(mine, ref)
 
+
+
+@pytest.fixture(scope="module")
+def plan_driver(tmp_path_factory):
+    import subprocess
+    from oracle import oracle
+    oracle.build()
+    exe = str(tmp_path_factory.mktemp("plan") / "nearfield_plan_driver")
+    csrc = os.path.join(ROOT, "3bem_gb300", "csrc")
+    odir = os.path.join(ROOT, "oracle")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I" + csrc,
+                           os.path.join(ROOT, "tests", "cpp", "nearfield_plan_driver.cpp"),
+                           os.path.join(csrc, "nearfield_host.cpp"), "-o", exe, "-lpthread",
+                           os.path.join(odir, "liboracle.so"), "-Wl,-rpath," + odir])
+    return exe
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(p)[10:-4] for p in CASES])
+def test_term_plan_and_csr_layout_match_reference(path, plan_driver):
+    """The host plan of both matrices (the terms in the reference's order,
+    their far / near / singular split and evaluations, the Richardson and
+    negation step and the CSR layout: nearfield_host.cpp plan_terms and
+    assemble_csr) reproduces the reference's row pointers and columns; with
+    the far evaluations done on the CPU by the oracle's kernels in the
+    reference's summation order, the correction matrix's values equal the
+    reference's bit for bit (the product evaluates the same items on the
+    GPU, lanes summing in a different order)."""
+    import subprocess
+    from oracle import oracle
+    g = dict(np.load(path))
+    dim = g["facets"].shape[1]
+    verts = np.zeros((len(g["vertices"]), 3))
+    verts[:, :g["vertices"].shape[1]] = g["vertices"]
+    for which in (0, 1):
+        order = int(g["obs_near_order"] if which == 0 else g["obs_far_order"])
+        head = "%d %.17g %.17g %d %d %.17g %d %d %d" % (
+            oracle.kernel_id(str(g["kernel"]), dim), float(g["mu"]), float(g["nu"]), dim, order,
+            float(g["far_threshold"]),
+            int(g["n_singular_steps"]), int(g["src_far_order"]), which)
+        lines = [head, str(len(verts))] + ["%.17g %.17g %.17g" % tuple(v) for v in verts]
+        lines += [str(len(g["facets"]))] + [" ".join(str(int(i)) for i in f) for f in g["facets"]]
+        out = subprocess.run([plan_driver], input="\n".join(lines) + "\n", capture_output=True,
+                             text=True, check=True).stdout.split("\n")
+        n_rows, n_cols, nnz = (int(x) for x in out[0].split())
+        assert (n_rows, n_cols) == tuple(g["shape%d" % which])
+        assert np.array_equal(np.array(out[1].split(), dtype=np.int64), g["rowptr%d" % which])
+        assert np.array_equal(np.array(out[2].split(), dtype=np.int64), g["cols%d" % which])
+        if which == 1:
+            assert np.array_equal(np.array(out[3].split(), dtype=np.float64), g["values1"])
