@@ -257,6 +257,16 @@ def test_csr_create_validates():
         ThreeD.SparseOperator(2, 2, [1.0], [5], [0, 1, 1])   # column out of range
     with pytest.raises(TbemError):
         ThreeD.SparseOperator(2, 2, [1.0, 2.0], [0, 1], [0, 2, 1])  # decreasing row_ptrs
+    # the column check runs in blocks of 2^20 entries on all host cores: a bad
+    # column in the last of several blocks (or a negative one in the first)
+    nnz = 3 * (1 << 20) + 5
+    cols = np.zeros(nnz, dtype=np.int64)
+    for k, bad in ((nnz - 1, 7), (3, -1)):
+        c = cols.copy()
+        c[k] = bad
+        with pytest.raises(TbemError) as e:
+            ThreeD.SparseOperator(1, 7, np.ones(nnz), c, [0, nnz])
+        assert "column" in str(e.value)
 
 
 def test_graph_arguments_rejected_before_device_use():
