@@ -129,6 +129,18 @@ def test_nearfield_create_validates_before_device_use():
     rc = L.tbem_nearfield_create(1, None, P(v), 3, None, 1, P(f), 1, P(f), 1, C.byref(good), 0,
                                  C.byref(h))
     assert rc == -1 and "null" in L.tbem_last_error().decode() and not h.value
+    # a point on a source facet with no limit direction (all_facets far away)
+    # cannot take the sinh rule (the reference asserts): refused by the host
+    # plan, before any device use
+    allv = np.ascontiguousarray([[0, 0, 0], [1, 0, 0], [0, 1, 0], [50, 0, 0], [51, 0, 0], [50, 1, 0]],
+                                dtype=np.float64)
+    src_f = np.ascontiguousarray([[0, 1, 2]], dtype=np.int64)
+    far_f = np.ascontiguousarray([[3, 4, 5]], dtype=np.int64)
+    p = np.ascontiguousarray([[0.0, 0.0, 0.0]])  # a corner: distance exactly 0
+    pn = np.ascontiguousarray([[0.0, 0.0, 1.0]])
+    rc = L.tbem_nearfield_points_create(1, None, P(p), P(pn), 1, P(allv), 6, P(src_f), 1, P(far_f), 1,
+                                        C.byref(good), 0, C.byref(h))
+    assert rc == -1 and "lies on a source facet" in L.tbem_last_error().decode() and not h.value
     assert L.tbem_galerkin_obs_points(3, P(v), 3, None, 1, P(f), 1, 2, None, None, None) == -1
     assert L.tbem_interior_obs_points(3, P(v), 1, P(v), 3, None, 1, None) == -1
     assert L.tbem_gauss_facet(4, 3, None, None) == -1
