@@ -20,7 +20,11 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE] + ARCH
+# host code of the .cu files rounds as on any host: no FMA contraction (GCC
+# contracts by default on aarch64, not on x86-64); device code keeps nvcc's
+# default (--fmad=true)
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I" + INCLUDE] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-I" + INCLUDE]
 
 
@@ -46,7 +50,7 @@ def _run(cmd):
 def build(verbose=False, jobs=None):
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
-    deps = _headers()
+    deps = _headers() + [os.path.abspath(__file__)]  # a change of flags rebuilds everything
     steps = []
     objs = []
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):
