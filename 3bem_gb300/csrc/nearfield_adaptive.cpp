@@ -48,21 +48,30 @@ double error_is(double p_tol, double erri1, double erri2, double is, double a, d
     return r;
 }
 
+// A tree node: six children from `first`, or a leaf with its estimate i1.
 struct Node {
-    double a, b;
-    long fa, fb;      // value slots of f(a), f(b)
     long first = -1;  // first of six children, -1 for a leaf
     long value = -1;  // slot of the leaf's estimate i1
 };
 
+// An interval still open at this level: its node, local job and ends; its
+// f(a) and f(b) are the entry's 2 E values in the frontier's value array.
+struct Open {
+    long node, job;
+    double a, b;
+};
+
 // The jobs j = c, c + C, c + 2C, ... of chunk c (dealt round robin, so that
 // runs of hard terms spread over the chunks) with their trees and values.
+// Only the frontier holds interval ends and end values, so the trees keep
+// 16 bytes per node plus the leaves' estimates.
 struct Chunk {
     std::vector<long> job;        // job ids
     std::vector<long> root, err;  // per local job: root node, error-target slot
     std::vector<Node> nodes;
-    std::vector<double> pool;  // E values per slot
-    std::vector<long> open, open_job, next, next_job;  // open nodes, their local job
+    std::vector<double> pool;  // leaf estimates and error targets, E values per slot
+    std::vector<Open> open, next;
+    std::vector<double> fab, next_fab;  // per open interval: f(a), f(b)
     long offset = 0;  // this chunk's first point in the current batch
     long slot(const double* v, int E)
     {
@@ -72,9 +81,10 @@ struct Chunk {
     }
     void reset()  // empty, keeping the memory
     {
-        for (auto* v : {&job, &root, &err, &open, &open_job, &next, &next_job}) v->clear();
+        for (auto* v : {&job, &root, &err}) v->clear();
+        for (auto* v : {&open, &next}) v->clear();
+        for (auto* v : {&pool, &fab, &next_fab}) v->clear();
         nodes.clear();
-        pool.clear();
     }
 };
 
@@ -158,15 +168,11 @@ void run_batch(int E, const double* a, const double* b, long n, double p_tol, co
                                       b[j]);
                 }
                 k.err[q] = k.slot(err.data(), E);
-                Node root;
-                root.a = a[j];
-                root.b = b[j];
-                root.fa = k.slot(Y, E);
-                root.fb = k.slot(Y + 12 * E, E);
                 k.root[q] = (long)k.nodes.size();
-                k.nodes.push_back(root);
-                k.open.push_back(k.root[q]);
-                k.open_job.push_back(q);
+                k.nodes.push_back(Node());
+                k.open.push_back({k.root[q], q, a[j], b[j]});
+                k.fab.insert(k.fab.end(), Y, Y + E);                  // f(a)
+                k.fab.insert(k.fab.end(), Y + 12 * E, Y + 13 * E);    // f(b)
             }
         },
         1);
@@ -178,11 +184,10 @@ void run_batch(int E, const double* a, const double* b, long n, double p_tol, co
             [&](long c) {
                 const Chunk& k = ch[c];
                 long o = k.offset;
-                for (size_t i = 0; i < k.open.size(); i++) {
-                    const Node& nd = k.nodes[k.open[i]];
-                    const double m = (nd.a + nd.b) / 2., h = (nd.b - nd.a) / 2.;
+                for (const Open& op : k.open) {
+                    const double m = (op.a + op.b) / 2., h = (op.b - op.a) / 2.;
                     const double xs[5] = {m - kAlpha * h, m - kBeta * h, m, m + kBeta * h, m + kAlpha * h};
-                    const long j = k.job[k.open_job[i]];
+                    const long j = k.job[op.job];
                     for (double x : xs) {
                         pj[o] = j;
                         pt[o++] = x;
@@ -197,17 +202,17 @@ void run_batch(int E, const double* a, const double* b, long n, double p_tol, co
                 Chunk& k = ch[c];
                 std::vector<double> i1(E), i2(E);
                 k.next.clear();
-                k.next_job.clear();
+                k.next_fab.clear();
                 for (size_t i = 0; i < k.open.size(); i++) {
-                    const long id = k.open[i];
-                    const long q = k.open_job[i];
-                    const double na = k.nodes[id].a, nb = k.nodes[id].b;
+                    const long id = k.open[i].node;
+                    const long q = k.open[i].job;
+                    const double na = k.open[i].a, nb = k.open[i].b;
                     const double m = (na + nb) / 2., h = (nb - na) / 2.;
                     const double mll = m - kAlpha * h, ml = m - kBeta * h, mr = m + kBeta * h,
                                  mrr = m + kAlpha * h;
                     const double* Y = &y[(size_t)(k.offset + 5 * (long)i) * E];  // fmll, fml, fm, fmr, fmrr
-                    const double* fa = &k.pool[(size_t)k.nodes[id].fa * E];
-                    const double* fb = &k.pool[(size_t)k.nodes[id].fb * E];
+                    const double* fa = &k.fab[2 * E * i];
+                    const double* fb = fa + E;
                     const double* target = &k.pool[(size_t)k.err[q] * E];
                     bool converged = true;
                     for (int e = 0; e < E; e++) {
@@ -221,25 +226,19 @@ void run_batch(int E, const double* a, const double* b, long n, double p_tol, co
                         k.nodes[id].value = v;
                         continue;
                     }
-                    long s[5];
-                    for (int r = 0; r < 5; r++) s[r] = k.slot(Y + r * E, E);
                     const double cut[7] = {na, mll, ml, m, mr, mrr, nb};
-                    const long fs[7] = {k.nodes[id].fa, s[0], s[1], s[2], s[3], s[4], k.nodes[id].fb};
+                    const double* fs[7] = {fa, Y, Y + E, Y + 2 * E, Y + 3 * E, Y + 4 * E, fb};
                     const long first = (long)k.nodes.size();
                     for (int r = 0; r < 6; r++) {
-                        Node child;
-                        child.a = cut[r];
-                        child.b = cut[r + 1];
-                        child.fa = fs[r];
-                        child.fb = fs[r + 1];
-                        k.nodes.push_back(child);
-                        k.next.push_back(first + r);
-                        k.next_job.push_back(q);
+                        k.nodes.push_back(Node());
+                        k.next.push_back({first + r, q, cut[r], cut[r + 1]});
+                        k.next_fab.insert(k.next_fab.end(), fs[r], fs[r] + E);
+                        k.next_fab.insert(k.next_fab.end(), fs[r + 1], fs[r + 1] + E);
                     }
                     k.nodes[id].first = first;
                 }
                 k.open.swap(k.next);
-                k.open_job.swap(k.next_job);
+                k.fab.swap(k.next_fab);
             },
             1);
     }
