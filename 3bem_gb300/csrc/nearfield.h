@@ -154,9 +154,11 @@ using InfluenceEval = std::function<void(const std::vector<long>& item, const st
 // The facet integral of every item by the adaptive rule
 // (UnitFacetAdaptiveIntegrator, cpp/integral_term.cpp:96-128): over
 // x_hat in [-1, 1] in 2D; over x in [0, 1] of the integral over y in
-// [0, 1 - x] in 3D (zero at x = 1).  Returns [n_items][E].
+// [0, 1 - x] in 3D (zero at x = 1).  Returns [n_items][E].  At most
+// slice_jobs terms (and inner integrals) share one breadth-first batch,
+// which bounds the frontier's memory; the values do not depend on it.
 std::vector<double> adaptive_facet_integrals(int dim, int E, long n_items, double tol,
-                                             const InfluenceEval& eval);
+                                             const InfluenceEval& eval, long slice_jobs = 1L << 18);
 
 }  // namespace nf
 }  // namespace tbem

@@ -8,14 +8,18 @@
 // recursion runs at once, breadth first: each level asks the evaluator for
 // all new points of all open intervals in one batch (the GPU, in the
 // product), then every interval either stops or splits in six, exactly as
-// the recursive rule decides; at the end every tree is summed in the
-// recursion's order.  In 3D the outer rule's function values are inner
-// integrals, computed the same way in one batch per outer level.
+// the recursive rule decides.  In 3D the outer rule's function values are
+// inner integrals, computed the same way in one batch per outer level.
+//
+// An interval that splits waits for its six children's integrals; once the
+// sixth arrives it sums them in the recursion's order,
+// ((((c1 + c2) + c3) + c4) + c5) + c6, and passes the sum up in turn.  So the
+// results are the recursion's bit for bit, and memory follows the open
+// frontier and its pending ancestors, not the whole tree.
 //
 // The host work between the batches (emitting points, the stop rule, the
-// splits, the final sums) runs on all host cores: the terms are dealt to
-// chunks, each chunk keeps its own trees, and every term's arithmetic is the
-// recursion's, in its order, whichever chunk and thread it lands on.
+// splits and sums) runs on all host cores: the terms are dealt to chunks and
+// every term's arithmetic stays in its own chunk.
 #include <algorithm>
 #include <cmath>
 #include <limits>
@@ -48,49 +52,85 @@ double error_is(double p_tol, double erri1, double erri2, double is, double a, d
     return r;
 }
 
-// A tree node: six children from `first`, or a leaf with its estimate i1.
-struct Node {
-    long first = -1;  // first of six children, -1 for a leaf
-    long value = -1;  // slot of the leaf's estimate i1
+// An interval that split and waits for its children's integrals (6 E
+// values in the chunk's block values).
+struct Block {
+    long parent;  // the block of the interval it is a child of, -1 for a root
+    int child;    // which child of that interval it is
+    int done;     // children's integrals received
+    long job;     // local job
 };
 
-// An interval still open at this level: its node, local job and ends; its
-// f(a) and f(b) are the entry's 2 E values in the frontier's value array.
+// An interval still open at this level; its f(a) and f(b) are the entry's
+// 2 E values in the frontier's value array.
 struct Open {
-    long node, job;
+    long parent;  // block waiting for this interval's integral, -1 for a root
+    int child;
+    long job;  // local job
     double a, b;
 };
 
 // The jobs j = c, c + C, c + 2C, ... of chunk c (dealt round robin, so that
-// runs of hard terms spread over the chunks) with their trees and values.
-// Only the frontier holds interval ends and end values, so the trees keep
-// 16 bytes per node plus the leaves' estimates.
+// runs of hard terms spread over the chunks) with their pending intervals.
 struct Chunk {
-    std::vector<long> job;        // job ids
-    std::vector<long> root, err;  // per local job: root node, error-target slot
-    std::vector<Node> nodes;
-    std::vector<double> pool;  // leaf estimates and error targets, E values per slot
+    std::vector<long> job;     // job ids
+    std::vector<double> err;   // per local job: the error target (E values)
+    std::vector<Block> blocks;
+    std::vector<double> bvals;       // per block: six children's integrals
+    std::vector<long> free_blocks;   // blocks to reuse
     std::vector<Open> open, next;
     std::vector<double> fab, next_fab;  // per open interval: f(a), f(b)
+    std::vector<double> sum;            // scratch for a completed block's sum
     long offset = 0;  // this chunk's first point in the current batch
-    long slot(const double* v, int E)
-    {
-        const long s = (long)(pool.size() / E);
-        pool.insert(pool.end(), v, v + E);
-        return s;
-    }
     void reset()  // empty, keeping the memory
     {
-        for (auto* v : {&job, &root, &err}) v->clear();
-        for (auto* v : {&open, &next}) v->clear();
-        for (auto* v : {&pool, &fab, &next_fab}) v->clear();
-        nodes.clear();
+        job.clear();
+        for (auto* v : {&err, &bvals, &fab, &next_fab}) v->clear();
+        blocks.clear();
+        free_blocks.clear();
+        open.clear();
+        next.clear();
+    }
+    long new_block(const Block& b, int E)
+    {
+        if (!free_blocks.empty()) {
+            const long id = free_blocks.back();
+            free_blocks.pop_back();
+            blocks[id] = b;
+            return id;
+        }
+        blocks.push_back(b);
+        bvals.resize(bvals.size() + 6 * (size_t)E);
+        return (long)blocks.size() - 1;
+    }
+    // Hands the integral v of an interval to the block waiting for it (or,
+    // for a root, to the job's result) and completes every block it fills.
+    void deliver(long parent, int child, long q, const double* v, int E, std::vector<double>& total)
+    {
+        sum.assign(v, v + E);
+        while (parent >= 0) {
+            double* slots = &bvals[(size_t)parent * 6 * E];
+            std::copy(sum.begin(), sum.end(), slots + (size_t)child * E);
+            Block& bk = blocks[parent];
+            if (++bk.done < 6) return;
+            // adaptlobstp's return: the six children's integrals in order
+            for (int e = 0; e < E; e++) {
+                double s = slots[e];
+                for (int r = 1; r < 6; r++) s = s + slots[r * E + e];
+                sum[e] = s;
+            }
+            free_blocks.push_back(parent);
+            child = bk.child;
+            q = bk.job;
+            parent = bk.parent;
+        }
+        std::copy(sum.begin(), sum.end(), &total[(size_t)job[q] * E]);
     }
 };
 
 // The buffers of one batch driver, kept between its calls: the 3D inner
 // integrals run one batch per outer level, and reusing memory already
-// touched spares the page faults of fresh gigabyte-sized buffers.
+// touched spares the page faults of fresh buffers.
 struct Work {
     std::vector<Chunk> ch;
     std::vector<long> pj;
@@ -148,10 +188,9 @@ void run_batch(int E, const double* a, const double* b, long n, double p_tol, co
         C,
         [&](long c) {
             Chunk& k = ch[c];
-            std::vector<double> i1(E), i2(E), is(E), err(E);
+            std::vector<double> i1(E), i2(E), is(E);
             const long nj = (long)k.job.size();
-            k.root.resize(nj);
-            k.err.resize(nj);
+            k.err.resize((size_t)nj * E);
             for (long q = 0; q < nj; q++) {
                 const long j = k.job[q];
                 const double* Y = &y[(size_t)(k.offset + 13 * q) * E];
@@ -164,15 +203,12 @@ void run_batch(int E, const double* a, const double* b, long n, double p_tol, co
                     is[e] = h * (kW[0] * (v(0) + v(12)) + kW[1] * (v(1) + v(11)) + kW[2] * (v(2) + v(10)) +
                                  kW[3] * (v(3) + v(9)) + kW[4] * (v(4) + v(8)) + kW[5] * (v(5) + v(7)) +
                                  kW[6] * v(6));
-                    err[e] = error_is(p_tol, std::fabs(i1[e] - is[e]), std::fabs(i2[e] - is[e]), is[e], a[j],
-                                      b[j]);
+                    k.err[q * E + e] = error_is(p_tol, std::fabs(i1[e] - is[e]), std::fabs(i2[e] - is[e]),
+                                                is[e], a[j], b[j]);
                 }
-                k.err[q] = k.slot(err.data(), E);
-                k.root[q] = (long)k.nodes.size();
-                k.nodes.push_back(Node());
-                k.open.push_back({k.root[q], q, a[j], b[j]});
-                k.fab.insert(k.fab.end(), Y, Y + E);                  // f(a)
-                k.fab.insert(k.fab.end(), Y + 12 * E, Y + 13 * E);    // f(b)
+                k.open.push_back({-1, 0, q, a[j], b[j]});
+                k.fab.insert(k.fab.end(), Y, Y + E);                // f(a)
+                k.fab.insert(k.fab.end(), Y + 12 * E, Y + 13 * E);  // f(b)
             }
         },
         1);
@@ -204,16 +240,15 @@ void run_batch(int E, const double* a, const double* b, long n, double p_tol, co
                 k.next.clear();
                 k.next_fab.clear();
                 for (size_t i = 0; i < k.open.size(); i++) {
-                    const long id = k.open[i].node;
-                    const long q = k.open[i].job;
-                    const double na = k.open[i].a, nb = k.open[i].b;
+                    const Open op = k.open[i];
+                    const double na = op.a, nb = op.b;
                     const double m = (na + nb) / 2., h = (nb - na) / 2.;
                     const double mll = m - kAlpha * h, ml = m - kBeta * h, mr = m + kBeta * h,
                                  mrr = m + kAlpha * h;
                     const double* Y = &y[(size_t)(k.offset + 5 * (long)i) * E];  // fmll, fml, fm, fmr, fmrr
                     const double* fa = &k.fab[2 * E * i];
                     const double* fb = fa + E;
-                    const double* target = &k.pool[(size_t)k.err[q] * E];
+                    const double* target = &k.err[(size_t)op.job * E];
                     bool converged = true;
                     for (int e = 0; e < E; e++) {
                         i2[e] = (h / 6.) * (fa[e] + fb[e] + 5.0 * (Y[E + e] + Y[3 * E + e]));
@@ -222,65 +257,23 @@ void run_batch(int E, const double* a, const double* b, long n, double p_tol, co
                         converged = converged && (target[e] + (i1[e] - i2[e]) == target[e]);
                     }
                     if (converged || mll <= na || nb <= mrr) {
-                        const long v = k.slot(i1.data(), E);
-                        k.nodes[id].value = v;
+                        k.deliver(op.parent, op.child, op.job, i1.data(), E, total);
                         continue;
                     }
+                    const long blk = k.new_block({op.parent, op.child, 0, op.job}, E);
                     const double cut[7] = {na, mll, ml, m, mr, mrr, nb};
                     const double* fs[7] = {fa, Y, Y + E, Y + 2 * E, Y + 3 * E, Y + 4 * E, fb};
-                    const long first = (long)k.nodes.size();
                     for (int r = 0; r < 6; r++) {
-                        k.nodes.push_back(Node());
-                        k.next.push_back({first + r, q, cut[r], cut[r + 1]});
+                        k.next.push_back({blk, r, op.job, cut[r], cut[r + 1]});
                         k.next_fab.insert(k.next_fab.end(), fs[r], fs[r] + E);
                         k.next_fab.insert(k.next_fab.end(), fs[r + 1], fs[r + 1] + E);
                     }
-                    k.nodes[id].first = first;
                 }
                 k.open.swap(k.next);
                 k.fab.swap(k.next_fab);
             },
             1);
     }
-
-    // sum every tree in the recursion's order: ((((c1 + c2) + c3) + c4) + c5) + c6,
-    // post-order with an explicit stack and one partial sum per depth
-    parallel_for(
-        C,
-        [&](long c) {
-            const Chunk& k = ch[c];
-            std::vector<std::pair<long, int>> st;  // node, children entered
-            std::vector<double> part;
-            for (size_t q = 0; q < k.job.size(); q++) {
-                double* out = &total[(size_t)k.job[q] * E];
-                st.assign(1, {k.root[q], 0});
-                while (!st.empty()) {
-                    const Node& nd = k.nodes[st.back().first];
-                    const double* ret;
-                    if (nd.first < 0) {  // leaf: its estimate
-                        ret = &k.pool[(size_t)nd.value * E];
-                    } else if (st.back().second < 6) {
-                        const int r = st.back().second++;
-                        st.push_back({nd.first + r, 0});
-                        if (part.size() < st.size() * E) part.resize(st.size() * E);
-                        continue;
-                    } else {  // all six children summed
-                        ret = &part[(st.size() - 1) * E];
-                    }
-                    st.pop_back();
-                    if (st.empty()) {
-                        std::copy(ret, ret + E, out);
-                        break;
-                    }
-                    // fold ret into the parent: the first child starts the sum
-                    double* p = &part[(st.size() - 1) * E];
-                    if (st.back().second == 1) std::copy(ret, ret + E, p);
-                    else
-                        for (int e = 0; e < E; e++) p[e] = p[e] + ret[e];
-                }
-            }
-        },
-        1);
 }
 
 }  // namespace
@@ -298,62 +291,69 @@ std::vector<double> adaptive_batch(int E, const std::vector<double>& a, const st
 }
 
 std::vector<double> adaptive_facet_integrals(int dim, int E, long n_items, double tol,
-                                             const InfluenceEval& eval)
+                                             const InfluenceEval& eval, long slice_jobs)
 {
-    Work outer;
-    std::vector<double> total;
-    if (dim == 2) {
-        const std::vector<double> a(n_items, -1.0), b(n_items, 1.0);
-        std::vector<double> zeros;
-        run_batch(
-            E, a.data(), b.data(), n_items, tol,
-            [&](const std::vector<long>& job, const std::vector<double>& t, std::vector<double>& out) {
+    // A batch's frontier grows with its jobs (near-singular 3D terms reach
+    // tens of millions of open points in one level), so the terms -- and
+    // each outer level's inner integrals -- go in slices of slice_jobs jobs.
+    // The jobs are independent: the slicing changes no value.
+    const long S = std::max(1L, slice_jobs);
+    std::vector<double> total((size_t)n_items * E), part, zeros, ia, ib, ix, x0, v;
+    std::vector<long> jobs, inner_item, inner_of, it;
+    Work outer, inner;  // kept across slices and outer levels
+    for (long s0 = 0; s0 < n_items; s0 += S) {
+        const long m = std::min(S, n_items - s0);
+        const std::vector<double> a(m, dim == 2 ? -1.0 : 0.0), b(m, 1.0);
+        AdaptiveEval outer_eval;
+        if (dim == 2) {
+            outer_eval = [&](const std::vector<long>& job, const std::vector<double>& t,
+                             std::vector<double>& out) {
+                jobs.resize(job.size());
+                for (size_t k = 0; k < job.size(); k++) jobs[k] = job[k] + s0;
                 zeros.assign(t.size(), 0.0);
-                eval(job, t, zeros, out);
-            },
-            outer, total);
-        return total;
-    }
-    const std::vector<double> a(n_items, 0.0), b(n_items, 1.0);
-    // kept across the outer levels (each runs one inner batch)
-    Work inner;
-    std::vector<long> inner_item, inner_of, it;
-    std::vector<double> ia, ib, ix, x0, v;
-    run_batch(
-        E, a.data(), b.data(), n_items, tol,
-        [&](const std::vector<long>& job, const std::vector<double>& xs, std::vector<double>& out) {
-        // the outer function at x: the inner integral over y in [0, 1 - x]
-        out.assign(xs.size() * E, 0.0);
-        for (auto* u : {&inner_item, &inner_of}) u->clear();
-        for (auto* u : {&ia, &ib, &ix}) u->clear();
-        for (size_t k = 0; k < xs.size(); k++) {
-            if (xs[k] == 1.0) continue;  // zero, as the reference's outer lambda returns
-            inner_item.push_back(job[k]);
-            inner_of.push_back((long)k);
-            ia.push_back(0.0);
-            ib.push_back(1 - xs[k]);
-            ix.push_back(xs[k]);
+                eval(jobs, t, zeros, out);
+            };
+        } else {
+            outer_eval = [&](const std::vector<long>& job, const std::vector<double>& xs,
+                             std::vector<double>& out) {
+                // the outer function at x: the inner integral over y in [0, 1 - x]
+                out.assign(xs.size() * E, 0.0);
+                for (auto* u : {&inner_item, &inner_of}) u->clear();
+                for (auto* u : {&ia, &ib, &ix}) u->clear();
+                for (size_t k = 0; k < xs.size(); k++) {
+                    if (xs[k] == 1.0) continue;  // zero, as the reference's outer lambda returns
+                    inner_item.push_back(job[k] + s0);
+                    inner_of.push_back((long)k);
+                    ia.push_back(0.0);
+                    ib.push_back(1 - xs[k]);
+                    ix.push_back(xs[k]);
+                }
+                const long n_in = (long)ia.size();
+                for (long i0 = 0; i0 < n_in; i0 += S) {
+                    const long mi = std::min(S, n_in - i0);
+                    run_batch(
+                        E, ia.data() + i0, ib.data() + i0, mi, tol,
+                        [&](const std::vector<long>& ij, const std::vector<double>& ys, std::vector<double>& o) {
+                            it.resize(ij.size());
+                            x0.resize(ij.size());
+                            parallel_for(
+                                (long)ij.size(),
+                                [&](long q) {
+                                    it[q] = inner_item[i0 + ij[q]];
+                                    x0[q] = ix[i0 + ij[q]];
+                                },
+                                1 << 16);
+                            eval(it, x0, ys, o);
+                        },
+                        inner, v);
+                    for (long q = 0; q < mi; q++)
+                        for (int e = 0; e < E; e++) out[(size_t)inner_of[i0 + q] * E + e] = v[q * E + e];
+                }
+            };
         }
-        if (inner_item.empty()) return;
-        run_batch(
-            E, ia.data(), ib.data(), (long)ia.size(), tol,
-            [&](const std::vector<long>& ij, const std::vector<double>& ys, std::vector<double>& o) {
-                it.resize(ij.size());
-                x0.resize(ij.size());
-                parallel_for(
-                    (long)ij.size(),
-                    [&](long q) {
-                        it[q] = inner_item[ij[q]];
-                        x0[q] = ix[ij[q]];
-                    },
-                    1 << 16);
-                eval(it, x0, ys, o);
-            },
-            inner, v);
-        for (size_t q = 0; q < inner_of.size(); q++)
-            for (int e = 0; e < E; e++) out[(size_t)inner_of[q] * E + e] = v[q * E + e];
-        },
-        outer, total);
+        run_batch(E, a.data(), b.data(), m, tol, outer_eval, outer, part);
+        std::copy(part.begin(), part.end(), total.begin() + s0 * E);
+    }
     return total;
 }
 

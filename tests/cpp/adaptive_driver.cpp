@@ -4,9 +4,11 @@
 // facet integrals with the reference's recursive integrator on the CPU.  The
 // product evaluates the same points on the GPU.
 //
+// argv[1] (optional): terms per breadth-first batch.
 // stdin: kernel mu nu tol dim, then per term: obs[3] normal[3] facet[dim][3]
 // (until EOF); stdout: dim * R * R values per term.
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "nearfield.h"
@@ -16,8 +18,9 @@ extern "C" int oracle_kernel(int kernel, double mu, double nu, const double* obs
 
 using namespace tbem::nf;
 
-int main()
+int main(int argc, char** argv)
 {
+    const long slice = argc > 1 ? atol(argv[1]) : (1L << 18);
     int kernel, dim;
     double mu, nu, tol;
     if (scanf("%d %lf %lf %lf %d", &kernel, &mu, &nu, &tol, &dim) != 5) return 1;
@@ -63,7 +66,7 @@ int main()
                 for (int q = 0; q < R * R; q++) out[k * E + b * R * R + q] = bas[b] * (K[q] * fi.jacobian);
         }
     };
-    const std::vector<double> v = adaptive_facet_integrals(dim, E, (long)loc.size(), tol, eval);
+    const std::vector<double> v = adaptive_facet_integrals(dim, E, (long)loc.size(), tol, eval, slice);
     for (size_t t = 0; t < loc.size(); t++) {
         for (int e = 0; e < E; e++) printf("%.17g ", v[t * E + e]);
         printf("\n");

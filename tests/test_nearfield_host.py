@@ -229,6 +229,11 @@ def test_adaptive_engine_matches_reference(kernel, dim, n_terms, tmp_path):
         ref = oracle.ref_term(kernel, obs[:dim], n[:dim], np.zeros(dim), facet[:, :dim], "adaptive",
                               tol, 0, 2, 2, 2, 8, 1e9, 1.3, 0.27).ravel()
         assert np.array_equal(mine, ref)
+    if n_terms > 6:  # terms and inner integrals in small slices: the same values
+        for slice_jobs in ("7", "50"):
+            sliced = subprocess.run([exe, slice_jobs], input="\n".join(lines) + "\n", capture_output=True,
+                                    text=True, check=True).stdout.strip().split("\n")
+            assert sliced == out
 
 
 
