@@ -285,6 +285,21 @@ void tbem_fmm_graph_destroy(TbemGraph* g) { tbem::graph_delete(g); }
 
 long tbem_fmm_last_launches(const TbemFmm* h) { return h ? h->plan.launches : TBEM_ERR_ARG; }
 
+int tbem_fmm_sync(TbemFmm* h, void* stream)
+{
+    if (!h) return fail(TBEM_ERR_ARG, "null handle");
+    return guarded([&] { h->plan.sync((cudaStream_t)stream); });
+}
+
+int tbem_fmm_set_wait_cycles(TbemFmm* h, long long cycles)
+{
+    if (!h) return fail(TBEM_ERR_ARG, "null handle");
+    if (cycles < 0) return fail(TBEM_ERR_ARG, "negative wait budget");
+    h->plan.f.tc.wait_cycles = cycles;
+    h->plan.f.tc_c.wait_cycles = cycles;
+    return TBEM_OK;
+}
+
 int tbem_fmm_set_timing(TbemFmm* h, int enabled)
 {
     if (!h) return fail(TBEM_ERR_ARG, "null handle");

@@ -12,14 +12,15 @@
 // until the process exits.
 //
 // The array's host-side name is only a stand-in for the device object, so
-// its device address is looked up with cudaGetSymbolAddress once per device
-// (with that device current) on the first call made on that device, and
-// cached.  All calls share the array and it keeps the last call's contents;
-// everything this path reads from it is rewritten by the same call before
-// use.  Two calls whose work overlaps on the GPU (for example on two
-// streams) race on the array.
-#include <mutex>
-
+// its device address is looked up with cudaGetSymbolAddress on every call,
+// with the caller's device current.  Nothing is cached: after a device reset
+// (or any teardown of the primary context) the runtime loads the module
+// again and the lookup returns the new address.  The first call on a device
+// loads the module there, so make it before any stream capture.  All calls
+// share the array and it keeps the last call's contents; everything this
+// path reads from it is rewritten by the same call before use.  Two calls
+// whose work overlaps on the GPU (for example on two streams) race on the
+// array.
 #include "plan.h"
 
 namespace {
@@ -28,28 +29,20 @@ constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(16) << 20;
 constexpr size_t NOALLOC_TASK_BYTES = size_t(1) << 20;     // work-item descriptors
 constexpr int NOALLOC_CHUNK = 1024;                        // observation points per task
 constexpr int NOALLOC_TPB = tbem::EVAL_THREADS / 4;        // targets per CTA (4 threads each)
-constexpr int NOALLOC_MAX_DEVICES = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-std::mutex g_noalloc_mu;
-unsigned char* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
-
-// Device address of the scratch array on the current device (looked up once).
-unsigned char* scratch_address(int dev)
+// Device address of the scratch array on the current device.
+unsigned char* scratch_address()
 {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            throw tbem::Error(TBEM_ERR_CUDA, std::string("cudaGetSymbolAddress of the scratch "
-                                                         "array failed: ") + cudaGetErrorString(e));
-        }
-        g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        throw tbem::Error(TBEM_ERR_CUDA, std::string("cudaGetSymbolAddress of the scratch "
+                                                     "array failed: ") + cudaGetErrorString(e));
     }
-    return g_noalloc_addr[dev];
+    return static_cast<unsigned char*>(p);
 }
 
 struct TaskLayout {
@@ -135,8 +128,13 @@ extern "C" int tbem_direct_apply_noalloc(int kernel, const double* kernel_params
 {
     using namespace tbem;
     try {
-        if (kernel < 0 || kernel > 6 || n_obs < 0 || n_src < 0 || n_rhs <= 0)
-            throw Error(TBEM_ERR_ARG, "bad kernel id, point count or n_rhs");
+        if (kernel < 0 || kernel > 6)
+            throw Error(TBEM_ERR_ARG, "tbem_direct_apply_noalloc takes the 3D kernel ids 0..6 "
+                                      "only (2D points would need widening, i.e. scratch)");
+        if (n_obs < 0 || n_src < 0 || n_rhs <= 0) throw Error(TBEM_ERR_ARG, "bad point count or n_rhs");
+        if (kernel_params && on_device(kernel_params))
+            throw Error(TBEM_ERR_ARG, "tbem_direct_apply_noalloc: kernel_params is read on the "
+                                      "host: pass host memory (or NULL for the defaults)");
         if (n_obs == 0) return TBEM_OK;
         const int R = kernel_dim(kernel);
         const size_t str_bytes = sizeof(double) * (size_t)R * n_src * n_rhs;
@@ -162,10 +160,7 @@ extern "C" int tbem_direct_apply_noalloc(int kernel, const double* kernel_params
         if (!on_device(obs_locs) || !on_device(obs_normals) || !on_device(y) || !src_ok)
             throw Error(TBEM_ERR_ARG, "tbem_direct_apply_noalloc: every data pointer must be "
                                       "device memory (this entry point copies nothing)");
-        int dev = 0;
-        TBEM_CK(cudaGetDevice(&dev));
-        if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) throw Error(TBEM_ERR_ARG, "device ordinal too large");
-        unsigned char* base = scratch_address(dev);
+        unsigned char* base = scratch_address();
         double* str = reinterpret_cast<double*>(base + NOALLOC_TASK_BYTES);
         cudaStream_t s = (cudaStream_t)stream;
 

@@ -280,6 +280,14 @@ __global__ void pts_surf_matrix_kernel(const long* pt0, const int* npts, const i
         for (int d2 = 0; d2 < R; d2++) o[((long)i * R + d1) * ld + (long)d2 * ns + j] = k[d1 * R + d2];
 }
 
+// out = s * in (n values): a level's check-to-equivalent operator from
+// another level's, for a kernel homogeneous in the separation
+__global__ void scale_copy_kernel(const double* in, double* out, long n, double s)
+{
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+        out[t] = s * in[t];
+}
+
 // Column k of U (column-major) times 1/s_k, or zero below the cutoff
 // (svd_pseudoinverse, cpp/blas_wrapper.cpp:96-127).
 __global__ void pinv_scale_kernel(double* U, const double* S, int N, double threshold)
@@ -850,39 +858,79 @@ void Plan::build_tasks()
     }
 }
 
+// Homogeneity degree of a 3D kernel in the separation (K(s d) = s^deg K(d)
+// for s > 0); 1 (not homogeneous) for the 2D kernels, whose logarithms are not.
+namespace {
+int kernel_degree(int kid)
+{
+    switch (kid) {
+    case LAP_S: case EL_DISP: return -1;
+    case LAP_D: case EL_TRAC: case EL_ADJ: return -2;
+    case EL_HYP: return -3;
+    case IDENT: return 0;
+    default: return 1;
+    }
+}
+}  // namespace
+
 // Pseudo-inverses of the check-to-equivalent systems of every level
 // (build_check_to_equiv + svd_inverse_nbody, cpp/fmm.cpp:113-160), FP64 on
-// the GPU with cuSOLVER gesvd.
+// the GPU with cuSOLVER gesvd.  Every level's system is the same pair of
+// concentric spheres scaled by the level's cell radius r_l, so for a 3D
+// kernel homogeneous of degree deg the system of level l is (r_l / r_0)^deg
+// times that of level 0 and its pseudo-inverse (the same relative cutoff) is
+// (r_l / r_0)^-deg times level 0's: one SVD per tree side.  Levels whose
+// sphere separation falls below 1e-5 (where the r^2 < 1e-12 self-pair rule
+// could drop entries) and the 2D kernels get their own SVD, as in the
+// reference.  The scaled operators differ from per-level SVDs by rounding of
+// the size of the reference's own one-ulp sensitivity.
 void Plan::build_c2e(Form& F)
 {
     const Tree* trees[2] = {stree, &otree};
     double r_eq[2] = {F.r_ue, F.r_de}, r_ck[2] = {F.r_uc, F.r_dc};
-    std::vector<SurfJob> jobs;
+    std::vector<SurfJob> jobs;       // systems factored directly
+    std::vector<long> job_dst;       // their c2e offsets
+    struct Scaled { long src, dst; double s; };
+    std::vector<Scaled> scaled;      // levels derived from a factored one
     std::vector<long>* offs[2] = {&F.c2e_up_off, &F.c2e_dn_off};
     const long nn = (long)n * n;
+    const int deg = sdim == 3 ? kernel_degree(F.g_kid) : 1;
     long total = 0;
     for (int w = 0; w < 2; w++) {
         offs[w]->clear();
         const Tree& t = *trees[w];
+        const double sep = std::fabs(r_ck[w] - r_eq[w]);
+        long base_off = -1;
+        double base_r = 0;
         for (int l = 0; l < t.n_levels(); l++) {
             int c = t.first_at_level[l];
             const Cell& cc = t.cells[c];
-            SurfJob J;
             double r = hypot_ref(cc.hw);
-            for (int d = 0; d < 3; d++) J.tc[d] = J.sc[d] = cc.center[d];
-            J.tr = J.sr = r;
-            J.trref = r_ck[w];
-            J.srref = r_eq[w];
-            J.out_off = total;
-            jobs.push_back(J);
             offs[w]->push_back(total);
+            const bool scalable = deg <= 0 && r * sep > 1e-5;
+            if (scalable && base_off >= 0) {
+                scaled.push_back({base_off, total, std::pow(r / base_r, -(double)deg)});
+            } else {
+                SurfJob J;
+                for (int d = 0; d < 3; d++) J.tc[d] = J.sc[d] = cc.center[d];
+                J.tr = J.sr = r;
+                J.trref = r_ck[w];
+                J.srref = r_eq[w];
+                J.out_off = (long)jobs.size() * nn;
+                jobs.push_back(J);
+                job_dst.push_back(total);
+                if (scalable) {
+                    base_off = total;
+                    base_r = r;
+                }
+            }
             total += nn;
         }
     }
     F.c2e.alloc(total);
     if (jobs.empty()) return;
     DBuf<double> sys;
-    sys.alloc(total);
+    sys.alloc(jobs.size() * nn);
     DBuf<SurfJob> dj;
     dj.alloc(jobs.size());
     TBEM_CK(cudaMemcpy(dj.p, jobs.data(), jobs.size() * sizeof(SurfJob), cudaMemcpyHostToDevice));
@@ -911,7 +959,7 @@ void Plan::build_c2e(Form& F)
         TBEM_CK(cudaGetLastError());
         const double one = 1.0, zero = 0.0;
         TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_T, n, n, n, &one, VT.p, n, U.p, n, &zero,
-                             F.c2e.p + jobs[k].out_off, n));
+                             F.c2e.p + job_dst[k], n));
         int h_info = 0;
         TBEM_CK(cudaMemcpyAsync(&h_info, info.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
         TBEM_CK(cudaStreamSynchronize(stream));
@@ -919,6 +967,12 @@ void Plan::build_c2e(Form& F)
             throw Error(TBEM_ERR_CUDA, "cuSOLVER gesvd did not converge (info " +
                                            std::to_string(h_info) + ")");
     }
+    for (const Scaled& sc : scaled) {
+        scale_copy_kernel<<<(unsigned)std::min<long>((nn + 255) / 256, 4096), 256, 0, stream>>>(
+            F.c2e.p + sc.src, F.c2e.p + sc.dst, nn, sc.s);
+        TBEM_CK(cudaGetLastError());
+    }
+    TBEM_CK(cudaStreamSynchronize(stream));
 }
 
 void Plan::build_form()
@@ -2122,6 +2176,26 @@ void Plan::check_tc_flags(bool wait_device, cudaStream_t s)
     if (wait_device) {
         TBEM_CK(cudaStreamSynchronize(s));
         if (h_err[0] || h_err[1]) throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
+    }
+}
+
+void Plan::sync(cudaStream_t s)
+{
+    if (opt.host_only) return;
+    DeviceGuard guard(opt.device);
+    if (s) TBEM_CK(cudaStreamSynchronize(s));
+    TBEM_CK(cudaStreamSynchronize(stream));
+    TBEM_CK(cudaStreamSynchronize(side));
+    const TcPlanes* P[2] = {&f.tc, &f.tc_c};
+    int flag[2] = {0, 0};
+    for (int i = 0; i < 2; i++)
+        if (P[i]->err.p) TBEM_CK(cudaMemcpy(&flag[i], P[i]->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag[0] || flag[1] || (h_err && (h_err[0] || h_err[1]))) {
+        if (h_err) {
+            h_err[0] |= flag[0];
+            h_err[1] |= flag[1];
+        }
+        throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
     }
 }
 

@@ -191,6 +191,7 @@ struct TcPlanes {
     int m = 0, k = 0, m_pad = 0, k_pad = 0;  // operators m x k (row-major)
     DBuf<__nv_bfloat16> a[3], b[3];
     DBuf<int> err;  // set by a tensor-core GEMM whose bounded wait gave up
+    long long wait_cycles = 0;  // budget of the GEMM's bounded waits (0: the default)
     void build(const float* ops32, long n_ops, int m, int k, cudaStream_t s);
     void split_b(const float* cells, long rows, cudaStream_t s);
     // split only rows [row0, row0 + rows) of a [rows_total][k] buffer into
@@ -352,6 +353,9 @@ struct Plan {
     // an apply with device outputs reports a flag raised by the previous one
     int* h_err = nullptr;
     void check_tc_flags(bool wait_device, cudaStream_t s);
+    // waits for the plan's work (and stream s) and throws TBEM_ERR_TIMEOUT
+    // if a tensor-core pass of any earlier apply gave up
+    void sync(cudaStream_t s);
     bool timing = false;
     long launches = 0;  // kernel launches of the last apply
     // phase timing: events recorded on the apply's stream (no synchronization);

@@ -84,6 +84,7 @@ struct TcArgs {
     int n;
     int atomic;
     int* err;
+    long long wait_cycles;             // budget of every role's bounded wait
 };
 
 namespace {
@@ -227,7 +228,7 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
         const long long t0 = clock64();
         while (!mbar_try(b, parity)) {
             if (*reinterpret_cast<volatile int*>(&abort_flag)) return false;
-            if (clock64() - t0 > TC_WAIT_CYCLES) {
+            if (clock64() - t0 > a.wait_cycles) {
                 atomicExch(&abort_flag, 1);
                 return false;
             }
@@ -391,7 +392,8 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
     }
     __syncthreads();
     // drain: every MMA this CTA issued has completed before tensor memory is
-    // released (bounded; after an abort the MMAs in flight still finish)
+    // released (bounded by the fixed default budget, never by a shortened
+    // one: after an abort the MMAs in flight still finish)
     if (warp == 8 && lane == 0 && mma_issued) {
         mma_commit(smem_u32(&drain_bar));
         if (!mbar_wait(smem_u32(&drain_bar), 0)) atomicExch(&abort_flag, 1);
@@ -542,6 +544,7 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
     a.n = P.m;
     a.atomic = atomic;
     a.err = P.err.p;
+    a.wait_cycles = P.wait_cycles > 0 ? P.wait_cycles : TC_WAIT_CYCLES;
     const int n_ctiles = it->second.n, m_tiles = P.m_pad / TC_BM;
     const long total = (long)n_ctiles * m_tiles;
     if (total == 0) return;

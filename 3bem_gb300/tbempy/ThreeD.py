@@ -308,6 +308,19 @@ class FMMOperator(OperatorI):
         """Kernel launches made by the last apply."""
         return check(_L.lib().tbem_fmm_last_launches(self._h))
 
+    def sync(self, stream=None):
+        """Wait for this operator's device work; raises TbemError (code -5)
+        if a tensor-core pass of an earlier apply gave up waiting.  An apply
+        into device memory is asynchronous, so such a failure would otherwise
+        only surface on the next apply."""
+        check(_L.lib().tbem_fmm_sync(self._h, stream))
+
+    def set_wait_cycles(self, cycles):
+        """Budget (SM cycles) of the tensor-core kernels' bounded waits;
+        0 restores the default (about two seconds).  For tests of the
+        timeout path."""
+        check(_L.lib().tbem_fmm_set_wait_cycles(self._h, int(cycles)))
+
     def phase_times(self):
         cap = 32
         names = (C.c_char_p * cap)()

@@ -62,6 +62,8 @@ SIGNATURES = {
     "tbem_fmm_set_timing": (_I, [_P, _I]),
     "tbem_fmm_phase_times": (_I, [_P, _P, _P, _I]),
     "tbem_fmm_last_launches": (_L, [_P]),
+    "tbem_fmm_sync": (_I, [_P, _P]),
+    "tbem_fmm_set_wait_cycles": (_I, [_P, C.c_longlong]),
     "tbem_fmm_p2p_block": (_L, [_P]),
     "tbem_fmm_tc_tile": (_L, [_P]),
     "tbem_fmm_m2l_ranks": (_I, [_P, _P, _P]),

@@ -355,7 +355,7 @@ def main():
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath) and tensor and args.grid == N_GRID and n_rhs == 1:
         # DRAM bytes of one launch of the tensor kernel on this workload, from a
-        # one-pass ncu capture (profiles/tc_gemm_dram_elastic_fault_98k.md)
+        # one-pass ncu capture of this bench
         traffic = json.load(open(tpath)).get("m2l_tc_dram_bytes_per_launch")
 
     # -- the plain FP64 form on the same workload

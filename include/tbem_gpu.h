@@ -117,8 +117,28 @@ int tbem_fmm_create(int kernel, const double* kernel_params,
                     TbemFmm** out);
 
 /* Replaces FMMOperator::apply (cpp/fmm.cpp:551-557) for n_rhs right-hand
- * sides at once; stream is a cudaStream_t (NULL = the handle's stream). */
+ * sides at once; stream is a cudaStream_t (NULL = the handle's stream).
+ * With a host y the call is synchronous and a tensor-core pass that gave up
+ * waiting (TBEM_ERR_TIMEOUT) is reported by this call.  With a device y the
+ * call is asynchronous: such a timeout is only seen by the NEXT call on the
+ * handle (the result of the failed apply is garbage), so a caller that keeps
+ * its results on the device checks tbem_fmm_sync before using them.  Once
+ * raised, the timeout stays: every later apply returns TBEM_ERR_TIMEOUT. */
 int tbem_fmm_apply(TbemFmm* h, const double* x, double* y, int n_rhs, void* stream);
+
+/* Waits for the handle's device work (its own stream and, when given, the
+ * caller's stream) and returns TBEM_ERR_TIMEOUT if a tensor-core pass of any
+ * earlier apply gave up waiting, else TBEM_OK.  No reference counterpart
+ * (the reference's apply is synchronous). */
+int tbem_fmm_sync(TbemFmm* h, void* stream);
+
+/* Budget, in SM clock cycles, of every bounded wait in the tensor-core
+ * kernels of this operator (0: the default of about two seconds).  A
+ * smaller budget makes a slow wait give up sooner: the kernel then stops,
+ * finishes the matrix products already issued, frees its tensor memory and
+ * reports TBEM_ERR_TIMEOUT.  For tests of that error path; no reference
+ * counterpart. */
+int tbem_fmm_set_wait_cycles(TbemFmm* h, long long cycles);
 
 /* Transpose apply: w = A^T z with A the operator tbem_fmm_apply applies
  * (the FMM passes run transposed and in reverse order).  No reference
@@ -228,13 +248,17 @@ int tbem_direct_gradients(int kernel, const double* kernel_params,
                           double* g_src_weights, double* g_x, void* stream);
 
 /* The direct FP64 sum of tbem_direct_apply for callers that cannot allocate
- * device memory.  No counterpart in the reference.  Every data pointer must be
- * device memory; nothing is copied, allocated or freed.  Its scratch (weighted
- * strengths and work items) is a static 16 MiB device array kept by every GPU
- * that loads the library: R * n_src * n_rhs must not exceed 1,966,080 and
- * n_obs must stay below about 3 million, else TBEM_ERR_ARG.  The first call on
- * a device looks up the array's device address (make it before any stream
- * capture).  All calls share the array: calls that overlap on the GPU race.
+ * device memory.  No counterpart in the reference.  3D kernel ids 0..6 only
+ * (2D points would have to be widened into scratch).  Every point, weight,
+ * density and output pointer must be device memory; kernel_params is read on
+ * the host and must be host memory (or NULL for the defaults).  Nothing is
+ * copied, allocated or freed.  Its scratch (weighted strengths and work
+ * items) is a static 16 MiB device array kept by every GPU that loads the
+ * library: R * n_src * n_rhs must not exceed 1,966,080 and n_obs must stay
+ * below about 3 million, else TBEM_ERR_ARG.  Every call looks up the array's
+ * device address on the current device (so a device reset is harmless); the
+ * first call on a device loads the module there: make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.
  * Asynchronous on `stream`. */
 int tbem_direct_apply_noalloc(int kernel, const double* kernel_params,
                               const double* obs_locs, const double* obs_normals, long n_obs,

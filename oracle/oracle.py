@@ -65,7 +65,17 @@ def build(force=False):
     return LIB_PATH
 
 
-REF_ROOT = "/root/reference"  # the reference checkout, where one exists
+def _ref_root():
+    """The reference checkout: $TBEM_REFERENCE_ROOT, else a folder named
+    `reference` beside this repository, where one exists ("" when neither)."""
+    env = os.environ.get("TBEM_REFERENCE_ROOT")
+    if env:
+        return env
+    sib = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return sib if os.path.isdir(os.path.join(sib, "cpp")) else ""
+
+
+REF_ROOT = _ref_root()
 
 
 def build_ref(ref_root=REF_ROOT):

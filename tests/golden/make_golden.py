@@ -6,7 +6,10 @@ small seeded inputs, and stores inputs, reference outputs, the reference's
 check-to-equivalent operators, trees and task lists.  The GPU tests compare
 the product against these without needing the reference checkout.
 
-    python tests/golden/make_golden.py [/root/reference] [all|2d|nearfield]
+    python tests/golden/make_golden.py [<reference checkout>] [all|2d|nearfield|config1|interior]
+
+(the checkout defaults to $TBEM_REFERENCE_ROOT, else a `reference` folder
+beside this repository)
 
 ("2d" writes only the 2D fixtures: fmm_*2_*.npz and kernels_2d.npz;
 "nearfield" only the nearfield / farfield-correction matrices,
@@ -111,6 +114,38 @@ def make_case(name, kernel, n_src, n_obs, order, leaf, small, seed, geom):
         a, b = ref.list(kind)
         out["list_%s_obs" % kind] = a
         out["list_%s_src" % kind] = b
+    return out
+
+
+def make_config1():
+    """The plain FP64 Laplace single-layer workload at its stated size: an
+    icosahedron subdivided 4 times (5,120 triangles, radius 1), 3 Gauss points
+    per triangle (15,360 points, obs = src), weights area / 3, outward normals,
+    density uniform[-1, 1] from seed 0; "order 6" read as 6 (6 - 1)^2 + 2 =
+    152 requested surface points, MAC 0.3, 50 points per leaf, d = 0.05.
+    Stores the reference's apply, its pseudo-inverses, trees, lists, its
+    one-ulp sensitivity and the FP64 direct sum."""
+    locs, nrm, w = meshes.sphere_points(4)
+    x = np.random.default_rng(0).uniform(-1, 1, len(locs))
+    ref = oracle.RefFMM("LaplaceSingle", locs, nrm, locs, nrm, w, 0.3, 152, 50, 0.05, False)
+    out = dict(kernel="LaplaceSingle", order=152, leaf=50, small=0, mac=0.3, d=0.05,
+               obs_locs=locs, obs_normals=nrm, src_locs=locs, src_normals=nrm, src_weights=w,
+               x=x, y_ref=ref.apply(x), n_surf=ref.n_surf(),
+               y_direct=oracle.direct("LaplaceSingle", locs, nrm, locs, nrm, w, x))
+    for which in (0, 1):
+        t = ref.tree(which)
+        for k in ("level", "index", "n_idx", "n_children"):
+            out["tree%d_%s" % (which, k)] = t[k].astype(np.int32)
+        for k in ("center", "hw"):
+            out["tree%d_%s" % (which, k)] = t[k]
+        out["tree%d_indices" % which] = np.concatenate(t["indices"]).astype(np.int32)
+        out["c2e%d" % which] = np.stack([ref.c2e(which, lev) for lev in range(ref.n_levels(which))])
+    for kind in oracle.LISTS:
+        a, b = ref.list(kind)
+        out["list_%s_obs" % kind] = a.astype(np.int32)
+        out["list_%s_src" % kind] = b.astype(np.int32)
+    orc = oracle.OracleFMM("LaplaceSingle", locs, nrm, locs, nrm, w, 0.3, 152, 50, 0.05, False)
+    out["ulp_floor"] = orc.ulp_floor(x)
     return out
 
 
@@ -315,10 +350,16 @@ def make_dense_boundary_cases():
         print("wrote dense boundary", name, A.shape, np.abs(A - B).max() / np.abs(A).max())
 
 
-def main(ref_root="/root/reference", which="all"):
+def main(ref_root=None, which="all"):
+    ref_root = ref_root or oracle.REF_ROOT
     oracle.build()
     if oracle.build_ref(ref_root) is None:
         raise SystemExit("the reference checkout is needed to regenerate the fixtures")
+    if which == "config1":
+        data = make_config1()
+        np.savez_compressed(os.path.join(HERE, "fmm_laps_config1.npz"), **data)
+        print("wrote laps_config1", len(data["x"]), "points, ulp floor %.3g" % data["ulp_floor"])
+        return
     if which == "nearfield":
         make_nearfield_cases()
         make_interior_cases()
