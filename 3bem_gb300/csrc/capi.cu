@@ -91,6 +91,36 @@ int tbem_fmm_create(int kernel, const double* kernel_params, const double* obs_l
     return TBEM_OK;
 }
 
+int tbem_fmm_batch_create(int kernel, const double* kernel_params, int n_meshes,
+                          const long* mesh_offsets, const double* locs, const double* normals,
+                          const double* weights, const TbemFmmConfig* config,
+                          const TbemGpuOptions* options, TbemFmm** out)
+{
+    if (!out || !config) return fail(TBEM_ERR_ARG, "null config or output handle");
+    *out = nullptr;
+    TbemGpuOptions opt;
+    tbem_default_options(&opt);
+    if (options) opt = *options;
+    TbemFmm* h = nullptr;
+    int rc = guarded([&] {
+        h = new TbemFmm();
+        h->plan.build_batch(kernel, kernel_params, n_meshes, mesh_offsets, locs, normals, weights,
+                            *config, opt);
+    });
+    if (rc != TBEM_OK) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return TBEM_OK;
+}
+
+long tbem_fmm_n_meshes(const TbemFmm* h)
+{
+    if (!h) return fail(TBEM_ERR_ARG, "null handle");
+    return h->plan.batch_off.empty() ? 1 : (long)h->plan.batch_off.size() - 1;
+}
+
 int tbem_fmm_apply(TbemFmm* h, const double* x, double* y, int n_rhs, void* stream)
 {
     if (!h || !y || (!x && tbem_fmm_n_cols(h) > 0)) return fail(TBEM_ERR_ARG, "null argument");
@@ -123,8 +153,13 @@ int tbem_fmm_clone(const TbemFmm* h, TbemFmm** out)
         };
         const std::vector<double> ol = narrow(p.h_obs_locs), on = narrow(p.h_obs_normals),
                                   sl = narrow(p.h_src_locs), sn = narrow(p.h_src_normals);
-        const int created = tbem_fmm_create(p.kid, params, ol.data(), on.data(), p.n_obs, sl.data(),
-                                            sn.data(), p.h_src_weights.data(), p.n_src, &p.cfg, &p.opt, &c);
+        const int created =
+            p.batch_off.empty()
+                ? tbem_fmm_create(p.kid, params, ol.data(), on.data(), p.n_obs, sl.data(), sn.data(),
+                                  p.h_src_weights.data(), p.n_src, &p.cfg, &p.opt, &c)
+                : tbem_fmm_batch_create(p.kid, params, (int)p.batch_off.size() - 1,
+                                        p.batch_off.data(), sl.data(), sn.data(),
+                                        p.h_src_weights.data(), &p.cfg, &p.opt, &c);
         if (created != TBEM_OK) throw tbem::Error(created, g_last_error);
         if (!p.f.mixed && !p.opt.host_only) {
             // carry over installed check-to-equivalent operators (a host-only

@@ -89,10 +89,15 @@ eval_kernel(const EvalArgs<T> a)
     constexpr int R = kernel_dim(KID);
     constexpr int TPB = EVAL_THREADS / TPT;  // targets per CTA
     constexpr bool COMP = sizeof(T) == 4;    // compensated accumulation in FP32
+    // scalar kernels with point sources and many right-hand sides: the
+    // densities of four right-hand sides share one 4-vector, and the kernel
+    // value is computed once per pair and applied to every right-hand side
+    constexpr bool PACK = R == 1 && NR >= 4 && NR % 4 == 0 && !SRC_SURF && !TRANS;
+    constexpr int NV = PACK ? NR / 4 : NR;
     // per source: position, normal, and the R density components of every
     // right-hand side, each a 4-vector (one shared load in the pair loop)
     __shared__ Vec4<T> sp[EVAL_THREADS], sn[EVAL_THREADS];
-    __shared__ Vec4<T> sv[NR][EVAL_THREADS];
+    __shared__ Vec4<T> sv[NV][EVAL_THREADS];
 
     const int task = a.item_task[blockIdx.x];
     const int t0 = a.item_start[blockIdx.x];
@@ -160,13 +165,26 @@ eval_kernel(const EvalArgs<T> a)
                 const long p = sb + li;
                 qx = a.s_xyz[3 * p]; qy = a.s_xyz[3 * p + 1]; qz = a.s_xyz[3 * p + 2];
                 nx = a.s_nrm[3 * p]; ny = a.s_nrm[3 * p + 1]; nz = a.s_nrm[3 * p + 2];
+                if constexpr (PACK) {
 #pragma unroll
-                for (int r_ = 0; r_ < NR; r_++) {
-                    T vv[3] = {T(0), T(0), T(0)};
+                    for (int r4 = 0; r4 < NV; r4++) {
+                        T vv[4];
 #pragma unroll
-                    for (int d = 0; d < R; d++)
-                        vv[d] = r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
-                    sv[r_][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                        for (int k = 0; k < 4; k++) {
+                            const int r_ = 4 * r4 + k;
+                            vv[k] = r_ < nr_here ? a.s_str[(long)(a.rhs0 + r_) * a.s_n + p] : T(0);
+                        }
+                        sv[r4][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], vv[3]};
+                    }
+                } else {
+#pragma unroll
+                    for (int r_ = 0; r_ < NR; r_++) {
+                        T vv[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                        for (int d = 0; d < R; d++)
+                            vv[d] = r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
+                        sv[r_][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                    }
                 }
             }
             sp[threadIdx.x] = Vec4<T>{T(qx - ox), T(qy - oy), T(qz - oz), T(0)};
@@ -179,6 +197,21 @@ eval_kernel(const EvalArgs<T> a)
                 const Vec4<T> q = sp[j];
                 const T dx = q.x - px, dy = q.y - py, dz = q.z - pz;
                 const Vec4<T> nq = sn[j];
+                if constexpr (PACK) {
+                    // the kernel value once (accumulate with a unit density)
+                    T kv = 0;
+                    const T one[3] = {T(1), T(0), T(0)};
+                    accumulate<KID, false, T>(dx, dy, dz, pnx, pny, pnz, nq.x, nq.y, nq.z, a.c2, one, &kv);
+#pragma unroll
+                    for (int r4 = 0; r4 < NV; r4++) {
+                        const Vec4<T> vq = sv[r4][j];
+                        part[4 * r4] += kv * vq.x;
+                        part[4 * r4 + 1] += kv * vq.y;
+                        part[4 * r4 + 2] += kv * vq.z;
+                        part[4 * r4 + 3] += kv * vq.w;
+                    }
+                    continue;
+                }
 #pragma unroll
                 for (int r_ = 0; r_ < NR; r_++) {
                     const Vec4<T> vq = sv[r_][j];

@@ -9,10 +9,18 @@ namespace {
 template <typename T, bool TR, bool TS, bool SS, int TPT>
 void go_tpt(int nr, int n_items, const EvalArgs<T>& a, cudaStream_t s)
 {
-    if (nr == 1)
+    if (nr == 1) {
         eval_kernel<EVAL_KID, TR, T, 1, TS, SS, TPT><<<n_items, EVAL_THREADS, 0, s>>>(a);
-    else
-        eval_kernel<EVAL_KID, TR, T, EVAL_NR, TS, SS, TPT><<<n_items, EVAL_THREADS, 0, s>>>(a);
+        return;
+    }
+    if constexpr (sizeof(T) == 4 && kernel_dim(EVAL_KID) == 1 && kernel_space_dim(EVAL_KID) == 3 &&
+                  !TR && !SS) {
+        if (nr == EVAL_NR_WIDE) {
+            eval_kernel<EVAL_KID, TR, T, EVAL_NR_WIDE, TS, SS, TPT><<<n_items, EVAL_THREADS, 0, s>>>(a);
+            return;
+        }
+    }
+    eval_kernel<EVAL_KID, TR, T, EVAL_NR, TS, SS, TPT><<<n_items, EVAL_THREADS, 0, s>>>(a);
 }
 
 template <typename T, bool TR, bool TS, bool SS>
@@ -34,7 +42,7 @@ template <typename T>
 cudaError_t go_t(const EvalLaunch& L, const void* args, cudaStream_t s)
 {
     const EvalArgs<T>& a = *static_cast<const EvalArgs<T>*>(args);
-    const int nr = (a.nrhs - a.rhs0) > 1 ? EVAL_NR : 1;
+    const int nr = eval_rhs_block(L.kid, sizeof(T) == 4, L.trans, L.src_surf, a.nrhs - a.rhs0);
     const int idx = (L.trans ? 4 : 0) + (L.tgt_surf ? 2 : 0) + (L.src_surf ? 1 : 0);
     switch (idx) {
     case 0: return go<T, false, false, false>(nr, L.n_items, L.tpt, args, s);

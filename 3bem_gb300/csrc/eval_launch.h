@@ -36,6 +36,20 @@ cudaError_t launch_eval_k23(const EvalLaunch&, const void* args, bool fp32, cuda
 
 // rhs chunk per launch (the kernel keeps NR x R accumulators per thread)
 constexpr int EVAL_NR = 4;
+// FP32 scalar kernels with point sources, not transposed: 16 right-hand
+// sides per launch (the kernel value is shared by all of them)
+constexpr int EVAL_NR_WIDE = 16;
+
+// Right-hand sides one launch of the evaluation kernel handles when
+// `remaining` are left from the launch's first one.
+inline int eval_rhs_block(int kid, bool fp32, bool trans, bool src_surf, int remaining)
+{
+    if (remaining <= 1) return 1;
+    if (fp32 && kernel_dim(kid) == 1 && kernel_space_dim(kid) == 3 && !trans && !src_surf &&
+        remaining >= EVAL_NR_WIDE)
+        return EVAL_NR_WIDE;
+    return EVAL_NR;
+}
 
 template <typename T>
 inline cudaError_t launch_eval(const EvalLaunch& L, const EvalArgs<T>& a, cudaStream_t s)

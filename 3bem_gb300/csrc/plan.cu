@@ -16,6 +16,7 @@
 #include <numeric>
 #include <tuple>
 
+#include "nearfield.h"
 #include "plan.h"
 
 namespace tbem {
@@ -448,6 +449,21 @@ inline double hypot_ref(const double* v)
 
 }  // namespace
 
+// Homogeneity degree of a 3D kernel in the separation (K(s d) = s^deg K(d)
+// for s > 0); 1 (not homogeneous) for the 2D kernels, whose logarithms are not.
+namespace {
+int kernel_degree(int kid)
+{
+    switch (kid) {
+    case LAP_S: case EL_DISP: return -1;
+    case LAP_D: case EL_TRAC: case EL_ADJ: return -2;
+    case EL_HYP: return -3;
+    case IDENT: return 0;
+    default: return 1;
+    }
+}
+}  // namespace
+
 // ------------------------------------------------------------------ plan
 
 Plan::~Plan()
@@ -545,14 +561,7 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     std::unique_ptr<DeviceGuard> guard;
     if (!opt.host_only) {
         guard.reset(new DeviceGuard(opt.device));
-        TBEM_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        TBEM_CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-        TBEM_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-        TBEM_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-        TBEM_CKB(cublasCreate(&cublas));
-        TBEM_CKB(cublasSetStream(cublas, stream));
-        TBEM_CKS(cusolverDnCreate(&solver));
-        TBEM_CKS(cusolverDnSetStream(solver, stream));
+        create_streams();
     }
 
     otree = build_tree(h_obs_locs.data(), n_obs, cfg.min_pts_per_cell, sdim);
@@ -570,9 +579,31 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     n = R * ns;
     L = build_lists(otree, *stree, cfg.mac, ns, cfg.account_for_small_cells != 0);
     if (opt.host_only) return;
+    finish_build(h_obs_locs.data(), h_obs_normals.data(), h_src_locs.data(), h_src_normals.data(),
+                 h_src_weights.data());
+}
+
+void Plan::create_streams()
+{
+    TBEM_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    TBEM_CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    TBEM_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    TBEM_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    TBEM_CKB(cublasCreate(&cublas));
+    TBEM_CKB(cublasSetStream(cublas, stream));
+    TBEM_CKS(cusolverDnCreate(&solver));
+    TBEM_CKS(cusolverDnSetStream(solver, stream));
+}
+
+// Device side of a build once the trees and lists exist: the trees' points
+// (in the coordinates the operators are built in), the task sets, the
+// form's operators and the autotuned launch shapes.
+void Plan::finish_build(const double* o_locs, const double* o_nrm, const double* s_locs,
+                        const double* s_nrm, const double* s_w)
+{
     d_unit.upload(unit);
-    upload_tree(otree, h_obs_locs.data(), h_obs_normals.data(), nullptr, dobs);
-    upload_tree(*stree, h_src_locs.data(), h_src_normals.data(), h_src_weights.data(), dsrc_own);
+    upload_tree(otree, o_locs, o_nrm, nullptr, dobs);
+    upload_tree(*stree, s_locs, s_nrm, s_w, dsrc_own);
     dsrc = &dsrc_own;
     build_tasks();
     build_form();
@@ -582,6 +613,105 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     if (opt.p2m_block == 1 || opt.p2m_block == 2 || opt.p2m_block == 4) p2m_tpt = opt.p2m_block;
     else autotune_p2m();
     autotune_tc();
+}
+
+// The batched form: n_meshes independent point sets (observation = source
+// points within each mesh) in one plan.  Mesh m is moved and scaled into the
+// cube [-1, 1]^3 (x' = (x - c_m) / H_m, c_m its bounding box's centre, H_m
+// its largest half width) and its tree is cut from that cube, so every
+// mesh's level-l cells are the same cubes of half width 2^-l and all meshes
+// share one set of check-to-equivalent and translation operators.  The
+// kernel is homogeneous of degree deg in the separation at fixed normals,
+// K(x, y) = H^deg K(x', y'), so the weights become w' = H^deg w and the
+// scaled problem has exactly the original's outputs.  The trees of the
+// meshes form one forest (level-major), and the task lists of all meshes
+// are concatenated: every pass of an apply covers every mesh in one launch
+// per pass (per level for M2M / L2L).
+void Plan::build_batch(int kernel, const double* params, int n_meshes, const long* offsets,
+                       const double* locs, const double* normals, const double* weights,
+                       const TbemFmmConfig& cfg_, const TbemGpuOptions& opt_)
+{
+    if (!kernel_valid(kernel) || kernel_space_dim(kernel) != 3)
+        throw Error(TBEM_ERR_ARG, "the batched form takes the 3D kernel ids 0..6");
+    if (cfg_.min_pts_per_cell <= 0) throw Error(TBEM_ERR_ARG, "min_pts_per_cell must be > 0");
+    if (cfg_.order <= 0) throw Error(TBEM_ERR_ARG, "order must be > 0");
+    if (!(cfg_.mac > 0)) throw Error(TBEM_ERR_ARG, "mac must be > 0");
+    if (cfg_.account_for_small_cells)
+        throw Error(TBEM_ERR_ARG, "the batched form has no small-cell routing");
+    if (opt_.precision != TBEM_PRECISION_FP64 && opt_.precision != TBEM_PRECISION_MIXED)
+        throw Error(TBEM_ERR_ARG, "unknown precision form");
+    if (n_meshes < 0 || (n_meshes > 0 && !offsets)) throw Error(TBEM_ERR_ARG, "bad mesh offsets");
+    if (n_meshes > 0 && offsets[0] != 0) throw Error(TBEM_ERR_ARG, "mesh offsets must start at 0");
+    for (int m = 0; m < n_meshes; m++)
+        if (offsets[m + 1] < offsets[m]) throw Error(TBEM_ERR_ARG, "mesh offsets must not decrease");
+    const long N = n_meshes > 0 ? offsets[n_meshes] : 0;
+    if (N > 0 && (!locs || !normals || !weights)) throw Error(TBEM_ERR_ARG, "null point array");
+    kid = kernel;
+    R = kernel_dim(kid);
+    sdim = 3;
+    mu = (params && R > 1) ? params[0] : 1.0;
+    nu = (params && R > 1) ? params[1] : 0.25;
+    kp = make_kparams(kid, mu, nu);
+    cfg = cfg_;
+    opt = opt_;
+    if (!(opt.svd_threshold > 0)) opt.svd_threshold = 1e-10;
+    n_obs = n_src = N;
+    batch_off.assign(offsets, offsets + n_meshes + 1);
+    h_obs_locs.assign(locs, locs + 3 * N);
+    h_obs_normals.assign(normals, normals + 3 * N);
+    h_src_locs = h_obs_locs;
+    h_src_normals = h_obs_normals;
+    h_src_weights.assign(weights, weights + N);
+
+    const int deg = kernel_degree(kid);
+    std::vector<double> xl(3 * N), xw(N);
+    batch_center.assign(3 * (size_t)n_meshes, 0.0);
+    batch_scale.assign(n_meshes, 1.0);
+    std::vector<Tree> trees(n_meshes);
+    std::vector<TaskLists> lists(n_meshes);
+    unit = sphere_surface(cfg.order);
+    ns = (int)(unit.size() / 3);
+    n = R * ns;
+    const double origin[3] = {0.0, 0.0, 0.0};
+    nf::parallel_for(
+        n_meshes,
+        [&](long m) {
+            const long p0 = offsets[m], p1 = offsets[m + 1];
+            double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+            for (long i = p0; i < p1; i++)
+                for (int d = 0; d < 3; d++) {
+                    const double v = locs[3 * i + d];
+                    if (i == p0 || v < mn[d]) mn[d] = v;
+                    if (i == p0 || v > mx[d]) mx[d] = v;
+                }
+            double c[3], H = 0;
+            for (int d = 0; d < 3; d++) {
+                c[d] = (mx[d] + mn[d]) / 2.0;
+                H = std::max(H, (mx[d] - mn[d]) / 2.0);
+            }
+            if (!(H > 0)) H = 1.0;  // a single point (or coincident points)
+            for (int d = 0; d < 3; d++) batch_center[3 * m + d] = c[d];
+            batch_scale[m] = H;
+            const double wscale = std::pow(H, (double)deg);
+            for (long i = p0; i < p1; i++) {
+                for (int d = 0; d < 3; d++) xl[3 * i + d] = (locs[3 * i + d] - c[d]) / H;
+                xw[i] = weights[i] * wscale;
+            }
+            trees[m] = build_tree_cube(&xl[3 * p0], p1 - p0, cfg.min_pts_per_cell, origin, 1.0);
+            lists[m] = build_lists(trees[m], trees[m], cfg.mac, ns, false);
+        },
+        1);
+    std::vector<std::vector<int>> gid;
+    otree = merge_forest(trees, std::vector<long>(offsets, offsets + std::max(n_meshes, 0)), gid);
+    trees.clear();
+    L = merge_lists(lists, gid);
+    lists.clear();
+    same_tree = true;
+    stree = &otree;
+    if (opt.host_only) return;
+    DeviceGuard guard(opt.device);
+    create_streams();
+    finish_build(xl.data(), h_obs_normals.data(), xl.data(), h_obs_normals.data(), xw.data());
 }
 
 // Picks the tensor-core GEMM's N tile for the M2L set (and uses it for the
@@ -857,21 +987,6 @@ void Plan::build_tasks()
         }
     }
 }
-
-// Homogeneity degree of a 3D kernel in the separation (K(s d) = s^deg K(d)
-// for s > 0); 1 (not homogeneous) for the 2D kernels, whose logarithms are not.
-namespace {
-int kernel_degree(int kid)
-{
-    switch (kid) {
-    case LAP_S: case EL_DISP: return -1;
-    case LAP_D: case EL_TRAC: case EL_ADJ: return -2;
-    case EL_HYP: return -3;
-    case IDENT: return 0;
-    default: return 1;
-    }
-}
-}  // namespace
 
 // Pseudo-inverses of the check-to-equivalent systems of every level
 // (build_check_to_equiv + svd_inverse_nbody, cpp/fmm.cpp:113-160), FP64 on
@@ -1797,7 +1912,7 @@ void Plan::eval(const TaskSet& ts, int ekid, bool tgt_surf, bool src_surf, const
     a.scale = ep.scale;
     EvalLaunch Lc{ekid, trans, tgt_surf, src_surf, ts.n_items()};
     Lc.tpt = ts.tpt;
-    for (int r0 = 0; r0 < nrhs; r0 += (nrhs - r0 > 1 ? EVAL_NR : 1)) {
+    for (int r0 = 0; r0 < nrhs; r0 += eval_rhs_block(ekid, sizeof(T) == 4, trans, src_surf, nrhs - r0)) {
         a.rhs0 = r0;
         TBEM_CK(launch_eval<T>(Lc, a, s));
         launches++;
@@ -1816,7 +1931,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
     if (F.mixed && F.m2l_compressed) {
         forward_compressed(nrhs, s);
     } else if (!F.mixed) {
-        gather_kernel<double><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s64.p, NS, R, nrhs);
+        gather_kernel<double><<<grid_for(NS * R * nrhs), 256, 0, s>>>(xin, dsrc->perm.p, dsrc->w.p, s64.p, NS, R, nrhs);
         TBEM_CK(cudaGetLastError());
         launches++;
         TBEM_CK(cudaMemsetAsync(cu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
@@ -1847,7 +1962,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
         eval<double>(l2p, F.kt_kid, false, true, O, dobs, 0, dobs, F.r_de, nullptr, 0, qd64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
         mark("l2p", s);
     } else {
-        gather_kernel<float><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s32.p, NS, R, nrhs);
+        gather_kernel<float><<<grid_for(NS * R * nrhs), 256, 0, s>>>(xin, dsrc->perm.p, dsrc->w.p, s32.p, NS, R, nrhs);
         TBEM_CK(cudaGetLastError());
         launches++;
         TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
@@ -1917,7 +2032,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
         }
         mark("l2p", s);
     }
-    scatter_kernel<<<grid_for(NO * R * nrhs), 256, 0, s>>>(y64.p, dobs.perm.p, nullptr, io_y.p, NO, R, nrhs);
+    scatter_kernel<<<grid_for(NO * R * nrhs), 256, 0, s>>>(y64.p, dobs.perm.p, nullptr, yout, NO, R, nrhs);
     TBEM_CK(cudaGetLastError());
     launches++;
     mark("scatter", s);
@@ -1937,7 +2052,7 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
     if (F.mixed && F.m2l_compressed) {
         adjoint_compressed(nrhs, s);
     } else if (!F.mixed) {
-        gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
+        gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
         TBEM_CK(cudaGetLastError());
         launches++;
         TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
@@ -1963,7 +2078,7 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
         }
         eval<double>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
     } else {
-        gather_kernel<float><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, s32.p, NO, R, nrhs);
+        gather_kernel<float><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, s32.p, NO, R, nrhs);
         TBEM_CK(cudaGetLastError());
         launches++;
         TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
@@ -1978,7 +2093,7 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
         if (need64) {
             TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
             // obs-space inputs in FP64 for the FP64 sub-paths
-            gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
+            gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
             TBEM_CK(cudaGetLastError());
             launches++;
             eval<double>(m2p_t, F.kt_kid, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
@@ -2005,7 +2120,7 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
             if (l < (int)F.m2m_t.size()) F.m2m_t[l].run<float>(cu32.p, cu32.p, n, nrhs, 1, GEMM_ADD, s, &launches);
         eval<float>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
     }
-    scatter_kernel<<<grid_for(NS * R * nrhs), 256, 0, s>>>(s64.p, dsrc->perm.p, dsrc->w.p, io_y.p, NS, R, nrhs);
+    scatter_kernel<<<grid_for(NS * R * nrhs), 256, 0, s>>>(s64.p, dsrc->perm.p, dsrc->w.p, yout, NS, R, nrhs);
     TBEM_CK(cudaGetLastError());
     launches++;
     mark("scatter", s);
@@ -2021,7 +2136,7 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     const long ncs = (long)S.cells.size(), nco = (long)O.cells.size();
     Form& F = f;
     const int ri = F.r_in, ro = F.r_out;
-    gather_kernel<float><<<grid_for(NS * R * nrhs), 256, 0, s>>>(io_x.p, dsrc->perm.p, dsrc->w.p, s32.p, NS, R, nrhs);
+    gather_kernel<float><<<grid_for(NS * R * nrhs), 256, 0, s>>>(xin, dsrc->perm.p, dsrc->w.p, s32.p, NS, R, nrhs);
     TBEM_CK(cudaGetLastError());
     launches++;
     TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
@@ -2084,7 +2199,7 @@ void Plan::adjoint_compressed(int nrhs, cudaStream_t s)
     const long ncs = (long)S.cells.size(), nco = (long)O.cells.size();
     Form& F = f;
     const int ri = F.r_in, ro = F.r_out;
-    gather_kernel<float><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, s32.p, NO, R, nrhs);
+    gather_kernel<float><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, s32.p, NO, R, nrhs);
     TBEM_CK(cudaGetLastError());
     launches++;
     TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
@@ -2105,7 +2220,7 @@ void Plan::adjoint_compressed(int nrhs, cudaStream_t s)
     if (!L.m2p.empty()) {
         // density gradients in FP64, folded into u~ through (2^-l W)^T
         TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
-        gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(io_x.p, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
+        gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
         TBEM_CK(cudaGetLastError());
         launches++;
         eval<double>(m2p_t, F.kt_kid, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
@@ -2144,15 +2259,44 @@ void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
     }
     if (h_err && (h_err[0] || h_err[1]))  // raised by an earlier apply
         throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
-    ensure_rhs(nrhs);
+    // the right-hand sides run in chunks whose work buffers stay within a
+    // fixed budget (the cell buffers grow with cells x right-hand sides)
+    const int chunk = rhs_chunk(nrhs);
+    io_x.ensure((size_t)n_in * nrhs);
+    io_y.ensure((size_t)n_out * nrhs);
+    ensure_rhs(chunk);
     launches = 0;
     TBEM_CK(cudaMemcpyAsync(io_x.p, x, sizeof(double) * n_in * nrhs,
                             x_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
-    if (adj) adjoint(nrhs, s);
-    else forward(nrhs, s);
+    for (int r0 = 0; r0 < nrhs; r0 += chunk) {
+        const int nr = std::min(chunk, nrhs - r0);
+        xin = io_x.p + (long)r0 * n_in;
+        yout = io_y.p + (long)r0 * n_out;
+        if (adj) adjoint(nr, s);
+        else forward(nr, s);
+    }
     TBEM_CK(cudaMemcpyAsync(y, io_y.p, sizeof(double) * n_out * nrhs,
                             y_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     check_tc_flags(!y_dev, s);
+}
+
+// Right-hand sides per pass: as many as keep the per-right-hand-side work
+// buffers (cell states, their tensor-core planes, point strengths and
+// outputs) within RHS_WORK_BUDGET bytes; at least one.
+int Plan::rhs_chunk(int nrhs) const
+{
+    constexpr double RHS_WORK_BUDGET = 24.0 * (1L << 30);
+    const double ncs = (double)stree->cells.size(), nco = (double)otree.cells.size();
+    const double N = (double)std::max(n_obs, n_src);
+    double per = 8.0 * R * N * 4;  // io copies, strengths, outputs
+    if (f.mixed) {
+        per += 4.0 * (ncs + nco) * n;
+        if (f.m2l_compressed) per += 4.0 * (ncs * f.r_in + nco * f.r_out) + 6.0 * std::max(ncs, nco) * 128;
+        if (!L.m2p.empty() || f.m2l_on_the_fly) per += 8.0 * (2 * ncs + nco) * n;
+    } else {
+        per += 8.0 * 2 * (ncs + nco) * n;
+    }
+    return (int)std::max<double>(1.0, std::min<double>(nrhs, std::floor(RHS_WORK_BUDGET / per)));
 }
 
 // Copies the tensor-core timeout flags into pinned memory on stream s and,

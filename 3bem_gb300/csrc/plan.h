@@ -231,8 +231,7 @@ struct GemmSet {
     // tensor-core path (B taken from P's split planes; D columns of P.m rows);
     // nn = elements per operator in the pool the groups' offsets refer to
     struct TcTiles {
-        DBuf<int> op;          // per column tile: operator index
-        DBuf<int> brow, drow;  // per column tile and column: B row / D column, -1 past the end
+        DBuf<int4> t;  // per column tile: operator, group's first pair, first column, group columns
         int n = 0;
     };
     std::map<int, TcTiles> tc_tiles;  // per (nrhs, N tile)
@@ -336,6 +335,9 @@ struct Plan {
     // work buffers
     int cap_rhs = 0;
     DBuf<double> io_x, io_y;            // device staging of caller data (original order)
+    double* xin = nullptr;              // the current chunk of right-hand sides in io_x
+    double* yout = nullptr;             // and its outputs in io_y
+    int rhs_chunk(int nrhs) const;
     DBuf<double> s64, y64;              // strengths / outputs in tree order
     DBuf<float> s32;
     DBuf<double> cu64, qu64, cd64, qd64;  // cell buffers [cell][rhs][n]
@@ -367,12 +369,23 @@ struct Plan {
     void read_phases();
     // kept for clone()
     std::vector<double> h_obs_locs, h_obs_normals, h_src_locs, h_src_normals, h_src_weights;
+    // batched form (build_batch): mesh m owns points [batch_off[m],
+    // batch_off[m + 1]); its centre and half width map it into [-1, 1]^3.
+    // Empty for a single-mesh operator.
+    std::vector<long> batch_off;
+    std::vector<double> batch_center, batch_scale;
 
     ~Plan();
     void build(int kernel, const double* params, const double* obs_locs, const double* obs_normals,
                long n_obs, const double* src_locs, const double* src_normals,
                const double* src_weights, long n_src, const TbemFmmConfig& cfg,
                const TbemGpuOptions& opt);
+    void build_batch(int kernel, const double* params, int n_meshes, const long* offsets,
+                     const double* locs, const double* normals, const double* weights,
+                     const TbemFmmConfig& cfg, const TbemGpuOptions& opt);
+    void create_streams();
+    void finish_build(const double* o_locs, const double* o_nrm, const double* s_locs,
+                      const double* s_nrm, const double* s_w);
     void apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adjoint);
     void set_c2e(int which, long level, const double* op);
     void get_c2e(int which, long level, double* out) const;

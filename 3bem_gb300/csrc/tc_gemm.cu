@@ -76,9 +76,14 @@ struct TcArgs {
     const __nv_bfloat16* A[TC_TERMS];  // [op][m_pad][k_pad] per term
     long a_op_stride;                  // m_pad * k_pad
     int k_pad;
-    const int* tile_op;    // per column tile: operator index
-    const int* tile_brow;  // per column tile and column: B row (cell * nrhs + rhs), -1 past the end
-    const int* tile_drow;  // per column tile and column: D column (cell * nrhs + rhs), -1 past the end
+    // per column tile: {operator, first pair of its group, first column of
+    // the tile within the group, columns of the group}; column c of a group
+    // is (pair pair0 + c / nrhs, right-hand side c % nrhs), its B row
+    // in_cell[pair] * nrhs + rhs and its D column out_cell[pair] * nrhs + rhs
+    const int4* tiles;
+    const int* in_cell;
+    const int* out_cell;
+    int nrhs;
     const __nv_bfloat16* B[TC_TERMS];  // [cell][rhs][k_pad] per term
     float* D;                          // [cell][rhs][n]
     int n;
@@ -251,10 +256,13 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
         // independent loads: their latency hides behind the current tile)
         int nop = 0, nb[B_PER];
         auto prefetch = [&](int t) {
-            const int tile = t / m_tiles;
-            nop = a.tile_op[tile];
+            const int4 ti = a.tiles[t / m_tiles];
+            nop = ti.x;
 #pragma unroll
-            for (int i = 0; i < B_PER; i++) nb[i] = a.tile_brow[(long)tile * BN + prow + RSTEP * i];
+            for (int i = 0; i < B_PER; i++) {
+                const int c = ti.z + prow + RSTEP * i;
+                nb[i] = c < ti.w ? a.in_cell[ti.y + c / a.nrhs] * a.nrhs + c % a.nrhs : -1;
+            }
         };
         if (blockIdx.x < total) prefetch(blockIdx.x);
         int j = 0;  // chunks issued (over all tiles of this CTA)
@@ -358,12 +366,16 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
         int tc = 0;
         for (int t = blockIdx.x; t < total; t += gridDim.x, tc++) {
             const int b = tc % Sh::NBUF, bu = tc / Sh::NBUF;
-            const int tile = t / m_tiles, m0 = (t % m_tiles) * TC_BM;
+            const int m0 = (t % m_tiles) * TC_BM;
             // lane q of a 32-column chunk resolves column q's destination; the
             // loads overlap the wait for the accumulator
+            const int4 ti = a.tiles[t / m_tiles];
             int drow[NCC];
 #pragma unroll
-            for (int cc = 0; cc < NCC; cc++) drow[cc] = a.tile_drow[(long)tile * BN + cc * 32 + lane];
+            for (int cc = 0; cc < NCC; cc++) {
+                const int c = ti.z + cc * 32 + lane;
+                drow[cc] = c < ti.w ? a.out_cell[ti.y + c / a.nrhs] * a.nrhs + c % a.nrhs : -1;
+            }
             if (!wait(&accf_bar[b], bu & 1)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int row = m0 + warp * 32 + lane;
@@ -503,31 +515,20 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
     const int key = nrhs * 1024 + bn;
     auto it = tc_tiles.find(key);
     if (it == tc_tiles.end()) {
-        // column tiles of every group, with each column's B row and D column
-        std::vector<int> op, brow, drow;
+        // column tiles of every group: (operator, group's first pair, first
+        // column, the group's column count)
+        std::vector<int4> t;
         for (size_t g = 0; g < npairs.size(); g++) {
-            const int ncols = npairs[g] * nrhs;
-            for (int c = 0; c < ncols; c += bn) {
-                op.push_back((int)(A_off[g] / nn));
-                for (int jj = 0; jj < bn; jj++) {
-                    const int col = c + jj;
-                    if (col < ncols) {
-                        const long p = pair0[g] + col / nrhs;
-                        const int r = col % nrhs;
-                        brow.push_back(in_cell[p] * nrhs + r);
-                        drow.push_back(out_cell[p] * nrhs + r);
-                    } else {
-                        brow.push_back(-1);
-                        drow.push_back(-1);
-                    }
-                }
-            }
+            const long ncols = (long)npairs[g] * nrhs;
+            if (ncols > INT32_MAX || pair0[g] > INT32_MAX)
+                throw Error(TBEM_ERR_ARG, "tensor-core GEMM group too large");
+            for (long c = 0; c < ncols; c += bn)
+                t.push_back(make_int4((int)(A_off[g] / nn), (int)pair0[g], (int)c, (int)ncols));
         }
+        if (t.size() > (size_t)INT32_MAX / 4) throw Error(TBEM_ERR_ARG, "too many tensor-core tiles");
         TcTiles& e = tc_tiles[key];
-        e.op.upload(op);
-        e.brow.upload(brow);
-        e.drow.upload(drow);
-        e.n = (int)op.size();
+        e.t.upload(t);
+        e.n = (int)t.size();
         it = tc_tiles.find(key);
     }
     TcArgs a;
@@ -537,9 +538,10 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
     }
     a.a_op_stride = (long)P.m_pad * P.k_pad;
     a.k_pad = P.k_pad;
-    a.tile_op = it->second.op.p;
-    a.tile_brow = it->second.brow.p;
-    a.tile_drow = it->second.drow.p;
+    a.tiles = it->second.t.p;
+    a.in_cell = d_in.p;
+    a.out_cell = d_out.p;
+    a.nrhs = nrhs;
     a.D = D;
     a.n = P.m;
     a.atomic = atomic;

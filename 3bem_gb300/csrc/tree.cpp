@@ -116,6 +116,10 @@ struct Builder {
 
 }  // namespace
 
+namespace {
+Tree flatten(const std::vector<Node>& N, long n);
+}  // namespace
+
 Tree build_tree(const double* pts, long n, long min_pts, int dim)
 {
     Builder B;
@@ -135,8 +139,106 @@ Tree build_tree(const double* pts, long n, long min_pts, int dim)
     B.nodes.reserve(2 * (size_t)(n / std::max<long>(min_pts, 1)) + 16);
     B.nodes.push_back(std::move(root));
     B.build_children(0, box, 0);  // ... but its children are cut from the unexpanded one
+    return flatten(B.nodes, n);
+}
 
-    const auto& N = B.nodes;
+Tree build_tree_cube(const double* pts, long n, long min_pts, const double center[3], double hw)
+{
+    Builder B;
+    B.pts = pts;
+    B.min_pts = min_pts;
+    B.dim = 3;
+    std::vector<long> all(n);
+    for (long i = 0; i < n; i++) all[i] = i;
+    Box box{{center[0], center[1], center[2]}, {hw, hw, hw}};
+    Node root;
+    root.b = box;
+    root.idx = all;
+    root.level = 0;
+    root.ref_index = 0;
+    root.octant = -1;
+    for (int k = 0; k < 8; k++) root.child[k] = -1;
+    B.nodes.reserve(2 * (size_t)(n / std::max<long>(min_pts, 1)) + 16);
+    B.nodes.push_back(std::move(root));
+    B.build_children(0, box, 0);
+    return flatten(B.nodes, n);
+}
+
+Tree merge_forest(const std::vector<Tree>& trees, const std::vector<long>& pt_off,
+                  std::vector<std::vector<int>>& gid)
+{
+    Tree F;
+    const size_t M = trees.size();
+    gid.assign(M, {});
+    int max_l = -1;
+    size_t total = 0;
+    for (size_t m = 0; m < M; m++) {
+        max_l = std::max(max_l, trees[m].n_levels() - 1);
+        total += trees[m].cells.size();
+        gid[m].assign(trees[m].cells.size(), -1);
+    }
+    F.cells.reserve(total);
+    F.level_start.assign(max_l + 2, 0);
+    // level-major over the meshes: level l of mesh 0, of mesh 1, ...
+    for (int l = 0; l <= max_l; l++) {
+        F.level_start[l] = (int)F.cells.size();
+        for (size_t m = 0; m < M; m++) {
+            const Tree& t = trees[m];
+            if (l >= t.n_levels()) continue;
+            for (int i = t.level_start[l]; i < t.level_start[l + 1]; i++) {
+                gid[m][i] = (int)F.cells.size();
+                F.cells.push_back(t.cells[i]);
+            }
+        }
+    }
+    F.level_start[max_l + 1] = (int)F.cells.size();
+    for (size_t m = 0; m < M; m++) {
+        const Tree& t = trees[m];
+        for (size_t i = 0; i < t.cells.size(); i++) {
+            Cell& c = F.cells[gid[m][i]];
+            if (c.parent >= 0) c.parent = gid[m][c.parent];
+            if (c.first_child >= 0) c.first_child = gid[m][c.first_child];
+            c.pt_begin += pt_off[m];
+            c.pt_end += pt_off[m];
+        }
+        for (long k = 0; k < t.n_points(); k++) F.perm.push_back(pt_off[m] + t.perm[k]);
+        for (int p : t.preorder) F.preorder.push_back(gid[m][p]);
+    }
+    F.first_at_level.assign(max_l + 1, -1);
+    for (int p : F.preorder) {
+        const int l = F.cells[p].level;
+        if (F.first_at_level[l] < 0) F.first_at_level[l] = p;
+    }
+    return F;
+}
+
+TaskLists merge_lists(const std::vector<TaskLists>& lists, const std::vector<std::vector<int>>& gid)
+{
+    TaskLists L;
+    for (size_t m = 0; m < lists.size(); m++) {
+        const TaskLists& a = lists[m];
+        const std::vector<int>& g = gid[m];
+        auto cells = [&](const std::vector<int>& in, std::vector<int>& out) {
+            for (int c : in) out.push_back(g[c]);
+        };
+        auto pairs = [&](const std::vector<CellPair>& in, std::vector<CellPair>& out) {
+            for (const CellPair& p : in) out.push_back({g[p.obs], g[p.src]});
+        };
+        cells(a.p2m, L.p2m);
+        cells(a.m2m, L.m2m);
+        cells(a.l2l, L.l2l);
+        cells(a.l2p, L.l2p);
+        pairs(a.p2p, L.p2p);
+        pairs(a.m2p, L.m2p);
+        pairs(a.p2l, L.p2l);
+        pairs(a.m2l, L.m2l);
+    }
+    return L;
+}
+
+namespace {
+Tree flatten(const std::vector<Node>& N, long n)
+{
     Tree T;
     // level-major flattening: FIFO over the nodes, children pushed in octant order
     std::vector<int> order;
@@ -208,6 +310,7 @@ Tree build_tree(const double* pts, long n, long min_pts, int dim)
     }
     return T;
 }
+}  // namespace
 
 namespace {
 

@@ -59,6 +59,19 @@ struct TaskLists {
 TaskLists build_lists(const Tree& obs, const Tree& src, double mac, long n_surf,
                       bool small_cells);
 
+// The batched form's trees.  build_tree_cube: the same splitting rules with
+// the root's bounds, and the box its children are cut from, both the given
+// cube -- trees of different point sets in the same cube then have
+// bit-identical cells level by level.  merge_forest: several trees as one
+// forest, level-major (level l of tree 0, of tree 1, ...), each tree's points
+// offset by pt_off[m] in the permuted and the original order; gid[m][i] is
+// the forest id of cell i of tree m.  merge_lists: the trees' task lists in
+// forest ids, tree after tree.
+Tree build_tree_cube(const double* pts, long n, long min_pts, const double center[3], double hw);
+Tree merge_forest(const std::vector<Tree>& trees, const std::vector<long>& pt_off,
+                  std::vector<std::vector<int>>& gid);
+TaskLists merge_lists(const std::vector<TaskLists>& lists, const std::vector<std::vector<int>>& gid);
+
 // Unit points of surrounding_surface_sphere(order) (cpp/fmm.cpp:22-45).
 std::vector<double> sphere_surface(long order);
 // The 2D surface of order points on the unit circle (cpp/fmm.cpp:7-20), [n][3].

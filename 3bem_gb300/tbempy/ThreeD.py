@@ -329,6 +329,57 @@ class FMMOperator(OperatorI):
         return [(names[i].decode(), float(ms[i])) for i in range(min(k, cap))]
 
 
+class BatchedFMMOperator(FMMOperator):
+    """One operator over many independent meshes (the batched form; the
+    reference builds one FMMOperator per mesh).  ``offsets[m]:offsets[m+1]``
+    are mesh m's rows of ``locs`` / ``normals`` / ``weights``; within a mesh
+    the observation points are its source points.  Applies take
+    x[rhs][C][N] over all N points (meshes concatenated) and return
+    y[rhs][R][N]; every pass covers all meshes in one launch."""
+
+    def __init__(self, K, locs, normals, weights, offsets, config, precision="mixed", device=0,
+                 svd_threshold=1e-10, host_only=False, m2l_path=0, m2l_rank_tol=1e-7,
+                 p2p_block=0, p2m_block=0, tc_shape=0, _handle=None):
+        self.K = K
+        self.config = config
+        self.precision = precision
+        self.R = K.tensor_dim
+        if _handle is not None:
+            self._h = _handle
+            return
+        self._locs = _f64(locs, (-1, 3))
+        self._normals = _f64(normals, (-1, 3))
+        self._weights = _f64(weights, (-1,))
+        self.offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        opt = _L.TbemGpuOptions()
+        _L.lib().tbem_default_options(C.byref(opt))
+        opt.precision = _L.PRECISION[precision]
+        opt.device = int(device)
+        opt.svd_threshold = float(svd_threshold)
+        opt.host_only = int(bool(host_only))
+        opt.m2l_path = int(m2l_path)
+        opt.m2l_rank_tol = float(m2l_rank_tol)
+        opt.p2p_block = int(p2p_block)
+        opt.p2m_block = int(p2m_block)
+        opt.tc_shape = int(tc_shape)
+        cfg = config._c()
+        h = C.c_void_p()
+        check(_L.lib().tbem_fmm_batch_create(
+            K.kernel_id, _ptr(K.params()), len(self.offsets) - 1, _ptr(self.offsets),
+            _ptr(self._locs), _ptr(self._normals), _ptr(self._weights), C.byref(cfg),
+            C.byref(opt), C.byref(h)))
+        self._h = h
+
+    def n_meshes(self):
+        return check(_L.lib().tbem_fmm_n_meshes(self._h))
+
+    def clone(self):
+        h = C.c_void_p()
+        check(_L.lib().tbem_fmm_clone(self._h, C.byref(h)))
+        return BatchedFMMOperator(self.K, None, None, None, None, self.config,
+                                  precision=self.precision, _handle=h)
+
+
 class FMMGraph:
     """One CUDA graph replaying the applies of several operators (e.g. one per
     mesh of a batch) between fixed float64 CUDA tensors (tbem_fmm_graph_*).

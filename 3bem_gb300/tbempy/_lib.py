@@ -46,6 +46,8 @@ _P, _L, _I, _D = C.c_void_p, C.c_long, C.c_int, C.c_double
 SIGNATURES = {
     "tbem_default_options": (None, [_P]),
     "tbem_fmm_create": (_I, [_I, _P, _P, _P, _L, _P, _P, _P, _L, _P, _P, _P]),
+    "tbem_fmm_batch_create": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "tbem_fmm_n_meshes": (_L, [_P]),
     "tbem_fmm_apply": (_I, [_P, _P, _P, _I, _P]),
     "tbem_fmm_apply_adjoint": (_I, [_P, _P, _P, _I, _P]),
     "tbem_fmm_n_rows": (_L, [_P]),

@@ -119,6 +119,37 @@ def sphere_points(n_subdiv=4):
     return points_from_mesh(v, t)
 
 
+_SPHERE_CACHE = {}
+
+
+def sphere_batch(n_meshes=200, seed=2, levels=(2, 6), n_rhs=64):
+    """The batched Laplace workload: ``n_meshes`` icospheres with subdivision
+    levels drawn uniformly from ``levels`` (inclusive; 320 to 81,920
+    triangles), radii lognormal(0, 0.5), centres uniform in [-100, 100]^3, 3
+    Gauss points per triangle, outward normals; then ``n_rhs`` densities
+    uniform[-1, 1] over all points, all from one generator seeded ``seed``.
+    Returns (locs [N,3], normals [N,3], weights [N], offsets [n_meshes + 1],
+    x [n_rhs, N])."""
+    rng = np.random.default_rng(seed)
+    lev = rng.integers(levels[0], levels[1] + 1, n_meshes)
+    rad = rng.lognormal(0.0, 0.5, n_meshes)
+    cen = rng.uniform(-100.0, 100.0, (n_meshes, 3))
+    L, Nm, W, off = [], [], [], [0]
+    for m in range(n_meshes):
+        k = int(lev[m])
+        if k not in _SPHERE_CACHE:
+            _SPHERE_CACHE[k] = sphere_points(k)
+        l0, n0, w0 = _SPHERE_CACHE[k]
+        L.append(l0 * rad[m] + cen[m])
+        Nm.append(n0)
+        W.append(w0 * rad[m] ** 2)
+        off.append(off[-1] + len(l0))
+    locs = np.ascontiguousarray(np.concatenate(L))
+    x = rng.uniform(-1.0, 1.0, (n_rhs, len(locs)))
+    return (locs, np.ascontiguousarray(np.concatenate(Nm)), np.ascontiguousarray(np.concatenate(W)),
+            np.asarray(off, dtype=np.int64), x)
+
+
 def fault_points(n=128, dip_deg=45.0):
     """Dipping-fault points (98,304 at n=128) plus each point's (u, v)."""
     v, t, uv = dipping_fault(n, dip_deg)

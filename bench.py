@@ -213,6 +213,364 @@ def config_dict(n_rhs):
             "l2": "flushed before every timed step (256 MB write, outside the step timing)"}
 
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no measured FP64 peak exists)
+
+
+def _events_ms(torch, fn, steps, stream, flush=None):
+    """Mean device milliseconds of fn over `steps` runs, CUDA events on the
+    stream the work is issued to (L2 flushed before each when given)."""
+    pairs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+             for _ in range(steps)]
+    for e0, e1 in pairs:
+        if flush is not None:
+            flush.fill_(1)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return sum(e0.elapsed_time(e1) for e0, e1 in pairs) / steps
+
+
+def _phases(op, fn):
+    """Per-phase milliseconds of one run of fn (events between the passes)."""
+    op.phase_times()
+    op.set_timing(True)
+    fn()
+    ph = dict(op.phase_times())
+    op.set_timing(False)
+    return ph
+
+
+# ---------------------------------------------------------------- sphere workload
+
+SPHERE_ORDER, SPHERE_LEAF = 152, 50
+
+
+def sphere_workload():
+    """The plain FP64 Laplace single-layer workload: icosahedron subdivided 4
+    times (5,120 triangles, radius 1), 3 Gauss points per triangle (15,360
+    points), weights area / 3, outward normals, density uniform[-1, 1] seed 0."""
+    from tbempy import meshes
+    locs, nrm, w = meshes.sphere_points(4)
+    x = np.random.default_rng(0).uniform(-1, 1, len(locs))
+    return locs, nrm, w, x
+
+
+def sphere_config():
+    return {"workload": "Laplace single layer 1/(4 pi r) FMM apply, 15,360 points (icosahedron "
+                        "subdivided 4 times, 3 Gauss points per triangle), 1 RHS",
+            "kernel": "LaplaceSingle",
+            "fmm": {"order_requested": SPHERE_ORDER, "surface_points": 152, "mac": MAC,
+                    "min_pts_per_cell": SPHERE_LEAF, "d": D, "account_for_small_cells": False},
+            "n_points": 15360, "n_rhs": 1,
+            "precision": "plain FP64 (the reference's formulation)",
+            "l2": "flushed before every timed step (256 MB write, outside the step timing)"}
+
+
+def run_sphere(args, rank, world, local):
+    from oracle import oracle
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        locs, nrm, w, x = sphere_workload()
+        threads = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        oracle.build()
+        t0 = time.perf_counter()
+        o = oracle.OracleFMM("LaplaceSingle", locs, nrm, locs, nrm, w, MAC, SPHERE_ORDER, SPHERE_LEAF, D)
+        setup = time.perf_counter() - t0
+        ts = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            o.apply(x)
+            if i >= args.warmup:
+                ts.append(time.perf_counter() - t0)
+        t = float(np.median(ts))
+        value = len(locs) / t
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "points*RHS/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded icosphere)", "config": sphere_config(),
+            "cpu_baseline": {"value": value, "unit": "points*RHS/s", "cores": oracle.max_threads(),
+                             "kind": "port", "sample": "one full oracle FMM apply per step"},
+            "e2e": {"value": value, "unit": "points*RHS/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "setup_s": setup}), flush=True)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    from tbempy import ThreeD
+    from tbempy import _lib
+    import ctypes as C
+    locs, nrm, w, x = sphere_workload()
+    N = len(locs)
+    K = ThreeD.LaplaceSingle()
+    cfg = ThreeD.FMMConfig(MAC, SPHERE_ORDER, SPHERE_LEAF, D, False)
+    t0 = time.perf_counter()
+    op = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="fp64", device=local)
+    setup_s = time.perf_counter() - t0
+    opm = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed", device=local)
+    xd = torch.tensor(x, device="cuda")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        op.apply(xd)
+        opm.apply(xd)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = _events_ms(torch, lambda: op.apply(xd), args.steps, stream, flush)
+        ms_mixed = _events_ms(torch, lambda: opm.apply(xd), args.steps, stream, flush)
+    launches = op.last_launches() * args.steps
+    phases = _phases(op, lambda: op.apply(xd))
+    phases_mixed = _phases(opm, lambda: opm.apply(xd))
+    # end to end through the C ABI, pinned host buffers
+    xh = torch.tensor(x).pin_memory()
+    yh = torch.empty(N, dtype=torch.float64).pin_memory()
+    L = _lib.lib()
+    for _ in range(2):
+        _lib.check(L.tbem_fmm_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), 1, None))
+    e2e = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _lib.check(L.tbem_fmm_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), 1, None))
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e))
+    y = yh.numpy().copy()
+    exact = ThreeD.DirectOperator(K, locs, nrm, locs, nrm, w).apply(x)
+    err = float(np.linalg.norm(y - exact) / np.linalg.norm(exact))
+    ym = opm.apply(x)
+    err_m = float(np.linalg.norm(ym - exact) / np.linalg.norm(exact))
+    parity = None
+    fx = os.path.join(ROOT, "tests", "golden", "fmm_laps_config1.npz")
+    if os.path.exists(fx):
+        g = np.load(fx)
+        own = float(np.linalg.norm(y - g["y_ref"]) / np.linalg.norm(g["y_ref"]))
+        for which in (0, 1):
+            for lev, m in enumerate(g["c2e%d" % which]):
+                op.set_c2e(which, lev, m)
+        yr = op.apply(x)
+        parity = {"own_operators_vs_reference": own,
+                  "reference_operators_vs_reference": float(np.linalg.norm(yr - g["y_ref"]) /
+                                                            np.linalg.norm(g["y_ref"])),
+                  "reference_ulp_floor": float(g["ulp_floor"])}
+    # roofline: the plain form's M2L products (FP64 grouped GEMM over the
+    # deduplicated operators), 2 n^2 flops per pair
+    n = op.n_surface()
+    pairs = len(op.list("m2l")[0])
+    m2l_ms = phases.get("m2l", float("nan"))
+    achieved = 2.0 * n * n * pairs / (m2l_ms / 1e3) / 1e12
+    cpu = None
+    if not args.no_cpu:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        oracle.build()
+        o = oracle.OracleFMM("LaplaceSingle", locs, nrm, locs, nrm, w, MAC, SPHERE_ORDER, SPHERE_LEAF, D)
+        t0 = time.perf_counter()
+        o.apply(x)
+        tc = time.perf_counter() - t0
+        cpu = {"value": N / tc, "unit": "points*RHS/s", "cores": oracle.max_threads(), "kind": "port",
+               "sample": "one full oracle FMM apply (%.2f s)" % tc}
+    print(json.dumps({
+        "metric": METRIC, "value": N / (ms / 1e3), "unit": "points*RHS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded icosphere)", "config": sphere_config(), "clocks": clk.summary(),
+        "e2e": {"value": N / e2e_s, "unit": "points*RHS/s", "h2d_bytes_per_step": 8 * N,
+                "d2h_bytes_per_step": 8 * N},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp64", "kernel": "grouped_gemm_kernel<double>: M2L products",
+                     "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                     "frac": achieved / FP64_NOMINAL_TFLOPS, "peak_kind": "nominal FP64",
+                     "traffic": None, "flops_per_launch": 2.0 * n * n * pairs, "launch_ms": m2l_ms},
+        "phases_ms": phases, "rel_err_vs_direct": err, "parity": parity,
+        "precision_form": {"ms_per_step": ms_mixed, "points_rhs_per_s": N / (ms_mixed / 1e3),
+                           "rel_err_vs_direct": err_m, "phases_ms": phases_mixed,
+                           "speedup_vs_plain": ms / ms_mixed},
+        "cpu_baseline": cpu, "setup_s": setup_s}), flush=True)
+
+
+# --------------------------------------------------------------- batched workload
+
+BATCH_ORDER, BATCH_LEAF = 152, 64
+
+
+def batched_config(n_meshes, n_rhs, n_points):
+    return {"workload": "Laplace double layer FMM apply on %d icospheres (subdivision 2..6, "
+                        "radius lognormal(0, 0.5), centres in [-100, 100]^3, 3 Gauss points per "
+                        "triangle), %d right-hand sides, one operator" % (n_meshes, n_rhs),
+            "kernel": "LaplaceDouble", "n_meshes": n_meshes, "n_points": n_points, "n_rhs": n_rhs,
+            "fmm": {"order_requested": BATCH_ORDER, "surface_points": 152, "mac": MAC,
+                    "min_pts_per_cell": BATCH_LEAF, "d": D, "account_for_small_cells": False},
+            "precision": "mixed: far field in the M2L SVD bases (FP32), M2L products on tcgen05 "
+                         "3xBF16, P2P FP32 compensated; every mesh in the cube [-1,1]^3 of its own",
+            "launch": "the whole apply captured in one CUDA graph, replayed once per step",
+            "l2": "inputs (%.1f GB) larger than L2; no flush" % (8.0 * n_points * n_rhs / 1e9)}
+
+
+def _batched_cpu_seconds(locs, nrm, w, off, n_rhs):
+    """The reference's way: one operator per mesh, one right-hand side per
+    apply (the oracle port, all host threads).  One mesh per subdivision
+    level is timed -- levels 2-4 with a full apply, levels 5-6 on the leading
+    fraction of every task list, extrapolated -- and the batch's time is
+    the sum over meshes of their level's time, times n_rhs.  Level 4 is also
+    timed sampled, to state the extrapolation's error."""
+    from oracle import oracle
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    oracle.build()
+    sizes = np.diff(off)
+    per_size, detail = {}, {}
+    rng = np.random.default_rng(0)
+    for n in sorted(set(sizes.tolist())):
+        m = int(np.nonzero(sizes == n)[0][0])
+        sl = slice(off[m], off[m + 1])
+        o = oracle.OracleFMM("LaplaceDouble", locs[sl], nrm[sl], locs[sl], nrm[sl], w[sl], MAC,
+                             BATCH_ORDER, BATCH_LEAF, D)
+        x = rng.uniform(-1, 1, n)
+        frac = 1.0 if n <= 15360 else (0.1 if n <= 61440 else 0.02)
+        t0 = time.perf_counter()
+        o.apply(x, list_fraction=frac)
+        t = (time.perf_counter() - t0) / frac
+        per_size[n] = t
+        detail[str(n)] = {"seconds_per_apply": t, "list_fraction": frac}
+        if n == 15360:
+            t0 = time.perf_counter()
+            o.apply(x, list_fraction=0.1)
+            ts = (time.perf_counter() - t0) / 0.1
+            detail["extrapolation_check"] = {"points": n, "full_s": t, "sampled_0.1_s": ts,
+                                             "ratio": ts / t}
+        del o
+    total = sum(per_size[int(n)] for n in sizes) * n_rhs
+    return total, detail, oracle.max_threads()
+
+
+def run_batched(args, rank, world, local):
+    from tbempy import meshes
+    locs, nrm, w, off, X = meshes.sphere_batch(n_meshes=args.meshes, seed=2, n_rhs=args.batch_rhs)
+    N, B = len(locs), X.shape[0]
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        t, detail, cores = _batched_cpu_seconds(locs, nrm, w, off, B)
+        value = N * B / t
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "points*RHS/s",
+            "n_gpus": world, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * t,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded icospheres)", "config": batched_config(len(off) - 1, B, N),
+            "cpu_baseline": {"value": value, "unit": "points*RHS/s", "cores": cores, "kind": "port",
+                             "sample": "one mesh per subdivision level timed (levels 5-6 on a "
+                                       "fraction of the task lists), summed over the meshes, "
+                                       "one RHS per apply", "detail": detail},
+            "e2e": {"value": value, "unit": "points*RHS/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    import torch
+    import ctypes as C
+    torch.cuda.set_device(local)
+    from tbempy import ThreeD
+    from tbempy import _lib
+    K = ThreeD.LaplaceDouble()
+    cfg = ThreeD.FMMConfig(MAC, BATCH_ORDER, BATCH_LEAF, D, False)
+    t0 = time.perf_counter()
+    op = ThreeD.BatchedFMMOperator(K, locs, nrm, w, off, cfg, precision="mixed", device=local)
+    setup_s = time.perf_counter() - t0
+    xd = torch.tensor(X, device="cuda")
+    yd = torch.empty_like(xd)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream if stream.cuda_stream else 1)
+    t0 = time.perf_counter()
+    graph = ThreeD.FMMGraph([op], [xd], [yd], n_rhs=B)  # runs one apply, then captures one
+    graph_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        graph.launch(sp)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = _events_ms(torch, lambda: graph.launch(sp), args.steps, stream)
+    launches = op.last_launches() * args.steps
+    phases = _phases(op, lambda: op.apply(xd))
+    # end to end through the C ABI, pinned host buffers
+    xh = torch.tensor(X).pin_memory()
+    yh = torch.empty((B, N), dtype=torch.float64).pin_memory()
+    L = _lib.lib()
+    _lib.check(L.tbem_fmm_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), B, None))
+    e2e = []
+    for _ in range(max(2, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _lib.check(L.tbem_fmm_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), B, None))
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e))
+    Y = yh.numpy()
+    # accuracy: every mesh against the FP64 direct sum on up to 128 sampled rows
+    rng = np.random.default_rng(7)
+    errs = []
+    rows_of = []
+    for m in range(len(off) - 1):
+        sl = slice(off[m], off[m + 1])
+        rows = np.sort(rng.choice(off[m + 1] - off[m], min(128, off[m + 1] - off[m]), replace=False))
+        rows_of.append(rows)
+        d = ThreeD.DirectOperator(K, locs[sl][rows], nrm[sl][rows], locs[sl], nrm[sl], w[sl])
+        ex = d.apply(np.ascontiguousarray(X[:, sl]))
+        got = Y[:, off[m] + rows]
+        errs.append(float(np.linalg.norm(got - ex) / np.linalg.norm(ex)))
+    # roofline: the M2L products on the tensor cores (one launch per RHS chunk)
+    ri, ro = op.m2l_ranks()
+    pairs = len(op.list("m2l")[0])
+    m2l_ms = phases.get("m2l", float("nan"))
+    hbm, bf16, peak_kind = peaks()
+    flops = 6 * 2.0 * ri * ro * pairs * B
+    achieved = flops / (m2l_ms / 1e3) / 1e12
+    del xh, yh
+    # the plain FP64 form on the same meshes, one right-hand side
+    plain = None
+    if not args.no_plain:
+        t0 = time.perf_counter()
+        pop = ThreeD.BatchedFMMOperator(K, locs, nrm, w, off, cfg, precision="fp64", device=local)
+        psetup = time.perf_counter() - t0
+        x0 = torch.tensor(X[0], device="cuda")
+        pop.apply(x0)
+        pms = _events_ms(torch, lambda: pop.apply(x0), 1, stream)
+        y0 = pop.apply(X[0])
+        perr = []
+        for m in range(len(off) - 1):
+            sl = slice(off[m], off[m + 1])
+            rows = rows_of[m]
+            d = ThreeD.DirectOperator(K, locs[sl][rows], nrm[sl][rows], locs[sl], nrm[sl], w[sl])
+            ex = d.apply(np.ascontiguousarray(X[0, sl]))
+            perr.append(float(np.linalg.norm(y0[off[m] + rows] - ex) / np.linalg.norm(ex)))
+        plain = {"ms_per_apply_1rhs": pms, "points_rhs_per_s": N / (pms / 1e3), "setup_s": psetup,
+                 "rel_err_vs_direct_max": max(perr),
+                 "speedup_mixed_batched_vs_plain": (N * B / (ms / 1e3)) / (N / (pms / 1e3))}
+        del pop
+    cpu = None
+    if not args.no_cpu:
+        t, detail, cores = _batched_cpu_seconds(locs, nrm, w, off, B)
+        cpu = {"value": N * B / t, "unit": "points*RHS/s", "cores": cores, "kind": "port",
+               "sample": "one mesh per subdivision level timed (levels 5-6 on a fraction of the "
+                         "task lists), summed over the meshes, one RHS per apply",
+               "detail": detail}
+    print(json.dumps({
+        "metric": METRIC, "value": N * B / (ms / 1e3), "unit": "points*RHS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded icospheres)", "config": batched_config(len(off) - 1, B, N),
+        "clocks": clk.summary(),
+        "e2e": {"value": N * B / e2e_s, "unit": "points*RHS/s", "h2d_bytes_per_step": 8 * N * B,
+                "d2h_bytes_per_step": 8 * N * B},
+        "gpu_launches": launches,
+        "roofline": {"bound": "tensor", "kernel": "tc_gemm_kernel: compressed M2L products, tcgen05 3xBF16",
+                     "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+                     "peak_kind": peak_kind + " bf16 dense (burst)", "traffic": None,
+                     "flops_per_apply": flops, "m2l_ms_per_apply": m2l_ms},
+        "phases_ms": phases, "m2l_ranks": [ri, ro], "m2l_pairs": pairs,
+        "rel_err_vs_direct": {"max_over_meshes": max(errs), "median": float(np.median(errs)),
+                              "rows_per_mesh": 128},
+        "plain_fp64": plain, "cpu_baseline": cpu, "setup_s": setup_s, "graph_capture_s": graph_s,
+        }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -230,11 +588,20 @@ def main():
                     help="0 auto, 1 SIMT FP32, 2 tcgen05 M2L, 3 tcgen05 all, 4 compressed M2L")
     ap.add_argument("--m2l-rank-tol", type=float, default=1e-7,
                     help="singular-value cut of the compressed M2L")
+    ap.add_argument("--workload", default="fault", choices=["fault", "sphere", "batched"],
+                    help="fault: the elastic fault (default); sphere: plain FP64 Laplace single "
+                         "layer on the 15,360-point icosphere; batched: Laplace double layer on "
+                         "200 icospheres x 64 right-hand sides in one operator")
+    ap.add_argument("--meshes", type=int, default=200, help="batched workload: meshes")
+    ap.add_argument("--batch-rhs", type=int, default=64, help="batched workload: right-hand sides")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.workload != "fault":
+        (run_sphere if args.workload == "sphere" else run_batched)(args, rank, world, local)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

@@ -116,6 +116,27 @@ int tbem_fmm_create(int kernel, const double* kernel_params,
                     const TbemFmmConfig* config, const TbemGpuOptions* options,
                     TbemFmm** out);
 
+/* Batched form: one operator over n_meshes independent meshes (no reference
+ * counterpart: the reference builds one FMMOperator per mesh,
+ * cpp/fmm.cpp:72-101, and applies one right-hand side per call,
+ * cpp/fmm.cpp:551-557).  Mesh m owns points [mesh_offsets[m],
+ * mesh_offsets[m+1]) of locs / normals [N][3] and weights [N]; within a
+ * mesh the observation points are its source points, and meshes do not
+ * interact.  Each mesh is mapped into the cube [-1, 1]^3 (its bounding box's
+ * centre to the origin, its largest half width to 1, the weights rescaled by
+ * the kernel's homogeneity) and its octree is cut from that cube, so all
+ * meshes share one set of translation operators and every pass of an apply
+ * covers every mesh in one launch.  3D kernels (ids 0..6); either precision
+ * form; no small-cell routing.  Apply with tbem_fmm_apply: x[r][d][j] over
+ * all N points (meshes concatenated), y likewise; tbem_fmm_graph_create
+ * captures it. */
+int tbem_fmm_batch_create(int kernel, const double* kernel_params, int n_meshes,
+                          const long* mesh_offsets, const double* locs, const double* normals,
+                          const double* weights, const TbemFmmConfig* config,
+                          const TbemGpuOptions* options, TbemFmm** out);
+/* Number of meshes of an operator (1 for tbem_fmm_create's). */
+long tbem_fmm_n_meshes(const TbemFmm* h);
+
 /* Replaces FMMOperator::apply (cpp/fmm.cpp:551-557) for n_rhs right-hand
  * sides at once; stream is a cudaStream_t (NULL = the handle's stream).
  * With a host y the call is synchronous and a tensor-core pass that gave up
