@@ -207,6 +207,88 @@ void GemmSet::run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int tr
 template void GemmSet::run_rect<double>(const double*, double*, int, int, int, int, int, int, cudaStream_t, long*);
 template void GemmSet::run_rect<float>(const float*, float*, int, int, int, int, int, int, cudaStream_t, long*);
 
+namespace {
+// D[tgt][:] += the target's slots, summed in slot order; one CTA per target,
+// the threads over the target's rhs x m values (contiguous in every slot)
+__global__ void slot_reduce_kernel(const double* slots, const int* tgt, const int* ptr,
+                                   const int* idx, int m, int nrhs, double* D)
+{
+    const int t = blockIdx.x;
+    const long len = (long)nrhs * m;
+    const int b = ptr[t], e = ptr[t + 1];
+    double* d = D + (long)tgt[t] * len;
+    for (long j = threadIdx.x; j < len; j += blockDim.x) {
+        double acc = 0.0;
+        for (int q = b; q < e; q++) acc += slots[(long)idx[q] * len + j];
+        d[j] += acc;
+    }
+}
+}  // namespace
+
+void SlotPlan::build(const GemmSet& G, long cap, const void* pool, size_t esz)
+{
+    chunks.clear();
+    max_slots = 0;
+    cap = std::max<long>(cap, 1);
+    std::vector<std::pair<int, int>> out_slot;  // (output cell, local slot) of the chunk
+    auto close = [&]() {
+        if (chunks.empty() || out_slot.empty()) return;
+        Chunk& c = chunks.back();
+        std::stable_sort(out_slot.begin(), out_slot.end());
+        std::vector<int> tgt, ptr{0}, idx;
+        for (size_t i = 0; i < out_slot.size(); i++) {
+            if (i == 0 || out_slot[i].first != out_slot[i - 1].first) {
+                if (i > 0) ptr.push_back((int)idx.size());
+                tgt.push_back(out_slot[i].first);
+            }
+            idx.push_back(out_slot[i].second);
+        }
+        ptr.push_back((int)idx.size());
+        c.tgt.upload(tgt);
+        c.ptr.upload(ptr);
+        c.idx.upload(idx);
+        c.n_tgt = (int)tgt.size();
+        c.gemm.upload(pool, esz);
+        max_slots = std::max(max_slots, (long)idx.size());
+        out_slot.clear();
+    };
+    long used = cap;  // slots of the open chunk (none open yet)
+    for (size_t g = 0; g < G.npairs.size(); g++) {
+        long p = G.pair0[g];
+        const long p1 = p + G.npairs[g];
+        while (p < p1) {
+            if (used >= cap) {
+                close();
+                chunks.emplace_back();
+                used = 0;
+            }
+            const long take = std::min(p1 - p, cap - used);
+            std::vector<std::pair<int, int>> pr;
+            for (long q = p; q < p + take; q++) {
+                pr.push_back({G.in_cell[q], (int)used});
+                out_slot.push_back({G.out_cell[q], (int)used});
+                used++;
+            }
+            chunks.back().gemm.add_group(G.A_off[g], pr);
+            p += take;
+        }
+    }
+    close();
+}
+
+void SlotPlan::run(const double* B, double* D, int m, int nrhs, int trans, double* slots, cudaStream_t s,
+                   long* launches)
+{
+    for (Chunk& c : chunks) {
+        c.gemm.run_rect<double>(B, slots, m, m, m, nrhs, trans, GEMM_STORE, s, launches);
+        if (c.n_tgt > 0) {
+            slot_reduce_kernel<<<c.n_tgt, 256, 0, s>>>(slots, c.tgt.p, c.ptr.p, c.idx.p, m, nrhs, D);
+            TBEM_CK(cudaGetLastError());
+            if (launches) (*launches)++;
+        }
+    }
+}
+
 // ------------------------------------------------------------ device kernels
 
 namespace {
@@ -333,27 +415,29 @@ __global__ void scatter_kernel(const double* acc, const long* perm, const double
 }
 
 // rows of length n -> rows of stride ld (the padding columns are zeroed)
-__global__ void convert_rows_kernel(const double* in, float* out, long rows, int n, int ld)
+template <typename T>
+__global__ void convert_rows_kernel(const double* in, T* out, long rows, int n, int ld)
 {
     const long total = rows * ld;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long)gridDim.x * blockDim.x) {
         const long r = t / ld;
         const int k = (int)(t % ld);
-        out[t] = k < n ? float(in[r * n + k]) : 0.f;
+        out[t] = k < n ? T(in[r * n + k]) : T(0);
     }
 }
 
 // the last r columns (largest eigenvalues) of a column-major n x n
 // eigenvector matrix, times scale -> row-major n x r FP32
-__global__ void basis_rows_kernel(const double* evec, int n, int r, double scale, float* out)
+template <typename T>
+__global__ void basis_rows_kernel(const double* evec, int n, int r, double scale, T* out)
 {
     const long total = (long)n * r;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long)gridDim.x * blockDim.x) {
         const long i = t / r;
         const int j = (int)(t % r);
-        out[t] = float(scale * evec[(long)(n - r + j) * n + i]);
+        out[t] = T(scale * evec[(long)(n - r + j) * n + i]);
     }
 }
 
@@ -367,6 +451,61 @@ __global__ void promote_kernel(const float* in, double* out, long n)
 {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
         out[i] = double(in[i]);
+}
+
+// Precision-form L2P for many right-hand sides: the same sum with E read
+// once per block of L2P_NRB right-hand sides.  One CTA of 64 threads per
+// leaf; the block's coefficients sit in shared memory k-major ([ld][NRB],
+// every read a broadcast); each thread owns one row of E, streams it with
+// float4 loads (the 32 rows of a warp share their cache lines over
+// consecutive k) and keeps NRB accumulators.
+constexpr int L2P_NRB = 16;
+constexpr int L2P_MULTI_THREADS = 64;
+template <typename T>
+__global__ void __launch_bounds__(L2P_MULTI_THREADS) l2p_multi_kernel(
+    const T* E, const long* row0, const int* leaf, const long* pt0, const int* npts, const T* cd,
+    int n, int ld, int R, int nrhs, double* y, long y_n)
+{
+    extern __shared__ __align__(16) unsigned char l2p_smem[];
+    T* c = reinterpret_cast<T*>(l2p_smem);  // [ld][L2P_NRB]
+    const int t = blockIdx.x;
+    const int rows = npts[t] * R;
+    const T* c0 = cd + (long)leaf[t] * nrhs * n;
+    const T* Et = E + row0[t] * (long)ld;
+    for (int r0 = 0; r0 < nrhs; r0 += L2P_NRB) {
+        const int nr = min(L2P_NRB, nrhs - r0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < ld * L2P_NRB; k += blockDim.x) {
+            const int kk = k / L2P_NRB, rr = k % L2P_NRB;
+            c[k] = (rr < nr && kk < n) ? c0[(long)(r0 + rr) * n + kk] : T(0);
+        }
+        __syncthreads();
+        for (int row = threadIdx.x; row < rows; row += blockDim.x) {
+            T acc[L2P_NRB];
+#pragma unroll
+            for (int q = 0; q < L2P_NRB; q++) acc[q] = T(0);
+            const T* er = Et + (long)row * ld;
+            for (int k = 0; k < ld; k += 4) {
+                T a[4];
+                if constexpr (sizeof(T) == 4) {
+                    const float4 v = __ldcs(reinterpret_cast<const float4*>(er + k));
+                    a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w;
+                } else {
+                    const double2 v0 = __ldcs(reinterpret_cast<const double2*>(er + k));
+                    const double2 v1 = __ldcs(reinterpret_cast<const double2*>(er + k + 2));
+                    a[0] = v0.x; a[1] = v0.y; a[2] = v1.x; a[3] = v1.y;
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const T* cb = c + (k + j) * L2P_NRB;
+#pragma unroll
+                    for (int q = 0; q < L2P_NRB; q++) acc[q] += a[j] * cb[q];
+                }
+            }
+            const int i = row / R, d = row % R;
+            for (int q = 0; q < nr; q++) y[((long)(r0 + q) * R + d) * y_n + pt0[t] + i] += (double)acc[q];
+        }
+    }
 }
 
 // Precision-form L2P: y[r][d][pt0 + i] += sum_k E[row0 + i R + d][k] cd[leaf][r][k].
@@ -418,15 +557,16 @@ __global__ void __launch_bounds__(256) l2p_mixed_kernel(const float* E, const lo
 }
 
 // Its transpose: cd[leaf][r][k] = sum_rows E[row][k] z[r][d][pt0 + i].
-__global__ void l2p_mixed_t_kernel(const float* E, const long* row0, const int* leaf,
-                                   const long* pt0, const int* npts, const float* z, long z_n,
-                                   int n, int ld, int R, int nrhs, float* cd)
+template <typename T>
+__global__ void l2p_mixed_t_kernel(const T* E, const long* row0, const int* leaf,
+                                   const long* pt0, const int* npts, const T* z, long z_n,
+                                   int n, int ld, int R, int nrhs, T* cd)
 {
     const int t = blockIdx.x;
     const int rows = npts[t] * R;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         for (int r = 0; r < nrhs; r++) {
-            float acc = 0.f;
+            T acc = 0;
             for (int row = 0; row < rows; row++) {
                 const int i = row / R, d = row % R;
                 acc += E[(row0[t] + row) * (long)ld + k] * z[((long)r * R + d) * z_n + pt0[t] + i];
@@ -530,7 +670,7 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     if ((n_obs_ > 0 && (!obs_locs || !obs_normals)) ||
         (n_src_ > 0 && (!src_locs || !src_normals || !src_weights)))
         throw Error(TBEM_ERR_ARG, "null point array");
-    if (opt_.precision != TBEM_PRECISION_FP64 && opt_.precision != TBEM_PRECISION_MIXED)
+    if (opt_.precision < TBEM_PRECISION_FP64 || opt_.precision > TBEM_PRECISION_FP64_COMPRESSED)
         throw Error(TBEM_ERR_ARG, "unknown precision form");
     kid = kernel;
     R = kernel_dim(kid);
@@ -638,7 +778,7 @@ void Plan::build_batch(int kernel, const double* params, int n_meshes, const lon
     if (!(cfg_.mac > 0)) throw Error(TBEM_ERR_ARG, "mac must be > 0");
     if (cfg_.account_for_small_cells)
         throw Error(TBEM_ERR_ARG, "the batched form has no small-cell routing");
-    if (opt_.precision != TBEM_PRECISION_FP64 && opt_.precision != TBEM_PRECISION_MIXED)
+    if (opt_.precision < TBEM_PRECISION_FP64 || opt_.precision > TBEM_PRECISION_FP64_COMPRESSED)
         throw Error(TBEM_ERR_ARG, "unknown precision form");
     if (n_meshes < 0 || (n_meshes > 0 && !offsets)) throw Error(TBEM_ERR_ARG, "bad mesh offsets");
     if (n_meshes > 0 && offsets[0] != 0) throw Error(TBEM_ERR_ARG, "mesh offsets must start at 0");
@@ -770,7 +910,7 @@ void Plan::autotune_p2p()
 {
     if (p2p.n_items() == 0) return;
     ensure_rhs(1);
-    const bool mixed = f.mixed;
+    const bool mixed = f.mixed && !f.f64;  // FP32 evaluation passes
     if (mixed) TBEM_CK(cudaMemsetAsync(s32.p, 0, sizeof(float) * R * n_src, stream));
     else TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * n_src, stream));
     ScopedEvent t0, t1;
@@ -808,7 +948,7 @@ void Plan::autotune_p2m()
 {
     if (p2m.n_items() == 0) return;
     ensure_rhs(1);
-    const bool mixed = f.mixed;
+    const bool mixed = f.mixed && !f.f64;  // FP32 evaluation passes
     if (mixed) TBEM_CK(cudaMemsetAsync(s32.p, 0, sizeof(float) * R * n_src, stream));
     else TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * n_src, stream));
     ScopedEvent t0, t1;
@@ -1093,7 +1233,9 @@ void Plan::build_c2e(Form& F)
 void Plan::build_form()
 {
     Form& F = f;
-    F.mixed = opt.precision == TBEM_PRECISION_MIXED;
+    // the FP64 compressed form is the precision form's construction in FP64
+    F.mixed = opt.precision == TBEM_PRECISION_MIXED || opt.precision == TBEM_PRECISION_FP64_COMPRESSED;
+    F.f64 = opt.precision == TBEM_PRECISION_FP64_COMPRESSED;
     if (!F.mixed) {
         // reference radii (cpp/fmm.h:42-66) and the operator's own kernel everywhere
         const double far = 4.0 - std::sqrt(2) - 2 * cfg.d;
@@ -1255,6 +1397,12 @@ void Plan::build_gemm_sets(Form& F, long, long, long, const std::vector<long>& m
     for (auto& g : F.l2l_t) g.upload(pool, esz);
     F.m2l.upload(pool, esz);
     F.m2l_t.upload(pool, esz);
+    if (!F.mixed) {
+        // the plain form's M2L through slots, at most ~1 GB of slots per RHS
+        const long cap = std::max<long>(1, (1L << 30) / (8L * n));
+        F.m2l_slots.build(F.m2l, cap, pool, esz);
+        F.m2l_t_slots.build(F.m2l_t, cap, pool, esz);
+    }
     // check-to-equivalent products, one group per level (FP64 pool)
     F.c2e_up.clear();
     F.c2e_up.resize(LS);
@@ -1339,7 +1487,8 @@ void Plan::build_mixed_ops(Form& F)
     // compress, else SIMT FP32),
     // 1 SIMT FP32 for all, 2 tensor cores for the M2L only, 3 tensor cores for
     // all, 4 compressed, 5 compressed with the M2L products on tensor cores
-    const int path = opt.m2l_path == 0 ? 5 : opt.m2l_path;
+    // (the FP64 compressed form: compressed, FP64 SIMT)
+    const int path = F.f64 ? 4 : opt.m2l_path == 0 ? 5 : opt.m2l_path;
     // FP64 copies of the M2L kernel matrices for the compression (compact
     // index), scaled to the root level (see build_m2l_compression)
     const bool compress = (path == 4 || path == 5) && !F.m2l_on_the_fly && !m2l_off.empty();
@@ -1367,9 +1516,10 @@ void Plan::build_mixed_ops(Form& F)
     }
     if (!jobs.empty()) {
         // in chunks to bound the FP64 scratch
-        const size_t chunk = std::max<size_t>(1, (size_t)(2e9 / (8.0 * nn)));
-        DBuf<double> K, Y;
+        // (one grid row per job: at most 65,535 jobs per chunk)
+        const size_t chunk = std::min<size_t>(65535, std::max<size_t>(1, (size_t)(2e9 / (8.0 * nn))));
         DBuf<SurfJob> dj;
+        DBuf<double> K, Y;
         K.alloc(std::min(chunk, jobs.size()) * nn);
         Y.alloc(std::min(chunk, jobs.size()) * nn);
         for (size_t j0 = 0; j0 < jobs.size(); j0 += chunk) {
@@ -1422,12 +1572,20 @@ void Plan::build_mixed_ops(Form& F)
     U64.release();
     KM.release();
     YL.release();
+    if (F.f64 && !F.m2l_compressed)
+        throw Error(TBEM_ERR_ARG, "the FP64 compressed form needs M2L operators that compress (the "
+                                  "observation and source points must be the same, and the "
+                                  "compressed products cheaper than the dense ones)");
     if (F.m2l_compressed && path == 5) {
         F.use_tc_c = true;
         F.tc_c.build(F.Cops.p, n_m2l_ops, F.r_out, F.r_in, stream);
         TBEM_CK(cudaStreamSynchronize(stream));
     }
-    F.use_tc = (path == 2 || path == 3) && !jobs.empty();
+    // the auto path keeps the M2L products on the tensor cores when they do
+    // not compress (uncompressed 3xBF16 planes)
+    const bool auto_tc = opt.m2l_path == 0 && !F.f64 && !F.m2l_compressed && !F.m2l_on_the_fly &&
+                         !m2l_off.empty();
+    F.use_tc = (path == 2 || path == 3 || auto_tc) && !jobs.empty();
     F.use_tc_updown = F.use_tc && path == 3;
     if (F.use_tc) {
         F.tc.build(F.ops32.p, (long)jobs.size(), n, n, stream);
@@ -1456,7 +1614,14 @@ void Plan::build_mixed_ops(Form& F)
     const int ecols = F.m2l_compressed ? F.r_out : n;
     F.E_ld = (ecols + 127) / 128 * 128;
     if (F.E_ld > 2048) throw Error(TBEM_ERR_ARG, "translation surface too large for the L2P kernel");
-    F.E.alloc(std::max<long>(rows * F.E_ld, 1));
+    if (F.f64) F.E64.alloc(std::max<long>(rows * F.E_ld, 1));
+    else F.E.alloc(std::max<long>(rows * F.E_ld, 1));
+    auto store_rows = [&](const double* src, long off, long r, int cols) {
+        if (F.f64)
+            convert_rows_kernel<double><<<grid_for(r * F.E_ld), 256, 0, stream>>>(src, F.E64.p + off, r, cols, F.E_ld);
+        else
+            convert_rows_kernel<float><<<grid_for(r * F.E_ld), 256, 0, stream>>>(src, F.E.p + off, r, cols, F.E_ld);
+    };
     F.E_row0.upload(row0);
     F.E_pt0.upload(pt0);
     F.E_leaf.upload(cell);
@@ -1470,7 +1635,8 @@ void Plan::build_mixed_ops(Form& F)
             const int lev = O.cells[cell[t0]].level;
             size_t t1 = t0;
             long r = 0;
-            while (t1 < cell.size() && O.cells[cell[t1]].level == lev &&
+            // (one grid row per leaf: at most 65,535 leaves per chunk)
+            while (t1 < cell.size() && O.cells[cell[t1]].level == lev && t1 - t0 < 65535 &&
                    (r + (long)npts[t1] * R <= max_rows || t1 == t0)) {
                 r += (long)npts[t1] * R;
                 t1++;
@@ -1492,11 +1658,9 @@ void Plan::build_mixed_ops(Form& F)
                 EV.ensure(r * F.r_out);
                 TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, F.r_out, (int)r, n, &one, F.V64.p, n,
                                      Y.p, n, &zero, EV.p, F.r_out));
-                convert_rows_kernel<<<grid_for(r * F.E_ld), 256, 0, stream>>>(EV.p, F.E.p + row0[t0] * F.E_ld,
-                                                                             r, F.r_out, F.E_ld);
+                store_rows(EV.p, row0[t0] * F.E_ld, r, F.r_out);
             } else {
-                convert_rows_kernel<<<grid_for(r * F.E_ld), 256, 0, stream>>>(Y.p, F.E.p + row0[t0] * F.E_ld,
-                                                                             r, n, F.E_ld);
+                store_rows(Y.p, row0[t0] * F.E_ld, r, n);
             }
             TBEM_CK(cudaGetLastError());
             TBEM_CK(cudaStreamSynchronize(stream));
@@ -1591,16 +1755,32 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
     };
     const int ri = std::min(n, (rank_of(h_ev.data()) + 15) / 16 * 16);
     const int ro = std::min(n, (rank_of(h_ev.data() + n) + 63) / 64 * 64);
-    // no gain once the compressed products approach the dense ones
-    if ((long)ri * ro > nn / 2) return;
+    // no gain once the compressed products, padded to the tensor-core tiles
+    // (128 output rows, 64-deep K chunks), cost as much as the dense ones
+    auto pad = [](long v, long q) { return (v + q - 1) / q * q; };
+    if (pad(ro, 128) * pad(ri, 64) >= pad(n, 128) * pad(n, 64) || (long)ri * ro > nn * 9 / 10) return;
     F.r_in = ri;
     F.r_out = ro;
     const double* W = Gi.p + (long)(n - ri) * n;  // column-major n x ri
     const double* V = Go.p + (long)(n - ro) * n;  // column-major n x ro
     F.V64.alloc((size_t)n * ro);
     TBEM_CK(cudaMemcpyAsync(F.V64.p, V, sizeof(double) * n * ro, cudaMemcpyDeviceToDevice, stream));
-    F.Vb.alloc((size_t)n * ro);
-    basis_rows_kernel<<<grid_for((long)n * ro), 256, 0, stream>>>(Go.p, n, ro, 1.0, F.Vb.p);
+    // the operator pools: FP32 (the precision form) or FP64 (the FP64
+    // compressed form); `store` copies count FP64 values into one of them
+    const bool f64 = F.f64;
+    auto store = [&](const double* src, long count, DBuf<float>& p32, DBuf<double>& p64, long off) {
+        if (count <= 0) return;
+        if (f64) convert_kernel<double><<<grid_for(count), 256, 0, stream>>>(src, p64.p + off, count);
+        else convert_kernel<float><<<grid_for(count), 256, 0, stream>>>(src, p32.p + off, count);
+        TBEM_CK(cudaGetLastError());
+    };
+    auto alloc_pool = [&](size_t count, DBuf<float>& p32, DBuf<double>& p64) {
+        if (f64) p64.alloc(count);
+        else p32.alloc(count);
+    };
+    alloc_pool((size_t)n * ro, F.Vb, F.Vb64);
+    if (f64) basis_rows_kernel<double><<<grid_for((long)n * ro), 256, 0, stream>>>(Go.p, n, ro, 1.0, F.Vb64.p);
+    else basis_rows_kernel<float><<<grid_for((long)n * ro), 256, 0, stream>>>(Go.p, n, ro, 1.0, F.Vb.p);
     TBEM_CK(cudaGetLastError());
     const Tree& S = *stree;
     const Tree& O = otree;
@@ -1610,22 +1790,25 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
     // the stored operator); kept in FP64 for the M2M operators
     DBuf<double> P64;
     P64.alloc((size_t)LS * n * ri);
-    F.Pb.alloc((size_t)LS * n * ri);
-    F.Wl.alloc((size_t)LS * n * ri);
+    alloc_pool((size_t)LS * n * ri, F.Pb, F.Pb64);
+    alloc_pool((size_t)LS * n * ri, F.Wl, F.Wl64);
     for (int l = 0; l < LS; l++) {
         const double f = std::ldexp(1.0, l);
         TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ri, n, &f, F.c2e.p + F.c2e_up_off[l], n, W,
                              n, &zero, P64.p + (long)l * n * ri, n));
-        basis_rows_kernel<<<grid_for((long)n * ri), 256, 0, stream>>>(Gi.p, n, ri, std::ldexp(1.0, -l),
-                                                                     F.Wl.p + (long)l * n * ri);
+        if (f64)
+            basis_rows_kernel<double><<<grid_for((long)n * ri), 256, 0, stream>>>(
+                Gi.p, n, ri, std::ldexp(1.0, -l), F.Wl64.p + (long)l * n * ri);
+        else
+            basis_rows_kernel<float><<<grid_for((long)n * ri), 256, 0, stream>>>(
+                Gi.p, n, ri, std::ldexp(1.0, -l), F.Wl.p + (long)l * n * ri);
         TBEM_CK(cudaGetLastError());
     }
-    convert_kernel<float><<<grid_for((long)LS * n * ri), 256, 0, stream>>>(P64.p, F.Pb.p, (long)LS * n * ri);
-    TBEM_CK(cudaGetLastError());
+    store(P64.p, (long)LS * n * ri, F.Pb, F.Pb64, 0);
     // C_k (row-major ro x ri) = column-major C_k^T = W^T T_k^T V, T_k^T being
     // the column-major view of the stored matrix
     const long cc = (long)ro * ri;
-    F.Cops.alloc((size_t)n_ops * cc);
+    alloc_pool((size_t)n_ops * cc, F.Cops, F.Cops64);
     const long cb = std::max<long>(1, std::min<long>(n_ops, (long)(1e9 / (8.0 * n * ro))));
     const long n_m2m = (long)in.m2m_lc->size();
     long n_l2l = 0;
@@ -1640,12 +1823,11 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
                                            (long long)n * ro, (int)kb));
         TBEM_CKB(cublasDgemmStridedBatched(cublas, CUBLAS_OP_T, CUBLAS_OP_N, ri, ro, n, &one, W, n, 0,
                                            P.p, n, (long long)n * ro, &zero, CT.p, ri, cc, (int)kb));
-        convert_kernel<float><<<grid_for(kb * cc), 256, 0, stream>>>(CT.p, F.Cops.p + k0 * cc, kb * cc);
-        TBEM_CK(cudaGetLastError());
+        store(CT.p, kb * cc, F.Cops, F.Cops64, k0 * cc);
         TBEM_CK(cudaStreamSynchronize(stream));
     }
     // X (row-major ri x ri) = column-major X^T = 2^-l_c W^T (K^T P_(l_p)^T)
-    F.Xops.alloc(std::max<long>(n_m2m, 1) * ri * ri);
+    alloc_pool(std::max<long>(n_m2m, 1) * ri * ri, F.Xops, F.Xops64);
     for (long j = 0; j < n_m2m; j++) {
         const int lc = (*in.m2m_lc)[j], lp = lc - 1;
         const double f = std::ldexp(1.0, -lc);
@@ -1654,24 +1836,18 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
         TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, ri, ri, n, &f, W, n, P.p, n, &zero,
                              CT.p + j * (long)ri * ri, ri));
     }
-    if (n_m2m > 0) {
-        convert_kernel<float><<<grid_for(n_m2m * ri * ri), 256, 0, stream>>>(CT.p, F.Xops.p, n_m2m * ri * ri);
-        TBEM_CK(cudaGetLastError());
-    }
+    store(CT.p, n_m2m * ri * ri, F.Xops, F.Xops64, 0);
     TBEM_CK(cudaStreamSynchronize(stream));
     // Y (row-major ro x ro) = column-major Y^T = V^T (L^T V), L^T the
     // column-major view of the combined operator
-    F.Yops.alloc(std::max<long>(n_l2l, 1) * ro * ro);
+    alloc_pool(std::max<long>(n_l2l, 1) * ro * ro, F.Yops, F.Yops64);
     for (long j = 0; j < n_l2l; j++) {
         TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, ro, n, &one, in.YL + j * nn, n, V, n,
                              &zero, P.p, n));
         TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, ro, ro, n, &one, V, n, P.p, n, &zero,
                              CT.p + j * (long)ro * ro, ro));
     }
-    if (n_l2l > 0) {
-        convert_kernel<float><<<grid_for(n_l2l * ro * ro), 256, 0, stream>>>(CT.p, F.Yops.p, n_l2l * ro * ro);
-        TBEM_CK(cudaGetLastError());
-    }
+    store(CT.p, n_l2l * ro * ro, F.Yops, F.Yops64, 0);
     TBEM_CK(cudaStreamSynchronize(stream));
 
     // GEMM sets.  M2L: F.m2l's groups on the C_k pool.
@@ -1770,15 +1946,20 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
             if (is_p2l[c]) a.push_back({c, c});
         F.comp_p2l.add_group(0, a);
     }
-    F.m2l_c.upload(F.Cops.p, sizeof(float));
-    F.m2l_c_t.upload(F.Cops.p, sizeof(float));
-    for (auto& g : F.m2m_c) g.upload(F.Xops.p, sizeof(float));
-    for (auto& g : F.m2m_c_t) g.upload(F.Xops.p, sizeof(float));
-    for (auto& g : F.l2l_c) g.upload(F.Yops.p, sizeof(float));
-    for (auto& g : F.l2l_c_t) g.upload(F.Yops.p, sizeof(float));
-    F.comp_p2m.upload(F.Pb.p, sizeof(float));
-    F.decomp_m2p.upload(F.Wl.p, sizeof(float));
-    F.comp_p2l.upload(F.Vb.p, sizeof(float));
+    // the sets resolve their operators in the pool of the form's precision
+    const size_t es = f64 ? sizeof(double) : sizeof(float);
+    auto pool = [&](DBuf<float>& p32, DBuf<double>& p64) -> const void* {
+        return f64 ? static_cast<const void*>(p64.p) : static_cast<const void*>(p32.p);
+    };
+    F.m2l_c.upload(pool(F.Cops, F.Cops64), es);
+    F.m2l_c_t.upload(pool(F.Cops, F.Cops64), es);
+    for (auto& g : F.m2m_c) g.upload(pool(F.Xops, F.Xops64), es);
+    for (auto& g : F.m2m_c_t) g.upload(pool(F.Xops, F.Xops64), es);
+    for (auto& g : F.l2l_c) g.upload(pool(F.Yops, F.Yops64), es);
+    for (auto& g : F.l2l_c_t) g.upload(pool(F.Yops, F.Yops64), es);
+    F.comp_p2m.upload(pool(F.Pb, F.Pb64), es);
+    F.decomp_m2p.upload(pool(F.Wl, F.Wl64), es);
+    F.comp_p2l.upload(pool(F.Vb, F.Vb64), es);
     F.m2l_compressed = true;
 }
 
@@ -1817,7 +1998,14 @@ void Plan::ensure_rhs(int nrhs)
     io_y.ensure((size_t)R * N * nrhs);
     s64.ensure((size_t)R * N * nrhs);
     y64.ensure((size_t)R * N * nrhs);
-    if (f.mixed) {
+    if (f.f64) {
+        // the FP64 compressed form: check potentials, coefficients, M2P densities
+        cu64.ensure((size_t)ncs * nrhs * n);
+        if (!L.p2l.empty()) cd64.ensure((size_t)nco * nrhs * n);
+        cuc64.ensure((size_t)ncs * nrhs * f.r_in);
+        cdc64.ensure((size_t)nco * nrhs * f.r_out);
+        if (!L.m2p.empty()) qu64.ensure((size_t)ncs * nrhs * n);
+    } else if (f.mixed) {
         s32.ensure((size_t)R * N * nrhs);
         cu32.ensure((size_t)ncs * nrhs * n);
         cd32.ensure((size_t)nco * nrhs * n);
@@ -1835,8 +2023,39 @@ void Plan::ensure_rhs(int nrhs)
         qu64.ensure((size_t)ncs * nrhs * n);
         cd64.ensure((size_t)nco * nrhs * n);
         qd64.ensure((size_t)nco * nrhs * n);
+        const long slots = std::max(f.m2l_slots.max_slots, f.m2l_t_slots.max_slots);
+        if (slots > 0) slots64.ensure((size_t)slots * nrhs * n);
     }
     cap_rhs = nrhs;
+}
+
+// The precision form's L2P of `nrhs` right-hand sides from the per-leaf
+// states cd ([cell][rhs][len]): one right-hand side at a time streams the
+// leaf operators E once per right-hand side; from two on, E is read once per
+// block of L2P_NRB.
+template <typename T>
+void Plan::launch_l2p(const T* cd, int len, int nrhs, cudaStream_t s)
+{
+    Form& F = f;
+    const size_t smem = sizeof(T) * (size_t)F.E_ld * L2P_NRB;
+    const T* E;
+    if constexpr (sizeof(T) == 4) E = F.E.p; else E = F.E64.p;
+    if ((nrhs > 1 || sizeof(T) == 8) && smem <= 200 * 1024) {
+        if (smem > 48 * 1024 && smem > l2p_smem_set[sizeof(T) / 8]) {
+            TBEM_CK(cudaFuncSetAttribute(l2p_multi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+            l2p_smem_set[sizeof(T) / 8] = smem;
+        }
+        l2p_multi_kernel<T><<<F.n_l2p, L2P_MULTI_THREADS, smem, s>>>(
+            E, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cd, len, F.E_ld, R, nrhs, y64.p, n_obs);
+    } else if constexpr (sizeof(T) == 4) {
+        l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(E, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cd,
+                                                  len, F.E_ld, R, nrhs, y64.p, n_obs);
+    } else {
+        throw Error(TBEM_ERR_ARG, "translation surface too large for the FP64 L2P kernel");
+    }
+    TBEM_CK(cudaGetLastError());
+    launches++;
 }
 
 void Plan::mark(const char* name, cudaStream_t s)
@@ -1929,7 +2148,8 @@ void Plan::forward(int nrhs, cudaStream_t s)
     mark("start", s);
     TBEM_CK(cudaMemsetAsync(y64.p, 0, sizeof(double) * R * NO * nrhs, s));
     if (F.mixed && F.m2l_compressed) {
-        forward_compressed(nrhs, s);
+        if (F.f64) forward_compressed<double>(nrhs, s);
+        else forward_compressed<float>(nrhs, s);
     } else if (!F.mixed) {
         gather_kernel<double><<<grid_for(NS * R * nrhs), 256, 0, s>>>(xin, dsrc->perm.p, dsrc->w.p, s64.p, NS, R, nrhs);
         TBEM_CK(cudaGetLastError());
@@ -1952,7 +2172,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
         if (F.m2l_on_the_fly)
             eval<double>(m2l_fly, F.g_kid, true, true, O, dobs, F.r_dc, *dsrc, F.r_ue, nullptr, 0, qu64.p, nullptr, 0, cd64.p, 1, nrhs, s, false);
         else
-            F.m2l.run<double>(qu64.p, cd64.p, n, nrhs, 0, GEMM_WAVES, s, &launches);
+            F.m2l_slots.run(qu64.p, cd64.p, n, nrhs, 0, slots64.p, s, &launches);
         mark("m2l", s);
         for (int l = 0; l < O.n_levels(); l++) {
             if (l > 0 && l - 1 < (int)F.l2l.size()) F.l2l[l - 1].run<double>(qd64.p, cd64.p, n, nrhs, 0, GEMM_ADD, s, &launches);
@@ -2025,11 +2245,7 @@ void Plan::forward(int nrhs, cudaStream_t s)
             }
         }
         mark("l2l", s);
-        if (F.n_l2p > 0) {
-            l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cd32.p, n, F.E_ld, R, nrhs, y64.p, NO);
-            TBEM_CK(cudaGetLastError());
-            launches++;
-        }
+        if (F.n_l2p > 0) launch_l2p(cd32.p, n, nrhs, s);
         mark("l2p", s);
     }
     scatter_kernel<<<grid_for(NO * R * nrhs), 256, 0, s>>>(y64.p, dobs.perm.p, nullptr, yout, NO, R, nrhs);
@@ -2050,7 +2266,8 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
     // accumulated outputs (source space) before the weights
     TBEM_CK(cudaMemsetAsync(s64.p, 0, sizeof(double) * R * NS * nrhs, s));
     if (F.mixed && F.m2l_compressed) {
-        adjoint_compressed(nrhs, s);
+        if (F.f64) adjoint_compressed<double>(nrhs, s);
+        else adjoint_compressed<float>(nrhs, s);
     } else if (!F.mixed) {
         gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
         TBEM_CK(cudaGetLastError());
@@ -2069,7 +2286,7 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
         if (F.m2l_on_the_fly)
             eval<double>(m2l_fly_t, F.g_kid, true, true, S, *dsrc, F.r_ue, dobs, F.r_dc, nullptr, 0, cd64.p, nullptr, 0, qu64.p, 1, nrhs, s, true);
         else
-            F.m2l_t.run<double>(cd64.p, qu64.p, n, nrhs, 1, GEMM_WAVES, s, &launches);
+            F.m2l_t_slots.run(cd64.p, qu64.p, n, nrhs, 1, slots64.p, s, &launches);
         eval<double>(p2l_t, F.ks_kid, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd64.p, s64.p, NS, nullptr, 1, nrhs, s, true);
         // up pass reversed: root first
         for (int l = 0; l < S.n_levels(); l++) {
@@ -2084,7 +2301,7 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
         TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
         TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
         if (F.n_l2p > 0) {
-            l2p_mixed_t_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, s32.p, NO, n, F.E_ld, R, nrhs, cd32.p);
+            l2p_mixed_t_kernel<float><<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, s32.p, NO, n, F.E_ld, R, nrhs, cd32.p);
             TBEM_CK(cudaGetLastError());
             launches++;
         }
@@ -2126,8 +2343,20 @@ void Plan::adjoint(int nrhs, cudaStream_t s)
     mark("scatter", s);
 }
 
-// The compressed precision form (see build_compression): the same passes as
-// the uncompressed one with every cell state in the SVD bases.
+namespace {
+// the FP32 or the FP64 buffer of a pair
+template <typename T>
+T* pick(DBuf<float>& a, DBuf<double>& b)
+{
+    if constexpr (sizeof(T) == 4) return a.p;
+    else return b.p;
+}
+}  // namespace
+
+// The compressed forms (see build_compression): the same passes as the
+// uncompressed precision form with every cell state in the SVD bases; T =
+// float for the precision form, double for the FP64 compressed form.
+template <typename T>
 void Plan::forward_compressed(int nrhs, cudaStream_t s)
 {
     const Tree& S = *stree;
@@ -2136,61 +2365,72 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     const long ncs = (long)S.cells.size(), nco = (long)O.cells.size();
     Form& F = f;
     const int ri = F.r_in, ro = F.r_out;
-    gather_kernel<float><<<grid_for(NS * R * nrhs), 256, 0, s>>>(xin, dsrc->perm.p, dsrc->w.p, s32.p, NS, R, nrhs);
+    T* str = pick<T>(s32, s64);
+    T* cu = pick<T>(cu32, cu64);
+    T* cd = pick<T>(cd32, cd64);
+    T* cuc = pick<T>(cuc32, cuc64);
+    T* cdc = pick<T>(cdc32, cdc64);
+    gather_kernel<T><<<grid_for(NS * R * nrhs), 256, 0, s>>>(xin, dsrc->perm.p, dsrc->w.p, str, NS, R, nrhs);
     TBEM_CK(cudaGetLastError());
     launches++;
-    TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
-    TBEM_CK(cudaMemsetAsync(cdc32.p, 0, sizeof(float) * nco * nrhs * ro, s));
+    TBEM_CK(cudaMemsetAsync(cuc, 0, sizeof(T) * ncs * nrhs * ri, s));
+    TBEM_CK(cudaMemsetAsync(cdc, 0, sizeof(T) * nco * nrhs * ro, s));
     mark("gather", s);
     // the near field on the side stream, beside the far-field passes below
     TBEM_CK(cudaEventRecord(ev_fork, s));
     TBEM_CK(cudaStreamWaitEvent(side, ev_fork, 0));
-    eval<float>(p2p_set(), kid, false, false, O, dobs, 0, *dsrc, 0, s32.p, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, side, false);
+    eval<T>(p2p_set(), kid, false, false, O, dobs, 0, *dsrc, 0, str, NS, nullptr, y64.p, NO, nullptr, 1, nrhs, side, false);
     TBEM_CK(cudaEventRecord(ev_join, side));
     // P2M into the leaves' check potentials, then u~ = P_l u
-    eval<float>(p2m_set(), F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cu32.p, 0, nrhs, s, false);
-    F.comp_p2m.run_rect<float>(cu32.p, cuc32.p, ri, n, n, nrhs, 0, GEMM_ATOMIC, s, &launches);  // into zeros
+    eval<T>(p2m_set(), F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, str, NS, nullptr, nullptr, 0, cu, 0, nrhs, s, false);
+    F.comp_p2m.run_rect<T>(cu, cuc, ri, n, n, nrhs, 0, GEMM_ATOMIC, s, &launches);  // into zeros
     mark("p2m", s);
     for (int l = S.n_levels() - 1; l >= 0; l--)
-        if (l < (int)F.m2m_c.size()) F.m2m_c[l].run_rect<float>(cuc32.p, cuc32.p, ri, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
+        if (l < (int)F.m2m_c.size()) F.m2m_c[l].run_rect<T>(cuc, cuc, ri, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("m2m", s);
     if (!L.p2l.empty()) {
-        TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * nrhs * n, s));
-        eval<float>(p2l, F.ks_kid, true, false, O, dobs, F.r_dc, *dsrc, 0, s32.p, NS, nullptr, nullptr, 0, cd32.p, 1, nrhs, s, false);
-        F.comp_p2l.run_rect<float>(cd32.p, cdc32.p, ro, n, ro, nrhs, 1, GEMM_ATOMIC, s, &launches);
+        TBEM_CK(cudaMemsetAsync(cd, 0, sizeof(T) * nco * nrhs * n, s));
+        eval<T>(p2l, F.ks_kid, true, false, O, dobs, F.r_dc, *dsrc, 0, str, NS, nullptr, nullptr, 0, cd, 1, nrhs, s, false);
+        F.comp_p2l.run_rect<T>(cd, cdc, ro, n, ro, nrhs, 1, GEMM_ATOMIC, s, &launches);
     }
     mark("m2p+p2l", s);
-    if (F.use_tc_c) {
-        F.tc_c.split_b_rows(cuc32.p, 0, ncs * nrhs, std::max(ncs, nco) * nrhs, s);
-        launches++;
-        mark("m2l_split", s);
-        F.m2l_c.run_tc(F.tc_c, cdc32.p, nrhs, 1, (long)ro * ri, s, &launches);
-    } else {
-        F.m2l_c.run_rect<float>(cuc32.p, cdc32.p, ro, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
+    bool tc_done = false;
+    if constexpr (sizeof(T) == 4) {
+        if (F.use_tc_c) {
+            F.tc_c.split_b_rows(cuc, 0, ncs * nrhs, std::max(ncs, nco) * nrhs, s);
+            launches++;
+            mark("m2l_split", s);
+            F.m2l_c.run_tc(F.tc_c, cdc, nrhs, 1, (long)ro * ri, s, &launches);
+            tc_done = true;
+        }
     }
+    if (!tc_done) F.m2l_c.run_rect<T>(cuc, cdc, ro, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("m2l", s);
     for (int l = 1; l < O.n_levels(); l++)
-        if (l - 1 < (int)F.l2l_c.size()) F.l2l_c[l - 1].run_rect<float>(cdc32.p, cdc32.p, ro, ro, ro, nrhs, 0, GEMM_ATOMIC, s, &launches);
+        if (l - 1 < (int)F.l2l_c.size()) F.l2l_c[l - 1].run_rect<T>(cdc, cdc, ro, ro, ro, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("l2l", s);
     // join the near field: the passes below add into the same outputs
     TBEM_CK(cudaStreamWaitEvent(s, ev_join, 0));
     mark("p2p_wait", s);
     if (!L.m2p.empty()) {
         // equivalent densities 2^-l W u~ of the M2P sources, evaluated in FP64
-        F.decomp_m2p.run_rect<float>(cuc32.p, cu32.p, n, ri, ri, nrhs, 0, GEMM_STORE, s, &launches);
-        promote_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu32.p, qu64.p, ncs * nrhs * n);
-        TBEM_CK(cudaGetLastError());
-        launches++;
-        eval<double>(m2p, F.kt_kid, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, qu64.p, y64.p, NO, nullptr, 1, nrhs, s, false);
+        F.decomp_m2p.run_rect<T>(cuc, cu, n, ri, ri, nrhs, 0, GEMM_STORE, s, &launches);
+        const double* q64 = nullptr;
+        if constexpr (sizeof(T) == 4) {
+            promote_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(cu, qu64.p, ncs * nrhs * n);
+            TBEM_CK(cudaGetLastError());
+            launches++;
+            q64 = qu64.p;
+        } else {
+            q64 = cu;
+        }
+        eval<double>(m2p, F.kt_kid, false, true, O, dobs, 0, *dsrc, F.r_ue, nullptr, 0, q64, y64.p, NO, nullptr, 1, nrhs, s, false);
     }
-    if (F.n_l2p > 0) {
-        l2p_mixed_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, cdc32.p, ro, F.E_ld, R, nrhs, y64.p, NO);
-        TBEM_CK(cudaGetLastError());
-        launches++;
-    }
+    if (F.n_l2p > 0) launch_l2p<T>(cdc, ro, nrhs, s);
     mark("l2p", s);
 }
 
+template <typename T>
 void Plan::adjoint_compressed(int nrhs, cudaStream_t s)
 {
     const Tree& S = *stree;
@@ -2199,41 +2439,56 @@ void Plan::adjoint_compressed(int nrhs, cudaStream_t s)
     const long ncs = (long)S.cells.size(), nco = (long)O.cells.size();
     Form& F = f;
     const int ri = F.r_in, ro = F.r_out;
-    gather_kernel<float><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, s32.p, NO, R, nrhs);
+    // the observation-side input: FP32 strengths, or (FP64 form) the FP64 buffer
+    T* zin;
+    if constexpr (sizeof(T) == 4) zin = s32.p; else zin = y64.p;
+    T* cu = pick<T>(cu32, cu64);
+    T* cd = pick<T>(cd32, cd64);
+    T* cuc = pick<T>(cuc32, cuc64);
+    T* cdc = pick<T>(cdc32, cdc64);
+    const T* E;
+    if constexpr (sizeof(T) == 4) E = F.E.p; else E = F.E64.p;
+    gather_kernel<T><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, zin, NO, R, nrhs);
     TBEM_CK(cudaGetLastError());
     launches++;
-    TBEM_CK(cudaMemsetAsync(cuc32.p, 0, sizeof(float) * ncs * nrhs * ri, s));
-    TBEM_CK(cudaMemsetAsync(cdc32.p, 0, sizeof(float) * nco * nrhs * ro, s));
+    TBEM_CK(cudaMemsetAsync(cuc, 0, sizeof(T) * ncs * nrhs * ri, s));
+    TBEM_CK(cudaMemsetAsync(cdc, 0, sizeof(T) * nco * nrhs * ro, s));
     if (F.n_l2p > 0) {
-        l2p_mixed_t_kernel<<<F.n_l2p, 256, 0, s>>>(F.E.p, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, s32.p, NO, ro, F.E_ld, R, nrhs, cdc32.p);
+        l2p_mixed_t_kernel<T><<<F.n_l2p, 256, 0, s>>>(E, F.E_row0.p, F.E_leaf.p, F.E_pt0.p, F.E_npts.p, zin, NO, ro, F.E_ld, R, nrhs, cdc);
         TBEM_CK(cudaGetLastError());
         launches++;
     }
-    eval<float>(p2p_t, kid, false, false, S, *dsrc, 0, dobs, 0, s32.p, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
+    eval<T>(p2p_t, kid, false, false, S, *dsrc, 0, dobs, 0, zin, NO, nullptr, s64.p, NS, nullptr, 1, nrhs, s, true);
     for (int l = O.n_levels() - 1; l >= 1; l--)
-        if (l - 1 < (int)F.l2l_c_t.size()) F.l2l_c_t[l - 1].run_rect<float>(cdc32.p, cdc32.p, ro, ro, ro, nrhs, 1, GEMM_ATOMIC, s, &launches);
-    F.m2l_c_t.run_rect<float>(cdc32.p, cuc32.p, ri, ro, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
+        if (l - 1 < (int)F.l2l_c_t.size()) F.l2l_c_t[l - 1].run_rect<T>(cdc, cdc, ro, ro, ro, nrhs, 1, GEMM_ATOMIC, s, &launches);
+    F.m2l_c_t.run_rect<T>(cdc, cuc, ri, ro, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
     if (!L.p2l.empty()) {
-        F.comp_p2l.run_rect<float>(cdc32.p, cd32.p, n, ro, ro, nrhs, 0, GEMM_STORE, s, &launches);
-        eval<float>(p2l_t, F.ks_kid, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+        F.comp_p2l.run_rect<T>(cdc, cd, n, ro, ro, nrhs, 0, GEMM_STORE, s, &launches);
+        eval<T>(p2l_t, F.ks_kid, false, true, S, *dsrc, 0, dobs, F.r_dc, nullptr, 0, cd, s64.p, NS, nullptr, 1, nrhs, s, true);
     }
     if (!L.m2p.empty()) {
         // density gradients in FP64, folded into u~ through (2^-l W)^T
         TBEM_CK(cudaMemsetAsync(qu64.p, 0, sizeof(double) * ncs * nrhs * n, s));
-        gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
-        TBEM_CK(cudaGetLastError());
-        launches++;
+        if constexpr (sizeof(T) == 4) {
+            gather_kernel<double><<<grid_for(NO * R * nrhs), 256, 0, s>>>(xin, dobs.perm.p, nullptr, y64.p, NO, R, nrhs);
+            TBEM_CK(cudaGetLastError());
+            launches++;
+        }
         eval<double>(m2p_t, F.kt_kid, true, false, S, *dsrc, F.r_ue, dobs, 0, y64.p, NO, nullptr, nullptr, 0, qu64.p, 1, nrhs, s, true);
-        TBEM_CK(cudaMemsetAsync(cu32.p, 0, sizeof(float) * ncs * nrhs * n, s));
-        add_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(qu64.p, cu32.p, ncs * nrhs * n);
-        TBEM_CK(cudaGetLastError());
-        launches++;
-        F.decomp_m2p.run_rect<float>(cu32.p, cuc32.p, ri, n, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
+        if constexpr (sizeof(T) == 4) {
+            TBEM_CK(cudaMemsetAsync(cu, 0, sizeof(float) * ncs * nrhs * n, s));
+            add_kernel<<<grid_for(ncs * nrhs * n), 256, 0, s>>>(qu64.p, cu, ncs * nrhs * n);
+            TBEM_CK(cudaGetLastError());
+            launches++;
+            F.decomp_m2p.run_rect<float>(cu, cuc, ri, n, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
+        } else {
+            F.decomp_m2p.run_rect<double>(qu64.p, cuc, ri, n, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
+        }
     }
     for (int l = 0; l < S.n_levels(); l++)
-        if (l < (int)F.m2m_c_t.size()) F.m2m_c_t[l].run_rect<float>(cuc32.p, cuc32.p, ri, ri, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
-    F.comp_p2m.run_rect<float>(cuc32.p, cu32.p, n, ri, n, nrhs, 1, GEMM_STORE, s, &launches);
-    eval<float>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu32.p, s64.p, NS, nullptr, 1, nrhs, s, true);
+        if (l < (int)F.m2m_c_t.size()) F.m2m_c_t[l].run_rect<T>(cuc, cuc, ri, ri, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
+    F.comp_p2m.run_rect<T>(cuc, cu, n, ri, n, nrhs, 1, GEMM_STORE, s, &launches);
+    eval<T>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu, s64.p, NS, nullptr, 1, nrhs, s, true);
 }
 
 void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
@@ -2289,12 +2544,17 @@ int Plan::rhs_chunk(int nrhs) const
     const double ncs = (double)stree->cells.size(), nco = (double)otree.cells.size();
     const double N = (double)std::max(n_obs, n_src);
     double per = 8.0 * R * N * 4;  // io copies, strengths, outputs
-    if (f.mixed) {
+    if (f.f64) {
+        per += 8.0 * (ncs * n + ncs * f.r_in + nco * f.r_out);
+        if (!L.p2l.empty()) per += 8.0 * nco * n;
+        if (!L.m2p.empty()) per += 8.0 * ncs * n;
+    } else if (f.mixed) {
         per += 4.0 * (ncs + nco) * n;
         if (f.m2l_compressed) per += 4.0 * (ncs * f.r_in + nco * f.r_out) + 6.0 * std::max(ncs, nco) * 128;
         if (!L.m2p.empty() || f.m2l_on_the_fly) per += 8.0 * (2 * ncs + nco) * n;
     } else {
         per += 8.0 * 2 * (ncs + nco) * n;
+        per += 8.0 * std::max(f.m2l_slots.max_slots, f.m2l_t_slots.max_slots) * n;
     }
     return (int)std::max<double>(1.0, std::min<double>(nrhs, std::floor(RHS_WORK_BUDGET / per)));
 }

@@ -241,6 +241,28 @@ struct GemmSet {
                 long* launches);
 };
 
+// Deterministic accumulation of a GEMM set whose groups add into the same
+// outputs (the plain form's M2L: every observation cell receives one product
+// per source of its interaction list).  Every pair's product is stored in a
+// slot of its own -- one GEMM launch over all groups, [slot][rhs][m] -- and
+// each output column then sums its slots in pair order: a fixed summation
+// order with no atomics and two launches per chunk.  The pairs run in chunks
+// of at most `cap` slots, which bounds the slot buffer.
+struct SlotPlan {
+    struct Chunk {
+        GemmSet gemm;             // the chunk's groups, out_cell = local slot
+        DBuf<int> tgt, ptr, idx;  // output cells with slots, CSR of their local slots
+        int n_tgt = 0;
+    };
+    std::vector<Chunk> chunks;
+    long max_slots = 0;
+    bool empty() const { return chunks.empty(); }
+    void build(const GemmSet& G, long cap, const void* pool, size_t esz);
+    // D[out][rhs][:] += sum over the pairs of op(A_g) B[in][rhs][:]
+    void run(const double* B, double* D, int m, int nrhs, int trans, double* slots, cudaStream_t s,
+             long* launches);
+};
+
 struct DTree {
     DBuf<double> center, rad, xyz, w;
     DBuf<double> nrm64;
@@ -263,6 +285,8 @@ struct Form {
     DBuf<float> ops32;                          // mixed: combined M2M', L2L', U_k
     std::vector<GemmSet> c2e_up, m2m, l2l, c2e_dn;  // per level
     GemmSet m2l;
+    // plain form: the M2L products through slots (deterministic, no waves)
+    SlotPlan m2l_slots, m2l_t_slots;
     // transposed sets (in/out swapped) for the adjoint apply
     std::vector<GemmSet> c2e_up_t, m2m_t, l2l_t, c2e_dn_t;
     GemmSet m2l_t;
@@ -288,6 +312,10 @@ struct Form {
     bool m2l_compressed = false;
     int r_in = 0, r_out = 0;
     DBuf<float> Pb, Wl, Vb, Cops, Xops, Yops;
+    // the FP64 compressed form (TBEM_PRECISION_FP64_COMPRESSED): the same
+    // operators kept in FP64 and applied on the FP64 pipes
+    bool f64 = false;
+    DBuf<double> Pb64, Wl64, Vb64, Cops64, Xops64, Yops64, E64;
     DBuf<double> V64;  // V in FP64 (column-major n x r_out) while the L2P operators are built
     GemmSet m2l_c, m2l_c_t, comp_p2m, decomp_m2p, comp_p2l;
     std::vector<GemmSet> m2m_c, m2m_c_t, l2l_c, l2l_c_t;  // per level
@@ -341,8 +369,10 @@ struct Plan {
     DBuf<double> s64, y64;              // strengths / outputs in tree order
     DBuf<float> s32;
     DBuf<double> cu64, qu64, cd64, qd64;  // cell buffers [cell][rhs][n]
+    DBuf<double> slots64;                 // plain form: M2L product slots [slot][rhs][n]
     DBuf<float> cu32, cd32;
     DBuf<float> cuc32, cdc32;  // compressed M2L coefficients [cell][rhs][r_in | r_out]
+    DBuf<double> cuc64, cdc64;  // the same in the FP64 compressed form
     cudaStream_t stream = nullptr;
     // second stream for the near field, which runs beside the far-field
     // passes of the compressed form (forked after the gather, joined before
@@ -410,7 +440,10 @@ struct Plan {
         const std::vector<long>* l2l_off;
     };
     void build_compression(Form& F, const CompressionInput& in);
+    // T = float: the precision form; T = double: the FP64 compressed form
+    template <typename T>
     void forward_compressed(int nrhs, cudaStream_t s);
+    template <typename T>
     void adjoint_compressed(int nrhs, cudaStream_t s);
     void build_gemm_sets(Form& F, long op_base_m2m, long op_base_l2l, long op_base_m2l,
                          const std::vector<long>& m2m_off, const std::vector<long>& l2l_off,
@@ -424,6 +457,9 @@ struct Plan {
               long s_n, const T* q, double* y, long y_n, T* c, int add, int nrhs, cudaStream_t s,
               bool trans);
     void mark(const char* name, cudaStream_t s);
+    template <typename T>
+    void launch_l2p(const T* cd, int len, int nrhs, cudaStream_t s);
+    size_t l2p_smem_set[2] = {0, 0};  // dynamic shared memory opted in for the many-RHS L2P (FP32, FP64)
     // operator pool layout of the current form
     std::vector<int> m2m_key_level, l2l_key_level;
     std::vector<std::vector<int>> m2l_groups;  // pair indices per M2L key

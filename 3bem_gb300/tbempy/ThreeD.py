@@ -168,9 +168,11 @@ class OperatorI:
 class FMMOperator(OperatorI):
     """KIFMM operator (cpp/fmm.h:131-237) on the GPU.
 
-    precision: "fp64" (plain form: the reference's surfaces and formulation)
-    or "mixed" (precision form: pre-combined operators applied with FP32 /
-    tensor-core arithmetic, FP32 P2P with compensated sums).
+    precision: "fp64" (plain form: the reference's surfaces and formulation),
+    "mixed" (precision form: pre-combined operators applied with FP32 /
+    tensor-core arithmetic, FP32 P2P with compensated sums) or
+    "fp64_compressed" (the precision form's operators applied in FP64:
+    linear to rounding, the O(N) residual operator of iterative refinement).
     """
 
     def __init__(self, K, obs_locs, obs_normals, src_locs, src_normals, src_weights, config,

@@ -13,7 +13,7 @@ TBEM_OK = 0
 ERRORS = {-1: "invalid argument", -2: "CUDA failure", -3: "allocation failure",
           -4: "invalid state", -5: "device wait timed out"}
 
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "fp64_compressed": 2}
 
 
 class TbemFmmConfig(C.Structure):

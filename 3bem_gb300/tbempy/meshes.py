@@ -150,6 +150,28 @@ def sphere_batch(n_meshes=200, seed=2, levels=(2, 6), n_rhs=64):
             np.asarray(off, dtype=np.int64), x)
 
 
+def misfit_workload(n=64, n_obs=16384, seed=3):
+    """The differentiated workload's geometry and slips: an n x n-quad fault
+    dipping 45 degrees (2 n^2 triangles, 3 Gauss points each) whose vertices
+    are lifted by 0.05 sin(3x) cos(2y), ``n_obs`` observers uniform on the
+    free surface z = 0 over [-3, 3]^2 (normals +z), and two 3-component
+    slips uniform[-1, 1] (the one differentiated, and the one that makes the
+    data) and the data's noise N(0, 1e-3) per observed component, all from
+    one generator seeded ``seed``.  Returns (verts, tris, obs_locs,
+    obs_normals, s, s2, noise) with slips component-major ([3 N])."""
+    v, t, _ = dipping_fault(n, 45.0)
+    v = v.copy()
+    v[:, 2] += 0.05 * np.sin(3 * v[:, 0]) * np.cos(2 * v[:, 1])
+    rng = np.random.default_rng(seed)
+    obs = np.column_stack([rng.uniform(-3, 3, n_obs), rng.uniform(-3, 3, n_obs), np.zeros(n_obs)])
+    on = np.tile([0.0, 0.0, 1.0], (n_obs, 1))
+    n_pts = 3 * len(t)
+    s = rng.uniform(-1, 1, 3 * n_pts)
+    s2 = rng.uniform(-1, 1, 3 * n_pts)
+    noise = rng.normal(0.0, 1e-3, 3 * n_obs)
+    return v, t, obs, on, s, s2, noise
+
+
 def fault_points(n=128, dip_deg=45.0):
     """Dipping-fault points (98,304 at n=128) plus each point's (u, v)."""
     v, t, uv = dipping_fault(n, dip_deg)

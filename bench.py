@@ -168,6 +168,20 @@ def cpu_apply_seconds(ops, x, fraction):
     return total
 
 
+def cpu_calibration(ops, x, fraction):
+    """One FULL oracle apply of the first operator (the displacement kernel)
+    against its sampled, extrapolated time: the ratio full / sampled that
+    corrects the extrapolation of every sampled step."""
+    t0 = time.perf_counter()
+    ops[0].apply(x, list_fraction=fraction)
+    sampled = (time.perf_counter() - t0) / fraction
+    t0 = time.perf_counter()
+    ops[0].apply(x)
+    full = time.perf_counter() - t0
+    return {"full_apply_s": full, "sampled_extrapolated_s": sampled, "ratio": full / sampled,
+            "operator": "ElasticDisplacement", "fraction": fraction}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference algorithm on the host cores (the oracle
     port; the reference's own build needs its checkout, absent on the GPU machine)."""
@@ -178,9 +192,10 @@ def run_reference(args, rank, world):
     frac = args.cpu_fraction
     # built once, like the operator of the GPU arm; each step is one apply
     ops, setup, cores = cpu_operators(locs, nrm, w, threads)
+    calib = cpu_calibration(ops, x, frac)
     samples = []
     for i in range(args.warmup + args.steps):
-        t_full = cpu_apply_seconds(ops, x, frac)
+        t_full = cpu_apply_seconds(ops, x, frac) * calib["ratio"]
         if i >= args.warmup:
             samples.append(t_full)
     t = float(np.median(samples))
@@ -193,7 +208,9 @@ def run_reference(args, rank, world):
         "config": config_dict(1),
         "cpu_baseline": {"value": value, "unit": "points*RHS/s", "cores": cores, "kind": "port",
                          "sample": "leading %.3g of every FMM task list per step, both kernels, "
-                                   "extrapolated to a full apply" % frac},
+                                   "extrapolated to a full apply and scaled by the measured "
+                                   "full / sampled ratio of one full displacement apply" % frac,
+                         "calibration": calib},
         "e2e": {"value": value, "unit": "points*RHS/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "setup_s": setup,
@@ -571,6 +588,103 @@ def run_batched(args, rank, world, local):
         }), flush=True)
 
 
+def misfit_config():
+    return {"workload": "differentiated misfit L = 0.5 ||G s - d||^2, elastic displacement, "
+                        "64 x 64-quad bumpy fault (24,576 points) -> 16,384 observers on z = 0",
+            "kernel": "ElasticDisplacement", "n_src": 24576, "n_obs": 16384, "n_rhs": 1,
+            "fmm": {"order_requested": ORDER, "surface_points": 295, "mac": MAC,
+                    "min_pts_per_cell": LEAF, "d": D, "account_for_small_cells": False},
+            "step": "one gradient dL/ds: a forward apply and a transposed apply (value counts "
+                    "the observation points of the forward apply)",
+            "precision": "mixed (M2L between the two trees evaluated on the fly in FP64)",
+            "l2": "flushed before every timed step (256 MB write, outside the step timing)"}
+
+
+def run_misfit(args, rank, world, local):
+    from tbempy import meshes
+    v, t, obs, on, s_np, s2_np, noise = meshes.misfit_workload()
+    sl, sn, sw = meshes.points_from_mesh(v, t)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import oracle
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        oracle.build()
+        o = oracle.OracleFMM("ElasticDisplacement", obs, on, sl, sn, sw, MAC, ORDER, LEAF, D)
+        frac = args.cpu_fraction * 10
+        ts = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            o.apply(s_np, list_fraction=frac)
+            if i >= args.warmup:
+                ts.append((time.perf_counter() - t0) / frac)
+        tt = float(np.median(ts))
+        value = len(obs) / tt
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "points*RHS/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tt,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded bumpy fault)", "config": misfit_config(),
+            "cpu_baseline": {"value": value, "unit": "points*RHS/s", "cores": oracle.max_threads(),
+                             "kind": "port", "sample": "forward oracle apply on the leading %.2g of "
+                                                       "every task list, extrapolated (the reference "
+                                                       "has no transposed apply)" % frac},
+            "e2e": {"value": value, "unit": "points*RHS/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    from tbempy import ThreeD, autograd
+    K = ThreeD.ElasticDisplacement(MU, NU)
+    Dop = ThreeD.DirectOperator(K, obs, on, sl, sn, sw)
+    d = torch.tensor(Dop.apply(s2_np) + noise, device="cuda")
+    s = torch.tensor(s_np, device="cuda")
+    t0 = time.perf_counter()
+    op = ThreeD.FMMOperator(K, obs, on, sl, sn, sw, ThreeD.FMMConfig(MAC, ORDER, LEAF, D, False),
+                            precision="mixed", device=local)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+
+    def grad_step():
+        r = op.apply(s) - d
+        return op.apply_adjoint(r)
+
+    for _ in range(args.warmup):
+        grad_step()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = _events_ms(torch, grad_step, args.steps, stream, flush)
+        ms_fwd = _events_ms(torch, lambda: op.apply(s), args.steps, stream, flush)
+    phases = _phases(op, lambda: op.apply(s))
+    # the vertex-coordinate gradient (kernel-gradient pass of the direct operator)
+    V = torch.tensor(v, device="cuda", requires_grad=True)
+    OL, ON = torch.tensor(obs, device="cuda"), torch.tensor(on, device="cuda")
+
+    def vertex_grad():
+        V.grad = None
+        a, b, c = meshes.points_from_mesh_torch(V, t)
+        y = autograd.direct_apply(K, OL, ON, a, b, c, s)
+        (0.5 * ((y - d) ** 2).sum()).backward()
+
+    vertex_grad()
+    ms_vert = _events_ms(torch, vertex_grad, 2, stream)
+    g = grad_step().cpu().numpy()
+    r = Dop.apply(s_np) - d.cpu().numpy()
+    gd = ThreeD.direct_gradients(K, obs, on, sl, sn, sw, s_np, r)["x"]
+    err = float(np.linalg.norm(g - gd) / np.linalg.norm(gd))
+    y = op.apply(s_np)
+    err_f = float(np.linalg.norm(y - Dop.apply(s_np)) / np.linalg.norm(Dop.apply(s_np)))
+    print(json.dumps({
+        "metric": METRIC, "value": len(obs) / (ms / 1e3), "unit": "points*RHS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded bumpy fault, free-surface observers)", "config": misfit_config(),
+        "clocks": clk.summary(), "gpu_launches": 2 * op.last_launches() * args.steps,
+        "forward_ms": ms_fwd, "vertex_gradient_ms": ms_vert, "phases_ms_forward": phases,
+        "rel_err_vs_direct": {"forward": err_f, "gradient_ds": err}, "setup_s": setup_s}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -588,10 +702,11 @@ def main():
                     help="0 auto, 1 SIMT FP32, 2 tcgen05 M2L, 3 tcgen05 all, 4 compressed M2L")
     ap.add_argument("--m2l-rank-tol", type=float, default=1e-7,
                     help="singular-value cut of the compressed M2L")
-    ap.add_argument("--workload", default="fault", choices=["fault", "sphere", "batched"],
+    ap.add_argument("--workload", default="fault", choices=["fault", "sphere", "batched", "misfit"],
                     help="fault: the elastic fault (default); sphere: plain FP64 Laplace single "
                          "layer on the 15,360-point icosphere; batched: Laplace double layer on "
-                         "200 icospheres x 64 right-hand sides in one operator")
+                         "200 icospheres x 64 right-hand sides in one operator; misfit: the "
+                         "gradient of the elastic misfit on the 64 x 64 bumpy fault")
     ap.add_argument("--meshes", type=int, default=200, help="batched workload: meshes")
     ap.add_argument("--batch-rhs", type=int, default=64, help="batched workload: right-hand sides")
     args = ap.parse_args()
@@ -600,7 +715,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
     if args.workload != "fault":
-        (run_sphere if args.workload == "sphere" else run_batched)(args, rank, world, local)
+        {"sphere": run_sphere, "batched": run_batched, "misfit": run_misfit}[args.workload](
+            args, rank, world, local)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
@@ -753,12 +869,15 @@ def main():
     if not args.no_cpu and rank == 0:
         threads = os.cpu_count() or 1
         cops, _, cores = cpu_operators(locs, nrm, w, threads)
-        t_full = cpu_apply_seconds(cops, x, args.cpu_fraction)
+        calib = cpu_calibration(cops, x, args.cpu_fraction)
+        t_full = cpu_apply_seconds(cops, x, args.cpu_fraction) * calib["ratio"]
         del cops
         cpu = {"value": 2 * N / t_full, "unit": "points*RHS/s", "cores": cores, "kind": "port",
                "sample": "oracle FMM apply of both kernels on the leading %.3g of every task "
-                         "list, extrapolated to a full apply (%.1f s measured)"
-                         % (args.cpu_fraction, t_full * args.cpu_fraction)}
+                         "list, extrapolated to a full apply and scaled by the full / sampled "
+                         "ratio of one full displacement apply (%.1f s)"
+                         % (args.cpu_fraction, calib["full_apply_s"]),
+               "calibration": calib}
 
     if rank == 0:
         line = {

@@ -62,6 +62,14 @@ extern "C" {
 /* precision forms */
 #define TBEM_PRECISION_FP64 0   /* plain: reference surfaces and formulation, FP64 */
 #define TBEM_PRECISION_MIXED 1  /* precision form: tensor-core M2L/M2M/L2L, FP32 P2P */
+/* The precision form's operators (enclosing surfaces, single-layer
+ * equivalent sources, the far field in the M2L SVD bases) applied in FP64 on
+ * the SIMT FP64 pipes: the precision form's accuracy against the direct sum
+ * (~1e-7 at the workload orders), but linear to FP64 rounding (its states
+ * are well-conditioned check potentials, never the plain form's cancelling
+ * equivalent densities) -- the O(N) FP64 residual operator of iterative
+ * refinement.  3D kernels; the M2L operators must compress. */
+#define TBEM_PRECISION_FP64_COMPRESSED 2
 
 /* FMMConfig, cpp/fmm.h:73-96 (same five fields and meaning; `order` is the
  * requested number of translation-surface points, cpp/fmm.h:76-82). */
@@ -80,7 +88,10 @@ typedef struct {
     double svd_threshold;  /* singular-value cutoff (reference: 1e-10, fmm.cpp:122) */
     int m2l_path;          /* precision form's dense translations:
                               0 auto (= 5 where the M2L operators are precomputed
-                                and compress; SIMT FP32 otherwise),
+                                and compress, = 2 where they are precomputed but
+                                the compressed products, padded to the tensor-core
+                                tiles, would not be cheaper; SIMT FP32 when the
+                                M2L runs on the fly),
                               1 SIMT FP32 for all (uncompressed M2L),
                               2 tcgen05 3xBF16 for the uncompressed M2L only,
                               3 tcgen05 3xBF16 for M2L, M2M and L2L,

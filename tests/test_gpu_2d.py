@@ -6,7 +6,9 @@ Tolerances (written here, checked below):
   * plain FP64 FMM with the reference's own check-to-equivalent operators
     installed vs the reference's apply (fixtures) or the oracle: 1e-10
     relative L2, or -- for the 2D operators -- 100 x the case's conditioning
-    floor when that is larger.  The floor is measured on the CPU: the
+    floor when that is larger (10 x the floor stored with a 3D fixture at a
+    high order: the 152-point icosphere case, floor 2.7e-8).  The floor is
+    measured on the CPU: the
     relative change of the oracle's own apply when its check-to-equivalent
     systems are perturbed by one ulp (OracleFMM.ulp_floor).  The reference
     algorithm keeps singular values down to 1e-10 of the largest, and with
@@ -80,6 +82,13 @@ def test_plain_form_reproduces_reference_fixture(path):
         for lev, m in enumerate(ops):
             op.set_c2e(which, lev, m)
     tol = 1e-10
+    if "ulp_floor" in g:
+        # 3D at a high order (the 15,360-point icosphere at 152 surface
+        # points): the reference's own one-ulp floor is above 1e-10 (2.7e-8),
+        # so two correct FP64 evaluations of its algorithm -- even with the
+        # same pseudo-inverses -- differ by a fraction of that floor (measured
+        # on GB300: 0.35 floors); the bar is 10 floors there
+        tol = max(1e-10, 10 * float(g["ulp_floor"]))
     if dim == 2:
         orc = oracle.OracleFMM(str(g["kernel"]), g["obs_locs"], g["obs_normals"], g["src_locs"],
                                g["src_normals"], g["src_weights"], float(g["mac"]),

@@ -6,7 +6,7 @@ Tolerances (written here, checked below):
     1e-10 relative L2 (the reference's own FMM is the target; the operators
     are injected so that only the apply is compared);
   * plain FP64 form with its own cuSOLVER operators vs the reference's
-    fixtures: max(1e-10, 100 x the reference's one-ulp conditioning floor of
+    fixtures: max(1e-10, 10 x the reference's one-ulp conditioning floor of
     each case);
   * precision form vs FP64 direct sum at the workload orders: 2e-6.
 """
@@ -117,7 +117,7 @@ def test_plain_own_operators_within_reference_floor(path):
     conditioning floor -- how far its result moves when every
     check-to-equivalent system is perturbed by one ulp before its
     pseudo-inverse (measured on the CPU, or stored with the fixture) -- at
-    max(1e-10, 100 floors), as for the 2D operators."""
+    max(1e-10, 10 floors) (measured on GB300: 0.6 to 1.5 floors)."""
     from tbempy import ThreeD
     g = dict(np.load(path))
     cfg = ThreeD.FMMConfig(float(g["mac"]), int(g["order"]), int(g["leaf"]), float(g["d"]),
@@ -134,7 +134,7 @@ def test_plain_own_operators_within_reference_floor(path):
         floor = orc.ulp_floor(g["x"])
     err = rel(y, g["y_ref"])
     print("own operators: %.3g of the reference's apply, floor %.3g" % (err, floor))
-    assert err <= max(1e-10, 100 * floor), "%.3g vs floor %.3g" % (err, floor)
+    assert err <= max(1e-10, 10 * floor), "%.3g vs floor %.3g" % (err, floor)
 
 
 def test_distinct_trees_plain():

@@ -73,6 +73,56 @@ def test_plain_fmm_linearity_floor():
     assert np.array_equal(op.apply(x1), y1)
 
 
+@pytest.mark.parametrize("name,order", [("LaplaceSingle", 152), ("LaplaceDouble", 296),
+                                        ("ElasticTraction", 296)])
+def test_fp64_compressed_form_is_linear_and_accurate(name, order):
+    """The FP64 compressed form (the precision form's operators applied in
+    FP64): against the FP64 direct sum at the precision form's bound (2e-6);
+    linear to rounding, A(x1 + x2) = A x1 + A x2 to 1e-13 (the plain form's
+    floor is ~1e-9); its transpose satisfies <A x, z> = <x, A^T z> to 1e-13;
+    and the FP32 precision form agrees with it to 2e-6."""
+    from tbempy import ThreeD, meshes
+    locs, nrm, w = meshes.sphere_points(3)
+    K = getattr(ThreeD, name)(1.0, 0.25) if name.startswith("Elastic") else getattr(ThreeD, name)()
+    cfg = ThreeD.FMMConfig(0.3, order, 40, 0.05, False)
+    op = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="fp64_compressed")
+    rng = np.random.default_rng(6)
+    x1, x2 = rng.uniform(-1, 1, (2, op.n_cols()))
+    y1, y2, y12 = op.apply(x1), op.apply(x2), op.apply(x1 + x2)
+    assert np.linalg.norm(y12 - y1 - y2) <= 1e-13 * np.linalg.norm(y12)
+    exact = ThreeD.DirectOperator(K, locs, nrm, locs, nrm, w).apply(x1)
+    assert np.linalg.norm(y1 - exact) <= 2e-6 * np.linalg.norm(exact)
+    z = rng.uniform(-1, 1, op.n_rows())
+    lhs, rhs = float(y1 @ z), float(x1 @ op.apply_adjoint(z))
+    assert abs(lhs - rhs) <= 1e-13 * np.linalg.norm(y1) * np.linalg.norm(z)
+    mixed = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed")
+    assert np.linalg.norm(mixed.apply(x1) - y1) <= 2e-6 * np.linalg.norm(y1)
+    X = np.stack([x1, x2, x1 - x2])
+    assert np.linalg.norm(op.apply(X)[2] - (y1 - y2)) <= 1e-13 * np.linalg.norm(y1 - y2)
+
+
+def test_refined_gmres_with_an_fmm_fp64_residual():
+    """The refinement's FP64 residual through the FP64 compressed form -- an
+    O(N) operator linear to rounding -- instead of the O(N^2) direct sum: the
+    refined solve (inner GMRES on the FP32 / tensor-core precision form)
+    reaches 1e-10 against that operator, and the solution satisfies the
+    direct operator's system to the FMM's own accuracy."""
+    from tbempy import ThreeD, meshes, solve
+    locs, nrm, w = meshes.sphere_points(3)
+    cfg = ThreeD.FMMConfig(0.3, 152, 40, 0.05, False)
+    K = ThreeD.LaplaceDouble()
+    f64 = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="fp64_compressed")
+    fast = ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision="mixed")
+    A64 = lambda v: 0.5 * v + f64.apply(v)
+    A32 = lambda v: 0.5 * v + fast.apply(v)
+    f = 1.0 / np.linalg.norm(locs - np.array([0.1, 0.2, 0.3]), axis=1)
+    x, hist = solve.refined_solve(A64, A32, f, tol=1e-10, inner_tol=1e-6)
+    assert hist[-1][2] <= 1e-10, hist
+    assert np.linalg.norm(A64(x) - f) <= 1e-10 * np.linalg.norm(f)
+    direct = ThreeD.DirectOperator(K, locs, nrm, locs, nrm, w)
+    assert np.linalg.norm(0.5 * x + direct.apply(x) - f) <= 1e-5 * np.linalg.norm(f)
+
+
 def test_refined_gmres_reaches_fp64_residual():
     """Second-kind Laplace system (0.5 I + D) sigma = f on a sphere: the inner
     GMRES runs on the precision-form FMM, the FP64 residual uses the GPU FP64
@@ -177,3 +227,73 @@ def test_vertex_gradients_match_central_differences(name):
             fd = (loss(torch.tensor(vp.reshape(v.shape), device=dev)) -
                   loss(torch.tensor(vm.reshape(v.shape), device=dev))).item() / (2 * h)
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, np.abs(g).max()), (k, fd, g[k])
+
+
+def test_misfit_workload_at_size():
+    """The differentiated workload at its stated size: a 64 x 64-quad bumpy
+    fault (8,192 triangles, 24,576 points), 16,384 observers on z = 0,
+    L = 0.5 ||G s - d||^2 with the elastic displacement kernel and
+    d = G s2 + N(0, 1e-3).
+
+    * dL/ds through the precision-form FMM and its transposed apply (torch
+      autograd) against the FP64 direct operator's transpose,
+      G^T (G s - d) (the kernel-gradient pass's dL/dx): 2e-6 relative L2
+      (the FMM's own error against the direct sum);
+    * the same gradient against FP64 central differences (h = 1e-6) of the
+      direct loss on 64 random slip coordinates: 2e-6 of the largest entry;
+    * dL/d(vertex coordinates) through the kernel-gradient pass against FP64
+      central differences (h = 1e-6) on 64 random coordinates: 1e-6 of the
+      largest entry."""
+    torch = pytest.importorskip("torch")
+    from tbempy import ThreeD, autograd, meshes
+    v, t, obs, on, s_np, s2_np, noise = meshes.misfit_workload()
+    assert len(t) == 8192 and len(obs) == 16384
+    K = ThreeD.ElasticDisplacement(1.0, 0.25)
+    dev = "cuda"
+    sl, sn, sw = meshes.points_from_mesh(v, t)
+    assert len(sl) == 24576
+    D = ThreeD.DirectOperator(K, obs, on, sl, sn, sw)
+    d = torch.tensor(D.apply(s2_np) + noise, device=dev)
+    s = torch.tensor(s_np, device=dev)
+    op = ThreeD.FMMOperator(K, obs, on, sl, sn, sw, ThreeD.FMMConfig(0.3, 296, 64, 0.05, False),
+                            precision="mixed")
+    sg = s.clone().requires_grad_(True)
+    autograd.misfit(op, sg, d).backward()
+    g = sg.grad.cpu().numpy()
+    r = D.apply(s_np) - d.cpu().numpy()
+    gd = ThreeD.direct_gradients(K, obs, on, sl, sn, sw, s_np, r)["x"]
+    gd = np.asarray(gd.cpu() if hasattr(gd, "cpu") else gd).ravel()
+    assert np.linalg.norm(g - gd) <= 2e-6 * np.linalg.norm(gd), np.linalg.norm(g - gd) / np.linalg.norm(gd)
+    rng = np.random.default_rng(31)
+    h = 1e-6
+
+    def direct_loss(x):
+        y = D.apply(x) - d.cpu().numpy()
+        return 0.5 * float(y @ y)
+
+    for j in rng.choice(len(s_np), 64, replace=False):
+        e = np.zeros_like(s_np)
+        e[j] = h
+        fd = (direct_loss(s_np + e) - direct_loss(s_np - e)) / (2 * h)
+        assert abs(fd - g[j]) <= 2e-6 * np.abs(gd).max(), (j, fd, g[j])
+    # vertex coordinates through the kernel-gradient pass
+    V = torch.tensor(v, device=dev, requires_grad=True)
+    OL = torch.tensor(obs, device=dev)
+    ON = torch.tensor(on, device=dev)
+
+    def loss(Vt):
+        a, b, c = meshes.points_from_mesh_torch(Vt, t)
+        y = autograd.direct_apply(K, OL, ON, a, b, c, s)
+        return 0.5 * ((y - d) ** 2).sum()
+
+    loss(V).backward()
+    gv = V.grad.cpu().numpy().ravel()
+    flat = v.ravel()
+    for k in rng.choice(flat.size, 64, replace=False):
+        vp, vm = flat.copy(), flat.copy()
+        vp[k] += h
+        vm[k] -= h
+        with torch.no_grad():
+            fd = (loss(torch.tensor(vp.reshape(v.shape), device=dev)) -
+                  loss(torch.tensor(vm.reshape(v.shape), device=dev))).item() / (2 * h)
+        assert abs(fd - gv[k]) <= 1e-6 * max(1.0, np.abs(gv).max()), (k, fd, gv[k])
