@@ -64,8 +64,12 @@ struct GemmK {
     static constexpr int BK = sizeof(T) == 4 ? 16 : 8;
 };
 
+// One output tile (column tile `tile`, row tile `mtile`, K split `kz`) of a
+// grouped GEMM: the body of grouped_gemm_kernel, shared with the persistent
+// level chain (chain_gemm_kernel).  Ends after a barrier that follows the
+// last shared-memory read, so a CTA can run the next tile right away.
 template <typename T, int BM>
-__global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs<T> a)
+__device__ __forceinline__ void gemm_tile(const GemmArgs<T>& a, int tile, int mtile, int kz)
 {
     constexpr int BN = GM_BN, BK = GemmK<T>::BK;
     constexpr int TM = BM / 16, TN = BN / 16;  // outputs per thread (rows x columns)
@@ -76,10 +80,9 @@ __global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs
     __shared__ __align__(16) T As[2][BK][PA];
     __shared__ __align__(16) T Bs[2][BK][PB];
 
-    const int tile = blockIdx.x;
     const int g = a.tile_group[tile];
     const int col0 = a.tile_col0[tile];
-    const int m0 = blockIdx.y * BM;
+    const int m0 = mtile * BM;
     if (m0 >= a.m) return;
     const T* __restrict__ A = a.A[g];
     const long pair0 = a.g_pair0[g];
@@ -118,7 +121,7 @@ __global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs
 
     T ra[NA], rb[NB];
     // this CTA's K range (split K: the partial products meet in GEMM_ATOMIC)
-    const int kb = blockIdx.z * a.kchunk;
+    const int kb = kz * a.kchunk;
     const int kend = min(K, kb + a.kchunk);
     auto load = [&](int k0) {
 #pragma unroll
@@ -131,7 +134,8 @@ __global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs
 #pragma unroll
         for (int i = 0; i < NB; i++) {
             const int gk = k0 + bk[i];
-            rb[i] = (bcol[i] && gk < kend) ? bcol[i][gk] : T(0);
+            // (through L2: in a level chain the states were just written by other SMs)
+            rb[i] = (bcol[i] && gk < kend) ? __ldcg(&bcol[i][gk]) : T(0);
         }
     };
     auto store = [&](int buf) {
@@ -206,6 +210,78 @@ __global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs
             if (a.mode == GEMM_STORE) dcol[gm] = acc[i][j];
             else if (a.mode == GEMM_ADD) dcol[gm] += acc[i][j];
             else atomic_add_t<T>(&dcol[gm], acc[i][j]);
+        }
+    }
+}
+
+template <typename T, int BM>
+__global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs<T> a)
+{
+    gemm_tile<T, BM>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// A chain of grouped GEMMs that must run one after the other (the levels of
+// the upward M2M pass, deepest first, or of the downward L2L pass) in one
+// persistent launch.  Every GEMM's launch grid becomes a range of work items
+// (column tile x row tile x K split); CTAs take items in order from a ticket
+// counter, and an item of link li starts once every item of link li - 1 has
+// finished (a per-link completion counter).  A CTA only ever waits for items
+// with smaller tickets, which CTAs already running hold, so the chain cannot
+// deadlock whatever the number of resident CTAs; the waits are bounded all
+// the same (a wait that runs out raises `err` and the CTA carries on).
+constexpr int CHAIN_MAX_LINKS = 64;
+
+template <typename T>
+struct ChainLink {
+    GemmArgs<T> a;
+    int n_tiles, m_tiles, splits;  // the GEMM's grid
+    int item0, n_items;            // its items in the chain
+};
+
+struct ChainSync {
+    int ticket;
+    int err;
+    int done[CHAIN_MAX_LINKS];
+};
+
+template <typename T, int BM>
+__global__ void __launch_bounds__(GM_THREADS) chain_gemm_kernel(const ChainLink<T>* links, int n_links,
+                                                               int total, ChainSync* sync,
+                                                               long long wait_cycles)
+{
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&sync->ticket, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= total) return;
+        int li = 0;
+        while (li + 1 < n_links && item >= links[li + 1].item0) li++;
+        const ChainLink<T>& L = links[li];
+        if (li > 0 && threadIdx.x == 0) {
+            const int need = links[li - 1].n_items;
+            volatile int* done = &sync->done[li - 1];
+            const long long t0 = clock64();
+            while (*done < need) {
+                if (clock64() - t0 > wait_cycles) {
+                    atomicExch(&sync->err, 1);
+                    break;
+                }
+                __nanosleep(128);
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        const int local = item - L.item0;
+        const int tile = local % L.n_tiles;
+        const int mtile = (local / L.n_tiles) % L.m_tiles;
+        const int kz = local / (L.n_tiles * L.m_tiles);
+        gemm_tile<T, BM>(L.a, tile, mtile, kz);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(&sync->done[li], 1);
         }
     }
 }

@@ -113,8 +113,8 @@ void graph_delete(TbemGraph* g) { delete g; }
 void graph_launch(TbemGraph& g, cudaStream_t s)
 {
     for (TbemFmm* op : g.ops) {
-        const int* e = op->plan.h_err;
-        if (e && (e[0] || e[1])) throw Error(TBEM_ERR_TIMEOUT, "a tensor-core GEMM gave up waiting on its MMAs");
+        if (op->plan.flags_raised())
+            throw Error(TBEM_ERR_TIMEOUT, "a bounded device wait of an earlier replay gave up");
     }
     DeviceGuard guard(g.device);
     TBEM_CK(cudaGraphLaunch(g.exec, s ? s : g.cap));

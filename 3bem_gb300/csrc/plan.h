@@ -8,6 +8,7 @@
 
 #include <map>
 #include <memory>
+#include <tuple>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -227,7 +228,11 @@ struct GemmSet {
     // op(A) is m x k; A is stored row-major with rows of length lda
     template <typename T>
     void run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int trans, int mode,
-                  cudaStream_t s, long* launches = nullptr);
+                  cudaStream_t s, long* launches = nullptr, bool tables_only = false);
+    // the set as one link of a level chain (gemm.cuh: chain_gemm_kernel)
+    template <typename T>
+    ChainLink<T> chain_link(const T* B, T* D, int m, int k, int lda, int nrhs, int trans, int mode,
+                            int sms);
     // tensor-core path (B taken from P's split planes; D columns of P.m rows);
     // nn = elements per operator in the pool the groups' offsets refer to
     struct TcTiles {
@@ -381,10 +386,14 @@ struct Plan {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t solver = nullptr;
-    // tensor-core timeout flags copied to pinned memory after every apply;
-    // an apply with device outputs reports a flag raised by the previous one
+    // timeout flags of the bounded device waits (tensor-core GEMMs, level
+    // chains) copied to pinned memory after every apply; an apply with device
+    // outputs reports a flag raised by the previous one
+    static constexpr int N_ERR_FLAGS = 4;
     int* h_err = nullptr;
     void check_tc_flags(bool wait_device, cudaStream_t s);
+    std::vector<const int*> device_flags() const;
+    bool flags_raised() const;
     // waits for the plan's work (and stream s) and throws TBEM_ERR_TIMEOUT
     // if a tensor-core pass of any earlier apply gave up
     void sync(cudaStream_t s);
@@ -457,6 +466,22 @@ struct Plan {
               long s_n, const T* q, double* y, long y_n, T* c, int add, int nrhs, cudaStream_t s,
               bool trans);
     void mark(const char* name, cudaStream_t s);
+    // the compressed form's upward and downward level passes as persistent
+    // level chains (chain 0: M2M deepest level first, chain 1: L2L): the
+    // device copies of their links per (chain, right-hand sides), and the
+    // completion counters of each chain
+    struct ChainCache {
+        DBuf<char> links;
+        int n_links = 0, total = 0, bm = 128;
+    };
+    // keyed by (chain and type, right-hand sides, state buffer); cleared
+    // whenever the state buffers are reallocated
+    std::map<std::tuple<int, int, const void*>, ChainCache> chains;
+    DBuf<ChainSync> chain_sync;  // [2]
+    bool use_chains = true;
+    template <typename T>
+    void run_chain(int id, const std::vector<GemmSet*>& sets, const T* B, T* D, int m, int nrhs,
+                   cudaStream_t s);
     template <typename T>
     void launch_l2p(const T* cd, int len, int nrhs, cudaStream_t s);
     size_t l2p_smem_set[2] = {0, 0};  // dynamic shared memory opted in for the many-RHS L2P (FP32, FP64)

@@ -119,6 +119,66 @@ def sphere_points(n_subdiv=4):
     return points_from_mesh(v, t)
 
 
+def real_sph_harm(lmax, theta, phi):
+    """Real orthonormal spherical harmonics Y_lm(theta, phi) for 0 <= l <= lmax,
+    -l <= m <= l (theta the polar angle): a dict {(l, m): values}.  The
+    associated Legendre functions come from the standard three-term
+    recurrences (P_m^m, P_{m+1}^m, then upward in l), normalised so that
+    the Y_lm are orthonormal on the unit sphere."""
+    from math import factorial
+    x = np.cos(theta)
+    s = np.sqrt(np.maximum(0.0, 1.0 - x * x))
+    P = {}
+    pmm = np.ones_like(x)
+    for m in range(lmax + 1):
+        if m > 0:
+            pmm = -(2 * m - 1) * s * pmm
+        P[(m, m)] = pmm
+        if m + 1 <= lmax:
+            P[(m + 1, m)] = x * (2 * m + 1) * pmm
+        for l in range(m + 2, lmax + 1):
+            P[(l, m)] = ((2 * l - 1) * x * P[(l - 1, m)] - (l + m - 1) * P[(l - 2, m)]) / (l - m)
+    Y = {}
+    for l in range(lmax + 1):
+        for m in range(-l, l + 1):
+            am = abs(m)
+            norm = np.sqrt((2 * l + 1) / (4 * np.pi) * factorial(l - am) / factorial(l + am))
+            if m == 0:
+                Y[(l, m)] = norm * P[(l, 0)]
+            elif m > 0:
+                Y[(l, m)] = np.sqrt(2.0) * norm * P[(l, am)] * np.cos(am * phi)
+            else:
+                Y[(l, m)] = np.sqrt(2.0) * norm * P[(l, am)] * np.sin(am * phi)
+    return Y
+
+
+def bumpy_sphere(n_subdiv=8, seed=4, amplitude=0.1, lmax=8):
+    """The full-solve workload's surface: an icosphere subdivided ``n_subdiv``
+    times (20 4^n triangles; 1,310,720 at 8) whose vertices are moved to
+    r = 1 + amplitude Y(theta, phi), Y = sum over 1 <= l <= lmax, |m| <= l of
+    c_lm Y_lm with c_lm ~ N(0, 1 / l^2) (real orthonormal harmonics) drawn
+    from a generator seeded ``seed``.  Returns (verts, tris)."""
+    v, t = icosphere(n_subdiv)
+    rng = np.random.default_rng(seed)
+    theta = np.arccos(np.clip(v[:, 2], -1.0, 1.0))
+    phi = np.arctan2(v[:, 1], v[:, 0])
+    Y = real_sph_harm(lmax, theta, phi)
+    bump = np.zeros(len(v))
+    for l in range(1, lmax + 1):
+        for m in range(-l, l + 1):
+            bump += rng.normal(0.0, 1.0 / l) * Y[(l, m)]
+    return v * (1.0 + amplitude * bump)[:, None], t
+
+
+def interior_charges(n=10, seed=4, radius=0.3):
+    """``n`` unit point charges uniform in the ball of ``radius`` about the
+    origin (inside the bumpy sphere), from a generator seeded ``seed`` + 1."""
+    rng = np.random.default_rng(seed + 1)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    return d * (radius * rng.uniform(0, 1, n) ** (1.0 / 3.0))[:, None]
+
+
 _SPHERE_CACHE = {}
 
 

@@ -106,6 +106,22 @@ def refined_solve(apply_fp64, apply_fast, b, tol=1e-10, inner_tol=1e-6, restart=
     return x, history
 
 
+def exterior_dirichlet_system(single, double):
+    """The exterior Laplace Dirichlet problem as a second-kind system.
+
+    The field outside a closed surface is represented by a combined layer,
+    u = D_std mu + S mu (D_std the standard double layer, with kernel
+    dG/dn_y, G = 1 / (4 pi r)); its exterior limit on the surface gives
+    (1/2 I + K + S) mu = g, uniquely solvable for every Dirichlet datum g
+    (the single layer carries the field's monopole, which a double layer
+    cannot).  The library's LaplaceDouble kernel is n_y . (y - x) / (4 pi r^3)
+    = -dG/dn_y, so with its operators D and S the system reads
+    (1/2 I - D + S) mu = g, and the field u = -D mu + S mu.  single, double:
+    callables applying S and D (any precision form).  Returns the system's
+    apply."""
+    return lambda v: 0.5 * v - double(v) + single(v)
+
+
 def ilu_preconditioner(nearfield, drop_tol=1e-4, fill_factor=10.0):
     """Incomplete LU of a nearfield matrix as an approximate inverse.
 

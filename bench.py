@@ -685,6 +685,202 @@ def run_misfit(args, rank, world, local):
         "rel_err_vs_direct": {"forward": err_f, "gradient_ds": err}, "setup_s": setup_s}), flush=True)
 
 
+def solve_config(n_subdiv, n_points):
+    return {"workload": "exterior Laplace Dirichlet solve on a bumpy sphere r = 1 + 0.1 Y "
+                        "(icosphere subdivided %d times, %d points), data of 10 interior unit "
+                        "charges, second-kind combined-layer system (1/2 I - D + S) mu = g"
+                        % (n_subdiv, n_points),
+            "kernels": ["LaplaceSingle", "LaplaceDouble"], "n_points": n_points, "n_rhs": 1,
+            "fmm": {"order_requested": ORDER, "surface_points": 295, "mac": MAC,
+                    "min_pts_per_cell": LEAF, "d": D, "account_for_small_cells": False},
+            "solver": "GMRES(50) to 1e-10: FP64 (FP64 compressed operators) and refined "
+                      "(inner GMRES on the precision form, FP64 residuals)",
+            "step": "one apply of the system with the precision-form operators (S and D)",
+            "l2": "inputs larger than L2 at full size; no flush"}
+
+
+def run_solve(args, rank, world, local):
+    from tbempy import meshes
+    v, t = meshes.bumpy_sphere(args.solve_subdiv)
+    locs, nrm, w = meshes.points_from_mesh(v, t)
+    N = len(locs)
+    q = meshes.interior_charges()
+    g = sum(1.0 / (4 * np.pi * np.linalg.norm(locs - p, axis=1)) for p in q)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import oracle
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        oracle.build()
+        frac = args.cpu_fraction
+        ops = [oracle.OracleFMM(k, locs, nrm, locs, nrm, w, MAC, ORDER, LEAF, D)
+               for k in ("LaplaceSingle", "LaplaceDouble")]
+        ts = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            for o in ops:
+                o.apply(g, list_fraction=frac)
+            if i >= args.warmup:
+                ts.append((time.perf_counter() - t0) / frac)
+        tt = float(np.median(ts))
+        value = N / tt
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "points*RHS/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tt,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded bumpy sphere)", "config": solve_config(args.solve_subdiv, N),
+            "cpu_baseline": {"value": value, "unit": "points*RHS/s", "cores": oracle.max_threads(),
+                             "kind": "port", "sample": "both oracle operators on the leading %.2g "
+                                                       "of every task list, extrapolated" % frac},
+            "e2e": {"value": value, "unit": "points*RHS/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    from tbempy import ThreeD, solve
+    cfg = ThreeD.FMMConfig(MAC, ORDER, LEAF, D, False)
+    kernels = (ThreeD.LaplaceSingle(), ThreeD.LaplaceDouble())
+    t0 = time.perf_counter()
+    ops = {p: [ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision=p, device=local)
+               for K in kernels] for p in ("mixed", "fp64_compressed")}
+    setup_s = time.perf_counter() - t0
+    A32 = solve.exterior_dirichlet_system(ops["mixed"][0].apply, ops["mixed"][1].apply)
+    A64 = solve.exterior_dirichlet_system(ops["fp64_compressed"][0].apply,
+                                          ops["fp64_compressed"][1].apply)
+    gt = torch.tensor(g, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        A32(gt)
+        A64(gt)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = _events_ms(torch, lambda: A32(gt), args.steps, stream)
+        ms64 = _events_ms(torch, lambda: A64(gt), 1, stream)
+    # the FP64 solve and the refined solve, both to 1e-10
+    counts = {"fp64": 0, "mixed": 0}
+
+    def counted(A, key):
+        def f(x):
+            counts[key] += 1
+            return A(x)
+        return f
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x64, info, its64 = solve.gmres(counted(A64, "fp64"), gt, restart=50, tol=1e-10, maxiter=400)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    res64 = float(torch.linalg.norm(A64(x64) - gt) / torch.linalg.norm(gt))
+    n64_plain = counts["fp64"]
+    counts = {"fp64": 0, "mixed": 0}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xr, hist = solve.refined_solve(counted(A64, "fp64"), counted(A32, "mixed"), gt, tol=1e-10,
+                                   inner_tol=1e-6)
+    torch.cuda.synchronize()
+    tref = time.perf_counter() - t0
+    resr = float(torch.linalg.norm(A64(xr) - gt) / torch.linalg.norm(gt))
+    # the field at 1,000 exterior points against the charges' potential
+    rng = np.random.default_rng(8)
+    d = rng.normal(size=(1000, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    X = d * rng.uniform(2.0, 3.0, 1000)[:, None]
+    XN = np.tile([0.0, 0.0, 1.0], (1000, 1))
+    mu = xr.cpu().numpy()
+    u = (-ThreeD.DirectOperator(kernels[1], X, XN, locs, nrm, w).apply(mu)
+         + ThreeD.DirectOperator(kernels[0], X, XN, locs, nrm, w).apply(mu))
+    exact = sum(1.0 / (4 * np.pi * np.linalg.norm(X - p, axis=1)) for p in q)
+    ext_err = float(np.linalg.norm(u - exact) / np.linalg.norm(exact))
+    print(json.dumps({
+        "metric": METRIC, "value": N / (ms / 1e3), "unit": "points*RHS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded bumpy sphere, interior charges)",
+        "config": solve_config(args.solve_subdiv, N), "clocks": clk.summary(),
+        "gpu_launches": sum(o.last_launches() for o in ops["mixed"]) * args.steps,
+        "fp64_system_apply_ms": ms64,
+        "fp64_solve": {"seconds": t64, "gmres_iterations": its64, "fp64_applies": n64_plain,
+                       "relative_residual": res64, "converged": info == 0},
+        "refined_solve": {"seconds": tref, "fp64_applies": counts["fp64"],
+                          "precision_form_applies": counts["mixed"],
+                          "history": [list(h) for h in hist], "relative_residual": resr},
+        "solution_difference": float(torch.linalg.norm(xr - x64) / torch.linalg.norm(x64)),
+        "exterior_rel_err_vs_analytic": ext_err, "setup_s": setup_s}), flush=True)
+
+
+def nearfield_config(n_subdiv, n_facets, shape, nnz):
+    return {"workload": "nearfield matrix of the Laplace double layer on the unit icosphere "
+                        "subdivided %d times (%d facets): GPU construction (sinh rule) and its CSR "
+                        "apply (the nearfield correction's SpMV)" % (n_subdiv, n_facets),
+            "kernel": "LaplaceDouble", "integrator": {"strategy": "sinh", "sinh_order": 5,
+                                                      "obs_near_order": 2, "obs_far_order": 2,
+                                                      "src_far_order": 2, "n_singular_steps": 8,
+                                                      "far_threshold": 3.0},
+            "csr": {"rows": shape[0], "cols": shape[1], "nnz": nnz, "index": "int64", "value": "f64"},
+            "step": "one CSR apply, 1 RHS",
+            "l2": "flushed before every timed step (256 MB write, outside the step timing)"}
+
+
+def run_nearfield(args, rank, world, local):
+    """The nearfield side of the operator: the GPU construction of the
+    nearfield and farfield-correction matrices (timed once) and the CSR apply
+    (SparseOperator::apply, cpp/sparse_operator.cpp:19-28), HBM-bound."""
+    import torch
+    torch.cuda.set_device(local)
+    from tbempy import ThreeD, meshes
+    v, f = meshes.icosphere(args.nf_subdiv)
+    m = ThreeD.Mesh(v, f)
+    K = ThreeD.LaplaceDouble()
+    mthd = ThreeD.make_sinh_integrator(5, 2, 2, 2, 8, 3.0, K)
+    t0 = time.perf_counter()
+    near = ThreeD.nearfield_operator(m, m, mthd, m)
+    t_near = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    corr = ThreeD.farfield_correction_operator(m, m, mthd, m)
+    t_corr = time.perf_counter() - t0
+    rows, cols, nnz = near.n_rows(), near.n_cols(), near.nnz()
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, cols)
+    xd = torch.tensor(x, device="cuda")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        near.apply(xd)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = _events_ms(torch, lambda: near.apply(xd), args.steps, stream, flush)
+    # algorithmic bytes of one apply: values and column indices once, row
+    # pointers, the output, and x once (a lower bound for the gathers)
+    algo = nnz * (8 + 8) + (rows + 1) * 8 + rows * 8 + cols * 8
+    hbm, _, peak_kind = peaks()
+    achieved = algo / (ms / 1e3) / 1e9
+    import scipy.sparse as sp
+    A = sp.csr_matrix((near.values(), near.column_indices(), near.row_ptrs()), shape=(rows, cols))
+    y_gpu = near.apply(x)
+    err = float(np.linalg.norm(y_gpu - A @ x) / np.linalg.norm(A @ x))
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        A @ x
+        ts.append(time.perf_counter() - t0)
+    tc = float(np.median(ts))
+    print(json.dumps({
+        "metric": METRIC, "value": rows / (ms / 1e3), "unit": "nearfield rows*RHS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (icosphere)",
+        "config": nearfield_config(args.nf_subdiv, m.n_facets(), (rows, cols), nnz),
+        "clocks": clk.summary(), "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "kernel": "csr_kernel", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind + " copy bandwidth",
+                     "traffic": None, "algorithmic_bytes_per_launch": algo},
+        "construction_s": {"nearfield": t_near, "farfield_correction": t_corr,
+                           "correction_nnz": corr.nnz()},
+        "rel_err_vs_scipy": err,
+        "cpu_baseline": {"value": rows / tc, "unit": "nearfield rows*RHS/s", "cores": 1, "kind": "port",
+                         "sample": "scipy CSR matvec of the same matrix (a serial loop like "
+                                   "SparseOperator::apply), median of 3"}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -702,20 +898,26 @@ def main():
                     help="0 auto, 1 SIMT FP32, 2 tcgen05 M2L, 3 tcgen05 all, 4 compressed M2L")
     ap.add_argument("--m2l-rank-tol", type=float, default=1e-7,
                     help="singular-value cut of the compressed M2L")
-    ap.add_argument("--workload", default="fault", choices=["fault", "sphere", "batched", "misfit"],
+    ap.add_argument("--workload", default="fault",
+                    choices=["fault", "sphere", "batched", "misfit", "solve", "nearfield"],
                     help="fault: the elastic fault (default); sphere: plain FP64 Laplace single "
                          "layer on the 15,360-point icosphere; batched: Laplace double layer on "
                          "200 icospheres x 64 right-hand sides in one operator; misfit: the "
                          "gradient of the elastic misfit on the 64 x 64 bumpy fault")
     ap.add_argument("--meshes", type=int, default=200, help="batched workload: meshes")
     ap.add_argument("--batch-rhs", type=int, default=64, help="batched workload: right-hand sides")
+    ap.add_argument("--nf-subdiv", type=int, default=6,
+                    help="nearfield workload: icosphere subdivisions")
+    ap.add_argument("--solve-subdiv", type=int, default=8,
+                    help="solve workload: icosphere subdivisions (8: 3.9M points)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
     if args.workload != "fault":
-        {"sphere": run_sphere, "batched": run_batched, "misfit": run_misfit}[args.workload](
+        {"sphere": run_sphere, "batched": run_batched, "misfit": run_misfit,
+         "solve": run_solve, "nearfield": run_nearfield}[args.workload](
             args, rank, world, local)
         return
     if args.impl == "reference":
