@@ -278,11 +278,10 @@ __global__ void __launch_bounds__(GM_THREADS) chain_gemm_kernel(const ChainLink<
         const int mtile = (local / L.n_tiles) % L.m_tiles;
         const int kz = local / (L.n_tiles * L.m_tiles);
         gemm_tile<T, BM>(L.a, tile, mtile, kz);
+        // every thread's writes are ordered before the item is counted done
+        __threadfence();
         __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(&sync->done[li], 1);
-        }
+        if (threadIdx.x == 0) atomicAdd(&sync->done[li], 1);
     }
 }
 
