@@ -753,15 +753,43 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
         create_streams();
     }
 
-    otree = build_tree(h_obs_locs.data(), n_obs, cfg.min_pts_per_cell, sdim);
     same_tree = n_obs == n_src &&
                 (n_obs == 0 || std::memcmp(h_obs_locs.data(), h_src_locs.data(),
                                            3 * n_obs * sizeof(double)) == 0);
-    if (same_tree) {
-        stree = &otree;
-    } else {
-        stree_own = build_tree(h_src_locs.data(), n_src, cfg.min_pts_per_cell, sdim);
+    // The precision forms with different observation and source points cut
+    // both trees from one cube (the bounding cube of all points): the cells
+    // of a level are then the same cubes in both trees, every M2L pair is an
+    // integer offset between congruent cells, and the M2L operators are
+    // precomputed (and compressed) as for a single tree.  The plain form
+    // keeps the reference's trees (each over its own bounding box).
+    common_cube = !same_tree && sdim == 3 && opt.precision != TBEM_PRECISION_FP64 && n_obs > 0 &&
+                  n_src > 0;
+    if (common_cube) {
+        double mn[3], mx[3];
+        for (int d = 0; d < 3; d++) mn[d] = mx[d] = h_obs_locs[d];
+        for (const std::vector<double>* v : {&h_obs_locs, &h_src_locs})
+            for (size_t i = 0; i < v->size() / 3; i++)
+                for (int d = 0; d < 3; d++) {
+                    mn[d] = std::min(mn[d], (*v)[3 * i + d]);
+                    mx[d] = std::max(mx[d], (*v)[3 * i + d]);
+                }
+        double c[3], H = 0;
+        for (int d = 0; d < 3; d++) {
+            c[d] = (mx[d] + mn[d]) / 2.0;
+            H = std::max(H, (mx[d] - mn[d]) / 2.0);
+        }
+        if (!(H > 0)) H = 1.0;
+        otree = build_tree_cube(h_obs_locs.data(), n_obs, cfg.min_pts_per_cell, c, H);
+        stree_own = build_tree_cube(h_src_locs.data(), n_src, cfg.min_pts_per_cell, c, H);
         stree = &stree_own;
+    } else {
+        otree = build_tree(h_obs_locs.data(), n_obs, cfg.min_pts_per_cell, sdim);
+        if (same_tree) {
+            stree = &otree;
+        } else {
+            stree_own = build_tree(h_src_locs.data(), n_src, cfg.min_pts_per_cell, sdim);
+            stree = &stree_own;
+        }
     }
     unit = sdim == 2 ? circle_surface(cfg.order) : sphere_surface(cfg.order);
     ns = (int)(unit.size() / 3);
@@ -1140,8 +1168,8 @@ void Plan::build_tasks()
     m2l_groups.clear();
     m2l_key_ls.clear();
     m2l_canon.clear();
-    f.m2l_on_the_fly = !same_tree;
-    if (same_tree) {
+    f.m2l_on_the_fly = !(same_tree || common_cube);
+    if (same_tree || common_cube) {
         std::map<std::tuple<int, int, long, long, long>, int> keys;
         for (size_t pi = 0; pi < L.m2l.size() && !f.m2l_on_the_fly; pi++) {
             const Cell& o = O.cells[L.m2l[pi].obs];
@@ -1623,7 +1651,6 @@ void Plan::build_mixed_ops(Form& F)
     YL.release();
     if (F.f64 && !F.m2l_compressed)
         throw Error(TBEM_ERR_ARG, "the FP64 compressed form needs M2L operators that compress (the "
-                                  "observation and source points must be the same, and the "
                                   "compressed products cheaper than the dense ones)");
     if (F.m2l_compressed && path == 5) {
         F.use_tc_c = true;

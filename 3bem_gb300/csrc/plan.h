@@ -343,6 +343,9 @@ struct Plan {
     long n_obs = 0, n_src = 0;
     int ns = 0, n = 0;
     bool same_tree = false;
+    // precision forms with different observation and source points: both
+    // trees cut from one bounding cube (integer M2L offsets between them)
+    bool common_cube = false;
     Tree otree, stree_own;
     const Tree* stree = nullptr;
     TaskLists L;
