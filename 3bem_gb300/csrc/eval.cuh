@@ -282,4 +282,155 @@ eval_kernel(const EvalArgs<T> a)
     }
 }
 
+// Scalar 3D kernels in FP32, point sources, not transposed, WIDE right-hand
+// sides per launch: the many-right-hand-side point-to-point and points-to-
+// check-surface passes.  The work items are those of eval_kernel (TPB =
+// 128 / TPT targets per CTA), run by half as many threads: every thread owns
+// two targets (t and t + TPB / 2), so each source read from shared memory --
+// position, normal and the densities of all WIDE right-hand sides, packed
+// four to a 4-vector -- serves two targets, and each kernel value is applied
+// to all right-hand sides.  Sums as in eval_kernel (per tile in FP32, folded
+// into a compensated pair; TPT partial sums met by warp shuffles).
+template <int KID, bool TGT_SURF, int TPT, int WIDE>
+__global__ void __launch_bounds__(EVAL_THREADS / 2)
+eval_wide_kernel(const EvalArgs<float> a)
+{
+    static_assert(kernel_dim(KID) == 1 && WIDE % 4 == 0, "scalar kernels, packed right-hand sides");
+    constexpr int NT = EVAL_THREADS / 2;     // threads of the CTA
+    constexpr int NV = WIDE / 4;             // 4-vectors of densities per source
+    constexpr int TPB = EVAL_THREADS / TPT;  // targets per CTA (as the items were cut)
+    constexpr int HALF = TPB / 2;            // a thread's second target is HALF further
+    __shared__ Vec4<float> sp[EVAL_THREADS], sn[EVAL_THREADS];
+    __shared__ Vec4<float> sv[NV][EVAL_THREADS];
+
+    const int task = a.item_task[blockIdx.x];
+    const int t0 = a.item_start[blockIdx.x];
+    const int ntgt = a.task_tgt_count[task];
+    const int lt = threadIdx.x / TPT;  // < HALF
+    const int lane = threadIdx.x % TPT;
+    const double ox = a.task_origin[3 * task], oy = a.task_origin[3 * task + 1],
+                 oz = a.task_origin[3 * task + 2];
+    const long tb = a.task_tgt[task];
+
+    float px[2], py[2], pz[2], pnx[2], pny[2], pnz[2];
+    bool act[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int ti = t0 + lt + q * HALF;
+        act[q] = ti < ntgt;
+        px[q] = py[q] = pz[q] = pnx[q] = pny[q] = pnz[q] = 0.f;
+        if (!act[q]) continue;
+        if (TGT_SURF) {
+            const double r = a.t_rad[tb];
+            const double ux = a.unit[3 * ti], uy = a.unit[3 * ti + 1], uz = a.unit[3 * ti + 2];
+            px[q] = float(r * (a.t_rref * ux) + a.t_center[3 * tb] - ox);
+            py[q] = float(r * (a.t_rref * uy) + a.t_center[3 * tb + 1] - oy);
+            pz[q] = float(r * (a.t_rref * uz) + a.t_center[3 * tb + 2] - oz);
+            pnx[q] = float(ux); pny[q] = float(uy); pnz[q] = float(uz);
+        } else {
+            const long p = tb + ti;
+            px[q] = float(a.t_xyz[3 * p] - ox);
+            py[q] = float(a.t_xyz[3 * p + 1] - oy);
+            pz[q] = float(a.t_xyz[3 * p + 2] - oz);
+            pnx[q] = a.t_nrm[3 * p]; pny[q] = a.t_nrm[3 * p + 1]; pnz[q] = a.t_nrm[3 * p + 2];
+        }
+    }
+
+    float acc[2][WIDE], lo[2][WIDE], part[2][WIDE];
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int i = 0; i < WIDE; i++) { acc[q][i] = 0.f; lo[q][i] = 0.f; part[q][i] = 0.f; }
+
+    const int b0 = a.task_src_ptr[task], b1 = a.task_src_ptr[task + 1];
+    const int total = b1 > b0 ? a.src_blk_prefix[b1 - 1] + a.src_blk_count[b1 - 1] : 0;
+    const int nr_here = min(WIDE, a.nrhs - a.rhs0);
+    int blk = b0;  // advances monotonically: a thread's slots only grow
+    for (int tile = 0; tile < total; tile += EVAL_THREADS) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int slot = threadIdx.x + h * NT;
+            const int g = tile + slot;
+            if (g >= total) continue;
+            while (blk + 1 < b1 && a.src_blk_prefix[blk + 1] <= g) blk++;
+            const long p = a.src_blk[blk] + (g - a.src_blk_prefix[blk]);
+            const double qx = a.s_xyz[3 * p], qy = a.s_xyz[3 * p + 1], qz = a.s_xyz[3 * p + 2];
+            sp[slot] = Vec4<float>{float(qx - ox), float(qy - oy), float(qz - oz), 0.f};
+            sn[slot] = Vec4<float>{a.s_nrm[3 * p], a.s_nrm[3 * p + 1], a.s_nrm[3 * p + 2], 0.f};
+#pragma unroll
+            for (int r4 = 0; r4 < NV; r4++) {
+                float vv[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int r_ = 4 * r4 + k;
+                    vv[k] = r_ < nr_here ? a.s_str[(long)(a.rhs0 + r_) * a.s_n + p] : 0.f;
+                }
+                sv[r4][slot] = Vec4<float>{vv[0], vv[1], vv[2], vv[3]};
+            }
+        }
+        __syncthreads();
+        if (act[0] || act[1]) {
+            const int n_here = min(EVAL_THREADS, total - tile);
+            const float one[3] = {1.f, 0.f, 0.f};
+            for (int j = lane; j < n_here; j += TPT) {
+                const Vec4<float> s = sp[j];
+                const Vec4<float> nq = sn[j];
+                float kv[2] = {0.f, 0.f};
+#pragma unroll
+                for (int q = 0; q < 2; q++)
+                    accumulate<KID, false, float>(s.x - px[q], s.y - py[q], s.z - pz[q], pnx[q], pny[q],
+                                                  pnz[q], nq.x, nq.y, nq.z, a.c2, one, &kv[q]);
+#pragma unroll
+                for (int r4 = 0; r4 < NV; r4++) {
+                    const Vec4<float> vq = sv[r4][j];
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        part[q][4 * r4] += kv[q] * vq.x;
+                        part[q][4 * r4 + 1] += kv[q] * vq.y;
+                        part[q][4 * r4 + 2] += kv[q] * vq.z;
+                        part[q][4 * r4 + 3] += kv[q] * vq.w;
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++)
+#pragma unroll
+                for (int i = 0; i < WIDE; i++) { kahan_add(acc[q][i], lo[q][i], part[q][i]); part[q][i] = 0.f; }
+        }
+        __syncthreads();
+    }
+    // the TPT partial sums of a target pair (consecutive lanes of one warp)
+#pragma unroll
+    for (int off = TPT / 2; off > 0; off /= 2) {
+#pragma unroll
+        for (int q = 0; q < 2; q++)
+#pragma unroll
+            for (int i = 0; i < WIDE; i++) {
+                const float o = __shfl_xor_sync(0xffffffffu, acc[q][i], off);
+                const float ol = __shfl_xor_sync(0xffffffffu, lo[q][i], off);
+                kahan_add(acc[q][i], lo[q][i], o);
+                lo[q][i] += ol;
+            }
+    }
+    if (lane != 0) return;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        if (!act[q]) continue;
+        const int ti = t0 + lt + q * HALF;
+#pragma unroll
+        for (int r_ = 0; r_ < WIDE; r_++) {
+            if (r_ >= nr_here) break;
+            if (TGT_SURF) {
+                const float val = float(a.scale) * (acc[q][r_] - lo[q][r_]);
+                float* dst = &a.c[(tb * a.nrhs + a.rhs0 + r_) * (long)a.ns + ti];
+                *dst = a.add ? *dst + val : val;
+            } else {
+                const double val = a.scale * ((double)acc[q][r_] - (double)lo[q][r_]);
+                double* dst = &a.y[(long)(a.rhs0 + r_) * a.y_n + tb + ti];
+                *dst = a.add ? *dst + val : val;
+            }
+        }
+    }
+}
+
 }  // namespace tbem

@@ -16,7 +16,7 @@ void go_tpt(int nr, int n_items, const EvalArgs<T>& a, cudaStream_t s)
     if constexpr (sizeof(T) == 4 && kernel_dim(EVAL_KID) == 1 && kernel_space_dim(EVAL_KID) == 3 &&
                   !TR && !SS) {
         if (nr == EVAL_NR_WIDE) {
-            eval_kernel<EVAL_KID, TR, T, EVAL_NR_WIDE, TS, SS, TPT><<<n_items, EVAL_THREADS, 0, s>>>(a);
+            eval_wide_kernel<EVAL_KID, TS, TPT, EVAL_NR_WIDE><<<n_items, EVAL_THREADS / 2, 0, s>>>(a);
             return;
         }
     }
