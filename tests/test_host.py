@@ -181,6 +181,28 @@ def test_host_tree_and_lists_match_oracle_on_elastic_fault_workload():
     assert len(op.list("m2l")[0]) > 100000
 
 
+def test_precision_form_cuts_distinct_trees_from_one_cube():
+    """Different observation and source points: the plain form keeps the
+    reference's trees (each over its own bounding box), the precision forms
+    cut both from the bounding cube of all points, so that every level's
+    cells are the same cubes in both trees."""
+    from tbempy import ThreeD, meshes
+    v, t, obs, on, _, _, _ = meshes.misfit_workload(n=16, n_obs=2000)
+    sl, sn, sw = meshes.points_from_mesh(v, t)
+    cfg = ThreeD.FMMConfig(0.3, 296, 64, 0.05, False)
+    K = ThreeD.ElasticDisplacement(1.0, 0.25)
+    for prec in ("mixed", "fp64_compressed"):
+        op = ThreeD.FMMOperator(K, obs, on, sl, sn, sw, cfg, precision=prec, host_only=True)
+        to, ts = op.tree(1), op.tree(0)
+        root = to["hw"][0]
+        assert root[0] == root[1] == root[2] and np.array_equal(ts["hw"][0], root)
+        assert np.array_equal(to["center"][0], ts["center"][0])
+        for tr in (to, ts):
+            assert np.array_equal(tr["hw"], root[None, :] * 2.0 ** -tr["level"][:, None])
+    plain = ThreeD.FMMOperator(K, obs, on, sl, sn, sw, cfg, host_only=True)
+    assert not np.array_equal(plain.tree(1)["hw"][0], plain.tree(0)["hw"][0])
+
+
 def test_degenerate_inputs_build():
     """Coincident and nearly coincident points (unit_tests/test_octree.cpp:113-125)."""
     from tbempy import ThreeD
