@@ -408,8 +408,8 @@ def test_default_precision_form_transpose(name):
 @pytest.mark.parametrize("name", ["LaplaceDouble", "ElasticTraction"])
 def test_precision_form_distinct_point_sets(name):
     """Observation points apart from the sources (a free surface above the
-    fault): the precision form's M2L between different trees runs in FP64
-    on the fly; against the FP64 direct sum."""
+    fault): both trees come from one cube, so the precision form's M2L
+    between them is precomputed and compressed; against the FP64 direct sum."""
     from tbempy import ThreeD, meshes
     locs, nrm, w, uv = meshes.fault_points(16)
     rng = np.random.default_rng(61)
@@ -419,7 +419,7 @@ def test_precision_form_distinct_point_sets(name):
     order = 152 if name.startswith("Laplace") else 296
     op = ThreeD.FMMOperator(K, obs, on, locs, nrm, w, ThreeD.FMMConfig(0.3, order, 40, 0.05, False),
                             precision="mixed")
-    assert op.m2l_ranks() == (0, 0)  # no compression between different trees
+    assert op.m2l_ranks()[0] > 0  # compressed between the two trees
     x = rng.uniform(-1, 1, op.n_cols())
     exact = ThreeD.DirectOperator(K, obs, on, locs, nrm, w).apply(x)
     assert rel(op.apply(x), exact) < 2e-6
