@@ -65,9 +65,7 @@ struct GemmK {
 };
 
 // One output tile (column tile `tile`, row tile `mtile`, K split `kz`) of a
-// grouped GEMM: the body of grouped_gemm_kernel, shared with the persistent
-// level chain (chain_gemm_kernel).  Ends after a barrier that follows the
-// last shared-memory read, so a CTA can run the next tile right away.
+// grouped GEMM (the body of grouped_gemm_kernel).
 template <typename T, int BM>
 __device__ __forceinline__ void gemm_tile(const GemmArgs<T>& a, int tile, int mtile, int kz)
 {
@@ -134,8 +132,7 @@ __device__ __forceinline__ void gemm_tile(const GemmArgs<T>& a, int tile, int mt
 #pragma unroll
         for (int i = 0; i < NB; i++) {
             const int gk = k0 + bk[i];
-            // (through L2: in a level chain the states were just written by other SMs)
-            rb[i] = (bcol[i] && gk < kend) ? __ldcg(&bcol[i][gk]) : T(0);
+            rb[i] = (bcol[i] && gk < kend) ? bcol[i][gk] : T(0);
         }
     };
     auto store = [&](int buf) {
@@ -218,71 +215,6 @@ template <typename T, int BM>
 __global__ void __launch_bounds__(GM_THREADS) grouped_gemm_kernel(const GemmArgs<T> a)
 {
     gemm_tile<T, BM>(a, blockIdx.x, blockIdx.y, blockIdx.z);
-}
-
-// A chain of grouped GEMMs that must run one after the other (the levels of
-// the upward M2M pass, deepest first, or of the downward L2L pass) in one
-// persistent launch.  Every GEMM's launch grid becomes a range of work items
-// (column tile x row tile x K split); CTAs take items in order from a ticket
-// counter, and an item of link li starts once every item of link li - 1 has
-// finished (a per-link completion counter).  A CTA only ever waits for items
-// with smaller tickets, which CTAs already running hold, so the chain cannot
-// deadlock whatever the number of resident CTAs; the waits are bounded all
-// the same (a wait that runs out raises `err` and the CTA carries on).
-constexpr int CHAIN_MAX_LINKS = 64;
-
-template <typename T>
-struct ChainLink {
-    GemmArgs<T> a;
-    int n_tiles, m_tiles, splits;  // the GEMM's grid
-    int item0, n_items;            // its items in the chain
-};
-
-struct ChainSync {
-    int ticket;
-    int err;
-    int done[CHAIN_MAX_LINKS];
-};
-
-template <typename T, int BM>
-__global__ void __launch_bounds__(GM_THREADS) chain_gemm_kernel(const ChainLink<T>* links, int n_links,
-                                                               int total, ChainSync* sync,
-                                                               long long wait_cycles)
-{
-    __shared__ int s_item;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&sync->ticket, 1);
-        __syncthreads();
-        const int item = s_item;
-        __syncthreads();
-        if (item >= total) return;
-        int li = 0;
-        while (li + 1 < n_links && item >= links[li + 1].item0) li++;
-        const ChainLink<T>& L = links[li];
-        if (li > 0 && threadIdx.x == 0) {
-            const int need = links[li - 1].n_items;
-            volatile int* done = &sync->done[li - 1];
-            const long long t0 = clock64();
-            while (*done < need) {
-                if (clock64() - t0 > wait_cycles) {
-                    atomicExch(&sync->err, 1);
-                    break;
-                }
-                __nanosleep(128);
-            }
-            __threadfence();
-        }
-        __syncthreads();
-        const int local = item - L.item0;
-        const int tile = local % L.n_tiles;
-        const int mtile = (local / L.n_tiles) % L.m_tiles;
-        const int kz = local / (L.n_tiles * L.m_tiles);
-        gemm_tile<T, BM>(L.a, tile, mtile, kz);
-        // every thread's writes are ordered before the item is counted done
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) atomicAdd(&sync->done[li], 1);
-    }
 }
 
 // Row tile for m rows: the one that pads m the least (128 on a tie).

@@ -208,53 +208,6 @@ void GemmSet::run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int tr
 template void GemmSet::run_rect<double>(const double*, double*, int, int, int, int, int, int, cudaStream_t, long*, bool);
 template void GemmSet::run_rect<float>(const float*, float*, int, int, int, int, int, int, cudaStream_t, long*, bool);
 
-// The set as one link of a level chain: its GEMM arguments and launch grid
-// as run_rect would choose them (no waves; K split as for an atomic launch).
-template <typename T>
-ChainLink<T> GemmSet::chain_link(const T* B, T* D, int m, int k, int lda, int nrhs, int trans, int mode,
-                                 int sms)
-{
-    if (!wave_of.empty()) throw Error(TBEM_ERR_STATE, "a wave-ordered GEMM set in a level chain");
-    // the tile tables (the run_rect ones: one wave)
-    if (tiles.find(nrhs) == tiles.end()) run_rect<T>(B, D, m, k, lda, nrhs, trans, mode, nullptr, nullptr, true);
-    auto it = tiles.find(nrhs);
-    ChainLink<T> L{};
-    GemmArgs<T>& a = L.a;
-    a.A = reinterpret_cast<const T* const*>(d_A.p);
-    a.g_pair0 = d_pair0.p;
-    a.g_npairs = d_npairs.p;
-    a.tile_group = it->second.first.p;
-    a.tile_col0 = it->second.second.p;
-    a.in_cell = d_in.p;
-    a.out_cell = d_out.p;
-    a.B = B;
-    a.D = D;
-    a.m = m;
-    a.k = k;
-    a.lda = lda;
-    a.nrhs = nrhs;
-    a.trans = trans;
-    a.mode = mode;
-    const int nt = wave_tile_start[nrhs][1] - wave_tile_start[nrhs][0];
-    const int bm = gemm_bm(m);
-    const long ctas = (long)nt * ((m + bm - 1) / bm);
-    a.kchunk = k;
-    int split = 1;
-    if (mode == GEMM_ATOMIC && ctas < 2L * sms && k >= 128) {
-        const int bk = GemmK<T>::BK;
-        split = (int)std::min<long>(std::min<long>((2L * sms + ctas - 1) / ctas, 8), k / 64);
-        a.kchunk = ((k + split - 1) / split + bk - 1) / bk * bk;
-        split = (k + a.kchunk - 1) / a.kchunk;
-    }
-    L.n_tiles = nt;
-    L.m_tiles = (m + bm - 1) / bm;
-    L.splits = split;
-    L.n_items = nt * L.m_tiles * split;
-    return L;
-}
-
-template ChainLink<double> GemmSet::chain_link<double>(const double*, double*, int, int, int, int, int, int, int);
-template ChainLink<float> GemmSet::chain_link<float>(const float*, float*, int, int, int, int, int, int, int);
 
 namespace {
 // D[tgt][:] += the target's slots, summed in slot order; one CTA per target,
@@ -2068,7 +2021,6 @@ void Plan::get_c2e(int which, long level, double* out) const
 void Plan::ensure_rhs(int nrhs)
 {
     if (nrhs <= cap_rhs) return;
-    chains.clear();  // the level chains' links name the state buffers reallocated below
     const long ncs = (long)stree->cells.size(), nco = (long)otree.cells.size();
     const long N = std::max(n_obs, n_src);
     io_x.ensure((size_t)R * std::max<long>(n_src, n_obs) * nrhs);
@@ -2131,60 +2083,6 @@ void Plan::launch_l2p(const T* cd, int len, int nrhs, cudaStream_t s)
     } else {
         throw Error(TBEM_ERR_ARG, "translation surface too large for the FP64 L2P kernel");
     }
-    TBEM_CK(cudaGetLastError());
-    launches++;
-}
-
-// One level chain (gemm.cuh: chain_gemm_kernel): the atomic GEMM sets `sets`
-// in their dependency order, D (+)= op(A) B with square m x m operators,
-// in one persistent launch.  Falls back to one launch per set when the
-// chain has more links than the kernel takes.
-template <typename T>
-void Plan::run_chain(int id, const std::vector<GemmSet*>& sets, const T* B, T* D, int m, int nrhs,
-                     cudaStream_t s)
-{
-    std::vector<GemmSet*> live;
-    for (GemmSet* g : sets)
-        if (!g->empty()) live.push_back(g);
-    if (live.empty()) return;
-    if (!use_chains || (int)live.size() > CHAIN_MAX_LINKS) {
-        for (GemmSet* g : live) g->run_rect<T>(B, D, m, m, m, nrhs, 0, GEMM_ATOMIC, s, &launches);
-        return;
-    }
-    int dev = 0, sms = 0;
-    TBEM_CK(cudaGetDevice(&dev));
-    TBEM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    ChainCache& c = chains[std::make_tuple(id * 2 + (sizeof(T) == 8 ? 1 : 0), nrhs, (const void*)B)];
-    if (c.n_links == 0) {
-        // (the state buffers B and D are the plan's own, fixed once sized)
-        std::vector<ChainLink<T>> links;
-        int total = 0;
-        for (GemmSet* g : live) {
-            ChainLink<T> L = g->chain_link<T>(B, D, m, m, m, nrhs, 0, GEMM_ATOMIC, sms);
-            L.item0 = total;
-            total += L.n_items;
-            links.push_back(L);
-        }
-        c.links.upload(reinterpret_cast<const char*>(links.data()), links.size() * sizeof(ChainLink<T>));
-        c.n_links = (int)links.size();
-        c.total = total;
-        c.bm = gemm_bm(m);
-    }
-    if (!chain_sync.p) chain_sync.alloc(2);
-    ChainSync* sync = chain_sync.p + id;
-    TBEM_CK(cudaMemsetAsync(sync, 0, sizeof(ChainSync), s));
-    int per_sm = 0;
-    if (c.bm == 128)
-        TBEM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain_gemm_kernel<T, 128>, GM_THREADS, 0));
-    else
-        TBEM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain_gemm_kernel<T, 64>, GM_THREADS, 0));
-    const unsigned grid = (unsigned)std::max(1, std::min(c.total, std::max(per_sm, 1) * sms));
-    const long long wait = 4000000000LL;  // ~2 s: no link waits longer than its predecessors' work
-    const ChainLink<T>* dl = reinterpret_cast<const ChainLink<T>*>(c.links.p);
-    if (c.bm == 128)
-        chain_gemm_kernel<T, 128><<<grid, GM_THREADS, 0, s>>>(dl, c.n_links, c.total, sync, wait);
-    else
-        chain_gemm_kernel<T, 64><<<grid, GM_THREADS, 0, s>>>(dl, c.n_links, c.total, sync, wait);
     TBEM_CK(cudaGetLastError());
     launches++;
 }
@@ -2516,13 +2414,8 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     eval<T>(p2m_set(), F.ks_kid, true, false, S, *dsrc, F.r_uc, *dsrc, 0, str, NS, nullptr, nullptr, 0, cu, 0, nrhs, s, false);
     F.comp_p2m.run_rect<T>(cu, cuc, ri, n, n, nrhs, 0, GEMM_ATOMIC, s, &launches);  // into zeros
     mark("p2m", s);
-    {
-        // the upward pass, deepest level first, as one persistent level chain
-        std::vector<GemmSet*> up;
-        for (int l = S.n_levels() - 1; l >= 0; l--)
-            if (l < (int)F.m2m_c.size()) up.push_back(&F.m2m_c[l]);
-        run_chain<T>(0, up, cuc, cuc, ri, nrhs, s);
-    }
+    for (int l = S.n_levels() - 1; l >= 0; l--)
+        if (l < (int)F.m2m_c.size()) F.m2m_c[l].run_rect<T>(cuc, cuc, ri, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("m2m", s);
     if (!L.p2l.empty()) {
         TBEM_CK(cudaMemsetAsync(cd, 0, sizeof(T) * nco * nrhs * n, s));
@@ -2542,13 +2435,8 @@ void Plan::forward_compressed(int nrhs, cudaStream_t s)
     }
     if (!tc_done) F.m2l_c.run_rect<T>(cuc, cdc, ro, ri, ri, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("m2l", s);
-    {
-        // the downward pass, parents first, as one persistent level chain
-        std::vector<GemmSet*> down;
-        for (int l = 1; l < O.n_levels(); l++)
-            if (l - 1 < (int)F.l2l_c.size()) down.push_back(&F.l2l_c[l - 1]);
-        run_chain<T>(1, down, cdc, cdc, ro, nrhs, s);
-    }
+    for (int l = 1; l < O.n_levels(); l++)
+        if (l - 1 < (int)F.l2l_c.size()) F.l2l_c[l - 1].run_rect<T>(cdc, cdc, ro, ro, ro, nrhs, 0, GEMM_ATOMIC, s, &launches);
     mark("l2l", s);
     // join the near field: the passes below add into the same outputs
     TBEM_CK(cudaStreamWaitEvent(s, ev_join, 0));
@@ -2724,15 +2612,13 @@ void Plan::check_tc_flags(bool wait_device, cudaStream_t s)
     }
 }
 
-// The device error flags of the bounded waits: the tensor-core GEMMs' and
-// the level chains' (in that order; at most N_ERR_FLAGS).
+// The device error flags of the bounded waits (the tensor-core GEMMs'; at
+// most N_ERR_FLAGS).
 std::vector<const int*> Plan::device_flags() const
 {
     std::vector<const int*> v;
     if (f.tc.err.p) v.push_back(f.tc.err.p);
     if (f.tc_c.err.p) v.push_back(f.tc_c.err.p);
-    if (chain_sync.p)
-        for (int i = 0; i < 2; i++) v.push_back(&chain_sync.p[i].err);
     return v;
 }
 

@@ -229,14 +229,11 @@ struct GemmSet {
     template <typename T>
     void run_rect(const T* B, T* D, int m, int k, int lda, int nrhs, int trans, int mode,
                   cudaStream_t s, long* launches = nullptr, bool tables_only = false);
-    // the set as one link of a level chain (gemm.cuh: chain_gemm_kernel)
-    template <typename T>
-    ChainLink<T> chain_link(const T* B, T* D, int m, int k, int lda, int nrhs, int trans, int mode,
-                            int sms);
     // tensor-core path (B taken from P's split planes; D columns of P.m rows);
     // nn = elements per operator in the pool the groups' offsets refer to
     struct TcTiles {
         DBuf<int4> t;  // per column tile: operator, group's first pair, first column, group columns
+        DBuf<int> brow, drow;  // per column tile and column (when small): B row / D column, -1 past the end
         int n = 0;
     };
     std::map<int, TcTiles> tc_tiles;  // per (nrhs, N tile)
@@ -389,8 +386,8 @@ struct Plan {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t solver = nullptr;
-    // timeout flags of the bounded device waits (tensor-core GEMMs, level
-    // chains) copied to pinned memory after every apply; an apply with device
+    // timeout flags of the bounded device waits (the tensor-core GEMMs)
+    // copied to pinned memory after every apply; an apply with device
     // outputs reports a flag raised by the previous one
     static constexpr int N_ERR_FLAGS = 4;
     int* h_err = nullptr;
@@ -469,22 +466,6 @@ struct Plan {
               long s_n, const T* q, double* y, long y_n, T* c, int add, int nrhs, cudaStream_t s,
               bool trans);
     void mark(const char* name, cudaStream_t s);
-    // the compressed form's upward and downward level passes as persistent
-    // level chains (chain 0: M2M deepest level first, chain 1: L2L): the
-    // device copies of their links per (chain, right-hand sides), and the
-    // completion counters of each chain
-    struct ChainCache {
-        DBuf<char> links;
-        int n_links = 0, total = 0, bm = 128;
-    };
-    // keyed by (chain and type, right-hand sides, state buffer); cleared
-    // whenever the state buffers are reallocated
-    std::map<std::tuple<int, int, const void*>, ChainCache> chains;
-    DBuf<ChainSync> chain_sync;  // [2]
-    bool use_chains = true;
-    template <typename T>
-    void run_chain(int id, const std::vector<GemmSet*>& sets, const T* B, T* D, int m, int nrhs,
-                   cudaStream_t s);
     template <typename T>
     void launch_l2p(const T* cd, int len, int nrhs, cudaStream_t s);
     size_t l2p_smem_set[2] = {0, 0};  // dynamic shared memory opted in for the many-RHS L2P (FP32, FP64)

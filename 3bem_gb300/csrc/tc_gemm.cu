@@ -81,6 +81,10 @@ struct TcArgs {
     // is (pair pair0 + c / nrhs, right-hand side c % nrhs), its B row
     // in_cell[pair] * nrhs + rhs and its D column out_cell[pair] * nrhs + rhs
     const int4* tiles;
+    // when they fit: every column's B row and D column precomputed per tile
+    // ([tile][BN], -1 past the end), one load with no division; else null
+    const int* tile_brow;
+    const int* tile_drow;
     const int* in_cell;
     const int* out_cell;
     int nrhs;
@@ -256,12 +260,18 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
         // independent loads: their latency hides behind the current tile)
         int nop = 0, nb[B_PER];
         auto prefetch = [&](int t) {
-            const int4 ti = a.tiles[t / m_tiles];
+            const int tile = t / m_tiles;
+            const int4 ti = a.tiles[tile];
             nop = ti.x;
+            if (a.tile_brow) {
 #pragma unroll
-            for (int i = 0; i < B_PER; i++) {
-                const int c = ti.z + prow + RSTEP * i;
-                nb[i] = c < ti.w ? a.in_cell[ti.y + c / a.nrhs] * a.nrhs + c % a.nrhs : -1;
+                for (int i = 0; i < B_PER; i++) nb[i] = a.tile_brow[(long)tile * BN + prow + RSTEP * i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < B_PER; i++) {
+                    const int c = ti.z + prow + RSTEP * i;
+                    nb[i] = c < ti.w ? a.in_cell[ti.y + c / a.nrhs] * a.nrhs + c % a.nrhs : -1;
+                }
             }
         };
         if (blockIdx.x < total) prefetch(blockIdx.x);
@@ -369,12 +379,18 @@ __global__ void __launch_bounds__(TC_THREADS_P, 1) tc_gemm_kernel(const TcArgs a
             const int m0 = (t % m_tiles) * TC_BM;
             // lane q of a 32-column chunk resolves column q's destination; the
             // loads overlap the wait for the accumulator
-            const int4 ti = a.tiles[t / m_tiles];
+            const int tile = t / m_tiles;
             int drow[NCC];
+            if (a.tile_drow) {
 #pragma unroll
-            for (int cc = 0; cc < NCC; cc++) {
-                const int c = ti.z + cc * 32 + lane;
-                drow[cc] = c < ti.w ? a.out_cell[ti.y + c / a.nrhs] * a.nrhs + c % a.nrhs : -1;
+                for (int cc = 0; cc < NCC; cc++) drow[cc] = a.tile_drow[(long)tile * BN + cc * 32 + lane];
+            } else {
+                const int4 ti = a.tiles[tile];
+#pragma unroll
+                for (int cc = 0; cc < NCC; cc++) {
+                    const int c = ti.z + cc * 32 + lane;
+                    drow[cc] = c < ti.w ? a.out_cell[ti.y + c / a.nrhs] * a.nrhs + c % a.nrhs : -1;
+                }
             }
             if (!wait(&accf_bar[b], bu & 1)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -529,6 +545,21 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
         TcTiles& e = tc_tiles[key];
         e.t.upload(t);
         e.n = (int)t.size();
+        // per-column rows as well while they stay small (up to 2^25 columns,
+        // 128 MB per table): the kernel then reads each column's row directly
+        if (t.size() * bn <= (size_t(1) << 25)) {
+            std::vector<int> brow(t.size() * bn), drow(t.size() * bn);
+            for (size_t i = 0; i < t.size(); i++)
+                for (int jj = 0; jj < bn; jj++) {
+                    const int c = t[i].z + jj;
+                    const bool v = c < t[i].w;
+                    const long p = t[i].y + c / nrhs;
+                    brow[i * bn + jj] = v ? in_cell[p] * nrhs + c % nrhs : -1;
+                    drow[i * bn + jj] = v ? out_cell[p] * nrhs + c % nrhs : -1;
+                }
+            e.brow.upload(brow);
+            e.drow.upload(drow);
+        }
         it = tc_tiles.find(key);
     }
     TcArgs a;
@@ -539,6 +570,8 @@ void GemmSet::run_tc(const TcPlanes& P, float* D, int nrhs, int atomic, long nn,
     a.a_op_stride = (long)P.m_pad * P.k_pad;
     a.k_pad = P.k_pad;
     a.tiles = it->second.t.p;
+    a.tile_brow = it->second.brow.p;
+    a.tile_drow = it->second.drow.p;
     a.in_cell = d_in.p;
     a.out_cell = d_out.p;
     a.nrhs = nrhs;
