@@ -94,9 +94,12 @@ eval_kernel(const EvalArgs<T> a)
     // value is computed once per pair and applied to every right-hand side
     constexpr bool PACK = R == 1 && NR >= 4 && NR % 4 == 0 && !SRC_SURF && !TRANS;
     constexpr int NV = PACK ? NR / 4 : NR;
+    // point-to-point in FP32 for a kernel with n . d: positions as hi + lo
+    constexpr bool SPLIT = COMP && !SRC_SURF && !TGT_SURF && normal_dot_kernel(KID);
     // per source: position, normal, and the R density components of every
     // right-hand side, each a 4-vector (one shared load in the pair loop)
     __shared__ Vec4<T> sp[EVAL_THREADS], sn[EVAL_THREADS];
+    __shared__ Vec4<T> sl[SPLIT ? EVAL_THREADS : 1];  // low parts of the positions
     __shared__ Vec4<T> sv[NV][EVAL_THREADS];
 
     const int task = a.item_task[blockIdx.x];
@@ -110,8 +113,8 @@ eval_kernel(const EvalArgs<T> a)
                  oz = a.task_origin[3 * task + 2];
     const long tb = a.task_tgt[task];
 
-    // target point relative to the origin
-    T px = 0, py = 0, pz = 0, pnx = 0, pny = 0, pnz = 0;
+    // target point relative to the origin (low parts: SPLIT only)
+    T px = 0, py = 0, pz = 0, pnx = 0, pny = 0, pnz = 0, plx = 0, ply = 0, plz = 0;
     if (active) {
         if (TGT_SURF) {
             const double r = a.t_rad[tb];
@@ -122,9 +125,10 @@ eval_kernel(const EvalArgs<T> a)
             pnx = T(ux); pny = T(uy); pnz = T(uz);
         } else {
             const long p = tb + ti;
-            px = T(a.t_xyz[3 * p] - ox);
-            py = T(a.t_xyz[3 * p + 1] - oy);
-            pz = T(a.t_xyz[3 * p + 2] - oz);
+            const double rx = a.t_xyz[3 * p] - ox, ry = a.t_xyz[3 * p + 1] - oy,
+                         rz = a.t_xyz[3 * p + 2] - oz;
+            px = T(rx); py = T(ry); pz = T(rz);
+            if (SPLIT) { plx = T(rx - double(px)); ply = T(ry - double(py)); plz = T(rz - double(pz)); }
             pnx = a.t_nrm[3 * p]; pny = a.t_nrm[3 * p + 1]; pnz = a.t_nrm[3 * p + 2];
         }
     }
@@ -187,7 +191,11 @@ eval_kernel(const EvalArgs<T> a)
                     }
                 }
             }
-            sp[threadIdx.x] = Vec4<T>{T(qx - ox), T(qy - oy), T(qz - oz), T(0)};
+            const double rx = qx - ox, ry = qy - oy, rz = qz - oz;
+            const Vec4<T> hi{T(rx), T(ry), T(rz), T(0)};
+            sp[threadIdx.x] = hi;
+            if (SPLIT)
+                sl[threadIdx.x] = Vec4<T>{T(rx - double(hi.x)), T(ry - double(hi.y)), T(rz - double(hi.z)), T(0)};
             sn[threadIdx.x] = Vec4<T>{nx, ny, nz, T(0)};
         }
         __syncthreads();
@@ -195,7 +203,12 @@ eval_kernel(const EvalArgs<T> a)
             const int n_here = min(EVAL_THREADS, total - tile);
             for (int j = lane; j < n_here; j += TPT) {
                 const Vec4<T> q = sp[j];
-                const T dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                T dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                if (SPLIT) {
+                    // (q_hi - p_hi) + (q_lo - p_lo): rounding errors O(eps |d|)
+                    const Vec4<T> ql = sl[j];
+                    dx += ql.x - plx; dy += ql.y - ply; dz += ql.z - plz;
+                }
                 const Vec4<T> nq = sn[j];
                 if constexpr (PACK) {
                     // the kernel value once (accumulate with a unit density)
@@ -300,7 +313,9 @@ eval_wide_kernel(const EvalArgs<float> a)
     constexpr int NV = WIDE / 4;             // 4-vectors of densities per source
     constexpr int TPB = EVAL_THREADS / TPT;  // targets per CTA (as the items were cut)
     constexpr int HALF = TPB / 2;            // a thread's second target is HALF further
+    constexpr bool SPLIT = !TGT_SURF && normal_dot_kernel(KID);  // positions as hi + lo
     __shared__ Vec4<float> sp[EVAL_THREADS], sn[EVAL_THREADS];
+    __shared__ Vec4<float> sl[SPLIT ? EVAL_THREADS : 1];
     __shared__ Vec4<float> sv[NV][EVAL_THREADS];
 
     const int task = a.item_task[blockIdx.x];
@@ -312,13 +327,14 @@ eval_wide_kernel(const EvalArgs<float> a)
                  oz = a.task_origin[3 * task + 2];
     const long tb = a.task_tgt[task];
 
-    float px[2], py[2], pz[2], pnx[2], pny[2], pnz[2];
+    float px[2], py[2], pz[2], pnx[2], pny[2], pnz[2], plx[2], ply[2], plz[2];
     bool act[2];
 #pragma unroll
     for (int q = 0; q < 2; q++) {
         const int ti = t0 + lt + q * HALF;
         act[q] = ti < ntgt;
         px[q] = py[q] = pz[q] = pnx[q] = pny[q] = pnz[q] = 0.f;
+        plx[q] = ply[q] = plz[q] = 0.f;
         if (!act[q]) continue;
         if (TGT_SURF) {
             const double r = a.t_rad[tb];
@@ -329,9 +345,14 @@ eval_wide_kernel(const EvalArgs<float> a)
             pnx[q] = float(ux); pny[q] = float(uy); pnz[q] = float(uz);
         } else {
             const long p = tb + ti;
-            px[q] = float(a.t_xyz[3 * p] - ox);
-            py[q] = float(a.t_xyz[3 * p + 1] - oy);
-            pz[q] = float(a.t_xyz[3 * p + 2] - oz);
+            const double rx = a.t_xyz[3 * p] - ox, ry = a.t_xyz[3 * p + 1] - oy,
+                         rz = a.t_xyz[3 * p + 2] - oz;
+            px[q] = float(rx); py[q] = float(ry); pz[q] = float(rz);
+            if (SPLIT) {
+                plx[q] = float(rx - double(px[q]));
+                ply[q] = float(ry - double(py[q]));
+                plz[q] = float(rz - double(pz[q]));
+            }
             pnx[q] = a.t_nrm[3 * p]; pny[q] = a.t_nrm[3 * p + 1]; pnz[q] = a.t_nrm[3 * p + 2];
         }
     }
@@ -354,8 +375,13 @@ eval_wide_kernel(const EvalArgs<float> a)
             if (g >= total) continue;
             while (blk + 1 < b1 && a.src_blk_prefix[blk + 1] <= g) blk++;
             const long p = a.src_blk[blk] + (g - a.src_blk_prefix[blk]);
-            const double qx = a.s_xyz[3 * p], qy = a.s_xyz[3 * p + 1], qz = a.s_xyz[3 * p + 2];
-            sp[slot] = Vec4<float>{float(qx - ox), float(qy - oy), float(qz - oz), 0.f};
+            const double rx = a.s_xyz[3 * p] - ox, ry = a.s_xyz[3 * p + 1] - oy,
+                         rz = a.s_xyz[3 * p + 2] - oz;
+            const Vec4<float> hi{float(rx), float(ry), float(rz), 0.f};
+            sp[slot] = hi;
+            if (SPLIT)
+                sl[slot] = Vec4<float>{float(rx - double(hi.x)), float(ry - double(hi.y)),
+                                       float(rz - double(hi.z)), 0.f};
             sn[slot] = Vec4<float>{a.s_nrm[3 * p], a.s_nrm[3 * p + 1], a.s_nrm[3 * p + 2], 0.f};
 #pragma unroll
             for (int r4 = 0; r4 < NV; r4++) {
@@ -375,11 +401,15 @@ eval_wide_kernel(const EvalArgs<float> a)
             for (int j = lane; j < n_here; j += TPT) {
                 const Vec4<float> s = sp[j];
                 const Vec4<float> nq = sn[j];
+                const Vec4<float> sq = SPLIT ? sl[j] : Vec4<float>{0.f, 0.f, 0.f, 0.f};
                 float kv[2] = {0.f, 0.f};
 #pragma unroll
-                for (int q = 0; q < 2; q++)
-                    accumulate<KID, false, float>(s.x - px[q], s.y - py[q], s.z - pz[q], pnx[q], pny[q],
-                                                  pnz[q], nq.x, nq.y, nq.z, a.c2, one, &kv[q]);
+                for (int q = 0; q < 2; q++) {
+                    float dx = s.x - px[q], dy = s.y - py[q], dz = s.z - pz[q];
+                    if (SPLIT) { dx += sq.x - plx[q]; dy += sq.y - ply[q]; dz += sq.z - plz[q]; }
+                    accumulate<KID, false, float>(dx, dy, dz, pnx[q], pny[q], pnz[q], nq.x, nq.y, nq.z,
+                                                  a.c2, one, &kv[q]);
+                }
 #pragma unroll
                 for (int r4 = 0; r4 < NV; r4++) {
                     const Vec4<float> vq = sv[r4][j];

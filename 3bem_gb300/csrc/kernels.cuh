@@ -27,6 +27,17 @@ enum KernelId {
     EL_HYP2 = 22, IDENT2 = 23
 };
 
+// Kernels whose value holds a normal component n . d of the separation d.
+// For a nearly tangent pair on a curved surface n . d is O(kappa h^2) while
+// the positions are O(cell width) from the FP32 origin, so FP32 separations
+// cancel badly there; the FP32 point-to-point passes of these kernels carry
+// the low parts of the positions as well (separation error O(eps |d|)).
+__host__ __device__ constexpr bool normal_dot_kernel(int kid)
+{
+    return kid == LAP_D || kid == EL_TRAC || kid == EL_ADJ || kid == EL_HYP || kid == LAP_D2 ||
+           kid == LAP_H2 || kid == EL_TRAC2 || kid == EL_ADJ2 || kid == EL_HYP2;
+}
+
 // R (= C): the number of components of the kernel's tensor
 __host__ __device__ constexpr int kernel_dim(int kid)
 {
