@@ -443,6 +443,27 @@ def ref_interior_dirs(locs, vertices, facets):
     return out
 
 
+def ref_dense_interior(kernel, vertices, facets, locs, normals, sinh_order=5, obs_near_order=2,
+                       obs_far_order=2, src_far_order=2, n_singular_steps=8, far_threshold=3.0,
+                       mu=1.0, nu=0.25):
+    """The reference's dense_interior_operator (sinh strategy) for given points
+    against a mesh: the dense matrix [R n, C n_dofs]."""
+    dim = np.asarray(vertices).shape[1]
+    k = kernel_id(kernel, dim)
+    v, f = _mesh_args(vertices, facets)
+    l, n = _pts3(locs), _pts3(normals)
+    fn = _ref().fn("dense_interior", _L, [_I, _D, _D, _I, _P, _L, _P, _L, _P, _P, _L, _L, _L, _L,
+                                          _L, _L, _D, _P])
+    args = [k, mu, nu, dim, _ptr(v), len(v), _ptr(f), len(f), _ptr(l), _ptr(n), len(l), sinh_order,
+            obs_near_order, obs_far_order, src_far_order, n_singular_steps, far_threshold]
+    cnt = fn(*args, None)
+    if cnt < 0:
+        raise ValueError("reference dense interior operator failed")
+    out = np.zeros(cnt)
+    fn(*args, _ptr(out))
+    return out.reshape(kernel_components(k) * len(l), -1)
+
+
 def ref_mass(vertices, facets, R, n_q):
     """The reference's mass_operator<dim,R,R>: (n_rows, n_cols, values, cols, rowptr)."""
     dim = np.asarray(vertices).shape[1]

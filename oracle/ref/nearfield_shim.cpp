@@ -291,6 +291,52 @@ long ref_dense_boundary(int kernel, double mu, double nu, int dim, const double*
     return (long)data.size();
 }
 
+// dense_interior_operator (cpp/integral_operator.h:133-158) for given points
+// [n][3] against a mesh (also the all-mesh) with the sinh strategy: the dense
+// (R n) x (C n_dofs) matrix, row-major, written when out != NULL; returns the
+// number of entries (or -1).
+long ref_dense_interior(int kernel, double mu, double nu, int dim, const double* verts,
+                        long n_verts, const long* facets, long n_facets, const double* locs,
+                        const double* nrms, long n, long sinh_order, long obs_near_order,
+                        long obs_far_order, long src_far_order, long n_singular_steps,
+                        double far_threshold, double* out)
+{
+    Strategy s{1, 0.0, sinh_order, obs_near_order, obs_far_order, src_far_order, n_singular_steps,
+               far_threshold};
+    int saved = omp_get_max_threads();
+    omp_set_num_threads(1);
+    std::vector<double> data;
+    bool done = false;
+    auto run = [&](const auto& K, const auto& m, auto dimc) {
+        constexpr size_t D = decltype(dimc)::value;
+        auto mthd = make_strategy(s, K);
+        std::vector<Vec<double, D>> l(n), nn(n);
+        for (long i = 0; i < n; i++)
+            for (size_t d = 0; d < D; d++) { l[i][d] = locs[3 * i + d]; nn[i][d] = nrms[3 * i + d]; }
+        auto op = dense_interior_operator(l, nn, m, mthd, m);
+        data = op.data();
+        done = true;
+    };
+    if (dim == 3) {
+        auto m = make_mesh<3>(verts, n_verts, facets, n_facets);
+        std::integral_constant<size_t, 3> d3;
+        if (kernel == 0) run(LaplaceSingle<3>(), m, d3);
+        else if (kernel == 1) run(LaplaceDouble<3>(), m, d3);
+        else if (kernel == 2) run(ElasticDisplacement<3>(mu, nu), m, d3);
+        else if (kernel == 3) run(ElasticTraction<3>(mu, nu), m, d3);
+    } else {
+        auto m = make_mesh<2>(verts, n_verts, facets, n_facets);
+        std::integral_constant<size_t, 2> d2;
+        if (kernel == 16) run(LaplaceSingle<2>(), m, d2);
+        else if (kernel == 17) run(LaplaceDouble<2>(), m, d2);
+        else if (kernel == 19) run(ElasticDisplacement<2>(mu, nu), m, d2);
+    }
+    omp_set_num_threads(saved);
+    if (!done) return -1;
+    if (out) std::memcpy(out, data.data(), data.size() * sizeof(double));
+    return (long)data.size();
+}
+
 // One IntegrationStrategy::compute_term (cpp/integral_term.cpp:33-53) for an
 // observation point (loc, normal, Richardson direction, 3-vectors) against
 // one facet ([dim][3]); out [dim basis][R][C].  Returns dim * R * C or -1.

@@ -321,6 +321,15 @@ def make_interior_cases():
                                              mu, nu)
             a, b = _dense(*res), _dense(*pr)
             out["ulp_floor%d" % which] = np.abs(a - b).max() / max(np.abs(a).max(), 1e-300)
+        # the reference's whole operator (nearfield + correction + interpolated
+        # direct farfield), its apply to a seeded density, and that apply's
+        # one-ulp sensitivity (the same vertex perturbation)
+        args = (so, on, of, sf, st, ft, mu, nu)
+        A = oracle.ref_dense_interior(kernel, v, f, pts, nrms, *args)
+        Ap = oracle.ref_dense_interior(kernel, vp, f, pts, nrms, *args)
+        x = np.random.default_rng(3).uniform(-1, 1, A.shape[1])
+        out["dense"], out["apply_x"], out["apply_y"] = A, x, A @ x
+        out["apply_ulp_floor"] = np.linalg.norm(A @ x - Ap @ x) / np.linalg.norm(A @ x)
         for R in sorted({1, dim}):
             for nq in (2, 3):
                 res = oracle.ref_mass(v, f, R, nq)
@@ -359,6 +368,9 @@ def main(ref_root=None, which="all"):
         data = make_config1()
         np.savez_compressed(os.path.join(HERE, "fmm_laps_config1.npz"), **data)
         print("wrote laps_config1", len(data["x"]), "points, ulp floor %.3g" % data["ulp_floor"])
+        return
+    if which == "interior":
+        make_interior_cases()
         return
     if which == "nearfield":
         make_nearfield_cases()

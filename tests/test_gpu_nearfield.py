@@ -93,9 +93,11 @@ INTERIOR = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "interior_*.np
 @pytest.mark.parametrize("path", INTERIOR, ids=[os.path.basename(p)[9:-4] for p in INTERIOR])
 def test_interior_operator_matches_reference(path):
     """dense_interior_operator: its nearfield and correction matrices against
-    the reference's (same tolerance as above), and its apply against
-    N x + C x + F (I x) with F the FP64 direct sum of the oracle (to 1e-10 of
-    the contributions' size)."""
+    the reference's (same tolerance as above); its apply against the
+    reference's own dense operator applied to the same density
+    (cpp/integral_operator.h:133-158), within max(1e-10, 100 x the one-ulp
+    sensitivity of that apply); and against N x + C x + F (I x) with F the
+    FP64 direct sum of the oracle (to 1e-10 of the contributions' size)."""
     from oracle import oracle
     from tbempy import ThreeD
     g = dict(np.load(path))
@@ -112,7 +114,10 @@ def test_interior_operator_matches_reference(path):
         ref = g["values%d" % which]
         tol = max(1e-10, 100 * float(g["ulp_floor%d" % which])) * np.abs(ref).max()
         assert np.abs(op.values() - ref).max() <= tol
-    x = np.random.default_rng(3).uniform(-1, 1, A.n_cols())
+    x = g["apply_x"]
+    y_ref = g["apply_y"]
+    bar = max(1e-10, 100 * float(g["apply_ulp_floor"]))
+    assert np.linalg.norm(A.apply(x) - y_ref) <= bar * np.linalg.norm(y_ref)
     N = dense(g["shape0"], g["values0"], g["cols0"], g["rowptr0"])
     Cc = dense(g["shape1"], g["values1"], g["cols1"], g["rowptr1"])
     I = A.interp
