@@ -357,4 +357,17 @@ int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int c
     return k;
 }
 
+int tbem_fmm_setup_times(const TbemFmm* h, const char** names, double* seconds, int cap)
+{
+    if (!h) return fail(TBEM_ERR_ARG, "null handle");
+    const auto& v = h->plan.setup_s;
+    int k = 0;
+    for (size_t i = 0; i < v.size(); i++, k++) {
+        if (k >= cap) continue;
+        if (names) names[k] = v[i].first.c_str();
+        if (seconds) seconds[k] = v[i].second;
+    }
+    return k;
+}
+
 }  // extern "C"

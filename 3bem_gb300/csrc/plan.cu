@@ -10,6 +10,7 @@
 // bottom-up / top-down instead of the serial post-/pre-order walks
 // (cpp/fmm.cpp:467-482, 523-538), which respects the same dependencies.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -674,6 +675,7 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
         throw Error(TBEM_ERR_ARG, "null point array");
     if (opt_.precision < TBEM_PRECISION_FP64 || opt_.precision > TBEM_PRECISION_FP64_COMPRESSED)
         throw Error(TBEM_ERR_ARG, "unknown precision form");
+    setup_start();
     kid = kernel;
     R = kernel_dim(kid);
     sdim = kernel_space_dim(kid);
@@ -748,6 +750,7 @@ void Plan::build(int kernel, const double* params, const double* obs_locs,
     ns = (int)(unit.size() / 3);
     n = R * ns;
     L = build_lists(otree, *stree, cfg.mac, ns, cfg.account_for_small_cells != 0);
+    setup_mark("trees_lists");
     if (opt.host_only) return;
     finish_build(h_obs_locs.data(), h_obs_normals.data(), h_src_locs.data(), h_src_normals.data(),
                  h_src_weights.data());
@@ -776,6 +779,7 @@ void Plan::finish_build(const double* o_locs, const double* o_nrm, const double*
     upload_tree(*stree, s_locs, s_nrm, s_w, dsrc_own);
     dsrc = &dsrc_own;
     build_tasks();
+    setup_mark("upload_tasks");
     build_form();
     TBEM_CK(cudaStreamSynchronize(stream));
     if (opt.p2p_block == 2 || opt.p2p_block == 4 || opt.p2p_block == 8) p2p_tpt = opt.p2p_block;
@@ -783,6 +787,7 @@ void Plan::finish_build(const double* o_locs, const double* o_nrm, const double*
     if (opt.p2m_block == 1 || opt.p2m_block == 2 || opt.p2m_block == 4) p2m_tpt = opt.p2m_block;
     else autotune_p2m();
     autotune_tc();
+    setup_mark("autotune");
 }
 
 // The batched form: n_meshes independent point sets (observation = source
@@ -816,6 +821,7 @@ void Plan::build_batch(int kernel, const double* params, int n_meshes, const lon
         if (offsets[m + 1] < offsets[m]) throw Error(TBEM_ERR_ARG, "mesh offsets must not decrease");
     const long N = n_meshes > 0 ? offsets[n_meshes] : 0;
     if (N > 0 && (!locs || !normals || !weights)) throw Error(TBEM_ERR_ARG, "null point array");
+    setup_start();
     kid = kernel;
     R = kernel_dim(kid);
     sdim = 3;
@@ -878,6 +884,7 @@ void Plan::build_batch(int kernel, const double* params, int n_meshes, const lon
     lists.clear();
     same_tree = true;
     stree = &otree;
+    setup_mark("trees_lists");
     if (opt.host_only) return;
     DeviceGuard guard(opt.device);
     create_streams();
@@ -1295,8 +1302,10 @@ void Plan::build_form()
         F.kt_kid = (kid == EL_ADJ || kid == EL_HYP) ? EL_ADJ : F.g_kid;
     }
     build_c2e(F);
+    setup_mark("c2e");
     if (F.mixed) build_mixed_ops(F);
     else build_plain_ops(F);
+    setup_mark("operators");
 }
 
 namespace {
@@ -2099,6 +2108,27 @@ void Plan::mark(const char* name, cudaStream_t s)
     }
     TBEM_CK(cudaEventRecord(e, s));
     marks.push_back({name, e});
+}
+
+namespace {
+double steady_seconds()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+void Plan::setup_start()
+{
+    setup_s.clear();
+    setup_t = steady_seconds();
+}
+
+void Plan::setup_mark(const char* name)
+{
+    if (!opt.host_only && stream) TBEM_CK(cudaStreamSynchronize(stream));
+    const double t = steady_seconds();
+    setup_s.push_back({name, t - setup_t});
+    setup_t = t;
 }
 
 void Plan::read_phases()

@@ -406,6 +406,13 @@ struct Plan {
     std::vector<cudaEvent_t> event_pool;
     std::vector<std::pair<std::string, double>> phase_ms;
     void read_phases();
+    // construction phases: wall seconds of each, the device synchronized at
+    // every mark (host work, uploads, factorisations, operator tables,
+    // autotuning)
+    std::vector<std::pair<std::string, double>> setup_s;
+    double setup_t = 0;  // time of the last mark (steady clock seconds)
+    void setup_start();
+    void setup_mark(const char* name);
     // kept for clone()
     std::vector<double> h_obs_locs, h_obs_normals, h_src_locs, h_src_normals, h_src_weights;
     // batched form (build_batch): mesh m owns points [batch_off[m],

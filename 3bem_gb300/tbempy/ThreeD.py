@@ -330,6 +330,14 @@ class FMMOperator(OperatorI):
         k = check(_L.lib().tbem_fmm_phase_times(self._h, names, _ptr(ms), cap))
         return [(names[i].decode(), float(ms[i])) for i in range(min(k, cap))]
 
+    def setup_times(self):
+        """Wall seconds of the construction phases, [(name, seconds)]."""
+        cap = 16
+        names = (C.c_char_p * cap)()
+        s = np.zeros(cap)
+        k = check(_L.lib().tbem_fmm_setup_times(self._h, names, _ptr(s), cap))
+        return [(names[i].decode(), float(s[i])) for i in range(min(k, cap))]
+
 
 class BatchedFMMOperator(FMMOperator):
     """One operator over many independent meshes (the batched form; the

@@ -44,6 +44,15 @@ N_GRID = 128
 N_ERR_ROWS = 4096
 
 
+
+def setup_phases(ops):
+    """Construction phase seconds summed over the operators (FMMOperator.setup_times)."""
+    out = {}
+    for op in ops:
+        for name, sec in op.setup_times():
+            out[name] = round(out.get(name, 0.0) + sec, 4)
+    return out
+
 def workload(grid=N_GRID):
     from tbempy import meshes
     locs, nrm, w, uv = meshes.fault_points(grid, 45.0)
@@ -405,7 +414,7 @@ def run_sphere(args, rank, world, local):
         "precision_form": {"ms_per_step": ms_mixed, "points_rhs_per_s": N / (ms_mixed / 1e3),
                            "rel_err_vs_direct": err_m, "phases_ms": phases_mixed,
                            "speedup_vs_plain": ms / ms_mixed},
-        "cpu_baseline": cpu, "setup_s": setup_s}), flush=True)
+        "cpu_baseline": cpu, "setup_s": setup_s, "setup_phases_s": setup_phases([op])}), flush=True)
 
 
 # --------------------------------------------------------------- batched workload
@@ -584,7 +593,8 @@ def run_batched(args, rank, world, local):
         "phases_ms": phases, "m2l_ranks": [ri, ro], "m2l_pairs": pairs,
         "rel_err_vs_direct": {"max_over_meshes": max(errs), "median": float(np.median(errs)),
                               "rows_per_mesh": 128},
-        "plain_fp64": plain, "cpu_baseline": cpu, "setup_s": setup_s, "graph_capture_s": graph_s,
+        "plain_fp64": plain, "cpu_baseline": cpu, "setup_s": setup_s,
+        "setup_phases_s": setup_phases([op]), "graph_capture_s": graph_s,
         }), flush=True)
 
 
@@ -682,7 +692,8 @@ def run_misfit(args, rank, world, local):
         "data": "synthetic (seeded bumpy fault, free-surface observers)", "config": misfit_config(),
         "clocks": clk.summary(), "gpu_launches": 2 * op.last_launches() * args.steps,
         "forward_ms": ms_fwd, "vertex_gradient_ms": ms_vert, "phases_ms_forward": phases,
-        "rel_err_vs_direct": {"forward": err_f, "gradient_ds": err}, "setup_s": setup_s}), flush=True)
+        "rel_err_vs_direct": {"forward": err_f, "gradient_ds": err}, "setup_s": setup_s,
+        "setup_phases_s": setup_phases([op])}), flush=True)
 
 
 def solve_config(n_subdiv, n_points):
@@ -805,7 +816,8 @@ def run_solve(args, rank, world, local):
                           "precision_form_applies": counts["mixed"],
                           "history": [list(h) for h in hist], "relative_residual": resr},
         "solution_difference": float(torch.linalg.norm(xr - x64) / torch.linalg.norm(x64)),
-        "exterior_rel_err_vs_analytic": ext_err, "setup_s": setup_s}), flush=True)
+        "exterior_rel_err_vs_analytic": ext_err, "setup_s": setup_s,
+        "setup_phases_s": setup_phases(ops["mixed"] + ops["fp64_compressed"])}), flush=True)
 
 
 def nearfield_config(n_subdiv, n_facets, shape, nnz):
@@ -1109,6 +1121,7 @@ def main():
             "plain_fp64": plain,
             "cpu_baseline": cpu,
             "setup_s": setup_s,
+            "setup_phases_s": setup_phases(ops),
             "m2l_ranks": [list(op.m2l_ranks()) for op in ops],
             "tc_tiles": [op.tc_tile() for op in ops],
             "p2p_threads_per_target": [op.p2p_block() for op in ops],

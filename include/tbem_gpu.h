@@ -220,6 +220,16 @@ int tbem_fmm_set_c2e(TbemFmm* h, int which, long level, const double* op);
 int tbem_fmm_set_timing(TbemFmm* h, int enabled);
 int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int cap);
 
+/* Wall seconds of the construction phases of this operator, in order
+ * (trees_lists: octrees and task lists on the host; upload_tasks: device
+ * geometry and work lists; c2e: check-to-equivalent pseudo-inverses;
+ * operators: translation tables and their compression; autotune: launch
+ * shape choices), the device synchronized at each phase end.  Replaces the
+ * reference's construction inside FMMOperator's constructor
+ * (cpp/fmm.cpp:71-101).  names/seconds are NULL-able; returns the number of
+ * phases. */
+int tbem_fmm_setup_times(const TbemFmm* h, const char** names, double* seconds, int cap);
+
 /* Threads per target the point-to-point pass uses (chosen by timing the
  * candidates 2, 4, 8 at creation unless TbemGpuOptions.p2p_block fixed it). */
 long tbem_fmm_p2p_block(const TbemFmm* h);

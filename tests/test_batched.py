@@ -58,6 +58,9 @@ def test_batched_trees_are_cubes_and_lists_stay_within_meshes():
         assert np.all(mesh_of_point[ix] == m)
     for kind in ("p2p", "m2l"):
         assert len(op.list(kind)[0]) > 0
+    # a host-only operator's construction is its trees and lists alone
+    phases = op.setup_times()
+    assert [n for n, _ in phases] == ["trees_lists"] and phases[0][1] >= 0
     # a mesh inside the batch has the tree of the same mesh alone (and its
     # lists: next test), so no list pairs cells of two meshes
     for m in range(len(off) - 1):

@@ -385,6 +385,10 @@ def test_phase_timing_means_over_applies():
     op.set_timing(False)
     op.apply(x)
     assert dict(op.phase_times()) == ph
+    # construction phases, in order
+    names = [n for n, _ in op.setup_times()]
+    assert names == ["trees_lists", "upload_tasks", "c2e", "operators", "autotune"]
+    assert all(s >= 0 for _, s in op.setup_times())
 
 
 @pytest.mark.parametrize("name", KERNELS)
