@@ -87,6 +87,68 @@ __global__ void csr_kernel(const long* rowptr, const long* col, const double* va
         }
     }
 }
+
+// FMA-rate microbenchmark: FMA_CHAINS independent chains a = a * b + c per
+// thread, FMA_UNROLL steps per iteration.  b < 1 keeps the values bounded;
+// the store happens only for a sum no chain reaches, so nothing is written
+// while the compiler must still compute every chain.
+constexpr int FMA_CHAINS = 8, FMA_UNROLL = 16, FMA_THREADS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(FMA_THREADS) fma_peak_kernel(T* out, int iters, T b, T c)
+{
+    T a[FMA_CHAINS];
+#pragma unroll
+    for (int i = 0; i < FMA_CHAINS; i++) a[i] = T(threadIdx.x + i) * T(1e-3);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int k = 0; k < FMA_UNROLL; k++)
+#pragma unroll
+            for (int i = 0; i < FMA_CHAINS; i++) a[i] = fma(a[i], b, c);
+    }
+    T s = T(0);
+#pragma unroll
+    for (int i = 0; i < FMA_CHAINS; i++) s += a[i];
+    if (s == T(-1)) out[(long)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <typename T>
+double fma_peak(int device)
+{
+    using namespace tbem;
+    DeviceGuard guard(device);
+    int sms = 0, threads = 0;
+    TBEM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    TBEM_CK(cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, device));
+    const int blocks = sms * std::max(threads / FMA_THREADS, 1);
+    const double per_iter = 2.0 * FMA_CHAINS * FMA_UNROLL * (double)blocks * FMA_THREADS;
+    DBuf<T> out;
+    out.alloc((size_t)blocks * FMA_THREADS);
+    cudaStream_t s;
+    TBEM_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    TBEM_CK(cudaEventCreate(&e0));
+    TBEM_CK(cudaEventCreate(&e1));
+    // size the run to ~10 ms from a short first run
+    int iters = 64;
+    double best = 0.0;
+    for (int run = 0; run < 5; run++) {
+        TBEM_CK(cudaEventRecord(e0, s));
+        fma_peak_kernel<T><<<blocks, FMA_THREADS, 0, s>>>(out.p, iters, T(0.999), T(1e-3));
+        TBEM_CK(cudaGetLastError());
+        TBEM_CK(cudaEventRecord(e1, s));
+        TBEM_CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        TBEM_CK(cudaEventElapsedTime(&ms, e0, e1));
+        const double tf = per_iter * iters / (ms * 1e-3) / 1e12;
+        if (run >= 2) best = std::max(best, tf);  // runs 0-1: sizing and warm-up
+        if (run == 0) iters = std::max(1, (int)std::min(1e8, iters * 10.0 / std::max((double)ms, 1e-3)));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    return best;
+}
 }  // namespace
 
 struct TbemCsr {
@@ -371,5 +433,20 @@ int tbem_integral_apply(TbemIntegral* h, const double* x, double* y, int n_rhs, 
 long tbem_integral_n_rows(const TbemIntegral* h) { return h ? h->n_rows : TBEM_ERR_ARG; }
 long tbem_integral_n_cols(const TbemIntegral* h) { return h ? h->n_cols : TBEM_ERR_ARG; }
 void tbem_integral_destroy(TbemIntegral* h) { delete h; }
+
+int tbem_fma_peak(int device, int fp64, double* tflops)
+{
+    using namespace tbem;
+    if (!tflops) {
+        set_last_error("null output");
+        return TBEM_ERR_ARG;
+    }
+    try {
+        *tflops = fp64 ? fma_peak<double>(device) : fma_peak<float>(device);
+        return TBEM_OK;
+    } catch (...) {
+        return api_status();
+    }
+}
 
 }  // extern "C"

@@ -457,6 +457,15 @@ class DirectOperator(OperatorI):
                               self._src_normals, self._src_weights)
 
 
+def fma_peak_tflops(fp64=False, device=0):
+    """The device's measured FMA rate (TFLOP/s, FMA = 2 flops) from the
+    library's microbenchmark: the denominator of the evaluation kernels'
+    roofline."""
+    out = np.zeros(1)
+    check(_L.lib().tbem_fma_peak(int(device), int(bool(fp64)), _ptr(out)))
+    return float(out[0])
+
+
 def direct_gradients(K, obs_locs, obs_normals, src_locs, src_normals, src_weights, x, r):
     """Kernel-gradient pass: derivatives of L = r^T A x (A the direct
     operator) with respect to every point position, normal and weight and to

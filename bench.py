@@ -955,6 +955,9 @@ def main():
                               m2l_path=args.m2l_path, m2l_rank_tol=args.m2l_rank_tol)
            for K in kernels]
     setup_s = time.perf_counter() - t0
+    # the evaluation kernels' denominators: FMA microbenchmark, before the timed region
+    fma_peak = {"fp32": ThreeD.fma_peak_tflops(False, local), "fp64": ThreeD.fma_peak_tflops(True, local),
+                "unit": "TFLOP/s", "method": "independent FMA chains on every SM, best of 3 ~10 ms runs"}
     n_rhs = args.rhs
     X = np.ascontiguousarray(np.tile(x, (n_rhs, 1)))
     xd = torch.tensor(X, device="cuda")
@@ -1119,6 +1122,7 @@ def main():
             "phases_ms": phase,
             "rel_err_vs_direct": errs,
             "plain_fp64": plain,
+            "fma_peak_measured": fma_peak,
             "cpu_baseline": cpu,
             "setup_s": setup_s,
             "setup_phases_s": setup_phases(ops),

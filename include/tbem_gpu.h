@@ -408,6 +408,13 @@ long tbem_interior_obs_points(int dim, const double* locs, long n, const double*
                               long n_vertices, const long* all_facets, long n_all_facets,
                               double* dirs);
 
+/* Measurement helper (no reference counterpart): the device's FMA rate in
+ * TFLOP/s (FMA = 2 flops), FP32 (fp64 = 0) or FP64 (fp64 = 1), from a
+ * microbenchmark of independent FMA chains filling every SM (2,048 threads
+ * per SM, 8 chains per thread, ~10 ms per run, the best of 3 timed runs).
+ * The denominator of the evaluation kernels' roofline. */
+int tbem_fma_peak(int device, int fp64, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -385,6 +385,10 @@ def test_phase_timing_means_over_applies():
     op.set_timing(False)
     op.apply(x)
     assert dict(op.phase_times()) == ph
+    # the FMA-rate microbenchmark (the evaluation kernels' denominator): FP32
+    # well above FP64, both within a plausible range for one GPU
+    f32, f64 = ThreeD.fma_peak_tflops(False), ThreeD.fma_peak_tflops(True)
+    assert 10.0 < f32 < 400.0 and 0.05 < f64 < f32
     # construction phases, in order
     names = [n for n, _ in op.setup_times()]
     assert names == ["trees_lists", "upload_tasks", "c2e", "operators", "autotune"]
