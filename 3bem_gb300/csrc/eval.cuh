@@ -39,6 +39,8 @@ struct EvalArgs {
     const long* src_blk;         // first point, or cell id for surfaces
     const int* src_blk_count;
     const int* src_blk_prefix;   // sources before this block within its task
+    const int* src_blk_near;     // per source block: 1 when its cell touches the target leaf
+                                 // (point-to-point sets only; may be null)
     // target geometry
     const double* t_xyz;         // [N][3] permuted points (point targets)
     const T* t_nrm;              // [N][3]
@@ -48,6 +50,7 @@ struct EvalArgs {
     // source geometry and strengths
     const double* s_xyz;
     const T* s_nrm;
+    const double* s_nrm64;       // FP64 source normals (the double-float n . d)
     const T* s_str;              // point strengths [rhs][C][N] (weights applied)
     long s_n;                    // N (component stride); rhs stride = C * N
     const double* s_center;
@@ -73,6 +76,62 @@ struct alignas(4 * sizeof(T)) Vec4 {
     T x, y, z, w;
 };
 
+// Error-free transformation of a sum (Knuth's TwoSum): s + e = a + b exactly.
+// The building block, with the FMA product error, of the compensated dot
+// product of Ogita, Rump and Oishi ("Accurate sum and dot product", SIAM J.
+// Sci. Comput. 26 (2005), algorithm Dot2).  The _rn intrinsics keep the
+// compiler from contracting or reassociating the steps.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    const float z = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+}
+
+// The double-layer value n . d / |d|^3 of a near pair (d = q - p) from
+// positions held as hi + lo FP32 pairs (relative to the task origin) and the
+// source normal as hi + lo: the separation as an unevaluated pair (TwoSum of
+// the high parts, the TwoSum error and the low parts' difference folded into
+// the low part), n . d by Dot2 on the high parts plus the first-order cross
+// terms.  The error of n . d is a few ulps of n . d itself, where the plain
+// FP32 form's is eps |d| -- for a nearly tangent pair on a curved surface
+// (n . d = O(kappa h^2)) the difference between 1e-5 and 1e-7 of the pair's
+// value.  Returns 0 for the self pair (|d|^2 < 1e-12).
+__device__ __forceinline__ float lapd_near_df(const Vec4<float>& qh, const Vec4<float>& ql,
+                                              const Vec4<float>& nh, const Vec4<float>& nl,
+                                              float phx, float phy, float phz, float plx, float ply,
+                                              float plz)
+{
+    float dh[3], dl[3];
+    const float qa[3] = {qh.x, qh.y, qh.z}, qb[3] = {ql.x, ql.y, ql.z};
+    const float pa[3] = {phx, phy, phz}, pb[3] = {plx, ply, plz};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float e;
+        two_sum(qa[k], -pa[k], dh[k], e);
+        dl[k] = __fadd_rn(e, __fsub_rn(qb[k], pb[k]));
+    }
+    const float dx = dh[0] + dl[0], dy = dh[1] + dl[1], dz = dh[2] + dl[2];
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < 1e-12f) return 0.f;
+    const float na[3] = {nh.x, nh.y, nh.z}, nb[3] = {nl.x, nl.y, nl.z};
+    float s = __fmul_rn(na[0], dh[0]);
+    float c = __fmaf_rn(na[0], dh[0], -s);
+#pragma unroll
+    for (int k = 1; k < 3; k++) {
+        const float p = __fmul_rn(na[k], dh[k]);
+        const float pe = __fmaf_rn(na[k], dh[k], -p);
+        float q;
+        two_sum(s, p, s, q);
+        c = __fadd_rn(c, __fadd_rn(q, pe));
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) c = __fmaf_rn(na[k], dl[k], __fmaf_rn(nb[k], dh[k], c));
+    const float dn = __fadd_rn(s, c);
+    const float ir = rsqrtf(r2);
+    return dn * (ir * ir * ir);
+}
+
 template <typename T>
 __device__ __forceinline__ void kahan_add(T& hi, T& lo, T v)
 {
@@ -96,10 +155,14 @@ eval_kernel(const EvalArgs<T> a)
     constexpr int NV = PACK ? NR / 4 : NR;
     // point-to-point in FP32 for a kernel with n . d: positions as hi + lo
     constexpr bool SPLIT = COMP && !SRC_SURF && !TGT_SURF && normal_dot_kernel(KID);
+    // the double layer's pairs with a source block touching the target leaf:
+    // double-float n . d (lapd_near_df), the block's flag in the position's w
+    constexpr bool DF = SPLIT && KID == LAP_D && !TRANS;
     // per source: position, normal, and the R density components of every
     // right-hand side, each a 4-vector (one shared load in the pair loop)
     __shared__ Vec4<T> sp[EVAL_THREADS], sn[EVAL_THREADS];
     __shared__ Vec4<T> sl[SPLIT ? EVAL_THREADS : 1];  // low parts of the positions
+    __shared__ Vec4<T> snl[DF ? EVAL_THREADS : 1];    // low parts of the normals
     __shared__ Vec4<T> sv[NV][EVAL_THREADS];
 
     const int task = a.item_task[blockIdx.x];
@@ -192,10 +255,17 @@ eval_kernel(const EvalArgs<T> a)
                 }
             }
             const double rx = qx - ox, ry = qy - oy, rz = qz - oz;
-            const Vec4<T> hi{T(rx), T(ry), T(rz), T(0)};
+            const bool near = DF && a.src_blk_near && a.src_blk_near[blk];
+            const Vec4<T> hi{T(rx), T(ry), T(rz), near ? T(1) : T(0)};
             sp[threadIdx.x] = hi;
             if (SPLIT)
                 sl[threadIdx.x] = Vec4<T>{T(rx - double(hi.x)), T(ry - double(hi.y)), T(rz - double(hi.z)), T(0)};
+            if (near) {
+                const long p = sb + li;
+                const double mx = a.s_nrm64[3 * p], my = a.s_nrm64[3 * p + 1], mz = a.s_nrm64[3 * p + 2];
+                nx = T(mx); ny = T(my); nz = T(mz);
+                snl[threadIdx.x] = Vec4<T>{T(mx - double(nx)), T(my - double(ny)), T(mz - double(nz)), T(0)};
+            }
             sn[threadIdx.x] = Vec4<T>{nx, ny, nz, T(0)};
         }
         __syncthreads();
@@ -203,6 +273,24 @@ eval_kernel(const EvalArgs<T> a)
             const int n_here = min(EVAL_THREADS, total - tile);
             for (int j = lane; j < n_here; j += TPT) {
                 const Vec4<T> q = sp[j];
+                if constexpr (DF) {
+                    if (q.w != T(0)) {
+                        const T kv = lapd_near_df(q, sl[j], sn[j], snl[j], px, py, pz, plx, ply, plz);
+#pragma unroll
+                        for (int r4 = 0; r4 < NV; r4++) {
+                            const Vec4<T> vq = sv[r4][j];
+                            if constexpr (PACK) {
+                                part[4 * r4] += kv * vq.x;
+                                part[4 * r4 + 1] += kv * vq.y;
+                                part[4 * r4 + 2] += kv * vq.z;
+                                part[4 * r4 + 3] += kv * vq.w;
+                            } else {
+                                part[r4] += kv * vq.x;  // R = 1: one density per right-hand side
+                            }
+                        }
+                        continue;
+                    }
+                }
                 T dx = q.x - px, dy = q.y - py, dz = q.z - pz;
                 if (SPLIT) {
                     // (q_hi - p_hi) + (q_lo - p_lo): rounding errors O(eps |d|)
@@ -314,8 +402,13 @@ eval_wide_kernel(const EvalArgs<float> a)
     constexpr int TPB = EVAL_THREADS / TPT;  // targets per CTA (as the items were cut)
     constexpr int HALF = TPB / 2;            // a thread's second target is HALF further
     constexpr bool SPLIT = !TGT_SURF && normal_dot_kernel(KID);  // positions as hi + lo
+    // the double layer's pairs with a source block touching the target leaf
+    // take the double-float n . d (lapd_near_df; the block's flag rides in
+    // the position's w); the source normals' low parts are staged for them
+    constexpr bool DF = SPLIT && KID == LAP_D;
     __shared__ Vec4<float> sp[EVAL_THREADS], sn[EVAL_THREADS];
     __shared__ Vec4<float> sl[SPLIT ? EVAL_THREADS : 1];
+    __shared__ Vec4<float> snl[DF ? EVAL_THREADS : 1];
     __shared__ Vec4<float> sv[NV][EVAL_THREADS];
 
     const int task = a.item_task[blockIdx.x];
@@ -377,12 +470,21 @@ eval_wide_kernel(const EvalArgs<float> a)
             const long p = a.src_blk[blk] + (g - a.src_blk_prefix[blk]);
             const double rx = a.s_xyz[3 * p] - ox, ry = a.s_xyz[3 * p + 1] - oy,
                          rz = a.s_xyz[3 * p + 2] - oz;
-            const Vec4<float> hi{float(rx), float(ry), float(rz), 0.f};
+            const bool near = DF && a.src_blk_near && a.src_blk_near[blk];
+            const Vec4<float> hi{float(rx), float(ry), float(rz), near ? 1.f : 0.f};
             sp[slot] = hi;
             if (SPLIT)
                 sl[slot] = Vec4<float>{float(rx - double(hi.x)), float(ry - double(hi.y)),
                                        float(rz - double(hi.z)), 0.f};
-            sn[slot] = Vec4<float>{a.s_nrm[3 * p], a.s_nrm[3 * p + 1], a.s_nrm[3 * p + 2], 0.f};
+            if (near) {
+                const double nx = a.s_nrm64[3 * p], ny = a.s_nrm64[3 * p + 1], nz = a.s_nrm64[3 * p + 2];
+                const Vec4<float> nh{float(nx), float(ny), float(nz), 0.f};
+                sn[slot] = nh;
+                snl[slot] = Vec4<float>{float(nx - double(nh.x)), float(ny - double(nh.y)),
+                                        float(nz - double(nh.z)), 0.f};
+            } else {
+                sn[slot] = Vec4<float>{a.s_nrm[3 * p], a.s_nrm[3 * p + 1], a.s_nrm[3 * p + 2], 0.f};
+            }
 #pragma unroll
             for (int r4 = 0; r4 < NV; r4++) {
                 float vv[4];
@@ -403,12 +505,19 @@ eval_wide_kernel(const EvalArgs<float> a)
                 const Vec4<float> nq = sn[j];
                 const Vec4<float> sq = SPLIT ? sl[j] : Vec4<float>{0.f, 0.f, 0.f, 0.f};
                 float kv[2] = {0.f, 0.f};
+                if (DF && s.w != 0.f) {
+                    const Vec4<float> nl = snl[j];
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    float dx = s.x - px[q], dy = s.y - py[q], dz = s.z - pz[q];
-                    if (SPLIT) { dx += sq.x - plx[q]; dy += sq.y - ply[q]; dz += sq.z - plz[q]; }
-                    accumulate<KID, false, float>(dx, dy, dz, pnx[q], pny[q], pnz[q], nq.x, nq.y, nq.z,
-                                                  a.c2, one, &kv[q]);
+                    for (int q = 0; q < 2; q++)
+                        kv[q] = lapd_near_df(s, sq, nq, nl, px[q], py[q], pz[q], plx[q], ply[q], plz[q]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        float dx = s.x - px[q], dy = s.y - py[q], dz = s.z - pz[q];
+                        if (SPLIT) { dx += sq.x - plx[q]; dy += sq.y - ply[q]; dz += sq.z - plz[q]; }
+                        accumulate<KID, false, float>(dx, dy, dz, pnx[q], pny[q], pnz[q], nq.x, nq.y,
+                                                      nq.z, a.c2, one, &kv[q]);
+                    }
                 }
 #pragma unroll
                 for (int r4 = 0; r4 < NV; r4++) {

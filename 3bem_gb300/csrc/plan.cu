@@ -47,7 +47,8 @@ void check_cusolver(cusolverStatus_t e, const char* what, const char* file, int 
 // ------------------------------------------------------------------ helpers
 
 void TaskSet::add(long target, int count, const double* org,
-                  const std::vector<std::pair<long, int>>& srcs, int targets_per_cta)
+                  const std::vector<std::pair<long, int>>& srcs, int targets_per_cta,
+                  const std::vector<int>& near)
 {
     int pre = 0;
     for (auto& s : srcs) pre += std::max(s.second, 0);
@@ -57,8 +58,13 @@ void TaskSet::add(long target, int count, const double* org,
     tgt_count.push_back(count);
     origin.insert(origin.end(), org, org + 3);
     pre = 0;
-    for (auto& s : srcs) {
+    for (size_t i = 0; i < srcs.size(); i++) {
+        const auto& s = srcs[i];
         if (s.second <= 0) continue;
+        if (!near.empty()) {
+            blk_near.resize(blk.size(), 0);  // earlier tasks without flags
+            blk_near.push_back(near[i]);
+        }
         blk.push_back(s.first);
         blk_count.push_back(s.second);
         blk_prefix.push_back(pre);
@@ -81,6 +87,10 @@ void TaskSet::upload()
     d_blk.upload(blk);
     d_blk_count.upload(blk_count);
     d_blk_prefix.upload(blk_prefix);
+    if (!blk_near.empty()) {
+        blk_near.resize(blk.size(), 0);
+        d_blk_near.upload(blk_near);
+    }
     d_item_task.upload(item_task);
     d_item_start.upload(item_start);
 }
@@ -1038,18 +1048,32 @@ void Plan::build_tasks()
     for (auto& p : L.p2l) { p2l_of[p.obs].push_back(p.src); p2l_by_src[p.src].push_back(p.obs); }
     for (auto& p : L.m2l) { m2l_of[p.obs].push_back(p.src); m2l_by_src[p.src].push_back(p.obs); }
 
+    // A source cell "touches" a target leaf when their boxes overlap or share
+    // a face, edge or corner: its pairs are the closest ones, where the FP32
+    // double layer takes the double-float n . d
+    auto touches = [](const Cell& a, const Cell& b) {
+        for (int d = 0; d < 3; d++) {
+            const double gap = std::fabs(a.center[d] - b.center[d]) - a.hw[d] - b.hw[d];
+            if (gap > 1e-9 * std::max(a.hw[d] + b.hw[d], 1e-300)) return false;
+        }
+        return true;
+    };
     // point targets collect the lists of the leaf and of all its ancestors
     for (size_t c = 0; c < O.cells.size(); c++) {
         const Cell& leaf = O.cells[c];
         if (!leaf.is_leaf()) continue;
         std::vector<std::pair<long, int>> pp, mp;
+        std::vector<int> near;
         for (int a = (int)c; a >= 0; a = O.cells[a].parent) {
-            for (int s : p2p_of[a]) pp.push_back({S.cells[s].pt_begin, (int)S.cells[s].n_points()});
+            for (int s : p2p_of[a]) {
+                pp.push_back({S.cells[s].pt_begin, (int)S.cells[s].n_points()});
+                near.push_back(touches(leaf, S.cells[s]) ? 1 : 0);
+            }
             for (int s : m2p_of[a]) mp.push_back({s, ns});
         }
-        p2p.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, TPB);
-        p2p_tpt2.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, EVAL_THREADS / 2);
-        p2p_tpt8.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, EVAL_THREADS / 8);
+        p2p.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, TPB, near);
+        p2p_tpt2.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, EVAL_THREADS / 2, near);
+        p2p_tpt8.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, pp, EVAL_THREADS / 8, near);
         m2p.add(leaf.pt_begin, (int)leaf.n_points(), leaf.center, mp, TPB);
     }
     for (size_t c = 0; c < O.cells.size(); c++) {
@@ -2163,7 +2187,7 @@ void Plan::eval(const TaskSet& ts, int ekid, bool tgt_surf, bool src_surf, const
                 cudaStream_t s, bool trans)
 {
     if (ts.n_items() == 0) return;
-    EvalArgs<T> a;
+    EvalArgs<T> a{};
     ts.fill(a);
     a.t_xyz = dt.xyz.p;
     if constexpr (sizeof(T) == 4) a.t_nrm = dt.nrm32.p; else a.t_nrm = dt.nrm64.p;
@@ -2172,6 +2196,7 @@ void Plan::eval(const TaskSet& ts, int ekid, bool tgt_surf, bool src_surf, const
     a.t_rref = t_rref;
     a.s_xyz = ds.xyz.p;
     if constexpr (sizeof(T) == 4) a.s_nrm = ds.nrm32.p; else a.s_nrm = ds.nrm64.p;
+    a.s_nrm64 = ds.nrm64.p;
     a.s_str = s_str;
     a.s_n = s_n;
     a.s_center = ds.center.p;
@@ -2546,6 +2571,11 @@ void Plan::adjoint_compressed(int nrhs, cudaStream_t s)
     }
     for (int l = 0; l < S.n_levels(); l++)
         if (l < (int)F.m2m_c_t.size()) F.m2m_c_t[l].run_rect<T>(cuc, cuc, ri, ri, ri, nrhs, 1, GEMM_ATOMIC, s, &launches);
+    // the compression set skips the P2M leaves whose states reach no result
+    // (their transposed states are zero), but the transposed P2M below reads
+    // every P2M leaf: clear the buffer first (it still holds the M2P densities
+    // or an earlier apply's values)
+    TBEM_CK(cudaMemsetAsync(cu, 0, sizeof(T) * ncs * nrhs * n, s));
     F.comp_p2m.run_rect<T>(cuc, cu, n, ri, n, nrhs, 1, GEMM_STORE, s, &launches);
     eval<T>(p2m_t, F.ks_kid, false, true, S, *dsrc, 0, *dsrc, F.r_uc, nullptr, 0, cu, s64.p, NS, nullptr, 1, nrhs, s, true);
 }

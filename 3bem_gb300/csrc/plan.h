@@ -159,17 +159,19 @@ struct TaskSet {
     std::vector<int> src_ptr{0};
     std::vector<long> blk;
     std::vector<int> blk_count, blk_prefix;
+    std::vector<int> blk_near;  // per block: its cell touches the target leaf (point-to-point sets)
     std::vector<int> item_task, item_start;
     DBuf<long> d_tgt, d_blk;
-    DBuf<int> d_tgt_count, d_src_ptr, d_blk_count, d_blk_prefix, d_item_task, d_item_start;
+    DBuf<int> d_tgt_count, d_src_ptr, d_blk_count, d_blk_prefix, d_item_task, d_item_start, d_blk_near;
     DBuf<double> d_origin;
     long n_pairs = 0;  // sum over tasks of targets x sources (work estimate)
     int tpt = 4;       // threads per target the items were cut for
 
     int n_tasks() const { return (int)tgt.size(); }
     int n_items() const { return (int)item_task.size(); }
+    // near: one flag per entry of srcs (empty: no flags)
     void add(long target, int count, const double* org, const std::vector<std::pair<long, int>>& srcs,
-             int targets_per_cta);
+             int targets_per_cta, const std::vector<int>& near = {});
     void upload();
     template <typename T>
     void fill(EvalArgs<T>& a) const
@@ -183,6 +185,7 @@ struct TaskSet {
         a.src_blk = d_blk.p;
         a.src_blk_count = d_blk_count.p;
         a.src_blk_prefix = d_blk_prefix.p;
+        a.src_blk_near = d_blk_near.p;
     }
 };
 

@@ -413,6 +413,40 @@ def test_default_precision_form_transpose(name):
         assert abs(lhs - rhs) <= 1e-6 * np.linalg.norm(AX[r]) * np.linalg.norm(Z[r])
 
 
+@pytest.mark.parametrize("prec", ["mixed", "fp64_compressed"])
+@pytest.mark.parametrize("name", ["LaplaceSingle", "ElasticDisplacement"])
+@pytest.mark.parametrize("distinct", [False, True])
+def test_compressed_adjoint_many_rhs(name, distinct, prec):
+    """The compressed forms' transposed apply: 1 to 64 right-hand sides at
+    once equal the same right-hand sides one at a time, whatever forward
+    applies left in the work buffers, and equal the transpose of the forward
+    operator (every leaf's transposed P2M reads only states of this apply)."""
+    from tbempy import ThreeD
+    src, sn, w = cloud(400, 1)
+    ol, on = (src, sn) if not distinct else cloud(300, 2)[:2]
+    op = ThreeD.FMMOperator(kernel_obj(name), ol, on, src, sn, w,
+                            ThreeD.FMMConfig(0.3, 296, 30, 0.05, False), precision=prec)
+    rng = np.random.default_rng(5)
+    Z = rng.uniform(-1, 1, (64, op.n_rows()))
+    X = rng.uniform(-1, 1, (64, op.n_cols()))
+    tol = 1e-6 if prec == "mixed" else 1e-12
+    single = []
+    for i in range(16):
+        op.apply(X[i])  # leaves forward states behind
+        single.append(op.apply_adjoint(Z[i]))
+    single = np.stack(single)
+    for nr in (2, 3, 5, 16):
+        op.apply(X[:nr])
+        W = op.apply_adjoint(Z[:nr])
+        assert np.all(np.isfinite(W))
+        assert rel(W, single[:nr]) < tol
+    AX = op.apply(X[:16])
+    W = op.apply_adjoint(Z[:16])
+    for r in range(16):
+        lhs, rhs = AX[r] @ Z[r], X[r] @ W[r]
+        assert abs(lhs - rhs) <= 10 * tol * np.linalg.norm(AX[r]) * np.linalg.norm(Z[r])
+
+
 @pytest.mark.parametrize("name", ["LaplaceDouble", "ElasticTraction"])
 def test_precision_form_distinct_point_sets(name):
     """Observation points apart from the sources (a free surface above the
