@@ -133,6 +133,16 @@ int tbem_fmm_apply_adjoint(TbemFmm* h, const double* z, double* w, int n_rhs, vo
     return guarded([&] { h->plan.apply(z, w, n_rhs, (cudaStream_t)stream, true); });
 }
 
+int tbem_fmm_source_gradients(TbemFmm* h, const double* x, const double* r, double* g_src_locs,
+                              double* g_src_normals, double* g_src_weights, void* stream)
+{
+    if (!h || (tbem_fmm_n_cols(h) > 0 && (!x || (!r && tbem_fmm_n_rows(h) > 0))))
+        return fail(TBEM_ERR_ARG, "null argument");
+    return guarded([&] {
+        h->plan.source_gradients(x, r, g_src_locs, g_src_normals, g_src_weights, (cudaStream_t)stream);
+    });
+}
+
 long tbem_fmm_n_rows(const TbemFmm* h) { return h ? h->plan.R * h->plan.n_obs : TBEM_ERR_ARG; }
 long tbem_fmm_n_cols(const TbemFmm* h) { return h ? h->plan.R * h->plan.n_src : TBEM_ERR_ARG; }
 

@@ -159,6 +159,116 @@ __global__ void grad_obs_kernel(int kid, KParams p, const double* ox, const doub
     }
 }
 
+// Source-side gradients through the FMM's transposed passes.  For every
+// source point j (a target here) and every source z of one transposed pass
+// -- an observation point with density r (P2P^T), or a point of a check
+// surface with the transposed state as its density (P2M^T, P2L^T) -- the
+// contraction c = v(z)^T K(y_j - z; n_z, n_j) x_j, its gradient in y_j and
+// (kernels with a source normal) in n_j are summed; the sums of c are
+// dL/dw_j.  GRAD_TPT threads per target split its sources and meet in warp
+// shuffles; the work items are those of the transposed task sets (32
+// targets per CTA of 128 threads).
+struct GradEvalArgs {
+    const int* item_task;
+    const int* item_start;
+    const long* task_tgt;
+    const int* task_tgt_count;
+    const int* task_src_ptr;
+    const long* src_blk;
+    const int* src_blk_count;
+    const double* t_xyz;   // source points, tree order [n][3]
+    const double* t_nrm;
+    const double* t_x;     // their densities x, tree order [R][t_n]
+    long t_n;
+    const double* s_xyz;   // point sources (observation points, tree order)
+    const double* s_nrm;
+    const double* s_v;     // their densities r [R][s_n]
+    long s_n;
+    const double* s_center;  // surface sources: cell centres, radii, the unit sphere
+    const double* s_rad;
+    double s_rref;
+    const double* unit;
+    int ns;
+    const float* q32;      // surface densities [cell][R ns] (one right-hand side)
+    const double* q64;
+    int kid;
+    KParams kp;
+    int want_n;
+    double* g;             // [t_n][7]: d/dy (3), d/dn (3), value (1); accumulated
+};
+constexpr int GRAD_TPT = 4, GRAD_THREADS = 128;
+
+template <bool SRC_SURF>
+__global__ void __launch_bounds__(GRAD_THREADS) grad_eval_kernel(const GradEvalArgs a)
+{
+    const int task = a.item_task[blockIdx.x];
+    const int ti = a.item_start[blockIdx.x] + (int)threadIdx.x / GRAD_TPT;
+    const int lane = threadIdx.x % GRAD_TPT;
+    const bool active = ti < a.task_tgt_count[task];
+    const int R = kernel_dim(a.kid);
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    if (active) {
+        const long j = a.task_tgt[task] + ti;
+        const double y[3] = {a.t_xyz[3 * j], a.t_xyz[3 * j + 1], a.t_xyz[3 * j + 2]};
+        const double nj[3] = {a.t_nrm[3 * j], a.t_nrm[3 * j + 1], a.t_nrm[3 * j + 2]};
+        double xv[3] = {0, 0, 0};
+        for (int b = 0; b < R; b++) xv[b] = a.t_x[b * a.t_n + j];
+        for (int blk = a.task_src_ptr[task]; blk < a.task_src_ptr[task + 1]; blk++) {
+            const long sb = a.src_blk[blk];
+            const int cnt = a.src_blk_count[blk];
+            for (int li = lane; li < cnt; li += GRAD_TPT) {
+                double z[3], nz[3], rv[3] = {0, 0, 0};
+                if (SRC_SURF) {
+                    const double rr = a.s_rad[sb];
+                    for (int k = 0; k < 3; k++) {
+                        const double u = a.unit[3 * li + k];
+                        z[k] = rr * (a.s_rref * u) + a.s_center[3 * sb + k];
+                        nz[k] = u;
+                    }
+                    const long base = sb * (long)(R * a.ns) + li;
+                    for (int d = 0; d < R; d++)
+                        rv[d] = a.q32 ? (double)a.q32[base + d * a.ns] : a.q64[base + d * a.ns];
+                } else {
+                    const long p = sb + li;
+                    for (int k = 0; k < 3; k++) {
+                        z[k] = a.s_xyz[3 * p + k];
+                        nz[k] = a.s_nrm[3 * p + k];
+                    }
+                    for (int d = 0; d < R; d++) rv[d] = a.s_v[d * a.s_n + p];
+                }
+                const double dd[3] = {y[0] - z[0], y[1] - z[1], y[2] - z[2]};
+                const Dual3 c = contraction(a.kid, 0, dd, nz, nj, rv, xv, a.kp);
+                acc[6] += c.v;
+                for (int k = 0; k < 3; k++) acc[k] += c.g[k];
+                if (a.want_n) {
+                    const Dual3 cn = contraction(a.kid, 1, dd, nz, nj, rv, xv, a.kp);
+                    for (int k = 0; k < 3; k++) acc[3 + k] += cn.g[k];
+                }
+            }
+        }
+    }
+    for (int off = GRAD_TPT / 2; off > 0; off /= 2)
+        for (int i = 0; i < 7; i++) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+    if (!active || lane != 0) return;
+    double* g = a.g + 7 * (a.task_tgt[task] + ti);
+    for (int i = 0; i < 7; i++) g[i] += acc[i];
+}
+
+// Tree order [n][7] -> the caller's order: g_y = w dL/dy, g_n = w dL/dn,
+// g_w = the value sum (any output may be null).
+__global__ void grad_scatter_kernel(const double* g7, const long* perm, const double* w, long n,
+                                    double* g_y, double* g_n, double* g_w)
+{
+    for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
+        const long o = perm[j];
+        for (int k = 0; k < 3; k++) {
+            if (g_y) g_y[3 * o + k] = w[j] * g7[7 * j + k];
+            if (g_n) g_n[3 * o + k] = w[j] * g7[7 * j + 3 + k];
+        }
+        if (g_w) g_w[o] = g7[7 * j + 6];
+    }
+}
+
 bool dev_ptr(const void* p)
 {
     cudaPointerAttributes a{};
@@ -202,7 +312,125 @@ struct Out {
     }
 };
 
+// One transposed pass of the source gradients over a task set.
+void grad_pass(const TaskSet& ts, bool src_surf, GradEvalArgs a, cudaStream_t s, long* launches)
+{
+    if (ts.n_items() == 0) return;
+    a.item_task = ts.d_item_task.p;
+    a.item_start = ts.d_item_start.p;
+    a.task_tgt = ts.d_tgt.p;
+    a.task_tgt_count = ts.d_tgt_count.p;
+    a.task_src_ptr = ts.d_src_ptr.p;
+    a.src_blk = ts.d_blk.p;
+    a.src_blk_count = ts.d_blk_count.p;
+    if (src_surf) grad_eval_kernel<true><<<ts.n_items(), GRAD_THREADS, 0, s>>>(a);
+    else grad_eval_kernel<false><<<ts.n_items(), GRAD_THREADS, 0, s>>>(a);
+    TBEM_CK(cudaGetLastError());
+    if (launches) (*launches)++;
+}
+
+__global__ void gather_rows_kernel(const double* x, const long* perm, double* out, long n, int R)
+{
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n * R; t += (long)gridDim.x * blockDim.x) {
+        const long i = t % n, d = t / n;
+        out[t] = x[d * n + perm[i]];
+    }
+}
+
+unsigned blocks_for(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 32)); }
+
 }  // namespace
+
+// The transposed apply of r leaves the transposed states of the source
+// leaves' up-check surfaces (cu) and of the P2L cells' down-check surfaces
+// (cd) in the work buffers; the three passes that reach source points
+// (P2P^T, P2M^T, P2L^T) are then run again with the kernel's derivatives.
+// The compressed forms only: their transposed states are check potentials
+// on fixed surfaces, so every dependence on a source point's position and
+// normal sits in these three passes.
+void Plan::source_gradients(const double* x, const double* r, double* g_y, double* g_n,
+                            double* g_w, cudaStream_t s)
+{
+    if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
+    if (sdim != 3) throw Error(TBEM_ERR_ARG, "source gradients take the 3D kernels");
+    if (!batch_off.empty())
+        throw Error(TBEM_ERR_STATE, "source gradients are not defined for the batched form "
+                                    "(its meshes are rescaled by their own bounding boxes)");
+    if (!(f.mixed && f.m2l_compressed) || f.m2l_on_the_fly)
+        throw Error(TBEM_ERR_STATE, "source gradients need a compressed form (the precision or "
+                                    "FP64 compressed form with compressible M2L operators)");
+    if (!x || !r) throw Error(TBEM_ERR_ARG, "null input");
+    DeviceGuard guard(opt.device);
+    if (!s) s = stream;
+    const long NS = n_src, NO = n_obs;
+    if (NS == 0) return;
+    // the work arrays: tree-order gradients [NS][7], x in tree order, r in
+    // tree order, the transposed apply's output, the caller-order outputs
+    const size_t off_x = 7 * (size_t)NS, off_r = off_x + R * (size_t)NS,
+                 off_o = off_r + R * (size_t)std::max<long>(NO, 1), off_u = off_o + R * (size_t)NS,
+                 total = off_u + 7 * (size_t)NS;
+    grad_buf.ensure(total);
+    double* g7 = grad_buf.p;
+    double* xt = grad_buf.p + off_x;
+    double* rt = grad_buf.p + off_r;
+    double* out = grad_buf.p + off_o;
+    double* gu = grad_buf.p + off_u;
+    apply(r, out, 1, s, true);  // r is in io_x now, the transposed states in cu / cd
+    // x to the device (io_y is free after the apply), then both to tree order
+    TBEM_CK(cudaMemcpyAsync(io_y.p, x, sizeof(double) * R * NS, cudaMemcpyDefault, s));
+    gather_rows_kernel<<<blocks_for(NS * R), 256, 0, s>>>(io_y.p, dsrc->perm.p, xt, NS, R);
+    TBEM_CK(cudaGetLastError());
+    if (NO > 0) {
+        gather_rows_kernel<<<blocks_for(NO * R), 256, 0, s>>>(io_x.p, dobs.perm.p, rt, NO, R);
+        TBEM_CK(cudaGetLastError());
+    }
+    TBEM_CK(cudaMemsetAsync(g7, 0, sizeof(double) * 7 * NS, s));
+    GradEvalArgs a{};
+    a.t_xyz = dsrc->xyz.p;
+    a.t_nrm = dsrc->nrm64.p;
+    a.t_x = xt;
+    a.t_n = NS;
+    a.unit = d_unit.p;
+    a.ns = ns;
+    a.g = g7;
+    auto with_normals = [](int k) { return k == LAP_D || k == EL_TRAC || k == EL_HYP; };
+    // P2P^T: the observation points with the densities r
+    a.kid = kid;
+    a.kp = make_kparams(kid, mu, nu);
+    a.want_n = with_normals(kid);
+    a.s_xyz = dobs.xyz.p;
+    a.s_nrm = dobs.nrm64.p;
+    a.s_v = rt;
+    a.s_n = NO;
+    grad_pass(p2p_t, false, a, s, &launches);
+    // P2M^T and P2L^T: check surfaces with the transposed states
+    a.kid = f.ks_kid;
+    a.kp = make_kparams(f.ks_kid, mu, nu);
+    a.want_n = with_normals(f.ks_kid);
+    a.q32 = f.f64 ? nullptr : cu32.p;
+    a.q64 = f.f64 ? cu64.p : nullptr;
+    a.s_center = dsrc->center.p;
+    a.s_rad = dsrc->rad.p;
+    a.s_rref = f.r_uc;
+    grad_pass(p2m_t, true, a, s, &launches);
+    if (!L.p2l.empty()) {
+        a.q32 = f.f64 ? nullptr : cd32.p;
+        a.q64 = f.f64 ? cd64.p : nullptr;
+        a.s_center = dobs.center.p;
+        a.s_rad = dobs.rad.p;
+        a.s_rref = f.r_dc;
+        grad_pass(p2l_t, true, a, s, &launches);
+    }
+    // to the caller's order (device scratch, then wherever the caller's arrays are)
+    grad_scatter_kernel<<<blocks_for(NS), 256, 0, s>>>(g7, dsrc->perm.p, dsrc->w.p, NS, gu, gu + 3 * NS,
+                                                       gu + 6 * NS);
+    TBEM_CK(cudaGetLastError());
+    if (g_y) TBEM_CK(cudaMemcpyAsync(g_y, gu, sizeof(double) * 3 * NS, cudaMemcpyDefault, s));
+    if (g_n) TBEM_CK(cudaMemcpyAsync(g_n, gu + 3 * NS, sizeof(double) * 3 * NS, cudaMemcpyDefault, s));
+    if (g_w) TBEM_CK(cudaMemcpyAsync(g_w, gu + 6 * NS, sizeof(double) * NS, cudaMemcpyDefault, s));
+    check_tc_flags(true, s);
+}
+
 }  // namespace tbem
 
 extern "C" int tbem_direct_gradients(int kernel, const double* kernel_params,

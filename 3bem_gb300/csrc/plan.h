@@ -436,6 +436,13 @@ struct Plan {
     void finish_build(const double* o_locs, const double* o_nrm, const double* s_locs,
                       const double* s_nrm, const double* s_w);
     void apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adjoint);
+    // Derivatives of L = r^T A x with respect to the source points'
+    // positions, normals and weights (device arrays [n_src][3], [n_src][3],
+    // [n_src] in the caller's order; any may be null) through the transposed
+    // passes of the compressed forms (grad.cu).
+    void source_gradients(const double* x, const double* r, double* g_y, double* g_n, double* g_w,
+                          cudaStream_t s);
+    DBuf<double> grad_buf;  // source_gradients' work arrays
     void set_c2e(int which, long level, const double* op);
     void get_c2e(int which, long level, double* out) const;
 

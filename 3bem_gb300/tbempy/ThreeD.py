@@ -239,6 +239,29 @@ class FMMOperator(OperatorI):
         """w = A^T z (the FMM passes transposed, in reverse order)."""
         return self._run(_L.lib().tbem_fmm_apply_adjoint, z, self.n_rows(), self.n_cols())
 
+    def source_gradients(self, x, r):
+        """Derivatives of L = r^T A x (one right-hand side) with respect to
+        the source points' positions, normals and weights, through the FMM
+        (the compressed forms): a dict keyed src_locs [n_src, 3],
+        src_normals [n_src, 3], src_weights [n_src], numpy or float64 CUDA
+        tensors like x."""
+        is_t = torch is not None and isinstance(x, torch.Tensor)
+        n = self.n_cols() // self.K.tensor_dim
+        if is_t:
+            xx, rr = x.reshape(-1).contiguous(), r.reshape(-1).contiguous()
+            out = {k: torch.empty(s, dtype=torch.float64, device=xx.device)
+                   for k, s in (("src_locs", (n, 3)), ("src_normals", (n, 3)), ("src_weights", (n,)))}
+        else:
+            xx, rr = _f64(x, (-1,)), _f64(r, (-1,))
+            out = {"src_locs": np.empty((n, 3)), "src_normals": np.empty((n, 3)),
+                   "src_weights": np.empty(n)}
+        if xx.shape[0] != self.n_cols() or rr.shape[0] != self.n_rows():
+            raise ValueError("x has n_cols and r n_rows entries (one right-hand side)")
+        check(_L.lib().tbem_fmm_source_gradients(
+            self._h, _ptr(xx), _ptr(rr), _ptr(out["src_locs"]), _ptr(out["src_normals"]),
+            _ptr(out["src_weights"]), _stream_of(xx)))
+        return out
+
     def clone(self):
         h = C.c_void_p()
         check(_L.lib().tbem_fmm_clone(self._h, C.byref(h)))

@@ -29,6 +29,34 @@ def fmm_apply(op, x):
     return _OperatorApply.apply(x, op)
 
 
+class _SourceGeometryApply(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, src_locs, src_normals, src_weights, x, op):
+        ctx.op = op
+        ctx.save_for_backward(x)
+        return op.apply(x.contiguous())
+
+    @staticmethod
+    def backward(ctx, grad):
+        (x,) = ctx.saved_tensors
+        g = ctx.op.source_gradients(x.detach().contiguous(), grad.contiguous())
+        gx = ctx.op.apply_adjoint(grad.contiguous())
+        return g["src_locs"], g["src_normals"], g["src_weights"], gx, None
+
+
+def fmm_apply_sources(op, src_locs, src_normals, src_weights, x):
+    """Differentiable y = A x whose gradients also reach the source geometry.
+
+    ``op`` is an FMMOperator (a compressed form) built at the values of
+    ``src_locs`` [n, 3], ``src_normals`` [n, 3] and ``src_weights`` [n]
+    (float64 CUDA tensors, e.g. computed from mesh vertices that require
+    grad); x is the density [n_cols].  The backward pass runs the operator's
+    transposed apply for x and ``source_gradients`` (the FMM's transposed
+    passes with the kernel's derivatives) for the geometry: O(N), where the
+    direct kernel-gradient pass (``direct_apply``) is O(N M)."""
+    return _SourceGeometryApply.apply(src_locs, src_normals, src_weights, x, op)
+
+
 def misfit(op, s, d):
     """L = 0.5 ||A s - d||^2 (the differentiated workload's loss)."""
     r = fmm_apply(op, s) - d

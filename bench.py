@@ -606,7 +606,7 @@ def misfit_config():
                     "min_pts_per_cell": LEAF, "d": D, "account_for_small_cells": False},
             "step": "one gradient dL/ds: a forward apply and a transposed apply (value counts "
                     "the observation points of the forward apply)",
-            "precision": "mixed (M2L between the two trees evaluated on the fly in FP64)",
+            "precision": "mixed (both trees cut from one cube: compressed tensor-core M2L)",
             "l2": "flushed before every timed step (256 MB write, outside the step timing)"}
 
 
@@ -667,18 +667,27 @@ def run_misfit(args, rank, world, local):
         ms = _events_ms(torch, grad_step, args.steps, stream, flush)
         ms_fwd = _events_ms(torch, lambda: op.apply(s), args.steps, stream, flush)
     phases = _phases(op, lambda: op.apply(s))
-    # the vertex-coordinate gradient (kernel-gradient pass of the direct operator)
+    # the vertex-coordinate gradient: the FMM's source gradients (transposed
+    # passes with the kernel's derivatives) through torch's chain rule from the
+    # vertices to the points, normals and weights; the direct kernel-gradient
+    # pass (O(N M)) beside it as the check
     V = torch.tensor(v, device="cuda", requires_grad=True)
     OL, ON = torch.tensor(obs, device="cuda"), torch.tensor(on, device="cuda")
 
-    def vertex_grad():
+    def vertex_grad(use_fmm):
         V.grad = None
         a, b, c = meshes.points_from_mesh_torch(V, t)
-        y = autograd.direct_apply(K, OL, ON, a, b, c, s)
+        y = (autograd.fmm_apply_sources(op, a, b, c, s) if use_fmm
+             else autograd.direct_apply(K, OL, ON, a, b, c, s))
         (0.5 * ((y - d) ** 2).sum()).backward()
 
-    vertex_grad()
-    ms_vert = _events_ms(torch, vertex_grad, 2, stream)
+    vertex_grad(True)
+    gv_fmm = V.grad.clone()
+    ms_vert = _events_ms(torch, lambda: vertex_grad(True), args.steps, stream)
+    vertex_grad(False)
+    gv_dir = V.grad.clone()
+    ms_vert_direct = _events_ms(torch, lambda: vertex_grad(False), 1, stream)
+    err_vert = float(torch.linalg.norm(gv_fmm - gv_dir) / torch.linalg.norm(gv_dir))
     g = grad_step().cpu().numpy()
     r = Dop.apply(s_np) - d.cpu().numpy()
     gd = ThreeD.direct_gradients(K, obs, on, sl, sn, sw, s_np, r)["x"]
@@ -691,8 +700,10 @@ def run_misfit(args, rank, world, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic (seeded bumpy fault, free-surface observers)", "config": misfit_config(),
         "clocks": clk.summary(), "gpu_launches": 2 * op.last_launches() * args.steps,
-        "forward_ms": ms_fwd, "vertex_gradient_ms": ms_vert, "phases_ms_forward": phases,
-        "rel_err_vs_direct": {"forward": err_f, "gradient_ds": err}, "setup_s": setup_s,
+        "forward_ms": ms_fwd, "vertex_gradient_ms": ms_vert,
+        "vertex_gradient_direct_ms": ms_vert_direct, "phases_ms_forward": phases,
+        "rel_err_vs_direct": {"forward": err_f, "gradient_ds": err,
+                              "gradient_vertices_fmm_vs_direct_pass": err_vert}, "setup_s": setup_s,
         "setup_phases_s": setup_phases([op])}), flush=True)
 
 

@@ -178,6 +178,21 @@ int tbem_fmm_set_wait_cycles(TbemFmm* h, long long cycles);
  * ElasticAdjointTraction (cpp/elastic_kernels.h:272-311). */
 int tbem_fmm_apply_adjoint(TbemFmm* h, const double* z, double* w, int n_rhs, void* stream);
 
+/* Source-side gradients of L = r^T A x (one right-hand side) through the
+ * FMM: derivatives with respect to the source points' positions
+ * (g_src_locs [n_src][3]), normals (g_src_normals [n_src][3]) and weights
+ * (g_src_weights [n_src]); any output may be NULL.  One transposed apply of
+ * r, then the three transposed passes that reach source points (near
+ * field, points to up-check surfaces, points to down-check surfaces) again
+ * with the kernel's exact derivatives (FP64 dual numbers), the far field
+ * entering through the transposed check-surface states of that apply
+ * (recomputed per call, nothing stored).  The O(N) counterpart of
+ * tbem_direct_gradients' source outputs for the compressed forms (precision
+ * and FP64 compressed; TBEM_ERR_STATE for the plain and batched forms).
+ * Synchronous.  No reference counterpart. */
+int tbem_fmm_source_gradients(TbemFmm* h, const double* x, const double* r, double* g_src_locs,
+                              double* g_src_normals, double* g_src_weights, void* stream);
+
 /* OperatorI::n_rows / n_cols (cpp/operator.h:15-16, cpp/fmm.h:235-236). */
 long tbem_fmm_n_rows(const TbemFmm* h);
 long tbem_fmm_n_cols(const TbemFmm* h);

@@ -56,6 +56,59 @@ def test_misfit_gradient_matches_transpose_and_finite_differences(prec):
         assert abs(fd - g[j]) <= fd_tol * max(1.0, np.abs(g).max())
 
 
+@pytest.mark.parametrize("prec", ["mixed", "fp64_compressed"])
+@pytest.mark.parametrize("name", ["LaplaceSingle", "LaplaceDouble", "ElasticDisplacement",
+                                  "ElasticTraction"])
+@pytest.mark.parametrize("distinct", [False, True])
+def test_fmm_source_gradients_match_the_direct_pass(name, distinct, prec):
+    """tbem_fmm_source_gradients (the FMM's transposed passes with the
+    kernel's derivatives) against the direct kernel-gradient pass: positions,
+    normals and weights of the sources, to the form's approximation error."""
+    from tbempy import ThreeD
+    src, sn, w = cloud(600, 11)
+    obs, on = (src, sn) if not distinct else cloud(500, 12)[:2]
+    K = ThreeD.ElasticDisplacement(1.0, 0.25) if name == "ElasticDisplacement" else \
+        ThreeD.ElasticTraction(1.0, 0.25) if name == "ElasticTraction" else getattr(ThreeD, name)()
+    op = ThreeD.FMMOperator(K, obs, on, src, sn, w, ThreeD.FMMConfig(0.3, 296, 30, 0.05, False),
+                            precision=prec)
+    rng = np.random.default_rng(13)
+    x = rng.uniform(-1, 1, op.n_cols())
+    r = rng.uniform(-1, 1, op.n_rows())
+    op.apply(rng.uniform(-1, 1, op.n_cols()))  # leave other states in the work buffers
+    g = op.source_gradients(x, r)
+    gd = ThreeD.direct_gradients(K, obs, on, src, sn, w, x, r)
+    tol = 2e-5 if prec == "mixed" else 2e-6
+    for k in ("src_locs", "src_weights") + (("src_normals",) if name in ("LaplaceDouble", "ElasticTraction") else ()):
+        err = np.linalg.norm(g[k] - gd[k]) / np.linalg.norm(gd[k])
+        assert err < tol, (k, err)
+
+
+def test_fmm_vertex_gradient_through_autograd():
+    """fmm_apply_sources: the misfit's gradient with respect to mesh vertices
+    (points, normals and weights from the vertices by torch) through the
+    FMM's source gradients equals the direct kernel-gradient pass's."""
+    torch = pytest.importorskip("torch")
+    from tbempy import ThreeD, autograd, meshes
+    v, t, obs, on, _, _, _ = meshes.misfit_workload(n=12, n_obs=400)
+    sl, sn, sw = meshes.points_from_mesh(v, t)
+    K = ThreeD.ElasticDisplacement(1.0, 0.25)
+    op = ThreeD.FMMOperator(K, obs, on, sl, sn, sw, ThreeD.FMMConfig(0.3, 296, 30, 0.05, False),
+                            precision="mixed")
+    s = torch.tensor(np.random.default_rng(4).uniform(-1, 1, op.n_cols()), device="cuda")
+    d = torch.tensor(np.random.default_rng(5).normal(size=op.n_rows()), device="cuda")
+    OL, ON = torch.tensor(obs, device="cuda"), torch.tensor(on, device="cuda")
+    grads = []
+    for use_fmm in (True, False):
+        V = torch.tensor(v, device="cuda", requires_grad=True)
+        a, b, c = meshes.points_from_mesh_torch(V, t)
+        y = (autograd.fmm_apply_sources(op, a, b, c, s) if use_fmm
+             else autograd.direct_apply(K, OL, ON, a, b, c, s))
+        (0.5 * ((y - d) ** 2).sum()).backward()
+        grads.append(V.grad.cpu().numpy())
+    err = np.linalg.norm(grads[0] - grads[1]) / np.linalg.norm(grads[1])
+    assert err < 2e-5, err
+
+
 def test_plain_fmm_linearity_floor():
     """The reference's FMM formulation is linear only up to ~1e-9: its
     pseudo-inverse (condition ~1e9) turns rounding into input-dependent noise.
