@@ -141,17 +141,24 @@ __device__ __forceinline__ void influence(const NfArgs& a, int f, const double* 
 {
     const double* c = a.fac + 9 * f;
     double y[3], bas[3];
+    // ref_to_real (cpp/numerics.h:81-100): left to right, every product
+    // rounded (no contraction), the positions the farfield's source points
+    // have too -- near a facet the kernel turns a one-ulp move of the point
+    // into ~1e-12 of a ~1e5 entry, which the farfield and this correction only
+    // cancel when both see the same point
     if (DIM == 2) {
-        bas[0] = 0.5 - 0.5 * xh0;
-        bas[1] = 0.5 + 0.5 * xh0;
-        y[0] = bas[0] * c[0] + bas[1] * c[3];
-        y[1] = bas[0] * c[1] + bas[1] * c[4];
+        bas[0] = __dsub_rn(0.5, __dmul_rn(0.5, xh0));
+        bas[1] = __dadd_rn(0.5, __dmul_rn(0.5, xh0));
+        y[0] = __dadd_rn(__dmul_rn(bas[0], c[0]), __dmul_rn(bas[1], c[3]));
+        y[1] = __dadd_rn(__dmul_rn(bas[0], c[1]), __dmul_rn(bas[1], c[4]));
         y[2] = 0.0;
     } else {
-        bas[0] = 1 - xh0 - xh1;
+        bas[0] = __dsub_rn(__dsub_rn(1.0, xh0), xh1);
         bas[1] = xh0;
         bas[2] = xh1;
-        for (int d = 0; d < 3; d++) y[d] = bas[0] * c[d] + bas[1] * c[3 + d] + bas[2] * c[6 + d];
+        for (int d = 0; d < 3; d++)
+            y[d] = __dadd_rn(__dadd_rn(__dmul_rn(bas[0], c[d]), __dmul_rn(bas[1], c[3 + d])),
+                             __dmul_rn(bas[2], c[6 + d]));
     }
     double K[9];
     const double* n = a.fn + 3 * f;

@@ -217,7 +217,14 @@ def quadrature_points(mesh, order):
     x, w = gauss_facet(dim, order)
     c = mesh.corners()
     bas = _basis(x, dim)
-    locs = np.einsum("qb,fbd->fqd", bas, c).reshape(-1, dim)
+    # ref_to_real (cpp/numerics.h:81-100): the basis dotted with the corners
+    # left to right, each product rounded -- the positions the nearfield
+    # construction's far rule uses too (nearfield.cu: influence), so a
+    # farfield and its correction cancel to rounding of their own size
+    locs = bas[None, :, 0, None] * c[:, None, 0, :]
+    for b in range(1, dim):
+        locs = locs + bas[None, :, b, None] * c[:, None, b, :]
+    locs = locs.reshape(-1, dim)
     if dim == 2:
         d = c[:, 1] - c[:, 0]
         n = np.stack([-d[:, 1], d[:, 0]], axis=1)
