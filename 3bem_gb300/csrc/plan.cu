@@ -2163,10 +2163,13 @@ void Plan::read_phases()
     std::vector<std::pair<std::string, double>> sum;
     int applies = 0;
     for (size_t i = 0; i < marks.size(); i++) {
-        if (marks[i].first == "start") {
+        // "apply" opens an apply; "start" a right-hand-side chunk of it (the
+        // copies and the time between chunks belong to no phase)
+        if (marks[i].first == "apply") {
             applies++;
             continue;
         }
+        if (marks[i].first == "start") continue;
         if (i == 0) continue;
         float ms = 0.f;
         TBEM_CK(cudaEventElapsedTime(&ms, marks[i - 1].second, marks[i].second));
@@ -2610,6 +2613,7 @@ void Plan::apply(const double* x, double* y, int nrhs, cudaStream_t s, bool adj)
     io_y.ensure((size_t)n_out * nrhs);
     ensure_rhs(chunk);
     launches = 0;
+    mark("apply", s);  // phase means are per apply, whatever the right-hand-side chunks
     TBEM_CK(cudaMemcpyAsync(io_x.p, x, sizeof(double) * n_in * nrhs,
                             x_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
     for (int r0 = 0; r0 < nrhs; r0 += chunk) {
