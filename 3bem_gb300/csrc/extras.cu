@@ -67,22 +67,45 @@ __global__ void weight_kernel(const double* x, const double* w, double* s, long 
         s[t] = w[t % N] * x[t];
 }
 
-// y = A x (add = 0) or y += A x (add = 1); one warp per row.
-__global__ void csr_kernel(const long* rowptr, const long* col, const double* val, const double* x,
-                           double* y, long n_rows, long n_cols, int nrhs, int add = 0)
+// y = A x (add = 0) or y += A x (add = 1).  L lanes per row (L chosen per
+// matrix from its mean row length): a lane takes the row's entries k = b +
+// lane, + L, ..., CSR_UNROLL of them per step, loading all their values and
+// columns before any gather of x, so every lane keeps CSR_UNROLL independent
+// loads in flight (the gather x[col[k]] waits on the column load: with one
+// entry per lane per step the SpMV was latency-bound at a third of the
+// copy bandwidth); the L partial sums meet in shuffles.
+constexpr int CSR_UNROLL = 4, CSR_THREADS = 256;
+
+template <int L>
+__global__ void __launch_bounds__(CSR_THREADS)
+csr_kernel(const long* __restrict__ rowptr, const long* __restrict__ col, const double* __restrict__ val,
+           const double* __restrict__ x, double* y, long n_rows, long n_cols, int nrhs, int add)
 {
-    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-    const int lane = threadIdx.x % 32;
-    if (warp >= n_rows) return;
-    const long b = rowptr[warp], e = rowptr[warp + 1];
+    const long row = ((long)blockIdx.x * blockDim.x + threadIdx.x) / L;
+    const int lane = threadIdx.x % L;
+    if (row >= n_rows) return;  // whole L-lane groups leave together
+    const unsigned mask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << ((threadIdx.x % 32) / L * L));
+    const long b = rowptr[row], e = rowptr[row + 1];
     for (int r = 0; r < nrhs; r++) {
         const double* xr = x + (long)r * n_cols;
         double acc = 0.0;
-        for (long k = b + lane; k < e; k += 32) acc += val[k] * xr[col[k]];
+        for (long k0 = b + lane; k0 < e; k0 += (long)CSR_UNROLL * L) {
+            double v[CSR_UNROLL];
+            long c[CSR_UNROLL];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            for (int u = 0; u < CSR_UNROLL; u++) {
+                const long k = k0 + (long)u * L;
+                v[u] = k < e ? val[k] : 0.0;
+                c[u] = k < e ? col[k] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < CSR_UNROLL; u++)
+                if (c[u] >= 0) acc += v[u] * xr[c[u]];
+        }
+#pragma unroll
+        for (int o = L / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(mask, acc, o);
         if (lane == 0) {
-            double* d = y + (long)r * n_rows + warp;
+            double* d = y + (long)r * n_rows + row;
             *d = add ? *d + acc : acc;
         }
     }
@@ -153,9 +176,28 @@ double fma_peak(int device)
 
 struct TbemCsr {
     long n_rows = 0, n_cols = 0, nnz = 0;
+    int lanes = 32;  // lanes per row of the SpMV kernel
     tbem::DBuf<long> rowptr, col;
     tbem::DBuf<double> val;
 };
+
+namespace {
+// y (+)= A x on stream s (A non-empty)
+void csr_launch(const TbemCsr* A, const double* x, double* y, int nrhs, int add, cudaStream_t s)
+{
+    const int L = A->lanes;
+    const unsigned blocks = (unsigned)((A->n_rows * L + CSR_THREADS - 1) / CSR_THREADS);
+    auto go = [&](auto kern) {
+        kern<<<blocks, CSR_THREADS, 0, s>>>(A->rowptr.p, A->col.p, A->val.p, x, y, A->n_rows, A->n_cols,
+                                            nrhs, add);
+    };
+    if (L == 4) go(csr_kernel<4>);
+    else if (L == 8) go(csr_kernel<8>);
+    else if (L == 16) go(csr_kernel<16>);
+    else go(csr_kernel<32>);
+    TBEM_CK(cudaGetLastError());
+}
+}  // namespace
 
 extern "C" {
 
@@ -262,6 +304,9 @@ int tbem_csr_create(long n_rows, long n_cols, const double* values, const long* 
         h->n_rows = n_rows;
         h->n_cols = n_cols;
         h->nnz = nnz;
+        // lanes per row: the fewest that take a mean row in one unrolled step
+        const double mean = n_rows > 0 ? (double)nnz / (double)n_rows : 0.0;
+        h->lanes = mean <= 4 * CSR_UNROLL ? 4 : mean <= 8 * CSR_UNROLL ? 8 : mean <= 16 * CSR_UNROLL ? 16 : 32;
         h->rowptr.upload(row_ptrs, (size_t)n_rows + 1);
         if (nnz > 0) {
             h->col.upload(column_indices, (size_t)nnz);
@@ -294,9 +339,7 @@ int tbem_csr_apply(TbemCsr* h, const double* x, double* y, int n_rhs, void* stre
         } else {
             Staged xs;
             stage(xs, x, (size_t)h->n_cols * n_rhs, s);
-            const long threads = h->n_rows * 32;
-            csr_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(h->rowptr.p, h->col.p, h->val.p, xs.p, yd, h->n_rows, h->n_cols, n_rhs);
-            TBEM_CK(cudaGetLastError());
+            csr_launch(h, xs.p, yd, n_rhs, 0, s);
         }
         if (!y_dev) TBEM_CK(cudaMemcpyAsync(y, yd, ny * sizeof(double), cudaMemcpyDeviceToHost, s));
         TBEM_CK(cudaStreamSynchronize(s));
@@ -355,10 +398,7 @@ void csr_into(const TbemCsr* A, const double* x, double* y, int nrhs, int add, c
         if (!add) TBEM_CK(cudaMemsetAsync(y, 0, sizeof(double) * A->n_rows * nrhs, s));
         return;
     }
-    const long threads = A->n_rows * 32;
-    csr_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(A->rowptr.p, A->col.p, A->val.p, x, y,
-                                                                 A->n_rows, A->n_cols, nrhs, add);
-    TBEM_CK(cudaGetLastError());
+    csr_launch(A, x, y, nrhs, add, s);
 }
 }  // namespace
 
