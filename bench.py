@@ -239,6 +239,14 @@ def config_dict(n_rhs):
             "l2": "flushed before every timed step (256 MB write, outside the step timing)"}
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the tensor-core M2L kernel on the default workload, from a one-pass ncu
+# capture of this bench (ncu --metrics dram__bytes_read.sum,
+# dram__bytes_write.sum --clock-control none -k regex:tc_gemm -s 40 -c 1
+# python bench.py --steps 2 --warmup 3 --no-cpu --no-plain)
+M2L_TC_DRAM_BYTES = 59.8e6
+
+
 def _events_ms(torch, fn, steps, stream, flush=None):
     """Mean device milliseconds of fn over `steps` runs, CUDA events on the
     stream the work is issued to (L2 flushed before each when given)."""
@@ -1062,11 +1070,8 @@ def main():
     achieved = per_launch / launch_s / 1e12
     ref_form = float(np.mean([f["reference"] for f in fl]))
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath) and tensor and args.grid == N_GRID and n_rhs == 1:
-        # DRAM bytes of one launch of the tensor kernel on this workload, from a
-        # one-pass ncu capture of this bench
-        traffic = json.load(open(tpath)).get("m2l_tc_dram_bytes_per_launch")
+    if tensor and args.grid == N_GRID and n_rhs == 1:
+        traffic = M2L_TC_DRAM_BYTES
 
     # -- the plain FP64 form on the same workload
     plain = None
