@@ -159,14 +159,11 @@ eval_kernel(const EvalArgs<T> a)
     // double-float n . d (lapd_near_df), the block's flag in the position's w
     constexpr bool DF = SPLIT && KID == LAP_D && !TRANS;
     // per source: position, normal, and the R density components of every
-    // right-hand side, each a 4-vector (one shared load in the pair loop).
-    // FP32: two buffers, so the next tile's global loads are in flight (in
-    // registers) while this tile's pairs run, and one barrier per tile
-    constexpr int NB = COMP ? 2 : 1;
-    __shared__ Vec4<T> sp[NB][EVAL_THREADS], sn[NB][EVAL_THREADS];
-    __shared__ Vec4<T> sl[NB][SPLIT ? EVAL_THREADS : 1];  // low parts of the positions
-    __shared__ Vec4<T> snl[NB][DF ? EVAL_THREADS : 1];    // low parts of the normals
-    __shared__ Vec4<T> sv[NB][NV][EVAL_THREADS];
+    // right-hand side, each a 4-vector (one shared load in the pair loop)
+    __shared__ Vec4<T> sp[EVAL_THREADS], sn[EVAL_THREADS];
+    __shared__ Vec4<T> sl[SPLIT ? EVAL_THREADS : 1];  // low parts of the positions
+    __shared__ Vec4<T> snl[DF ? EVAL_THREADS : 1];    // low parts of the normals
+    __shared__ Vec4<T> sv[NV][EVAL_THREADS];
 
     const int task = a.item_task[blockIdx.x];
     const int t0 = a.item_start[blockIdx.x];
@@ -207,99 +204,81 @@ eval_kernel(const EvalArgs<T> a)
     const int total = b1 > b0 ? a.src_blk_prefix[b1 - 1] + a.src_blk_count[b1 - 1] : 0;
     const int nr_here = min(NR, a.nrhs - a.rhs0);
     int blk = b0;  // block containing this thread's next slot (advances monotonically)
-    struct Slot {
-        Vec4<T> p, n, l, nl, v[NV];
-    };
-    // one source of the task (slot g) into registers
-    auto load = [&](int g, Slot& st) {
-        while (blk + 1 < b1 && a.src_blk_prefix[blk + 1] <= g) blk++;
-        const int li = g - a.src_blk_prefix[blk];
-        const long sb = a.src_blk[blk];
-        double qx, qy, qz;
-        T nx, ny, nz;
-        if (SRC_SURF) {
-            const double r = a.s_rad[sb];
-            const double ux = a.unit[3 * li], uy = a.unit[3 * li + 1], uz = a.unit[3 * li + 2];
-            qx = r * (a.s_rref * ux) + a.s_center[3 * sb];
-            qy = r * (a.s_rref * uy) + a.s_center[3 * sb + 1];
-            qz = r * (a.s_rref * uz) + a.s_center[3 * sb + 2];
-            nx = T(ux); ny = T(uy); nz = T(uz);
-            const int cn = R * a.ns;
-#pragma unroll
-            for (int r_ = 0; r_ < NR; r_++) {
-                T vv[3] = {T(0), T(0), T(0)};
-#pragma unroll
-                for (int d = 0; d < R; d++)
-                    vv[d] = r_ < nr_here ? a.q[(sb * a.nrhs + a.rhs0 + r_) * cn + d * a.ns + li] : T(0);
-                st.v[r_] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
-            }
-        } else {
-            const long p = sb + li;
-            qx = a.s_xyz[3 * p]; qy = a.s_xyz[3 * p + 1]; qz = a.s_xyz[3 * p + 2];
-            nx = a.s_nrm[3 * p]; ny = a.s_nrm[3 * p + 1]; nz = a.s_nrm[3 * p + 2];
-            if constexpr (PACK) {
-#pragma unroll
-                for (int r4 = 0; r4 < NV; r4++) {
-                    T vv[4];
-#pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        const int r_ = 4 * r4 + k;
-                        vv[k] = r_ < nr_here ? a.s_str[(long)(a.rhs0 + r_) * a.s_n + p] : T(0);
-                    }
-                    st.v[r4] = Vec4<T>{vv[0], vv[1], vv[2], vv[3]};
-                }
-            } else {
+    for (int tile = 0; tile < total; tile += EVAL_THREADS) {
+        const int g = tile + threadIdx.x;
+        if (g < total) {
+            while (blk + 1 < b1 && a.src_blk_prefix[blk + 1] <= g) blk++;
+            const int li = g - a.src_blk_prefix[blk];
+            const long sb = a.src_blk[blk];
+            double qx, qy, qz;
+            T nx, ny, nz;
+            if (SRC_SURF) {
+                const double r = a.s_rad[sb];
+                const double ux = a.unit[3 * li], uy = a.unit[3 * li + 1], uz = a.unit[3 * li + 2];
+                qx = r * (a.s_rref * ux) + a.s_center[3 * sb];
+                qy = r * (a.s_rref * uy) + a.s_center[3 * sb + 1];
+                qz = r * (a.s_rref * uz) + a.s_center[3 * sb + 2];
+                nx = T(ux); ny = T(uy); nz = T(uz);
+                const int cn = R * a.ns;
 #pragma unroll
                 for (int r_ = 0; r_ < NR; r_++) {
                     T vv[3] = {T(0), T(0), T(0)};
 #pragma unroll
                     for (int d = 0; d < R; d++)
-                        vv[d] = r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
-                    st.v[r_] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                        vv[d] = r_ < nr_here ? a.q[(sb * a.nrhs + a.rhs0 + r_) * cn + d * a.ns + li] : T(0);
+                    sv[r_][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                }
+            } else {
+                const long p = sb + li;
+                qx = a.s_xyz[3 * p]; qy = a.s_xyz[3 * p + 1]; qz = a.s_xyz[3 * p + 2];
+                nx = a.s_nrm[3 * p]; ny = a.s_nrm[3 * p + 1]; nz = a.s_nrm[3 * p + 2];
+                if constexpr (PACK) {
+#pragma unroll
+                    for (int r4 = 0; r4 < NV; r4++) {
+                        T vv[4];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const int r_ = 4 * r4 + k;
+                            vv[k] = r_ < nr_here ? a.s_str[(long)(a.rhs0 + r_) * a.s_n + p] : T(0);
+                        }
+                        sv[r4][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], vv[3]};
+                    }
+                } else {
+#pragma unroll
+                    for (int r_ = 0; r_ < NR; r_++) {
+                        T vv[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                        for (int d = 0; d < R; d++)
+                            vv[d] = r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
+                        sv[r_][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                    }
                 }
             }
+            const double rx = qx - ox, ry = qy - oy, rz = qz - oz;
+            const bool near = DF && a.src_blk_near && a.src_blk_near[blk];
+            const Vec4<T> hi{T(rx), T(ry), T(rz), near ? T(1) : T(0)};
+            sp[threadIdx.x] = hi;
+            if (SPLIT)
+                sl[threadIdx.x] = Vec4<T>{T(rx - double(hi.x)), T(ry - double(hi.y)), T(rz - double(hi.z)), T(0)};
+            if (near) {
+                const long p = sb + li;
+                const double mx = a.s_nrm64[3 * p], my = a.s_nrm64[3 * p + 1], mz = a.s_nrm64[3 * p + 2];
+                nx = T(mx); ny = T(my); nz = T(mz);
+                snl[threadIdx.x] = Vec4<T>{T(mx - double(nx)), T(my - double(ny)), T(mz - double(nz)), T(0)};
+            }
+            sn[threadIdx.x] = Vec4<T>{nx, ny, nz, T(0)};
         }
-        const double rx = qx - ox, ry = qy - oy, rz = qz - oz;
-        const bool near = DF && a.src_blk_near && a.src_blk_near[blk];
-        st.p = Vec4<T>{T(rx), T(ry), T(rz), near ? T(1) : T(0)};
-        if (SPLIT)
-            st.l = Vec4<T>{T(rx - double(st.p.x)), T(ry - double(st.p.y)), T(rz - double(st.p.z)), T(0)};
-        if (near) {
-            const long p = sb + li;
-            const double mx = a.s_nrm64[3 * p], my = a.s_nrm64[3 * p + 1], mz = a.s_nrm64[3 * p + 2];
-            nx = T(mx); ny = T(my); nz = T(mz);
-            st.nl = Vec4<T>{T(mx - double(nx)), T(my - double(ny)), T(mz - double(nz)), T(0)};
-        }
-        st.n = Vec4<T>{nx, ny, nz, T(0)};
-    };
-    auto store = [&](int buf, const Slot& st) {
-        sp[buf][threadIdx.x] = st.p;
-        sn[buf][threadIdx.x] = st.n;
-        if (SPLIT) sl[buf][threadIdx.x] = st.l;
-        if (DF) snl[buf][threadIdx.x] = st.nl;
-#pragma unroll
-        for (int r_ = 0; r_ < NV; r_++) sv[buf][r_][threadIdx.x] = st.v[r_];
-    };
-    Slot st;
-    if ((int)threadIdx.x < total) load(threadIdx.x, st);
-    int buf = 0;
-    for (int tile = 0; tile < total; tile += EVAL_THREADS) {
-        const int g_next = tile + EVAL_THREADS + threadIdx.x;
-        if (tile + (int)threadIdx.x < total) store(buf, st);
         __syncthreads();
-        // the next tile's sources: their loads land while this tile's pairs run
-        if (NB == 2 && g_next < total) load(g_next, st);
         if (active) {
             const int n_here = min(EVAL_THREADS, total - tile);
             for (int j = lane; j < n_here; j += TPT) {
-                const Vec4<T> q = sp[buf][j];
+                const Vec4<T> q = sp[j];
                 if constexpr (DF) {
                     if (q.w != T(0)) {
-                        const T kv = lapd_near_df(q, sl[buf][j], sn[buf][j], snl[buf][j], px, py, pz, plx,
-                                                  ply, plz);
+                        const T kv = lapd_near_df(q, sl[j], sn[j], snl[j], px, py, pz, plx, ply, plz);
 #pragma unroll
                         for (int r4 = 0; r4 < NV; r4++) {
-                            const Vec4<T> vq = sv[buf][r4][j];
+                            const Vec4<T> vq = sv[r4][j];
                             if constexpr (PACK) {
                                 part[4 * r4] += kv * vq.x;
                                 part[4 * r4 + 1] += kv * vq.y;
@@ -315,10 +294,10 @@ eval_kernel(const EvalArgs<T> a)
                 T dx = q.x - px, dy = q.y - py, dz = q.z - pz;
                 if (SPLIT) {
                     // (q_hi - p_hi) + (q_lo - p_lo): rounding errors O(eps |d|)
-                    const Vec4<T> ql = sl[buf][j];
+                    const Vec4<T> ql = sl[j];
                     dx += ql.x - plx; dy += ql.y - ply; dz += ql.z - plz;
                 }
-                const Vec4<T> nq = sn[buf][j];
+                const Vec4<T> nq = sn[j];
                 if constexpr (PACK) {
                     // the kernel value once (accumulate with a unit density)
                     T kv = 0;
@@ -326,7 +305,7 @@ eval_kernel(const EvalArgs<T> a)
                     accumulate<KID, false, T>(dx, dy, dz, pnx, pny, pnz, nq.x, nq.y, nq.z, a.c2, one, &kv);
 #pragma unroll
                     for (int r4 = 0; r4 < NV; r4++) {
-                        const Vec4<T> vq = sv[buf][r4][j];
+                        const Vec4<T> vq = sv[r4][j];
                         part[4 * r4] += kv * vq.x;
                         part[4 * r4 + 1] += kv * vq.y;
                         part[4 * r4 + 2] += kv * vq.z;
@@ -336,7 +315,7 @@ eval_kernel(const EvalArgs<T> a)
                 }
 #pragma unroll
                 for (int r_ = 0; r_ < NR; r_++) {
-                    const Vec4<T> vq = sv[buf][r_][j];
+                    const Vec4<T> vq = sv[r_][j];
                     const T v[3] = {vq.x, vq.y, vq.z};
                     // transposed apply: the target is the forward source and
                     // the source the forward observer, so the separation
@@ -354,12 +333,7 @@ eval_kernel(const EvalArgs<T> a)
                 for (int i = 0; i < NR * R; i++) { kahan_add(acc[i], lo[i], part[i]); part[i] = 0; }
             }
         }
-        if (NB == 1) {
-            // one buffer: every thread is done with it before it is refilled
-            __syncthreads();
-            if (g_next < total) load(g_next, st);
-        }
-        buf ^= NB - 1;
+        __syncthreads();
     }
     if (!COMP) {
 #pragma unroll
