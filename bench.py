@@ -236,6 +236,9 @@ def config_dict(n_rhs):
             "n_points": 3 * 2 * N_GRID * N_GRID, "n_rhs": n_rhs,
             "precision": "mixed: far field in the M2L SVD bases (FP32), M2L products on "
                          "tcgen05 3xBF16, P2P FP32 compensated",
+            "step": "one displacement apply and one traction apply, replayed as one CUDA graph "
+                    "with the two applies in parallel branches (tbem_fmm_graph_launch); "
+                    "ms_per_step_sequential: the same applies one after the other",
             "l2": "flushed before every timed step (256 MB write, outside the step timing)"}
 
 
@@ -979,39 +982,57 @@ def main():
     n_rhs = args.rhs
     X = np.ascontiguousarray(np.tile(x, (n_rhs, 1)))
     xd = torch.tensor(X, device="cuda")
+    yd = [torch.empty((n_rhs, op.n_rows()), dtype=torch.float64, device="cuda") for op in ops]
     stream = torch.cuda.current_stream()
+    import ctypes as C
+    sp = C.c_void_p(stream.cuda_stream if stream.cuda_stream else 1)
+    # one step = every operator's apply, replayed as one CUDA graph with the
+    # applies in parallel branches (tbem_fmm_graph_*): the two operators'
+    # latency-bound passes overlap; the same kernels as the applies
+    graph = ThreeD.FMMGraph(ops, [xd] * len(ops), yd, n_rhs=n_rhs)
 
     def step():
+        graph.launch(sp)
+
+    def step_sequential():
         for op in ops:
             op.apply(xd)
 
     for _ in range(args.warmup):
         step()
+        step_sequential()
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
     torch.cuda.synchronize()
 
-    # -- device-resident timed region (per-phase CUDA events recorded on the
-    # operators' stream inside it, read after it)
-    for op in ops:
-        op.phase_times()  # drop the warm-up marks
-        op.set_timing(True)
-    with ClockSampler(local) as clk:
+    def timed_region(fn):
+        """Mean device ms of fn over args.steps runs, CUDA events on the
+        stream; L2 flushed before every run (a 256 MB write, outside the
+        events): the M2L operator planes alone would fit in L2."""
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
-        # L2 flushed before every timed step (a 256 MB write, outside the
-        # step's events): the M2L operator planes alone would fit in L2
         pairs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                  for _ in range(args.steps)]
         for e0, e1 in pairs:
             flush.fill_(1)
             e0.record(stream)
-            step()
+            fn()
             e1.record(stream)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    ms = sum(e0.elapsed_time(e1) for e0, e1 in pairs) / args.steps
+        return sum(e0.elapsed_time(e1) for e0, e1 in pairs) / args.steps
+
+    # -- device-resident timed region: the graph
+    with ClockSampler(local) as clk:
+        ms = timed_region(step)
+        # the same step with the applies one after the other on one stream,
+        # per-phase CUDA events recorded between the passes (read after it):
+        # the phases and the M2L kernel's launch time of the roofline
+        for op in ops:
+            op.phase_times()  # drop the warm-up marks
+            op.set_timing(True)
+        ms_seq = timed_region(step_sequential)
     launches = sum(op.last_launches() for op in ops) * args.steps
     phase = {}       # ms per step (both operators)
     m2l_launch = []  # ms of the M2L kernel per launch, per operator
@@ -1024,17 +1045,18 @@ def main():
     value, sec = aggregate(ms / 1e3, len(ops) * N * n_rhs, dist, "cuda")
     ms = sec * 1e3
 
-    # -- end to end through the C ABI with host buffers (pinned)
+    # -- end to end through the public API with host buffers (pinned): the
+    # slip copied to the device, the graph launched (tbem_fmm_graph_launch),
+    # both results copied back, all inside the timed step
     xh = torch.tensor(X).pin_memory()
     yh = [torch.empty((n_rhs, op.n_rows()), dtype=torch.float64).pin_memory() for op in ops]
-    from tbempy import _lib
-    L = _lib.lib()
-    import ctypes as C
 
     def step_e2e():
-        for op, y in zip(ops, yh):
-            _lib.check(L.tbem_fmm_apply(op._h, C.c_void_p(xh.data_ptr()),
-                                        C.c_void_p(y.data_ptr()), n_rhs, None))
+        xd.copy_(xh, non_blocking=True)
+        graph.launch(sp)
+        for y, d in zip(yh, yd):
+            y.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
 
     for _ in range(2):
         step_e2e()
@@ -1081,6 +1103,7 @@ def main():
         for op in pops:
             op.apply(xd)
         torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for op in pops:
             op.apply(xd)
@@ -1120,9 +1143,10 @@ def main():
             "config": config_dict(n_rhs),
             "clocks": clk.summary(),
             "e2e": {"value": e2e_value, "unit": "points*RHS/s",
-                    "h2d_bytes_per_step": 2 * 8 * X.size,
+                    "h2d_bytes_per_step": 8 * X.size,
                     "d2h_bytes_per_step": 8 * sum(y.numel() for y in yh)},
             "gpu_launches": launches,
+            "ms_per_step_sequential": ms_seq,
             "roofline": {"bound": "tensor",
                          "kernel": ("tc_gemm_kernel: compressed M2L products, tcgen05 3xBF16"
                                     if tensor else "grouped_gemm_kernel: M2L products, FP32 SIMT"),
