@@ -42,11 +42,16 @@ def test_oracle_matches_reference_fixture(path):
     for kind in oracle.LISTS:
         a, b = o.list(kind)
         assert np.array_equal(a, g["list_%s_obs" % kind]) and np.array_equal(b, g["list_%s_src" % kind])
-    # the reference's own check-to-equivalent operators: the apply agrees to rounding
+    # the reference's own check-to-equivalent operators: the apply agrees to
+    # rounding.  The oracle's OpenMP passes add in a thread-dependent order;
+    # where the fixture carries the reference's one-ulp floor (config 1's
+    # size, where that floor is 2.7e-8) a hundredth of it bounds what a
+    # different order of the same sums may move
     for which in (0, 1):
         for lev, op in enumerate(g["c2e%d" % which]):
             o.set_c2e(which, lev, op)
-    assert rel(o.apply(g["x"]), g["y_ref"]) < 1e-12
+    tol = max(1e-12, 0.01 * float(g["ulp_floor"])) if "ulp_floor" in g else 1e-12
+    assert rel(o.apply(g["x"]), g["y_ref"]) < tol
 
 
 @pytest.mark.parametrize("path", CASES, ids=[os.path.basename(p)[4:-4] for p in CASES])
