@@ -919,6 +919,12 @@ void Plan::autotune_tc()
     P.split_b_rows(in, 0, ncs, std::max(ncs, nco), stream);
     ScopedEvent t0, t1;
     const cudaEvent_t e0 = t0.e, e1 = t1.e;
+    // every timed run starts from a cold L2 (a 256 MB write evicts it), as
+    // the M2L of an apply does: with the operator planes left in L2 between
+    // runs the 32-deep shape looked fastest, cold it was 25 % slower
+    DBuf<char> flush;
+    constexpr size_t FLUSH_BYTES = 256u << 20;
+    flush.alloc(FLUSH_BYTES);
     float best = 1e30f;
     int best_bn = 128, best_bk = 64;
     const int shapes[4][2] = {{128, 64}, {64, 64}, {128, 32}, {256, 32}};
@@ -930,6 +936,7 @@ void Plan::autotune_tc()
         G.tc_bk = sh[1];
         float ms = 1e30f;  // best of five (the first also builds the tile tables)
         for (int rep = 0; rep < 6; rep++) {
+            TBEM_CK(cudaMemsetAsync(flush.p, rep, FLUSH_BYTES, stream));
             TBEM_CK(cudaEventRecord(e0, stream));
             G.run_tc(P, out, 1, 1, nn, stream, nullptr);
             TBEM_CK(cudaEventRecord(e1, stream));

@@ -247,7 +247,7 @@ def config_dict(n_rhs):
 # capture of this bench (ncu --metrics dram__bytes_read.sum,
 # dram__bytes_write.sum --clock-control none -k regex:tc_gemm -s 40 -c 1
 # python bench.py --steps 2 --warmup 3 --no-cpu --no-plain)
-M2L_TC_DRAM_BYTES = 59.8e6
+M2L_TC_DRAM_BYTES = 59.53e6
 
 
 def _events_ms(torch, fn, steps, stream, flush=None):
