@@ -1334,9 +1334,13 @@ void Plan::build_form()
     }
     build_c2e(F);
     setup_mark("c2e");
-    if (F.mixed) build_mixed_ops(F);
-    else build_plain_ops(F);
-    setup_mark("operators");
+    if (F.mixed) {
+        build_mixed_ops(F);  // marks "translations" and "compression" inside
+        setup_mark("leaf_operators");
+    } else {
+        build_plain_ops(F);
+        setup_mark("operators");
+    }
 }
 
 namespace {
@@ -1633,6 +1637,7 @@ void Plan::build_mixed_ops(Form& F)
         }
     }
     build_gemm_sets(F, 0, 0, 0, m2m_off, l2l_off, m2l_off);
+    setup_mark("translations");
     F.m2l_compressed = false;
     if (compress) {
         CompressionInput in{U64.p, n_m2l_ops, &m2l_index, KM.p, &m2m_lc, &m2m_index,
@@ -1660,6 +1665,7 @@ void Plan::build_mixed_ops(Form& F)
         F.tc.build(F.ops32.p, (long)jobs.size(), n, n, stream);
         TBEM_CK(cudaStreamSynchronize(stream));
     }
+    setup_mark("compression");
 
     // per-leaf L2P operators E = K(points, down-equiv) * C2E_down(level)
     const Tree& O = otree;

@@ -237,9 +237,12 @@ int tbem_fmm_phase_times(const TbemFmm* h, const char** names, double* ms, int c
 
 /* Wall seconds of the construction phases of this operator, in order
  * (trees_lists: octrees and task lists on the host; upload_tasks: device
- * geometry and work lists; c2e: check-to-equivalent pseudo-inverses;
- * operators: translation tables and their compression; autotune: launch
- * shape choices), the device synchronized at each phase end.  Replaces the
+ * geometry and work lists; c2e: check-to-equivalent pseudo-inverses; then
+ * for the plain form operators: the translation tables, for the precision
+ * forms translations: the translation tables, compression: the M2L SVD
+ * bases and the compressed operators, leaf_operators: the per-leaf L2P
+ * operators; autotune: launch shape choices), the device synchronized at
+ * each phase end.  Replaces the
  * reference's construction inside FMMOperator's constructor
  * (cpp/fmm.cpp:71-101).  names/seconds are NULL-able; returns the number of
  * phases. */

@@ -391,7 +391,8 @@ def test_phase_timing_means_over_applies():
     assert 10.0 < f32 < 400.0 and 0.05 < f64 < f32
     # construction phases, in order
     names = [n for n, _ in op.setup_times()]
-    assert names == ["trees_lists", "upload_tasks", "c2e", "operators", "autotune"]
+    assert names == ["trees_lists", "upload_tasks", "c2e", "translations", "compression",
+                     "leaf_operators", "autotune"]
     assert all(s >= 0 for _, s in op.setup_times())
 
 
