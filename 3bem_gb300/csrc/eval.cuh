@@ -9,8 +9,8 @@
 // one task, so every output is written by exactly one thread: no atomics and
 // a fixed summation order.  TPT threads share a target and split its
 // sources; their partial sums meet in a warp-shuffle reduction.  Sources are
-// staged through shared memory in tiles (256 sources in FP32, two per thread;
-// 128 in FP64) that run across source-block boundaries (each source's position, normal and densities stored as
+// staged through shared memory in tiles of 128 that run across source-block
+// boundaries (each source's position, normal and densities stored as
 // 4-vectors, one shared load each in the pair loop).  Coordinates are
 // shifted to the task's origin (the target
 // cell's centre) in FP64 before the pair arithmetic, so the FP32 variant
@@ -158,15 +158,12 @@ eval_kernel(const EvalArgs<T> a)
     // the double layer's pairs with a source block touching the target leaf:
     // double-float n . d (lapd_near_df), the block's flag in the position's w
     constexpr bool DF = SPLIT && KID == LAP_D && !TRANS;
-    // sources per shared-memory tile: FP32 stages two per thread (half as
-    // many barriers per pair; FP64 keeps one, its tiles are twice the bytes)
-    constexpr int TILE = COMP ? 2 * EVAL_THREADS : EVAL_THREADS;
     // per source: position, normal, and the R density components of every
     // right-hand side, each a 4-vector (one shared load in the pair loop)
-    __shared__ Vec4<T> sp[TILE], sn[TILE];
-    __shared__ Vec4<T> sl[SPLIT ? TILE : 1];  // low parts of the positions
-    __shared__ Vec4<T> snl[DF ? TILE : 1];    // low parts of the normals
-    __shared__ Vec4<T> sv[NV][TILE];
+    __shared__ Vec4<T> sp[EVAL_THREADS], sn[EVAL_THREADS];
+    __shared__ Vec4<T> sl[SPLIT ? EVAL_THREADS : 1];  // low parts of the positions
+    __shared__ Vec4<T> snl[DF ? EVAL_THREADS : 1];    // low parts of the normals
+    __shared__ Vec4<T> sv[NV][EVAL_THREADS];
 
     const int task = a.item_task[blockIdx.x];
     const int t0 = a.item_start[blockIdx.x];
@@ -207,77 +204,73 @@ eval_kernel(const EvalArgs<T> a)
     const int total = b1 > b0 ? a.src_blk_prefix[b1 - 1] + a.src_blk_count[b1 - 1] : 0;
     const int nr_here = min(NR, a.nrhs - a.rhs0);
     int blk = b0;  // block containing this thread's next slot (advances monotonically)
-    for (int tile = 0; tile < total; tile += TILE) {
+    for (int tile = 0; tile < total; tile += EVAL_THREADS) {
+        const int g = tile + threadIdx.x;
+        if (g < total) {
+            while (blk + 1 < b1 && a.src_blk_prefix[blk + 1] <= g) blk++;
+            const int li = g - a.src_blk_prefix[blk];
+            const long sb = a.src_blk[blk];
+            double qx, qy, qz;
+            T nx, ny, nz;
+            if (SRC_SURF) {
+                const double r = a.s_rad[sb];
+                const double ux = a.unit[3 * li], uy = a.unit[3 * li + 1], uz = a.unit[3 * li + 2];
+                qx = r * (a.s_rref * ux) + a.s_center[3 * sb];
+                qy = r * (a.s_rref * uy) + a.s_center[3 * sb + 1];
+                qz = r * (a.s_rref * uz) + a.s_center[3 * sb + 2];
+                nx = T(ux); ny = T(uy); nz = T(uz);
+                const int cn = R * a.ns;
 #pragma unroll
-        for (int h = 0; h < TILE / EVAL_THREADS; h++) {
-            const int slot = threadIdx.x + h * EVAL_THREADS;
-            const int g = tile + slot;
-            if (g < total) {
-                while (blk + 1 < b1 && a.src_blk_prefix[blk + 1] <= g) blk++;
-                const int li = g - a.src_blk_prefix[blk];
-                const long sb = a.src_blk[blk];
-                double qx, qy, qz;
-                T nx, ny, nz;
-                if (SRC_SURF) {
-                    const double r = a.s_rad[sb];
-                    const double ux = a.unit[3 * li], uy = a.unit[3 * li + 1], uz = a.unit[3 * li + 2];
-                    qx = r * (a.s_rref * ux) + a.s_center[3 * sb];
-                    qy = r * (a.s_rref * uy) + a.s_center[3 * sb + 1];
-                    qz = r * (a.s_rref * uz) + a.s_center[3 * sb + 2];
-                    nx = T(ux); ny = T(uy); nz = T(uz);
-                    const int cn = R * a.ns;
-    #pragma unroll
-                    for (int r_ = 0; r_ < NR; r_++) {
-                        T vv[3] = {T(0), T(0), T(0)};
-    #pragma unroll
-                        for (int d = 0; d < R; d++)
-                            vv[d] = r_ < nr_here ? a.q[(sb * a.nrhs + a.rhs0 + r_) * cn + d * a.ns + li] : T(0);
-                        sv[r_][slot] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                for (int r_ = 0; r_ < NR; r_++) {
+                    T vv[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                    for (int d = 0; d < R; d++)
+                        vv[d] = r_ < nr_here ? a.q[(sb * a.nrhs + a.rhs0 + r_) * cn + d * a.ns + li] : T(0);
+                    sv[r_][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
+                }
+            } else {
+                const long p = sb + li;
+                qx = a.s_xyz[3 * p]; qy = a.s_xyz[3 * p + 1]; qz = a.s_xyz[3 * p + 2];
+                nx = a.s_nrm[3 * p]; ny = a.s_nrm[3 * p + 1]; nz = a.s_nrm[3 * p + 2];
+                if constexpr (PACK) {
+#pragma unroll
+                    for (int r4 = 0; r4 < NV; r4++) {
+                        T vv[4];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const int r_ = 4 * r4 + k;
+                            vv[k] = r_ < nr_here ? a.s_str[(long)(a.rhs0 + r_) * a.s_n + p] : T(0);
+                        }
+                        sv[r4][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], vv[3]};
                     }
                 } else {
-                    const long p = sb + li;
-                    qx = a.s_xyz[3 * p]; qy = a.s_xyz[3 * p + 1]; qz = a.s_xyz[3 * p + 2];
-                    nx = a.s_nrm[3 * p]; ny = a.s_nrm[3 * p + 1]; nz = a.s_nrm[3 * p + 2];
-                    if constexpr (PACK) {
-    #pragma unroll
-                        for (int r4 = 0; r4 < NV; r4++) {
-                            T vv[4];
-    #pragma unroll
-                            for (int k = 0; k < 4; k++) {
-                                const int r_ = 4 * r4 + k;
-                                vv[k] = r_ < nr_here ? a.s_str[(long)(a.rhs0 + r_) * a.s_n + p] : T(0);
-                            }
-                            sv[r4][slot] = Vec4<T>{vv[0], vv[1], vv[2], vv[3]};
-                        }
-                    } else {
-    #pragma unroll
-                        for (int r_ = 0; r_ < NR; r_++) {
-                            T vv[3] = {T(0), T(0), T(0)};
-    #pragma unroll
-                            for (int d = 0; d < R; d++)
-                                vv[d] = r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
-                            sv[r_][slot] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
-                        }
+#pragma unroll
+                    for (int r_ = 0; r_ < NR; r_++) {
+                        T vv[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                        for (int d = 0; d < R; d++)
+                            vv[d] = r_ < nr_here ? a.s_str[((long)(a.rhs0 + r_) * R + d) * a.s_n + p] : T(0);
+                        sv[r_][threadIdx.x] = Vec4<T>{vv[0], vv[1], vv[2], T(0)};
                     }
                 }
-                const double rx = qx - ox, ry = qy - oy, rz = qz - oz;
-                const bool near = DF && a.src_blk_near && a.src_blk_near[blk];
-                const Vec4<T> hi{T(rx), T(ry), T(rz), near ? T(1) : T(0)};
-                sp[slot] = hi;
-                if (SPLIT)
-                    sl[slot] = Vec4<T>{T(rx - double(hi.x)), T(ry - double(hi.y)), T(rz - double(hi.z)), T(0)};
-                if (near) {
-                    const long p = sb + li;
-                    const double mx = a.s_nrm64[3 * p], my = a.s_nrm64[3 * p + 1], mz = a.s_nrm64[3 * p + 2];
-                    nx = T(mx); ny = T(my); nz = T(mz);
-                    snl[slot] = Vec4<T>{T(mx - double(nx)), T(my - double(ny)), T(mz - double(nz)), T(0)};
-                }
-                sn[slot] = Vec4<T>{nx, ny, nz, T(0)};
             }
+            const double rx = qx - ox, ry = qy - oy, rz = qz - oz;
+            const bool near = DF && a.src_blk_near && a.src_blk_near[blk];
+            const Vec4<T> hi{T(rx), T(ry), T(rz), near ? T(1) : T(0)};
+            sp[threadIdx.x] = hi;
+            if (SPLIT)
+                sl[threadIdx.x] = Vec4<T>{T(rx - double(hi.x)), T(ry - double(hi.y)), T(rz - double(hi.z)), T(0)};
+            if (near) {
+                const long p = sb + li;
+                const double mx = a.s_nrm64[3 * p], my = a.s_nrm64[3 * p + 1], mz = a.s_nrm64[3 * p + 2];
+                nx = T(mx); ny = T(my); nz = T(mz);
+                snl[threadIdx.x] = Vec4<T>{T(mx - double(nx)), T(my - double(ny)), T(mz - double(nz)), T(0)};
+            }
+            sn[threadIdx.x] = Vec4<T>{nx, ny, nz, T(0)};
         }
         __syncthreads();
         if (active) {
-            const int n_here = min(TILE, total - tile);
+            const int n_here = min(EVAL_THREADS, total - tile);
             for (int j = lane; j < n_here; j += TPT) {
                 const Vec4<T> q = sp[j];
                 if constexpr (DF) {
