@@ -193,7 +193,8 @@ def cpu_calibration(ops, x, fraction):
 
 def run_reference(args, rank, world):
     """--impl reference: the reference algorithm on the host cores (the oracle
-    port; the reference's own build needs its checkout, absent on the GPU machine)."""
+    port; the reference's own build needs its checkout, which does not travel
+    with this repository)."""
     if rank != 0:
         return
     locs, nrm, w, x = workload()
@@ -378,7 +379,7 @@ def run_sphere(args, rank, world, local):
     ym = opm.apply(x)
     err_m = float(np.linalg.norm(ym - exact) / np.linalg.norm(exact))
     parity = None
-    fx = os.path.join(ROOT, "tests", "golden", "fmm_laps_config1.npz")
+    fx = os.path.join(ROOT, "tests", "golden", "fmm_laps_icosphere15k.npz")
     if os.path.exists(fx):
         g = np.load(fx)
         own = float(np.linalg.norm(y - g["y_ref"]) / np.linalg.norm(g["y_ref"]))

@@ -4,7 +4,7 @@
 // cpp/fmm.{h,cpp}, cpp/octree.cpp, cpp/geometry.cpp, cpp/kernel.h,
 // cpp/laplace_kernels.h, cpp/elastic_kernels.h, cpp/nbody_operator.h), used
 // only by tests/, __graft_entry__.smoke() and bench.py's CPU baseline /
-// reference arm as the checker.  The product (3bem_gb300/) never links it.
+// reference arm, to check results.  The product (3bem_gb300/) never links it.
 //
 // Floating-point operations are written in the reference's evaluation order
 // (and this file is compiled with -ffp-contract=off) so that with one thread

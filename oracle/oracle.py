@@ -8,7 +8,7 @@ LAPACK, singular values <= 1e-10 * s_max are dropped, cpp/fmm.cpp:122), and
 exposes the apply, the direct sum and the tree/list dumps.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline / reference
-arm import this module, and only as the checker.  ``RefLib`` wraps the
+arm import this module, and only to check results.  ``RefLib`` wraps the
 reference itself compiled from its own sources (oracle/_ref, built by
 oracle/ref/Makefile where the reference checkout exists) to pin this
 restatement.

@@ -6,7 +6,7 @@ small seeded inputs, and stores inputs, reference outputs, the reference's
 check-to-equivalent operators, trees and task lists.  The GPU tests compare
 the product against these without needing the reference checkout.
 
-    python tests/golden/make_golden.py [<reference checkout>] [all|2d|nearfield|config1|interior]
+    python tests/golden/make_golden.py [<reference checkout>] [all|2d|nearfield|icosphere15k|interior]
 
 (the checkout defaults to $TBEM_REFERENCE_ROOT, else a `reference` folder
 beside this repository)
@@ -117,7 +117,7 @@ def make_case(name, kernel, n_src, n_obs, order, leaf, small, seed, geom):
     return out
 
 
-def make_config1():
+def make_icosphere15k():
     """The plain FP64 Laplace single-layer workload at its stated size: an
     icosahedron subdivided 4 times (5,120 triangles, radius 1), 3 Gauss points
     per triangle (15,360 points, obs = src), weights area / 3, outward normals,
@@ -364,10 +364,10 @@ def main(ref_root=None, which="all"):
     oracle.build()
     if oracle.build_ref(ref_root) is None:
         raise SystemExit("the reference checkout is needed to regenerate the fixtures")
-    if which == "config1":
-        data = make_config1()
-        np.savez_compressed(os.path.join(HERE, "fmm_laps_config1.npz"), **data)
-        print("wrote laps_config1", len(data["x"]), "points, ulp floor %.3g" % data["ulp_floor"])
+    if which == "icosphere15k":
+        data = make_icosphere15k()
+        np.savez_compressed(os.path.join(HERE, "fmm_laps_icosphere15k.npz"), **data)
+        print("wrote laps_icosphere15k", len(data["x"]), "points, ulp floor %.3g" % data["ulp_floor"])
         return
     if which == "interior":
         make_interior_cases()

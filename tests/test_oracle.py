@@ -44,9 +44,9 @@ def test_oracle_matches_reference_fixture(path):
         assert np.array_equal(a, g["list_%s_obs" % kind]) and np.array_equal(b, g["list_%s_src" % kind])
     # the reference's own check-to-equivalent operators: the apply agrees to
     # rounding.  The oracle's OpenMP passes add in a thread-dependent order;
-    # where the fixture carries the reference's one-ulp floor (config 1's
-    # size, where that floor is 2.7e-8) a hundredth of it bounds what a
-    # different order of the same sums may move
+    # where the fixture carries the reference's one-ulp floor (the
+    # 15,360-point icosphere, where that floor is 2.7e-8) a hundredth of it
+    # bounds what a different order of the same sums may move
     for which in (0, 1):
         for lev, op in enumerate(g["c2e%d" % which]):
             o.set_c2e(which, lev, op)
