@@ -143,6 +143,16 @@ int tbem_fmm_source_gradients(TbemFmm* h, const double* x, const double* r, doub
     });
 }
 
+int tbem_fmm_observation_gradients(TbemFmm* h, const double* x, const double* r, double* g_obs_locs,
+                                   double* g_obs_normals, void* stream)
+{
+    if (!h || (tbem_fmm_n_rows(h) > 0 && (!r || (!x && tbem_fmm_n_cols(h) > 0))))
+        return fail(TBEM_ERR_ARG, "null argument");
+    return guarded([&] {
+        h->plan.observation_gradients(x, r, g_obs_locs, g_obs_normals, (cudaStream_t)stream);
+    });
+}
+
 long tbem_fmm_n_rows(const TbemFmm* h) { return h ? h->plan.R * h->plan.n_obs : TBEM_ERR_ARG; }
 long tbem_fmm_n_cols(const TbemFmm* h) { return h ? h->plan.R * h->plan.n_src : TBEM_ERR_ARG; }
 

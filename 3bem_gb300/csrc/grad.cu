@@ -194,7 +194,11 @@ struct GradEvalArgs {
     int kid;
     KParams kp;
     int want_n;
-    double* g;             // [t_n][7]: d/dy (3), d/dn (3), value (1); accumulated
+    // 0: the targets are the operator's source points (contraction v^T K x_j,
+    // derivatives in y_j and n_j); 1: its observation points (r_i^T K v,
+    // derivatives in x_i and the observation normal n_i)
+    int obs_side;
+    double* g;             // [t_n][7]: d/dposition (3), d/dnormal (3), value (1); accumulated
 };
 constexpr int GRAD_TPT = 4, GRAD_THREADS = 128;
 
@@ -236,13 +240,26 @@ __global__ void __launch_bounds__(GRAD_THREADS) grad_eval_kernel(const GradEvalA
                     }
                     for (int d = 0; d < R; d++) rv[d] = a.s_v[d * a.s_n + p];
                 }
-                const double dd[3] = {y[0] - z[0], y[1] - z[1], y[2] - z[2]};
-                const Dual3 c = contraction(a.kid, 0, dd, nz, nj, rv, xv, a.kp);
-                acc[6] += c.v;
-                for (int k = 0; k < 3; k++) acc[k] += c.g[k];
-                if (a.want_n) {
-                    const Dual3 cn = contraction(a.kid, 1, dd, nz, nj, rv, xv, a.kp);
-                    for (int k = 0; k < 3; k++) acc[3 + k] += cn.g[k];
+                if (!a.obs_side) {
+                    // forward separation y_j - z, the target the source side
+                    const double dd[3] = {y[0] - z[0], y[1] - z[1], y[2] - z[2]};
+                    const Dual3 c = contraction(a.kid, 0, dd, nz, nj, rv, xv, a.kp);
+                    acc[6] += c.v;
+                    for (int k = 0; k < 3; k++) acc[k] += c.g[k];
+                    if (a.want_n) {
+                        const Dual3 cn = contraction(a.kid, 1, dd, nz, nj, rv, xv, a.kp);
+                        for (int k = 0; k < 3; k++) acc[3 + k] += cn.g[k];
+                    }
+                } else {
+                    // forward separation z - x_i: d/dx_i = -d/dd
+                    const double dd[3] = {z[0] - y[0], z[1] - y[1], z[2] - y[2]};
+                    const Dual3 c = contraction(a.kid, 0, dd, nj, nz, xv, rv, a.kp);
+                    acc[6] += c.v;
+                    for (int k = 0; k < 3; k++) acc[k] -= c.g[k];
+                    if (a.want_n) {
+                        const Dual3 cn = contraction(a.kid, 2, dd, nj, nz, xv, rv, a.kp);
+                        for (int k = 0; k < 3; k++) acc[3 + k] += cn.g[k];
+                    }
                 }
             }
         }
@@ -255,15 +272,16 @@ __global__ void __launch_bounds__(GRAD_THREADS) grad_eval_kernel(const GradEvalA
 }
 
 // Tree order [n][7] -> the caller's order: g_y = w dL/dy, g_n = w dL/dn,
-// g_w = the value sum (any output may be null).
+// g_w = the value sum (any output may be null; w null: no weight).
 __global__ void grad_scatter_kernel(const double* g7, const long* perm, const double* w, long n,
                                     double* g_y, double* g_n, double* g_w)
 {
     for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
         const long o = perm[j];
+        const double wj = w ? w[j] : 1.0;
         for (int k = 0; k < 3; k++) {
-            if (g_y) g_y[3 * o + k] = w[j] * g7[7 * j + k];
-            if (g_n) g_n[3 * o + k] = w[j] * g7[7 * j + 3 + k];
+            if (g_y) g_y[3 * o + k] = wj * g7[7 * j + k];
+            if (g_n) g_n[3 * o + k] = wj * g7[7 * j + 3 + k];
         }
         if (g_w) g_w[o] = g7[7 * j + 6];
     }
@@ -329,12 +347,20 @@ void grad_pass(const TaskSet& ts, bool src_surf, GradEvalArgs a, cudaStream_t s,
     if (launches) (*launches)++;
 }
 
-__global__ void gather_rows_kernel(const double* x, const long* perm, double* out, long n, int R)
+// [R][n] in the caller's order -> tree order, times w (tree order) when given
+__global__ void gather_rows_kernel(const double* x, const long* perm, double* out, long n, int R,
+                                   const double* w = nullptr)
 {
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n * R; t += (long)gridDim.x * blockDim.x) {
         const long i = t % n, d = t / n;
-        out[t] = x[d * n + perm[i]];
+        out[t] = w ? w[i] * x[d * n + perm[i]] : x[d * n + perm[i]];
     }
+}
+
+__global__ void widen_kernel(const float* in, double* out, long n)
+{
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+        out[t] = (double)in[t];
 }
 
 unsigned blocks_for(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 32)); }
@@ -428,6 +454,123 @@ void Plan::source_gradients(const double* x, const double* r, double* g_y, doubl
     if (g_y) TBEM_CK(cudaMemcpyAsync(g_y, gu, sizeof(double) * 3 * NS, cudaMemcpyDefault, s));
     if (g_n) TBEM_CK(cudaMemcpyAsync(g_n, gu + 3 * NS, sizeof(double) * 3 * NS, cudaMemcpyDefault, s));
     if (g_w) TBEM_CK(cudaMemcpyAsync(g_w, gu + 6 * NS, sizeof(double) * NS, cudaMemcpyDefault, s));
+    check_tc_flags(true, s);
+}
+
+// The forward apply of x leaves the downward coefficients of every cell
+// (cdc) and the M2P sources' equivalent densities in the work buffers.  The
+// passes that reach observation points -- P2P (the source points with
+// densities w x), M2P (those densities on the sources' up-equivalent
+// surfaces) and L2P (the leaves' down-equivalent densities, rebuilt here as
+// C2E_down(level) V cdc, the product the leaf operators E V fold in) -- are
+// run again with the kernel's derivatives in the observation point and its
+// normal.  Compressed forms only, as for the source side.
+void Plan::observation_gradients(const double* x, const double* r, double* g_x, double* g_n,
+                                 cudaStream_t s)
+{
+    if (opt.host_only) throw Error(TBEM_ERR_STATE, "operator was built with host_only");
+    if (sdim != 3) throw Error(TBEM_ERR_ARG, "observation gradients take the 3D kernels");
+    if (!batch_off.empty())
+        throw Error(TBEM_ERR_STATE, "observation gradients are not defined for the batched form "
+                                    "(its meshes are rescaled by their own bounding boxes)");
+    if (!(f.mixed && f.m2l_compressed) || f.m2l_on_the_fly)
+        throw Error(TBEM_ERR_STATE, "observation gradients need a compressed form (the precision "
+                                    "or FP64 compressed form with compressible M2L operators)");
+    if (!x || !r) throw Error(TBEM_ERR_ARG, "null input");
+    DeviceGuard guard(opt.device);
+    if (!s) s = stream;
+    const long NS = n_src, NO = n_obs;
+    if (NO == 0) return;
+    const Tree& O = otree;
+    const long nco = (long)O.cells.size();
+    // work arrays: tree-order gradients [NO][7], r and w x in tree order, the
+    // forward output, the caller-order outputs, the leaves' down-check
+    // potentials and down-equivalent densities (FP64, [cell][n])
+    const size_t off_r = 7 * (size_t)NO, off_x = off_r + R * (size_t)NO,
+                 off_o = off_x + R * (size_t)std::max<long>(NS, 1), off_u = off_o + R * (size_t)NO,
+                 off_c = off_u + 6 * (size_t)NO, off_q = off_c + (size_t)nco * n,
+                 total = off_q + (size_t)nco * n;
+    grad_buf.ensure(total);
+    double* g7 = grad_buf.p;
+    double* rt = grad_buf.p + off_r;
+    double* xt = grad_buf.p + off_x;
+    double* out = grad_buf.p + off_o;
+    double* gu = grad_buf.p + off_u;
+    double* uck = grad_buf.p + off_c;
+    double* qdn = grad_buf.p + off_q;
+    apply(x, out, 1, s, false);  // x is in io_x now, the states in cdc / the M2P buffers
+    TBEM_CK(cudaMemcpyAsync(io_y.p, r, sizeof(double) * R * NO, cudaMemcpyDefault, s));
+    gather_rows_kernel<<<blocks_for(NO * R), 256, 0, s>>>(io_y.p, dobs.perm.p, rt, NO, R);
+    TBEM_CK(cudaGetLastError());
+    if (NS > 0) {
+        gather_rows_kernel<<<blocks_for(NS * R), 256, 0, s>>>(io_x.p, dsrc->perm.p, xt, NS, R, dsrc->w.p);
+        TBEM_CK(cudaGetLastError());
+    }
+    // down-check potentials of the L2P leaves (V cdc), then their
+    // down-equivalent densities C2E_down(level) u, level by level in FP64
+    TBEM_CK(cudaMemsetAsync(uck, 0, sizeof(double) * nco * n, s));
+    if (f.f64) {
+        f.decomp_l2p.run_rect<double>(cdc64.p, uck, n, f.r_out, f.r_out, 1, 0, GEMM_STORE, s, &launches);
+    } else {
+        TBEM_CK(cudaMemsetAsync(cd32.p, 0, sizeof(float) * nco * n, s));
+        f.decomp_l2p.run_rect<float>(cdc32.p, cd32.p, n, f.r_out, f.r_out, 1, 0, GEMM_STORE, s, &launches);
+        widen_kernel<<<blocks_for(nco * n), 256, 0, s>>>(cd32.p, uck, nco * n);
+        TBEM_CK(cudaGetLastError());
+    }
+    TBEM_CKB(cublasSetStream(cublas, s));
+    const double one = 1.0, zero = 0.0;
+    for (int l = 0; l < O.n_levels() && l < (int)f.c2e_dn_off.size(); l++) {
+        const long c0 = O.level_start[l], c1 = O.level_start[l + 1];
+        if (c1 <= c0) continue;
+        // column-major q (n x cells) = C2E^T-as-stored^T u: the row-major
+        // pseudo-inverse applied to every cell's potential
+        TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, n, (int)(c1 - c0), n, &one,
+                             f.c2e.p + f.c2e_dn_off[l], n, uck + c0 * n, n, &zero, qdn + c0 * n, n));
+    }
+    TBEM_CKB(cublasSetStream(cublas, stream));
+    TBEM_CK(cudaMemsetAsync(g7, 0, sizeof(double) * 7 * NO, s));
+    GradEvalArgs a{};
+    a.obs_side = 1;
+    a.t_xyz = dobs.xyz.p;
+    a.t_nrm = dobs.nrm64.p;
+    a.t_x = rt;
+    a.t_n = NO;
+    a.unit = d_unit.p;
+    a.ns = ns;
+    a.g = g7;
+    auto with_obs_normals = [](int k) { return k == EL_ADJ || k == EL_HYP; };
+    // P2P: the source points with densities w x
+    a.kid = kid;
+    a.kp = make_kparams(kid, mu, nu);
+    a.want_n = with_obs_normals(kid);
+    a.s_xyz = dsrc->xyz.p;
+    a.s_nrm = dsrc->nrm64.p;
+    a.s_v = xt;
+    a.s_n = NS;
+    grad_pass(p2p, false, a, s, &launches);
+    // M2P and L2P: equivalent surfaces, the kernel that reaches the targets
+    a.kid = f.kt_kid;
+    a.kp = make_kparams(f.kt_kid, mu, nu);
+    a.want_n = with_obs_normals(f.kt_kid);
+    if (!L.m2p.empty()) {
+        a.q32 = nullptr;
+        a.q64 = f.f64 ? cu64.p : qu64.p;
+        a.s_center = dsrc->center.p;
+        a.s_rad = dsrc->rad.p;
+        a.s_rref = f.r_ue;
+        grad_pass(m2p, true, a, s, &launches);
+    }
+    a.q32 = nullptr;
+    a.q64 = qdn;
+    a.s_center = dobs.center.p;
+    a.s_rad = dobs.rad.p;
+    a.s_rref = f.r_de;
+    grad_pass(l2p, true, a, s, &launches);
+    grad_scatter_kernel<<<blocks_for(NO), 256, 0, s>>>(g7, dobs.perm.p, nullptr, NO, gu, gu + 3 * NO,
+                                                       nullptr);
+    TBEM_CK(cudaGetLastError());
+    if (g_x) TBEM_CK(cudaMemcpyAsync(g_x, gu, sizeof(double) * 3 * NO, cudaMemcpyDefault, s));
+    if (g_n) TBEM_CK(cudaMemcpyAsync(g_n, gu + 3 * NO, sizeof(double) * 3 * NO, cudaMemcpyDefault, s));
     check_tc_flags(true, s);
 }
 

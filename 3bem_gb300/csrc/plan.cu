@@ -2021,6 +2021,12 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
             if (is_p2l[c]) a.push_back({c, c});
         F.comp_p2l.add_group(0, a);
     }
+    F.decomp_l2p = GemmSet();
+    {
+        std::vector<std::pair<int, int>> a;
+        for (int c : L.l2p) a.push_back({c, c});
+        F.decomp_l2p.add_group(0, a);
+    }
     // the sets resolve their operators in the pool of the form's precision
     const size_t es = f64 ? sizeof(double) : sizeof(float);
     auto pool = [&](DBuf<float>& p32, DBuf<double>& p64) -> const void* {
@@ -2035,6 +2041,7 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
     F.comp_p2m.upload(pool(F.Pb, F.Pb64), es);
     F.decomp_m2p.upload(pool(F.Wl, F.Wl64), es);
     F.comp_p2l.upload(pool(F.Vb, F.Vb64), es);
+    F.decomp_l2p.upload(pool(F.Vb, F.Vb64), es);
     F.m2l_compressed = true;
 }
 

@@ -323,6 +323,7 @@ struct Form {
     DBuf<double> Pb64, Wl64, Vb64, Cops64, Xops64, Yops64, E64;
     DBuf<double> V64;  // V in FP64 (column-major n x r_out) while the L2P operators are built
     GemmSet m2l_c, m2l_c_t, comp_p2m, decomp_m2p, comp_p2l;
+    GemmSet decomp_l2p;  // V over the L2P leaves: their down-check potentials (gradients)
     std::vector<GemmSet> m2m_c, m2m_c_t, l2l_c, l2l_c_t;  // per level
     // mixed: per-leaf L2P operators
     DBuf<float> E;
@@ -442,6 +443,11 @@ struct Plan {
     // passes of the compressed forms (grad.cu).
     void source_gradients(const double* x, const double* r, double* g_y, double* g_n, double* g_w,
                           cudaStream_t s);
+    // The same for the observation points' positions and normals
+    // ([n_obs][3] each): one forward apply, then its passes that reach
+    // observation points with the kernel's derivatives (grad.cu).
+    void observation_gradients(const double* x, const double* r, double* g_x, double* g_n,
+                               cudaStream_t s);
     DBuf<double> grad_buf;  // source_gradients' work arrays
     void set_c2e(int which, long level, const double* op);
     void get_c2e(int which, long level, double* out) const;

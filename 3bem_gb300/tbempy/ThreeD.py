@@ -262,6 +262,27 @@ class FMMOperator(OperatorI):
             _ptr(out["src_weights"]), _stream_of(xx)))
         return out
 
+    def observation_gradients(self, x, r):
+        """Derivatives of L = r^T A x (one right-hand side) with respect to
+        the observation points' positions and normals, through the FMM (the
+        compressed forms): a dict keyed obs_locs [n_obs, 3] and obs_normals
+        [n_obs, 3], numpy or float64 CUDA tensors like x."""
+        is_t = torch is not None and isinstance(x, torch.Tensor)
+        n = self.n_rows() // self.K.tensor_dim
+        if is_t:
+            xx, rr = x.reshape(-1).contiguous(), r.reshape(-1).contiguous()
+            out = {k: torch.empty((n, 3), dtype=torch.float64, device=xx.device)
+                   for k in ("obs_locs", "obs_normals")}
+        else:
+            xx, rr = _f64(x, (-1,)), _f64(r, (-1,))
+            out = {"obs_locs": np.empty((n, 3)), "obs_normals": np.empty((n, 3))}
+        if xx.shape[0] != self.n_cols() or rr.shape[0] != self.n_rows():
+            raise ValueError("x has n_cols and r n_rows entries (one right-hand side)")
+        check(_L.lib().tbem_fmm_observation_gradients(
+            self._h, _ptr(xx), _ptr(rr), _ptr(out["obs_locs"]), _ptr(out["obs_normals"]),
+            _stream_of(xx)))
+        return out
+
     def clone(self):
         h = C.c_void_p()
         check(_L.lib().tbem_fmm_clone(self._h, C.byref(h)))

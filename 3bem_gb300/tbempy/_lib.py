@@ -51,6 +51,7 @@ SIGNATURES = {
     "tbem_fmm_apply": (_I, [_P, _P, _P, _I, _P]),
     "tbem_fmm_apply_adjoint": (_I, [_P, _P, _P, _I, _P]),
     "tbem_fmm_source_gradients": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "tbem_fmm_observation_gradients": (_I, [_P, _P, _P, _P, _P, _P]),
     "tbem_fmm_n_rows": (_L, [_P]),
     "tbem_fmm_n_cols": (_L, [_P]),
     "tbem_fmm_clone": (_I, [_P, _P]),

@@ -57,6 +57,40 @@ def fmm_apply_sources(op, src_locs, src_normals, src_weights, x):
     return _SourceGeometryApply.apply(src_locs, src_normals, src_weights, x, op)
 
 
+class _GeometryApply(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, obs_locs, obs_normals, src_locs, src_normals, src_weights, x, op):
+        ctx.op = op
+        ctx.save_for_backward(x)
+        return op.apply(x.contiguous())
+
+    @staticmethod
+    def backward(ctx, grad):
+        (x,) = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        xd, gd = x.detach().contiguous(), grad.contiguous()
+        go = {"obs_locs": None, "obs_normals": None}
+        gs = {"src_locs": None, "src_normals": None, "src_weights": None}
+        if need[0] or need[1]:
+            go = ctx.op.observation_gradients(xd, gd)
+        if need[2] or need[3] or need[4]:
+            gs = ctx.op.source_gradients(xd, gd)
+        gx = ctx.op.apply_adjoint(gd) if need[5] else None
+        return (go["obs_locs"], go["obs_normals"], gs["src_locs"], gs["src_normals"],
+                gs["src_weights"], gx, None)
+
+
+def fmm_apply_geometry(op, obs_locs, obs_normals, src_locs, src_normals, src_weights, x):
+    """Differentiable y = A x whose gradients reach both point sets.
+
+    As ``fmm_apply_sources``, with the observation points' positions and
+    normals [n_obs, 3] as inputs too: their gradients come from
+    ``observation_gradients`` (one forward apply, then the passes that reach
+    observation points with the kernel's derivatives).  Only the gradients
+    that are needed are computed."""
+    return _GeometryApply.apply(obs_locs, obs_normals, src_locs, src_normals, src_weights, x, op)
+
+
 def misfit(op, s, d):
     """L = 0.5 ||A s - d||^2 (the differentiated workload's loss)."""
     r = fmm_apply(op, s) - d

@@ -193,6 +193,21 @@ int tbem_fmm_apply_adjoint(TbemFmm* h, const double* z, double* w, int n_rhs, vo
 int tbem_fmm_source_gradients(TbemFmm* h, const double* x, const double* r, double* g_src_locs,
                               double* g_src_normals, double* g_src_weights, void* stream);
 
+/* Observation-side gradients of L = r^T A x (one right-hand side) through
+ * the FMM: derivatives with respect to the observation points' positions
+ * (g_obs_locs [n_obs][3]) and normals (g_obs_normals [n_obs][3], nonzero
+ * for the kernels with an observation normal); either output may be NULL.
+ * One forward apply of x, then the three passes that reach observation
+ * points (near field, M2P from the sources' up-equivalent surfaces, L2P from
+ * the leaves' down-equivalent surfaces) again with the kernel's exact
+ * derivatives (FP64 dual numbers); the down-equivalent densities are
+ * rebuilt from the apply's compressed local coefficients.  The O(N)
+ * counterpart of tbem_direct_gradients' observation outputs for the
+ * compressed forms (TBEM_ERR_STATE for the plain and batched forms).
+ * Synchronous.  No reference counterpart. */
+int tbem_fmm_observation_gradients(TbemFmm* h, const double* x, const double* r,
+                                   double* g_obs_locs, double* g_obs_normals, void* stream);
+
 /* OperatorI::n_rows / n_cols (cpp/operator.h:15-16, cpp/fmm.h:235-236). */
 long tbem_fmm_n_rows(const TbemFmm* h);
 long tbem_fmm_n_cols(const TbemFmm* h);

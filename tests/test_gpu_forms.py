@@ -83,6 +83,65 @@ def test_fmm_source_gradients_match_the_direct_pass(name, distinct, prec):
         assert err < tol, (k, err)
 
 
+@pytest.mark.parametrize("prec", ["mixed", "fp64_compressed"])
+@pytest.mark.parametrize("name", ["LaplaceSingle", "LaplaceDouble", "ElasticAdjointTraction",
+                                  "ElasticHypersingular"])
+@pytest.mark.parametrize("distinct", [False, True])
+def test_fmm_observation_gradients_match_the_direct_pass(name, distinct, prec):
+    """tbem_fmm_observation_gradients (the passes that reach observation
+    points, with the kernel's derivatives) against the direct
+    kernel-gradient pass: positions of the observation points and, for the
+    kernels with an observation normal, the normals."""
+    from tbempy import ThreeD
+    src, sn, w = cloud(600, 11)
+    obs, on = (src, sn) if not distinct else cloud(500, 12)[:2]
+    K = ThreeD.ElasticAdjointTraction(1.0, 0.25) if name == "ElasticAdjointTraction" else \
+        ThreeD.ElasticHypersingular(1.0, 0.25) if name == "ElasticHypersingular" else getattr(ThreeD, name)()
+    op = ThreeD.FMMOperator(K, obs, on, src, sn, w, ThreeD.FMMConfig(0.3, 296, 30, 0.05, False),
+                            precision=prec)
+    rng = np.random.default_rng(17)
+    x = rng.uniform(-1, 1, op.n_cols())
+    r = rng.uniform(-1, 1, op.n_rows())
+    op.apply_adjoint(rng.uniform(-1, 1, op.n_rows()))  # leave other states in the work buffers
+    g = op.observation_gradients(x, r)
+    gd = ThreeD.direct_gradients(K, obs, on, src, sn, w, x, r)
+    tol = 2e-5 if prec == "mixed" else 2e-6
+    keys = ("obs_locs",) + (("obs_normals",) if name.startswith("Elastic") else ())
+    for k in keys:
+        err = np.linalg.norm(g[k] - gd[k]) / np.linalg.norm(gd[k])
+        assert err < tol, (k, err)
+    if not name.startswith("Elastic"):
+        assert np.all(g["obs_normals"] == 0.0)
+
+
+def test_fmm_geometry_gradient_through_autograd():
+    """fmm_apply_geometry: the misfit's gradient with respect to mesh vertices
+    that place both the sources and the observation points (pushed off the
+    surface along the normals) through the FMM's source and observation
+    gradients equals the direct kernel-gradient pass's."""
+    torch = pytest.importorskip("torch")
+    from tbempy import ThreeD, autograd, meshes
+    v, t, _, _, _, _, _ = meshes.misfit_workload(n=12, n_obs=400)
+    K = ThreeD.ElasticAdjointTraction(1.0, 0.25)
+    sl, sn, sw = meshes.points_from_mesh(v, t)
+    ol, on = sl + 0.05 * sn, sn
+    op = ThreeD.FMMOperator(K, ol, on, sl, sn, sw, ThreeD.FMMConfig(0.3, 296, 30, 0.05, False),
+                            precision="mixed")
+    s = torch.tensor(np.random.default_rng(4).uniform(-1, 1, op.n_cols()), device="cuda")
+    d = torch.tensor(np.random.default_rng(5).normal(size=op.n_rows()), device="cuda")
+    grads = []
+    for use_fmm in (True, False):
+        V = torch.tensor(v, device="cuda", requires_grad=True)
+        a, b, c = meshes.points_from_mesh_torch(V, t)
+        o = a + 0.05 * b
+        y = (autograd.fmm_apply_geometry(op, o, b, a, b, c, s) if use_fmm
+             else autograd.direct_apply(K, o, b, a, b, c, s))
+        (0.5 * ((y - d) ** 2).sum()).backward()
+        grads.append(V.grad.cpu().numpy())
+    err = np.linalg.norm(grads[0] - grads[1]) / np.linalg.norm(grads[1])
+    assert err < 2e-5, err
+
+
 def test_fmm_vertex_gradient_through_autograd():
     """fmm_apply_sources: the misfit's gradient with respect to mesh vertices
     (points, normals and weights from the vertices by torch) through the
