@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <tuple>
 
@@ -1207,6 +1208,34 @@ void Plan::build_tasks()
 // could drop entries) and the 2D kernels get their own SVD, as in the
 // reference.  The scaled operators differ from per-level SVDs by rounding of
 // the size of the reference's own one-ulp sensitivity.
+namespace {
+// Pseudo-inverses factored in this process, by everything the factored
+// system depends on (kernel and its parameters, the unit surface, the
+// surface radii and centre, the cut-off, the device).  Operators that share
+// a translation kernel over the same tree -- the displacement and traction
+// operators of one mesh, or a clone -- then factor each level once.  The
+// values are host copies (n^2 doubles each), the oldest dropped past
+// C2E_CACHE_BYTES.
+using C2EKey = std::tuple<int, int, int, double, double, double, double, double, double, double,
+                          double, double, uint64_t, int>;
+constexpr size_t C2E_CACHE_BYTES = 512u << 20;
+std::mutex c2e_cache_mu;
+std::map<C2EKey, std::vector<double>> c2e_cache;
+std::vector<C2EKey> c2e_cache_order;
+size_t c2e_cache_bytes = 0;
+
+uint64_t hash_doubles(const std::vector<double>& v)
+{
+    uint64_t h = 1469598103934665603ull;  // FNV-1a over the bytes
+    for (double d : v) {
+        unsigned char b[sizeof(double)];
+        std::memcpy(b, &d, sizeof(double));
+        for (unsigned char c : b) h = (h ^ c) * 1099511628211ull;
+    }
+    return h;
+}
+}  // namespace
+
 void Plan::build_c2e(Form& F)
 {
     const Tree* trees[2] = {stree, &otree};
@@ -1252,6 +1281,43 @@ void Plan::build_c2e(Form& F)
     }
     F.c2e.alloc(total);
     if (jobs.empty()) return;
+    int device = 0;
+    TBEM_CK(cudaGetDevice(&device));
+    const uint64_t unit_hash = hash_doubles(unit);
+    auto key_of = [&](const SurfJob& J) {
+        return C2EKey(F.g_kid, sdim, ns, mu, nu, J.tr, J.trref, J.srref, J.tc[0], J.tc[1], J.tc[2],
+                      opt.svd_threshold, unit_hash, device);
+    };
+    {
+        // levels factored before: copied in, the rest factored below
+        std::lock_guard<std::mutex> lock(c2e_cache_mu);
+        std::vector<SurfJob> todo;
+        std::vector<long> todo_dst;
+        for (size_t k = 0; k < jobs.size(); k++) {
+            auto it = c2e_cache.find(key_of(jobs[k]));
+            if (it != c2e_cache.end() && (long)it->second.size() == nn) {
+                TBEM_CK(cudaMemcpyAsync(F.c2e.p + job_dst[k], it->second.data(), sizeof(double) * nn,
+                                        cudaMemcpyHostToDevice, stream));
+            } else {
+                SurfJob J = jobs[k];
+                J.out_off = (long)todo.size() * nn;
+                todo.push_back(J);
+                todo_dst.push_back(job_dst[k]);
+            }
+        }
+        TBEM_CK(cudaStreamSynchronize(stream));
+        jobs.swap(todo);
+        job_dst.swap(todo_dst);
+    }
+    if (jobs.empty()) {
+        for (const Scaled& sc : scaled) {
+            scale_copy_kernel<<<(unsigned)std::min<long>((nn + 255) / 256, 4096), 256, 0, stream>>>(
+                F.c2e.p + sc.src, F.c2e.p + sc.dst, nn, sc.s);
+            TBEM_CK(cudaGetLastError());
+        }
+        TBEM_CK(cudaStreamSynchronize(stream));
+        return;
+    }
     DBuf<double> sys;
     sys.alloc(jobs.size() * nn);
     DBuf<SurfJob> dj;
@@ -1289,6 +1355,19 @@ void Plan::build_c2e(Form& F)
         if (h_info != 0)
             throw Error(TBEM_ERR_CUDA, "cuSOLVER gesvd did not converge (info " +
                                            std::to_string(h_info) + ")");
+        std::vector<double> h(nn);
+        TBEM_CK(cudaMemcpy(h.data(), F.c2e.p + job_dst[k], sizeof(double) * nn, cudaMemcpyDeviceToHost));
+        std::lock_guard<std::mutex> lock(c2e_cache_mu);
+        const C2EKey key = key_of(jobs[k]);
+        if (c2e_cache.count(key)) continue;
+        while (!c2e_cache_order.empty() && c2e_cache_bytes + sizeof(double) * nn > C2E_CACHE_BYTES) {
+            c2e_cache_bytes -= sizeof(double) * c2e_cache[c2e_cache_order.front()].size();
+            c2e_cache.erase(c2e_cache_order.front());
+            c2e_cache_order.erase(c2e_cache_order.begin());
+        }
+        c2e_cache[key] = std::move(h);
+        c2e_cache_order.push_back(key);
+        c2e_cache_bytes += sizeof(double) * nn;
     }
     for (const Scaled& sc : scaled) {
         scale_copy_kernel<<<(unsigned)std::min<long>((nn + 255) / 256, 4096), 256, 0, stream>>>(
@@ -1588,7 +1667,14 @@ void Plan::build_mixed_ops(Form& F)
         KM.alloc(std::max<long>(n_m2m_ops, 1) * nn);
         YL.alloc(std::max<long>(n_l2l_ops, 1) * nn);
     }
-    if (!jobs.empty()) {
+    // The kernel matrices of every job, and the combined operators K C2E:
+    // `dense` fills the FP32 pool with all of them (the uncompressed paths);
+    // without it only the L2L jobs' combined operators are formed, the
+    // compression taking the M2L and M2M jobs' kernel matrices alone (each
+    // skipped product is 2 n^3 FP64 flops).  `copies` saves the compression's
+    // inputs.
+    auto build_jobs = [&](bool dense, bool copies) {
+        if (jobs.empty()) return;
         // in chunks to bound the FP64 scratch
         // (one grid row per job: at most 65,535 jobs per chunk)
         const size_t chunk = std::min<size_t>(65535, std::max<size_t>(1, (size_t)(2e9 / (8.0 * nn))));
@@ -1608,15 +1694,18 @@ void Plan::build_mixed_ops(Form& F)
                                                        make_kparams(F.g_kid, mu, nu), K.p);
             TBEM_CK(cudaGetLastError());
             for (size_t k = 0; k < nj; k++) {
+                if (!dense && l2l_index[j0 + k] < 0) continue;
                 // row-major Y = K * C  <=>  column-major Y^T = C^T K^T
                 TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one,
                                      F.c2e.p + c2e_of[j0 + k], n, K.p + k * nn, n, &zero,
                                      Y.p + k * nn, n));
             }
-            convert_kernel<float><<<grid_for(nj * nn), 256, 0, stream>>>(Y.p, F.ops32.p + j0 * nn, nj * nn);
-            TBEM_CK(cudaGetLastError());
-            if (compress)
-                for (size_t k = 0; k < nj; k++)
+            if (dense) {
+                convert_kernel<float><<<grid_for(nj * nn), 256, 0, stream>>>(Y.p, F.ops32.p + j0 * nn, nj * nn);
+                TBEM_CK(cudaGetLastError());
+            }
+            if (copies)
+                for (size_t k = 0; k < nj; k++) {
                     if (m2l_index[j0 + k] >= 0) {
                         double* dst = U64.p + m2l_index[j0 + k] * nn;
                         TBEM_CK(cudaMemcpyAsync(dst, K.p + k * nn, sizeof(double) * nn,
@@ -1624,8 +1713,6 @@ void Plan::build_mixed_ops(Form& F)
                         const double f = std::ldexp(1.0, -job_ls[j0 + k]);
                         TBEM_CKB(cublasDscal(cublas, (int)nn, &f, dst, 1));
                     }
-            if (compress)
-                for (size_t k = 0; k < nj; k++) {
                     if (m2m_index[j0 + k] >= 0)
                         TBEM_CK(cudaMemcpyAsync(KM.p + m2m_index[j0 + k] * nn, K.p + k * nn, sizeof(double) * nn,
                                                 cudaMemcpyDeviceToDevice, stream));
@@ -1635,7 +1722,8 @@ void Plan::build_mixed_ops(Form& F)
                 }
             TBEM_CK(cudaStreamSynchronize(stream));
         }
-    }
+    };
+    build_jobs(!compress, compress);
     build_gemm_sets(F, 0, 0, 0, m2m_off, l2l_off, m2l_off);
     setup_mark("translations");
     F.m2l_compressed = false;
@@ -1647,6 +1735,8 @@ void Plan::build_mixed_ops(Form& F)
     U64.release();
     KM.release();
     YL.release();
+    // the compression declined: the dense combined operators after all
+    if (compress && !F.m2l_compressed && !F.f64) build_jobs(true, false);
     if (F.f64 && !F.m2l_compressed)
         throw Error(TBEM_ERR_ARG, "the FP64 compressed form needs M2L operators that compress (the "
                                   "compressed products cheaper than the dense ones)");
@@ -1703,7 +1793,13 @@ void Plan::build_mixed_ops(Form& F)
     F.E_npts.upload(npts);
     if (rows > 0) {
         const long max_rows = std::max<long>((long)R * 64, (long)(1.5e9 / (8.0 * n)));
-        DBuf<double> K, Y, EV;
+        DBuf<double> K, Y, EV, CV;
+        // compressed form: E V = K (C2E_down(level) V), the n x r_out factor
+        // formed once per level -- 2 r r_out n flops per chunk of r rows
+        // where (K C2E) V took 2 r n (n + r_out), and the setup's FP64 GEMMs
+        // run at about 1.25 TFLOP/s on this part
+        if (F.m2l_compressed) CV.alloc((size_t)n * F.r_out);
+        int cv_level = -1;
         // chunks of consecutive leaves of one level
         size_t t0 = 0;
         while (t0 < cell.size()) {
@@ -1717,7 +1813,6 @@ void Plan::build_mixed_ops(Form& F)
                 t1++;
             }
             K.ensure(r * n);
-            Y.ensure(r * n);
             int maxp = 0;
             for (size_t t = t0; t < t1; t++) maxp = std::max(maxp, npts[t]);
             dim3 g((unsigned)(((long)maxp * ns + 255) / 256), (unsigned)(t1 - t0));
@@ -1726,15 +1821,23 @@ void Plan::build_mixed_ops(Form& F)
                 dobs.nrm64.p, dobs.center.p, dobs.rad.p, F.r_de, d_unit.p, ns, F.kt_kid,
                 make_kparams(F.kt_kid, mu, nu), K.p, row0[t0]);
             TBEM_CK(cudaGetLastError());
-            TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)r, n, &one,
-                                 F.c2e.p + F.c2e_dn_off[lev], n, K.p, n, &zero, Y.p, n));
             if (F.m2l_compressed) {
-                // row-major E V (r x r_out) = column-major V^T E^T
+                // column-major CV = C^T V (C the stored pseudo-inverse, its
+                // column-major transpose being the row-major operator), then
+                // row-major E V (r x r_out) = column-major CV^T K^T
+                if (lev != cv_level) {
+                    TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, n, F.r_out, n, &one,
+                                         F.c2e.p + F.c2e_dn_off[lev], n, F.V64.p, n, &zero, CV.p, n));
+                    cv_level = lev;
+                }
                 EV.ensure(r * F.r_out);
-                TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, F.r_out, (int)r, n, &one, F.V64.p, n,
-                                     Y.p, n, &zero, EV.p, F.r_out));
+                TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_T, CUBLAS_OP_N, F.r_out, (int)r, n, &one, CV.p, n,
+                                     K.p, n, &zero, EV.p, F.r_out));
                 store_rows(EV.p, row0[t0] * F.E_ld, r, F.r_out);
             } else {
+                Y.ensure(r * n);
+                TBEM_CKB(cublasDgemm(cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)r, n, &one,
+                                     F.c2e.p + F.c2e_dn_off[lev], n, K.p, n, &zero, Y.p, n));
                 store_rows(Y.p, row0[t0] * F.E_ld, r, n);
             }
             TBEM_CK(cudaGetLastError());

@@ -699,10 +699,17 @@ def run_misfit(args, rank, world, local):
     gv_dir = V.grad.clone()
     ms_vert_direct = _events_ms(torch, lambda: vertex_grad(False), 1, stream)
     err_vert = float(torch.linalg.norm(gv_fmm - gv_dir) / torch.linalg.norm(gv_dir))
+    # the observers' position gradient of the same loss through the FMM's
+    # forward passes with the kernel's derivatives at the observers
+    rr = (op.apply(s) - d).contiguous()
+    go = op.observation_gradients(s, rr)["obs_locs"].cpu().numpy()
+    ms_obs = _events_ms(torch, lambda: op.observation_gradients(s, rr), args.steps, stream)
     g = grad_step().cpu().numpy()
     r = Dop.apply(s_np) - d.cpu().numpy()
-    gd = ThreeD.direct_gradients(K, obs, on, sl, sn, sw, s_np, r)["x"]
+    gdd = ThreeD.direct_gradients(K, obs, on, sl, sn, sw, s_np, r)
+    gd = gdd["x"]
     err = float(np.linalg.norm(g - gd) / np.linalg.norm(gd))
+    err_obs = float(np.linalg.norm(go - gdd["obs_locs"]) / np.linalg.norm(gdd["obs_locs"]))
     y = op.apply(s_np)
     err_f = float(np.linalg.norm(y - Dop.apply(s_np)) / np.linalg.norm(Dop.apply(s_np)))
     print(json.dumps({
@@ -712,9 +719,11 @@ def run_misfit(args, rank, world, local):
         "data": "synthetic (seeded bumpy fault, free-surface observers)", "config": misfit_config(),
         "clocks": clk.summary(), "gpu_launches": 2 * op.last_launches() * args.steps,
         "forward_ms": ms_fwd, "vertex_gradient_ms": ms_vert,
-        "vertex_gradient_direct_ms": ms_vert_direct, "phases_ms_forward": phases,
+        "vertex_gradient_direct_ms": ms_vert_direct, "observer_gradient_ms": ms_obs,
+        "phases_ms_forward": phases,
         "rel_err_vs_direct": {"forward": err_f, "gradient_ds": err,
-                              "gradient_vertices_fmm_vs_direct_pass": err_vert}, "setup_s": setup_s,
+                              "gradient_vertices_fmm_vs_direct_pass": err_vert,
+                              "gradient_observers_fmm_vs_direct_pass": err_obs}, "setup_s": setup_s,
         "setup_phases_s": setup_phases([op])}), flush=True)
 
 
