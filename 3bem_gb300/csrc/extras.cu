@@ -474,6 +474,12 @@ long tbem_integral_n_rows(const TbemIntegral* h) { return h ? h->n_rows : TBEM_E
 long tbem_integral_n_cols(const TbemIntegral* h) { return h ? h->n_cols : TBEM_ERR_ARG; }
 void tbem_integral_destroy(TbemIntegral* h) { delete h; }
 
+int tbem_setup_cache_clear(void)
+{
+    tbem::clear_setup_cache();
+    return TBEM_OK;
+}
+
 int tbem_fma_peak(int device, int fp64, double* tflops)
 {
     using namespace tbem;

@@ -1224,17 +1224,45 @@ std::map<C2EKey, std::vector<double>> c2e_cache;
 std::vector<C2EKey> c2e_cache_order;
 size_t c2e_cache_bytes = 0;
 
-uint64_t hash_doubles(const std::vector<double>& v)
+// FNV-1a over bytes, from a given basis (two bases give two hashes)
+uint64_t hash_bytes(const void* p, size_t n, uint64_t h = 1469598103934665603ull)
 {
-    uint64_t h = 1469598103934665603ull;  // FNV-1a over the bytes
-    for (double d : v) {
-        unsigned char b[sizeof(double)];
-        std::memcpy(b, &d, sizeof(double));
-        for (unsigned char c : b) h = (h ^ c) * 1099511628211ull;
-    }
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
     return h;
 }
+
+uint64_t hash_doubles(const std::vector<double>& v)
+{
+    return hash_bytes(v.data(), v.size() * sizeof(double));
+}
+
+// The eigen-decompositions of the M2L Gram matrices (both n x n eigenvector
+// sets and their 2n eigenvalues), by two hashes of the M2L matrices'
+// description (kernel, parameters, unit surface, every class's surfaces),
+// the surface size and the device: operators sharing the translation kernel
+// over the same trees compress with the same bases.  Oldest dropped past
+// GRAM_CACHE_BYTES.
+struct GramEntry {
+    std::vector<double> gi, go, ev;
+};
+using GramKey = std::tuple<uint64_t, uint64_t, int, int>;
+constexpr size_t GRAM_CACHE_BYTES = 512u << 20;
+std::map<GramKey, GramEntry> gram_cache;
+std::vector<GramKey> gram_cache_order;
+size_t gram_cache_bytes = 0;
 }  // namespace
+
+void clear_setup_cache()
+{
+    std::lock_guard<std::mutex> lock(c2e_cache_mu);
+    c2e_cache.clear();
+    c2e_cache_order.clear();
+    c2e_cache_bytes = 0;
+    gram_cache.clear();
+    gram_cache_order.clear();
+    gram_cache_bytes = 0;
+}
 
 void Plan::build_c2e(Form& F)
 {
@@ -1729,7 +1757,29 @@ void Plan::build_mixed_ops(Form& F)
     F.m2l_compressed = false;
     if (compress) {
         CompressionInput in{U64.p, n_m2l_ops, &m2l_index, KM.p, &m2m_lc, &m2m_index,
-                            YL.p, &l2l_index, &m2m_off, &l2l_off};
+                            YL.p, &l2l_index, &m2m_off, &l2l_off, {0, 0}};
+        // what the root-scaled M2L matrices depend on, in compact order
+        const uint64_t bases[2] = {1469598103934665603ull, 0x9e3779b97f4a7c15ull};
+        const uint64_t uh = hash_doubles(unit);
+        const double prm[2] = {mu, nu};
+        const int ints[3] = {F.g_kid, ns, sdim};
+        for (int h = 0; h < 2; h++) {
+            uint64_t k = hash_bytes(ints, sizeof(ints), bases[h]);
+            k = hash_bytes(prm, sizeof(prm), k);
+            k = hash_bytes(&uh, sizeof(uh), k);
+            k = hash_bytes(&n_m2l_ops, sizeof(n_m2l_ops), k);
+            std::vector<long> order(n_m2l_ops, -1);
+            for (size_t j = 0; j < jobs.size(); j++)
+                if (m2l_index[j] >= 0) order[m2l_index[j]] = (long)j;
+            for (long j : order) {
+                const SurfJob& J = jobs[j];
+                const double g[10] = {J.tc[0], J.tc[1], J.tc[2], J.tr, J.trref,
+                                      J.sc[0], J.sc[1], J.sc[2], J.sr, J.srref};
+                k = hash_bytes(g, sizeof(g), k);
+                k = hash_bytes(&job_ls[j], sizeof(int), k);
+            }
+            in.t0_key[h] = k;
+        }
         build_compression(F, in);
     }
     U64.release();
@@ -1891,6 +1941,23 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
     DBuf<double> Gi, Go;
     Gi.alloc(nn);
     Go.alloc(nn);
+    DBuf<double> ev;
+    ev.alloc(2 * (size_t)n);
+    int device = 0;
+    TBEM_CK(cudaGetDevice(&device));
+    const GramKey gkey(in.t0_key[0], in.t0_key[1], n, device);
+    std::vector<double> h_ev;
+    {
+        std::lock_guard<std::mutex> lock(c2e_cache_mu);
+        auto it = gram_cache.find(gkey);
+        if (it != gram_cache.end()) {
+            TBEM_CK(cudaMemcpyAsync(Gi.p, it->second.gi.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, stream));
+            TBEM_CK(cudaMemcpyAsync(Go.p, it->second.go.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, stream));
+            TBEM_CK(cudaStreamSynchronize(stream));
+            h_ev = it->second.ev;
+        }
+    }
+    if (h_ev.empty()) {
     // G_in = sum_k T_k^T T_k = X X^T, X = [T_1^T ... T_K^T]: the column-major
     // view of the row-major matrices side by side (chunks bound the int sizes)
     const long step = std::max<long>(1, (1L << 30) / std::max(nn, 1L));
@@ -1907,8 +1974,6 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
                              &beta, Go.p, n));
     }
     // eigenvectors (ascending eigenvalues) overwrite the Gram matrices
-    DBuf<double> ev;
-    ev.alloc(2 * (size_t)n);
     int lwork = 0;
     TBEM_CKS(cusolverDnDsyevd_bufferSize(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
                                          Gi.p, n, ev.p, &lwork));
@@ -1920,10 +1985,25 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
                               ev.p, work.p, lwork, info.p));
     TBEM_CKS(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, Go.p, n,
                               ev.p + n, work.p, lwork, info.p + 1));
-    std::vector<double> h_ev = ev.download();
+    h_ev = ev.download();
     std::vector<int> h_info = info.download();
     if (h_info[0] != 0 || h_info[1] != 0)
         throw Error(TBEM_ERR_CUDA, "eigen-decomposition of the M2L Gram matrices failed");
+    GramEntry e{Gi.download(), Go.download(), h_ev};
+    std::lock_guard<std::mutex> lock(c2e_cache_mu);
+    if (!gram_cache.count(gkey)) {
+        const size_t bytes = sizeof(double) * (e.gi.size() + e.go.size() + e.ev.size());
+        while (!gram_cache_order.empty() && gram_cache_bytes + bytes > GRAM_CACHE_BYTES) {
+            const GramEntry& old = gram_cache[gram_cache_order.front()];
+            gram_cache_bytes -= sizeof(double) * (old.gi.size() + old.go.size() + old.ev.size());
+            gram_cache.erase(gram_cache_order.front());
+            gram_cache_order.erase(gram_cache_order.begin());
+        }
+        gram_cache[gkey] = std::move(e);
+        gram_cache_order.push_back(gkey);
+        gram_cache_bytes += bytes;
+    }
+    }
     auto rank_of = [&](const double* e) {
         const double top = e[n - 1];
         int r = 0;

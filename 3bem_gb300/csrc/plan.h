@@ -36,6 +36,8 @@ void set_last_error(const std::string& msg);
 int api_status();
 
 void check_cuda(cudaError_t e, const char* what, const char* file, int line);
+// empties the process's cache of factored pseudo-inverses and M2L eigenbases
+void clear_setup_cache();
 void check_cublas(cublasStatus_t e, const char* what, const char* file, int line);
 void check_cusolver(cusolverStatus_t e, const char* what, const char* file, int line);
 #define TBEM_CK(x) ::tbem::check_cuda((x), #x, __FILE__, __LINE__)
@@ -470,6 +472,7 @@ struct Plan {
         const std::vector<long>* l2l_index;
         const std::vector<long>* m2m_off;
         const std::vector<long>* l2l_off;
+        uint64_t t0_key[2];                // two hashes of what the M2L matrices depend on
     };
     void build_compression(Form& F, const CompressionInput& in);
     // T = float: the precision form; T = double: the FP64 compressed form

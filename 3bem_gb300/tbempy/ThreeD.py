@@ -501,6 +501,13 @@ class DirectOperator(OperatorI):
                               self._src_normals, self._src_weights)
 
 
+def clear_setup_cache():
+    """Empty the process's setup cache (the pseudo-inverses and M2L
+    eigenbases later constructions with the same kernel parameters and cell
+    geometry reuse)."""
+    check(_L.lib().tbem_setup_cache_clear())
+
+
 def fma_peak_tflops(fp64=False, device=0):
     """The device's measured FMA rate (TFLOP/s, FMA = 2 flops) from the
     library's microbenchmark: the denominator of the evaluation kernels'

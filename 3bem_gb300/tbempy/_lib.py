@@ -67,6 +67,7 @@ SIGNATURES = {
     "tbem_fmm_phase_times": (_I, [_P, _P, _P, _I]),
     "tbem_fmm_setup_times": (_I, [_P, _P, _P, _I]),
     "tbem_fma_peak": (_I, [_I, _I, _P]),
+    "tbem_setup_cache_clear": (_I, []),
     "tbem_fmm_last_launches": (_L, [_P]),
     "tbem_fmm_sync": (_I, [_P, _P]),
     "tbem_fmm_set_wait_cycles": (_I, [_P, C.c_longlong]),

@@ -448,6 +448,14 @@ long tbem_interior_obs_points(int dim, const double* locs, long n, const double*
  * The denominator of the evaluation kernels' roofline. */
 int tbem_fma_peak(int device, int fp64, double* tflops);
 
+/* Setup cache (no reference counterpart): operator constructions in one
+ * process reuse the check-to-equivalent pseudo-inverses and the M2L
+ * compression's eigenbases of earlier constructions with the same kernel
+ * parameters, surfaces and cell geometry (the displacement and traction
+ * operators of one mesh factor once).  Host copies, at most 1 GB; this
+ * empties the cache.  Returns TBEM_OK. */
+int tbem_setup_cache_clear(void);
+
 #ifdef __cplusplus
 }
 #endif

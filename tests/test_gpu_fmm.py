@@ -396,6 +396,41 @@ def test_phase_timing_means_over_applies():
     assert all(s >= 0 for _, s in op.setup_times())
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_compressed"])
+def test_setup_cache_reuse_matches_a_fresh_build(precision):
+    """A traction operator built after another operator with the same
+    translation kernel over the same points (the precision forms translate
+    with the displacement kernel whatever the operator's kernel; the plain
+    form with the operator's own) takes its pseudo-inverses and M2L
+    eigenbases from the setup cache: they are bit-identical to those of a
+    build from an empty cache, and so are the ranks; the two applies agree
+    to the form's summation-order noise."""
+    from tbempy import ThreeD
+    locs, nrm, w = cloud(3000, 41)
+    cfg = ThreeD.FMMConfig(0.3, 152 if precision == "fp64" else 296, 40, 0.05, False)
+
+    def build(K):
+        return ThreeD.FMMOperator(K, locs, nrm, locs, nrm, w, cfg, precision=precision)
+
+    ThreeD.clear_setup_cache()
+    first = ThreeD.ElasticTraction(1.0, 0.25) if precision == "fp64" else \
+        ThreeD.ElasticDisplacement(1.0, 0.25)
+    t0 = dict(build(first).setup_times())
+    warm = build(ThreeD.ElasticTraction(1.0, 0.25))
+    ThreeD.clear_setup_cache()
+    cold = build(ThreeD.ElasticTraction(1.0, 0.25))
+    for which in (0, 1):
+        assert warm.n_c2e_levels(which) == cold.n_c2e_levels(which)
+        for lev in range(cold.n_c2e_levels(which)):
+            assert np.array_equal(warm.get_c2e(which, lev), cold.get_c2e(which, lev))
+    assert warm.m2l_ranks() == cold.m2l_ranks()
+    x = np.random.default_rng(42).uniform(-1, 1, cold.n_cols())
+    yw, yc = warm.apply(x), cold.apply(x)
+    assert rel(yw, yc) < {"fp64": 1e-12, "fp64_compressed": 1e-10, "mixed": 1e-6}[precision]
+    # the reused phase takes a fraction of the factoring one
+    assert dict(warm.setup_times())["c2e"] < 0.5 * t0["c2e"] + 0.01
+
+
 @pytest.mark.parametrize("name", KERNELS)
 def test_default_precision_form_transpose(name):
     """The default precision form (compressed far field, tensor-core M2L) and
