@@ -455,6 +455,18 @@ __global__ void basis_rows_kernel(const double* evec, int n, int r, double scale
     }
 }
 
+// out[k] = in[k]^T for kb row-major n x n blocks: the column-major view of
+// each output block is the row-major matrix itself
+__global__ void transpose_blocks_kernel(const double* in, double* out, int n, long kb)
+{
+    const long nn = (long)n * n, total = kb * nn;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long k = t / nn, r = t % nn;
+        const long j = r / n, i = r % n;
+        out[t] = in[k * nn + i * n + j];
+    }
+}
+
 __global__ void add_kernel(const double* in, float* out, long n)
 {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -1056,6 +1068,82 @@ void Plan::build_tasks()
     for (auto& p : L.p2l) { p2l_of[p.obs].push_back(p.src); p2l_by_src[p.src].push_back(p.obs); }
     for (auto& p : L.m2l) { m2l_of[p.obs].push_back(p.src); m2l_by_src[p.src].push_back(p.obs); }
 
+    // M2L keys: (obs level, src level, integer offset in units of the finer
+    // half width), numbered in order of first appearance.  Found first: the
+    // on-the-fly M2L task sets below are built only when the pairs are not
+    // all integer offsets between congruent cells.
+    m2l_groups.clear();
+    m2l_key_ls.clear();
+    m2l_canon.clear();
+    f.m2l_on_the_fly = !(same_tree || common_cube);
+    if (same_tree || common_cube) {
+        // open-addressing table of packed keys (levels < 256, offsets within
+        // +-2^15: beyond that the pair is computed on the fly)
+        std::vector<unsigned long long> hkey(1024, ~0ull);
+        std::vector<int> hval(1024, -1);
+        auto slot_of = [&](unsigned long long k) {
+            unsigned long long h = k * 0x9e3779b97f4a7c15ull;
+            size_t i = (size_t)(h >> 20) & (hkey.size() - 1);
+            while (hkey[i] != ~0ull && hkey[i] != k) i = (i + 1) & (hkey.size() - 1);
+            return i;
+        };
+        for (size_t pi = 0; pi < L.m2l.size() && !f.m2l_on_the_fly; pi++) {
+            const Cell& o = O.cells[L.m2l[pi].obs];
+            const Cell& sc = S.cells[L.m2l[pi].src];
+            const double* hf = o.level >= sc.level ? o.hw : sc.hw;
+            long off[3];
+            for (int d = 0; d < 3; d++) {
+                double delta = sc.center[d] - o.center[d];
+                if (hf[d] == 0.0) {
+                    if (delta != 0.0) f.m2l_on_the_fly = true;
+                    off[d] = 0;
+                    continue;
+                }
+                double q = delta / hf[d];
+                double r = std::nearbyint(q);
+                if (std::fabs(q - r) > 1e-6 * std::max(1.0, std::fabs(q))) f.m2l_on_the_fly = true;
+                if (std::fabs(r) >= 32767.0) f.m2l_on_the_fly = true;
+                off[d] = (long)r;
+            }
+            if (f.m2l_on_the_fly || o.level > 255 || sc.level > 255) {
+                f.m2l_on_the_fly = true;
+                break;
+            }
+            const unsigned long long key =
+                ((unsigned long long)o.level << 56) | ((unsigned long long)sc.level << 48) |
+                ((unsigned long long)(off[0] + 32768) << 32) | ((unsigned long long)(off[1] + 32768) << 16) |
+                (unsigned long long)(off[2] + 32768);
+            size_t i = slot_of(key);
+            int g = hval[i];
+            if (g < 0) {
+                g = (int)m2l_groups.size();
+                hkey[i] = key;
+                hval[i] = g;
+                m2l_groups.push_back({});
+                m2l_key_ls.push_back(sc.level);
+                m2l_canon.push_back({L.m2l[pi].obs, L.m2l[pi].src});
+                if (2 * m2l_groups.size() > hkey.size()) {  // keep the load under one half
+                    std::vector<unsigned long long> ok(hkey.size() * 2, ~0ull);
+                    std::vector<int> ov(hkey.size() * 2, -1);
+                    ok.swap(hkey);
+                    ov.swap(hval);
+                    for (size_t j = 0; j < ok.size(); j++)
+                        if (ok[j] != ~0ull) {
+                            const size_t t = slot_of(ok[j]);
+                            hkey[t] = ok[j];
+                            hval[t] = ov[j];
+                        }
+                }
+            }
+            m2l_groups[g].push_back((int)pi);
+        }
+        if (f.m2l_on_the_fly) {
+            m2l_groups.clear();
+            m2l_key_ls.clear();
+            m2l_canon.clear();
+        }
+    }
+
     // A source cell "touches" a target leaf when their boxes overlap or share
     // a face, edge or corner: its pairs are the closest ones, where the FP32
     // double layer takes the double-float n . d
@@ -1090,7 +1178,7 @@ void Plan::build_tasks()
         for (int s : p2l_of[c]) pl.push_back({S.cells[s].pt_begin, (int)S.cells[s].n_points()});
         for (int s : m2l_of[c]) ml.push_back({s, ns});
         p2l.add((long)c, ns, oc.center, pl, TPB);
-        m2l_fly.add((long)c, ns, oc.center, ml, TPB);
+        if (f.m2l_on_the_fly) m2l_fly.add((long)c, ns, oc.center, ml, TPB);
     }
     for (int c : L.l2p) {
         const Cell& cc = O.cells[c];
@@ -1118,7 +1206,7 @@ void Plan::build_tasks()
         for (int o : m2p_by_src[c]) mp.push_back({O.cells[o].pt_begin, (int)O.cells[o].n_points()});
         for (int o : m2l_by_src[c]) ml.push_back({o, ns});
         m2p_t.add((long)c, ns, sc.center, mp, TPB);
-        m2l_fly_t.add((long)c, ns, sc.center, ml, TPB);
+        if (f.m2l_on_the_fly) m2l_fly_t.add((long)c, ns, sc.center, ml, TPB);
     }
     for (int c : L.l2p) {
         const Cell& cc = O.cells[c];
@@ -1154,45 +1242,6 @@ void Plan::build_tasks()
             int key = p.level * 8 + O.cells[ch].octant;
             if (l2l_canon[key].first < 0) l2l_canon[key] = {c, ch};
             l2l_pairs[key].push_back({c, ch});  // (in = parent, out = child)
-        }
-    }
-    // M2L keys: (obs level, src level, integer offset in units of the finer half width)
-    m2l_groups.clear();
-    m2l_key_ls.clear();
-    m2l_canon.clear();
-    f.m2l_on_the_fly = !(same_tree || common_cube);
-    if (same_tree || common_cube) {
-        std::map<std::tuple<int, int, long, long, long>, int> keys;
-        for (size_t pi = 0; pi < L.m2l.size() && !f.m2l_on_the_fly; pi++) {
-            const Cell& o = O.cells[L.m2l[pi].obs];
-            const Cell& s = S.cells[L.m2l[pi].src];
-            const double* hf = o.level >= s.level ? o.hw : s.hw;
-            long off[3];
-            for (int d = 0; d < 3; d++) {
-                double delta = s.center[d] - o.center[d];
-                if (hf[d] == 0.0) {
-                    if (delta != 0.0) f.m2l_on_the_fly = true;
-                    off[d] = 0;
-                    continue;
-                }
-                double q = delta / hf[d];
-                double r = std::nearbyint(q);
-                if (std::fabs(q - r) > 1e-6 * std::max(1.0, std::fabs(q))) f.m2l_on_the_fly = true;
-                off[d] = (long)r;
-            }
-            auto key = std::make_tuple(o.level, s.level, off[0], off[1], off[2]);
-            auto it = keys.find(key);
-            int g;
-            if (it == keys.end()) {
-                g = (int)m2l_groups.size();
-                keys[key] = g;
-                m2l_groups.push_back({});
-                m2l_key_ls.push_back(s.level);
-                m2l_canon.push_back({L.m2l[pi].obs, L.m2l[pi].src});
-            } else {
-                g = it->second;
-            }
-            m2l_groups[g].push_back((int)pi);
         }
     }
 }
@@ -1958,51 +2007,82 @@ void Plan::build_compression(Form& F, const CompressionInput& in)
         }
     }
     if (h_ev.empty()) {
-    // G_in = sum_k T_k^T T_k = X X^T, X = [T_1^T ... T_K^T]: the column-major
-    // view of the row-major matrices side by side (chunks bound the int sizes)
-    const long step = std::max<long>(1, (1L << 30) / std::max(nn, 1L));
-    for (long k0 = 0; k0 < n_ops; k0 += step) {
-        const long kb = std::min(step, n_ops - k0);
-        const double beta = k0 == 0 ? 0.0 : 1.0;
-        TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, n, (int)(kb * n), &one,
-                             T0 + k0 * nn, n, &beta, Gi.p, n));
-    }
-    // G_out = sum_k T_k T_k^T: one rank-n update per matrix
-    for (long k = 0; k < n_ops; k++) {
-        const double beta = k == 0 ? 0.0 : 1.0;
-        TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, n, n, &one, T0 + k * nn, n,
-                             &beta, Go.p, n));
-    }
-    // eigenvectors (ascending eigenvalues) overwrite the Gram matrices
-    int lwork = 0;
-    TBEM_CKS(cusolverDnDsyevd_bufferSize(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
-                                         Gi.p, n, ev.p, &lwork));
-    DBuf<double> work;
-    work.alloc(std::max(lwork, 1));
-    DBuf<int> info;
-    info.alloc(2);
-    TBEM_CKS(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, Gi.p, n,
-                              ev.p, work.p, lwork, info.p));
-    TBEM_CKS(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, Go.p, n,
-                              ev.p + n, work.p, lwork, info.p + 1));
-    h_ev = ev.download();
-    std::vector<int> h_info = info.download();
-    if (h_info[0] != 0 || h_info[1] != 0)
-        throw Error(TBEM_ERR_CUDA, "eigen-decomposition of the M2L Gram matrices failed");
-    GramEntry e{Gi.download(), Go.download(), h_ev};
-    std::lock_guard<std::mutex> lock(c2e_cache_mu);
-    if (!gram_cache.count(gkey)) {
-        const size_t bytes = sizeof(double) * (e.gi.size() + e.go.size() + e.ev.size());
-        while (!gram_cache_order.empty() && gram_cache_bytes + bytes > GRAM_CACHE_BYTES) {
-            const GramEntry& old = gram_cache[gram_cache_order.front()];
-            gram_cache_bytes -= sizeof(double) * (old.gi.size() + old.go.size() + old.ev.size());
-            gram_cache.erase(gram_cache_order.front());
-            gram_cache_order.erase(gram_cache_order.begin());
+        // G (+)= A A^T for A = kb n x n blocks side by side (column-major
+        // n x kb n).  A small n leaves the product a few output tiles for the
+        // whole k = kb n, most SMs idle: there the blocks are cut into groups
+        // whose products run as one strided-batched GEMM, summed by a GEMV.
+        constexpr long GRAM_GROUPS = 64;
+        DBuf<double> part, ones;
+        if (n <= 512) {
+            part.alloc((size_t)GRAM_GROUPS * nn);
+            std::vector<double> h1(GRAM_GROUPS, 1.0);
+            ones.upload(h1);
         }
-        gram_cache[gkey] = std::move(e);
-        gram_cache_order.push_back(gkey);
-        gram_cache_bytes += bytes;
-    }
+        auto gram_add = [&](const double* A, long kb, double* G, bool first) {
+            const double beta = first ? 0.0 : 1.0;
+            if (n > 512 || kb < 2 * GRAM_GROUPS) {
+                TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, n, (int)(kb * n), &one, A, n,
+                                     &beta, G, n));
+                return;
+            }
+            const long gk = kb / GRAM_GROUPS, rem = kb - GRAM_GROUPS * gk;
+            TBEM_CKB(cublasDgemmStridedBatched(cublas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, (int)(gk * n), &one, A, n,
+                                               (long long)(gk * nn), A, n, (long long)(gk * nn), &zero, part.p, n,
+                                               (long long)nn, (int)GRAM_GROUPS));
+            TBEM_CKB(cublasDgemv(cublas, CUBLAS_OP_N, (int)nn, (int)GRAM_GROUPS, &one, part.p, (int)nn, ones.p, 1,
+                                 &beta, G, 1));
+            if (rem > 0)
+                TBEM_CKB(cublasDsyrk(cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, n, (int)(rem * n), &one,
+                                     A + GRAM_GROUPS * gk * nn, n, &one, G, n));
+        };
+        // G_in = sum_k T_k^T T_k = X X^T, X = [T_1^T ... T_K^T]: the column-major
+        // view of the row-major matrices side by side (chunks bound the int sizes)
+        const long step = std::max<long>(1, (1L << 30) / std::max(nn, 1L));
+        for (long k0 = 0; k0 < n_ops; k0 += step)
+            gram_add(T0 + k0 * nn, std::min(step, n_ops - k0), Gi.p, k0 == 0);
+        // G_out = sum_k T_k T_k^T: chunks of the matrices transposed side by
+        // side (column-major n x kb n = [T_1 ... T_kb], 256 MB of staging) and
+        // one rank-(kb n) update per chunk instead of one rank-n update per
+        // matrix
+        const long tstep = std::max<long>(1, std::min<long>(step, (256L << 20) / (long)sizeof(double) / nn));
+        DBuf<double> Tt;
+        Tt.alloc((size_t)std::min(tstep, n_ops) * nn);
+        for (long k0 = 0; k0 < n_ops; k0 += tstep) {
+            const long kb = std::min(tstep, n_ops - k0);
+            transpose_blocks_kernel<<<grid_for(kb * nn), 256, 0, stream>>>(T0 + k0 * nn, Tt.p, n, kb);
+            TBEM_CK(cudaGetLastError());
+            gram_add(Tt.p, kb, Go.p, k0 == 0);
+        }
+        // eigenvectors (ascending eigenvalues) overwrite the Gram matrices
+        int lwork = 0;
+        TBEM_CKS(cusolverDnDsyevd_bufferSize(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
+                                             Gi.p, n, ev.p, &lwork));
+        DBuf<double> work;
+        work.alloc(std::max(lwork, 1));
+        DBuf<int> info;
+        info.alloc(2);
+        TBEM_CKS(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, Gi.p, n,
+                                  ev.p, work.p, lwork, info.p));
+        TBEM_CKS(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, Go.p, n,
+                                  ev.p + n, work.p, lwork, info.p + 1));
+        h_ev = ev.download();
+        std::vector<int> h_info = info.download();
+        if (h_info[0] != 0 || h_info[1] != 0)
+            throw Error(TBEM_ERR_CUDA, "eigen-decomposition of the M2L Gram matrices failed");
+        GramEntry e{Gi.download(), Go.download(), h_ev};
+        std::lock_guard<std::mutex> lock(c2e_cache_mu);
+        if (!gram_cache.count(gkey)) {
+            const size_t bytes = sizeof(double) * (e.gi.size() + e.go.size() + e.ev.size());
+            while (!gram_cache_order.empty() && gram_cache_bytes + bytes > GRAM_CACHE_BYTES) {
+                const GramEntry& old = gram_cache[gram_cache_order.front()];
+                gram_cache_bytes -= sizeof(double) * (old.gi.size() + old.go.size() + old.ev.size());
+                gram_cache.erase(gram_cache_order.front());
+                gram_cache_order.erase(gram_cache_order.begin());
+            }
+            gram_cache[gkey] = std::move(e);
+            gram_cache_order.push_back(gkey);
+            gram_cache_bytes += bytes;
+        }
     }
     auto rank_of = [&](const double* e) {
         const double top = e[n - 1];
