@@ -1066,7 +1066,6 @@ void Plan::build_tasks()
     for (auto& p : L.p2p) { p2p_of[p.obs].push_back(p.src); p2p_by_src[p.src].push_back(p.obs); }
     for (auto& p : L.m2p) { m2p_of[p.obs].push_back(p.src); m2p_by_src[p.src].push_back(p.obs); }
     for (auto& p : L.p2l) { p2l_of[p.obs].push_back(p.src); p2l_by_src[p.src].push_back(p.obs); }
-    for (auto& p : L.m2l) { m2l_of[p.obs].push_back(p.src); m2l_by_src[p.src].push_back(p.obs); }
 
     // M2L keys: (obs level, src level, integer offset in units of the finer
     // half width), numbered in order of first appearance.  Found first: the
@@ -1143,6 +1142,10 @@ void Plan::build_tasks()
             m2l_canon.clear();
         }
     }
+
+    // the per-cell M2L lists feed only the on-the-fly M2L task sets
+    if (f.m2l_on_the_fly)
+        for (auto& p : L.m2l) { m2l_of[p.obs].push_back(p.src); m2l_by_src[p.src].push_back(p.obs); }
 
     // A source cell "touches" a target leaf when their boxes overlap or share
     // a face, edge or corner: its pairs are the closest ones, where the FP32
