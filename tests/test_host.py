@@ -260,6 +260,11 @@ def test_argument_errors_are_status_codes():
     assert L.tbem_direct_apply(0, None, P(p), P(p), 10, P(p), P(p), None, 10, P(y), P(y), 1,
                                None) == -1
     assert "null" in L.tbem_last_error().decode()
+    # the gradient entry points check their arguments before any device use
+    assert L.tbem_fmm_observation_gradients(None, P(y), P(y), None, None, None) == -1
+    assert L.tbem_fmm_source_gradients(None, P(y), P(y), None, None, None, None) == -1
+    # the setup cache is host memory: emptying it needs no device
+    ThreeD.clear_setup_cache()
 
 
 def test_2d_operators_build_quadtrees_and_refuse_the_precision_form():
