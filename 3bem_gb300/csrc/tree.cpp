@@ -3,8 +3,12 @@
 #include "tree.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <exception>
 #include <memory>
+#include <mutex>
+#include <thread>
 
 namespace tbem {
 namespace {
@@ -390,12 +394,140 @@ struct ListBuilder {
 
 }  // namespace
 
+namespace {
+
+// The dual-tree traversal in parallel with the sequential order kept.  The
+// recursion is walked to a fixed depth on one thread; what it emits there
+// goes into ordered segments, and every call it would make below that depth
+// becomes a segment of its own (a subtree of the traversal).  The subtrees
+// then run the sequential recursion on worker threads, each into its own
+// segment, and the segments are concatenated in order: every list comes out
+// exactly as the sequential traversal emits it.
+struct DualSegment {
+    int o = -1, s = -1;  // a subtree still to traverse, or -1 for emitted pairs
+    std::vector<CellPair> p2p, m2p, p2l, m2l;
+};
+
+struct DualFrontier {
+    const Tree& obs;
+    const Tree& src;
+    double mac;
+    long n_surf;
+    bool small_cells;
+    int max_depth;
+    std::vector<DualSegment> seg;
+
+    DualSegment& open()
+    {
+        if (seg.empty() || seg.back().o >= 0) seg.emplace_back();
+        return seg.back();
+    }
+    // the branch rules of ListBuilder::dual, one level
+    void walk(int o, int s, int depth)
+    {
+        if (depth >= max_depth) {
+            seg.emplace_back();
+            seg.back().o = o;
+            seg.back().s = s;
+            return;
+        }
+        const Cell& oc = obs.cells[o];
+        const Cell& sc = src.cells[s];
+        double r_src = hyp(sc.hw), r_obs = hyp(oc.hw);
+        double r_max = std::max(r_src, r_obs), r_min = std::min(r_src, r_obs);
+        double dc[3] = {oc.center[0] - sc.center[0], oc.center[1] - sc.center[1],
+                        oc.center[2] - sc.center[2]};
+        double sep = hyp(dc);
+        if (r_max + mac * r_min <= mac * sep) {
+            bool small_src = sc.n_points() <= n_surf;
+            bool small_obs = oc.n_points() <= n_surf;
+            DualSegment& g = open();
+            if (small_cells) {
+                if (small_obs && small_src) g.p2p.push_back({o, s});
+                else if (small_obs) g.m2p.push_back({o, s});
+                else if (small_src) g.p2l.push_back({o, s});
+                else g.m2l.push_back({o, s});
+            } else {
+                g.m2l.push_back({o, s});
+            }
+            return;
+        }
+        if (oc.is_leaf() && sc.is_leaf()) {
+            open().p2p.push_back({o, s});
+            return;
+        }
+        bool src_is_shallower = oc.level > sc.level;
+        bool split_src = (src_is_shallower && !sc.is_leaf()) || oc.is_leaf();
+        if (split_src) {
+            for (int k = 0; k < sc.n_children; k++) walk(o, sc.first_child + k, depth + 1);
+        } else {
+            for (int k = 0; k < oc.n_children; k++) walk(oc.first_child + k, s, depth + 1);
+        }
+    }
+};
+
+void dual_parallel(ListBuilder& B)
+{
+    // depth 6 of the traversal: up to a few thousand subtrees for the
+    // workers, and nothing for small trees (their recursion ends first)
+    DualFrontier F{B.obs, B.src, B.mac, B.n_surf, B.small_cells, 6, {}};
+    F.walk(0, 0, 0);
+    std::vector<long> todo;
+    for (size_t i = 0; i < F.seg.size(); i++)
+        if (F.seg[i].o >= 0) todo.push_back((long)i);
+    const long hw = (long)std::max(1u, std::thread::hardware_concurrency());
+    const long nt = std::min<long>(hw, (long)todo.size());
+    auto run = [&](long i) {
+        DualSegment& g = F.seg[todo[i]];
+        ListBuilder W{B.obs, B.src, B.mac, B.n_surf, B.small_cells, {}};
+        W.dual(g.o, g.s);
+        g.p2p = std::move(W.L.p2p);
+        g.m2p = std::move(W.L.m2p);
+        g.p2l = std::move(W.L.p2l);
+        g.m2l = std::move(W.L.m2l);
+    };
+    if (nt <= 1) {
+        for (long i = 0; i < (long)todo.size(); i++) run(i);
+    } else {
+        std::atomic<long> next{0};
+        std::exception_ptr failure;
+        std::mutex m;
+        std::vector<std::thread> th;
+        for (long t = 0; t < nt; t++)
+            th.emplace_back([&] {
+                try {
+                    for (long i = next++; i < (long)todo.size(); i = next++) run(i);
+                } catch (...) {  // handed to the caller after the join
+                    std::lock_guard<std::mutex> lock(m);
+                    if (!failure) failure = std::current_exception();
+                }
+            });
+        for (auto& x : th) x.join();
+        if (failure) std::rethrow_exception(failure);
+    }
+    auto gather = [&](std::vector<CellPair>& out, std::vector<CellPair> DualSegment::*list) {
+        size_t total = out.size();
+        for (const DualSegment& g : F.seg) total += (g.*list).size();
+        out.reserve(total);
+        for (DualSegment& g : F.seg) {
+            out.insert(out.end(), (g.*list).begin(), (g.*list).end());
+            std::vector<CellPair>().swap(g.*list);
+        }
+    };
+    gather(B.L.p2p, &DualSegment::p2p);
+    gather(B.L.m2p, &DualSegment::m2p);
+    gather(B.L.p2l, &DualSegment::p2l);
+    gather(B.L.m2l, &DualSegment::m2l);
+}
+
+}  // namespace
+
 TaskLists build_lists(const Tree& obs, const Tree& src, double mac, long n_surf,
                       bool small_cells)
 {
     ListBuilder B{obs, src, mac, n_surf, small_cells, {}};
     if (src.n_points() > 0) B.upward(0);
-    if (obs.n_points() > 0 && src.n_points() > 0) B.dual(0, 0);
+    if (obs.n_points() > 0 && src.n_points() > 0) dual_parallel(B);
     if (obs.n_points() > 0) B.downward(0);
     return std::move(B.L);
 }
