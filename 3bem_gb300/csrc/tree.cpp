@@ -93,8 +93,10 @@ struct Builder {
     // index is taken after its subtree is built (post-order).
     void build_children(int node, const Box& bounds, int level)
     {
-        const std::vector<long> idx = nodes[node].idx;  // copy: nodes may reallocate
-        if ((long)idx.size() <= min_pts) return;
+        if ((long)nodes[node].idx.size() <= min_pts) return;
+        // an inner cell keeps no point list (only the leaves' are read)
+        const std::vector<long> idx = std::move(nodes[node].idx);
+        nodes[node].idx.clear();
         std::vector<long> part[8];
         for (long i : idx) part[containing(bounds, &pts[3 * i], dim)].push_back(i);
         for (int o = 0; o < (1 << dim); o++) {
@@ -122,6 +124,97 @@ struct Builder {
 
 namespace {
 Tree flatten(const std::vector<Node>& N, long n);
+
+// build_children(0, bounds, 0) with the root's children's subtrees built on
+// threads, each in a builder of its own numbered from 1 (the subtree's root
+// last, as post-order gives it), then merged with the node ids and the
+// reference indices offset: subtree k's indices follow those of subtrees
+// 0 .. k-1, exactly the sequential post-order numbering.
+constexpr long TREE_THREADS_MIN_POINTS = 1L << 17;
+
+template <typename S>
+long n_points_of(const std::vector<S>& sub)
+{
+    long n = 0;
+    for (const S& w : sub) n += (long)w.b.nodes[0].idx.size();
+    return n;
+}
+
+void build_root_children(Builder& B, const Box& bounds)
+{
+    if ((long)B.nodes[0].idx.size() <= B.min_pts) return;
+    std::vector<long> idx = std::move(B.nodes[0].idx);
+    B.nodes[0].idx.clear();
+    std::vector<long> part[8];
+    for (long i : idx) part[containing(bounds, &B.pts[3 * i], B.dim)].push_back(i);
+    std::vector<long>().swap(idx);
+    struct Sub {
+        Builder b;
+        Box cb;
+        bool recurse;
+        int octant;
+    };
+    std::vector<Sub> sub;
+    for (int o = 0; o < (1 << B.dim); o++) {
+        if (part[o].empty()) continue;
+        Sub w;
+        w.b.pts = B.pts;
+        w.b.min_pts = B.min_pts;
+        w.b.dim = B.dim;
+        w.cb = subcell(bounds, o, B.dim);
+        const Box tight = bounding_box(B.pts, part[o]);
+        w.recurse = tight.h[0] != 0.0 || tight.h[1] != 0.0 || tight.h[2] != 0.0;
+        w.octant = o;
+        Node n;
+        n.b = w.cb;
+        n.idx = std::move(part[o]);
+        n.level = 1;
+        n.ref_index = -1;
+        n.octant = o;
+        for (int k = 0; k < 8; k++) n.child[k] = -1;
+        w.b.nodes.push_back(std::move(n));
+        sub.push_back(std::move(w));
+    }
+    auto run = [&](size_t k) {
+        Sub& w = sub[k];
+        if (w.recurse) w.b.build_children(0, w.cb, 1);
+        w.b.nodes[0].ref_index = w.b.next_index++;
+    };
+    // threads only for large trees (small ones are often built many at a
+    // time already, one per mesh)
+    const bool threaded = n_points_of(sub) >= TREE_THREADS_MIN_POINTS;
+    if (threaded && sub.size() > 1 && std::thread::hardware_concurrency() > 1) {
+        std::vector<std::thread> th;
+        std::exception_ptr failure;
+        std::mutex m;
+        for (size_t k = 0; k < sub.size(); k++)
+            th.emplace_back([&, k] {
+                try {
+                    run(k);
+                } catch (...) {  // handed to the caller after the join
+                    std::lock_guard<std::mutex> lock(m);
+                    if (!failure) failure = std::current_exception();
+                }
+            });
+        for (auto& t : th) t.join();
+        if (failure) std::rethrow_exception(failure);
+    } else {
+        for (size_t k = 0; k < sub.size(); k++) run(k);
+    }
+    long offset = 0;
+    for (Sub& w : sub) {
+        const int base = (int)B.nodes.size();
+        B.nodes[0].child[w.octant] = base;
+        for (Node& n : w.b.nodes) {
+            for (int k = 0; k < 8; k++)
+                if (n.child[k] >= 0) n.child[k] += base;
+            n.ref_index += offset;
+            B.nodes.push_back(std::move(n));
+        }
+        offset += w.b.next_index - 1;
+    }
+    B.next_index = offset + 1;
+}
 }  // namespace
 
 Tree build_tree(const double* pts, long n, long min_pts, int dim)
@@ -142,7 +235,7 @@ Tree build_tree(const double* pts, long n, long min_pts, int dim)
     for (int k = 0; k < 8; k++) root.child[k] = -1;
     B.nodes.reserve(2 * (size_t)(n / std::max<long>(min_pts, 1)) + 16);
     B.nodes.push_back(std::move(root));
-    B.build_children(0, box, 0);  // ... but its children are cut from the unexpanded one
+    build_root_children(B, box);  // ... but its children are cut from the unexpanded one
     return flatten(B.nodes, n);
 }
 
@@ -164,7 +257,7 @@ Tree build_tree_cube(const double* pts, long n, long min_pts, const double cente
     for (int k = 0; k < 8; k++) root.child[k] = -1;
     B.nodes.reserve(2 * (size_t)(n / std::max<long>(min_pts, 1)) + 16);
     B.nodes.push_back(std::move(root));
-    B.build_children(0, box, 0);
+    build_root_children(B, box);
     return flatten(B.nodes, n);
 }
 
@@ -527,7 +620,12 @@ TaskLists build_lists(const Tree& obs, const Tree& src, double mac, long n_surf,
 {
     ListBuilder B{obs, src, mac, n_surf, small_cells, {}};
     if (src.n_points() > 0) B.upward(0);
-    if (obs.n_points() > 0 && src.n_points() > 0) dual_parallel(B);
+    // threads only for large trees (small ones are often built many at a
+    // time already, one per mesh)
+    if (obs.n_points() > 0 && src.n_points() > 0) {
+        if (obs.cells.size() + src.cells.size() >= 8192) dual_parallel(B);
+        else B.dual(0, 0);
+    }
     if (obs.n_points() > 0) B.downward(0);
     return std::move(B.L);
 }
